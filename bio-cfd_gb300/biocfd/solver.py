@@ -1,0 +1,227 @@
+"""GPU solver over the C ABI: block registration, the reference's set-up
+sequence (app/main.F90:43-127) and the per-step phases (app/main.F90:129-265).
+
+Every call goes to ``libbiocfd_gb300.so``; the Python layer only moves host
+mirrors in and out and sequences the module routines like the reference's
+driver does.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Optional
+
+import numpy as np
+
+from . import _lib
+from ._lib import P_d, P_i64, check
+from .synth import Case
+
+
+def _pd(a: np.ndarray):
+    return a.ctypes.data_as(P_d)
+
+
+def _pi(a: np.ndarray):
+    return a.ctypes.data_as(P_i64)
+
+
+def full_grid(faces: np.ndarray):
+    """x1(1..n+3) and deltax(1..n+2) from the faces x1(2..n+2) (src/ReadInput.f90:254-268)."""
+    n = len(faces) - 1
+    x1 = np.zeros(n + 3)
+    x1[1:n + 2] = faces
+    d = np.zeros(n + 2)
+    d[1:n + 1] = x1[2:n + 2] - x1[1:n + 1]
+    d[0] = d[1]
+    d[n + 1] = d[n]
+    x1[0] = x1[1] - d[0]
+    x1[n + 2] = x1[n + 1] + d[n + 1]
+    return x1, d
+
+
+class Solver:
+    """All blocks and interfaces of one case on the GPU."""
+
+    def __init__(self, case: Case, device: int = 0):
+        # The library keeps one block registry per process (block 1 is the
+        # coarse block, as in the reference); a new Solver starts a fresh one.
+        self.L = _lib.load()
+        check(self.L.bcfd_finalize(), "bcfd_finalize")
+        check(self.L.bcfd_init(device), "bcfd_init")
+        self.case = case
+        self.handles: List[int] = []
+        self.ifaces: List[int] = []
+
+    # ---- set-up --------------------------------------------------------------
+    def setup(self, with_fields: bool = True):
+        L, case = self.L, self.case
+        if self.handles:
+            raise _lib.BcfdError("setup called twice")
+        for spec in case.blocks:
+            x1, dx = full_grid(spec.x_faces)
+            y1, dy = full_grid(spec.y_faces)
+            z1, dz = full_grid(spec.z_faces)
+            h = C.c_int64()
+            check(L.bcfd_block_create(spec.nx, spec.ny, spec.nz, _pd(x1), _pd(y1), _pd(z1), _pd(dx),
+                                      _pd(dy), _pd(dz), C.byref(h)), "block_create")
+            g = h.value
+            self.handles.append(g)
+            check(L.bcfd_block_set_scalars(g, dx[1], dy[1], dz[1], spec.omega), "set_scalars")
+            check(L.bcfd_block_set_role(g, int(spec.is_coarse), int(spec.has_body)), "set_role")
+            kin = np.array([spec.xdot, spec.ydot, spec.yddot, 0, 0, 0, 0, 0, *spec.piv], dtype=np.float64)
+            check(L.bcfd_block_set_kinematics(g, _pd(kin)), "set_kinematics")
+            if spec.has_body:
+                m = spec.mesh
+                tri = np.ascontiguousarray(m.tris, dtype=np.int64)
+                e1, e2, e3 = (np.ascontiguousarray(tri[:, q]) for q in range(3))
+                sid = np.ascontiguousarray(m.surf_id, dtype=np.int64)
+                xs, ys, zs = (np.ascontiguousarray(m.nodes[:, q]) for q in range(3))
+                check(L.bcfd_block_set_surface(g, len(tri), len(xs), _pi(e1), _pi(e2), _pi(e3), _pi(sid),
+                                               _pd(xs), _pd(ys), _pd(zs)), "set_surface")
+                check(L.bcfd_block_set_search_box(g, *spec.search_box), "set_search_box")
+                check(L.bcfd_compute_surface_norm(g, m.inor), "compute_surface_norm")
+        for it in case.interfaces:
+            box = np.asarray(it.box, dtype=np.float64)
+            h = C.c_int64()
+            check(L.bcfd_interface_create(self.handles[it.a_blk - 1], self.handles[it.b_blk - 1],
+                                          it.a_msh, it.b_msh, _pd(box), C.byref(h)), "interface_create")
+            self.ifaces.append(h.value)
+        for g, spec in zip(self.handles, case.blocks):
+            if spec.has_body:
+                check(L.bcfd_tagging_th(g), "tagging_th")
+                check(L.bcfd_cellcount_solid(g), "cellcount_solid")
+        if case.interfaces and not case.blocks[0].has_body:
+            check(L.bcfd_fine_block_cell(), "fine_block_cell")
+            check(L.bcfd_cellcount_solid_coarse(self.handles[0]), "cellcount_solid_coarse")
+        if with_fields:
+            for g, ini in zip(self.handles, case.init):
+                self.upload_fields(g, ini)
+        for g, spec in zip(self.handles, case.blocks):
+            if spec.has_body:
+                check(L.bcfd_compute_norm_distance(g), "compute_norm_distance")
+                check(L.bcfd_find_ts_cells(g), "find_ts_cells")
+            check(L.bcfd_coefficient_matrix(g, int(spec.is_coarse)), "coefficient_matrix")
+        for g in self.handles:
+            check(L.bcfd_non_uni_coeff(g), "non_uni_coeff")
+        self.sync()
+
+    def upload_fields(self, g: int, ini: dict):
+        u, v, w, p = (np.asfortranarray(ini[k], dtype=np.float64) for k in ("u", "v", "w", "p"))
+        check(self.L.bcfd_block_upload_fields(g, _pd(u), _pd(v), _pd(w), _pd(p), _pd(u), _pd(v), _pd(w)),
+              "upload_fields")
+
+    # ---- per-step phases (routine by routine, for parity checks) -------------
+    def momentum_phase(self):
+        L, c = self.L, self.case
+        for g, spec in zip(self.handles, c.blocks):
+            check(L.bcfd_ns_momentum_2order(g, c.dt, c.re), "ns_momentum_2order")
+            if spec.is_coarse:
+                check(L.bcfd_velocity_bc(g, c.dt, c.uc), "velocity_bc")
+            if spec.has_body:
+                check(L.bcfd_solid_cell_bc(g), "solid_cell_bc")
+                check(L.bcfd_velocity_forcing1(g), "velocity_forcing1")
+            if spec.is_coarse:
+                check(L.bcfd_velocity_bc(g, c.dt, c.uc), "velocity_bc")
+
+    def poisson_phase(self):
+        c = self.case
+        tt = C.c_double(0.0)
+        check(self.L.bcfd_poisson_solver(c.pc_ita_max, c.epsi, 0, c.dt, 0.0, c.uc, C.byref(tt), 1,
+                                         len(self.handles), 1), "poisson_solver")
+
+    def research_phase(self):
+        L = self.L
+        for g, spec in zip(self.handles, self.case.blocks):
+            if spec.has_body:
+                check(L.bcfd_pressure_forcing1(g), "pressure_forcing1")
+        for g, spec in zip(self.handles, self.case.blocks):
+            if not spec.has_body:
+                continue
+            check(L.bcfd_block_set_flags(g, 0, 0), "set_flags")
+            check(L.bcfd_selective_retagging_th(g), "selective_retagging_th")
+            check(L.bcfd_cellcount_solid(g), "cellcount_solid")
+            check(L.bcfd_solid_cell_bc_move(g), "solid_cell_bc_move")
+            check(L.bcfd_update_velocity_newv(g), "update_velocity_newv")
+            check(L.bcfd_compute_norm_distance(g), "compute_norm_distance")
+            check(L.bcfd_find_ts_cells(g), "find_ts_cells")
+            check(L.bcfd_velocity_forcing_field(g), "velocity_forcing_field")
+            check(L.bcfd_pressure_forcing_field(g), "pressure_forcing_field")
+            check(L.bcfd_velocity_forcing_ghost(g), "velocity_forcing_ghost")
+            check(L.bcfd_pressure_forcing_ghost(g), "pressure_forcing_ghost")
+
+    def step(self):
+        self.momentum_phase()
+        self.poisson_phase()
+        self.research_phase()
+        self.sync()
+
+    # ---- the native whole-step driver ---------------------------------------
+    def config(self, precision: int = 0, div_tol: float = 1e-6, use_graph: int = 0) -> _lib.StepConfig:
+        c = self.case
+        return _lib.StepConfig(c.dt, c.re, c.uc, c.epsi, c.pc_ita_max, precision, div_tol, use_graph)
+
+    def run(self, n_steps: int, precision: int = 0, div_tol: float = 1e-6, use_graph: int = 0):
+        cfg = self.config(precision, div_tol, use_graph)
+        check(self.L.bcfd_run_steps(C.byref(cfg), n_steps), "run_steps")
+
+    # ---- host mirrors --------------------------------------------------------
+    def sync(self):
+        check(self.L.bcfd_synchronize(), "synchronize")
+
+    def fields(self, g: int) -> dict:
+        spec = self.case.blocks[self.handles.index(g)]
+        out = {k: np.zeros(spec.shape, order="F") for k in ("u", "v", "w", "p", "ut", "vt", "wt")}
+        check(self.L.bcfd_block_download_fields(g, *(_pd(out[k]) for k in ("u", "v", "w", "p", "ut", "vt", "wt"))),
+              "download_fields")
+        return out
+
+    def tags(self, g: int) -> dict:
+        spec = self.case.blocks[self.handles.index(g)]
+        s2 = (spec.nx + 2, spec.ny + 2, spec.nz + 2)
+        s3 = (spec.nx + 3, spec.ny + 3, spec.nz + 3)
+        out = {"cell": np.zeros(s2, np.int64, order="F"), "cell2": np.zeros(s3, np.int64, order="F"),
+               "nodeIdTag": np.zeros(s3, np.int64, order="F"), "cell_n": np.zeros(s2, np.int64, order="F"),
+               "cell_pr": np.zeros(s3, np.int64, order="F")}
+        check(self.L.bcfd_block_download_tags(g, *(_pi(out[k]) for k in ("cell", "cell2", "nodeIdTag", "cell_n", "cell_pr"))),
+              "download_tags")
+        return out
+
+    def counts(self, g: int) -> dict:
+        a = np.zeros(6, np.int64)
+        check(self.L.bcfd_block_get_counts(g, _pi(a)), "get_counts")
+        return dict(zip(("ibCellCount", "solidCellCount", "fluidCellCount", "redCellCount",
+                         "blackCellCount", "TSCellCount"), (int(x) for x in a)))
+
+    def sor_stats(self, g: int):
+        n, d2, ds = C.c_int64(), C.c_double(), C.c_double()
+        check(self.L.bcfd_block_get_sor_stats(g, C.byref(n), C.byref(d2), C.byref(ds)), "sor_stats")
+        return n.value, d2.value, ds.value
+
+    def read(self, g: int, name: str, n: int, dtype=np.float64) -> np.ndarray:
+        out = np.zeros(max(n, 1), dtype=dtype)
+        w = C.c_int64()
+        check(self.L.bcfd_block_read(g, name.encode(), out.ctypes.data_as(C.c_void_p), n, C.byref(w)),
+              f"block_read({name})")
+        return out[:w.value]
+
+    def read_list(self, g: int, name: str, count: int) -> np.ndarray:
+        a = self.read(g, name, 3 * max(count, 1), np.int64)
+        return a.reshape(3, -1).T if a.size else np.zeros((0, 3), np.int64)
+
+    def max_divergence(self, g: int) -> float:
+        d = C.c_double()
+        check(self.L.bcfd_max_divergence(g, C.byref(d)), "max_divergence")
+        return d.value
+
+    def stream_ptr(self) -> int:
+        p = C.c_void_p()
+        check(self.L.bcfd_get_stream(C.byref(p)), "get_stream")
+        return p.value or 0
+
+    def kernel_launches(self) -> int:
+        return int(self.L.bcfd_kernel_launches())
+
+    def close(self):
+        for g in self.handles:
+            self.L.bcfd_block_destroy(g)
+        self.handles = []

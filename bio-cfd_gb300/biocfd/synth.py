@@ -1,0 +1,246 @@
+"""Seeded synthetic inputs for the Bio-CFD hot path.
+
+The reference reads its grids, surface mesh and restart fields from files
+that are not part of its repository (`.gitignore` excludes them), so every
+workload here is generated: uniform tensor-product grids, a Fibonacci-sphere
+surface triangulated by its convex hull (or an ellipsoidal plate), interface
+boxes, and the initial field u = uc plus N(0, 1e-3) noise on u, v, w drawn
+from ``numpy.random.default_rng(20261203)``.
+
+Coordinates are in metres (the reference converts its millimetre inputs with
+a factor 0.001 in src/ReadInput.f90:142-351; here they are generated directly
+in the converted units).  Grid conventions follow src/ReadInput.f90:250-351:
+a block with ``n`` interior cells along x has face coordinates
+``x1(2..n+2)``; the ghosts ``x1(1)``/``x1(n+3)`` and the spacings are
+derived by the same rules on the device side and in the oracle.
+"""
+from __future__ import annotations
+
+import dataclasses
+from dataclasses import dataclass, field
+from typing import List, Optional, Tuple
+
+import numpy as np
+
+SEED = 20261203
+
+
+@dataclass
+class Mesh:
+    """Triangulated immersed surface (the gmsh file of src/ReadInput.f90:365-426)."""
+    nodes: np.ndarray          # (n_nodes, 3) float64, world coordinates (xnode1 ...)
+    tris: np.ndarray           # (n_elems, 3) int64, 1-based node indices (ibElP1..3)
+    surf_id: np.ndarray        # (n_elems,) int64 physical tag: 50 static, 51/52 rotating
+    inor: int = 1              # normal orientation factor of computeSurfaceNorm
+
+
+@dataclass
+class BlockSpec:
+    nx: int
+    ny: int
+    nz: int
+    x_faces: np.ndarray        # nx+1 face coordinates = x1(2..nx+2)
+    y_faces: np.ndarray
+    z_faces: np.ndarray
+    omega: float = 1.7
+    is_coarse: bool = False    # domain BCs (velocityBC) and coarse Poisson folding
+    mesh: Optional[Mesh] = None
+    search_box: Tuple[int, int, int, int, int, int] = (0, -1, 0, -1, 0, -1)
+    # rigid-body kinematics read by the forcing routines
+    xdot: float = 0.0
+    ydot: float = 0.0
+    yddot: float = 0.0
+    piv: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+
+    @property
+    def has_body(self) -> bool:
+        return self.mesh is not None
+
+    @property
+    def shape(self) -> Tuple[int, int, int]:
+        """Array extents of the cell-centred fields, (nx+2, ny+2, nz+2)."""
+        return (self.nx + 2, self.ny + 2, self.nz + 2)
+
+    @property
+    def n_interior(self) -> int:
+        return self.nx * self.ny * self.nz
+
+
+@dataclass
+class InterfaceSpec:
+    """One coarse/fine coupling (interface_details.dat, src/ReadInput.f90:430-456)."""
+    a_blk: int                 # coarse block number (1-based)
+    b_blk: int                 # fine block number
+    a_msh: int
+    b_msh: int
+    box: Tuple[float, float, float, float, float, float]  # xs, xe, ys, ye, zs, ze
+
+
+@dataclass
+class Case:
+    name: str
+    blocks: List[BlockSpec]
+    interfaces: List[InterfaceSpec] = field(default_factory=list)
+    dt: float = 0.0
+    re: float = 100.0          # the reference's `re` argument: 1/nu (src/ReadInput.f90:155)
+    uc: float = 1.0
+    epsi: float = 1e-6
+    pc_ita_max: int = 5000
+    n_steps: int = 1
+    init: List[dict] = field(default_factory=list)   # per block: {"u","v","w","p"} arrays
+
+    @property
+    def n_interior(self) -> int:
+        return sum(b.n_interior for b in self.blocks)
+
+
+# ---------------------------------------------------------------------------
+# surfaces
+# ---------------------------------------------------------------------------
+
+def _canonical_hull(pts: np.ndarray, center: np.ndarray) -> np.ndarray:
+    """Convex-hull triangles, oriented outward, in a platform-independent order."""
+    from scipy.spatial import ConvexHull
+    tri = np.asarray(ConvexHull(pts).simplices, dtype=np.int64)
+    a, b, c = pts[tri[:, 0]], pts[tri[:, 1]], pts[tri[:, 2]]
+    nrm = np.cross(b - a, c - a)
+    out = np.einsum("ij,ij->i", nrm, (a + b + c) / 3.0 - center) > 0
+    tri[~out] = tri[~out][:, [0, 2, 1]]
+    # rotate each triangle so its smallest node comes first (keeps orientation)
+    r = np.argmin(tri, axis=1)
+    idx = (np.arange(3)[None, :] + r[:, None]) % 3
+    tri = np.take_along_axis(tri, idx, axis=1)
+    order = np.lexsort((tri[:, 2], tri[:, 1], tri[:, 0]))
+    return tri[order]
+
+
+def fibonacci_sphere(center, diameter: float, spacing: float, surf_id: int = 50) -> Mesh:
+    """Markers on a sphere at roughly `spacing`, triangulated by the convex hull."""
+    center = np.asarray(center, dtype=np.float64)
+    n = max(12, int(round(np.pi * (diameter / spacing) ** 2)))
+    i = np.arange(n, dtype=np.float64)
+    z = 1.0 - (2.0 * i + 1.0) / n
+    r = np.sqrt(1.0 - z * z)
+    phi = i * (np.pi * (3.0 - np.sqrt(5.0)))
+    pts = np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1) * (0.5 * diameter) + center
+    tri = _canonical_hull(pts, center)
+    return Mesh(nodes=pts, tris=tri + 1, surf_id=np.full(len(tri), surf_id, dtype=np.int64))
+
+
+def ellipsoid_plate(center, semi_axes, spacing: float, surf_id: int = 51) -> Mesh:
+    """A rigid ellipsoidal plate: Fibonacci directions mapped onto the ellipsoid."""
+    center = np.asarray(center, dtype=np.float64)
+    ax = np.asarray(semi_axes, dtype=np.float64)
+    area = 4 * np.pi * ((ax[0] * ax[1]) ** 1.6 + (ax[0] * ax[2]) ** 1.6 + (ax[1] * ax[2]) ** 1.6) ** (1 / 1.6) / 3 ** (1 / 1.6)
+    n = max(12, int(round(area / spacing ** 2)))
+    i = np.arange(n, dtype=np.float64)
+    z = 1.0 - (2.0 * i + 1.0) / n
+    r = np.sqrt(1.0 - z * z)
+    phi = i * (np.pi * (3.0 - np.sqrt(5.0)))
+    unit = np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
+    tri = _canonical_hull(unit, np.zeros(3))
+    pts = unit * ax + center
+    return Mesh(nodes=pts, tris=tri + 1, surf_id=np.full(len(tri), surf_id, dtype=np.int64))
+
+
+def search_box_for(spec: BlockSpec, lo, hi, margin_cells: int = 3):
+    """Cell-index box (body_search.dat) covering [lo, hi] plus a margin, clamped to 2..n+1."""
+    out = []
+    for faces, n, a, b in ((spec.x_faces, spec.nx, lo[0], hi[0]),
+                           (spec.y_faces, spec.ny, lo[1], hi[1]),
+                           (spec.z_faces, spec.nz, lo[2], hi[2])):
+        # cell i (1-based, interior 2..n+1) spans faces[i-2] .. faces[i-1]
+        i0 = int(np.searchsorted(faces, a, side="right")) + 1 - margin_cells
+        i1 = int(np.searchsorted(faces, b, side="left")) + 1 + margin_cells
+        out += [max(2, i0), min(n + 1, i1)]
+    return tuple(out)
+
+
+def uniform_faces(x0: float, x1: float, n: int) -> np.ndarray:
+    return x0 + (x1 - x0) * np.arange(n + 1, dtype=np.float64) / n
+
+
+def noisy_initial(spec: BlockSpec, uc: float, rng: np.random.Generator, sigma: float = 1e-3) -> dict:
+    """u = uc, v = w = p = 0 plus N(0, sigma) on u, v, w at every point (restart path)."""
+    shp = spec.shape
+    u = np.full(shp, uc, dtype=np.float64, order="F") + rng.normal(0.0, sigma, shp)
+    v = rng.normal(0.0, sigma, shp)
+    w = rng.normal(0.0, sigma, shp)
+    p = np.zeros(shp)
+    return {k: np.asfortranarray(a) for k, a in (("u", u), ("v", v), ("w", w), ("p", p))}
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+
+def sphere_single_block(n: int = 64, n_steps: int = 100, diameter: float = 0.25,
+                        center=(0.4, 0.5, 0.5), omega: float = 1.7, pc_ita_max: int = 5000,
+                        reynolds: float = 100.0, seed: int = SEED) -> Case:
+    """Single uniform n^3 block on the unit cube with a stationary sphere.
+
+    Re = U D / nu = 100 with U = uc = 1 -> the reference's `re` argument is
+    1/nu = Re / D; dt from CFL 0.3 (dt = 0.3 dx / U); SOR omega 1.7 to 1e-6.
+    The block carries both the domain BCs and the body (composed by the
+    harness; the reference driver applies IB only to blocks g >= 2).
+    """
+    f = uniform_faces(0.0, 1.0, n)
+    dx = 1.0 / n
+    spec = BlockSpec(n, n, n, f, f.copy(), f.copy(), omega=omega, is_coarse=True)
+    spec.mesh = fibonacci_sphere(center, diameter, dx)
+    c = np.asarray(center)
+    spec.search_box = search_box_for(spec, c - diameter / 2, c + diameter / 2)
+    rng = np.random.default_rng(seed)
+    case = Case(name=f"sphere{n}", blocks=[spec], dt=0.3 * dx / 1.0, re=reynolds / diameter,
+                uc=1.0, epsi=1e-6, pc_ita_max=pc_ita_max, n_steps=n_steps)
+    case.init = [noisy_initial(spec, case.uc, rng)]
+    return case
+
+
+def sphere_two_block(nf: int = 64, n_steps: int = 200, diameter: float = 0.5,
+                     reynolds: float = 300.0, omega_c: float = 1.7, omega_f: float = 1.7,
+                     pc_ita_max: int = 5000, seed: int = SEED, coarse=(96, 64, 64),
+                     domain=(3.0, 2.0, 2.0), fine_box=((1.0, 2.0), (0.5, 1.5), (0.5, 1.5)),
+                     center=None) -> Case:
+    """Coarse 96x64x64 over 3x2x2 plus a nested fine nf^3 block at ratio 2 around a sphere.
+
+    The fine block spans `fine_box` (a unit cube) at half the coarse spacing;
+    the interface box equals the fine block's extent.  Re = 300 on D = 0.5.
+    """
+    cnx, cny, cnz = coarse
+    L = domain
+    dxc = L[0] / cnx
+    cs = BlockSpec(cnx, cny, cnz, uniform_faces(0, L[0], cnx), uniform_faces(0, L[1], cny),
+                   uniform_faces(0, L[2], cnz), omega=omega_c, is_coarse=True)
+    (x0, x1), (y0, y1), (z0, z1) = fine_box
+    ratio = 2
+    nfx = int(round((x1 - x0) / dxc)) * ratio
+    nfy = int(round((y1 - y0) / (L[1] / cny))) * ratio
+    nfz = int(round((z1 - z0) / (L[2] / cnz))) * ratio
+    assert (nfx, nfy, nfz) == (nf, nf, nf), (nfx, nfy, nfz)
+    fs = BlockSpec(nfx, nfy, nfz, uniform_faces(x0, x1, nfx), uniform_faces(y0, y1, nfy),
+                   uniform_faces(z0, z1, nfz), omega=omega_f, is_coarse=False)
+    if center is None:
+        center = (0.5 * (x0 + x1), 0.5 * (y0 + y1), 0.5 * (z0 + z1))
+    c = np.asarray(center, dtype=np.float64)
+    fs.mesh = fibonacci_sphere(c, diameter, (x1 - x0) / nfx)
+    fs.search_box = search_box_for(fs, c - diameter / 2, c + diameter / 2)
+    it = InterfaceSpec(1, 2, 1, ratio, (x0, x1, y0, y1, z0, z1))
+    rng = np.random.default_rng(seed)
+    dxf = (x1 - x0) / nfx
+    case = Case(name=f"two_block_{cnx}x{cny}x{cnz}+{nf}^3", blocks=[cs, fs], interfaces=[it],
+                dt=0.3 * dxf, re=reynolds / diameter, uc=1.0, epsi=1e-6,
+                pc_ita_max=pc_ita_max, n_steps=n_steps)
+    case.init = [noisy_initial(b, case.uc, rng) for b in case.blocks]
+    return case
+
+
+def small_two_block(n_steps: int = 2, seed: int = SEED) -> Case:
+    """A 24x16x16 coarse + 16^3 fine version of the two-block case for fast parity tests."""
+    return sphere_two_block(nf=16, n_steps=n_steps, diameter=0.5, coarse=(24, 16, 16),
+                            domain=(3.0, 2.0, 2.0), fine_box=((1.0, 2.0), (0.5, 1.5), (0.5, 1.5)),
+                            pc_ita_max=2000, seed=seed)
+
+
+def replace(case: Case, **kw) -> Case:
+    return dataclasses.replace(case, **kw)

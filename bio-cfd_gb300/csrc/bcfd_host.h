@@ -1,0 +1,116 @@
+// Host-side objects of the library: registered blocks and interfaces, the
+// library stream and the launch helpers.  Shared by the .cu translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "bcfd_internal.cuh"
+
+namespace bcfd {
+
+struct HostBlock {
+  DevBlock d{};
+  std::vector<void*> allocs;  // device allocations owned by the block
+  // host copies of the 1-D grids (1-based meaning, v[i-1])
+  std::vector<double> x1, y1, z1, dxa, dya, dza, xu, yu, zu, xv, yv, zv, xw, yw, zw, xp, yp, zp;
+  std::vector<double> Acx, Acy, Acz;  // column-major (n,3)
+  std::vector<double> ca[N_TAB], ck[N_TAB];
+  double dx = 0, dy = 0, dz = 0, omega = 1.0;
+  int64_t move_check = 0, blk_mv_tag = 0;
+  bool is_coarse = false, has_body = false;
+  bool coeffs_ready = false;
+  int64_t inor = 1;
+  BlockStats* stats = nullptr;     // device
+  double* grid_buf = nullptr;      // device buffer holding all 1-D arrays
+  double* coef_buf = nullptr;      // device Acx/Acy/Acz + ca/ck tables
+  int surf_cap_e = 0, surf_cap_n = 0;
+  // per-block barrier words for persistent kernels: [count, gen]
+  unsigned* bar = nullptr;
+  // mixed-precision solve: FP32 sweeps per correction and their relaxation
+  // (0 = defaults chosen from the block size)
+  int dc_inner = 0;
+  double dc_omega = 0.0;
+};
+
+struct HostInterface {
+  bcfd_handle a = 0, b = 0;  // block handles (a coarse, b fine)
+  int64_t a_msh = 1, b_msh = 2;
+  double box[6] = {0, 0, 0, 0, 0, 0};
+  // 12 tables (3, cap) int64 in the reference layout, order px py pz ux uy uz vx vy vz wx wy wz
+  std::vector<int64_t> tab[12];
+  int64_t counter[12] = {0};
+  int64_t cap[12] = {0};
+  int* dtab = nullptr;  // device copy, int32, same layout, each table at offset off[t]
+  int64_t off[12] = {0};
+};
+
+enum TabId { TPX = 0, TPY, TPZ, TUX, TUY, TUZ, TVX, TVY, TVZ, TWX, TWY, TWZ };
+
+struct Lib {
+  std::recursive_mutex mu;
+  bool ready = false;
+  int device = 0;
+  int nsm = 0;
+  cudaStream_t s = nullptr;
+  std::vector<HostBlock*> blocks;      // handle h -> blocks[h-1] (nullptr when destroyed)
+  std::vector<HostInterface*> ifs;     // interface handle -> ifs[h-1]
+  int64_t launches = 0;
+  // roles for bcfd_run_steps
+};
+
+Lib& lib();
+HostBlock* get_block(bcfd_handle h);
+HostInterface* get_iface(bcfd_handle h);
+
+// record one kernel launch (for the launch counter) and check the launch
+int note_launch(cudaError_t e = cudaGetLastError());
+#define BCFD_LAUNCHED() do { int _r = ::bcfd::note_launch(); if (_r) return _r; } while (0)
+#define BCFD_CUDA(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { ::bcfd::report_cuda(_e, #x, __FILE__, __LINE__); return BCFD_E_CUDA; } } while (0)
+void report_cuda(cudaError_t e, const char* what, const char* file, int line);
+
+// read and clear a block's device error word (synchronises)
+int take_block_error(HostBlock* hb);
+
+// ---- launchers implemented by the kernel translation units (return status) ----
+// k_poisson.cu
+int launch_compute_div(HostBlock* hb);
+int launch_correct_pressure(HostBlock* hb);
+int launch_correct_velocity(HostBlock* hb, double dt);
+int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi);
+int launch_zero_poisson(HostBlock* hb);
+int launch_steady_state(HostBlock* hb, double dt);
+int launch_copy_t_to_n(HostBlock* hb);
+int launch_copy_n_to_t(HostBlock* hb);
+int launch_update_masks(HostBlock* hb);
+int launch_pack(HostBlock* hb, const double* natural_dev, double* packed[2]);
+int launch_unpack(HostBlock* hb, double* const packed[2], double* natural_dev);
+int launch_max_div(HostBlock* hb);
+int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol);
+// k_momentum.cu
+int launch_momentum(HostBlock* hb, double dt, double re);
+int launch_velocity_bc(HostBlock* hb, double dt, double uc);
+int launch_solid_bc(HostBlock* hb, bool move);
+// k_search.cu
+int launch_surface_norm(HostBlock* hb, int64_t inor);
+int launch_tagging(HostBlock* hb);
+int launch_retagging(HostBlock* hb);
+int launch_cellcount(HostBlock* hb, bool coarse);
+int launch_norm_distance(HostBlock* hb);
+int launch_find_ts(HostBlock* hb);
+int launch_fine_block_cell(HostBlock* a, HostInterface* it, bool first);
+int launch_build_list(HostBlock* hb, int which, int* out_ijk, int64_t cap, int64_t* count_host);
+// k_forcing.cu
+int launch_forcing_velocity(HostBlock* hb, int mode);  // 0 forcing1, 1 field, 2 ghost
+int launch_forcing_pressure(HostBlock* hb, int mode);
+// k_interp.cu
+int launch_face_fill(HostInterface* it, int comp, int which);  // which: 0 t-fields, 1 pc, 2 n-fields
+int launch_restrict(HostInterface* it, int comp, int which);
+int launch_fine_update_mv(HostInterface* it);
+// k_stress.cu
+int launch_stress(HostBlock* hb, double mu_f, double rho_f, double* out_host);
+
+}  // namespace bcfd

@@ -1,0 +1,450 @@
+// C-ABI entry points, part 2: interfaces, poissonSolver orchestration, the
+// whole-step driver and the named read-back of device arrays.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bcfd_host.h"
+
+namespace bcfd {
+namespace {
+
+#define TRY(x) do { int _r = (x); if (_r) return _r; } while (0)
+
+// set_interface_detail, src/InterfaceDetail.f90:168-241.  var is the coarse
+// coordinate array (1-based meaning, var[i-1]); the table is (3, n) int64.
+void set_interface_detail(const std::vector<double>& var, double s, double e, int64_t factor,
+                          std::vector<int64_t>& det, int64_t& counter, int64_t starter) {
+  const int64_t n = (int64_t)var.size();
+  int64_t xx1 = 0, xx2 = 0;
+  for (int64_t i = 1; i <= n; ++i)
+    if (var[i - 1] > s) {
+      xx1 = i;
+      break;
+    }
+  for (int64_t i = xx1; i <= n; ++i)
+    if (var[i - 1] > e) {
+      xx2 = i - 1;
+      break;
+    }
+  det.clear();
+  auto put = [&](int64_t a, int64_t b, int64_t c) {
+    det.push_back(a);
+    det.push_back(b);
+    det.push_back(c);
+  };
+  put(xx1 - 1, starter - 1, starter - 1);
+  int64_t ender = starter + factor - 1;
+  counter = 2;
+  for (;;) {
+    put(xx1, starter, ender);
+    starter = ender + 1;
+    ender = ender + factor;
+    counter = counter + 1;
+    xx1 = xx1 + 1;
+    if (xx1 > xx2) break;
+  }
+  put(xx2 + 1, starter, starter);
+}
+
+int upload_iface(HostInterface* it) {
+  size_t tot = 0;
+  for (int t = 0; t < 12; ++t) {
+    it->off[t] = (int64_t)tot;
+    tot += it->tab[t].size();
+  }
+  std::vector<int> h(tot);
+  for (int t = 0; t < 12; ++t)
+    for (size_t q = 0; q < it->tab[t].size(); ++q) h[it->off[t] + q] = (int)it->tab[t][q];
+  if (it->dtab) cudaFree(it->dtab);
+  BCFD_CUDA(cudaMalloc(&it->dtab, std::max<size_t>(tot, 1) * sizeof(int)));
+  BCFD_CUDA(cudaMemcpyAsync(it->dtab, h.data(), tot * sizeof(int), cudaMemcpyHostToDevice, stream()));
+  BCFD_CUDA(cudaStreamSynchronize(stream()));
+  return 0;
+}
+
+int sync_err(HostBlock* hb) { return take_block_error(hb); }
+
+// all registered blocks in registration order
+std::vector<std::pair<bcfd_handle, HostBlock*>> blocks() {
+  std::vector<std::pair<bcfd_handle, HostBlock*>> v;
+  for (size_t q = 0; q < lib().blocks.size(); ++q)
+    if (lib().blocks[q]) v.push_back({(bcfd_handle)(q + 1), lib().blocks[q]});
+  return v;
+}
+
+int fine_update_newv_bd() {
+  for (HostInterface* it : lib().ifs)
+    if (it) {
+      TRY(launch_face_fill(it, 1, 0));
+      TRY(launch_face_fill(it, 2, 0));
+      TRY(launch_face_fill(it, 3, 0));
+    }
+  return 0;
+}
+int fine_update_pc_bd() {
+  for (HostInterface* it : lib().ifs)
+    if (it) TRY(launch_face_fill(it, 0, 1));
+  return 0;
+}
+int fine_update_bd_mv(HostInterface* it) {
+  for (int c = 0; c < 4; ++c) TRY(launch_face_fill(it, c, 2));
+  return 0;
+}
+int coarse_update() {
+  for (HostInterface* it : lib().ifs)
+    if (it)
+      for (int c = 0; c < 4; ++c) TRY(launch_restrict(it, c, 2));
+  return 0;
+}
+int coarse_update_newv() {
+  for (HostInterface* it : lib().ifs)
+    if (it)
+      for (int c = 1; c < 4; ++c) TRY(launch_restrict(it, c, 0));
+  return 0;
+}
+int coarse_update_pc() {
+  for (HostInterface* it : lib().ifs)
+    if (it) TRY(launch_restrict(it, 0, 1));
+  return 0;
+}
+
+struct SolveCfg {
+  int64_t itmax;
+  double epsi, dt, uc;
+  int precision;
+  double div_tol;
+};
+
+int sor(HostBlock* hb, const SolveCfg& c) {
+  if (c.precision == 1) return launch_sor_mixed(hb, c.itmax, c.dt, c.div_tol);
+  return launch_sor(hb, c.itmax, c.dt, c.epsi);
+}
+
+// poissonSolver, src/PcorVcor.F90:22-220, over the blocks with 1-based
+// registration index in [start, finish] by step; no host round trip.
+int poisson(const SolveCfg& c, int start, int finish, int step) {
+  auto all = blocks();
+  auto in = [&](bcfd_handle g) { return g >= start && g <= finish && (g - start) % step == 0; };
+  for (auto& [g, hb] : all)
+    if (in(g)) TRY(launch_zero_poisson(hb));
+  TRY(fine_update_newv_bd());
+  TRY(coarse_update_newv());
+  for (auto& [g, hb] : all)
+    if (in(g)) {
+      TRY(launch_compute_div(hb));
+      if (g != 1) TRY(sor(hb, c));
+    }
+  TRY(coarse_update_pc());
+  for (auto& [g, hb] : all)
+    if (in(g) && g == 1) TRY(sor(hb, c));
+  TRY(fine_update_pc_bd());
+  for (auto& [g, hb] : all)
+    if (in(g) && g != 1) TRY(sor(hb, c));
+  TRY(coarse_update_pc());
+  for (auto& [g, hb] : all)
+    if (in(g)) {
+      TRY(launch_correct_pressure(hb));
+      TRY(launch_correct_velocity(hb, c.dt));
+    }
+  for (auto& [g, hb] : all)
+    if (in(g) && g == 1) TRY(launch_velocity_bc(hb, c.dt, c.uc));
+  for (auto& [g, hb] : all)
+    if (in(g)) TRY(launch_steady_state(hb, c.dt));
+  for (auto& [g, hb] : all)
+    if (in(g)) TRY(launch_copy_t_to_n(hb));
+  for (HostInterface* it : lib().ifs)
+    if (it && get_block(it->b)) TRY(fine_update_bd_mv(it));
+  TRY(coarse_update());
+  return 0;
+}
+
+// One time step in the phase order of app/main.F90:129-265 for blocks whose
+// roles are set by bcfd_block_set_role.  A block with domain BCs gets
+// velocityBC before and after its IB forcing (main.F90:139-145); body blocks
+// get pressureForcing1 and the per-step re-Search of main.F90:232-263.  The
+// body is stationary: the kinematics / block-move stage of main.F90:169-230
+// leaves the geometry unchanged and is not run.
+int step_once(const bcfd_step_config& cfg) {
+  SolveCfg c{cfg.pc_ita_max, cfg.epsi, cfg.deltat, cfg.uc, cfg.precision, cfg.div_tol};
+  auto all = blocks();
+  for (auto& [g, hb] : all) {
+    TRY(launch_momentum(hb, cfg.deltat, cfg.re));
+    if (hb->is_coarse) TRY(launch_velocity_bc(hb, cfg.deltat, cfg.uc));
+    if (hb->has_body) {
+      TRY(launch_solid_bc(hb, false));
+      TRY(launch_forcing_velocity(hb, 0));
+    }
+    if (hb->is_coarse) TRY(launch_velocity_bc(hb, cfg.deltat, cfg.uc));
+  }
+  TRY(poisson(c, 1, (int)lib().blocks.size(), 1));
+  for (auto& [g, hb] : all)
+    if (hb->has_body) TRY(launch_forcing_pressure(hb, 0));
+  for (auto& [g, hb] : all) {
+    if (!hb->has_body) continue;
+    hb->blk_mv_tag = 0;
+    TRY(launch_retagging(hb));
+    TRY(launch_cellcount(hb, false));
+    if (hb->move_check == 1) {
+      TRY(launch_solid_bc(hb, true));
+      TRY(launch_copy_n_to_t(hb));
+    }
+    hb->move_check = 0;
+    TRY(launch_norm_distance(hb));
+    TRY(launch_find_ts(hb));
+    TRY(launch_forcing_velocity(hb, 1));
+    TRY(launch_forcing_pressure(hb, 1));
+    TRY(launch_forcing_velocity(hb, 2));
+    TRY(launch_forcing_pressure(hb, 2));
+  }
+  return 0;
+}
+
+}  // namespace
+}  // namespace bcfd
+
+using namespace bcfd;
+
+#define LOCK() std::lock_guard<std::recursive_mutex> _lk(lib().mu)
+
+extern "C" {
+
+int bcfd_interface_create(bcfd_handle a, bcfd_handle b, int64_t a_msh, int64_t b_msh,
+                          const double* box, bcfd_handle* out) {
+  LOCK();
+  HostBlock* A = get_block(a);
+  HostBlock* B = get_block(b);
+  if (!A || !B) return BCFD_E_HANDLE;
+  if (!box || !out || a_msh <= 0 || b_msh <= 0 || b_msh % a_msh) return BCFD_E_ARG;
+  HostInterface* it = new HostInterface();
+  it->a = a;
+  it->b = b;
+  it->a_msh = a_msh;
+  it->b_msh = b_msh;
+  std::copy(box, box + 6, it->box);
+  const int64_t f = b_msh / a_msh;
+  const std::vector<double>* g[12] = {&A->xp, &A->yp, &A->zp, &A->xu, &A->yu, &A->zu,
+                                      &A->xv, &A->yv, &A->zv, &A->xw, &A->yw, &A->zw};
+  const int starter[12] = {2, 2, 2, 3, 2, 2, 2, 3, 2, 2, 2, 3};
+  for (int t = 0; t < 12; ++t) {
+    const int ax = t % 3;
+    set_interface_detail(*g[t], box[2 * ax], box[2 * ax + 1], f, it->tab[t], it->counter[t], starter[t]);
+  }
+  int r = upload_iface(it);
+  if (r) {
+    delete it;
+    return r;
+  }
+  lib().ifs.push_back(it);
+  *out = (bcfd_handle)lib().ifs.size();
+  return 0;
+}
+
+int bcfd_interface_table(bcfd_handle h, const char* name, int64_t* out, int64_t n, int64_t* counter) {
+  LOCK();
+  HostInterface* it = get_iface(h);
+  if (!it) return BCFD_E_HANDLE;
+  static const char* names[12] = {"px", "py", "pz", "ux", "uy", "uz", "vx", "vy", "vz", "wx", "wy", "wz"};
+  for (int t = 0; t < 12; ++t)
+    if (name && std::strcmp(name, names[t]) == 0) {
+      if (counter) *counter = it->counter[t];
+      const int64_t m = std::min<int64_t>(n, (int64_t)it->tab[t].size());
+      if (out) std::copy(it->tab[t].begin(), it->tab[t].begin() + m, out);
+      return 0;
+    }
+  return BCFD_E_ARG;
+}
+
+int bcfd_fine_update_pc_bd(void) { LOCK(); return fine_update_pc_bd(); }
+int bcfd_fine_update_newv_bd(void) { LOCK(); return fine_update_newv_bd(); }
+int bcfd_fine_update_bd_mv(bcfd_handle h) {
+  LOCK();
+  HostInterface* it = get_iface(h);
+  if (!it) return BCFD_E_HANDLE;
+  return fine_update_bd_mv(it);
+}
+int bcfd_coarse_update(void) { LOCK(); return coarse_update(); }
+int bcfd_coarse_update_newv(void) { LOCK(); return coarse_update_newv(); }
+int bcfd_coarse_update_pc(void) { LOCK(); return coarse_update_pc(); }
+int bcfd_fine_update_mv(bcfd_handle h) {
+  LOCK();
+  HostInterface* it = get_iface(h);
+  if (!it) return BCFD_E_HANDLE;
+  return launch_fine_update_mv(it);
+}
+
+int bcfd_poisson_solver(int64_t pc_ita_max, double epsi, int64_t ita, double deltat, double totime,
+                        double uc, double* total_time, int start, int finish, int step) {
+  LOCK();
+  (void)ita;
+  if (step <= 0 || start < 1) return BCFD_E_ARG;
+  SolveCfg c{pc_ita_max, epsi, deltat, uc, 0, 0.0};
+  TRY(poisson(c, start, finish, step));
+  int err = 0;
+  for (auto& [g, hb] : blocks())
+    if (g >= start && g <= finish && (g - start) % step == 0) {
+      const int e = sync_err(hb);
+      if (e && !err) err = e;
+      if (total_time) *total_time = totime + *total_time;
+    }
+  return err;
+}
+
+int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps) {
+  LOCK();
+  if (!cfg || n_steps < 0) return BCFD_E_ARG;
+  for (int64_t s = 0; s < n_steps; ++s) TRY(step_once(*cfg));
+  int err = 0;
+  for (auto& [g, hb] : blocks()) {
+    const int e = sync_err(hb);
+    if (e && !err) err = e;
+  }
+  return err;
+}
+
+int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64_t* written) {
+  LOCK();
+  HostBlock* hb = get_block(h);
+  if (!hb) return BCFD_E_HANDLE;
+  if (!name || !out) return BCFD_E_ARG;
+  const std::string s(name);
+  const Dims& d = hb->d.d;
+  DevBlock& D = hb->d;
+  int64_t cnt[6];
+  BCFD_CUDA(cudaMemcpyAsync(cnt, D.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, stream()));
+  BCFD_CUDA(cudaStreamSynchronize(stream()));
+  const int64_t nib = std::min<int64_t>(cnt[C_IB], D.cap_ib), nts = cnt[C_TS];
+  auto dcopy = [&](const double* src, int64_t m) -> int {
+    m = std::min(m, n);
+    BCFD_CUDA(cudaMemcpyAsync(out, src, m * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaStreamSynchronize(stream()));
+    if (written) *written = m;
+    return 0;
+  };
+  auto icopy = [&](const int* src, int64_t m) -> int {
+    m = std::min(m, n);
+    std::vector<int> t((size_t)m);
+    BCFD_CUDA(cudaMemcpyAsync(t.data(), src, m * sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaStreamSynchronize(stream()));
+    for (int64_t q = 0; q < m; ++q) ((int64_t*)out)[q] = t[q];
+    if (written) *written = m;
+    return 0;
+  };
+  auto hcopy = [&](const std::vector<double>& v) -> int {
+    const int64_t m = std::min<int64_t>(n, (int64_t)v.size());
+    std::copy(v.begin(), v.begin() + m, (double*)out);
+    if (written) *written = m;
+    return 0;
+  };
+  if (s == "pc" || s == "b") {
+    double* tmp;
+    BCFD_CUDA(cudaMalloc(&tmp, d.npts() * sizeof(double)));
+    double* const* src = s == "pc" ? D.pc : D.bpk;
+    int r = launch_unpack(hb, src, tmp);
+    if (!r) r = dcopy(tmp, d.npts());
+    cudaFree(tmp);
+    return r;
+  }
+  const char* fnames[7] = {"xcent", "ycent", "zcent", "cosAlpha", "cosBeta", "cosGamma", "element_length"};
+  double* fptr[7] = {D.xcent, D.ycent, D.zcent, D.cosA, D.cosB, D.cosG, D.elen};
+  for (int q = 0; q < 7; ++q)
+    if (s == fnames[q]) return dcopy(fptr[q], D.ne);
+  const char* ndn[7] = {"pNormDis", "u1NormDis", "u2NormDis", "v1NormDis", "v2NormDis", "w1NormDis", "w2NormDis"};
+  const char* neln[7] = {"nelp", "nelu1", "nelu2", "nelv1", "nelv2", "nelw1", "nelw2"};
+  for (int q = 0; q < 7; ++q) {
+    if (s == ndn[q]) return dcopy(D.nd[q], nib);
+    if (s == neln[q]) return icopy(D.nel[q], nib);
+  }
+  const char* gn[14] = {"p_ghost", "pt_ghost", "u2_ghost", "u2t_ghost", "v2_ghost", "v2t_ghost", "w2_ghost",
+                        "w2t_ghost", "u1_ghost", "u1t_ghost", "v1_ghost", "v1t_ghost", "w1_ghost", "w1t_ghost"};
+  for (int q = 0; q < 14; ++q)
+    if (s == gn[q]) return dcopy(D.ghost[q], nts);
+  if (s == "index_ts") return icopy(D.ts_idx, nts);
+  if (s == "Acx") return hcopy(hb->Acx);
+  if (s == "Acy") return hcopy(hb->Acy);
+  if (s == "Acz") return hcopy(hb->Acz);
+  const char* tn[N_TAB] = {"uu", "vv", "ww", "uv", "uw", "vu", "vw", "wu", "wv"};
+  for (int t = 0; t < N_TAB; ++t) {
+    if (s == std::string("ca_") + tn[t]) return hcopy(hb->ca[t]);
+    if (s == std::string("ck_") + tn[t]) return hcopy(hb->ck[t]);
+  }
+  const char* grn[18] = {"x1", "y1", "z1", "deltax", "deltay", "deltaz", "xu", "yu", "zu",
+                         "xv", "yv", "zv", "xw", "yw", "zw", "xp", "yp", "zp"};
+  const std::vector<double>* grv[18] = {&hb->x1, &hb->y1, &hb->z1, &hb->dxa, &hb->dya, &hb->dza,
+                                        &hb->xu, &hb->yu, &hb->zu, &hb->xv, &hb->yv, &hb->zv,
+                                        &hb->xw, &hb->yw, &hb->zw, &hb->xp, &hb->yp, &hb->zp};
+  for (int q = 0; q < 18; ++q)
+    if (s == grn[q]) return hcopy(*grv[q]);
+  // index lists as (count, 3) column-major int64
+  auto list_out = [&](const std::vector<int>& ijk, int64_t m, int64_t cap) -> int {
+    if (3 * m > n) return BCFD_E_ARG;
+    int64_t* o = (int64_t*)out;
+    for (int64_t q = 0; q < m; ++q) {
+      o[q] = ijk[q];
+      o[m + q] = ijk[cap + q];
+      o[2 * m + q] = ijk[2 * cap + q];
+    }
+    if (written) *written = 3 * m;
+    return 0;
+  };
+  if (s == "interceptedIndexPtr") {
+    std::vector<int> t(3 * (size_t)nib);
+    BCFD_CUDA(cudaMemcpyAsync(t.data(), D.ib_i, nib * sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaMemcpyAsync(t.data() + nib, D.ib_j, nib * sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaMemcpyAsync(t.data() + 2 * nib, D.ib_k, nib * sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaStreamSynchronize(stream()));
+    return list_out(t, nib, nib);
+  }
+  if (s == "TSIndexPtr") {
+    std::vector<int> ts((size_t)nts), ii((size_t)nib), jj((size_t)nib), kk((size_t)nib);
+    BCFD_CUDA(cudaMemcpyAsync(ts.data(), D.ts_idx, nts * sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaMemcpyAsync(ii.data(), D.ib_i, nib * sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaMemcpyAsync(jj.data(), D.ib_j, nib * sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaMemcpyAsync(kk.data(), D.ib_k, nib * sizeof(int), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaStreamSynchronize(stream()));
+    std::vector<int> t(3 * (size_t)nts);
+    for (int64_t q = 0; q < nts; ++q) {
+      t[q] = ii[ts[q] - 1];
+      t[nts + q] = jj[ts[q] - 1];
+      t[2 * nts + q] = kk[ts[q] - 1];
+    }
+    return list_out(t, nts, nts);
+  }
+  int which = -1;
+  if (s == "fluidIndexPtr" || s == "redCellIndexPtr" || s == "blackCellIndexPtr") which = 0;
+  if (s == "solidIndexPtr") which = 1;
+  if (which >= 0) {
+    const int64_t cap = (int64_t)d.nx * d.ny * d.nz;
+    int* buf;
+    BCFD_CUDA(cudaMalloc(&buf, 3 * cap * sizeof(int)));
+    int64_t m = 0;
+    int r = launch_build_list(hb, which, buf, cap, &m);
+    std::vector<int> t(3 * (size_t)cap);
+    if (!r) {
+      BCFD_CUDA(cudaMemcpy(t.data(), buf, 3 * cap * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    cudaFree(buf);
+    if (r) return r;
+    if (s == "redCellIndexPtr" || s == "blackCellIndexPtr") {
+      const int want = s == "redCellIndexPtr" ? 1 : 0;
+      std::vector<int> u;
+      std::vector<int> a, b2, c2;
+      for (int64_t q = 0; q < m; ++q)
+        if (((t[q] + t[cap + q] + t[2 * cap + q]) & 1) == want) {
+          a.push_back(t[q]);
+          b2.push_back(t[cap + q]);
+          c2.push_back(t[2 * cap + q]);
+        }
+      const int64_t mm = (int64_t)a.size();
+      u.insert(u.end(), a.begin(), a.end());
+      u.insert(u.end(), b2.begin(), b2.end());
+      u.insert(u.end(), c2.begin(), c2.end());
+      return list_out(u, mm, mm);
+    }
+    return list_out(t, m, cap);
+  }
+  return BCFD_E_ARG;
+}
+
+}  // extern "C"

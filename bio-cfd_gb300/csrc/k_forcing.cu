@@ -1,0 +1,485 @@
+// Immersed-boundary forcing of src/Forcing.f90 on the GPU.
+//
+// velocityForcing1 and pressureForcing1/Field write the very array their
+// probes interpolate from, inside one serial loop over the IB list: a probe
+// stencil can read a value that an earlier iteration just wrote.  The GPU
+// path reproduces that serial semantics exactly:
+//   * a task is one reconstruction (IB cell n, component c) at serial
+//     position pos = 6n + c (velocity: U2,U1,V2,V1,W2,W1) or n (pressure);
+//   * for every stencil point the task finds the latest task before it that
+//     writes that point (a u point u(a,b,c) is written by the U2 task of cell
+//     (a,b,c) and the U1 task of cell (a+1,b,c), the later one winning);
+//   * tasks are levelled (level = 1 + max level of their dependencies) and
+//     evaluated level by level, reading each stencil value either from the
+//     unmodified array or from the dependency's output slot;
+//   * last writers scatter their outputs into the array at the end.
+// Everything runs in one cooperative launch with bounded grid barriers.  The
+// Field / Ghost velocity variants read ut and write u (or ghost arrays) and
+// therefore run as plain data-parallel kernels.
+#include "bcfd_host.h"
+
+namespace bcfd {
+
+namespace {
+
+enum Comp { CU2 = 0, CU1, CV2, CV1, CW2, CW1 };
+
+struct Grid3 {
+  const double *x, *y, *z;
+  int nx, ny, nz;  // array lengths
+};
+
+__device__ __forceinline__ Grid3 comp_grid(const DevBlock& B, int axis) {
+  const Dims& d = B.d;
+  switch (axis) {
+    case 1: return {B.xu, B.yu, B.zu, d.NX + 1, d.NY, d.NZ};
+    case 2: return {B.xv, B.yv, B.zv, d.NX, d.NY + 1, d.NZ};
+    case 3: return {B.xw, B.yw, B.zw, d.NX, d.NY, d.NZ + 1};
+    default: return {B.xp, B.yp, B.zp, d.NX, d.NY, d.NZ};
+  }
+}
+
+// find_index_in_array (src/Forcing.f90:1165-1183): first i in [s, f] with
+// a(i) <= v < a(i+1).  Indices outside the array are skipped; when no
+// bracket exists the error word is set and a clamped start index returned.
+__device__ int find_index(const DevBlock& B, double v, const double* a, int len, int s, int f) {
+  for (int i = s; i <= f; ++i) {
+    if (i < 1 || i + 1 > len) continue;
+    if (v >= a[i - 1] && v < a[i]) return i;
+  }
+  set_err(B.err, BCFD_E_NOTFOUND);
+  int r = s < 1 ? 1 : s;
+  if (r + 1 > len) r = len - 1;
+  return r;
+}
+
+__device__ __forceinline__ double bilinear(double x, double y, double x1, double x2, double y1,
+                                           double y2, double f0, double f1, double f2, double f3) {
+  const double numer = f0 * (x2 - x) * (y2 - y) + f2 * (x2 - x) * (y - y1) +
+                       f1 * (x - x1) * (y2 - y) + f3 * (x - x1) * (y - y1);
+  const double denom = (x2 - x1) * (y2 - y1);
+  return numer / denom;
+}
+
+__device__ __forceinline__ double linear(double x, double x0, double x1, double y0, double y1) {
+  return y0 + (x - x0) * (y1 - y0) / (x1 - x0);
+}
+
+__device__ __forceinline__ double derivative(double x, double x2, double x1, double p_x,
+                                             double p_x2, double p_x1) {
+  const double h2 = fabs(x2 - x);
+  const double h1 = fabs(x1 - x);
+  return (h1 * h1 * p_x2 - h2 * h2 * p_x1 + (h2 * h2 - h1 * h1) * p_x) /
+         (h1 * h2 * (h1 + h2) + 1e-16);
+}
+
+// The probe of one reconstruction: position and bracketing indices.
+struct Probe {
+  double px, py, pz;   // probe point
+  int ix, iy, iz;      // find_index results
+  int ii, jj, kk;      // stencil base of the variable (offset axis applied)
+  double s2n, pt1;
+  int e;               // element (0-based)
+  int ti, tj, tk;      // written sample (target) index
+  int axis;            // 0 p, 1 u, 2 v, 3 w
+};
+
+// mode 0: ...Forcing1, 1: ...Field, 2: ...Ghost.  comp < 0 for pressure.
+// n is the IB index (0-based) for modes 0/1 and the TS index for mode 2.
+__device__ Probe make_probe(const DevBlock& B, int mode, int comp, int n) {
+  Probe P;
+  const Dims& d = B.d;
+  const int ib = mode == 2 ? B.ts_idx[n] - 1 : n;
+  const int i = B.ib_i[ib], j = B.ib_j[ib], k = B.ib_k[ib];
+  int slot;
+  if (comp < 0) {
+    slot = N_P;
+    P.axis = 0;
+  } else {
+    // nel / NormDis slots: U1=1, U2=2, V1=3, V2=4, W1=5, W2=6
+    slot = comp + ((comp & 1) ? 0 : 2);
+    P.axis = 1 + comp / 2;
+  }
+  P.e = B.nel[slot][ib] - 1;
+  const double sg = mode == 2 ? -1.0 : 1.0;
+  P.s2n = mode == 2 ? -B.nd[slot][ib] : B.nd[slot][ib];
+  const double s2n = P.s2n;
+  P.pt1 = 1.5 * sqrt(B.dxa[i - 1] * B.dxa[i - 1] + B.dya[j - 1] * B.dya[j - 1] +
+                     B.dza[k - 1] * B.dza[k - 1]) +
+          (fabs(s2n) - s2n) * 0.5;
+  const Grid3 G = comp_grid(B, P.axis);
+  double qx = G.x[i - 1], qy = G.y[j - 1], qz = G.z[k - 1];
+  if (comp == CU2) qx = G.x[i];
+  if (comp == CV2) qy = G.y[j];
+  if (comp == CW2) qz = G.z[k];
+  if (sg > 0) {
+    P.px = qx + P.pt1 * B.cosA[P.e];
+    P.py = qy + P.pt1 * B.cosB[P.e];
+    P.pz = qz + P.pt1 * B.cosG[P.e];
+  } else {
+    P.px = qx - P.pt1 * B.cosA[P.e];
+    P.py = qy - P.pt1 * B.cosB[P.e];
+    P.pz = qz - P.pt1 * B.cosG[P.e];
+  }
+  if (mode == 0) {
+    P.ix = find_index(B, P.px, G.x, G.nx, 1, d.nx + (comp == CU2 ? 2 : 1));
+    P.iy = find_index(B, P.py, G.y, G.ny, 1, d.ny + (comp == CV2 ? 2 : 1));
+    P.iz = find_index(B, P.pz, G.z, G.nz, 1, d.nz + (comp == CW2 ? 2 : 1));
+    if (comp == CU2 && P.ix == d.nx + 2) P.ix = d.nx + 1;
+    if (comp == CU1 && P.ix == 1) P.ix = 2;
+    if (comp == CV2 && P.iy == d.ny + 2) P.iy = d.ny + 1;
+    if (comp == CV1 && P.iy == 1) P.iy = 2;
+    if (comp == CW2 && P.iz == d.nz + 2) P.iz = d.nz + 1;
+    if (comp == CW1 && P.iz == 1) P.iz = 2;
+  } else {
+    P.ix = find_index(B, P.px, G.x, G.nx, i - 7, i + 7);
+    P.iy = find_index(B, P.py, G.y, G.ny, j - 7, j + 7);
+    P.iz = find_index(B, P.pz, G.z, G.nz, k - 7, k + 7);
+  }
+  P.ii = P.ix - (P.axis == 1);
+  P.jj = P.iy - (P.axis == 2);
+  P.kk = P.iz - (P.axis == 3);
+  // keep every stencil point inside the array (the reference would read out
+  // of bounds here; flag it instead)
+  if (P.ii < 1 || P.ii + 1 > d.NX || P.jj < 1 || P.jj + 1 > d.NY || P.kk < 1 || P.kk + 1 > d.NZ) {
+    set_err(B.err, BCFD_E_NOTFOUND);
+    P.ii = max(1, min(P.ii, d.NX - 1));
+    P.jj = max(1, min(P.jj, d.NY - 1));
+    P.kk = max(1, min(P.kk, d.NZ - 1));
+  }
+  P.ti = i - (comp == CU1);
+  P.tj = j - (comp == CV1);
+  P.tk = k - (comp == CW1);
+  return P;
+}
+
+// compute_value_and_derivatives (src/Forcing.f90:1091-1161) on the 8 values
+// f[a + 2b + 4c] = var(ii+a, jj+b, kk+c)
+__device__ void value_and_derivatives(const DevBlock& B, const Probe& P, const double f[8],
+                                      double& val, double der[3]) {
+  const Grid3 G = comp_grid(B, P.axis);
+  const int i = P.ix, j = P.iy, k = P.iz;
+  const double x = P.px, y = P.py, z = P.pz;
+  const double yj = G.y[j - 1], yj1 = G.y[j], zk = G.z[k - 1], zk1 = G.z[k], xi = G.x[i - 1],
+               xi1 = G.x[i];
+  const double t11 = bilinear(y, z, yj, yj1, zk, zk1, f[0], f[2], f[4], f[6]);
+  const double t12 = bilinear(y, z, yj, yj1, zk, zk1, f[1], f[3], f[5], f[7]);
+  const double t21 = bilinear(x, z, xi, xi1, zk, zk1, f[0], f[1], f[4], f[5]);
+  const double t22 = bilinear(x, z, xi, xi1, zk, zk1, f[2], f[3], f[6], f[7]);
+  const double t31 = bilinear(x, y, xi, xi1, yj, yj1, f[0], f[1], f[2], f[3]);
+  const double t32 = bilinear(x, y, xi, xi1, yj, yj1, f[4], f[5], f[6], f[7]);
+  val = linear(x, xi, xi1, t11, t12);
+  der[0] = derivative(x, xi1, xi, val, t12, t11);
+  der[1] = derivative(y, yj1, yj, val, t22, t21);
+  der[2] = derivative(z, zk1, zk, val, t32, t31);
+}
+
+__device__ __forceinline__ double dotn(const DevBlock& B, int e, const double d[3]) {
+  return d[0] * B.cosA[e] + d[1] * B.cosB[e] + d[2] * B.cosG[e];
+}
+
+// surface velocity of a sample (src/Forcing.f90: see the oracle for lines);
+// the `0 + ydot` forms of Forcing.f90:237 and :551 are kept (they map -0 to +0)
+__device__ double surf_velocity(const DevBlock& B, int e, int comp, int mode) {
+  const int sid = B.surf_id[e];
+  if (comp == CU2 || comp == CU1) return B.xdot;
+  if (comp == CV2 || comp == CV1) {
+    if (sid == 50) {
+      const bool plus0 = (comp == CV1 && mode == 0) || (comp == CV2 && mode == 2);
+      return plus0 ? 0.0 + B.ydot : B.ydot;
+    }
+    const double td = sid == 51 ? B.thetaDot1 : B.thetaDot2;
+    if (mode == 0) return -td * (B.zcent[e] - B.piv_z) + B.ydot;
+    return -td * (B.zcent[e] - B.piv_z) + (-B.alphaDot) * (B.xcent[e] - B.piv_x) + B.ydot;
+  }
+  if (sid == 50) return 0.0;
+  const double td = sid == 51 ? B.thetaDot1 : B.thetaDot2;
+  return td * (B.ycent[e] - B.piv_y);
+}
+
+__device__ __forceinline__ double vel_quad(double pos_val, double surf, double dn, double n1,
+                                           double s2n) {
+  const double cval = surf;
+  const double bval = 2.0 / n1 * (pos_val - surf) - dn;
+  const double aval = dn / n1 - (pos_val - surf) / (n1 * n1);
+  return aval * (s2n * s2n) + bval * s2n + cval;
+}
+
+// dpdn of the rigid-body acceleration (src/Forcing.f90:29-52, :381-412)
+__device__ double dpdn_body(const DevBlock& B, int e, int mode) {
+  const int sid = B.surf_id[e];
+  double ac_y = 0, ac_z = 0, at_y = 0, at_z = 0;
+  if (sid == 51 || sid == 52) {
+    const double td = sid == 51 ? B.thetaDot1 : B.thetaDot2;
+    const double tdd = sid == 51 ? B.thetaDDot1 : B.thetaDDot2;
+    ac_z = -(td * td) * (B.zcent[e] - B.piv_z);
+    ac_y = -(td * td) * (B.ycent[e] - B.piv_y);
+    at_z = tdd * (B.ycent[e] - B.piv_y);
+    at_y = -tdd * (B.zcent[e] - B.piv_z);
+  }
+  if (mode == 2)
+    return ((ac_z + at_z) * B.cosG[e] + (ac_y + at_y) * B.cosB[e]) + (B.yddot * (B.cosB[e]));
+  return -((ac_z + at_z) * B.cosG[e] + (ac_y + at_y) * B.cosB[e]) - B.yddot * B.cosB[e];
+}
+
+// value of one reconstruction from its 8 stencil values
+__device__ double reconstruct(const DevBlock& B, int mode, int comp, const Probe& P,
+                              const double f[8]) {
+  double val, der[3];
+  value_and_derivatives(B, P, f, val, der);
+  const double dn = mode == 2 ? -1.0 * dotn(B, P.e, der) : dotn(B, P.e, der);
+  const double n1 = P.pt1 + P.s2n;
+  const double s2n = P.s2n;
+  if (comp < 0) {
+    const double dpdn = dpdn_body(B, P.e, mode);
+    const double bval = dpdn;
+    const double aval = (dn - dpdn) / (2.0 * n1);
+    const double cval = val - (dn + dpdn) * n1 * 0.5;
+    return aval * (s2n * s2n) + bval * s2n + cval;
+  }
+  return vel_quad(val, surf_velocity(B, P.e, comp, mode), dn, n1, s2n);
+}
+
+__device__ __forceinline__ double* comp_array(const DevBlock& B, int axis, bool tfield) {
+  switch (axis) {
+    case 1: return tfield ? B.ut : B.u;
+    case 2: return tfield ? B.vt : B.v;
+    case 3: return tfield ? B.wt : B.w;
+    default: return B.p;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// the serial-order DAG path (velocityForcing1, pressureForcing1/Field)
+// ---------------------------------------------------------------------------
+struct DagScratch {
+  double* out;    // per task output
+  int* dep;       // per task 8 dependency task ids (-1: read the array)
+  int* level;     // per task level
+  int* flag;      // [0..1] changed flags, [2] max level, [3] rounds
+};
+
+struct DagArgs {
+  int mode;       // 0 or 1
+  int vel;        // 1: velocity (6 tasks per IB cell), 0: pressure
+};
+
+// latest task before `pos` writing stencil point (a,b,c) of component axis
+__device__ __forceinline__ int last_writer(const DevBlock& B, const DagArgs& g, int axis, int a,
+                                           int b, int c, int pos) {
+  const Dims& d = B.d;
+  if (!g.vel) {
+    const int A = B.ibmap[d.idx(a, b, c)];
+    return (A >= 0 && A < pos) ? A : -1;
+  }
+  const int cA = 2 * (axis - 1), cB = cA + 1;  // the "2" and "1" faces of the axis
+  const int A = B.ibmap[d.idx(a, b, c)];
+  int Bn = -1;
+  const int a1 = a + (axis == 1), b1 = b + (axis == 2), c1 = c + (axis == 3);
+  if (a1 <= d.NX && b1 <= d.NY && c1 <= d.NZ) Bn = B.ibmap[d.idx(a1, b1, c1)];
+  if (Bn >= 0 && 6 * Bn + cB < pos) return 6 * Bn + cB;
+  if (A >= 0 && 6 * A + cA < pos) return 6 * A + cA;
+  return -1;
+}
+
+// is task t the final writer of its target point?
+__device__ __forceinline__ bool is_last_writer(const DevBlock& B, const DagArgs& g, int t,
+                                               const Probe& P) {
+  if (!g.vel) return true;
+  const int comp = t % 6;
+  if (comp & 1) return true;  // a "1" face task is always the later writer
+  const Dims& d = B.d;
+  const int a1 = P.ti + (P.axis == 1), b1 = P.tj + (P.axis == 2), c1 = P.tk + (P.axis == 3);
+  if (a1 > d.NX || b1 > d.NY || c1 > d.NZ) return true;
+  return B.ibmap[d.idx(a1, b1, c1)] < 0;
+}
+
+__global__ void __launch_bounds__(256) k_forcing_dag(DevBlock B, DagArgs g, DagScratch s, GridBar gb) {
+  const int nib = (int)min(B.cnt[C_IB], (int64_t)B.cap_ib);
+  const int nt = g.vel ? 6 * nib : nib;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+  // phase 1: dependencies
+  for (int t = tid; t < nt; t += nthr) {
+    const int n = g.vel ? t / 6 : t, comp = g.vel ? t % 6 : -1;
+    const Probe P = make_probe(B, g.mode, comp, n);
+    int lv = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int w = last_writer(B, g, P.axis, P.ii + (q & 1), P.jj + ((q >> 1) & 1), P.kk + (q >> 2), t);
+      s.dep[8 * t + q] = w;
+      if (w >= 0) lv = 1;
+    }
+    s.level[t] = lv;
+  }
+  if (!grid_sync(gb)) return;
+  // phase 2: levels by monotone relaxation (bounded by the task count)
+  for (int round = 0;; ++round) {
+    __shared__ int s_changed;
+    if (threadIdx.x == 0) s_changed = 0;
+    __syncthreads();
+    int changed = 0, mx = 0;
+    for (int t = tid; t < nt; t += nthr) {
+      int lv = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int w = s.dep[8 * t + q];
+        if (w >= 0) lv = max(lv, __ldcg(s.level + w) + 1);
+      }
+      if (lv != __ldcg(s.level + t)) {
+        __stcg(s.level + t, lv);
+        changed = 1;
+      }
+      mx = max(mx, lv);
+    }
+    if (changed) atomicOr(&s_changed, 1);
+    if (mx) atomicMax(&s.flag[2], mx);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_changed) atomicOr(&s.flag[round & 1], 1);
+    if (!grid_sync(gb)) return;
+    const int any = *((volatile int*)&s.flag[round & 1]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.flag[(round + 1) & 1] = 0;
+    if (!any) break;
+    if (round > nt + 2) {  // cannot happen for a DAG; guard the loop anyway
+      if (threadIdx.x == 0) set_err(B.err, BCFD_E_TIMEOUT);
+      return;
+    }
+    if (!grid_sync(gb)) return;
+  }
+  const int maxl = *((volatile int*)&s.flag[2]);
+  // phase 3: evaluate level by level
+  for (int L = 0; L <= maxl; ++L) {
+    for (int t = tid; t < nt; t += nthr) {
+      if (__ldcg(s.level + t) != L) continue;
+      const int n = g.vel ? t / 6 : t, comp = g.vel ? t % 6 : -1;
+      const Probe P = make_probe(B, g.mode, comp, n);
+      const double* arr = comp_array(B, P.axis, g.vel != 0);
+      double f[8];
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int w = s.dep[8 * t + q];
+        f[q] = w >= 0 ? __ldcg(s.out + w)
+                      : arr[B.d.idx(P.ii + (q & 1), P.jj + ((q >> 1) & 1), P.kk + (q >> 2))];
+      }
+      __stcg(s.out + t, reconstruct(B, g.mode, comp, P, f));
+    }
+    if (!grid_sync(gb)) return;
+  }
+  // phase 4: scatter the final values
+  for (int t = tid; t < nt; t += nthr) {
+    const int n = g.vel ? t / 6 : t, comp = g.vel ? t % 6 : -1;
+    const Probe P = make_probe(B, g.mode, comp, n);
+    if (!is_last_writer(B, g, t, P)) continue;
+    double* arr = comp_array(B, P.axis, g.vel != 0);
+    arr[B.d.idx(P.ti, P.tj, P.tk)] = __ldcg(s.out + t);
+  }
+}
+
+// velocityForcingField (mode 1): reads ut/vt/wt, writes u/v/w -- independent
+__global__ void k_vel_field(DevBlock B) {
+  const int nib = (int)min(B.cnt[C_IB], (int64_t)B.cap_ib);
+  const int nt = 6 * nib;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+    const int n = t / 6, comp = t % 6;
+    const Probe P = make_probe(B, 1, comp, n);
+    const double* src = comp_array(B, P.axis, true);
+    double f[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      f[q] = src[B.d.idx(P.ii + (q & 1), P.jj + ((q >> 1) & 1), P.kk + (q >> 2))];
+    comp_array(B, P.axis, false)[B.d.idx(P.ti, P.tj, P.tk)] = reconstruct(B, 1, comp, P, f);
+  }
+}
+
+// velocityForcingGhost (mode 2): ghost values and the t-ghost saves
+__global__ void k_vel_ghost(DevBlock B) {
+  const int nts = (int)B.cnt[C_TS];
+  const int nt = 6 * nts;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+    const int n = t / 6, comp = t % 6;
+    // ghost slot of the component: U2 2, U1 8, V2 4, V1 10, W2 6, W1 12
+    const int gs = ((comp & 1) ? G_U1 : G_U2) + 2 * (comp >> 1);
+    const Probe P = make_probe(B, 2, comp, n);
+    const double* src = comp_array(B, P.axis, true);
+    double f[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      f[q] = src[B.d.idx(P.ii + (q & 1), P.jj + ((q >> 1) & 1), P.kk + (q >> 2))];
+    B.ghost[gs][n] = reconstruct(B, 2, comp, P, f);
+    B.ghost[gs + 1][n] = comp_array(B, P.axis, false)[B.d.idx(P.ti, P.tj, P.tk)];
+  }
+}
+
+// pressureForcingGhost (mode 2)
+__global__ void k_p_ghost(DevBlock B) {
+  const int nts = (int)B.cnt[C_TS];
+  for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nts; n += gridDim.x * blockDim.x) {
+    const Probe P = make_probe(B, 2, -1, n);
+    double f[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      f[q] = B.p[B.d.idx(P.ii + (q & 1), P.jj + ((q >> 1) & 1), P.kk + (q >> 2))];
+    B.ghost[G_P][n] = reconstruct(B, 2, -1, P, f);
+    B.ghost[G_PT][n] = B.p[B.d.idx(P.ti, P.tj, P.tk)];
+  }
+}
+
+}  // namespace
+
+static DagScratch& dag_scratch(HostBlock* hb, int* status) {
+  static std::vector<std::pair<HostBlock*, std::pair<DagScratch, int64_t>>> tab;
+  *status = 0;
+  const int64_t need = 6 * (int64_t)hb->d.cap_ib;
+  for (auto& p : tab)
+    if (p.first == hb && p.second.second >= need) return p.second.first;
+  DagScratch s{};
+  if (cudaMalloc(&s.out, need * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&s.dep, need * 8 * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s.level, need * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&s.flag, 8 * sizeof(int)) != cudaSuccess)
+    *status = BCFD_E_NOMEM;
+  tab.push_back({hb, {s, need}});
+  return tab.back().second.first;
+}
+
+static int launch_dag(HostBlock* hb, int mode, int vel) {
+  int st = 0;
+  DagScratch& s = dag_scratch(hb, &st);
+  if (st) return st;
+  BCFD_CUDA(cudaMemsetAsync(s.flag, 0, 8 * sizeof(int), stream()));
+  BCFD_CUDA(cudaMemsetAsync(hb->bar, 0, 2 * sizeof(unsigned), stream()));
+  const int threads = 256;
+  const unsigned want = (unsigned)((6 * (int64_t)hb->d.cap_ib + threads - 1) / threads);
+  const unsigned grid = coop_grid((const void*)k_forcing_dag, threads, 0, std::min(want, 2u * (unsigned)num_sms()));
+  GridBar gb = make_bar(hb->d.err, grid);
+  gb.count = hb->bar;
+  gb.gen = hb->bar + 1;
+  DagArgs g{mode, vel};
+  DevBlock B = hb->d;
+  void* args[] = {(void*)&B, (void*)&g, (void*)&s, (void*)&gb};
+  BCFD_CUDA(launch_coop((const void*)k_forcing_dag, grid, threads, args));
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+int launch_forcing_velocity(HostBlock* hb, int mode) {
+  if (hb->d.ne <= 0) return 0;
+  if (mode == 0) return launch_dag(hb, 0, 1);
+  if (mode == 1) {
+    k_vel_field<<<grid_for(6 * (int64_t)hb->d.cap_ib, 128, 2048), 128, 0, stream()>>>(hb->d);
+    BCFD_LAUNCHED();
+    return 0;
+  }
+  k_vel_ghost<<<grid_for(6 * (int64_t)hb->d.cap_ib, 128, 2048), 128, 0, stream()>>>(hb->d);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+int launch_forcing_pressure(HostBlock* hb, int mode) {
+  if (hb->d.ne <= 0) return 0;
+  if (mode == 0 || mode == 1) return launch_dag(hb, mode, 0);
+  k_p_ghost<<<grid_for(hb->d.cap_ib, 128, 2048), 128, 0, stream()>>>(hb->d);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+}  // namespace bcfd

@@ -1,0 +1,253 @@
+// Inter-block coupling kernels: coarse -> fine face ghosts
+// (src/FineInterp_bound.f90), fine -> coarse restriction (src/CoarseInterp.f90)
+// and the post-move volume fill (src/FineInterp.f90).
+//
+// Each interface-table entry (coarse index, fine start, fine end) per axis
+// maps a contiguous range of fine points to one coarse donor position; a
+// thread owns one entry triple (i,j,k) and visits its <= ratio^3 targets.
+// A target belongs to exactly one entry triple, so the edge points visited by
+// two face passes receive the same value -- the passes are order-free.
+#include "bcfd_host.h"
+
+namespace bcfd {
+
+namespace {
+
+struct Tab {
+  const int* t;  // (3, n) column-major, 1-based entries
+  int c;         // counter
+  __device__ int at(int r, int e) const { return t[(r - 1) + 3 * (e - 1)]; }
+};
+
+struct Field {  // a field in natural layout or in the colour-packed layout
+  double* nat;
+  double* pk0;
+  double* pk1;
+};
+
+__device__ __forceinline__ double fget(const Dims& d, const Field& f, int i, int j, int k) {
+  if (f.nat) return f.nat[d.idx(i, j, k)];
+  return (colour_of(i, j, k) ? f.pk1 : f.pk0)[d.pidx(i, j, k)];
+}
+__device__ __forceinline__ void fset(const Dims& d, const Field& f, int i, int j, int k, double v) {
+  if (f.nat) f.nat[d.idx(i, j, k)] = v;
+  else (colour_of(i, j, k) ? f.pk1 : f.pk0)[d.pidx(i, j, k)] = v;
+}
+
+struct Grids {
+  const double *x, *y, *z;
+};
+
+__device__ __forceinline__ double bilinear(double x, double y, double x1, double x2, double y1,
+                                           double y2, double f0, double f1, double f2, double f3) {
+  const double numer = f0 * (x2 - x) * (y2 - y) + f2 * (x2 - x) * (y - y1) +
+                       f1 * (x - x1) * (y2 - y) + f3 * (x - x1) * (y - y1);
+  const double denom = (x2 - x1) * (y2 - y1);
+  return numer / denom;
+}
+__device__ __forceinline__ double linear(double x, double x0, double x1, double y0, double y1) {
+  return y0 + (x - x0) * (y1 - y0) / (x1 - x0);
+}
+
+struct FaceArgs {
+  Tab tx, ty, tz;
+  int comp;          // 0 p, 1 u, 2 v, 3 w
+  Grids ga, gb;      // coarse (donor) and fine (target) grids of the component
+  Field src, dst, dst2;
+  int axis;          // face pass 1..3
+};
+
+// trilinear_interpolation of src/FineInterp_bound.f90:554-603 (donors loc+-1)
+__global__ void k_face(Dims da, Dims db, FaceArgs a) {
+  const int sx = a.axis == 1 ? a.tx.c - 1 : 1, sy = a.axis == 2 ? a.ty.c - 1 : 1,
+            sz = a.axis == 3 ? a.tz.c - 1 : 1;
+  const int nxs = (a.tx.c - 1) / sx + 1, nys = (a.ty.c - 1) / sy + 1, nzs = (a.tz.c - 1) / sz + 1;
+  const int n = nxs * nys * nzs;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int ei = 1 + (t % nxs) * sx, ej = 1 + ((t / nxs) % nys) * sy, ek = 1 + (t / (nxs * nys)) * sz;
+    const int vx1 = a.tx.at(2, ei), vx2 = a.tx.at(3, ei);
+    const int vy1 = a.ty.at(2, ej), vy2 = a.ty.at(3, ej);
+    const int vz1 = a.tz.at(2, ek), vz2 = a.tz.at(3, ek);
+    const int i = a.tx.at(1, ei), j = a.ty.at(1, ej), k = a.tz.at(1, ek);
+    int vi = i, vj = j, vk = k;
+    if (a.comp == 1) vi = i - 1;
+    if (a.comp == 2) vj = j - 1;
+    if (a.comp == 3) vk = k - 1;
+    const double x1 = a.ga.x[i - 2], x2 = a.ga.x[i], y1 = a.ga.y[j - 2], y2 = a.ga.y[j],
+                 z1 = a.ga.z[k - 2], z2 = a.ga.z[k];
+    const double f0 = fget(da, a.src, vi - 1, vj - 1, vk - 1), f1 = fget(da, a.src, vi + 1, vj - 1, vk - 1),
+                 f2 = fget(da, a.src, vi - 1, vj + 1, vk - 1), f3 = fget(da, a.src, vi + 1, vj + 1, vk - 1);
+    const double g0 = fget(da, a.src, vi - 1, vj - 1, vk + 1), g1 = fget(da, a.src, vi + 1, vj - 1, vk + 1),
+                 g2 = fget(da, a.src, vi - 1, vj + 1, vk + 1), g3 = fget(da, a.src, vi + 1, vj + 1, vk + 1);
+    for (int tz = vz1; tz <= vz2; ++tz)
+      for (int ty = vy1; ty <= vy2; ++ty)
+        for (int tx = vx1; tx <= vx2; ++tx) {
+          const double x = a.gb.x[tx - 1], y = a.gb.y[ty - 1], z = a.gb.z[tz - 1];
+          const double za = bilinear(x, y, x1, x2, y1, y2, f0, f1, f2, f3);
+          const double zb = bilinear(x, y, x1, x2, y1, y2, g0, g1, g2, g3);
+          const double r = linear(z, z1, z2, za, zb);
+          const int ox = tx - (a.comp == 1), oy = ty - (a.comp == 2), oz = tz - (a.comp == 3);
+          fset(db, a.dst, ox, oy, oz, r);
+          if (a.dst2.nat || a.dst2.pk0) fset(db, a.dst2, ox, oy, oz, r);
+        }
+  }
+}
+
+// trilinear_interpolation of src/CoarseInterp.f90:447-502 (adjacent donors);
+// the target coarse point of entry i is det(1,i); the donor index is the
+// middle fine index (start+end-1)/2, or `end` along the staggered axis.
+__global__ void k_restrict(Dims da, Dims db, FaceArgs a, int ci) {
+  const int nxs = a.tx.c - 2 * ci + 1, nys = a.ty.c - 2 * ci + 1, nzs = a.tz.c - 2 * ci + 1;
+  if (nxs <= 0 || nys <= 0 || nzs <= 0) return;
+  const int n = nxs * nys * nzs;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int ei = ci + t % nxs, ej = ci + (t / nxs) % nys, ek = ci + t / (nxs * nys);
+    const int tx = a.tx.at(1, ei), ty = a.ty.at(1, ej), tz = a.tz.at(1, ek);
+    int lx = (a.tx.at(2, ei) + a.tx.at(3, ei) - 1) / 2;
+    int ly = (a.ty.at(2, ej) + a.ty.at(3, ej) - 1) / 2;
+    int lz = (a.tz.at(2, ek) + a.tz.at(3, ek) - 1) / 2;
+    if (a.comp == 1) lx = a.tx.at(3, ei);
+    if (a.comp == 2) ly = a.ty.at(3, ej);
+    if (a.comp == 3) lz = a.tz.at(3, ek);
+    int ii = lx, jj = ly, kk = lz, vi = lx, vj = ly, vk = lz;
+    if (a.comp == 1) { ii = lx - 1; vi = lx - 2; }
+    if (a.comp == 2) { jj = ly - 1; vj = ly - 2; }
+    if (a.comp == 3) { kk = lz - 1; vk = lz - 2; }
+    const double x = a.ga.x[tx - 1], y = a.ga.y[ty - 1], z = a.ga.z[tz - 1];
+    const double x1 = a.gb.x[ii - 1], x2 = a.gb.x[ii], y1 = a.gb.y[jj - 1], y2 = a.gb.y[jj],
+                 z1 = a.gb.z[kk - 1], z2 = a.gb.z[kk];
+    const double za = bilinear(x, y, x1, x2, y1, y2, fget(db, a.src, vi, vj, vk),
+                               fget(db, a.src, vi + 1, vj, vk), fget(db, a.src, vi, vj + 1, vk),
+                               fget(db, a.src, vi + 1, vj + 1, vk));
+    const double zb = bilinear(x, y, x1, x2, y1, y2, fget(db, a.src, vi, vj, vk + 1),
+                               fget(db, a.src, vi + 1, vj, vk + 1), fget(db, a.src, vi, vj + 1, vk + 1),
+                               fget(db, a.src, vi + 1, vj + 1, vk + 1));
+    const double r = linear(z, z1, z2, za, zb);
+    const int ox = tx - (a.comp == 1), oy = ty - (a.comp == 2), oz = tz - (a.comp == 3);
+    fset(da, a.dst, ox, oy, oz, r);
+    if (a.dst2.nat || a.dst2.pk0) fset(da, a.dst2, ox, oy, oz, r);
+  }
+}
+
+// fineUpdate_mv (src/FineInterp.f90:10-281): fine points with cell_n /= 1
+__global__ void k_fine_mv(Dims da, Dims db, FaceArgs a, const int8_t* cell_n) {
+  const int nxs = a.tx.c - 2, nys = a.ty.c - 2, nzs = a.tz.c - 2;
+  if (nxs <= 0 || nys <= 0 || nzs <= 0) return;
+  const int n = nxs * nys * nzs;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int ei = 2 + t % nxs, ej = 2 + (t / nxs) % nys, ek = 2 + t / (nxs * nys);
+    const int vx1 = a.tx.at(2, ei), vx2 = a.tx.at(3, ei);
+    const int vy1 = a.ty.at(2, ej), vy2 = a.ty.at(3, ej);
+    const int vz1 = a.tz.at(2, ek), vz2 = a.tz.at(3, ek);
+    const int lx = a.tx.at(1, ei), ly = a.ty.at(1, ej), lz = a.tz.at(1, ek);
+    const int xm = a.comp == 1 ? lx - 2 : lx - 1, xq = a.comp == 1 ? lx : lx + 1;
+    const int ym = a.comp == 2 ? ly - 2 : ly - 1, yq = a.comp == 2 ? ly : ly + 1;
+    const int zm = a.comp == 3 ? lz - 2 : lz - 1, zq = a.comp == 3 ? lz : lz + 1;
+    for (int q = vz1; q <= vz2; ++q)
+      for (int l = vy1; l <= vy2; ++l)
+        for (int s = vx1; s <= vx2; ++s) {
+          if (cell_n[db.idx(s, l, q)] == 1) continue;
+          const double valx = a.gb.x[s - 1], valy = a.gb.y[l - 1], valz = a.gb.z[q - 1];
+          const double x1 = a.ga.x[lx - 2], x2 = a.ga.x[lx];
+          const double y1 = a.ga.y[ly - 2], y2 = a.ga.y[ly];
+          const double z1 = a.ga.z[lz - 2], z2 = a.ga.z[lz];
+          const double deno = (x2 - x1) * (y2 - y1);
+          const double xtx = (x2 - valx), xxo = (valx - x1);
+          const double yty = (y2 - valy), yyo = (valy - y1);
+          double f1 = fget(da, a.src, xm, ym, zm), f2 = fget(da, a.src, xq, ym, zm),
+                 f3 = fget(da, a.src, xq, yq, zm), f4 = fget(da, a.src, xm, yq, zm);
+          double num = (f1 * xtx + f2 * xxo) * yty + (f4 * xtx + f3 * xxo) * yyo;
+          const double a1 = (num / deno);
+          f1 = fget(da, a.src, xm, ym, zq);
+          f2 = fget(da, a.src, xq, ym, zq);
+          f3 = fget(da, a.src, xq, yq, zq);
+          f4 = fget(da, a.src, xm, yq, zq);
+          num = (f1 * xtx + f2 * xxo) * yty + (f4 * xtx + f3 * xxo) * yyo;
+          const double a2 = (num / deno);
+          const double r = a1 + ((valz - z1) * ((a2 - a1) / (z2 - z1)));
+          fset(db, a.dst, s - (a.comp == 1), l - (a.comp == 2), q - (a.comp == 3), r);
+        }
+  }
+}
+
+Grids grids_of(const DevBlock& B, int comp) {
+  switch (comp) {
+    case 1: return {B.xu, B.yu, B.zu};
+    case 2: return {B.xv, B.yv, B.zv};
+    case 3: return {B.xw, B.yw, B.zw};
+    default: return {B.xp, B.yp, B.zp};
+  }
+}
+
+// which: 0 = ut/vt/wt (p unused), 1 = pc (+ pco), 2 = u/v/w/p
+Field field_of(const DevBlock& B, int comp, int which) {
+  if (which == 1) return {nullptr, B.pc[0], B.pc[1]};
+  if (which == 0) {
+    double* f = comp == 1 ? B.ut : comp == 2 ? B.vt : B.wt;
+    return {f, nullptr, nullptr};
+  }
+  double* f = comp == 0 ? B.p : comp == 1 ? B.u : comp == 2 ? B.v : B.w;
+  return {f, nullptr, nullptr};
+}
+
+FaceArgs make_args(HostInterface* it, HostBlock* a, HostBlock* b, int comp) {
+  FaceArgs f{};
+  const int base = 3 * comp;  // px,py,pz | ux,uy,uz | vx.. | wx..
+  f.tx = {it->dtab + it->off[base + 0], (int)it->counter[base + 0]};
+  f.ty = {it->dtab + it->off[base + 1], (int)it->counter[base + 1]};
+  f.tz = {it->dtab + it->off[base + 2], (int)it->counter[base + 2]};
+  f.comp = comp;
+  f.ga = grids_of(a->d, comp);
+  f.gb = grids_of(b->d, comp);
+  return f;
+}
+
+}  // namespace
+
+int launch_face_fill(HostInterface* it, int comp, int which) {
+  HostBlock* a = get_block(it->a);
+  HostBlock* b = get_block(it->b);
+  if (!a || !b) return BCFD_E_HANDLE;
+  FaceArgs f = make_args(it, a, b, comp);
+  f.src = field_of(a->d, comp, which);
+  f.dst = field_of(b->d, comp, which);
+  f.dst2 = Field{nullptr, nullptr, nullptr};  // pco aliases pc in the packed layout
+  for (int axis = 1; axis <= 3; ++axis) {
+    f.axis = axis;
+    const int n = f.tx.c * f.ty.c * f.tz.c;
+    k_face<<<grid_for(n, 128), 128, 0, stream()>>>(a->d.d, b->d.d, f);
+    BCFD_LAUNCHED();
+  }
+  return 0;
+}
+
+int launch_restrict(HostInterface* it, int comp, int which) {
+  HostBlock* a = get_block(it->a);
+  HostBlock* b = get_block(it->b);
+  if (!a || !b) return BCFD_E_HANDLE;
+  FaceArgs f = make_args(it, a, b, comp);
+  f.src = field_of(b->d, comp, which);
+  f.dst = field_of(a->d, comp, which);
+  f.dst2 = Field{nullptr, nullptr, nullptr};
+  const int n = f.tx.c * f.ty.c * f.tz.c;
+  k_restrict<<<grid_for(n, 128), 128, 0, stream()>>>(a->d.d, b->d.d, f, 3);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+int launch_fine_update_mv(HostInterface* it) {
+  HostBlock* a = get_block(it->a);
+  HostBlock* b = get_block(it->b);
+  if (!a || !b) return BCFD_E_HANDLE;
+  for (int comp = 0; comp < 4; ++comp) {
+    FaceArgs f = make_args(it, a, b, comp);
+    f.src = field_of(a->d, comp, 2);
+    f.dst = field_of(b->d, comp, 2);
+    const int n = f.tx.c * f.ty.c * f.tz.c;
+    k_fine_mv<<<grid_for(n, 128), 128, 0, stream()>>>(a->d.d, b->d.d, f, b->d.cell_n);
+    BCFD_LAUNCHED();
+  }
+  return 0;
+}
+
+}  // namespace bcfd

@@ -1,0 +1,440 @@
+// Momentum predictor (nsMomentum2order, src/NavierStokes.f90:252-912) and the
+// boundary conditions of src/BoundaryConditions.f90.
+//
+// One thread per interior cell; non-fluid cells are skipped (the reference
+// loops over the fluid list, whose order does not matter without thin-surface
+// cells because the loop then only reads u,v,w,p and writes ut,vt,wt).  Cells
+// next to a thin-surface (TS) cell see the reference's in-place ghost
+// substitution; that serial-order effect is reproduced exactly by the overlay
+// in TsView (see k_ts_overlay below).  FP64, compiled without FMA contraction,
+// expressions in the reference's evaluation order.
+#include "bcfd_host.h"
+
+namespace bcfd {
+
+namespace {
+
+// Thin-surface overlay: the values the reference's serial loop would read at
+// the faces of TS cells.  For a fluid cell at linear position `self` the value
+// of a TS-face position is (1) the ghost value written by this cell's own
+// nn-loop if it wrote that position, else (2) the restore value written by
+// the latest earlier fluid cell that restored it, else (3) the original field.
+struct TsView {
+  bool active;
+};
+
+struct MomArgs {
+  double dt, re;
+};
+
+__device__ __forceinline__ bool adj_ok(const int8_t* c, const Dims& d, bool big, int i, int j, int k,
+                                       int s) {
+  // check_adjacent_cell (src/NavierStokes.f90:1002-1022): false if any of the
+  // 6 cells at distance s has tag 2
+  auto at = [&](int a, int b, int e) { return big ? c[d.idx3(a, b, e)] : c[d.idx(a, b, e)]; };
+  if (at(i - s, j, k) == 2) return false;
+  if (at(i + s, j, k) == 2) return false;
+  if (at(i, j - s, k) == 2) return false;
+  if (at(i, j + s, k) == 2) return false;
+  if (at(i, j, k - s) == 2) return false;
+  if (at(i, j, k + s) == 2) return false;
+  return true;
+}
+
+__global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
+  const Dims& d = B.d;
+  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
+  const double alpha = 1.0;
+  const double deltat = a.dt, re = a.re;
+  const int nx_var = d.nx, ny_var = d.ny, nz_var = d.nz;
+  const int64_t SX = 1, SY = d.NX, SZ = (int64_t)d.NX * d.NY;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(t % d.nx);
+    const int64_t r = t / d.nx;
+    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
+    const int64_t c = d.idx(i, j, k);
+    if (B.cell[c] != 0) continue;
+    const double* __restrict__ U = B.u;
+    const double* __restrict__ V = B.v;
+    const double* __restrict__ W = B.w;
+    const double* __restrict__ P = B.p;
+#define u(a, b, e) __ldg(U + c + (a) * SX + (b) * SY + (e) * SZ)
+#define v(a, b, e) __ldg(V + c + (a) * SX + (b) * SY + (e) * SZ)
+#define w(a, b, e) __ldg(W + c + (a) * SX + (b) * SY + (e) * SZ)
+#define p(a, b, e) __ldg(P + c + (a) * SX + (b) * SY + (e) * SZ)
+#define DX(q) B.dxa[(q) - 1]
+#define DY(q) B.dya[(q) - 1]
+#define DZ(q) B.dza[(q) - 1]
+#define CA(tab, row, q) B.ca[tab][((row) - 1) + 6 * ((q) - 1)]
+#define CK(tab, row, q) B.ck[tab][((row) - 1) + 6 * ((q) - 1)]
+    // offsets are relative to (i,j,k): u(-1,0,0) is u(i-1,j,k)
+    const double dxr = DX(i + 1), dx = DX(i), dxl = DX(i - 1);
+    const double dye = DY(j + 1), dy = DY(j), dyw = DY(j - 1);
+    const double dzt = DZ(k + 1), dz = DZ(k), dzb = DZ(k - 1);
+
+    const double u1a = u(-1, 0, 0) + u(0, 0, 0);
+    const double u22 = u(-1, 0, 0) - u(0, 0, 0);
+    const double u3 = u(0, 0, 0) + u(1, 0, 0);
+    const double u4 = u(0, 0, 0) - u(1, 0, 0);
+    const double u5 = u(0, -1, 0) + u(0, 0, 0);
+    const double u6 = u(0, -1, 0) - u(0, 0, 0);
+    const double u7 = u(0, 0, 0) + u(0, 1, 0);
+    const double u8 = u(0, 0, 0) - u(0, 1, 0);
+    const double u9 = u(0, 0, -1) + u(0, 0, 0);
+    const double u10 = u(0, 0, -1) - u(0, 0, 0);
+    const double u11 = u(0, 0, 0) + u(0, 0, 1);
+    const double u12 = u(0, 0, 0) - u(0, 0, 1);
+    const double u13 = u(-1, 0, 0) + u(-1, 1, 0);
+    const double u14 = u7;
+    const double u15 = u(-1, 0, 0) + u(-1, 0, 1);
+    const double u16 = u11;
+
+    const double v1a = v(0, -1, 0) + v(1, -1, 0);
+    const double v22 = v(0, 0, 0) + v(1, 0, 0);
+    const double v3 = v(-1, 0, 0) + v(0, 0, 0);
+    const double v4 = v(-1, 0, 0) - v(0, 0, 0);
+    const double v5 = v(0, 0, 0) + v(1, 0, 0);
+    const double v6 = v(0, 0, 0) - v(1, 0, 0);
+    const double v7 = v(0, -1, 0) + v(0, 0, 0);
+    const double v8 = v(0, -1, 0) - v(0, 0, 0);
+    const double v9 = v(0, 0, 0) + v(0, 1, 0);
+    const double v10 = v(0, 0, 0) - v(0, 1, 0);
+    const double v11 = v(0, 0, -1) + v(0, 0, 0);
+    const double v12 = v(0, 0, -1) - v(0, 0, 0);
+    const double v13 = v(0, 0, 0) + v(0, 0, 1);
+    const double v14 = v(0, 0, 0) - v(0, 0, 1);
+    const double v15 = v(0, -1, 0) + v(0, -1, 1);
+    const double v16 = v13;
+
+    const double w1a = w(0, 0, -1) + w(1, 0, -1);
+    const double w22 = w(0, 0, 0) + w(1, 0, 0);
+    const double w3 = w(0, 0, -1) + w(0, 1, -1);
+    const double w4 = w(0, 0, 0) + w(0, 1, 0);
+    const double w5 = w(-1, 0, 0) + w(0, 0, 0);
+    const double w6 = w(-1, 0, 0) - w(0, 0, 0);
+    const double w7 = w(0, 0, 0) + w(1, 0, 0);
+    const double w8 = w(0, 0, 0) - w(1, 0, 0);
+    const double w9 = w(0, -1, 0) + w(0, 0, 0);
+    const double w10 = w(0, -1, 0) - w(0, 0, 0);
+    const double w11 = w(0, 0, 0) + w(0, 1, 0);
+    const double w12 = w(0, 0, 0) - w(0, 1, 0);
+    const double w13 = w(0, 0, -1) + w(0, 0, 0);
+    const double w14 = w(0, 0, -1) - w(0, 0, 0);
+    const double w15 = w(0, 0, 0) + w(0, 0, 1);
+    const double w16 = w(0, 0, 0) - w(0, 0, 1);
+
+    const double dpdx = (p(0, 0, 0) - p(1, 0, 0)) / (0.5 * (dxr + dx));
+    const double dpdy = (p(0, 0, 0) - p(0, 1, 0)) / (0.5 * (dye + dy));
+    const double dpdz = (p(0, 0, 0) - p(0, 0, 1)) / (0.5 * (dzt + dz));
+
+    const double dx2xr = dx + dxr, dx2xl = dx + dxl, dy2ye = dy + dye, dy2yw = dy + dyw,
+                 dz2zt = dz + dzt, dz2zb = dz + dzb;
+
+    // thin-surface neighbours (cell2 == 2 next to this cell) need the ghost
+    // substitution of src/NavierStokes.f90:310-490, handled by k_momentum_ts
+    if (!adj_ok(B.cell2, d, true, i, j, k, 1)) {
+      set_err(B.err, BCFD_E_STATE);
+      continue;
+    }
+    // superset of the three components' third-order index ranges; inside it
+    // the distance-2 neighbours exist
+    const bool inner = i > 2 && j > 2 && k > 2 && i < nx_var + 1 && j < ny_var + 1 && k < nz_var + 1;
+    const bool smooth = inner && adj_ok(B.cell, d, false, i, j, k, 1) && adj_ok(B.cell2, d, true, i, j, k, 2);
+    const bool near_ib = !smooth, near_ts2 = false;
+
+    // ---------------- U momentum ----------------
+    {
+      const double vu_e = v(1, 0, 0) + (dxr / (dx2xr)) * (v(0, 0, 0) - v(1, 0, 0));
+      const double vu_w = v(1, -1, 0) + (dxr / (dx2xr)) * (v(0, -1, 0) - v(1, -1, 0));
+      const double v_in_um = 0.5 * (vu_e + vu_w);
+      const double wu_n = w(1, 0, 0) + (dxr / (dx2xr)) * (w(0, 0, 0) - w(1, 0, 0));
+      const double wu_s = w(1, 0, -1) + (dxr / (dx2xr)) * (w(0, 0, -1) - w(1, 0, -1));
+      const double w_in_um = 0.5 * (wu_n + wu_s);
+      double duudx, dvudy, dwudz;
+      const bool third = (i > 2 && i < nx_var && j > 2 && j < ny_var + 1 && k > 2 && k < nz_var + 1) &&
+                         !near_ib && !near_ts2;
+      if (third) {
+        const double ddy = 0.5 * (DY(j) + DY(j - 1));
+        const double ddye = 0.5 * (DY(j) + DY(j + 1));
+        const double ddz = 0.5 * (DZ(k) + DZ(k - 1));
+        const double ddzr = 0.5 * (DZ(k) + DZ(k + 1));
+        duudx = u(0, 0, 0) *
+                    (CA(T_UU, 1, i) * u(2, 0, 0) + CA(T_UU, 2, i) * u(1, 0, 0) +
+                     CA(T_UU, 3, i) * u(0, 0, 0) + CA(T_UU, 4, i) * u(-1, 0, 0) +
+                     CA(T_UU, 5, i) * u(-2, 0, 0)) /
+                    (CA(T_UU, 6, i) * DX(i + 1)) +
+                fabs(u(0, 0, 0)) *
+                    (CK(T_UU, 1, i) * u(2, 0, 0) + CK(T_UU, 2, i) * u(1, 0, 0) +
+                     CK(T_UU, 3, i) * u(0, 0, 0) + CK(T_UU, 4, i) * u(-1, 0, 0) +
+                     CK(T_UU, 5, i) * u(-2, 0, 0)) /
+                    (2.0 * CK(T_UU, 6, i) * DX(i));
+        dvudy = v_in_um *
+                    (CA(T_VU, 1, j) * u(0, 2, 0) + CA(T_VU, 2, j) * u(0, 1, 0) +
+                     CA(T_VU, 3, j) * u(0, 0, 0) + CA(T_VU, 4, j) * u(0, -1, 0) +
+                     CA(T_VU, 5, j) * u(0, -2, 0)) /
+                    (CA(T_VU, 6, j) * ddye) +
+                fabs(v_in_um) *
+                    (CK(T_VU, 1, j) * u(0, 2, 0) + CK(T_VU, 2, j) * u(0, 1, 0) +
+                     CK(T_VU, 3, j) * u(0, 0, 0) + CK(T_VU, 4, j) * u(0, -1, 0) +
+                     CK(T_VU, 5, j) * u(0, -2, 0)) /
+                    (2.0 * CK(T_VU, 6, j) * ddy);
+        dwudz = w_in_um *
+                    (CA(T_WU, 1, k) * u(0, 0, 2) + CA(T_WU, 2, k) * u(0, 0, 1) +
+                     CA(T_WU, 3, k) * u(0, 0, 0) + CA(T_WU, 4, k) * u(0, 0, -1) +
+                     CA(T_WU, 5, k) * u(0, 0, -2)) /
+                    (CA(T_WU, 6, k) * ddzr) +
+                fabs(w_in_um) *
+                    (CK(T_WU, 1, k) * u(0, 0, 2) + CK(T_WU, 2, k) * u(0, 0, 1) +
+                     CK(T_WU, 3, k) * u(0, 0, 0) + CK(T_WU, 4, k) * u(0, 0, -1) +
+                     CK(T_WU, 5, k) * u(0, 0, -2)) /
+                    (2.0 * CK(T_WU, 6, k) * ddz);
+      } else {
+        duudx = -0.25 * (u1a * u1a + alpha * fabs(u1a) * u22 - u3 * u3 - alpha * fabs(u3) * u4) / DX(i);
+        dvudy = -0.25 * (v1a * u5 + alpha * fabs(v1a) * u6 - v22 * u7 - alpha * fabs(v22) * u8) / DY(j);
+        dwudz = -0.25 * (w1a * u9 + alpha * fabs(w1a) * u10 - w22 * u11 - alpha * fabs(w22) * u12) / DZ(k);
+      }
+      const double d2udx2 = (2.0 / dx2xr) * ((-u4 / dxr) + (u22 / dx));
+      const double d2udy2 =
+          (2.0 / (0.5 * (dy2ye + dy2yw))) * ((-u8 / (0.5 * dy2ye)) + (u6 / (0.5 * dy2yw)));
+      const double d2udz2 =
+          (2.0 / (0.5 * (dz2zt + dz2zb))) * ((-u12 / (0.5 * dz2zt)) + (u10 / (0.5 * dz2zb)));
+      const double xtt2 = (d2udx2 + d2udy2 + d2udz2) / re;
+      const double residu = (-duudx - dvudy - dwudz + xtt2);
+      B.ut[c] = u(0, 0, 0) + deltat * (residu + dpdx);
+    }
+    // ---------------- V momentum ----------------
+    {
+      const double uv_e = u(0, 1, 0) + (dye / (dy2ye)) * (u(0, 0, 0) - u(0, 1, 0));
+      const double uv_w = u(-1, 1, 0) + (dye / (dy2ye)) * (u(-1, 0, 0) - u(-1, 1, 0));
+      const double u_in_vm = 0.5 * (uv_e + uv_w);
+      const double wv_n = w(0, 1, 0) + (dye / (dy2ye)) * (w(0, 0, 0) - w(0, 1, 0));
+      const double wv_s = w(0, 1, -1) + (dye / (dy2ye)) * (w(0, 0, -1) - w(0, 1, -1));
+      const double w_in_vm = 0.5 * (wv_n + wv_s);
+      double duvdx, dvvdy, dwvdz;
+      const bool third = (i > 2 && i < nx_var + 1 && j > 2 && j < ny_var && k > 2 && k < nz_var + 1) &&
+                         !near_ib && !near_ts2;
+      if (third) {
+        const double ddx = 0.5 * (DX(i) + DX(i - 1));
+        const double ddxr = 0.5 * (DX(i) + DX(i + 1));
+        const double ddz = 0.5 * (DZ(k) + DZ(k - 1));
+        const double ddzr = 0.5 * (DZ(k) + DZ(k + 1));
+        duvdx = u_in_vm *
+                    (CA(T_UW, 1, i) * v(2, 0, 0) + CA(T_UW, 2, i) * v(1, 0, 0) +
+                     CA(T_UW, 3, i) * v(0, 0, 0) + CA(T_UW, 4, i) * v(-1, 0, 0) +
+                     CA(T_UW, 5, i) * v(-2, 0, 0)) /
+                    (CA(T_UW, 6, i) * ddxr) +
+                fabs(u_in_vm) *
+                    (CK(T_UW, 1, i) * v(2, 0, 0) + CK(T_UW, 2, i) * v(1, 0, 0) +
+                     CK(T_UW, 3, i) * v(0, 0, 0) + CK(T_UW, 4, i) * v(-1, 0, 0) +
+                     CK(T_UW, 5, i) * v(-2, 0, 0)) /
+                    (2.0 * CK(T_UW, 6, i) * ddx);
+        dvvdy = v(0, 0, 0) *
+                    (CA(T_VV, 1, j) * v(0, 2, 0) + CA(T_VV, 2, j) * v(0, 1, 0) +
+                     CA(T_VV, 3, j) * v(0, 0, 0) + CA(T_VV, 4, j) * v(0, -1, 0) +
+                     CA(T_VV, 5, j) * v(0, -2, 0)) /
+                    (CA(T_VV, 6, j) * DY(j + 1)) +
+                fabs(v(0, 0, 0)) *
+                    (CK(T_VV, 1, j) * v(0, 2, 0) + CK(T_VV, 2, j) * v(0, 1, 0) +
+                     CK(T_VV, 3, j) * v(0, 0, 0) + CK(T_VV, 4, j) * v(0, -1, 0) +
+                     CK(T_VV, 5, j) * v(0, -2, 0)) /
+                    (2.0 * CK(T_VV, 6, j) * DY(j));
+        dwvdz = w_in_vm *
+                    (CA(T_WU, 1, k) * v(0, 0, 2) + CA(T_WU, 2, k) * v(0, 0, 1) +
+                     CA(T_WU, 3, k) * v(0, 0, 0) + CA(T_WU, 4, k) * v(0, 0, -1) +
+                     CA(T_WU, 5, k) * v(0, 0, -2)) /
+                    (CA(T_WU, 6, k) * ddzr) +
+                fabs(w_in_vm) *
+                    (CK(T_WU, 1, k) * v(0, 0, 2) + CK(T_WU, 2, k) * v(0, 0, 1) +
+                     CK(T_WU, 3, k) * v(0, 0, 0) + CK(T_WU, 4, k) * v(0, 0, -1) +
+                     CK(T_WU, 5, k) * v(0, 0, -2)) /
+                    (2.0 * CK(T_WU, 6, k) * ddz);
+      } else {
+        duvdx = -0.25 * (u13 * v3 + alpha * fabs(u13) * v4 - u14 * v5 - alpha * fabs(u14) * v6) / DX(i);
+        dvvdy = -0.25 * (v7 * v7 + alpha * fabs(v7) * v8 - v9 * v9 - alpha * fabs(v9) * v10) / DY(j);
+        dwvdz = -0.25 * (w3 * v11 + alpha * fabs(w3) * v12 - w4 * v13 - alpha * fabs(w4) * v14) / DZ(k);
+      }
+      const double d2vdx2 =
+          (2.0 / (0.5 * (dx2xr + dx2xl))) * ((-v6 / (0.5 * dx2xr)) + (v4 / (0.5 * dx2xl)));
+      const double d2vdy2 = (2.0 / dy2ye) * ((-v10 / dye) + (v8 / dy));
+      const double d2vdz2 =
+          (2.0 / (0.5 * (dz2zt + dz2zb))) * ((-v14 / (0.5 * dz2zt)) + (v12 / (0.5 * dz2zb)));
+      const double ytt2 = (d2vdx2 + d2vdy2 + d2vdz2) / re;
+      const double residv = (-duvdx - dvvdy - dwvdz + ytt2);
+      B.vt[c] = v(0, 0, 0) + deltat * (residv + dpdy);
+    }
+    // ---------------- W momentum ----------------
+    {
+      const double uw_e = u(0, 0, 1) + (dzt / (dz2zt)) * (u(0, 0, 0) - u(0, 0, 1));
+      const double uw_w = u(-1, 0, 1) + (dzt / (dz2zt)) * (u(-1, 0, 0) - u(-1, 0, 1));
+      const double u_in_wm = 0.5 * (uw_e + uw_w);
+      const double vw_n = v(0, 0, 1) + (dzt / (dz2zt)) * (v(0, 0, 0) - v(0, 0, 1));
+      const double vw_s = v(0, -1, 1) + (dzt / (dz2zt)) * (v(0, -1, 0) - v(0, -1, 1));
+      const double v_in_wm = 0.5 * (vw_n + vw_s);
+      double duwdx, dvwdy, dwwdz;
+      const bool third = (i > 2 && i < nx_var + 1 && j > 2 && j < ny_var + 1 && k > 2 && k < nz_var) &&
+                         !near_ib && !near_ts2;
+      if (third) {
+        const double ddx = 0.5 * (DX(i) + DX(i - 1));
+        const double ddxr = 0.5 * (DX(i) + DX(i + 1));
+        const double ddy = 0.5 * (DY(j) + DY(j - 1));
+        const double ddye = 0.5 * (DY(j) + DY(j + 1));
+        duwdx = u_in_wm *
+                    (CA(T_UW, 1, i) * w(2, 0, 0) + CA(T_UW, 2, i) * w(1, 0, 0) +
+                     CA(T_UW, 3, i) * w(0, 0, 0) + CA(T_UW, 4, i) * w(-1, 0, 0) +
+                     CA(T_UW, 5, i) * w(-2, 0, 0)) /
+                    (CA(T_UW, 6, i) * ddxr) +
+                fabs(u_in_wm) *
+                    (CK(T_UW, 1, i) * w(2, 0, 0) + CK(T_UW, 2, i) * w(1, 0, 0) +
+                     CK(T_UW, 3, i) * w(0, 0, 0) + CK(T_UW, 4, i) * w(-1, 0, 0) +
+                     CK(T_UW, 5, i) * w(-2, 0, 0)) /
+                    (2.0 * CK(T_UW, 6, i) * ddx);
+        dvwdy = v_in_wm *
+                    (CA(T_VW, 1, j) * w(0, 2, 0) + CA(T_VW, 2, j) * w(0, 1, 0) +
+                     CA(T_VW, 3, j) * w(0, 0, 0) + CA(T_VW, 4, j) * w(0, -1, 0) +
+                     CA(T_VW, 5, j) * w(0, -2, 0)) /
+                    (CA(T_VW, 6, j) * ddye) +
+                fabs(v_in_wm) *
+                    (CK(T_VW, 1, j) * w(0, 2, 0) + CK(T_VW, 2, j) * w(0, 1, 0) +
+                     CK(T_VW, 3, j) * w(0, 0, 0) + CK(T_VW, 4, j) * w(0, -1, 0) +
+                     CK(T_VW, 5, j) * w(0, -2, 0)) /
+                    (2.0 * CK(T_VW, 6, j) * ddy);
+        dwwdz = w(0, 0, 0) *
+                    (CA(T_WW, 1, k) * w(0, 0, 2) + CA(T_WW, 2, k) * w(0, 0, 1) +
+                     CA(T_WW, 3, k) * w(0, 0, 0) + CA(T_WW, 4, k) * w(0, 0, -1) +
+                     CA(T_WW, 5, k) * w(0, 0, -2)) /
+                    (CA(T_WW, 6, k) * DZ(k + 1)) +
+                fabs(w(0, 0, 0)) *
+                    (CK(T_WW, 1, k) * w(0, 0, 2) + CK(T_WW, 2, k) * w(0, 0, 1) +
+                     CK(T_WW, 3, k) * w(0, 0, 0) + CK(T_WW, 4, k) * w(0, 0, -1) +
+                     CK(T_WW, 5, k) * w(0, 0, -2)) /
+                    (2.0 * CK(T_WW, 6, k) * DZ(k));
+      } else {
+        duwdx = -0.5 * (u15 * w5 + alpha * fabs(u15) * w6 - u16 * w7 - alpha * fabs(u16) * w8) / DX(i);
+        dvwdy = -0.5 * (v15 * w9 + alpha * fabs(v15) * w10 - v16 * w11 - alpha * fabs(v16) * w12) / DY(j);
+        dwwdz = -0.5 * (w13 * w13 + alpha * fabs(w13) * w14 - w15 * w15 - alpha * fabs(w15) * w16) / DZ(k);
+      }
+      const double d2wdx2 =
+          (2.0 / (0.5 * (dx2xr + dx2xl))) * ((-w8 / (0.5 * dx2xr)) + (w6 / (0.5 * dx2xl)));
+      const double d2wdy2 =
+          (2.0 / (0.5 * (dy2ye + dy2yw))) * ((-w12 / (0.5 * dy2ye)) + (w10 / (0.5 * dy2yw)));
+      const double d2wdz2 = (2.0 / dz2zt) * ((-w16 / dzt) + (w14 / dz));
+      const double ztt2 = (d2wdx2 + d2wdy2 + d2wdz2) / re;
+      const double residw = (-duwdx - dvwdy - dwwdz + ztt2);
+      B.wt[c] = w(0, 0, 0) + deltat * (residw + dpdz);
+    }
+#undef u
+#undef v
+#undef w
+#undef p
+#undef DX
+#undef DY
+#undef DZ
+#undef CA
+#undef CK
+  }
+}
+
+// velocityBC loop 1 (x faces), src/BoundaryConditions.f90:16-40
+__global__ void k_vbc_x(DevBlock B, double deltat, double uc) {
+  const Dims& d = B.d;
+  const int n = d.ny * d.nz;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int j = 2 + t % d.ny, k = 2 + t / d.ny;
+    const int nx = d.nx;
+    const int64_t c1 = d.idx(1, j, k), cn = d.idx(nx, j, k), cn1 = d.idx(nx + 1, j, k),
+                  cn2 = d.idx(nx + 2, j, k);
+    B.ut[c1] = uc;
+    B.vt[c1] = -B.vt[cn1];
+    B.wt[c1] = -B.wt[cn1];
+    B.ut[cn1] = B.u[cn1] - (deltat / B.dxa[nx]) * uc * (B.u[cn1] - B.u[cn]);
+    B.vt[cn2] = -B.vt[cn1] + B.v[cn2] + B.v[cn1] -
+                (2.0 * deltat / B.dxa[nx + 1]) * uc * (B.v[cn2] - B.v[cn1]);
+    B.wt[cn2] = -B.wt[cn1] + B.w[cn2] + B.w[cn1] -
+                (2.0 * deltat / B.dxa[nx + 1]) * uc * (B.w[cn2] - B.w[cn1]);
+  }
+}
+
+// velocityBC loop 2 (y faces), src/BoundaryConditions.f90:42-58
+__global__ void k_vbc_y(DevBlock B) {
+  const Dims& d = B.d;
+  const int n = d.nx * d.nz;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int i = 2 + t % d.nx, k = 2 + t / d.nx;
+    const int ny = d.ny;
+    B.ut[d.idx(i, 1, k)] = B.ut[d.idx(i, 2, k)];
+    B.wt[d.idx(i, 1, k)] = B.wt[d.idx(i, 2, k)];
+    B.vt[d.idx(i, 2, k)] = 0.0;
+    B.ut[d.idx(i, ny + 2, k)] = B.ut[d.idx(i, ny + 1, k)];
+    B.wt[d.idx(i, ny + 2, k)] = B.wt[d.idx(i, ny + 1, k)];
+    B.vt[d.idx(i, ny + 1, k)] = 0.0;
+  }
+}
+
+// velocityBC loop 3 (z faces), src/BoundaryConditions.f90:60-73
+__global__ void k_vbc_z(DevBlock B) {
+  const Dims& d = B.d;
+  const int n = d.nx * d.ny;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int i = 2 + t % d.nx, j = 2 + t / d.nx;
+    const int nz = d.nz;
+    B.ut[d.idx(i, j, 1)] = B.ut[d.idx(i, j, 2)];
+    B.vt[d.idx(i, j, 1)] = B.vt[d.idx(i, j, 2)];
+    B.wt[d.idx(i, j, 1)] = 0.0;
+    B.ut[d.idx(i, j, nz + 2)] = B.ut[d.idx(i, j, nz + 1)];
+    B.vt[d.idx(i, j, nz + 2)] = B.vt[d.idx(i, j, nz + 1)];
+    B.wt[d.idx(i, j, nz + 1)] = 0.0;
+  }
+}
+
+// solidCellBC / solidCellBC_move (src/BoundaryConditions.f90:76-115)
+__global__ void k_solid_bc(DevBlock B, int move) {
+  const Dims& d = B.d;
+  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(t % d.nx);
+    const int64_t r = t / d.nx;
+    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
+    const int64_t c = d.idx(i, j, k);
+    if (B.cell[c] != 1) continue;
+    B.ut[c] = 0.0;
+    B.vt[c] = 0.0;
+    B.wt[c] = 0.0;
+    B.p[c] = 0.0;
+    if (move) {
+      B.u[c] = 0.0;
+      B.v[c] = 0.0;
+      B.w[c] = 0.0;
+    }
+  }
+}
+
+}  // namespace
+
+int launch_momentum(HostBlock* hb, double dt, double re) {
+  const int64_t n = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
+  k_momentum<<<grid_for(n, 128, 1u << 20), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+int launch_velocity_bc(HostBlock* hb, double dt, double uc) {
+  const Dims& d = hb->d.d;
+  k_vbc_x<<<grid_for((int64_t)d.ny * d.nz, 128), 128, 0, stream()>>>(hb->d, dt, uc);
+  BCFD_LAUNCHED();
+  k_vbc_y<<<grid_for((int64_t)d.nx * d.nz, 128), 128, 0, stream()>>>(hb->d);
+  BCFD_LAUNCHED();
+  k_vbc_z<<<grid_for((int64_t)d.nx * d.ny, 128), 128, 0, stream()>>>(hb->d);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+int launch_solid_bc(HostBlock* hb, bool move) {
+  const int64_t n = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
+  k_solid_bc<<<grid_for(n, 256), 256, 0, stream()>>>(hb->d, move ? 1 : 0);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+}  // namespace bcfd

@@ -1,0 +1,195 @@
+/*
+ * biocfd_gb300.h -- C ABI of the GB300-native Bio-CFD hot path.
+ *
+ * Each entry point replaces one Fortran module subroutine of the reference
+ * (BioFSILab/Bio-CFD) on its per-time-step path; the reference routine is
+ * cited beside the declaration as file:line.  A thin ISO_C_BINDING shim keeps
+ * the reference's module and subroutine names, so app/main.F90 relinks
+ * unchanged (the shim is bio-cfd_gb300/fortran/biocfd_gb300_shim.f90).
+ *
+ * Conventions
+ *   - Block data live on the GPU.  A block is registered once and addressed
+ *     by an opaque handle; the Fortran Block_t arrays are host mirrors that
+ *     are copied in with the upload calls and out with the download calls.
+ *   - Arrays passed in or out have the reference's layout: column-major,
+ *     1-based extents of src/AllocateArrays.f90 / src/ReadInput.f90, FP64
+ *     reals and int64 integers, so a Fortran caller passes c_loc(arr).
+ *   - Every function returns 0 (BCFD_OK) or a negative bcfd_status.  Calls
+ *     enqueue work on the library stream; calls that return data to the host
+ *     synchronise.  Calls on different handles may come from different host
+ *     threads (they are serialised inside the library).
+ */
+#ifndef BIOCFD_GB300_H
+#define BIOCFD_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int64_t bcfd_handle;
+
+enum bcfd_status {
+  BCFD_OK = 0,
+  BCFD_E_HANDLE = -1,      /* unknown block or interface handle               */
+  BCFD_E_NOMEM = -2,       /* device allocation failed                        */
+  BCFD_E_NONFINITE = -3,   /* NaN/Inf in a residual or reduction              */
+  BCFD_E_NOTFOUND = -4,    /* probe bracket not found (find_index_in_array)   */
+  BCFD_E_TIMEOUT = -5,     /* a bounded device-side wait gave up              */
+  BCFD_E_ARG = -6,         /* invalid argument                                */
+  BCFD_E_CUDA = -7,        /* CUDA runtime error                              */
+  BCFD_E_STATE = -8,       /* call out of order (e.g. lists before tagging)   */
+  BCFD_E_CAPACITY = -9     /* a list outgrew its device capacity              */
+};
+
+/* ---- library ---------------------------------------------------------- */
+int bcfd_init(int device);
+int bcfd_finalize(void);
+int bcfd_synchronize(void);
+/* the cudaStream_t all work is enqueued on (for event timing by a caller) */
+int bcfd_get_stream(void** stream);
+const char* bcfd_status_string(int status);
+/* number of kernels this library has launched since bcfd_init */
+int64_t bcfd_kernel_launches(void);
+
+/* ---- block registration and host mirrors (src/Blocks.f90:13-81) --------- */
+/* Allocates the per-block device arrays of src/AllocateArrays.f90:15-57 and
+ * sets the grid from x1(1:nx+3), y1, z1 and deltax(1:nx+2), deltay, deltaz
+ * (src/ReadInput.f90:250-351); xu..zp are derived as the reference does. */
+int bcfd_block_create(int64_t nx, int64_t ny, int64_t nz, const double* x1, const double* y1,
+                      const double* z1, const double* deltax, const double* deltay,
+                      const double* deltaz, bcfd_handle* out);
+int bcfd_block_destroy(bcfd_handle h);
+/* after a block move (src/Search.F90:1208-1264): new x1/y1/z1, deltas kept */
+int bcfd_block_set_grid(bcfd_handle h, const double* x1, const double* y1, const double* z1);
+/* Block_t scalars: dx, dy, dz (src/ReadInput.f90:233-239) and omega (:353-360) */
+int bcfd_block_set_scalars(bcfd_handle h, double dx, double dy, double dz, double omega);
+/* body_search.dat box of tagging_th_core (src/ReadInput.f90:103-111) */
+int bcfd_block_set_search_box(bcfd_handle h, int64_t i0, int64_t i1, int64_t j0, int64_t j1,
+                              int64_t k0, int64_t k1);
+/* surface mesh (src/ReadInput.f90:365-426): element node ids (1-based),
+ * physical tags, and the shifted node coordinates xnode1/ynode1/znode1 */
+int bcfd_block_set_surface(bcfd_handle h, int64_t n_elems, int64_t n_nodes, const int64_t* elp1,
+                           const int64_t* elp2, const int64_t* elp3, const int64_t* surf_id,
+                           const double* xnode1, const double* ynode1, const double* znode1);
+/* new node positions after the body kinematics (src/Search.F90:126-208) */
+int bcfd_block_set_nodes(bcfd_handle h, const double* xnode1, const double* ynode1,
+                         const double* znode1);
+/* rigid-body kinematics read by the forcing routines: kin[11] =
+ * {xdot, ydot, yddot, thetaDot1, thetaDDot1, thetaDot2, thetaDDot2, alphaDot,
+ *  piv_x, piv_y, piv_z} */
+int bcfd_block_set_kinematics(bcfd_handle h, const double* kin);
+/* Block_t move_check / blk_mv_tag */
+int bcfd_block_set_flags(bcfd_handle h, int64_t move_check, int64_t blk_mv_tag);
+/* fields (nx+2,ny+2,nz+2); any pointer may be NULL */
+int bcfd_block_upload_fields(bcfd_handle h, const double* u, const double* v, const double* w,
+                             const double* p, const double* ut, const double* vt, const double* wt);
+int bcfd_block_download_fields(bcfd_handle h, double* u, double* v, double* w, double* p,
+                               double* ut, double* vt, double* wt);
+/* tags: cell, cell_n (nx+2)^3 and cell2, nodeIdTag, cell_pr (nx+3)^3, int64 */
+int bcfd_block_upload_tags(bcfd_handle h, const int64_t* cell, const int64_t* cell2,
+                           const int64_t* node_id_tag, const int64_t* cell_n,
+                           const int64_t* cell_pr);
+int bcfd_block_download_tags(bcfd_handle h, int64_t* cell, int64_t* cell2, int64_t* node_id_tag,
+                             int64_t* cell_n, int64_t* cell_pr);
+/* counts[6] = ibCellCount, solidCellCount, fluidCellCount, redCellCount,
+ * blackCellCount, TSCellCount */
+int bcfd_block_get_counts(bcfd_handle h, int64_t* counts);
+/* the per-block Poisson statistics nIterPcor, derr2, derrStdSt */
+int bcfd_block_get_sor_stats(bcfd_handle h, int64_t* n_iter, double* derr2, double* derr_std_st);
+int bcfd_block_set_sor_iter(bcfd_handle h, int64_t n_iter);
+/* named host read-back of any other device array, in the reference layout:
+ * "pc", "b", "xcent", ..., "pNormDis", "nelp", "p_ghost", "fluidIndexPtr",
+ * "interceptedIndexPtr", "solidIndexPtr", "redCellIndexPtr", "TSIndexPtr",
+ * "index_ts", "Acx", "ca_uu", ...  (reals as double, integers as int64);
+ * n = capacity in elements, *written = elements written */
+int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64_t* written);
+
+/* ---- setup routines ------------------------------------------------------ */
+int bcfd_non_uni_coeff(bcfd_handle h);                    /* src/NavierStokes.f90:13-250 */
+int bcfd_coefficient_matrix(bcfd_handle h, int is_coarse); /* src/CoefficientMatrix.f90:10-71 */
+
+/* ---- momentum predictor and boundary conditions --------------------------- */
+int bcfd_ns_momentum_2order(bcfd_handle h, double deltat, double re); /* src/NavierStokes.f90:252-912 */
+int bcfd_velocity_bc(bcfd_handle h, double deltat, double uc);        /* src/BoundaryConditions.f90:11-74 */
+int bcfd_solid_cell_bc(bcfd_handle h);                                /* src/BoundaryConditions.f90:76-92 */
+int bcfd_solid_cell_bc_move(bcfd_handle h);                           /* src/BoundaryConditions.f90:94-115 */
+
+/* ---- immersed-boundary forcing ------------------------------------------ */
+int bcfd_velocity_forcing1(bcfd_handle h);       /* src/Forcing.f90:92-360   */
+int bcfd_pressure_forcing1(bcfd_handle h);       /* src/Forcing.f90:14-90    */
+int bcfd_velocity_forcing_field(bcfd_handle h);  /* src/Forcing.f90:813-1075 */
+int bcfd_pressure_forcing_field(bcfd_handle h);  /* src/Forcing.f90:737-811  */
+int bcfd_velocity_forcing_ghost(bcfd_handle h);  /* src/Forcing.f90:450-734  */
+int bcfd_pressure_forcing_ghost(bcfd_handle h);  /* src/Forcing.f90:362-448  */
+
+/* ---- Search / tagging ---------------------------------------------------- */
+int bcfd_compute_surface_norm(bcfd_handle h, int64_t inor); /* src/Search.F90:210-258  */
+int bcfd_tagging_th(bcfd_handle h);                         /* src/Search.F90:260-413  */
+int bcfd_selective_retagging_th(bcfd_handle h);             /* src/Search.F90:520-651  */
+int bcfd_cellcount_solid(bcfd_handle h);                    /* src/Search.F90:653-741  */
+int bcfd_compute_norm_distance(bcfd_handle h);              /* src/Search.F90:743-861  */
+int bcfd_find_ts_cells(bcfd_handle h);                      /* src/Search.F90:434-518  */
+int bcfd_cellcount_solid_coarse(bcfd_handle h);             /* src/Search.F90:1463-1532 */
+int bcfd_fine_block_cell(void);                             /* src/Search.F90:863-914  */
+
+/* ---- pressure correction ------------------------------------------------- */
+int bcfd_compute_div(bcfd_handle h);                        /* src/PcorVcor.F90:222-243 */
+int bcfd_correct_pressure(bcfd_handle h);                   /* src/PcorVcor.F90:245-259 */
+int bcfd_correct_velocity(bcfd_handle h, double deltat);    /* src/PcorVcor.F90:261-286 */
+int bcfd_redblack_sor_linear(bcfd_handle h, int64_t pc_ita_max, double deltat,
+                             double epsi);                  /* src/PcorVcor.F90:288-377 */
+int bcfd_update_velocity_newv(bcfd_handle h);               /* src/PcorVcor.F90:379-397 */
+/* poissonSolver over the registered blocks start..finish by step (1-based
+ * registration order; block 1 is the coarse block): src/PcorVcor.F90:22-220.
+ * totalTime accumulates totime per block as in the reference. */
+int bcfd_poisson_solver(int64_t pc_ita_max, double epsi, int64_t ita, double deltat,
+                        double totime, double uc, double* total_time, int start, int finish,
+                        int step);
+
+/* ---- inter-block coupling ------------------------------------------------ */
+/* interface between coarse block a and fine block b at mesh ratio b_msh/a_msh
+ * over box[6] = {xs, xe, ys, ye, zs, ze}; builds the tables of
+ * src/InterfaceDetail.f90:10-165 (set_interface_detail :168-241) */
+int bcfd_interface_create(bcfd_handle a, bcfd_handle b, int64_t a_msh, int64_t b_msh,
+                          const double* box, bcfd_handle* out);
+/* table read-back: name in {px,py,pz,ux,...,wz}; out (3, n) int64 */
+int bcfd_interface_table(bcfd_handle it, const char* name, int64_t* out, int64_t n,
+                         int64_t* counter);
+int bcfd_fine_update_pc_bd(void);              /* src/FineInterp_bound.f90:17-107   */
+int bcfd_fine_update_newv_bd(void);            /* src/FineInterp_bound.f90:109-309  */
+int bcfd_fine_update_bd_mv(bcfd_handle it);    /* src/FineInterp_bound.f90:311-544  */
+int bcfd_coarse_update(void);                  /* src/CoarseInterp.f90:16-204       */
+int bcfd_coarse_update_newv(void);             /* src/CoarseInterp.f90:206-346      */
+int bcfd_coarse_update_pc(void);               /* src/CoarseInterp.f90:347-437      */
+int bcfd_fine_update_mv(bcfd_handle it);       /* src/FineInterp.f90:10-281         */
+
+/* ---- drag / lift (src/StressCalc.f90:14-208, FP64, deterministic order) --- */
+/* out[4] = viscous drag, pressure drag, viscous lift, pressure lift coefficients */
+int bcfd_stress_calculation(bcfd_handle h, double mu_f, double rho_f, double* out);
+
+/* ---- whole time step (the phase order of app/main.F90:129-265) ----------- */
+typedef struct bcfd_step_config {
+  double deltat;       /* time step                                            */
+  double re;           /* the reference's `re` argument, 1/nu                  */
+  double uc;           /* inflow velocity                                      */
+  double epsi;         /* SOR stop threshold on max |pc - pco|                 */
+  int64_t pc_ita_max;  /* SOR iteration cap                                    */
+  int precision;       /* 0: FP64 reference arithmetic, 1: FP32 SOR + FP64
+                          defect correction                                    */
+  double div_tol;      /* precision 1: target max|div u| after correction      */
+  int use_graph;       /* capture the step in a CUDA graph and replay it       */
+} bcfd_step_config;
+
+/* Runs n_steps time steps over every registered block and interface with the
+ * per-block roles set by bcfd_block_set_role (domain BCs / immersed body). */
+int bcfd_block_set_role(bcfd_handle h, int is_coarse, int has_body);
+int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps);
+/* max over fluid cells of |div u| of the current u,v,w (FP64) */
+int bcfd_max_divergence(bcfd_handle h, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* BIOCFD_GB300_H */

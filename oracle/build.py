@@ -1,0 +1,54 @@
+"""Build recipe for the CPU oracle (test infrastructure only).
+
+Compiles the serial FP64 restatement in this directory into
+``oracle/build/liborc.so`` with ``-ffp-contract=off`` so that every
+expression rounds exactly as written (no fused multiply-adds), which is the
+arithmetic of the reference's serial CPU build.
+
+The reference itself (Fortran 2008 + OpenACC) cannot be compiled in this
+environment -- no Fortran compiler exists on either machine -- so there is
+no ``oracle/_ref`` build.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+SOURCES = ["orc_navier.cpp", "orc_forcing.cpp", "orc_pcor.cpp", "orc_search.cpp",
+           "orc_interp.cpp", "orc_stress.cpp", "orc_api.cpp"]
+
+
+def lib_path(checked: bool = True) -> Path:
+    return HERE / "build" / ("liborc.so" if checked else "liborc_fast.so")
+
+
+def build(checked: bool = True, force: bool = False) -> Path:
+    """Compile the oracle; ``checked`` keeps the 1-based bounds checks."""
+    out = lib_path(checked)
+    srcs = [HERE / s for s in SOURCES] + [HERE / "orc_core.h"]
+    if not force and out.exists() and all(out.stat().st_mtime >= s.stat().st_mtime for s in srcs):
+        return out
+    out.parent.mkdir(parents=True, exist_ok=True)
+    objdir = out.parent / ("obj" if checked else "obj_fast")
+    objdir.mkdir(exist_ok=True)
+    flags = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
+    if not checked:
+        flags.append("-DORC_NOCHECK")
+    procs, objs = [], []
+    for s in SOURCES:
+        o = objdir / (Path(s).stem + ".o")
+        objs.append(o)
+        procs.append(subprocess.Popen(["g++", *flags, "-c", str(HERE / s), "-o", str(o)]))
+    if any(p.wait() != 0 for p in procs):
+        raise RuntimeError("oracle compile failed")
+    tmp = out.with_suffix(".so.tmp%d" % os.getpid())
+    subprocess.check_call(["g++", "-shared", "-o", str(tmp), *map(str, objs)])
+    os.replace(tmp, out)
+    return out
+
+
+if __name__ == "__main__":
+    print(build(checked="--fast" not in sys.argv, force="--force" in sys.argv))

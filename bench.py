@@ -1,0 +1,309 @@
+#!/usr/bin/env python
+"""Bench: time steps/s of the Bio-CFD hot path on one GB300.
+
+Workload (one "step" = one time step of app/main.F90:129-265 over all blocks):
+the two-block refinement case -- coarse 96x64x64 over 3x2x2 plus a nested
+fine 64^3 block at ratio 2 around a stationary sphere D = 0.5, Re = 300,
+uniform inflow, seeded N(0, 1e-3) noise, dt from CFL 0.3, SOR to 1e-6.
+
+Two GPU paths run on the same GPU:
+  * "fp64": the drop-in -- FP64 red-black SOR with the reference's stop test
+    (max |pc - pco| < 1e-6 every 5th iteration), bit-identical to the
+    reference arithmetic;
+  * "mixed" (the flagship, reported as `value`): FP32 red-black SOR with an
+    FP64 defect-correction loop, stopped when the FP64 Poisson residual in
+    divergence units, dt * max|b/dt - A pc|, is at or below the residual the
+    fp64 path reaches (so both end at equal divergence residual).
+`e2e` repeats the flagship through the C ABI with host buffers: every step
+uploads u,v,w,p of both blocks from pinned host memory and downloads them.
+The CPU baseline is the serial FP64 oracle (the reference itself is Fortran
+and no Fortran compiler exists on either machine).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "bio-cfd_gb300"))
+sys.path.insert(0, str(ROOT))
+
+METRIC = "time steps/s at 1e-6 div residual: FP32+FP64-refine vs plain FP64, same GPU"
+WORKLOAD = "two-block sphere: coarse 96x64x64 over 3x2x2 + fine 64^3 at ratio 2, D=0.5, Re=300"
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles():
+    """dram read+write bytes per launch of the dominant kernel, from the committed ncu summary."""
+    f = ROOT / "profiles" / "sor_mixed_two_block.md"
+    if not f.exists():
+        return None
+    for line in f.read_text().splitlines():
+        if line.strip().startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class Clocks:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 2 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 2 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            for q, n in enumerate(names):
+                if len(r) > 5 + q and r[5 + q].lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def oracle_steps(case, n_steps: int):
+    """Serial FP64 oracle (CPU): steps/s over n_steps steps after set-up."""
+    from oracle.bridge import Oracle
+    o = Oracle(checked=False)
+    o.setup(case)
+    t0 = time.perf_counter()
+    for _ in range(n_steps):
+        o.step()
+    dt = time.perf_counter() - t0
+    return n_steps / dt, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from biocfd import synth
+    case = synth.sphere_two_block(n_steps=args.steps)
+    # bounded sample: warm-up and timed steps of the serial oracle, capped so
+    # the whole run stays within a few minutes
+    k = max(1, min(args.steps, 6))
+    sps, secs = oracle_steps(case, k)
+    line = {"metric": METRIC, "value": sps, "unit": "steps/s", "n_gpus": 0, "steps": k,
+            "warmup": 0, "ms_per_step": 1000.0 / sps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, numpy default_rng 20261203)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "precision": "fp64 serial oracle"},
+            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
+                             "sample": f"{k} time steps of the workload on the serial FP64 oracle "
+                                       f"(the Fortran reference is unbuildable: no Fortran compiler), {secs:.1f} s"},
+            "e2e": {"value": sps, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def time_path(solver, torch, flush, stream, steps: int, warmup: int, precision: int, div_tol: float,
+              clocks: "Clocks | None" = None):
+    """Per-step CUDA-event timing on the library stream, L2 flushed between steps."""
+    for _ in range(warmup):
+        solver.run(1, precision=precision, div_tol=div_tol)
+    times, divs, res, iters = [], [], [], []
+    solver.profile_begin()
+    ctx = clocks if clocks is not None else _Null()
+    with ctx:
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.add_(1.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            solver.run(1, precision=precision, div_tol=div_tol)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            d = [solver.divergence(g) for g in solver.handles]
+            divs.append(max(x[0] for x in d))
+            res.append(max(x[1] for x in d))
+            iters.append([solver.sor_stats(g)[0] for g in solver.handles])
+    prof = solver.profile_end()
+    return times, divs, res, iters, prof
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+    from biocfd import synth
+    from biocfd.solver import Solver
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    case = synth.sphere_two_block(n_steps=args.steps + args.warmup)
+    s = Solver(case, device=local)
+    s.setup()
+    stream = torch.cuda.ExternalStream(s.stream_ptr())
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
+
+    # plain FP64 drop-in path
+    t64, div64, res64, it64, prof64 = time_path(s, torch, flush, stream, args.steps, args.warmup, 0, 0.0)
+    tol = max(res64)  # equal final residual: the mixed path must reach what fp64 reaches
+    # flagship: FP32 SOR + FP64 defect correction, fresh state
+    s.close()
+    s = Solver(case, device=local)
+    s.setup()
+    stream = torch.cuda.ExternalStream(s.stream_ptr())
+    clocks = Clocks(local)
+    tmx, divmx, resmx, itmx, profmx = time_path(s, torch, flush, stream, args.steps, args.warmup, 1, tol,
+                                                clocks)
+    # e2e through the C ABI with host buffers (pinned), flagship precision
+    host = []
+    for spec, g in zip(case.blocks, s.handles):
+        f = s.fields(g)
+        host.append({k: torch.from_numpy(np.ascontiguousarray(f[k].ravel(order="F"))).pin_memory()
+                     for k in ("u", "v", "w", "p")})
+    import ctypes as C
+    from biocfd._lib import P_d, check
+    nbytes = sum(h[k].numel() * 8 for h in host for k in ("u", "v", "w", "p"))
+    e2e_times = []
+    for step in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for h, g in zip(host, s.handles):
+            ptr = [C.cast(h[k].data_ptr(), P_d) for k in ("u", "v", "w", "p")]
+            check(s.L.bcfd_block_upload_fields(g, *ptr, None, None, None), "upload")
+        s.run(1, precision=1, div_tol=tol)
+        for h, g in zip(host, s.handles):
+            ptr = [C.cast(h[k].data_ptr(), P_d) for k in ("u", "v", "w", "p")]
+            check(s.L.bcfd_block_download_fields(g, *ptr, None, None, None), "download")
+        e2e_times.append(time.perf_counter() - t0)
+
+    ms64 = statistics.mean(t64)
+    msmx = statistics.mean(tmx)
+    e2e_s = statistics.mean(e2e_times)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([msmx, ms64, e2e_s], dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        msmx, ms64, e2e_s = (float(x) for x in t)
+    nfluid = sum(s.counts(g)["fluidCellCount"] for g in s.handles)
+    hbm, peak_kind = peaks()
+    achieved = profmx["sor_bytes"] / (profmx["sor_ms"] * 1e-3) / 1e9 if profmx["sor_ms"] > 0 else 0.0
+    ach64 = prof64["sor_bytes"] / (prof64["sor_ms"] * 1e-3) / 1e9 if prof64["sor_ms"] > 0 else 0.0
+    traffic = traffic_from_profiles()
+    line = {
+        "metric": METRIC,
+        "value": world * 1000.0 / msmx,
+        "unit": "steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": msmx,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 sweeps + f64 defect correction",
+        "data": "synthetic (seeded, numpy default_rng 20261203)",
+        "config": {"workload": WORKLOAD, "blocks": "96x64x64 + 64^3", "parallelism": f"replicas x{world}",
+                   "l2": "flushed between timed steps (256 MB write)", "timed": "per-step CUDA events"},
+        "fp64": {"steps_per_s": 1000.0 / ms64, "ms_per_step": ms64, "div_residual": max(res64),
+                 "max_div_after_correction": max(div64), "sor_iters_last_step": it64[-1],
+                 "solve_gbs": ach64},
+        "mixed": {"steps_per_s": 1000.0 / msmx, "ms_per_step": msmx, "div_residual": max(resmx),
+                  "div_tol": tol, "max_div_after_correction": max(divmx), "fp32_sweeps_last_step": itmx[-1]},
+        "speedup_vs_fp64": ms64 / msmx,
+        "cell_updates_per_s": world * nfluid * 1000.0 / msmx,
+        "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes},
+        "gpu_launches": profmx["kernel_launches"],
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                     "frac": achieved / hbm, "traffic": traffic, "kernel": "k_sor_dc (mixed Poisson solve)",
+                     "peak_source": peak_kind,
+                     "note": "algorithmic bytes: 17 B per cell per FP32 sweep pair + FP64 residual/update passes; "
+                             "the 64^3 and 96x64x64 blocks are L2-resident during a solve"},
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        sps, secs = oracle_steps(case, 1)
+        line["cpu_baseline"] = {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
+                                "sample": f"1 time step of the same workload on the serial FP64 oracle, {secs:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

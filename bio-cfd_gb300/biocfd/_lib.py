@@ -31,7 +31,17 @@ class StepConfig(C.Structure):
                 ("use_graph", c_int)]
 
 
+class ProfileReport(C.Structure):
+    """bcfd_profile_report of include/biocfd_gb300.h."""
+    _fields_ = [("sor_launches", c_i64), ("sor_ms", c_double), ("sor_bytes", c_double),
+                ("sor_sweeps", c_i64), ("kernel_launches", c_i64)]
+
+
 _SIGS = {
+    "bcfd_block_get_divergence": [c_i64, P_d],
+    "bcfd_block_set_mixed_params": [c_i64, c_i64, c_double],
+    "bcfd_profile_begin": [],
+    "bcfd_profile_end": [C.POINTER(ProfileReport)],
     "bcfd_init": [c_int], "bcfd_finalize": [], "bcfd_synchronize": [],
     "bcfd_get_stream": [C.POINTER(C.c_void_p)],
     "bcfd_block_create": [c_i64, c_i64, c_i64, P_d, P_d, P_d, P_d, P_d, P_d, P_i64],

@@ -213,6 +213,24 @@ class Solver:
         check(self.L.bcfd_max_divergence(g, C.byref(d)), "max_divergence")
         return d.value
 
+    def divergence(self, g: int):
+        """(max |div ut| after the last correction, dt * max |Poisson residual| of the last solve)."""
+        d = np.zeros(2)
+        check(self.L.bcfd_block_get_divergence(g, _pd(d)), "get_divergence")
+        return float(d[0]), float(d[1])
+
+    def set_mixed_params(self, inner: int = 0, omega: float = 0.0):
+        for g in self.handles:
+            check(self.L.bcfd_block_set_mixed_params(g, inner, omega), "set_mixed_params")
+
+    def profile_begin(self):
+        check(self.L.bcfd_profile_begin(), "profile_begin")
+
+    def profile_end(self) -> dict:
+        r = _lib.ProfileReport()
+        check(self.L.bcfd_profile_end(C.byref(r)), "profile_end")
+        return {k: getattr(r, k) for k, _ in r._fields_}
+
     def stream_ptr(self) -> int:
         p = C.c_void_p()
         check(self.L.bcfd_get_stream(C.byref(p)), "get_stream")

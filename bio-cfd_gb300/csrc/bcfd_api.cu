@@ -66,6 +66,19 @@ GridBar make_bar(int* err, unsigned nblocks) {
   return g;
 }
 
+int64_t* prof_log() { return lib().prof_on ? lib().prof_dev : nullptr; }
+
+void prof_mark(bool /*begin*/) {
+  Lib& L = lib();
+  if (!L.prof_on) return;
+  if (L.prof_used == L.prof_events.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    L.prof_events.push_back(e);
+  }
+  cudaEventRecord(L.prof_events[L.prof_used++], stream());
+}
+
 int take_block_error(HostBlock* hb) {
   int e = 0;
   BCFD_CUDA(cudaMemcpyAsync(&e, hb->d.err, sizeof(int), cudaMemcpyDeviceToHost, stream()));
@@ -418,6 +431,8 @@ int bcfd_finalize(void) {
   for (HostBlock* hb : L.blocks)
     if (hb) {
       for (void* p : hb->allocs) cudaFree(p);
+      free_search_scratch(hb);
+      free_dag_scratch(hb);
       delete hb;
     }
   for (HostInterface* it : L.ifs)
@@ -531,6 +546,8 @@ int bcfd_block_destroy(bcfd_handle h) {
   GETB(h);
   cudaStreamSynchronize(stream());
   for (void* p : hb->allocs) cudaFree(p);
+  free_search_scratch(hb);
+  free_dag_scratch(hb);
   delete hb;
   lib().blocks[(size_t)(h - 1)] = nullptr;
   return 0;
@@ -607,6 +624,13 @@ int bcfd_block_set_nodes(bcfd_handle h, const double* x, const double* y, const 
   BCFD_CUDA(cudaMemcpyAsync((void*)hb->d.ynode1, y, nn * sizeof(double), cudaMemcpyHostToDevice, stream()));
   BCFD_CUDA(cudaMemcpyAsync((void*)hb->d.znode1, z, nn * sizeof(double), cudaMemcpyHostToDevice, stream()));
   BCFD_CUDA(cudaStreamSynchronize(stream()));
+  const Dims& d = hb->d.d;
+  const double cx = 0.5 * (hb->x1[0] + hb->x1[d.nx + 2]), cy = 0.5 * (hb->y1[0] + hb->y1[d.ny + 2]),
+               cz = 0.5 * (hb->z1[0] + hb->z1[d.nz + 2]);
+  double r2 = 0.0;
+  for (int q = 0; q < nn; ++q)
+    r2 = std::max(r2, (x[q] - cx) * (x[q] - cx) + (y[q] - cy) * (y[q] - cy) + (z[q] - cz) * (z[q] - cz));
+  hb->node_rmax = std::sqrt(r2);
   return 0;
 }
 
@@ -852,9 +876,73 @@ int bcfd_max_divergence(bcfd_handle h, double* out) {
   LOCK();
   GETB(h);
   if (!out) return BCFD_E_ARG;
-  TRY(launch_max_div(hb));
+  TRY(launch_max_div(hb, false));
   BCFD_CUDA(cudaMemcpyAsync(out, &hb->d.stats->maxdiv, sizeof(double), cudaMemcpyDeviceToHost, stream()));
   BCFD_CUDA(cudaStreamSynchronize(stream()));
+  return 0;
+}
+
+int bcfd_block_get_divergence(bcfd_handle h, double* out) {
+  LOCK();
+  GETB(h);
+  if (!out) return BCFD_E_ARG;
+  BCFD_CUDA(cudaMemcpyAsync(out, &hb->d.stats->pad[0], 2 * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+  BCFD_CUDA(cudaStreamSynchronize(stream()));
+  return 0;
+}
+
+int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega) {
+  LOCK();
+  GETB(h);
+  if (inner_sweeps < 0 || omega < 0.0 || omega >= 2.0) return BCFD_E_ARG;
+  hb->dc_inner = (int)inner_sweeps;
+  hb->dc_omega = omega;
+  return 0;
+}
+
+int bcfd_profile_begin(void) {
+  LOCK();
+  Lib& L = lib();
+  if (!L.ready) return BCFD_E_STATE;
+  if (!L.prof_dev) BCFD_CUDA(cudaMalloc(&L.prof_dev, (1 + 4 * kProfLogCap) * sizeof(int64_t)));
+  BCFD_CUDA(cudaMemsetAsync(L.prof_dev, 0, sizeof(int64_t), stream()));
+  L.prof_used = 0;
+  L.prof_on = true;
+  L.prof_launch0 = L.launches;
+  return 0;
+}
+
+int bcfd_profile_end(bcfd_profile_report* out) {
+  LOCK();
+  Lib& L = lib();
+  if (!L.prof_on || !out) return BCFD_E_STATE;
+  L.prof_on = false;
+  BCFD_CUDA(cudaStreamSynchronize(stream()));
+  std::memset(out, 0, sizeof(*out));
+  for (size_t q = 0; q + 1 < L.prof_used; q += 2) {
+    float ms = 0.f;
+    BCFD_CUDA(cudaEventElapsedTime(&ms, L.prof_events[q], L.prof_events[q + 1]));
+    out->sor_ms += ms;
+    out->sor_launches++;
+  }
+  int64_t n = 0;
+  BCFD_CUDA(cudaMemcpy(&n, L.prof_dev, sizeof(int64_t), cudaMemcpyDeviceToHost));
+  n = std::min<int64_t>(n, (int64_t)kProfLogCap);
+  std::vector<int64_t> e(4 * (size_t)std::max<int64_t>(n, 1));
+  if (n) BCFD_CUDA(cudaMemcpy(e.data(), L.prof_dev + 1, 4 * n * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  for (int64_t q = 0; q < n; ++q) {
+    const double sw = (double)e[4 * q], rp = (double)e[4 * q + 1], fl = (double)e[4 * q + 2];
+    out->sor_sweeps += e[4 * q];
+    if (e[4 * q + 3] == 0) {
+      out->sor_bytes += sw * fl * 33.0;  // 4w + 1, w = 8
+    } else {
+      // FP32 sweeps 4w + 1 (w = 4); FP64 residual: pc own + neighbours + b/dt
+      // read, r written as FP32, mask (8+8+8+4+1); update x += e: pc r/w,
+      // e r/w, mask (8+8+4+4+1)
+      out->sor_bytes += sw * fl * 17.0 + rp * fl * 29.0 + (rp - 1.0) * fl * 25.0;
+    }
+  }
+  out->kernel_launches = L.launches - L.prof_launch0;
   return 0;
 }
 

@@ -34,7 +34,16 @@ struct HostBlock {
   // (0 = defaults chosen from the block size)
   int dc_inner = 0;
   double dc_omega = 0.0;
+  // largest distance of a surface node from the block centre (for the FP32
+  // prefilter bound of the nearest-element search)
+  double node_rmax = 0.0;
+  // scratch owned by the search and forcing translation units
+  void* search_scratch = nullptr;
+  void* dag_scratch = nullptr;
 };
+
+void free_search_scratch(HostBlock* hb);
+void free_dag_scratch(HostBlock* hb);
 
 struct HostInterface {
   bcfd_handle a = 0, b = 0;  // block handles (a coarse, b fine)
@@ -59,7 +68,12 @@ struct Lib {
   std::vector<HostBlock*> blocks;      // handle h -> blocks[h-1] (nullptr when destroyed)
   std::vector<HostInterface*> ifs;     // interface handle -> ifs[h-1]
   int64_t launches = 0;
-  // roles for bcfd_run_steps
+  // measurement window
+  bool prof_on = false;
+  int64_t* prof_dev = nullptr;            // device solve log
+  std::vector<cudaEvent_t> prof_events;   // begin/end pairs, in order
+  size_t prof_used = 0;
+  int64_t prof_launch0 = 0;
 };
 
 Lib& lib();
@@ -88,7 +102,11 @@ int launch_copy_n_to_t(HostBlock* hb);
 int launch_update_masks(HostBlock* hb);
 int launch_pack(HostBlock* hb, const double* natural_dev, double* packed[2]);
 int launch_unpack(HostBlock* hb, double* const packed[2], double* natural_dev);
-int launch_max_div(HostBlock* hb);
+int launch_max_div(HostBlock* hb, bool tfield);
+// measurement window: device log of solves (nullptr when inactive) and CUDA
+// events around each persistent solve launch
+int64_t* prof_log();
+void prof_mark(bool begin);
 int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol);
 // k_momentum.cu
 int launch_momentum(HostBlock* hb, double dt, double re);

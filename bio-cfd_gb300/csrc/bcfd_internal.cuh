@@ -107,6 +107,10 @@ struct BlockStats {
 };
 
 enum CountSlot { C_IB = 0, C_SOLID, C_FLUID, C_RED, C_BLACK, C_TS, N_COUNT };
+
+// entries of the solve log of a measurement window ({sweeps, residual
+// passes, fluid cells, precision} each, after one counter word)
+constexpr unsigned long long kProfLogCap = 4096;
 enum GhostSlot { G_P = 0, G_PT, G_U2, G_U2T, G_V2, G_V2T, G_W2, G_W2T, G_U1, G_U1T, G_V1, G_V1T, G_W1, G_W1T };
 enum NelSlot { N_P = 0, N_U1, N_U2, N_V1, N_V2, N_W1, N_W2 };
 

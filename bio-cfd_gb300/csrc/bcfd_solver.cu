@@ -66,6 +66,40 @@ int upload_iface(HostInterface* it) {
 
 int sync_err(HostBlock* hb) { return take_block_error(hb); }
 
+// Every index the coupling kernels touch must lie inside both blocks' arrays;
+// the reference trusts its input files here, the GPU path refuses instead.
+bool iface_in_bounds(const HostInterface* it, const HostBlock* A, const HostBlock* B) {
+  const int na[3] = {A->d.d.NX, A->d.d.NY, A->d.d.NZ};
+  const int nb[3] = {B->d.d.NX, B->d.d.NY, B->d.d.NZ};
+  for (int comp = 0; comp < 4; ++comp)
+    for (int ax = 0; ax < 3; ++ax) {
+      const int t = 3 * comp + ax;
+      const bool stag = comp == ax + 1;  // u along x, v along y, w along z
+      const int64_t cnt = it->counter[t];
+      const auto& T = it->tab[t];
+      if ((int64_t)T.size() != 3 * cnt || cnt < 3) return false;
+      auto e = [&](int r, int64_t q) { return T[(size_t)(3 * (q - 1) + r - 1)]; };
+      const int64_t ga = na[ax] + (stag ? 1 : 0), gb = nb[ax] + (stag ? 1 : 0);  // grid lengths
+      for (int64_t q = 1; q <= cnt; ++q) {
+        const int64_t loc = e(1, q), s = e(2, q), f = e(3, q);
+        // coarse -> fine faces: donors loc-1..loc+1 (loc-2..loc on the staggered axis)
+        if (loc - 1 < 1 || loc + 1 > ga) return false;
+        if ((stag ? loc - 2 : loc - 1) < 1 || (stag ? loc : loc + 1) > na[ax]) return false;
+        if (s < 1 || f > gb || s > f) return false;
+        if ((stag ? s - 1 : s) < 1 || (stag ? f - 1 : f) > nb[ax]) return false;
+        if (q >= 2 && q <= cnt - 1 && f > nb[ax]) return false;  // cell_n(s) of fineUpdate_mv
+        // fine -> coarse restriction entries cintp..cnt-cintp
+        if (q >= 3 && q <= cnt - 3) {
+          const int64_t l = stag ? f : (s + f - 1) / 2;
+          const int64_t lo = stag ? l - 2 : l, hi = stag ? l - 1 : l + 1;
+          if (lo < 1 || hi > nb[ax] || (stag ? l - 1 : l) < 1 || (stag ? l : l + 1) > gb) return false;
+          if ((stag ? loc - 1 : loc) < 1 || loc > ga || (stag ? loc - 1 : loc) > na[ax]) return false;
+        }
+      }
+    }
+  return true;
+}
+
 // all registered blocks in registration order
 std::vector<std::pair<bcfd_handle, HostBlock*>> blocks() {
   std::vector<std::pair<bcfd_handle, HostBlock*>> v;
@@ -147,6 +181,8 @@ int poisson(const SolveCfg& c, int start, int finish, int step) {
     if (in(g)) {
       TRY(launch_correct_pressure(hb));
       TRY(launch_correct_velocity(hb, c.dt));
+      // the divergence the solve leaves behind (measurement, not in the reference)
+      TRY(launch_max_div(hb, true));
     }
   for (auto& [g, hb] : all)
     if (in(g) && g == 1) TRY(launch_velocity_bc(hb, c.dt, c.uc));
@@ -230,6 +266,10 @@ int bcfd_interface_create(bcfd_handle a, bcfd_handle b, int64_t a_msh, int64_t b
   for (int t = 0; t < 12; ++t) {
     const int ax = t % 3;
     set_interface_detail(*g[t], box[2 * ax], box[2 * ax + 1], f, it->tab[t], it->counter[t], starter[t]);
+  }
+  if (!iface_in_bounds(it, A, B)) {
+    delete it;
+    return BCFD_E_ARG;
   }
   int r = upload_iface(it);
   if (r) {

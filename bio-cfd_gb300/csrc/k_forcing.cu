@@ -374,13 +374,18 @@ __global__ void __launch_bounds__(256) k_forcing_dag(DevBlock B, DagArgs g, DagS
   }
 }
 
-// velocityForcingField (mode 1): reads ut/vt/wt, writes u/v/w -- independent
+// velocityForcingField (mode 1): reads ut/vt/wt, writes u/v/w.  No task reads
+// another's output, but two tasks write the same face (the "2" face of cell
+// (i,j,k) is the "1" face of cell (i+1,j,k)): only the serially later writer
+// stores.
 __global__ void k_vel_field(DevBlock B) {
   const int nib = (int)min(B.cnt[C_IB], (int64_t)B.cap_ib);
   const int nt = 6 * nib;
+  const DagArgs g{1, 1};
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
     const int n = t / 6, comp = t % 6;
     const Probe P = make_probe(B, 1, comp, n);
+    if (!is_last_writer(B, g, t, P)) continue;
     const double* src = comp_array(B, P.axis, true);
     double f[8];
 #pragma unroll
@@ -426,19 +431,27 @@ __global__ void k_p_ghost(DevBlock B) {
 }  // namespace
 
 static DagScratch& dag_scratch(HostBlock* hb, int* status) {
-  static std::vector<std::pair<HostBlock*, std::pair<DagScratch, int64_t>>> tab;
   *status = 0;
-  const int64_t need = 6 * (int64_t)hb->d.cap_ib;
-  for (auto& p : tab)
-    if (p.first == hb && p.second.second >= need) return p.second.first;
-  DagScratch s{};
-  if (cudaMalloc(&s.out, need * sizeof(double)) != cudaSuccess ||
-      cudaMalloc(&s.dep, need * 8 * sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&s.level, need * sizeof(int)) != cudaSuccess ||
-      cudaMalloc(&s.flag, 8 * sizeof(int)) != cudaSuccess)
-    *status = BCFD_E_NOMEM;
-  tab.push_back({hb, {s, need}});
-  return tab.back().second.first;
+  if (!hb->dag_scratch) {
+    const int64_t need = 6 * (int64_t)hb->d.cap_ib;
+    DagScratch* s = new DagScratch{};
+    if (cudaMalloc(&s->out, need * sizeof(double)) != cudaSuccess ||
+        cudaMalloc(&s->dep, need * 8 * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&s->level, need * sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&s->flag, 8 * sizeof(int)) != cudaSuccess)
+      *status = BCFD_E_NOMEM;
+    hb->dag_scratch = s;
+  }
+  return *static_cast<DagScratch*>(hb->dag_scratch);
+}
+
+void free_dag_scratch(HostBlock* hb) {
+  if (!hb->dag_scratch) return;
+  DagScratch* s = static_cast<DagScratch*>(hb->dag_scratch);
+  for (void* p : {(void*)s->out, (void*)s->dep, (void*)s->level, (void*)s->flag})
+    if (p) cudaFree(p);
+  delete s;
+  hb->dag_scratch = nullptr;
 }
 
 static int launch_dag(HostBlock* hb, int mode, int vel) {

@@ -99,7 +99,22 @@ __device__ __forceinline__ void half_sweep64(const DevBlock& B, const RowMap& rm
 struct SorArgs {
   int64_t itmax;
   double epsi, omega;
+  int64_t* log;  // measurement log (nullptr outside a profiling window)
 };
+
+// append {sweep pairs, FP64 residual passes, fluid cells, precision}
+__device__ __forceinline__ void log_solve(int64_t* log, int64_t sweeps, int64_t res_passes,
+                                          int64_t fluid, int64_t precision) {
+  if (!log) return;
+  const unsigned long long s = atomicAdd(reinterpret_cast<unsigned long long*>(log), 1ull);
+  if (s < kProfLogCap) {
+    int64_t* e = log + 1 + 4 * s;
+    e[0] = sweeps;
+    e[1] = res_passes;
+    e[2] = fluid;
+    e[3] = precision;
+  }
+}
 
 // REDBLACKSOR_linear (src/PcorVcor.F90:288-377) as one cooperative launch.
 // nIterPcor continues from stats->niter (the fine blocks accumulate it over
@@ -134,6 +149,7 @@ __global__ void __launch_bounds__(256) k_sor64(DevBlock B, SorArgs a, GridBar gb
     if (derr4 < a.epsi || it > a.itmax) break;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
+    log_solve(a.log, it - st->niter, 0, B.cnt[C_FLUID], 0);
     st->niter = it;
     st->derr2 = derr4;
     if (ok && !(derr4 == derr4)) set_err(B.err, BCFD_E_NONFINITE);
@@ -153,6 +169,7 @@ struct DcArgs {
   int inner;          // FP32 sweeps per correction
   float omega;        // relaxation of the FP32 sweeps
   double dt, div_tol;
+  int64_t* log;
 };
 
 __device__ __forceinline__ void cell_of(const DevBlock& B, const RowMap& rm, int64_t t, int C,
@@ -270,10 +287,39 @@ __global__ void __launch_bounds__(256) k_sor_dc(DevBlock B, DcArgs a, GridBar gb
     if (!grid_sync(gb)) return;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
+    log_solve(a.log, sweeps, outer + 1, B.cnt[C_FLUID], 1);
     st->niter = st->niter + sweeps;
     st->derr2 = a.dt * res;
     if (!(res == res)) set_err(B.err, BCFD_E_NONFINITE);
   }
+}
+
+// dt * max over fluid cells of |b/dt - A pc| (FP64, measurement) -> stats->pad[1]
+__global__ void k_resid(DevBlock B, double dt) {
+  __shared__ double sh[32];
+  const RowMap rm{B.d.NXH, B.d.ny};
+  const int64_t total = (int64_t)B.d.NXH * B.d.ny * B.d.nz;
+  const Dims& d = B.d;
+  double m = 0.0;
+  for (int c = 0; c < 2; ++c) {
+    const double* own = B.pc[c];
+    const double* o = B.pc[1 - c];
+    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
+         t += (int64_t)gridDim.x * blockDim.x) {
+      int i, j, k;
+      int64_t pi;
+      cell_of(B, rm, t, c, i, j, k, pi);
+      if (!B.upd[c][pi]) continue;
+      const int64_t row = pi - (i - 1) / 2, sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
+      double ax = (B.Acx[i - 2 + d.nx] + B.Acy[j - 2 + d.ny] + B.Acz[k - 2 + d.nz]) * own[pi];
+      ax += B.Acx[i - 2] * o[row + ((i - 2) >> 1)] + B.Acx[i - 2 + 2 * d.nx] * o[row + (i >> 1)];
+      ax += B.Acy[j - 2] * o[pi - sy] + B.Acy[j - 2 + 2 * d.ny] * o[pi + sy];
+      ax += B.Acz[k - 2] * o[pi - sz] + B.Acz[k - 2 + 2 * d.nz] * o[pi + sz];
+      m = fmax(m, fabs(B.rhs[c][pi] - ax));
+    }
+  }
+  m = block_max(m, sh);
+  if (threadIdx.x == 0) atomic_max_nonneg(&B.stats->pad[1], m * dt);
 }
 
 // correctPressure (src/PcorVcor.F90:245-259)
@@ -335,10 +381,14 @@ __global__ void k_steady(DevBlock B, double dt) {
   if (threadIdx.x == 0) atomic_max_nonneg(&B.stats->derr_std_st, m);
 }
 
-// max |div u| of the current u,v,w over the fluid cells (diagnostic, FP64)
-__global__ void k_maxdiv(DevBlock B) {
+// max |div| over the fluid cells of (u,v,w) (slot maxdiv) or, right after
+// the velocity correction, of (ut,vt,wt) (slot derr_pad[0]); FP64
+__global__ void k_maxdiv(DevBlock B, int tfield) {
   __shared__ double sh[32];
   const Dims& d = B.d;
+  const double* U = tfield ? B.ut : B.u;
+  const double* V = tfield ? B.vt : B.v;
+  const double* W = tfield ? B.wt : B.w;
   const int64_t n = (int64_t)d.nx * d.ny * d.nz;
   double m = 0.0;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
@@ -348,13 +398,12 @@ __global__ void k_maxdiv(DevBlock B) {
     const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
     const int64_t c = d.idx(i, j, k);
     if (B.cell[c] != 0) continue;
-    const double dv = (B.u[c] - B.u[c - 1]) / B.dxa[i - 1] +
-                      (B.v[c] - B.v[c - d.NX]) / B.dya[j - 1] +
-                      (B.w[c] - B.w[c - (int64_t)d.NX * d.NY]) / B.dza[k - 1];
+    const double dv = (U[c] - U[c - 1]) / B.dxa[i - 1] + (V[c] - V[c - d.NX]) / B.dya[j - 1] +
+                      (W[c] - W[c - (int64_t)d.NX * d.NY]) / B.dza[k - 1];
     m = fmax(m, fabs(dv));
   }
   m = block_max(m, sh);
-  if (threadIdx.x == 0) atomic_max_nonneg(&B.stats->maxdiv, m);
+  if (threadIdx.x == 0) atomic_max_nonneg(tfield ? &B.stats->pad[0] : &B.stats->maxdiv, m);
 }
 
 __global__ void k_copy3(double* a, double* b, double* c, const double* x, const double* y,
@@ -440,6 +489,14 @@ int launch_zero_poisson(HostBlock* hb) {
   return 0;
 }
 
+static int launch_residual(HostBlock* hb, double dt) {
+  BCFD_CUDA(cudaMemsetAsync(&hb->d.stats->pad[1], 0, sizeof(double), stream()));
+  const int64_t total = (int64_t)hb->d.d.NXH * hb->d.d.ny * hb->d.d.nz;
+  k_resid<<<grid_for(total, 256, 1024), 256, 0, stream()>>>(hb->d, dt);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
 int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi) {
   DevBlock& B = hb->d;
   const int64_t np = B.d.npacked();
@@ -452,14 +509,16 @@ int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi) {
   const int threads = 256;
   unsigned want = (unsigned)((total + threads - 1) / threads);
   const unsigned grid = coop_grid((const void*)k_sor64, threads, 0, want);
-  SorArgs a{itmax, epsi, hb->omega};
+  SorArgs a{itmax, epsi, hb->omega, prof_log()};
   GridBar gb = make_bar(B.err, grid);
   gb.count = hb->bar;
   gb.gen = hb->bar + 1;
   void* args[] = {(void*)&B, (void*)&a, (void*)&gb};
+  prof_mark(true);
   BCFD_CUDA(launch_coop((const void*)k_sor64, grid, threads, args));
+  prof_mark(false);
   BCFD_LAUNCHED();
-  return 0;
+  return launch_residual(hb, dt);
 }
 
 int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
@@ -481,13 +540,16 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   a.max_outer = itmax / a.inner + 1;
   a.dt = dt;
   a.div_tol = div_tol;
+  a.log = prof_log();
   GridBar gb = make_bar(B.err, grid);
   gb.count = hb->bar;
   gb.gen = hb->bar + 1;
   void* args[] = {(void*)&B, (void*)&a, (void*)&gb};
+  prof_mark(true);
   BCFD_CUDA(launch_coop((const void*)k_sor_dc, grid, threads, args));
+  prof_mark(false);
   BCFD_LAUNCHED();
-  return 0;
+  return launch_residual(hb, dt);
 }
 
 int launch_steady_state(HostBlock* hb, double dt) {
@@ -498,10 +560,11 @@ int launch_steady_state(HostBlock* hb, double dt) {
   return 0;
 }
 
-int launch_max_div(HostBlock* hb) {
+int launch_max_div(HostBlock* hb, bool tfield) {
   const int64_t n = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-  BCFD_CUDA(cudaMemsetAsync(&hb->d.stats->maxdiv, 0, sizeof(double), stream()));
-  k_maxdiv<<<grid_for(n, 256, 1024), 256, 0, stream()>>>(hb->d);
+  double* slot = tfield ? &hb->d.stats->pad[0] : &hb->d.stats->maxdiv;
+  BCFD_CUDA(cudaMemsetAsync(slot, 0, sizeof(double), stream()));
+  k_maxdiv<<<grid_for(n, 256, 1024), 256, 0, stream()>>>(hb->d, tfield ? 1 : 0);
   BCFD_LAUNCHED();
   return 0;
 }

@@ -524,11 +524,17 @@ struct SearchScratch {
 };
 
 static SearchScratch& scratch_of(HostBlock* hb) {
-  static std::vector<std::pair<HostBlock*, SearchScratch*>> tab;
-  for (auto& p : tab)
-    if (p.first == hb) return *p.second;
-  tab.push_back({hb, new SearchScratch()});
-  return *tab.back().second;
+  if (!hb->search_scratch) hb->search_scratch = new SearchScratch();
+  return *static_cast<SearchScratch*>(hb->search_scratch);
+}
+
+void free_search_scratch(HostBlock* hb) {
+  if (!hb->search_scratch) return;
+  SearchScratch* s = static_cast<SearchScratch*>(hb->search_scratch);
+  for (void* p : {(void*)s->cf, (void*)s->org, (void*)s->mark, (void*)s->list, (void*)s->count, (void*)s->cta})
+    if (p) cudaFree(p);
+  delete s;
+  hb->search_scratch = nullptr;
 }
 
 static int ensure_scratch(HostBlock* hb) {
@@ -559,7 +565,9 @@ static int ensure_scratch(HostBlock* hb) {
                z0 = hb->z1[0], z1 = hb->z1[d.nz + 2];
   float h[4] = {(float)(0.5 * (x0 + x1)), (float)(0.5 * (y0 + y1)), (float)(0.5 * (z0 + z1)), 0.f};
   const double R = 0.5 * std::sqrt((x1 - x0) * (x1 - x0) + (y1 - y0) * (y1 - y0) + (z1 - z0) * (z1 - z0));
-  h[3] = (float)(2.0 * R + 1.0);  // elements may lie slightly outside the block
+  // bound on |query - origin| and |centroid - origin| (centroids lie inside
+  // the hull of the nodes)
+  h[3] = (float)(1.01 * std::max(R, hb->node_rmax) + 1e-6);
   BCFD_CUDA(cudaMemcpyAsync(s.org, h, sizeof(h), cudaMemcpyHostToDevice, stream()));
   return 0;
 }

@@ -188,6 +188,27 @@ int bcfd_block_set_role(bcfd_handle h, int is_coarse, int has_body);
 int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps);
 /* max over fluid cells of |div u| of the current u,v,w (FP64) */
 int bcfd_max_divergence(bcfd_handle h, double* out);
+/* out[0] = max over fluid cells of |div ut| right after the last velocity
+ * correction; out[1] = deltat * max over fluid cells of |b/deltat - A pc|, the
+ * FP64 Poisson residual of the last solve in divergence units (the divergence
+ * the correction leaves wherever the operators are consistent) */
+int bcfd_block_get_divergence(bcfd_handle h, double* out);
+/* mixed-precision solve parameters of a block: FP32 sweeps per correction and
+ * their relaxation factor (0 selects the defaults) */
+int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega);
+
+/* ---- measurement window (no counterpart in the reference) ----------------- */
+typedef struct bcfd_profile_report {
+  int64_t sor_launches;   /* persistent Poisson-solve launches in the window      */
+  double sor_ms;          /* their summed device time (CUDA events, library stream) */
+  double sor_bytes;       /* algorithmic bytes they moved (4w+1 B per cell sweep
+                             pair, w = 8 FP64 / 4 FP32, plus the FP64 residual and
+                             update passes of the mixed solve)                     */
+  int64_t sor_sweeps;     /* red+black sweep pairs done by them                    */
+  int64_t kernel_launches;/* kernels launched in the window                        */
+} bcfd_profile_report;
+int bcfd_profile_begin(void);
+int bcfd_profile_end(bcfd_profile_report* out);
 
 #ifdef __cplusplus
 }

@@ -2,6 +2,13 @@
 //
 // Bio-CFD hot-path ORACLE -- TEST INFRASTRUCTURE ONLY.
 //
+// Parity status: pinned against the reference's own known-answer tests for
+// the interpolation primitives, cellCount_solid_coarse and
+// updateVelocity_newv; parity unpinned for the momentum, SOR, forcing,
+// Search and coupling routines (the reference ships no golden values for
+// them and cannot be compiled here: it is Fortran and no Fortran compiler
+// exists on either machine).
+//
 // A serial FP64 C++ restatement of the reference's per-time-step hot path,
 // used by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg as
 // the checker.  The shipped library (bio-cfd_gb300/) never links, loads or

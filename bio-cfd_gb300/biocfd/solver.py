@@ -219,9 +219,9 @@ class Solver:
         check(self.L.bcfd_block_get_divergence(g, _pd(d)), "get_divergence")
         return float(d[0]), float(d[1])
 
-    def set_mixed_params(self, inner: int = 0, omega: float = 0.0):
-        for g in self.handles:
-            check(self.L.bcfd_block_set_mixed_params(g, inner, omega), "set_mixed_params")
+    def set_mixed_params(self, inner: int = 0, omega: float = 0.0, variant: int = 0, block: int = None):
+        for g in (self.handles if block is None else [block]):
+            check(self.L.bcfd_block_set_mixed_params(g, inner, omega, variant), "set_mixed_params")
 
     def profile_begin(self):
         check(self.L.bcfd_profile_begin(), "profile_begin")

@@ -143,6 +143,15 @@ int upload_grids(HostBlock* hb) {
                             &hb->d.xu, &hb->d.yu, &hb->d.zu, &hb->d.xv, &hb->d.yv, &hb->d.zv,
                             &hb->d.xw, &hb->d.yw, &hb->d.zw, &hb->d.xp, &hb->d.yp, &hb->d.zp};
   for (int q = 0; q < 18; ++q) *dst[q] = hb->grid_buf + off[q];
+  std::vector<float> f;
+  for (const auto* a : {&hb->dxa, &hb->dya, &hb->dza})
+    for (double x : *a) f.push_back((float)x);
+  if (!hb->grid_f32) TRY(dalloc(hb, &hb->grid_f32, f.size()));
+  BCFD_CUDA(cudaMemcpyAsync(hb->grid_f32, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice, stream()));
+  BCFD_CUDA(cudaStreamSynchronize(stream()));
+  hb->d.dxf = hb->grid_f32;
+  hb->d.dyf = hb->grid_f32 + hb->dxa.size();
+  hb->d.dzf = hb->grid_f32 + hb->dxa.size() + hb->dya.size();
   return 0;
 }
 
@@ -323,6 +332,31 @@ int upload_coefs(HostBlock* hb) {
   hb->d.Acx = hb->coef_buf + off[0];
   hb->d.Acy = hb->coef_buf + off[1];
   hb->d.Acz = hb->coef_buf + off[2];
+  {
+    std::vector<float> f;
+    for (const auto* v : {&hb->Acx, &hb->Acy, &hb->Acz})
+      for (double x : *v) f.push_back((float)x);
+    std::vector<size_t> foff;
+    for (int t = 0; t < 2 * N_TAB; ++t) {
+      foff.push_back(f.size());
+      for (double x : (t < N_TAB ? hb->ca[t] : hb->ck[t - N_TAB])) f.push_back((float)x);
+    }
+    if (hb->coef_f32) {
+      cudaFree(hb->coef_f32);
+      hb->allocs.erase(std::remove(hb->allocs.begin(), hb->allocs.end(), (void*)hb->coef_f32), hb->allocs.end());
+      hb->coef_f32 = nullptr;
+    }
+    TRY(dalloc(hb, &hb->coef_f32, std::max<size_t>(f.size(), 1)));
+    BCFD_CUDA(cudaMemcpyAsync(hb->coef_f32, f.data(), f.size() * sizeof(float), cudaMemcpyHostToDevice, stream()));
+    BCFD_CUDA(cudaStreamSynchronize(stream()));
+    hb->d.Acxf = hb->coef_f32;
+    hb->d.Acyf = hb->coef_f32 + hb->Acx.size();
+    hb->d.Aczf = hb->coef_f32 + hb->Acx.size() + hb->Acy.size();
+    for (int t = 0; t < N_TAB; ++t) {
+      hb->d.caf[t] = hb->coef_f32 + foff[t];
+      hb->d.ckf[t] = hb->coef_f32 + foff[N_TAB + t];
+    }
+  }
   for (int t = 0; t < N_TAB; ++t) {
     hb->d.ca[t] = hb->coef_buf + off[3 + t];
     hb->d.ck[t] = hb->coef_buf + off[3 + N_TAB + t];
@@ -777,7 +811,7 @@ int bcfd_ns_momentum_2order(bcfd_handle h, double deltat, double re) {
   LOCK();
   GETB(h);
   if (!hb->d.ca[0]) return BCFD_E_STATE;
-  return launch_momentum(hb, deltat, re);
+  return launch_momentum(hb, deltat, re, false);
 }
 int bcfd_velocity_bc(bcfd_handle h, double deltat, double uc) {
   LOCK();
@@ -891,12 +925,14 @@ int bcfd_block_get_divergence(bcfd_handle h, double* out) {
   return 0;
 }
 
-int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega) {
+int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant) {
   LOCK();
   GETB(h);
-  if (inner_sweeps < 0 || omega < 0.0 || omega >= 2.0) return BCFD_E_ARG;
+  if (inner_sweeps < 0 || inner_sweeps > 100000 || omega < 0.0 || omega >= 2.0 || variant < 0 || variant > 1)
+    return BCFD_E_ARG;
   hb->dc_inner = (int)inner_sweeps;
   hb->dc_omega = omega;
+  hb->dc_variant = variant;
   return 0;
 }
 

@@ -27,6 +27,8 @@ struct HostBlock {
   BlockStats* stats = nullptr;     // device
   double* grid_buf = nullptr;      // device buffer holding all 1-D arrays
   double* coef_buf = nullptr;      // device Acx/Acy/Acz + ca/ck tables
+  float* grid_f32 = nullptr;       // device dxa/dya/dza rounded to FP32
+  float* coef_f32 = nullptr;       // device Acx/Acy/Acz rounded to FP32
   int surf_cap_e = 0, surf_cap_n = 0;
   // per-block barrier words for persistent kernels: [count, gen]
   unsigned* bar = nullptr;
@@ -34,6 +36,8 @@ struct HostBlock {
   // (0 = defaults chosen from the block size)
   int dc_inner = 0;
   double dc_omega = 0.0;
+  // mixed solve kernel: 0 = cluster-resident when the block fits, 1 = grid-wide
+  int dc_variant = 0;
   // largest distance of a surface node from the block centre (for the FP32
   // prefilter bound of the nearest-element search)
   double node_rmax = 0.0;
@@ -83,6 +87,7 @@ HostInterface* get_iface(bcfd_handle h);
 // record one kernel launch (for the launch counter) and check the launch
 int note_launch(cudaError_t e = cudaGetLastError());
 #define BCFD_LAUNCHED() do { int _r = ::bcfd::note_launch(); if (_r) return _r; } while (0)
+#define TRY_R(x) do { int _r = (x); if (_r) return _r; } while (0)
 #define BCFD_CUDA(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { ::bcfd::report_cuda(_e, #x, __FILE__, __LINE__); return BCFD_E_CUDA; } } while (0)
 void report_cuda(cudaError_t e, const char* what, const char* file, int line);
 
@@ -94,7 +99,8 @@ int take_block_error(HostBlock* hb);
 int launch_compute_div(HostBlock* hb);
 int launch_correct_pressure(HostBlock* hb);
 int launch_correct_velocity(HostBlock* hb, double dt);
-int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi);
+// res_tol > 0: stop on the FP64 residual dt*max|b/dt - A pc| <= res_tol
+int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol = 0.0);
 int launch_zero_poisson(HostBlock* hb);
 int launch_steady_state(HostBlock* hb, double dt);
 int launch_copy_t_to_n(HostBlock* hb);
@@ -108,8 +114,11 @@ int launch_max_div(HostBlock* hb, bool tfield);
 int64_t* prof_log();
 void prof_mark(bool begin);
 int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol);
+// k_sor_cluster.cu
+int cluster_solve_fits(HostBlock* hb);
+int launch_sor_cluster(HostBlock* hb, int64_t itmax, double dt, double div_tol, int inner, float omega);
 // k_momentum.cu
-int launch_momentum(HostBlock* hb, double dt, double re);
+int launch_momentum(HostBlock* hb, double dt, double re, bool fp32);
 int launch_velocity_bc(HostBlock* hb, double dt, double uc);
 int launch_solid_bc(HostBlock* hb, bool move);
 // k_search.cu

@@ -49,6 +49,35 @@ struct Dims {
 // colour of a cell: 1 = red (i+j+k odd, src/Search.F90:707,724), 0 = black
 __host__ __device__ inline int colour_of(int i, int j, int k) { return (i + j + k) & 1; }
 
+// Incremental (a, b, c) coordinates of t = t0, t0 + S, t0 + 2S, ... over an
+// n0 x n1 x n2 box in x-fastest order, without a division per step: the
+// stride is decomposed once and each step adds it with single carries.
+struct Walk3 {
+  int a, b, c;
+  int da, db, dc, n0, n1;
+  __device__ __forceinline__ void init(int t0, int S, int n0_, int n1_) {
+    n0 = n0_;
+    n1 = n1_;
+    a = t0 % n0;
+    const int r = t0 / n0;
+    b = r % n1;
+    c = r / n1;
+    da = S % n0;
+    const int rs = S / n0;
+    db = rs % n1;
+    dc = rs / n1;
+  }
+  __device__ __forceinline__ void next() {
+    a += da;
+    int carry = a >= n0;
+    a -= carry ? n0 : 0;
+    b += db + carry;
+    carry = b >= n1;
+    b -= carry ? n1 : 0;
+    c += dc + carry;
+  }
+};
+
 // Momentum coefficient tables, order of src/NavierStokes.f90:32-40
 enum CoefTab { T_UU = 0, T_VV, T_WW, T_UV, T_UW, T_VU, T_VW, T_WU, T_WV, N_TAB };
 
@@ -60,8 +89,13 @@ struct DevBlock {
   const double *xu, *yu, *zu, *xv, *yv, *zv, *xw, *yw, *zw, *xp, *yp, *zp;
   // Poisson line coefficients Acx(nx,3) etc., column-major like the reference
   const double *Acx, *Acy, *Acz;
+  // the same coefficients rounded to FP32 (mixed-precision sweeps)
+  const float *Acxf, *Acyf, *Aczf;
   // momentum tables ca/ck(6, n+2), column-major
   const double *ca[N_TAB], *ck[N_TAB];
+  // FP32 copies of dxa/dya/dza and ca/ck (FP32 momentum stencil)
+  const float *dxf, *dyf, *dzf;
+  const float *caf[N_TAB], *ckf[N_TAB];
   // fields
   double *u, *v, *w, *p, *ut, *vt, *wt;
   // tags

@@ -151,8 +151,11 @@ struct SolveCfg {
   double div_tol;
 };
 
+// precision 0: FP64, the reference's stop test (drop-in arithmetic);
+// 1: FP32 SOR + FP64 defect correction to div_tol; 2: FP64 SOR to div_tol
 int sor(HostBlock* hb, const SolveCfg& c) {
   if (c.precision == 1) return launch_sor_mixed(hb, c.itmax, c.dt, c.div_tol);
+  if (c.precision == 2) return launch_sor(hb, c.itmax, c.dt, c.epsi, c.div_tol);
   return launch_sor(hb, c.itmax, c.dt, c.epsi);
 }
 
@@ -206,7 +209,7 @@ int step_once(const bcfd_step_config& cfg) {
   SolveCfg c{cfg.pc_ita_max, cfg.epsi, cfg.deltat, cfg.uc, cfg.precision, cfg.div_tol};
   auto all = blocks();
   for (auto& [g, hb] : all) {
-    TRY(launch_momentum(hb, cfg.deltat, cfg.re));
+    TRY(launch_momentum(hb, cfg.deltat, cfg.re, cfg.precision == 1));
     if (hb->is_coarse) TRY(launch_velocity_bc(hb, cfg.deltat, cfg.uc));
     if (hb->has_body) {
       TRY(launch_solid_bc(hb, false));

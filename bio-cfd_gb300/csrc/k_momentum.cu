@@ -41,11 +41,23 @@ __device__ __forceinline__ bool adj_ok(const int8_t* c, const Dims& d, bool big,
   return true;
 }
 
+// a grid / coefficient value as T: the FP64 table or its FP32 copy
+template <typename T>
+__device__ __forceinline__ T grid_t(const double* d64, const float* f32, int q) {
+  if constexpr (sizeof(T) == 8) return d64[q];
+  else return f32[q];
+}
+
+// T = double: the reference arithmetic (bit-exact drop-in).  T = float: the
+// FP32 momentum stencil of the mixed-precision path (fields stay FP64 in HBM;
+// stencil values are rounded to FP32 on load, ut/vt/wt stored back as FP64).
+template <typename T>
 __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
+  const T Q25 = T(0.25), HALF = T(0.5), TWO = T(2.0), ONE = T(1.0);
   const Dims& d = B.d;
   const int64_t n = (int64_t)d.nx * d.ny * d.nz;
-  const double alpha = 1.0;
-  const double deltat = a.dt, re = a.re;
+  const T alpha = ONE;
+  const T deltat = T(a.dt), re = T(a.re);
   const int nx_var = d.nx, ny_var = d.ny, nz_var = d.nz;
   const int64_t SX = 1, SY = d.NX, SZ = (int64_t)d.NX * d.NY;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
@@ -59,76 +71,76 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
     const double* __restrict__ V = B.v;
     const double* __restrict__ W = B.w;
     const double* __restrict__ P = B.p;
-#define u(a, b, e) __ldg(U + c + (a) * SX + (b) * SY + (e) * SZ)
-#define v(a, b, e) __ldg(V + c + (a) * SX + (b) * SY + (e) * SZ)
-#define w(a, b, e) __ldg(W + c + (a) * SX + (b) * SY + (e) * SZ)
-#define p(a, b, e) __ldg(P + c + (a) * SX + (b) * SY + (e) * SZ)
-#define DX(q) B.dxa[(q) - 1]
-#define DY(q) B.dya[(q) - 1]
-#define DZ(q) B.dza[(q) - 1]
-#define CA(tab, row, q) B.ca[tab][((row) - 1) + 6 * ((q) - 1)]
-#define CK(tab, row, q) B.ck[tab][((row) - 1) + 6 * ((q) - 1)]
+#define u(a, b, e) (T)__ldg(U + c + (a) * SX + (b) * SY + (e) * SZ)
+#define v(a, b, e) (T)__ldg(V + c + (a) * SX + (b) * SY + (e) * SZ)
+#define w(a, b, e) (T)__ldg(W + c + (a) * SX + (b) * SY + (e) * SZ)
+#define p(a, b, e) (T)__ldg(P + c + (a) * SX + (b) * SY + (e) * SZ)
+#define DX(q) grid_t<T>(B.dxa, B.dxf, (q) - 1)
+#define DY(q) grid_t<T>(B.dya, B.dyf, (q) - 1)
+#define DZ(q) grid_t<T>(B.dza, B.dzf, (q) - 1)
+#define CA(tab, row, q) grid_t<T>(B.ca[tab], B.caf[tab], ((row) - 1) + 6 * ((q) - 1))
+#define CK(tab, row, q) grid_t<T>(B.ck[tab], B.ckf[tab], ((row) - 1) + 6 * ((q) - 1))
     // offsets are relative to (i,j,k): u(-1,0,0) is u(i-1,j,k)
-    const double dxr = DX(i + 1), dx = DX(i), dxl = DX(i - 1);
-    const double dye = DY(j + 1), dy = DY(j), dyw = DY(j - 1);
-    const double dzt = DZ(k + 1), dz = DZ(k), dzb = DZ(k - 1);
+    const T dxr = DX(i + 1), dx = DX(i), dxl = DX(i - 1);
+    const T dye = DY(j + 1), dy = DY(j), dyw = DY(j - 1);
+    const T dzt = DZ(k + 1), dz = DZ(k), dzb = DZ(k - 1);
 
-    const double u1a = u(-1, 0, 0) + u(0, 0, 0);
-    const double u22 = u(-1, 0, 0) - u(0, 0, 0);
-    const double u3 = u(0, 0, 0) + u(1, 0, 0);
-    const double u4 = u(0, 0, 0) - u(1, 0, 0);
-    const double u5 = u(0, -1, 0) + u(0, 0, 0);
-    const double u6 = u(0, -1, 0) - u(0, 0, 0);
-    const double u7 = u(0, 0, 0) + u(0, 1, 0);
-    const double u8 = u(0, 0, 0) - u(0, 1, 0);
-    const double u9 = u(0, 0, -1) + u(0, 0, 0);
-    const double u10 = u(0, 0, -1) - u(0, 0, 0);
-    const double u11 = u(0, 0, 0) + u(0, 0, 1);
-    const double u12 = u(0, 0, 0) - u(0, 0, 1);
-    const double u13 = u(-1, 0, 0) + u(-1, 1, 0);
-    const double u14 = u7;
-    const double u15 = u(-1, 0, 0) + u(-1, 0, 1);
-    const double u16 = u11;
+    const T u1a = u(-1, 0, 0) + u(0, 0, 0);
+    const T u22 = u(-1, 0, 0) - u(0, 0, 0);
+    const T u3 = u(0, 0, 0) + u(1, 0, 0);
+    const T u4 = u(0, 0, 0) - u(1, 0, 0);
+    const T u5 = u(0, -1, 0) + u(0, 0, 0);
+    const T u6 = u(0, -1, 0) - u(0, 0, 0);
+    const T u7 = u(0, 0, 0) + u(0, 1, 0);
+    const T u8 = u(0, 0, 0) - u(0, 1, 0);
+    const T u9 = u(0, 0, -1) + u(0, 0, 0);
+    const T u10 = u(0, 0, -1) - u(0, 0, 0);
+    const T u11 = u(0, 0, 0) + u(0, 0, 1);
+    const T u12 = u(0, 0, 0) - u(0, 0, 1);
+    const T u13 = u(-1, 0, 0) + u(-1, 1, 0);
+    const T u14 = u7;
+    const T u15 = u(-1, 0, 0) + u(-1, 0, 1);
+    const T u16 = u11;
 
-    const double v1a = v(0, -1, 0) + v(1, -1, 0);
-    const double v22 = v(0, 0, 0) + v(1, 0, 0);
-    const double v3 = v(-1, 0, 0) + v(0, 0, 0);
-    const double v4 = v(-1, 0, 0) - v(0, 0, 0);
-    const double v5 = v(0, 0, 0) + v(1, 0, 0);
-    const double v6 = v(0, 0, 0) - v(1, 0, 0);
-    const double v7 = v(0, -1, 0) + v(0, 0, 0);
-    const double v8 = v(0, -1, 0) - v(0, 0, 0);
-    const double v9 = v(0, 0, 0) + v(0, 1, 0);
-    const double v10 = v(0, 0, 0) - v(0, 1, 0);
-    const double v11 = v(0, 0, -1) + v(0, 0, 0);
-    const double v12 = v(0, 0, -1) - v(0, 0, 0);
-    const double v13 = v(0, 0, 0) + v(0, 0, 1);
-    const double v14 = v(0, 0, 0) - v(0, 0, 1);
-    const double v15 = v(0, -1, 0) + v(0, -1, 1);
-    const double v16 = v13;
+    const T v1a = v(0, -1, 0) + v(1, -1, 0);
+    const T v22 = v(0, 0, 0) + v(1, 0, 0);
+    const T v3 = v(-1, 0, 0) + v(0, 0, 0);
+    const T v4 = v(-1, 0, 0) - v(0, 0, 0);
+    const T v5 = v(0, 0, 0) + v(1, 0, 0);
+    const T v6 = v(0, 0, 0) - v(1, 0, 0);
+    const T v7 = v(0, -1, 0) + v(0, 0, 0);
+    const T v8 = v(0, -1, 0) - v(0, 0, 0);
+    const T v9 = v(0, 0, 0) + v(0, 1, 0);
+    const T v10 = v(0, 0, 0) - v(0, 1, 0);
+    const T v11 = v(0, 0, -1) + v(0, 0, 0);
+    const T v12 = v(0, 0, -1) - v(0, 0, 0);
+    const T v13 = v(0, 0, 0) + v(0, 0, 1);
+    const T v14 = v(0, 0, 0) - v(0, 0, 1);
+    const T v15 = v(0, -1, 0) + v(0, -1, 1);
+    const T v16 = v13;
 
-    const double w1a = w(0, 0, -1) + w(1, 0, -1);
-    const double w22 = w(0, 0, 0) + w(1, 0, 0);
-    const double w3 = w(0, 0, -1) + w(0, 1, -1);
-    const double w4 = w(0, 0, 0) + w(0, 1, 0);
-    const double w5 = w(-1, 0, 0) + w(0, 0, 0);
-    const double w6 = w(-1, 0, 0) - w(0, 0, 0);
-    const double w7 = w(0, 0, 0) + w(1, 0, 0);
-    const double w8 = w(0, 0, 0) - w(1, 0, 0);
-    const double w9 = w(0, -1, 0) + w(0, 0, 0);
-    const double w10 = w(0, -1, 0) - w(0, 0, 0);
-    const double w11 = w(0, 0, 0) + w(0, 1, 0);
-    const double w12 = w(0, 0, 0) - w(0, 1, 0);
-    const double w13 = w(0, 0, -1) + w(0, 0, 0);
-    const double w14 = w(0, 0, -1) - w(0, 0, 0);
-    const double w15 = w(0, 0, 0) + w(0, 0, 1);
-    const double w16 = w(0, 0, 0) - w(0, 0, 1);
+    const T w1a = w(0, 0, -1) + w(1, 0, -1);
+    const T w22 = w(0, 0, 0) + w(1, 0, 0);
+    const T w3 = w(0, 0, -1) + w(0, 1, -1);
+    const T w4 = w(0, 0, 0) + w(0, 1, 0);
+    const T w5 = w(-1, 0, 0) + w(0, 0, 0);
+    const T w6 = w(-1, 0, 0) - w(0, 0, 0);
+    const T w7 = w(0, 0, 0) + w(1, 0, 0);
+    const T w8 = w(0, 0, 0) - w(1, 0, 0);
+    const T w9 = w(0, -1, 0) + w(0, 0, 0);
+    const T w10 = w(0, -1, 0) - w(0, 0, 0);
+    const T w11 = w(0, 0, 0) + w(0, 1, 0);
+    const T w12 = w(0, 0, 0) - w(0, 1, 0);
+    const T w13 = w(0, 0, -1) + w(0, 0, 0);
+    const T w14 = w(0, 0, -1) - w(0, 0, 0);
+    const T w15 = w(0, 0, 0) + w(0, 0, 1);
+    const T w16 = w(0, 0, 0) - w(0, 0, 1);
 
-    const double dpdx = (p(0, 0, 0) - p(1, 0, 0)) / (0.5 * (dxr + dx));
-    const double dpdy = (p(0, 0, 0) - p(0, 1, 0)) / (0.5 * (dye + dy));
-    const double dpdz = (p(0, 0, 0) - p(0, 0, 1)) / (0.5 * (dzt + dz));
+    const T dpdx = (p(0, 0, 0) - p(1, 0, 0)) / (HALF * (dxr + dx));
+    const T dpdy = (p(0, 0, 0) - p(0, 1, 0)) / (HALF * (dye + dy));
+    const T dpdz = (p(0, 0, 0) - p(0, 0, 1)) / (HALF * (dzt + dz));
 
-    const double dx2xr = dx + dxr, dx2xl = dx + dxl, dy2ye = dy + dye, dy2yw = dy + dyw,
+    const T dx2xr = dx + dxr, dx2xl = dx + dxl, dy2ye = dy + dye, dy2yw = dy + dyw,
                  dz2zt = dz + dzt, dz2zb = dz + dzb;
 
     // thin-surface neighbours (cell2 == 2 next to this cell) need the ghost
@@ -145,20 +157,20 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
 
     // ---------------- U momentum ----------------
     {
-      const double vu_e = v(1, 0, 0) + (dxr / (dx2xr)) * (v(0, 0, 0) - v(1, 0, 0));
-      const double vu_w = v(1, -1, 0) + (dxr / (dx2xr)) * (v(0, -1, 0) - v(1, -1, 0));
-      const double v_in_um = 0.5 * (vu_e + vu_w);
-      const double wu_n = w(1, 0, 0) + (dxr / (dx2xr)) * (w(0, 0, 0) - w(1, 0, 0));
-      const double wu_s = w(1, 0, -1) + (dxr / (dx2xr)) * (w(0, 0, -1) - w(1, 0, -1));
-      const double w_in_um = 0.5 * (wu_n + wu_s);
-      double duudx, dvudy, dwudz;
+      const T vu_e = v(1, 0, 0) + (dxr / (dx2xr)) * (v(0, 0, 0) - v(1, 0, 0));
+      const T vu_w = v(1, -1, 0) + (dxr / (dx2xr)) * (v(0, -1, 0) - v(1, -1, 0));
+      const T v_in_um = HALF * (vu_e + vu_w);
+      const T wu_n = w(1, 0, 0) + (dxr / (dx2xr)) * (w(0, 0, 0) - w(1, 0, 0));
+      const T wu_s = w(1, 0, -1) + (dxr / (dx2xr)) * (w(0, 0, -1) - w(1, 0, -1));
+      const T w_in_um = HALF * (wu_n + wu_s);
+      T duudx, dvudy, dwudz;
       const bool third = (i > 2 && i < nx_var && j > 2 && j < ny_var + 1 && k > 2 && k < nz_var + 1) &&
                          !near_ib && !near_ts2;
       if (third) {
-        const double ddy = 0.5 * (DY(j) + DY(j - 1));
-        const double ddye = 0.5 * (DY(j) + DY(j + 1));
-        const double ddz = 0.5 * (DZ(k) + DZ(k - 1));
-        const double ddzr = 0.5 * (DZ(k) + DZ(k + 1));
+        const T ddy = HALF * (DY(j) + DY(j - 1));
+        const T ddye = HALF * (DY(j) + DY(j + 1));
+        const T ddz = HALF * (DZ(k) + DZ(k - 1));
+        const T ddzr = HALF * (DZ(k) + DZ(k + 1));
         duudx = u(0, 0, 0) *
                     (CA(T_UU, 1, i) * u(2, 0, 0) + CA(T_UU, 2, i) * u(1, 0, 0) +
                      CA(T_UU, 3, i) * u(0, 0, 0) + CA(T_UU, 4, i) * u(-1, 0, 0) +
@@ -168,7 +180,7 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
                     (CK(T_UU, 1, i) * u(2, 0, 0) + CK(T_UU, 2, i) * u(1, 0, 0) +
                      CK(T_UU, 3, i) * u(0, 0, 0) + CK(T_UU, 4, i) * u(-1, 0, 0) +
                      CK(T_UU, 5, i) * u(-2, 0, 0)) /
-                    (2.0 * CK(T_UU, 6, i) * DX(i));
+                    (TWO * CK(T_UU, 6, i) * DX(i));
         dvudy = v_in_um *
                     (CA(T_VU, 1, j) * u(0, 2, 0) + CA(T_VU, 2, j) * u(0, 1, 0) +
                      CA(T_VU, 3, j) * u(0, 0, 0) + CA(T_VU, 4, j) * u(0, -1, 0) +
@@ -178,7 +190,7 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
                     (CK(T_VU, 1, j) * u(0, 2, 0) + CK(T_VU, 2, j) * u(0, 1, 0) +
                      CK(T_VU, 3, j) * u(0, 0, 0) + CK(T_VU, 4, j) * u(0, -1, 0) +
                      CK(T_VU, 5, j) * u(0, -2, 0)) /
-                    (2.0 * CK(T_VU, 6, j) * ddy);
+                    (TWO * CK(T_VU, 6, j) * ddy);
         dwudz = w_in_um *
                     (CA(T_WU, 1, k) * u(0, 0, 2) + CA(T_WU, 2, k) * u(0, 0, 1) +
                      CA(T_WU, 3, k) * u(0, 0, 0) + CA(T_WU, 4, k) * u(0, 0, -1) +
@@ -188,37 +200,37 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
                     (CK(T_WU, 1, k) * u(0, 0, 2) + CK(T_WU, 2, k) * u(0, 0, 1) +
                      CK(T_WU, 3, k) * u(0, 0, 0) + CK(T_WU, 4, k) * u(0, 0, -1) +
                      CK(T_WU, 5, k) * u(0, 0, -2)) /
-                    (2.0 * CK(T_WU, 6, k) * ddz);
+                    (TWO * CK(T_WU, 6, k) * ddz);
       } else {
-        duudx = -0.25 * (u1a * u1a + alpha * fabs(u1a) * u22 - u3 * u3 - alpha * fabs(u3) * u4) / DX(i);
-        dvudy = -0.25 * (v1a * u5 + alpha * fabs(v1a) * u6 - v22 * u7 - alpha * fabs(v22) * u8) / DY(j);
-        dwudz = -0.25 * (w1a * u9 + alpha * fabs(w1a) * u10 - w22 * u11 - alpha * fabs(w22) * u12) / DZ(k);
+        duudx = -Q25 * (u1a * u1a + alpha * fabs(u1a) * u22 - u3 * u3 - alpha * fabs(u3) * u4) / DX(i);
+        dvudy = -Q25 * (v1a * u5 + alpha * fabs(v1a) * u6 - v22 * u7 - alpha * fabs(v22) * u8) / DY(j);
+        dwudz = -Q25 * (w1a * u9 + alpha * fabs(w1a) * u10 - w22 * u11 - alpha * fabs(w22) * u12) / DZ(k);
       }
-      const double d2udx2 = (2.0 / dx2xr) * ((-u4 / dxr) + (u22 / dx));
-      const double d2udy2 =
-          (2.0 / (0.5 * (dy2ye + dy2yw))) * ((-u8 / (0.5 * dy2ye)) + (u6 / (0.5 * dy2yw)));
-      const double d2udz2 =
-          (2.0 / (0.5 * (dz2zt + dz2zb))) * ((-u12 / (0.5 * dz2zt)) + (u10 / (0.5 * dz2zb)));
-      const double xtt2 = (d2udx2 + d2udy2 + d2udz2) / re;
-      const double residu = (-duudx - dvudy - dwudz + xtt2);
-      B.ut[c] = u(0, 0, 0) + deltat * (residu + dpdx);
+      const T d2udx2 = (TWO / dx2xr) * ((-u4 / dxr) + (u22 / dx));
+      const T d2udy2 =
+          (TWO / (HALF * (dy2ye + dy2yw))) * ((-u8 / (HALF * dy2ye)) + (u6 / (HALF * dy2yw)));
+      const T d2udz2 =
+          (TWO / (HALF * (dz2zt + dz2zb))) * ((-u12 / (HALF * dz2zt)) + (u10 / (HALF * dz2zb)));
+      const T xtt2 = (d2udx2 + d2udy2 + d2udz2) / re;
+      const T residu = (-duudx - dvudy - dwudz + xtt2);
+      B.ut[c] = (double)(u(0, 0, 0) + deltat * (residu + dpdx));
     }
     // ---------------- V momentum ----------------
     {
-      const double uv_e = u(0, 1, 0) + (dye / (dy2ye)) * (u(0, 0, 0) - u(0, 1, 0));
-      const double uv_w = u(-1, 1, 0) + (dye / (dy2ye)) * (u(-1, 0, 0) - u(-1, 1, 0));
-      const double u_in_vm = 0.5 * (uv_e + uv_w);
-      const double wv_n = w(0, 1, 0) + (dye / (dy2ye)) * (w(0, 0, 0) - w(0, 1, 0));
-      const double wv_s = w(0, 1, -1) + (dye / (dy2ye)) * (w(0, 0, -1) - w(0, 1, -1));
-      const double w_in_vm = 0.5 * (wv_n + wv_s);
-      double duvdx, dvvdy, dwvdz;
+      const T uv_e = u(0, 1, 0) + (dye / (dy2ye)) * (u(0, 0, 0) - u(0, 1, 0));
+      const T uv_w = u(-1, 1, 0) + (dye / (dy2ye)) * (u(-1, 0, 0) - u(-1, 1, 0));
+      const T u_in_vm = HALF * (uv_e + uv_w);
+      const T wv_n = w(0, 1, 0) + (dye / (dy2ye)) * (w(0, 0, 0) - w(0, 1, 0));
+      const T wv_s = w(0, 1, -1) + (dye / (dy2ye)) * (w(0, 0, -1) - w(0, 1, -1));
+      const T w_in_vm = HALF * (wv_n + wv_s);
+      T duvdx, dvvdy, dwvdz;
       const bool third = (i > 2 && i < nx_var + 1 && j > 2 && j < ny_var && k > 2 && k < nz_var + 1) &&
                          !near_ib && !near_ts2;
       if (third) {
-        const double ddx = 0.5 * (DX(i) + DX(i - 1));
-        const double ddxr = 0.5 * (DX(i) + DX(i + 1));
-        const double ddz = 0.5 * (DZ(k) + DZ(k - 1));
-        const double ddzr = 0.5 * (DZ(k) + DZ(k + 1));
+        const T ddx = HALF * (DX(i) + DX(i - 1));
+        const T ddxr = HALF * (DX(i) + DX(i + 1));
+        const T ddz = HALF * (DZ(k) + DZ(k - 1));
+        const T ddzr = HALF * (DZ(k) + DZ(k + 1));
         duvdx = u_in_vm *
                     (CA(T_UW, 1, i) * v(2, 0, 0) + CA(T_UW, 2, i) * v(1, 0, 0) +
                      CA(T_UW, 3, i) * v(0, 0, 0) + CA(T_UW, 4, i) * v(-1, 0, 0) +
@@ -228,7 +240,7 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
                     (CK(T_UW, 1, i) * v(2, 0, 0) + CK(T_UW, 2, i) * v(1, 0, 0) +
                      CK(T_UW, 3, i) * v(0, 0, 0) + CK(T_UW, 4, i) * v(-1, 0, 0) +
                      CK(T_UW, 5, i) * v(-2, 0, 0)) /
-                    (2.0 * CK(T_UW, 6, i) * ddx);
+                    (TWO * CK(T_UW, 6, i) * ddx);
         dvvdy = v(0, 0, 0) *
                     (CA(T_VV, 1, j) * v(0, 2, 0) + CA(T_VV, 2, j) * v(0, 1, 0) +
                      CA(T_VV, 3, j) * v(0, 0, 0) + CA(T_VV, 4, j) * v(0, -1, 0) +
@@ -238,7 +250,7 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
                     (CK(T_VV, 1, j) * v(0, 2, 0) + CK(T_VV, 2, j) * v(0, 1, 0) +
                      CK(T_VV, 3, j) * v(0, 0, 0) + CK(T_VV, 4, j) * v(0, -1, 0) +
                      CK(T_VV, 5, j) * v(0, -2, 0)) /
-                    (2.0 * CK(T_VV, 6, j) * DY(j));
+                    (TWO * CK(T_VV, 6, j) * DY(j));
         dwvdz = w_in_vm *
                     (CA(T_WU, 1, k) * v(0, 0, 2) + CA(T_WU, 2, k) * v(0, 0, 1) +
                      CA(T_WU, 3, k) * v(0, 0, 0) + CA(T_WU, 4, k) * v(0, 0, -1) +
@@ -248,37 +260,37 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
                     (CK(T_WU, 1, k) * v(0, 0, 2) + CK(T_WU, 2, k) * v(0, 0, 1) +
                      CK(T_WU, 3, k) * v(0, 0, 0) + CK(T_WU, 4, k) * v(0, 0, -1) +
                      CK(T_WU, 5, k) * v(0, 0, -2)) /
-                    (2.0 * CK(T_WU, 6, k) * ddz);
+                    (TWO * CK(T_WU, 6, k) * ddz);
       } else {
-        duvdx = -0.25 * (u13 * v3 + alpha * fabs(u13) * v4 - u14 * v5 - alpha * fabs(u14) * v6) / DX(i);
-        dvvdy = -0.25 * (v7 * v7 + alpha * fabs(v7) * v8 - v9 * v9 - alpha * fabs(v9) * v10) / DY(j);
-        dwvdz = -0.25 * (w3 * v11 + alpha * fabs(w3) * v12 - w4 * v13 - alpha * fabs(w4) * v14) / DZ(k);
+        duvdx = -Q25 * (u13 * v3 + alpha * fabs(u13) * v4 - u14 * v5 - alpha * fabs(u14) * v6) / DX(i);
+        dvvdy = -Q25 * (v7 * v7 + alpha * fabs(v7) * v8 - v9 * v9 - alpha * fabs(v9) * v10) / DY(j);
+        dwvdz = -Q25 * (w3 * v11 + alpha * fabs(w3) * v12 - w4 * v13 - alpha * fabs(w4) * v14) / DZ(k);
       }
-      const double d2vdx2 =
-          (2.0 / (0.5 * (dx2xr + dx2xl))) * ((-v6 / (0.5 * dx2xr)) + (v4 / (0.5 * dx2xl)));
-      const double d2vdy2 = (2.0 / dy2ye) * ((-v10 / dye) + (v8 / dy));
-      const double d2vdz2 =
-          (2.0 / (0.5 * (dz2zt + dz2zb))) * ((-v14 / (0.5 * dz2zt)) + (v12 / (0.5 * dz2zb)));
-      const double ytt2 = (d2vdx2 + d2vdy2 + d2vdz2) / re;
-      const double residv = (-duvdx - dvvdy - dwvdz + ytt2);
-      B.vt[c] = v(0, 0, 0) + deltat * (residv + dpdy);
+      const T d2vdx2 =
+          (TWO / (HALF * (dx2xr + dx2xl))) * ((-v6 / (HALF * dx2xr)) + (v4 / (HALF * dx2xl)));
+      const T d2vdy2 = (TWO / dy2ye) * ((-v10 / dye) + (v8 / dy));
+      const T d2vdz2 =
+          (TWO / (HALF * (dz2zt + dz2zb))) * ((-v14 / (HALF * dz2zt)) + (v12 / (HALF * dz2zb)));
+      const T ytt2 = (d2vdx2 + d2vdy2 + d2vdz2) / re;
+      const T residv = (-duvdx - dvvdy - dwvdz + ytt2);
+      B.vt[c] = (double)(v(0, 0, 0) + deltat * (residv + dpdy));
     }
     // ---------------- W momentum ----------------
     {
-      const double uw_e = u(0, 0, 1) + (dzt / (dz2zt)) * (u(0, 0, 0) - u(0, 0, 1));
-      const double uw_w = u(-1, 0, 1) + (dzt / (dz2zt)) * (u(-1, 0, 0) - u(-1, 0, 1));
-      const double u_in_wm = 0.5 * (uw_e + uw_w);
-      const double vw_n = v(0, 0, 1) + (dzt / (dz2zt)) * (v(0, 0, 0) - v(0, 0, 1));
-      const double vw_s = v(0, -1, 1) + (dzt / (dz2zt)) * (v(0, -1, 0) - v(0, -1, 1));
-      const double v_in_wm = 0.5 * (vw_n + vw_s);
-      double duwdx, dvwdy, dwwdz;
+      const T uw_e = u(0, 0, 1) + (dzt / (dz2zt)) * (u(0, 0, 0) - u(0, 0, 1));
+      const T uw_w = u(-1, 0, 1) + (dzt / (dz2zt)) * (u(-1, 0, 0) - u(-1, 0, 1));
+      const T u_in_wm = HALF * (uw_e + uw_w);
+      const T vw_n = v(0, 0, 1) + (dzt / (dz2zt)) * (v(0, 0, 0) - v(0, 0, 1));
+      const T vw_s = v(0, -1, 1) + (dzt / (dz2zt)) * (v(0, -1, 0) - v(0, -1, 1));
+      const T v_in_wm = HALF * (vw_n + vw_s);
+      T duwdx, dvwdy, dwwdz;
       const bool third = (i > 2 && i < nx_var + 1 && j > 2 && j < ny_var + 1 && k > 2 && k < nz_var) &&
                          !near_ib && !near_ts2;
       if (third) {
-        const double ddx = 0.5 * (DX(i) + DX(i - 1));
-        const double ddxr = 0.5 * (DX(i) + DX(i + 1));
-        const double ddy = 0.5 * (DY(j) + DY(j - 1));
-        const double ddye = 0.5 * (DY(j) + DY(j + 1));
+        const T ddx = HALF * (DX(i) + DX(i - 1));
+        const T ddxr = HALF * (DX(i) + DX(i + 1));
+        const T ddy = HALF * (DY(j) + DY(j - 1));
+        const T ddye = HALF * (DY(j) + DY(j + 1));
         duwdx = u_in_wm *
                     (CA(T_UW, 1, i) * w(2, 0, 0) + CA(T_UW, 2, i) * w(1, 0, 0) +
                      CA(T_UW, 3, i) * w(0, 0, 0) + CA(T_UW, 4, i) * w(-1, 0, 0) +
@@ -288,7 +300,7 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
                     (CK(T_UW, 1, i) * w(2, 0, 0) + CK(T_UW, 2, i) * w(1, 0, 0) +
                      CK(T_UW, 3, i) * w(0, 0, 0) + CK(T_UW, 4, i) * w(-1, 0, 0) +
                      CK(T_UW, 5, i) * w(-2, 0, 0)) /
-                    (2.0 * CK(T_UW, 6, i) * ddx);
+                    (TWO * CK(T_UW, 6, i) * ddx);
         dvwdy = v_in_wm *
                     (CA(T_VW, 1, j) * w(0, 2, 0) + CA(T_VW, 2, j) * w(0, 1, 0) +
                      CA(T_VW, 3, j) * w(0, 0, 0) + CA(T_VW, 4, j) * w(0, -1, 0) +
@@ -298,7 +310,7 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
                     (CK(T_VW, 1, j) * w(0, 2, 0) + CK(T_VW, 2, j) * w(0, 1, 0) +
                      CK(T_VW, 3, j) * w(0, 0, 0) + CK(T_VW, 4, j) * w(0, -1, 0) +
                      CK(T_VW, 5, j) * w(0, -2, 0)) /
-                    (2.0 * CK(T_VW, 6, j) * ddy);
+                    (TWO * CK(T_VW, 6, j) * ddy);
         dwwdz = w(0, 0, 0) *
                     (CA(T_WW, 1, k) * w(0, 0, 2) + CA(T_WW, 2, k) * w(0, 0, 1) +
                      CA(T_WW, 3, k) * w(0, 0, 0) + CA(T_WW, 4, k) * w(0, 0, -1) +
@@ -308,20 +320,20 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
                     (CK(T_WW, 1, k) * w(0, 0, 2) + CK(T_WW, 2, k) * w(0, 0, 1) +
                      CK(T_WW, 3, k) * w(0, 0, 0) + CK(T_WW, 4, k) * w(0, 0, -1) +
                      CK(T_WW, 5, k) * w(0, 0, -2)) /
-                    (2.0 * CK(T_WW, 6, k) * DZ(k));
+                    (TWO * CK(T_WW, 6, k) * DZ(k));
       } else {
-        duwdx = -0.5 * (u15 * w5 + alpha * fabs(u15) * w6 - u16 * w7 - alpha * fabs(u16) * w8) / DX(i);
-        dvwdy = -0.5 * (v15 * w9 + alpha * fabs(v15) * w10 - v16 * w11 - alpha * fabs(v16) * w12) / DY(j);
-        dwwdz = -0.5 * (w13 * w13 + alpha * fabs(w13) * w14 - w15 * w15 - alpha * fabs(w15) * w16) / DZ(k);
+        duwdx = -HALF * (u15 * w5 + alpha * fabs(u15) * w6 - u16 * w7 - alpha * fabs(u16) * w8) / DX(i);
+        dvwdy = -HALF * (v15 * w9 + alpha * fabs(v15) * w10 - v16 * w11 - alpha * fabs(v16) * w12) / DY(j);
+        dwwdz = -HALF * (w13 * w13 + alpha * fabs(w13) * w14 - w15 * w15 - alpha * fabs(w15) * w16) / DZ(k);
       }
-      const double d2wdx2 =
-          (2.0 / (0.5 * (dx2xr + dx2xl))) * ((-w8 / (0.5 * dx2xr)) + (w6 / (0.5 * dx2xl)));
-      const double d2wdy2 =
-          (2.0 / (0.5 * (dy2ye + dy2yw))) * ((-w12 / (0.5 * dy2ye)) + (w10 / (0.5 * dy2yw)));
-      const double d2wdz2 = (2.0 / dz2zt) * ((-w16 / dzt) + (w14 / dz));
-      const double ztt2 = (d2wdx2 + d2wdy2 + d2wdz2) / re;
-      const double residw = (-duwdx - dvwdy - dwwdz + ztt2);
-      B.wt[c] = w(0, 0, 0) + deltat * (residw + dpdz);
+      const T d2wdx2 =
+          (TWO / (HALF * (dx2xr + dx2xl))) * ((-w8 / (HALF * dx2xr)) + (w6 / (HALF * dx2xl)));
+      const T d2wdy2 =
+          (TWO / (HALF * (dy2ye + dy2yw))) * ((-w12 / (HALF * dy2ye)) + (w10 / (HALF * dy2yw)));
+      const T d2wdz2 = (TWO / dz2zt) * ((-w16 / dzt) + (w14 / dz));
+      const T ztt2 = (d2wdx2 + d2wdy2 + d2wdz2) / re;
+      const T residw = (-duwdx - dvwdy - dwwdz + ztt2);
+      B.wt[c] = (double)(w(0, 0, 0) + deltat * (residw + dpdz));
     }
 #undef u
 #undef v
@@ -412,9 +424,12 @@ __global__ void k_solid_bc(DevBlock B, int move) {
 
 }  // namespace
 
-int launch_momentum(HostBlock* hb, double dt, double re) {
+int launch_momentum(HostBlock* hb, double dt, double re, bool fp32) {
   const int64_t n = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-  k_momentum<<<grid_for(n, 128, 1u << 20), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
+  if (fp32)
+    k_momentum<float><<<grid_for(n, 128, 1u << 20), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
+  else
+    k_momentum<double><<<grid_for(n, 128, 1u << 20), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
   BCFD_LAUNCHED();
   return 0;
 }

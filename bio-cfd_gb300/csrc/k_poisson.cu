@@ -70,10 +70,12 @@ __device__ __forceinline__ void half_sweep64(const DevBlock& B, const RowMap& rm
   const uint8_t* __restrict__ upd = B.upd[C];
   const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int64_t sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    int h, j, k;
-    rm.at(t, h, j, k);
+  const int S = gridDim.x * blockDim.x;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  Walk3 w;
+  w.init(t, S, d.NXH, d.ny);
+  for (; t < (int)total; t += S, w.next()) {
+    const int h = w.a, j = 2 + w.b, k = 2 + w.c;
     const int64_t pi = h + sy * (j - 1) + sz * (k - 1);
     if (!upd[pi]) continue;
     int i = 2 * h + 1;
@@ -96,10 +98,45 @@ __device__ __forceinline__ void half_sweep64(const DevBlock& B, const RowMap& rm
   }
 }
 
+// max over fluid cells of colour C of |b/dt - A pc| (FP64, FMA allowed: this
+// is a stop test of the residual-target mode, not reference arithmetic)
+template <int C>
+__device__ __forceinline__ double resid_max64(const DevBlock& B, const RowMap& rm, int64_t total) {
+  const Dims& d = B.d;
+  const double* own = B.pc[C];
+  const double* o = B.pc[1 - C];
+  const int64_t sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
+  double m = 0.0;
+  const int S = gridDim.x * blockDim.x;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  Walk3 w;
+  w.init(t, S, d.NXH, d.ny);
+  for (; t < (int)total; t += S, w.next()) {
+    const int h = w.a, j = 2 + w.b, k = 2 + w.c;
+    const int64_t pi = h + sy * (j - 1) + sz * (k - 1);
+    if (!B.upd[C][pi]) continue;
+    int i = 2 * h + 1;
+    if (((i + j + k) & 1) != C) ++i;
+    const int64_t row = pi - h;
+    double ax = (B.Acx[i - 2 + d.nx] + B.Acy[j - 2 + d.ny] + B.Acz[k - 2 + d.nz]) * __ldcg(own + pi);
+    ax = fma(B.Acx[i - 2], __ldcg(o + row + ((i - 2) >> 1)), ax);
+    ax = fma(B.Acx[i - 2 + 2 * d.nx], __ldcg(o + row + (i >> 1)), ax);
+    ax = fma(B.Acy[j - 2], __ldcg(o + pi - sy), ax);
+    ax = fma(B.Acy[j - 2 + 2 * d.ny], __ldcg(o + pi + sy), ax);
+    ax = fma(B.Acz[k - 2], __ldcg(o + pi - sz), ax);
+    ax = fma(B.Acz[k - 2 + 2 * d.nz], __ldcg(o + pi + sz), ax);
+    m = fmax(m, fabs(B.rhs[C][pi] - ax));
+  }
+  return m;
+}
+
 struct SorArgs {
   int64_t itmax;
   double epsi, omega;
-  int64_t* log;  // measurement log (nullptr outside a profiling window)
+  int64_t* log;   // measurement log (nullptr outside a profiling window)
+  double res_tol; // > 0: stop on dt * max|b/dt - A pc| <= res_tol instead of
+                  // the reference's increment test (same check cadence)
+  double dt;
 };
 
 // append {sweep pairs, FP64 residual passes, fluid cells, precision}
@@ -136,6 +173,11 @@ __global__ void __launch_bounds__(256) k_sor64(DevBlock B, SorArgs a, GridBar gb
     if (!grid_sync(gb)) { ok = false; break; }
     half_sweep64<0>(B, rm, total, a.omega, lmax);
     const bool chk = (it % 5) == 0;
+    if (chk && a.res_tol > 0.0) {
+      // residual-target mode: the residual needs the whole sweep pair done
+      if (!grid_sync(gb)) { ok = false; break; }
+      lmax = fmax(resid_max64<1>(B, rm, total), resid_max64<0>(B, rm, total)) * a.dt;
+    }
     if (chk) {
       const double m = block_max(lmax, sh);
       if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[check & 1], m);
@@ -146,7 +188,8 @@ __global__ void __launch_bounds__(256) k_sor64(DevBlock B, SorArgs a, GridBar gb
       if (blockIdx.x == 0 && threadIdx.x == 0) st->slot[(check + 1) & 1] = 0.0;
       ++check;
     }
-    if (derr4 < a.epsi || it > a.itmax) break;
+    if (a.res_tol > 0.0 ? (derr4 <= a.res_tol) : (derr4 < a.epsi)) break;
+    if (it > a.itmax) break;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     log_solve(a.log, it - st->niter, 0, B.cnt[C_FLUID], 0);
@@ -172,28 +215,29 @@ struct DcArgs {
   int64_t* log;
 };
 
-__device__ __forceinline__ void cell_of(const DevBlock& B, const RowMap& rm, int64_t t, int C,
-                                        int& i, int& j, int& k, int64_t& pi) {
-  int h;
-  rm.at(t, h, j, k);
-  pi = h + (int64_t)B.d.NXH * (j - 1) + (int64_t)B.d.NXH * B.d.NY * (k - 1);
-  i = 2 * h + 1;
-  if (((i + j + k) & 1) != C) ++i;
-}
+// grid-stride walk over the interior packed positions of colour C: h, j, k,
+// the cell's i and its packed index pi
+#define FOR_PACKED(C_, total_)                                  \
+  const int _S = gridDim.x * blockDim.x;                        \
+  int _t = blockIdx.x * blockDim.x + threadIdx.x;               \
+  Walk3 _w;                                                     \
+  _w.init(_t, _S, B.d.NXH, B.d.ny);                             \
+  for (; _t < (int)(total_); _t += _S, _w.next())
+#define PACKED_CELL(C_)                                                                   \
+  const int h = _w.a, j = 2 + _w.b, k = 2 + _w.c;                                         \
+  const int64_t pi = h + (int64_t)B.d.NXH * (j - 1) + (int64_t)B.d.NXH * B.d.NY * (k - 1); \
+  const int i = 2 * h + 1 + ((((2 * h + 1) + j + k) & 1) != (C_))
 
 // FP64 residual of colour C into rhsf[C]; returns the local max |r|
 template <int C>
-__device__ __forceinline__ double residual64(const DevBlock& B, const RowMap& rm, int64_t total) {
+__device__ __forceinline__ double residual64(const DevBlock& B, int64_t total) {
   const Dims& d = B.d;
   const double* __restrict__ own = B.pc[C];
   const double* __restrict__ o = B.pc[1 - C];
   const int64_t sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
   double m = 0.0;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    int i, j, k;
-    int64_t pi;
-    cell_of(B, rm, t, C, i, j, k, pi);
+  FOR_PACKED(C, total) {
+    PACKED_CELL(C);
     if (!B.upd[C][pi]) continue;
     const int64_t row = pi - (i - 1) / 2;
     const double ax1 = B.Acx[i - 2], ax2 = B.Acx[i - 2 + d.nx], ax3 = B.Acx[i - 2 + 2 * d.nx];
@@ -215,25 +259,18 @@ __device__ __forceinline__ double residual64(const DevBlock& B, const RowMap& rm
 
 // one FP32 half-sweep on the correction e (stored in pcf)
 template <int C>
-__device__ __forceinline__ void half_sweep32(const DevBlock& B, const RowMap& rm, int64_t total,
-                                             float omega) {
+__device__ __forceinline__ void half_sweep32(const DevBlock& B, int64_t total, float omega) {
   const Dims& d = B.d;
   const float* __restrict__ o = B.pcf[1 - C];
   float* __restrict__ own = B.pcf[C];
   const int64_t sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    int i, j, k;
-    int64_t pi;
-    cell_of(B, rm, t, C, i, j, k, pi);
+  FOR_PACKED(C, total) {
+    PACKED_CELL(C);
     if (!B.upd[C][pi]) continue;
     const int64_t row = pi - (i - 1) / 2;
-    const float ax1 = (float)B.Acx[i - 2], ax2 = (float)B.Acx[i - 2 + d.nx],
-                ax3 = (float)B.Acx[i - 2 + 2 * d.nx];
-    const float ay1 = (float)B.Acy[j - 2], ay2 = (float)B.Acy[j - 2 + d.ny],
-                ay3 = (float)B.Acy[j - 2 + 2 * d.ny];
-    const float az1 = (float)B.Acz[k - 2], az2 = (float)B.Acz[k - 2 + d.nz],
-                az3 = (float)B.Acz[k - 2 + 2 * d.nz];
+    const float ax1 = B.Acxf[i - 2], ax2 = B.Acxf[i - 2 + d.nx], ax3 = B.Acxf[i - 2 + 2 * d.nx];
+    const float ay1 = B.Acyf[j - 2], ay2 = B.Acyf[j - 2 + d.ny], ay3 = B.Acyf[j - 2 + 2 * d.ny];
+    const float az1 = B.Aczf[k - 2], az2 = B.Aczf[k - 2 + d.nz], az3 = B.Aczf[k - 2 + 2 * d.nz];
     float s = B.rhsf[C][pi];
     s = __fmaf_rn(-ax1, __ldcg(o + row + ((i - 2) >> 1)), s);
     s = __fmaf_rn(-ax3, __ldcg(o + row + (i >> 1)), s);
@@ -267,8 +304,8 @@ __global__ void __launch_bounds__(256) k_sor_dc(DevBlock B, DcArgs a, GridBar gb
   double res = 0.0;
   int64_t outer = 0;
   for (;; ++outer) {
-    double m = residual64<1>(B, rm, total);
-    m = fmax(m, residual64<0>(B, rm, total));
+    double m = residual64<1>(B, total);
+    m = fmax(m, residual64<0>(B, total));
     m = block_max(m, sh);
     if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[outer & 1], m);
     if (!grid_sync(gb)) return;
@@ -276,9 +313,9 @@ __global__ void __launch_bounds__(256) k_sor_dc(DevBlock B, DcArgs a, GridBar gb
     if (blockIdx.x == 0 && threadIdx.x == 0) st->slot[(outer + 1) & 1] = 0.0;
     if (a.dt * res <= a.div_tol || outer >= a.max_outer || !(res == res)) break;
     for (int it = 0; it < a.inner; ++it) {
-      half_sweep32<1>(B, rm, total, a.omega);
+      half_sweep32<1>(B, total, a.omega);
       if (!grid_sync(gb)) return;
-      half_sweep32<0>(B, rm, total, a.omega);
+      half_sweep32<0>(B, total, a.omega);
       if (!grid_sync(gb)) return;
     }
     sweeps += a.inner;
@@ -297,28 +334,9 @@ __global__ void __launch_bounds__(256) k_sor_dc(DevBlock B, DcArgs a, GridBar gb
 // dt * max over fluid cells of |b/dt - A pc| (FP64, measurement) -> stats->pad[1]
 __global__ void k_resid(DevBlock B, double dt) {
   __shared__ double sh[32];
-  const RowMap rm{B.d.NXH, B.d.ny};
   const int64_t total = (int64_t)B.d.NXH * B.d.ny * B.d.nz;
-  const Dims& d = B.d;
-  double m = 0.0;
-  for (int c = 0; c < 2; ++c) {
-    const double* own = B.pc[c];
-    const double* o = B.pc[1 - c];
-    for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < total;
-         t += (int64_t)gridDim.x * blockDim.x) {
-      int i, j, k;
-      int64_t pi;
-      cell_of(B, rm, t, c, i, j, k, pi);
-      if (!B.upd[c][pi]) continue;
-      const int64_t row = pi - (i - 1) / 2, sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
-      double ax = (B.Acx[i - 2 + d.nx] + B.Acy[j - 2 + d.ny] + B.Acz[k - 2 + d.nz]) * own[pi];
-      ax += B.Acx[i - 2] * o[row + ((i - 2) >> 1)] + B.Acx[i - 2 + 2 * d.nx] * o[row + (i >> 1)];
-      ax += B.Acy[j - 2] * o[pi - sy] + B.Acy[j - 2 + 2 * d.ny] * o[pi + sy];
-      ax += B.Acz[k - 2] * o[pi - sz] + B.Acz[k - 2 + 2 * d.nz] * o[pi + sz];
-      m = fmax(m, fabs(B.rhs[c][pi] - ax));
-    }
-  }
-  m = block_max(m, sh);
+  const RowMap rm{B.d.NXH, B.d.ny};
+  const double m = block_max(fmax(resid_max64<1>(B, rm, total), resid_max64<0>(B, rm, total)), sh);
   if (threadIdx.x == 0) atomic_max_nonneg(&B.stats->pad[1], m * dt);
 }
 
@@ -497,7 +515,7 @@ static int launch_residual(HostBlock* hb, double dt) {
   return 0;
 }
 
-int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi) {
+int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol) {
   DevBlock& B = hb->d;
   const int64_t np = B.d.npacked();
   k_rhs<<<grid_for(np, 256), 256, 0, stream()>>>(B, dt);
@@ -509,7 +527,7 @@ int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi) {
   const int threads = 256;
   unsigned want = (unsigned)((total + threads - 1) / threads);
   const unsigned grid = coop_grid((const void*)k_sor64, threads, 0, want);
-  SorArgs a{itmax, epsi, hb->omega, prof_log()};
+  SorArgs a{itmax, epsi, hb->omega, prof_log(), res_tol, dt};
   GridBar gb = make_bar(B.err, grid);
   gb.count = hb->bar;
   gb.gen = hb->bar + 1;
@@ -526,6 +544,14 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   const int64_t np = B.d.npacked();
   k_rhs<<<grid_for(np, 256), 256, 0, stream()>>>(B, dt);
   BCFD_LAUNCHED();
+  const int nmax0 = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
+  if (hb->dc_variant != 1 && cluster_solve_fits(hb)) {
+    // the whole block fits in one cluster's distributed shared memory
+    const int inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
+    const double om = hb->dc_omega > 0 ? hb->dc_omega : 2.0 / (1.0 + std::sin(3.14159265358979323846 / nmax0));
+    TRY_R(launch_sor_cluster(hb, itmax, dt, div_tol, inner, (float)std::min(1.97, std::max(1.0, om))));
+    return launch_residual(hb, dt);
+  }
   for (int c = 0; c < 2; ++c) BCFD_CUDA(cudaMemsetAsync(B.pcf[c], 0, np * sizeof(float), stream()));
   BCFD_CUDA(cudaMemsetAsync(&B.stats->slot[0], 0, 2 * sizeof(double), stream()));
   BCFD_CUDA(cudaMemsetAsync(hb->bar, 0, 2 * sizeof(unsigned), stream()));

@@ -176,9 +176,11 @@ typedef struct bcfd_step_config {
   double uc;           /* inflow velocity                                      */
   double epsi;         /* SOR stop threshold on max |pc - pco|                 */
   int64_t pc_ita_max;  /* SOR iteration cap                                    */
-  int precision;       /* 0: FP64 reference arithmetic, 1: FP32 SOR + FP64
-                          defect correction                                    */
-  double div_tol;      /* precision 1: target max|div u| after correction      */
+  int precision;       /* 0: FP64 reference arithmetic and stop test (drop-in);
+                          1: FP32 SOR + FP64 defect correction to div_tol;
+                          2: FP64 SOR (reference sweeps) to div_tol            */
+  double div_tol;      /* precision 1/2: target FP64 Poisson residual in
+                          divergence units, deltat * max|b/deltat - A pc|      */
   int use_graph;       /* capture the step in a CUDA graph and replay it       */
 } bcfd_step_config;
 
@@ -193,9 +195,10 @@ int bcfd_max_divergence(bcfd_handle h, double* out);
  * FP64 Poisson residual of the last solve in divergence units (the divergence
  * the correction leaves wherever the operators are consistent) */
 int bcfd_block_get_divergence(bcfd_handle h, double* out);
-/* mixed-precision solve parameters of a block: FP32 sweeps per correction and
- * their relaxation factor (0 selects the defaults) */
-int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega);
+/* mixed-precision solve parameters of a block: FP32 sweeps per correction,
+ * their relaxation factor (0 selects the defaults) and the kernel variant
+ * (0: cluster-resident when the block fits in one 16-CTA cluster, 1: grid-wide) */
+int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant);
 
 /* ---- measurement window (no counterpart in the reference) ----------------- */
 typedef struct bcfd_profile_report {

@@ -85,6 +85,7 @@ _SIGS = {
     "bcfd_coarse_update_newv": [], "bcfd_coarse_update_pc": [],
     "bcfd_fine_update_mv": [c_i64],
     "bcfd_stress_calculation": [c_i64, c_double, c_double, P_d],
+    "bcfd_stress_calculation_noalloc": [c_i64, c_double, c_double, P_d],
     "bcfd_run_steps": [C.POINTER(StepConfig), c_i64],
     "bcfd_max_divergence": [c_i64, P_d],
 }

@@ -990,4 +990,12 @@ int bcfd_stress_calculation(bcfd_handle h, double mu_f, double rho_f, double* ou
   return take_block_error(hb);
 }
 
+int bcfd_stress_calculation_noalloc(bcfd_handle h, double mu_f, double rho_f, double* out) {
+  LOCK();
+  GETB(h);
+  if (!out) return BCFD_E_ARG;
+  TRY(launch_stress_noalloc(hb, mu_f, rho_f, out));
+  return take_block_error(hb);
+}
+
 }  // extern "C"

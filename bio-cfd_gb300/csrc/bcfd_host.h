@@ -139,5 +139,6 @@ int launch_restrict(HostInterface* it, int comp, int which);
 int launch_fine_update_mv(HostInterface* it);
 // k_stress.cu
 int launch_stress(HostBlock* hb, double mu_f, double rho_f, double* out_host);
+int launch_stress_noalloc(HostBlock* hb, double mu_f, double rho_f, double* out_host);
 
 }  // namespace bcfd

@@ -4,6 +4,8 @@
 // tree order, so the result is deterministic run to run (the reference's
 // OpenACC reduction order is unspecified; its serial build sums in element
 // order).
+#include <cstdio>
+
 #include "bcfd_host.h"
 
 namespace bcfd {
@@ -152,6 +154,66 @@ int launch_stress(HostBlock* hb, double mu_f, double rho_f, double* out_host) {
   cudaFree(part);
   cudaFree(out);
   return r;
+}
+
+// ---- allocation-free variant ------------------------------------------------
+// The same two kernels, with the per-element partials and the 4 coefficients
+// in a fixed device array of this translation unit instead of cudaMalloc'd
+// memory.  Nothing in it has to start at zero: k_stress_elem writes all
+// 7 * ne partials that k_stress_sum reads, and k_stress_sum writes out[0..3].
+// There is one array per device, so two calls that overlap on one device would
+// race on it; launch_stress_noalloc runs under the library lock on the library
+// stream and synchronises before returning, so calls through it never overlap.
+namespace {
+constexpr int kStressNoallocMaxElems = BCFD_STRESS_NOALLOC_MAX_ELEMS;
+constexpr size_t kStressScratchDoubles = 7 * (size_t)kStressNoallocMaxElems + 4;
+static __device__ __align__(256) double g_stress_scratch[kStressScratchDoubles];
+constexpr int kMaxDevices = 64;
+double* g_stress_scratch_ptr[kMaxDevices] = {};
+}  // namespace
+
+// Set-up, once per device with that device current: the address of the
+// device array.  The first call on a device does this, so it should come
+// before any stream capture begins on that device.  The cached address is
+// valid while the device's primary context lives (the library never resets
+// the device).
+static int stress_scratch(double** out) {
+  int dev = -1;
+  BCFD_CUDA(cudaGetDevice(&dev));
+  // the library stream belongs to the device bcfd_init selected
+  if (dev != lib().device) return BCFD_E_STATE;
+  if (dev < 0 || dev >= kMaxDevices) return BCFD_E_ARG;
+  if (!g_stress_scratch_ptr[dev]) {
+    void* p = nullptr;
+    BCFD_CUDA(cudaGetSymbolAddress(&p, g_stress_scratch));
+    if (!p) return BCFD_E_CUDA;
+    g_stress_scratch_ptr[dev] = (double*)p;
+  }
+  *out = g_stress_scratch_ptr[dev];
+  return 0;
+}
+
+int launch_stress_noalloc(HostBlock* hb, double mu_f, double rho_f, double* out_host) {
+  const int ne = hb->d.ne;
+  if (ne <= 0) return BCFD_E_STATE;
+  if (ne > kStressNoallocMaxElems) {
+    std::fprintf(stderr,
+                 "bcfd_stress_calculation_noalloc: block has %d surface elements, more than the "
+                 "%d its fixed device scratch holds (use bcfd_stress_calculation)\n",
+                 ne, kStressNoallocMaxElems);
+    return BCFD_E_CAPACITY;
+  }
+  double* scratch = nullptr;
+  TRY_R(stress_scratch(&scratch));
+  double* part = scratch;
+  double* out = scratch + 7 * (size_t)kStressNoallocMaxElems;
+  k_stress_elem<<<grid_for(ne, 128), 128, 0, stream()>>>(hb->d, mu_f, rho_f, part);
+  TRY_R(note_launch());
+  k_stress_sum<<<1, 256, 0, stream()>>>(part, ne, out);
+  TRY_R(note_launch());
+  BCFD_CUDA(cudaMemcpyAsync(out_host, out, 4 * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+  BCFD_CUDA(cudaStreamSynchronize(stream()));
+  return 0;
 }
 
 }  // namespace bcfd

@@ -168,6 +168,21 @@ int bcfd_fine_update_mv(bcfd_handle it);       /* src/FineInterp.f90:10-281     
 /* ---- drag / lift (src/StressCalc.f90:14-208, FP64, deterministic order) --- */
 /* out[4] = viscous drag, pressure drag, viscous lift, pressure lift coefficients */
 int bcfd_stress_calculation(bcfd_handle h, double mu_f, double rho_f, double* out);
+/* The same computation and result without any device allocation; this entry
+ * point has no counterpart in the reference.  bcfd_stress_calculation
+ * cudaMallocs and cudaFrees its scratch on every call, and cudaFree waits for
+ * the whole device, so a caller that samples drag/lift every step while other
+ * streams run, or one whose memory is held by a caching allocator, uses this
+ * instead.  Scratch is a fixed 7 * BCFD_STRESS_NOALLOC_MAX_ELEMS + 4 doubles
+ * (1.8 MB) per device inside the library; nothing in it has to start at zero.
+ * A block with more than BCFD_STRESS_NOALLOC_MAX_ELEMS surface elements
+ * returns BCFD_E_CAPACITY.  The first call on a device does set-up (looks up
+ * the scratch address), so make it before any stream capture begins.  Calls
+ * through the library are serialised and synchronise before returning; two
+ * calls overlapping on one device by any other route would race on the
+ * scratch. */
+#define BCFD_STRESS_NOALLOC_MAX_ELEMS 32768
+int bcfd_stress_calculation_noalloc(bcfd_handle h, double mu_f, double rho_f, double* out);
 
 /* ---- whole time step (the phase order of app/main.F90:129-265) ----------- */
 typedef struct bcfd_step_config {

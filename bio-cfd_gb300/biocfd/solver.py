@@ -219,6 +219,10 @@ class Solver:
         check(self.L.bcfd_block_get_divergence(g, _pd(d)), "get_divergence")
         return float(d[0]), float(d[1])
 
+    def set_solve_launch(self, threads: int = 0, ctas_per_sm: int = 0, fp64_sync: int = 0, block: int = None):
+        for g in (self.handles if block is None else [self.handles[block]]):
+            check(self.L.bcfd_block_set_solve_launch(g, threads, ctas_per_sm, fp64_sync), "set_solve_launch")
+
     def set_mixed_params(self, inner: int = 0, omega: float = 0.0, variant: int = 0, block: int = None):
         for g in (self.handles if block is None else [block]):
             check(self.L.bcfd_block_set_mixed_params(g, inner, omega, variant), "set_mixed_params")

@@ -551,6 +551,7 @@ int bcfd_block_create(int64_t nx, int64_t ny, int64_t nz, const double* x1, cons
   A(&D.scratch, 64);
   A(&D.stats, 1);
   A(&hb->bar, 2);
+  A(&hb->prog, (size_t)kMaxTiles * kTileStride);
   if (r) {
     for (void* p : hb->allocs) cudaFree(p);
     delete hb;
@@ -925,10 +926,22 @@ int bcfd_block_get_divergence(bcfd_handle h, double* out) {
   return 0;
 }
 
+int bcfd_block_set_solve_launch(bcfd_handle h, int threads, int ctas_per_sm, int fp64_sync) {
+  LOCK();
+  GETB(h);
+  if (!(threads == 0 || threads == 128 || threads == 256 || threads == 512) ||
+      ctas_per_sm < 0 || ctas_per_sm > 16 || fp64_sync < 0 || fp64_sync > 1)
+    return BCFD_E_ARG;
+  hb->solve_threads = threads;
+  hb->solve_ctas_per_sm = ctas_per_sm;
+  hb->solve_sync = fp64_sync;
+  return 0;
+}
+
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant) {
   LOCK();
   GETB(h);
-  if (inner_sweeps < 0 || inner_sweeps > 100000 || omega < 0.0 || omega >= 2.0 || variant < 0 || variant > 1)
+  if (inner_sweeps < 0 || inner_sweeps > 100000 || omega < 0.0 || omega >= 2.0 || variant < 0 || variant > 3)
     return BCFD_E_ARG;
   hb->dc_inner = (int)inner_sweeps;
   hb->dc_omega = omega;

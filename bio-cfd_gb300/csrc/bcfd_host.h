@@ -32,12 +32,16 @@ struct HostBlock {
   int surf_cap_e = 0, surf_cap_n = 0;
   // per-block barrier words for persistent kernels: [count, gen]
   unsigned* bar = nullptr;
+  unsigned* prog = nullptr;        // per-tile phase counters of the tiled solves
   // mixed-precision solve: FP32 sweeps per correction and their relaxation
   // (0 = defaults chosen from the block size)
   int dc_inner = 0;
   double dc_omega = 0.0;
   // mixed solve kernel: 0 = cluster-resident when the block fits, 1 = grid-wide
   int dc_variant = 0;
+  int solve_threads = 0;           // threads per CTA of the tiled solves (0: 256)
+  int solve_ctas_per_sm = 0;       // co-resident CTAs per SM cap (0: occupancy limit)
+  int solve_sync = 0;              // FP64 solve: 0 point-to-point, 1 grid-wide phase barriers
   // largest distance of a surface node from the block centre (for the FP32
   // prefilter bound of the nearest-element search)
   double node_rmax = 0.0;

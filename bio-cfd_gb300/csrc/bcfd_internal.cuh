@@ -135,7 +135,7 @@ struct BlockStats {
   int64_t niter;
   double derr2;
   double derr_std_st;
-  double slot[2];       // running max |pc - pco| of the SOR stop test
+  double slot[3];       // rotating running maxima of the SOR stop test
   double maxdiv;        // max |div u| (diagnostics and the mixed-precision stop)
   double pad[2];
 };
@@ -145,6 +145,10 @@ enum CountSlot { C_IB = 0, C_SOLID, C_FLUID, C_RED, C_BLACK, C_TS, N_COUNT };
 // entries of the solve log of a measurement window ({sweeps, residual
 // passes, fluid cells, precision} each, after one counter word)
 constexpr unsigned long long kProfLogCap = 4096;
+// most CTAs (tiles) of a tiled persistent solve; each tile's phase counter
+// sits on its own 128-byte line (kTileStride unsigned words apart)
+constexpr unsigned kMaxTiles = 4096;
+constexpr unsigned kTileStride = 32;
 enum GhostSlot { G_P = 0, G_PT, G_U2, G_U2T, G_V2, G_V2T, G_W2, G_W2T, G_U1, G_U1T, G_V1, G_V1T, G_W1, G_W1T };
 enum NelSlot { N_P = 0, N_U1, N_U2, N_V1, N_V2, N_W1, N_W2 };
 
@@ -154,12 +158,16 @@ __device__ inline void set_err(int* err, int code) { atomicCAS(err, 0, code); }
 // ---------------------------------------------------------------------------
 // bounded grid-wide barrier for cooperative persistent kernels
 // ---------------------------------------------------------------------------
+// Software grid barrier of a cooperative launch: one monotonic 64-bit arrival
+// counter (zeroed before the launch).  The k-th barrier completes when the
+// counter reaches k * nblocks; bit 63 set means "abandon": a CTA that gave up
+// (timeout or a recorded error) sets it so every waiter leaves at once.
 struct GridBar {
-  unsigned int* count;
-  unsigned int* gen;
+  unsigned long long* ctr;
   int* err;          // set to BCFD_E_TIMEOUT when a wait exceeds the limit
   unsigned nblocks;
 };
+constexpr unsigned long long kBarAbandon = 1ull << 63;
 
 __device__ inline unsigned long long globaltimer_ns() {
   unsigned long long t;
@@ -171,6 +179,27 @@ __device__ inline unsigned ld_acquire(const unsigned* p) {
   asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
   return v;
 }
+__device__ inline unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+// relaxed (L1-bypassing, no cache invalidation) loads for polling; an
+// acquire fence after the poll succeeds completes the acquire pattern
+__device__ inline unsigned ld_relaxed(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline void st_relaxed(unsigned* p, unsigned v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ inline void fence_acq_rel_gpu() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ inline void st_release(unsigned* p, unsigned v) {
   asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
@@ -182,37 +211,42 @@ __device__ inline int ld_acquire_i(const int* p) {
 
 constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // 2 s per wait
 
-// Returns false (on every thread of the CTA) once any CTA has recorded an
-// error; the caller then leaves its loops and returns.
+// Returns false (on every thread of the CTA) once the barrier was abandoned:
+// a wait timed out somewhere, or a CTA saw a recorded error while waiting.
+// The caller then leaves its loops and returns.
 __device__ inline bool grid_sync(const GridBar& gb) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
-    const unsigned my_gen = ld_acquire(gb.gen);
     __threadfence();
-    const unsigned arrived = atomicAdd(gb.count, 1u);
-    if (arrived == gb.nblocks - 1) {
-      *gb.count = 0;
-      __threadfence();
-      st_release(gb.gen, my_gen + 1);
+    const unsigned long long old = atomicAdd(gb.ctr, 1ull);
+    if (old & kBarAbandon) {
+      ok = 0;
     } else {
+      const unsigned long long target = (old / gb.nblocks + 1) * gb.nblocks;
       const unsigned long long t0 = globaltimer_ns();
       unsigned spins = 0;
-      while (ld_acquire(gb.gen) == my_gen) {
+      for (;;) {
+        const unsigned long long v = ld_acquire_u64(gb.ctr);
+        if (v & kBarAbandon) { ok = 0; break; }
+        if (v >= target) break;
         if (((++spins) & 63u) == 0) {
-          if (ld_acquire_i(gb.err) != 0) { ok = 0; break; }
+          if (ld_acquire_i(gb.err) != 0) {
+            atomicOr(gb.ctr, kBarAbandon);
+            ok = 0;
+            break;
+          }
           if (globaltimer_ns() - t0 > kBarrierLimitNs) {
             atomicCAS(gb.err, 0, BCFD_E_TIMEOUT);
+            atomicOr(gb.ctr, kBarAbandon);
             ok = 0;
             break;
           }
         }
-        __nanosleep(32);
       }
       __threadfence();
     }
-    if (ok && ld_acquire_i(gb.err) != 0) ok = 0;
     s_ok = ok;
   }
   __syncthreads();

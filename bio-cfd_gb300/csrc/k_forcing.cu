@@ -464,8 +464,7 @@ static int launch_dag(HostBlock* hb, int mode, int vel) {
   const unsigned want = (unsigned)((6 * (int64_t)hb->d.cap_ib + threads - 1) / threads);
   const unsigned grid = coop_grid((const void*)k_forcing_dag, threads, 0, std::min(want, 2u * (unsigned)num_sms()));
   GridBar gb = make_bar(hb->d.err, grid);
-  gb.count = hb->bar;
-  gb.gen = hb->bar + 1;
+  gb.ctr = reinterpret_cast<unsigned long long*>(hb->bar);
   DagArgs g{mode, vel};
   DevBlock B = hb->d;
   void* args[] = {(void*)&B, (void*)&g, (void*)&s, (void*)&gb};

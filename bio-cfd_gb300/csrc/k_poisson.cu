@@ -58,48 +58,238 @@ __global__ void k_rhs(DevBlock B, double dt) {
   }
 }
 
-// One half-sweep of colour C, FP64, reference arithmetic (no FMA; the
-// expression order of src/PcorVcor.F90:319-327).
+// ---------------------------------------------------------------------------
+// Tiled persistent solves.  Each CTA of a cooperative launch owns one 2-D
+// tile of interior rows (j in [j0, j0+nj), k in [k0, k0+nk), every h of both
+// colours).  A red-black half-sweep reads the other colour only at face
+// neighbours, so instead of a grid-wide barrier between half-sweeps each CTA
+// waits for the (at most four) CTAs owning the face-adjacent tiles: every
+// phase (half-sweep, residual pass, correction) ends with the CTA publishing
+// its count of completed phases, and a phase starts once the neighbours have
+// completed as many phases as this CTA.  That orders both the reads of the
+// neighbours' previous-phase values and the overwrite of values they read in
+// that phase, so every cell sees exactly the values a grid-wide barrier
+// would give it.  Grid-wide barriers remain only where a global max is taken.
+// With `global` set, every phase boundary is a grid-wide barrier instead
+// (fewer round trips per phase when a phase is only ~1 cell per thread).
+// ---------------------------------------------------------------------------
+// largest CTA of the tiled solves (the two-cell loops want ~70 registers)
+constexpr int kSolveMaxThreads = 512;
+
+struct TileMap {
+  int tj, tk;      // rows per tile along j and k
+  int ntj, ntk;    // tiles along j and k (gridDim.x == ntj * ntk)
+  unsigned* prog;  // completed-phase count per tile, zeroed before the launch
+  int global;      // 1: phase boundaries are grid-wide barriers
+};
+
+struct Tile {
+  int j0, nj, k0, nk;  // first interior row and row counts of this CTA's tile
+  int a, b;            // tile coordinates
+};
+
+__device__ __forceinline__ Tile my_tile(const Dims& d, const TileMap& tm) {
+  Tile t;
+  t.a = blockIdx.x % tm.ntj;
+  t.b = blockIdx.x / tm.ntj;
+  t.j0 = 2 + t.a * tm.tj;
+  t.k0 = 2 + t.b * tm.tk;
+  t.nj = min(tm.tj, d.ny + 2 - t.j0);
+  t.nk = min(tm.tk, d.nz + 2 - t.k0);
+  return t;
+}
+
+// publish `done` completed phases of this CTA, after all its threads' writes
+__device__ __forceinline__ void tile_publish(const TileMap& tm, const Tile& t, unsigned done) {
+  if (tm.global) return;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    fence_acq_rel_gpu();
+    st_relaxed(tm.prog + kTileStride * (t.a + tm.ntj * t.b), done);
+  }
+}
+
+// wait until the face-neighbour tiles have completed `need` phases (lanes 0-3
+// of warp 0 poll one neighbour each); false once the launch was abandoned
+__device__ __forceinline__ bool tile_wait(const TileMap& tm, const GridBar& gb, const Tile& t,
+                                          unsigned need) {
+  if (tm.global) return need == 0 ? true : grid_sync(gb);
+  __shared__ int s_ok;
+  if (threadIdx.x < 32) {
+    const int q = threadIdx.x;
+    int na = t.a, nb = t.b;
+    bool have = false;
+    if (q == 0 && t.a > 0) { na = t.a - 1; have = true; }
+    else if (q == 1 && t.a + 1 < tm.ntj) { na = t.a + 1; have = true; }
+    else if (q == 2 && t.b > 0) { nb = t.b - 1; have = true; }
+    else if (q == 3 && t.b + 1 < tm.ntk) { nb = t.b + 1; have = true; }
+    int ok = 1;
+    if (have) {
+      const unsigned* f = tm.prog + kTileStride * (na + tm.ntj * nb);
+      const unsigned long long t0 = globaltimer_ns();
+      unsigned spins = 0;
+      while (ld_relaxed(f) < need) {
+        if (((++spins) & 63u) == 0) {
+          if ((ld_relaxed_u64(gb.ctr) & kBarAbandon) || ld_acquire_i(gb.err) != 0) {
+            atomicOr(gb.ctr, kBarAbandon);
+            ok = 0;
+            break;
+          }
+          if (globaltimer_ns() - t0 > kBarrierLimitNs) {
+            atomicCAS(gb.err, 0, BCFD_E_TIMEOUT);
+            atomicOr(gb.ctr, kBarAbandon);
+            ok = 0;
+            break;
+          }
+        }
+      }
+      fence_acq_rel_gpu();
+    }
+    ok = __all_sync(0xffffffffu, ok);
+    if (q == 0) s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// walk over this CTA's tile, packed positions of one colour (h fastest), two
+// positions per pass (q and q + blockDim.x) so that the loads of both cells
+// are in flight together: a half-sweep of a small block is latency-bound
+#define FOR_TILE2(t_)                                              \
+  const int _n = B.d.NXH * (t_).nj * (t_).nk;                      \
+  const int _bd = blockDim.x;                                      \
+  Walk3 _wa, _wb;                                                  \
+  _wa.init(threadIdx.x, 2 * _bd, B.d.NXH, (t_).nj);                \
+  _wb.init(threadIdx.x + _bd, 2 * _bd, B.d.NXH, (t_).nj);          \
+  for (int _q = threadIdx.x; _q < _n; _q += 2 * _bd, _wa.next(), _wb.next())
+
+// A tile position of colour C: packed index, row start, cell indices and
+// whether the cell is updated.  A position past the tile end maps onto the
+// tile's first row (addresses in range, never updated).  `ic` is i clamped to
+// the interior for the coefficient tables (cells that are not updated may sit
+// at i = 1 or nx + 2); every neighbour address of a tile row is in range.
+struct Pos {
+  int64_t pi, row;
+  int i, ic, j, k;
+  bool on;
+};
+
 template <int C>
-__device__ __forceinline__ void half_sweep64(const DevBlock& B, const RowMap& rm, int64_t total,
-                                             double omega, double& lmax) {
+__device__ __forceinline__ Pos tile_pos(const DevBlock& B, const Tile& t, const Walk3& w, bool valid) {
+  Pos p;
+  const int h = valid ? w.a : 0;
+  p.j = valid ? t.j0 + w.b : t.j0;
+  p.k = valid ? t.k0 + w.c : t.k0;
+  p.row = (int64_t)B.d.NXH * (p.j - 1) + (int64_t)B.d.NXH * B.d.NY * (p.k - 1);
+  p.pi = p.row + h;
+  p.i = 2 * h + 1 + ((((2 * h + 1) + p.j + p.k) & 1) != C);
+  p.ic = min(max(p.i, 2), B.d.nx + 1);
+  p.on = valid && B.upd[C][p.pi] != 0;
+  return p;
+}
+
+// reference SOR update of one FP64 cell (no FMA; the expression order of
+// src/PcorVcor.F90:319-327); `old` returns the previous value
+template <int C>
+__device__ __forceinline__ double sor64_cell(const DevBlock& B, const Pos& p, double omega, double& old) {
   const Dims& d = B.d;
   const double* __restrict__ o = B.pc[1 - C];
-  double* __restrict__ own = B.pc[C];
-  const double* __restrict__ rhs = B.rhs[C];
-  const uint8_t* __restrict__ upd = B.upd[C];
-  const int nx = d.nx, ny = d.ny, nz = d.nz;
   const int64_t sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
-  const int S = gridDim.x * blockDim.x;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = p.ic, j = p.j, k = p.k, nx = d.nx, ny = d.ny, nz = d.nz;
+  // values written by other CTAs in this launch: read through L2 (ld.cg)
+  const double pl = __ldcg(o + p.row + ((p.i - 2) >> 1));
+  const double pr = __ldcg(o + p.row + (p.i >> 1));
+  const double ps = __ldcg(o + p.pi - sy), pn = __ldcg(o + p.pi + sy);
+  const double pb = __ldcg(o + p.pi - sz), pt = __ldcg(o + p.pi + sz);
+  old = __ldcg(B.pc[C] + p.pi);
+  const double ax1 = B.Acx[i - 2], ax2 = B.Acx[i - 2 + nx], ax3 = B.Acx[i - 2 + 2 * nx];
+  const double ay1 = B.Acy[j - 2], ay2 = B.Acy[j - 2 + ny], ay3 = B.Acy[j - 2 + 2 * ny];
+  const double az1 = B.Acz[k - 2], az2 = B.Acz[k - 2 + nz], az3 = B.Acz[k - 2 + 2 * nz];
+  double v = B.rhs[C][p.pi] - ax1 * pl - ax3 * pr - ay1 * ps - ay3 * pn - az1 * pb - az3 * pt;
+  v = v / (ax2 + ay2 + az2);
+  return (1.0 - omega) * old + omega * v;
+}
+
+// One half-sweep of colour C over the tile, FP64, reference arithmetic; one
+// cell per pass (the FP64 sweep is bound by the FP64 divide, and the lower
+// register count keeps two CTAs of 512 threads per SM)
+template <int C>
+__device__ __forceinline__ void tile_half64(const DevBlock& B, const Tile& t, double omega, double& lmax) {
+  double* __restrict__ own = B.pc[C];
+  const int n = B.d.NXH * t.nj * t.nk;
   Walk3 w;
-  w.init(t, S, d.NXH, d.ny);
-  for (; t < (int)total; t += S, w.next()) {
-    const int h = w.a, j = 2 + w.b, k = 2 + w.c;
-    const int64_t pi = h + sy * (j - 1) + sz * (k - 1);
-    if (!upd[pi]) continue;
-    int i = 2 * h + 1;
-    if (((i + j + k) & 1) != C) ++i;
-    const int64_t row = sy * (j - 1) + sz * (k - 1);
-    // values written by other CTAs in this launch: read through L2 (ld.cg)
-    const double pl = __ldcg(o + row + ((i - 2) >> 1));
-    const double pr = __ldcg(o + row + (i >> 1));
-    const double ps = __ldcg(o + pi - sy), pn = __ldcg(o + pi + sy);
-    const double pb = __ldcg(o + pi - sz), pt = __ldcg(o + pi + sz);
-    const double old = __ldcg(own + pi);
-    const double ax1 = B.Acx[i - 2], ax2 = B.Acx[i - 2 + nx], ax3 = B.Acx[i - 2 + 2 * nx];
-    const double ay1 = B.Acy[j - 2], ay2 = B.Acy[j - 2 + ny], ay3 = B.Acy[j - 2 + 2 * ny];
-    const double az1 = B.Acz[k - 2], az2 = B.Acz[k - 2 + nz], az3 = B.Acz[k - 2 + 2 * nz];
-    double v = rhs[pi] - ax1 * pl - ax3 * pr - ay1 * ps - ay3 * pn - az1 * pb - az3 * pt;
-    v = v / (ax2 + ay2 + az2);
-    const double nv = (1.0 - omega) * old + omega * v;
-    own[pi] = nv;
+  w.init(threadIdx.x, blockDim.x, B.d.NXH, t.nj);
+  for (int q = threadIdx.x; q < n; q += blockDim.x, w.next()) {
+    const Pos p = tile_pos<C>(B, t, w, true);
+    if (!p.on) continue;
+    double old;
+    const double nv = sor64_cell<C>(B, p, omega, old);
+    own[p.pi] = nv;
     lmax = fmax(lmax, fabs(nv - old));
   }
 }
 
-// max over fluid cells of colour C of |b/dt - A pc| (FP64, FMA allowed: this
-// is a stop test of the residual-target mode, not reference arithmetic)
+// FP64 residual b/dt - A pc of one cell of colour C (FMA allowed: a stop test
+// and correction source, not reference arithmetic)
+template <int C>
+__device__ __forceinline__ double resid64_cell(const DevBlock& B, const Pos& p) {
+  const Dims& d = B.d;
+  const double* __restrict__ own = B.pc[C];
+  const double* __restrict__ o = B.pc[1 - C];
+  const int64_t sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
+  const int i = p.ic, j = p.j, k = p.k;
+  const double ax1 = B.Acx[i - 2], ax2 = B.Acx[i - 2 + d.nx], ax3 = B.Acx[i - 2 + 2 * d.nx];
+  const double ay1 = B.Acy[j - 2], ay2 = B.Acy[j - 2 + d.ny], ay3 = B.Acy[j - 2 + 2 * d.ny];
+  const double az1 = B.Acz[k - 2], az2 = B.Acz[k - 2 + d.nz], az3 = B.Acz[k - 2 + 2 * d.nz];
+  double ax = (ax2 + ay2 + az2) * __ldcg(own + p.pi);
+  ax = fma(ax1, __ldcg(o + p.row + ((p.i - 2) >> 1)), ax);
+  ax = fma(ax3, __ldcg(o + p.row + (p.i >> 1)), ax);
+  ax = fma(ay1, __ldcg(o + p.pi - sy), ax);
+  ax = fma(ay3, __ldcg(o + p.pi + sy), ax);
+  ax = fma(az1, __ldcg(o + p.pi - sz), ax);
+  ax = fma(az3, __ldcg(o + p.pi + sz), ax);
+  return B.rhs[C][p.pi] - ax;
+}
+
+// max |residual| of colour C over the tile, one cell per pass (the stop test
+// of the FP64 residual-target solve)
+template <int C>
+__device__ __forceinline__ double tile_resid_max64(const DevBlock& B, const Tile& t) {
+  double m = 0.0;
+  const int n = B.d.NXH * t.nj * t.nk;
+  Walk3 w;
+  w.init(threadIdx.x, blockDim.x, B.d.NXH, t.nj);
+  for (int q = threadIdx.x; q < n; q += blockDim.x, w.next()) {
+    const Pos p = tile_pos<C>(B, t, w, true);
+    if (p.on) m = fmax(m, fabs(resid64_cell<C>(B, p)));
+  }
+  return m;
+}
+
+// residual of colour C over the tile; if `store`, written to rhsf as the FP32
+// right-hand side of the correction.  Returns the local max |r|.
+template <int C, bool store>
+__device__ __forceinline__ double tile_residual64(const DevBlock& B, const Tile& t) {
+  double m = 0.0;
+  FOR_TILE2(t) {
+    const Pos pa = tile_pos<C>(B, t, _wa, true);
+    const Pos pb = tile_pos<C>(B, t, _wb, _q + _bd < _n);
+    if (!pa.on && !pb.on) continue;
+    const double ra = resid64_cell<C>(B, pa);
+    const double rb = resid64_cell<C>(B, pb);
+    if (pa.on) {
+      if (store) B.rhsf[C][pa.pi] = (float)ra;
+      m = fmax(m, fabs(ra));
+    }
+    if (pb.on) {
+      if (store) B.rhsf[C][pb.pi] = (float)rb;
+      m = fmax(m, fabs(rb));
+    }
+  }
+  return m;
+}
+
+// max over fluid cells of colour C of |b/dt - A pc| (grid-stride; measurement)
 template <int C>
 __device__ __forceinline__ double resid_max64(const DevBlock& B, const RowMap& rm, int64_t total) {
   const Dims& d = B.d;
@@ -153,46 +343,60 @@ __device__ __forceinline__ void log_solve(int64_t* log, int64_t sweeps, int64_t 
   }
 }
 
+// The three stop-test slots rotate: slot c % 3 collects check c; after the
+// grid barrier of check c every CTA has read check c-1, so slot (c+2) % 3 is
+// cleared for check c+2 by CTA 0.
+__device__ __forceinline__ double take_slot(BlockStats* st, int c) {
+  const double v = *((volatile double*)&st->slot[c % 3]);
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->slot[(c + 2) % 3] = 0.0;
+  return v;
+}
+
 // REDBLACKSOR_linear (src/PcorVcor.F90:288-377) as one cooperative launch.
 // nIterPcor continues from stats->niter (the fine blocks accumulate it over
 // two solves per step, :78, :98, :116) and the stop test runs whenever the
 // accumulated count is a multiple of 5, exactly as the reference does.
-__global__ void __launch_bounds__(256) k_sor64(DevBlock B, SorArgs a, GridBar gb) {
+__global__ void __launch_bounds__(kSolveMaxThreads, 2) k_sor64(DevBlock B, SorArgs a, GridBar gb, TileMap tm) {
   __shared__ double sh[32];
-  const RowMap rm{B.d.NXH, B.d.ny};
-  const int64_t total = (int64_t)B.d.NXH * B.d.ny * B.d.nz;
+  const Tile t = my_tile(B.d, tm);
   BlockStats* st = B.stats;
-  int64_t it = st->niter;
+  const int64_t it0 = st->niter;
+  // every CTA has read niter before CTA 0 may rewrite it at the end
+  if (!grid_sync(gb)) return;
+  int64_t it = it0;
+  int r5 = (int)(it0 % 5);  // it mod 5, kept incrementally
   double derr4 = 11111.0;
   int check = 0;
+  unsigned ph = 0;
   bool ok = true;
   for (;;) {
     ++it;
+    if (++r5 == 5) r5 = 0;
     double lmax = 0.0;
-    half_sweep64<1>(B, rm, total, a.omega, lmax);
-    if (!grid_sync(gb)) { ok = false; break; }
-    half_sweep64<0>(B, rm, total, a.omega, lmax);
-    const bool chk = (it % 5) == 0;
-    if (chk && a.res_tol > 0.0) {
-      // residual-target mode: the residual needs the whole sweep pair done
-      if (!grid_sync(gb)) { ok = false; break; }
-      lmax = fmax(resid_max64<1>(B, rm, total), resid_max64<0>(B, rm, total)) * a.dt;
-    }
-    if (chk) {
+    if (!tile_wait(tm, gb, t, ph)) { ok = false; break; }
+    tile_half64<1>(B, t, a.omega, lmax);
+    tile_publish(tm, t, ++ph);
+    if (!tile_wait(tm, gb, t, ph)) { ok = false; break; }
+    tile_half64<0>(B, t, a.omega, lmax);
+    tile_publish(tm, t, ++ph);
+    if (r5 == 0) {
+      if (a.res_tol > 0.0) {
+        // residual-target mode: the residual needs the neighbours' sweep pair
+        if (!tile_wait(tm, gb, t, ph)) { ok = false; break; }
+        lmax = fmax(tile_resid_max64<1>(B, t), tile_resid_max64<0>(B, t)) * a.dt;
+        tile_publish(tm, t, ++ph);
+      }
       const double m = block_max(lmax, sh);
-      if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[check & 1], m);
-    }
-    if (!grid_sync(gb)) { ok = false; break; }
-    if (chk) {
-      derr4 = *((volatile double*)&st->slot[check & 1]);
-      if (blockIdx.x == 0 && threadIdx.x == 0) st->slot[(check + 1) & 1] = 0.0;
+      if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[check % 3], m);
+      if (!grid_sync(gb)) { ok = false; break; }
+      derr4 = take_slot(st, check);
       ++check;
     }
     if (a.res_tol > 0.0 ? (derr4 <= a.res_tol) : (derr4 < a.epsi)) break;
     if (it > a.itmax) break;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
-    log_solve(a.log, it - st->niter, 0, B.cnt[C_FLUID], 0);
+    log_solve(a.log, it - it0, 0, B.cnt[C_FLUID], 0);
     st->niter = it;
     st->derr2 = derr4;
     if (ok && !(derr4 == derr4)) set_err(B.err, BCFD_E_NONFINITE);
@@ -215,113 +419,91 @@ struct DcArgs {
   int64_t* log;
 };
 
-// grid-stride walk over the interior packed positions of colour C: h, j, k,
-// the cell's i and its packed index pi
-#define FOR_PACKED(C_, total_)                                  \
-  const int _S = gridDim.x * blockDim.x;                        \
-  int _t = blockIdx.x * blockDim.x + threadIdx.x;               \
-  Walk3 _w;                                                     \
-  _w.init(_t, _S, B.d.NXH, B.d.ny);                             \
-  for (; _t < (int)(total_); _t += _S, _w.next())
-#define PACKED_CELL(C_)                                                                   \
-  const int h = _w.a, j = 2 + _w.b, k = 2 + _w.c;                                         \
-  const int64_t pi = h + (int64_t)B.d.NXH * (j - 1) + (int64_t)B.d.NXH * B.d.NY * (k - 1); \
-  const int i = 2 * h + 1 + ((((2 * h + 1) + j + k) & 1) != (C_))
-
-// FP64 residual of colour C into rhsf[C]; returns the local max |r|
+// FP32 SOR update of one cell of colour C on the correction e (pcf)
 template <int C>
-__device__ __forceinline__ double residual64(const DevBlock& B, int64_t total) {
-  const Dims& d = B.d;
-  const double* __restrict__ own = B.pc[C];
-  const double* __restrict__ o = B.pc[1 - C];
-  const int64_t sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
-  double m = 0.0;
-  FOR_PACKED(C, total) {
-    PACKED_CELL(C);
-    if (!B.upd[C][pi]) continue;
-    const int64_t row = pi - (i - 1) / 2;
-    const double ax1 = B.Acx[i - 2], ax2 = B.Acx[i - 2 + d.nx], ax3 = B.Acx[i - 2 + 2 * d.nx];
-    const double ay1 = B.Acy[j - 2], ay2 = B.Acy[j - 2 + d.ny], ay3 = B.Acy[j - 2 + 2 * d.ny];
-    const double az1 = B.Acz[k - 2], az2 = B.Acz[k - 2 + d.nz], az3 = B.Acz[k - 2 + 2 * d.nz];
-    double ax = (ax2 + ay2 + az2) * __ldcg(own + pi);
-    ax = fma(ax1, __ldcg(o + row + ((i - 2) >> 1)), ax);
-    ax = fma(ax3, __ldcg(o + row + (i >> 1)), ax);
-    ax = fma(ay1, __ldcg(o + pi - sy), ax);
-    ax = fma(ay3, __ldcg(o + pi + sy), ax);
-    ax = fma(az1, __ldcg(o + pi - sz), ax);
-    ax = fma(az3, __ldcg(o + pi + sz), ax);
-    const double r = B.rhs[C][pi] - ax;
-    B.rhsf[C][pi] = (float)r;
-    m = fmax(m, fabs(r));
-  }
-  return m;
-}
-
-// one FP32 half-sweep on the correction e (stored in pcf)
-template <int C>
-__device__ __forceinline__ void half_sweep32(const DevBlock& B, int64_t total, float omega) {
+__device__ __forceinline__ float sor32_cell(const DevBlock& B, const Pos& p, float omega) {
   const Dims& d = B.d;
   const float* __restrict__ o = B.pcf[1 - C];
-  float* __restrict__ own = B.pcf[C];
   const int64_t sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
-  FOR_PACKED(C, total) {
-    PACKED_CELL(C);
-    if (!B.upd[C][pi]) continue;
-    const int64_t row = pi - (i - 1) / 2;
-    const float ax1 = B.Acxf[i - 2], ax2 = B.Acxf[i - 2 + d.nx], ax3 = B.Acxf[i - 2 + 2 * d.nx];
-    const float ay1 = B.Acyf[j - 2], ay2 = B.Acyf[j - 2 + d.ny], ay3 = B.Acyf[j - 2 + 2 * d.ny];
-    const float az1 = B.Aczf[k - 2], az2 = B.Aczf[k - 2 + d.nz], az3 = B.Aczf[k - 2 + 2 * d.nz];
-    float s = B.rhsf[C][pi];
-    s = __fmaf_rn(-ax1, __ldcg(o + row + ((i - 2) >> 1)), s);
-    s = __fmaf_rn(-ax3, __ldcg(o + row + (i >> 1)), s);
-    s = __fmaf_rn(-ay1, __ldcg(o + pi - sy), s);
-    s = __fmaf_rn(-ay3, __ldcg(o + pi + sy), s);
-    s = __fmaf_rn(-az1, __ldcg(o + pi - sz), s);
-    s = __fmaf_rn(-az3, __ldcg(o + pi + sz), s);
-    const float old = __ldcg(own + pi);
-    const float nv = __fmaf_rn(omega, __fdividef(s, ax2 + ay2 + az2) - old, old);
-    own[pi] = nv;
-  }
+  const int i = p.ic, j = p.j, k = p.k;
+  const float ax1 = B.Acxf[i - 2], ax2 = B.Acxf[i - 2 + d.nx], ax3 = B.Acxf[i - 2 + 2 * d.nx];
+  const float ay1 = B.Acyf[j - 2], ay2 = B.Acyf[j - 2 + d.ny], ay3 = B.Acyf[j - 2 + 2 * d.ny];
+  const float az1 = B.Aczf[k - 2], az2 = B.Aczf[k - 2 + d.nz], az3 = B.Aczf[k - 2 + 2 * d.nz];
+  float s = B.rhsf[C][p.pi];
+  s = __fmaf_rn(-ax1, __ldcg(o + p.row + ((p.i - 2) >> 1)), s);
+  s = __fmaf_rn(-ax3, __ldcg(o + p.row + (p.i >> 1)), s);
+  s = __fmaf_rn(-ay1, __ldcg(o + p.pi - sy), s);
+  s = __fmaf_rn(-ay3, __ldcg(o + p.pi + sy), s);
+  s = __fmaf_rn(-az1, __ldcg(o + p.pi - sz), s);
+  s = __fmaf_rn(-az3, __ldcg(o + p.pi + sz), s);
+  const float old = B.pcf[C][p.pi];
+  return __fmaf_rn(omega, __fdividef(s, ax2 + ay2 + az2) - old, old);
 }
 
+// one FP32 half-sweep of colour C over the tile
 template <int C>
-__device__ __forceinline__ void apply_correction(const DevBlock& B, int64_t np) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < np;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    if (!B.upd[C][t]) continue;
-    B.pc[C][t] = B.pc[C][t] + (double)__ldcg(B.pcf[C] + t);
-    B.pcf[C][t] = 0.0f;
+__device__ __forceinline__ void tile_half32(const DevBlock& B, const Tile& t, float omega) {
+  float* __restrict__ own = B.pcf[C];
+  FOR_TILE2(t) {
+    const Pos pa = tile_pos<C>(B, t, _wa, true);
+    const Pos pb = tile_pos<C>(B, t, _wb, _q + _bd < _n);
+    if (!pa.on && !pb.on) continue;
+    const float na = sor32_cell<C>(B, pa, omega);
+    const float nb = sor32_cell<C>(B, pb, omega);
+    if (pa.on) own[pa.pi] = na;
+    if (pb.on) own[pb.pi] = nb;
   }
 }
 
-__global__ void __launch_bounds__(256) k_sor_dc(DevBlock B, DcArgs a, GridBar gb) {
+// x += e in FP64 over the tile's fluid cells of colour C; e back to 0
+template <int C>
+__device__ __forceinline__ void tile_apply(const DevBlock& B, const Tile& t) {
+  FOR_TILE2(t) {
+    const Pos pa = tile_pos<C>(B, t, _wa, true);
+    const Pos pb = tile_pos<C>(B, t, _wb, _q + _bd < _n);
+    const float ea = B.pcf[C][pa.pi], eb = B.pcf[C][pb.pi];
+    const double xa = B.pc[C][pa.pi], xb = B.pc[C][pb.pi];
+    if (pa.on) {
+      B.pc[C][pa.pi] = xa + (double)ea;
+      B.pcf[C][pa.pi] = 0.0f;
+    }
+    if (pb.on) {
+      B.pc[C][pb.pi] = xb + (double)eb;
+      B.pcf[C][pb.pi] = 0.0f;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSolveMaxThreads) k_sor_dc(DevBlock B, DcArgs a, GridBar gb, TileMap tm) {
   __shared__ double sh[32];
-  const RowMap rm{B.d.NXH, B.d.ny};
-  const int64_t total = (int64_t)B.d.NXH * B.d.ny * B.d.nz;
-  const int64_t np = B.d.npacked();
+  const Tile t = my_tile(B.d, tm);
   BlockStats* st = B.stats;
   int64_t sweeps = 0;
   double res = 0.0;
-  int64_t outer = 0;
+  unsigned ph = 0;
+  int outer = 0;
   for (;; ++outer) {
-    double m = residual64<1>(B, total);
-    m = fmax(m, residual64<0>(B, total));
+    if (!tile_wait(tm, gb, t, ph)) return;
+    double m = fmax(tile_residual64<1, true>(B, t), tile_residual64<0, true>(B, t));
+    tile_publish(tm, t, ++ph);
     m = block_max(m, sh);
-    if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[outer & 1], m);
+    if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[outer % 3], m);
     if (!grid_sync(gb)) return;
-    res = *((volatile double*)&st->slot[outer & 1]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) st->slot[(outer + 1) & 1] = 0.0;
+    res = take_slot(st, outer);
     if (a.dt * res <= a.div_tol || outer >= a.max_outer || !(res == res)) break;
     for (int it = 0; it < a.inner; ++it) {
-      half_sweep32<1>(B, total, a.omega);
-      if (!grid_sync(gb)) return;
-      half_sweep32<0>(B, total, a.omega);
-      if (!grid_sync(gb)) return;
+      if (!tile_wait(tm, gb, t, ph)) return;
+      tile_half32<1>(B, t, a.omega);
+      tile_publish(tm, t, ++ph);
+      if (!tile_wait(tm, gb, t, ph)) return;
+      tile_half32<0>(B, t, a.omega);
+      tile_publish(tm, t, ++ph);
     }
     sweeps += a.inner;
-    apply_correction<1>(B, np);
-    apply_correction<0>(B, np);
-    if (!grid_sync(gb)) return;
+    if (!tile_wait(tm, gb, t, ph)) return;
+    tile_apply<1>(B, t);
+    tile_apply<0>(B, t);
+    tile_publish(tm, t, ++ph);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     log_solve(a.log, sweeps, outer + 1, B.cnt[C_FLUID], 1);
@@ -515,23 +697,52 @@ static int launch_residual(HostBlock* hb, double dt) {
   return 0;
 }
 
+// Tiles for a tiled persistent solve: the smallest tiles (most CTAs) whose
+// count fits the co-resident capacity of `fn`, squarest among equal areas.
+static TileMap choose_tiles(HostBlock* hb, const void* fn, int threads, int global) {
+  const Dims& d = hb->d.d;
+  unsigned cap = coop_grid(fn, threads, 0, 0xffffffffu);
+  if (hb->solve_ctas_per_sm > 0) cap = std::min<unsigned>(cap, (unsigned)(hb->solve_ctas_per_sm * num_sms()));
+  cap = std::min<unsigned>(cap, kMaxTiles);
+  TileMap best{d.ny, d.nz, 1, 1, hb->prog, global};
+  long barea = (long)d.ny * d.nz, bper = d.ny + d.nz;
+  for (int tk = 1; tk <= d.nz; ++tk) {
+    const int ntk = (d.nz + tk - 1) / tk;
+    if ((unsigned)ntk > cap) continue;
+    const int maxntj = (int)(cap / (unsigned)ntk);
+    const int tj = (d.ny + maxntj - 1) / maxntj;
+    const int ntj = (d.ny + tj - 1) / tj;
+    const long area = (long)tj * tk, per = tj + tk;
+    if (area < barea || (area == barea && per < bper)) {
+      best = TileMap{tj, tk, ntj, ntk, hb->prog, global};
+      barea = area;
+      bper = per;
+    }
+  }
+  return best;
+}
+
+// zeroed progress counters, stop-test slots and barrier word for one launch
+static int reset_solve_state(HostBlock* hb, const TileMap& tm) {
+  BCFD_CUDA(cudaMemsetAsync(hb->prog, 0, (size_t)tm.ntj * tm.ntk * kTileStride * sizeof(unsigned), stream()));
+  BCFD_CUDA(cudaMemsetAsync(&hb->d.stats->slot[0], 0, 3 * sizeof(double), stream()));
+  BCFD_CUDA(cudaMemsetAsync(hb->bar, 0, 2 * sizeof(unsigned), stream()));
+  return 0;
+}
+
 int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol) {
   DevBlock& B = hb->d;
   const int64_t np = B.d.npacked();
   k_rhs<<<grid_for(np, 256), 256, 0, stream()>>>(B, dt);
   BCFD_LAUNCHED();
-  // fresh stop-test slots and barrier words for this launch
-  BCFD_CUDA(cudaMemsetAsync(&B.stats->slot[0], 0, 2 * sizeof(double), stream()));
-  BCFD_CUDA(cudaMemsetAsync(hb->bar, 0, 2 * sizeof(unsigned), stream()));
-  const int64_t total = (int64_t)B.d.NXH * B.d.ny * B.d.nz;
-  const int threads = 256;
-  unsigned want = (unsigned)((total + threads - 1) / threads);
-  const unsigned grid = coop_grid((const void*)k_sor64, threads, 0, want);
+  const int threads = hb->solve_threads > 0 ? hb->solve_threads : 512;
+  TileMap tm = choose_tiles(hb, (const void*)k_sor64, threads, hb->solve_sync == 1 ? 1 : 0);
+  TRY_R(reset_solve_state(hb, tm));
+  const unsigned grid = (unsigned)(tm.ntj * tm.ntk);
   SorArgs a{itmax, epsi, hb->omega, prof_log(), res_tol, dt};
   GridBar gb = make_bar(B.err, grid);
-  gb.count = hb->bar;
-  gb.gen = hb->bar + 1;
-  void* args[] = {(void*)&B, (void*)&a, (void*)&gb};
+  gb.ctr = reinterpret_cast<unsigned long long*>(hb->bar);
+  void* args[] = {(void*)&B, (void*)&a, (void*)&gb, (void*)&tm};
   prof_mark(true);
   BCFD_CUDA(launch_coop((const void*)k_sor64, grid, threads, args));
   prof_mark(false);
@@ -545,7 +756,7 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   k_rhs<<<grid_for(np, 256), 256, 0, stream()>>>(B, dt);
   BCFD_LAUNCHED();
   const int nmax0 = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
-  if (hb->dc_variant != 1 && cluster_solve_fits(hb)) {
+  if (hb->dc_variant == 2 && cluster_solve_fits(hb)) {
     // the whole block fits in one cluster's distributed shared memory
     const int inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
     const double om = hb->dc_omega > 0 ? hb->dc_omega : 2.0 / (1.0 + std::sin(3.14159265358979323846 / nmax0));
@@ -553,11 +764,11 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
     return launch_residual(hb, dt);
   }
   for (int c = 0; c < 2; ++c) BCFD_CUDA(cudaMemsetAsync(B.pcf[c], 0, np * sizeof(float), stream()));
-  BCFD_CUDA(cudaMemsetAsync(&B.stats->slot[0], 0, 2 * sizeof(double), stream()));
-  BCFD_CUDA(cudaMemsetAsync(hb->bar, 0, 2 * sizeof(unsigned), stream()));
-  const int64_t total = (int64_t)B.d.NXH * B.d.ny * B.d.nz;
-  const int threads = 256;
-  const unsigned grid = coop_grid((const void*)k_sor_dc, threads, 0, (unsigned)((total + threads - 1) / threads));
+  const int threads = hb->solve_threads > 0 ? hb->solve_threads : 256;
+  // variant 3: point-to-point tile sync; otherwise grid-wide phase barriers
+  TileMap tm = choose_tiles(hb, (const void*)k_sor_dc, threads, hb->dc_variant == 3 ? 0 : 1);
+  TRY_R(reset_solve_state(hb, tm));
+  const unsigned grid = (unsigned)(tm.ntj * tm.ntk);
   const int nmax = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
   DcArgs a;
   a.inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
@@ -568,9 +779,8 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   a.div_tol = div_tol;
   a.log = prof_log();
   GridBar gb = make_bar(B.err, grid);
-  gb.count = hb->bar;
-  gb.gen = hb->bar + 1;
-  void* args[] = {(void*)&B, (void*)&a, (void*)&gb};
+  gb.ctr = reinterpret_cast<unsigned long long*>(hb->bar);
+  void* args[] = {(void*)&B, (void*)&a, (void*)&gb, (void*)&tm};
   prof_mark(true);
   BCFD_CUDA(launch_coop((const void*)k_sor_dc, grid, threads, args));
   prof_mark(false);

@@ -212,8 +212,16 @@ int bcfd_max_divergence(bcfd_handle h, double* out);
 int bcfd_block_get_divergence(bcfd_handle h, double* out);
 /* mixed-precision solve parameters of a block: FP32 sweeps per correction,
  * their relaxation factor (0 selects the defaults) and the kernel variant
- * (0: cluster-resident when the block fits in one 16-CTA cluster, 1: grid-wide) */
+ * (0: the library's choice, 1: tiled cooperative with grid-wide phase
+ * barriers, 2: cluster-resident when the block fits in one 16-CTA cluster,
+ * else 1, 3: tiled cooperative with point-to-point neighbour sync) */
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant);
+/* launch shape of a block's tiled Poisson solves (the autotuner's knobs; no
+ * effect on results): threads per CTA (0 = the default: 512 for the FP64
+ * solve, 256 for the mixed one; else 128/256/512), cap
+ * on co-resident CTAs per SM (0 = occupancy limit), and the FP64 solve's
+ * phase sync (0 point-to-point between neighbour tiles, 1 grid-wide) */
+int bcfd_block_set_solve_launch(bcfd_handle h, int threads, int ctas_per_sm, int fp64_sync);
 
 /* ---- measurement window (no counterpart in the reference) ----------------- */
 typedef struct bcfd_profile_report {

@@ -235,6 +235,24 @@ def sphere_two_block(nf: int = 64, n_steps: int = 200, diameter: float = 0.5,
     return case
 
 
+def uniform_block(n=(384, 256, 256), lengths=(3.0, 2.0, 2.0), seed: int = SEED,
+                  noise: bool = True) -> Case:
+    """One body-free uniform block with the domain BCs (the coarse block of the
+    tandem-plate workload is 384x256x256 over 3x2x2); used to measure the
+    Poisson sweeps at sizes far above the 129 MB L2."""
+    nx, ny, nz = n
+    spec = BlockSpec(nx, ny, nz, uniform_faces(0, lengths[0], nx), uniform_faces(0, lengths[1], ny),
+                     uniform_faces(0, lengths[2], nz), omega=1.7, is_coarse=True)
+    dx = lengths[0] / nx
+    case = Case(name=f"block{nx}x{ny}x{nz}", blocks=[spec], dt=0.3 * dx, re=1000.0, uc=1.0)
+    if noise:
+        case.init = [noisy_initial(spec, case.uc, np.random.default_rng(seed))]
+    else:
+        shp = spec.shape
+        case.init = [{"u": np.ones(shp), "v": np.zeros(shp), "w": np.zeros(shp), "p": np.zeros(shp)}]
+    return case
+
+
 def small_two_block(n_steps: int = 2, seed: int = SEED) -> Case:
     """A 24x16x16 coarse + 16^3 fine version of the two-block case for fast parity tests."""
     return sphere_two_block(nf=16, n_steps=n_steps, diameter=0.5, coarse=(24, 16, 16),

@@ -527,7 +527,9 @@ int bcfd_block_create(int64_t nx, int64_t ny, int64_t nz, const double* x1, cons
   d.NX = d.nx + 2;
   d.NY = d.ny + 2;
   d.NZ = d.nz + 2;
-  d.NXH = (d.NX + 1) / 2;
+  // packed row pitch: (NX+1)/2 cells rounded up to 4 so rows start 16-byte
+  // aligned (vector loads); the padding slots are never updated
+  d.NXH = (((d.NX + 1) / 2) + 3) & ~3;
   const int64_t np = d.npts(), np3 = d.npts3(), npk = d.npacked();
   DevBlock& D = hb->d;
   int r = 0;
@@ -540,7 +542,9 @@ int bcfd_block_create(int64_t nx, int64_t ny, int64_t nz, const double* x1, cons
     A(&D.pc[c], npk); A(&D.rhs[c], npk); A(&D.bpk[c], npk); A(&D.upd[c], npk);
     A(&D.pcf[c], npk); A(&D.rhsf[c], npk);
   }
-  D.cap_ib = (int)std::max<int64_t>(64, (int64_t)nx * ny * nz);
+  // IB / TS list capacity: every cell up to 4M cells (a list that outgrows it
+  // reports BCFD_E_CAPACITY)
+  D.cap_ib = (int)std::max<int64_t>(64, std::min<int64_t>((int64_t)nx * ny * nz, (int64_t)1 << 22));
   A(&D.ib_i, D.cap_ib); A(&D.ib_j, D.cap_ib); A(&D.ib_k, D.cap_ib);
   for (int q = 0; q < 7; ++q) { A(&D.nel[q], D.cap_ib); A(&D.nd[q], D.cap_ib); }
   A(&D.ts_idx, D.cap_ib);
@@ -900,6 +904,25 @@ int bcfd_redblack_sor_linear(bcfd_handle h, int64_t itmax, double dt, double eps
   TRY(launch_sor(hb, itmax, dt, epsi));
   return 0;
 }
+int bcfd_block_sor_sweeps(bcfd_handle h, int64_t n_pairs, int precision) {
+  LOCK();
+  GETB(h);
+  if (n_pairs < 1 || n_pairs > 1000000 || precision < 0 || precision > 1) return BCFD_E_ARG;
+  if (precision == 0) {
+    // the reference sweeps from iteration 0, stop test disabled (epsi < 0)
+    BCFD_CUDA(cudaMemsetAsync(&hb->d.stats->niter, 0, sizeof(int64_t), stream()));
+    TRY(launch_sor(hb, n_pairs - 1, 1.0, -1.0));
+  } else {
+    // one correction of n_pairs FP32 sweep pairs, stop test disabled
+    const int keep = hb->dc_inner;
+    hb->dc_inner = (int)n_pairs;
+    const int r = launch_sor_mixed(hb, 0, 1.0, -1.0);
+    hb->dc_inner = keep;
+    TRY(r);
+  }
+  return 0;
+}
+
 int bcfd_update_velocity_newv(bcfd_handle h) {
   LOCK();
   GETB(h);

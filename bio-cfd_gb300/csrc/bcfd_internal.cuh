@@ -9,7 +9,8 @@
 //     cell2 / nodeIdTag / cell_pr on (NX+1)(NY+1)(NZ+1);
 //   * the Poisson correction pc and the right-hand side b/dt live in a
 //     colour-packed red/black layout (one array per colour, NXH*NY*NZ with
-//     NXH = (NX+1)/2) so that each SOR half-sweep streams contiguous memory;
+//     the row pitch NXH = (NX+1)/2 rounded up to a multiple of 4) so that each
+//     SOR half-sweep streams contiguous, 16-byte aligned rows;
 //   * 1-D grid arrays keep the reference's 1-based meaning: ptr[i-1] = x(i).
 // Every FP64 kernel of the drop-in path is compiled with --fmad=false and
 // evaluates its expressions in the reference's order, so it rounds exactly
@@ -29,7 +30,7 @@ namespace bcfd {
 struct Dims {
   int nx, ny, nz;  // interior cells
   int NX, NY, NZ;  // nx+2, ny+2, nz+2
-  int NXH;         // packed row length of one colour, (NX+1)/2
+  int NXH;         // packed row pitch of one colour: (NX+1)/2 rounded up to 4
   __host__ __device__ int64_t idx(int i, int j, int k) const {
     return (int64_t)(i - 1) + (int64_t)NX * ((int64_t)(j - 1) + (int64_t)NY * (k - 1));
   }

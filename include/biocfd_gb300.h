@@ -218,10 +218,16 @@ int bcfd_block_get_divergence(bcfd_handle h, double* out);
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant);
 /* launch shape of a block's tiled Poisson solves (the autotuner's knobs; no
  * effect on results): threads per CTA (0 = the default: 512 for the FP64
- * solve, 256 for the mixed one; else 128/256/512), cap
+ * solve, 256 for the mixed one, which takes at most 256; else 128/256/512), cap
  * on co-resident CTAs per SM (0 = occupancy limit), and the FP64 solve's
  * phase sync (0 point-to-point between neighbour tiles, 1 grid-wide) */
 int bcfd_block_set_solve_launch(bcfd_handle h, int threads, int ctas_per_sm, int fp64_sync);
+/* measurement: exactly n_pairs red-black sweep pairs of the block's Poisson
+ * system b = the current computeDiv result (deltat = 1), stop test disabled.
+ * precision 0: the FP64 reference sweeps on pc; 1: one FP32 correction of
+ * n_pairs sweeps (with its two FP64 residual passes and the FP64 update).
+ * Changes pc; for timing and roofline measurement only. */
+int bcfd_block_sor_sweeps(bcfd_handle h, int64_t n_pairs, int precision);
 
 /* ---- measurement window (no counterpart in the reference) ----------------- */
 typedef struct bcfd_profile_report {

@@ -55,8 +55,20 @@ unsigned coop_grid(const void* fn, int threads, size_t smem, unsigned want) {
   return want < cap ? want : cap;
 }
 
+// cooperative launch (all CTAs co-resident) through cudaLaunchKernelEx, which
+// stream capture records as a cooperative kernel node
 cudaError_t launch_coop(const void* fn, unsigned grid, unsigned block, void** args, size_t smem) {
-  return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(block), args, smem, stream());
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream();
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 GridBar make_bar(int* err, unsigned nblocks) {
@@ -462,6 +474,9 @@ int bcfd_finalize(void) {
   Lib& L = lib();
   if (!L.ready) return 0;
   cudaStreamSynchronize(L.s);
+  if (L.step_graph) cudaGraphExecDestroy(L.step_graph);
+  L.step_graph = nullptr;
+  L.step_key.clear();
   for (HostBlock* hb : L.blocks)
     if (hb) {
       for (void* p : hb->allocs) cudaFree(p);

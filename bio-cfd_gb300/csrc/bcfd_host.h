@@ -82,6 +82,13 @@ struct Lib {
   std::vector<cudaEvent_t> prof_events;   // begin/end pairs, in order
   size_t prof_used = 0;
   int64_t prof_launch0 = 0;
+  // bumped whenever a scratch buffer that captured kernels point at is
+  // (re)allocated, so a captured step graph is rebuilt
+  uint64_t gen = 0;
+  // captured time step (bcfd_run_steps with use_graph)
+  cudaGraphExec_t step_graph = nullptr;
+  std::vector<unsigned char> step_key;  // what the capture depends on
+  int64_t step_kernels = 0;              // kernels in the captured step
 };
 
 Lib& lib();

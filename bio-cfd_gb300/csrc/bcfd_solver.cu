@@ -240,6 +240,88 @@ int step_once(const bcfd_step_config& cfg) {
   return 0;
 }
 
+// Everything a captured step's launches depend on: the step configuration,
+// every block's device view (all device pointers and scalars the kernels
+// receive) and host-side switches, the interfaces' device tables, and the
+// generation of the scratch buffers.  A different key means a new capture.
+std::vector<unsigned char> step_key(const bcfd_step_config& c) {
+  std::vector<unsigned char> k;
+  auto put = [&](const void* p, size_t n) {
+    const unsigned char* b = static_cast<const unsigned char*>(p);
+    k.insert(k.end(), b, b + n);
+  };
+  put(&c.deltat, sizeof c.deltat);
+  put(&c.re, sizeof c.re);
+  put(&c.uc, sizeof c.uc);
+  put(&c.epsi, sizeof c.epsi);
+  put(&c.pc_ita_max, sizeof c.pc_ita_max);
+  put(&c.precision, sizeof c.precision);
+  put(&c.div_tol, sizeof c.div_tol);
+  const Lib& L = lib();
+  put(&L.gen, sizeof L.gen);
+  for (const HostBlock* hb : L.blocks) {
+    const unsigned char none = 0;
+    if (!hb) { put(&none, 1); continue; }
+    put(&hb->d, sizeof hb->d);
+    const int sw[11] = {hb->is_coarse, hb->has_body, hb->move_check, hb->blk_mv_tag, hb->dc_inner,
+                        hb->dc_variant, hb->solve_threads, hb->solve_ctas_per_sm, hb->solve_sync, 0, 0};
+    put(sw, sizeof sw);
+    put(&hb->dc_omega, sizeof hb->dc_omega);
+    put(&hb->omega, sizeof hb->omega);
+    put(&hb->bar, sizeof hb->bar);
+    put(&hb->prog, sizeof hb->prog);
+  }
+  for (const HostInterface* it : L.ifs) {
+    const unsigned char none = 0;
+    if (!it) { put(&none, 1); continue; }
+    put(&it->a, sizeof it->a);
+    put(&it->b, sizeof it->b);
+    put(&it->dtab, sizeof it->dtab);
+    put(it->counter, sizeof it->counter);
+    put(it->off, sizeof it->off);
+  }
+  return k;
+}
+
+// n time steps as replays of one captured step.  When the key changed, the
+// first step runs eagerly (one-time allocations and host-side state changes
+// happen there, outside any capture), then one step is captured, not run.
+int run_steps_graph(const bcfd_step_config& cfg, int64_t n) {
+  Lib& L = lib();
+  int64_t done = 0;
+  if (!L.step_graph || step_key(cfg) != L.step_key) {
+    if (L.step_graph) cudaGraphExecDestroy(L.step_graph);
+    L.step_graph = nullptr;
+    L.step_key.clear();
+    if (n == 0) return 0;
+    TRY(step_once(cfg));
+    done = 1;
+    if (done == n) return 0;
+    const std::vector<unsigned char> key = step_key(cfg);
+    cudaGraph_t g = nullptr;
+    const int64_t k0 = L.launches;
+    BCFD_CUDA(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeRelaxed));
+    const int r = step_once(cfg);
+    const cudaError_t e = cudaStreamEndCapture(stream(), &g);
+    if (r) {
+      if (g) cudaGraphDestroy(g);
+      return r;
+    }
+    BCFD_CUDA(e);
+    const cudaError_t ei = cudaGraphInstantiate(&L.step_graph, g, 0);
+    cudaGraphDestroy(g);
+    BCFD_CUDA(ei);
+    L.step_kernels = L.launches - k0;
+    L.launches = k0;
+    L.step_key = key;
+  }
+  for (; done < n; ++done) {
+    BCFD_CUDA(cudaGraphLaunch(L.step_graph, stream()));
+    L.launches += L.step_kernels;
+  }
+  return 0;
+}
+
 }  // namespace
 }  // namespace bcfd
 
@@ -337,7 +419,11 @@ int bcfd_poisson_solver(int64_t pc_ita_max, double epsi, int64_t ita, double del
 int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps) {
   LOCK();
   if (!cfg || n_steps < 0) return BCFD_E_ARG;
-  for (int64_t s = 0; s < n_steps; ++s) TRY(step_once(*cfg));
+  if (cfg->use_graph && !lib().prof_on) {
+    TRY(run_steps_graph(*cfg, n_steps));
+  } else {
+    for (int64_t s = 0; s < n_steps; ++s) TRY(step_once(*cfg));
+  }
   int err = 0;
   for (auto& [g, hb] : blocks()) {
     const int e = sync_err(hb);

@@ -441,6 +441,7 @@ static DagScratch& dag_scratch(HostBlock* hb, int* status) {
         cudaMalloc(&s->flag, 8 * sizeof(int)) != cudaSuccess)
       *status = BCFD_E_NOMEM;
     hb->dag_scratch = s;
+    lib().gen++;
   }
   return *static_cast<DagScratch*>(hb->dag_scratch);
 }

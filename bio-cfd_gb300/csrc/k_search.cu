@@ -10,6 +10,8 @@
 // The result is bit-identical to the reference's argmin at a fraction of the
 // FP64 work.  Index lists are built by an order-preserving compaction over
 // the (k,j,i) loop order, the order of the reference's serial CPU build.
+#include <cstring>
+
 #include "bcfd_host.h"
 
 namespace bcfd {
@@ -521,6 +523,8 @@ struct SearchScratch {
   int* count = nullptr;
   int* cta = nullptr;
   int64_t cap_e = 0, npts = 0;
+  float org_host[4] = {0, 0, 0, 0};  // last uploaded origin / radius
+  bool org_set = false;
 };
 
 static SearchScratch& scratch_of(HostBlock* hb) {
@@ -553,11 +557,14 @@ static int ensure_scratch(HostBlock* hb) {
     BCFD_CUDA(cudaMalloc(&s.cta, ((nint + kChunk - 1) / kChunk + 1) * sizeof(int)));
     BCFD_CUDA(cudaMalloc(&s.org, 4 * sizeof(float)));
     s.npts = np;
+    s.org_set = false;
+    lib().gen++;
   }
   if (s.cap_e < hb->d.ne) {
     if (s.cf) cudaFree(s.cf);
     BCFD_CUDA(cudaMalloc(&s.cf, (size_t)std::max(hb->d.ne, 1) * sizeof(float4)));
     s.cap_e = hb->d.ne;
+    lib().gen++;
   }
   // origin: centre of the block; R: half diagonal of the padded block
   const Dims& d = hb->d.d;
@@ -568,7 +575,12 @@ static int ensure_scratch(HostBlock* hb) {
   // bound on |query - origin| and |centroid - origin| (centroids lie inside
   // the hull of the nodes)
   h[3] = (float)(1.01 * std::max(R, hb->node_rmax) + 1e-6);
-  BCFD_CUDA(cudaMemcpyAsync(s.org, h, sizeof(h), cudaMemcpyHostToDevice, stream()));
+  // upload only when it changes (a captured step contains no host copies)
+  if (!s.org_set || std::memcmp(h, s.org_host, sizeof(h)) != 0) {
+    std::memcpy(s.org_host, h, sizeof(h));
+    BCFD_CUDA(cudaMemcpyAsync(s.org, s.org_host, sizeof(h), cudaMemcpyHostToDevice, stream()));
+    s.org_set = true;
+  }
   return 0;
 }
 

@@ -51,7 +51,7 @@ def peaks():
 
 def traffic_from_profiles():
     """dram read+write bytes per launch of the dominant kernel, from the committed ncu summary."""
-    f = ROOT / "profiles" / "sor_mixed_two_block.md"
+    f = ROOT / "profiles" / "k_sor_dc_two_block.md"
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
@@ -194,7 +194,7 @@ class _Null:
         return False
 
 
-def sweep_roofline(torch, local, hbm):
+def sweep_roofline(torch, local, hbm, block=(384, 256, 256), fp32_pairs=40, fp64_pairs=4):
     """Poisson sweeps on one body-free 384x256x256 block (the coarse block of
     the tandem-plate workload, ~25M cells, far above the 129 MB L2): achieved
     GB/s of the FP32 and FP64 red-black sweep kernels, algorithmic bytes from
@@ -203,15 +203,19 @@ def sweep_roofline(torch, local, hbm):
     from biocfd import synth
     from biocfd.solver import Solver
     from biocfd._lib import check
-    case = synth.uniform_block((384, 256, 256), noise=True)
+    case = synth.uniform_block(tuple(block), noise=True)
     s = Solver(case, device=local)
     s.setup()
     g = s.handles[0]
     check(s.L.bcfd_cellcount_solid(g), "cellcount_solid")
     check(s.L.bcfd_compute_div(g), "compute_div")
     check(s.L.bcfd_block_sor_sweeps(g, 2, 1), "sor_sweeps")
-    out = {"block": "384x256x256 (25.2M cells), no body", "l2": "working set > L2 (FP32: 430 MB)"}
-    for prec, pairs, key in ((1, 40, "fp32"), (0, 4, "fp64")):
+    cells = block[0] * block[1] * block[2]
+    out = {"block": "x".join(map(str, block)) + f" ({cells / 1e6:.1f}M cells), no body",
+           "l2": f"FP32 working set {17 * cells / 1e6:.0f} MB vs 129 MB L2"}
+    for prec, pairs, key in ((1, fp32_pairs, "fp32"), (0, fp64_pairs, "fp64")):
+        if pairs <= 0:
+            continue
         s.profile_begin()
         check(s.L.bcfd_block_sor_sweeps(g, pairs, prec), "sor_sweeps")
         p = s.profile_end()
@@ -240,6 +244,14 @@ def run_gpu(args):
     flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
 
     tol = DIV_TOL
+
+    if args.mixed_only:
+        # the flagship arm alone (for profiler captures of its kernels)
+        t, _, res, it, _ = time_path(s, torch, flush, stream, args.steps, args.warmup, 1, tol)
+        print(json.dumps({"run": "mixed arm only", "ms_per_step": statistics.mean(t), "div_residual": max(res),
+                          "fp32_sweeps_last_step": it[-1]}), flush=True)
+        s.close()
+        return
 
     def arm(precision, clocks=None):
         nonlocal s, stream
@@ -347,7 +359,18 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sweep-roofline", action="store_true")
+    ap.add_argument("--mixed-only", action="store_true",
+                    help="time only the flagship arm and print a short line (profiler captures)")
+    ap.add_argument("--sweep-only", default="",
+                    help="nx,ny,nz[,fp32_pairs[,fp64_pairs]]: only the Poisson sweep measurement on that block")
     args = ap.parse_args()
+    if args.sweep_only:
+        import torch
+        v = [int(x) for x in args.sweep_only.split(",")]
+        hbm, _ = peaks()
+        r = sweep_roofline(torch, 0, hbm, v[:3], v[3] if len(v) > 3 else 40, v[4] if len(v) > 4 else 4)
+        print(json.dumps(r), flush=True)
+        return
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -197,6 +197,28 @@ def sphere_single_block(n: int = 64, n_steps: int = 100, diameter: float = 0.25,
     return case
 
 
+def plate_single_block(n: int = 32, n_steps: int = 2, semi_axes=(0.25, 0.125, 0.0125),
+                       center=(0.45, 0.5, 0.5), reynolds: float = 300.0, omega: float = 1.7,
+                       pc_ita_max: int = 5000, seed: int = SEED, surf_id: int = 51) -> Case:
+    """Single uniform n^3 block on the unit cube with a stationary rigid
+    ellipsoidal plate (surface 51) thinner than a cell, so that its IB cells are
+    thin-surface cells and the momentum predictor's ghost substitution runs.
+    Re = U c / nu on the chord c = 2 * semi_axes[0]."""
+    f = uniform_faces(0.0, 1.0, n)
+    dx = 1.0 / n
+    spec = BlockSpec(n, n, n, f, f.copy(), f.copy(), omega=omega, is_coarse=True)
+    spec.mesh = ellipsoid_plate(center, semi_axes, 0.5 * dx, surf_id=surf_id)
+    c = np.asarray(center)
+    ax = np.asarray(semi_axes)
+    spec.search_box = search_box_for(spec, c - ax, c + ax)
+    rng = np.random.default_rng(seed)
+    chord = 2.0 * semi_axes[0]
+    case = Case(name=f"plate{n}", blocks=[spec], dt=0.3 * dx, re=reynolds / chord, uc=1.0, epsi=1e-6,
+                pc_ita_max=pc_ita_max, n_steps=n_steps)
+    case.init = [noisy_initial(spec, case.uc, rng)]
+    return case
+
+
 def sphere_two_block(nf: int = 64, n_steps: int = 200, diameter: float = 0.5,
                      reynolds: float = 300.0, omega_c: float = 1.7, omega_f: float = 1.7,
                      pc_ita_max: int = 5000, seed: int = SEED, coarse=(96, 64, 64),

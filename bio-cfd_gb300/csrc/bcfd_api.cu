@@ -552,7 +552,7 @@ int bcfd_block_create(int64_t nx, int64_t ny, int64_t nz, const double* x1, cons
     if (!r) r = dalloc(hb, p, n);
   };
   A(&D.u, np); A(&D.v, np); A(&D.w, np); A(&D.p, np); A(&D.ut, np); A(&D.vt, np); A(&D.wt, np);
-  A(&D.cell, np); A(&D.cell_n, np); A(&D.cell2, np3); A(&D.nodeTag, np3); A(&D.cell_pr, np3);
+  A(&D.cell, np); A(&D.cell_n, np); A(&D.tsnear, np); A(&D.cell2, np3); A(&D.nodeTag, np3); A(&D.cell_pr, np3);
   for (int c = 0; c < 2; ++c) {
     A(&D.pc[c], npk); A(&D.rhs[c], npk); A(&D.bpk[c], npk); A(&D.upd[c], npk);
     A(&D.pcf[c], npk); A(&D.rhsf[c], npk);

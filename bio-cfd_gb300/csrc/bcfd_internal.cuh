@@ -101,6 +101,7 @@ struct DevBlock {
   double *u, *v, *w, *p, *ut, *vt, *wt;
   // tags
   int8_t *cell, *cell_n, *cell2, *nodeTag, *cell_pr;
+  uint8_t* tsnear;  // 1 where a cell is within [-3,3]^3 of a TS cell (overlay stencil)
   // colour-packed Poisson arrays: [0] black, [1] red
   double *pc[2], *rhs[2];
   float *pcf[2], *rhsf[2];

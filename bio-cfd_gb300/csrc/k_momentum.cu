@@ -1,27 +1,21 @@
 // Momentum predictor (nsMomentum2order, src/NavierStokes.f90:252-912) and the
 // boundary conditions of src/BoundaryConditions.f90.
 //
-// One thread per interior cell; non-fluid cells are skipped (the reference
-// loops over the fluid list, whose order does not matter without thin-surface
-// cells because the loop then only reads u,v,w,p and writes ut,vt,wt).  Cells
-// next to a thin-surface (TS) cell see the reference's in-place ghost
-// substitution; that serial-order effect is reproduced exactly by the overlay
-// in TsView (see k_ts_overlay below).  FP64, compiled without FMA contraction,
-// expressions in the reference's evaluation order.
+// One thread per interior cell; non-fluid cells are skipped.  The reference
+// loops over the fluid list in (k,j,i) order, and that order matters only next
+// to thin-surface (TS) cells: there the loop substitutes ghost values into
+// u,v,w,p before a cell's stencil and restores them after it
+// (src/NavierStokes.f90:310-490, 860-907), so a cell may read values written
+// by earlier cells.  Cells within reach of a TS cell go through a second
+// kernel whose reads reproduce that serial order exactly (TsReader below);
+// every other cell reads the fields directly.  FP64, compiled without FMA
+// contraction, expressions in the reference's evaluation order (T = double);
+// the same stencil in FP32 arithmetic serves the mixed-precision path.
 #include "bcfd_host.h"
 
 namespace bcfd {
 
 namespace {
-
-// Thin-surface overlay: the values the reference's serial loop would read at
-// the faces of TS cells.  For a fluid cell at linear position `self` the value
-// of a TS-face position is (1) the ghost value written by this cell's own
-// nn-loop if it wrote that position, else (2) the restore value written by
-// the latest earlier fluid cell that restored it, else (3) the original field.
-struct TsView {
-  bool active;
-};
 
 struct MomArgs {
   double dt, re;
@@ -48,33 +42,31 @@ __device__ __forceinline__ T grid_t(const double* d64, const float* f32, int q) 
   else return f32[q];
 }
 
-// T = double: the reference arithmetic (bit-exact drop-in).  T = float: the
-// FP32 momentum stencil of the mixed-precision path (fields stay FP64 in HBM;
-// stencil values are rounded to FP32 on load, ut/vt/wt stored back as FP64).
-template <typename T>
-__global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
+// Field reads of the stencil: field f (0 u, 1 v, 2 w, 3 p) at cell (a,b,e),
+// linear index x.  The plain reader loads the array.
+struct PlainReader {
+  const double* f[4];
+  __device__ __forceinline__ double get(int q, int, int, int, int64_t x) const { return __ldg(f[q] + x); }
+};
+
+// One fluid cell (i,j,k) of nsMomentum2order.  T = double: the reference
+// arithmetic (bit-exact drop-in).  T = float: the FP32 momentum stencil of the
+// mixed-precision path (fields stay FP64 in HBM; stencil values are rounded to
+// FP32 on load, ut/vt/wt stored back as FP64).
+template <typename T, class Rd>
+__device__ __forceinline__ void momentum_cell(const DevBlock& B, const MomArgs& a, int i, int j, int k,
+                                              int64_t c, const Rd& rd) {
   const T Q25 = T(0.25), HALF = T(0.5), TWO = T(2.0), ONE = T(1.0);
   const Dims& d = B.d;
-  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
   const T alpha = ONE;
   const T deltat = T(a.dt), re = T(a.re);
   const int nx_var = d.nx, ny_var = d.ny, nz_var = d.nz;
   const int64_t SX = 1, SY = d.NX, SZ = (int64_t)d.NX * d.NY;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = 2 + (int)(t % d.nx);
-    const int64_t r = t / d.nx;
-    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
-    const int64_t c = d.idx(i, j, k);
-    if (B.cell[c] != 0) continue;
-    const double* __restrict__ U = B.u;
-    const double* __restrict__ V = B.v;
-    const double* __restrict__ W = B.w;
-    const double* __restrict__ P = B.p;
-#define u(a, b, e) (T)__ldg(U + c + (a) * SX + (b) * SY + (e) * SZ)
-#define v(a, b, e) (T)__ldg(V + c + (a) * SX + (b) * SY + (e) * SZ)
-#define w(a, b, e) (T)__ldg(W + c + (a) * SX + (b) * SY + (e) * SZ)
-#define p(a, b, e) (T)__ldg(P + c + (a) * SX + (b) * SY + (e) * SZ)
+  {
+#define u(a, b, e) (T) rd.get(0, i + (a), j + (b), k + (e), c + (a) * SX + (b) * SY + (e) * SZ)
+#define v(a, b, e) (T) rd.get(1, i + (a), j + (b), k + (e), c + (a) * SX + (b) * SY + (e) * SZ)
+#define w(a, b, e) (T) rd.get(2, i + (a), j + (b), k + (e), c + (a) * SX + (b) * SY + (e) * SZ)
+#define p(a, b, e) (T) rd.get(3, i + (a), j + (b), k + (e), c + (a) * SX + (b) * SY + (e) * SZ)
 #define DX(q) grid_t<T>(B.dxa, B.dxf, (q) - 1)
 #define DY(q) grid_t<T>(B.dya, B.dyf, (q) - 1)
 #define DZ(q) grid_t<T>(B.dza, B.dzf, (q) - 1)
@@ -143,17 +135,12 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
     const T dx2xr = dx + dxr, dx2xl = dx + dxl, dy2ye = dy + dye, dy2yw = dy + dyw,
                  dz2zt = dz + dzt, dz2zb = dz + dzb;
 
-    // thin-surface neighbours (cell2 == 2 next to this cell) need the ghost
-    // substitution of src/NavierStokes.f90:310-490, handled by k_momentum_ts
-    if (!adj_ok(B.cell2, d, true, i, j, k, 1)) {
-      set_err(B.err, BCFD_E_STATE);
-      continue;
-    }
     // superset of the three components' third-order index ranges; inside it
     // the distance-2 neighbours exist
     const bool inner = i > 2 && j > 2 && k > 2 && i < nx_var + 1 && j < ny_var + 1 && k < nz_var + 1;
     const bool smooth = inner && adj_ok(B.cell, d, false, i, j, k, 1) && adj_ok(B.cell2, d, true, i, j, k, 2);
     const bool near_ib = !smooth, near_ts2 = false;
+    (void)near_ib;
 
     // ---------------- U momentum ----------------
     {
@@ -347,6 +334,213 @@ __global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
+  const Dims& d = B.d;
+  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
+  const PlainReader rd{{B.u, B.v, B.w, B.p}};
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(t % d.nx);
+    const int64_t r = t / d.nx;
+    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
+    const int64_t c = d.idx(i, j, k);
+    if (B.cell[c] != 0) continue;
+    if (B.tsnear[c]) continue;  // done by k_momentum_ts
+    momentum_cell<T>(B, a, i, j, k, c, rd);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Thin-surface overlay.  Every position the reference substitutes or
+// restores is one of a TS cell T's seven own positions; the kind K of the
+// position fixes the ghost slot, the element list and the face coordinate of
+// its sign test:
+//   U2 u(T), U1 u(T-ex), V2 v(T), V1 v(T-ey), W2 w(T), W1 w(T-ez), P p(T).
+// A fluid cell F whose +d neighbour is T handles six of them (direction d
+// excludes one kind: +x U1, -x U2, +y V1, -y V2, +z W1, -z W2):
+//  * before its stencil it writes kind K with ghost_K(nn) for the last TS
+//    list entry nn whose sign test at F's own face is negative (the test does
+//    not depend on which TS cell is F's neighbour);
+//  * after its stencil it restores kind K with tghost_K(n_ts), the saved value
+//    of the last TS entry (the index the reference's loop leaves behind).
+// So a cell G reads position X as: its own write if it made one, else the
+// restore of the latest fluid cell before G (list order = linear index order)
+// that restores X, else the original value; and after the loop X holds the
+// restore of the latest restorer overall (k_ts_restore).
+// ---------------------------------------------------------------------------
+enum TsKind { K_U2 = 0, K_U1, K_V2, K_V1, K_W2, K_W1, K_P, N_KIND };
+
+__device__ __forceinline__ int ghost_slot(int K) {
+  // ghost[] order: p, pt, u2, u2t, v2, v2t, w2, w2t, u1, u1t, v1, v1t, w1, w1t
+  return K == K_P ? G_P : (K & 1) ? (G_U1 + 2 * (K >> 1)) : (G_U2 + 2 * (K >> 1));
+}
+__device__ __forceinline__ int nel_slot(int K) {
+  // nel[] order: p, u1, u2, v1, v2, w1, w2
+  return K == K_P ? N_P : (N_U1 + 2 * (K >> 1) + ((K & 1) ? 0 : 1));
+}
+// the kind direction d (0..5 = +x,-x,+y,-y,+z,-z) does not handle
+__device__ __forceinline__ int excluded_kind(int dir) {
+  return 2 * (dir >> 1) + ((dir & 1) ? 0 : 1);
+}
+__device__ __forceinline__ void dir_vec(int dir, int& a, int& b, int& e) {
+  const int s = (dir & 1) ? -1 : 1;
+  a = (dir >> 1) == 0 ? s : 0;
+  b = (dir >> 1) == 1 ? s : 0;
+  e = (dir >> 1) == 2 ? s : 0;
+}
+
+// latest restorer F (linear index < before) of position kind K of TS cell T;
+// updates best / val
+__device__ __forceinline__ void latest_restore(const DevBlock& B, int ti, int tj, int tk, int K,
+                                               int64_t before, const double* rconst, int64_t& best,
+                                               double& val) {
+  const Dims& d = B.d;
+#pragma unroll
+  for (int dir = 0; dir < 6; ++dir) {
+    if (K == excluded_kind(dir)) continue;
+    int a, b, e;
+    dir_vec(dir, a, b, e);
+    // F's +dir neighbour is T
+    const int fi = ti - a, fj = tj - b, fk = tk - e;
+    if (fi < 2 || fj < 2 || fk < 2 || fi > d.nx + 1 || fj > d.ny + 1 || fk > d.nz + 1) continue;
+    const int64_t lf = d.idx(fi, fj, fk);
+    if (lf >= before || lf <= best) continue;
+    if (B.cell[lf] != 0) continue;
+    best = lf;
+    val = rconst[K];
+  }
+}
+
+// the (up to two) TS cells and kinds a position of field q belongs to
+__device__ __forceinline__ int owners(const DevBlock& B, int q, int xi, int xj, int xk, int ot[2][4]) {
+  const Dims& d = B.d;
+  int n = 0;
+  auto ts = [&](int a, int b, int e) {
+    return a >= 1 && b >= 1 && e >= 1 && a <= d.nx + 3 && b <= d.ny + 3 && e <= d.nz + 3 &&
+           B.cell2[d.idx3(a, b, e)] == 2;
+  };
+  if (q == 3) {
+    if (ts(xi, xj, xk)) { ot[n][0] = xi; ot[n][1] = xj; ot[n][2] = xk; ot[n][3] = K_P; ++n; }
+    return n;
+  }
+  if (ts(xi, xj, xk)) { ot[n][0] = xi; ot[n][1] = xj; ot[n][2] = xk; ot[n][3] = 2 * q; ++n; }
+  const int ai = xi + (q == 0), aj = xj + (q == 1), ak = xk + (q == 2);
+  if (ts(ai, aj, ak)) { ot[n][0] = ai; ot[n][1] = aj; ot[n][2] = ak; ot[n][3] = 2 * q + 1; ++n; }
+  return n;
+}
+
+// Reads of a cell G near TS cells, in the reference's serial order.
+struct TsReader {
+  const DevBlock* B;
+  int gi, gj, gk;
+  int64_t glin;
+  int last[N_KIND];      // own substitution: last TS entry with a negative test, -1: none
+  double rconst[N_KIND]; // restore value of each kind
+  // not inlined: one copy of the overlay logic serves all ~150 stencil reads
+  __device__ __noinline__ double get(int q, int xi, int xj, int xk, int64_t x) const {
+    const double* f = q == 0 ? B->u : q == 1 ? B->v : q == 2 ? B->w : B->p;
+    const double orig = __ldg(f + x);
+    int ot[2][4];
+    const int n = owners(*B, q, xi, xj, xk, ot);
+    if (n == 0) return orig;
+    // own substitution: T is an axis neighbour of G and the direction handles K
+    for (int m = 0; m < n; ++m) {
+      const int di = ot[m][0] - gi, dj = ot[m][1] - gj, dk = ot[m][2] - gk;
+      const int ad = abs(di) + abs(dj) + abs(dk);
+      if (ad != 1) continue;
+      const int dir = di ? (di > 0 ? 0 : 1) : dj ? (dj > 0 ? 2 : 3) : (dk > 0 ? 4 : 5);
+      const int K = ot[m][3];
+      if (K == excluded_kind(dir)) continue;
+      if (last[K] >= 0) return B->ghost[ghost_slot(K)][last[K]];
+    }
+    int64_t best = -1;
+    double val = orig;
+    for (int m = 0; m < n; ++m)
+      latest_restore(*B, ot[m][0], ot[m][1], ot[m][2], ot[m][3], glin, rconst, best, val);
+    return val;
+  }
+};
+
+__device__ __forceinline__ void restore_consts(const DevBlock& B, int nts, double* rc) {
+#pragma unroll
+  for (int K = 0; K < N_KIND; ++K) rc[K] = nts > 0 ? B.ghost[ghost_slot(K) + 1][nts - 1] : 0.0;
+}
+
+// sign tests of src/NavierStokes.f90:321-354 for every TS entry: the last
+// entry with a negative test, per kind
+__device__ void own_substitution(const DevBlock& B, int i, int j, int k, int nts, int* last) {
+  const double X[N_KIND] = {B.x1[i], B.x1[i - 1], B.xp[i - 1], B.xp[i - 1], B.xp[i - 1], B.xp[i - 1], B.xp[i - 1]};
+  const double Y[N_KIND] = {B.yp[j - 1], B.yp[j - 1], B.y1[j], B.y1[j - 1], B.yp[j - 1], B.yp[j - 1], B.yp[j - 1]};
+  const double Z[N_KIND] = {B.zp[k - 1], B.zp[k - 1], B.zp[k - 1], B.zp[k - 1], B.z1[k], B.z1[k - 1], B.zp[k - 1]};
+#pragma unroll
+  for (int K = 0; K < N_KIND; ++K) last[K] = -1;
+  for (int nn = 0; nn < nts; ++nn) {
+    const int bt = B.ts_idx[nn] - 1;
+#pragma unroll
+    for (int K = 0; K < N_KIND; ++K) {
+      const int e = B.nel[nel_slot(K)][bt] - 1;
+      const double t = (X[K] - B.xcent[e]) * B.cosA[e] + (Y[K] - B.ycent[e]) * B.cosB[e] +
+                       (Z[K] - B.zcent[e]) * B.cosG[e];
+      if (t < 0) last[K] = nn;
+    }
+  }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(128) k_momentum_ts(DevBlock B, MomArgs a) {
+  const Dims& d = B.d;
+  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(t % d.nx);
+    const int64_t r = t / d.nx;
+    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
+    const int64_t c = d.idx(i, j, k);
+    if (B.cell[c] != 0 || !B.tsnear[c]) continue;
+    TsReader rd;
+    rd.B = &B;
+    rd.gi = i;
+    rd.gj = j;
+    rd.gk = k;
+    rd.glin = c;
+    restore_consts(B, nts, rd.rconst);
+    const bool adj = !adj_ok(B.cell2, d, true, i, j, k, 1);
+    if (adj) {
+      own_substitution(B, i, j, k, nts, rd.last);
+    } else {
+#pragma unroll
+      for (int K = 0; K < N_KIND; ++K) rd.last[K] = -1;
+    }
+    momentum_cell<T>(B, a, i, j, k, c, rd);
+  }
+}
+
+// u,v,w,p at TS positions after the loop: the restore of the latest restorer
+__global__ void k_ts_restore(DevBlock B) {
+  const Dims& d = B.d;
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  double rc[N_KIND];
+  restore_consts(B, nts, rc);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nts * N_KIND; t += gridDim.x * blockDim.x) {
+    const int nn = t / N_KIND, K = t % N_KIND;
+    const int bt = B.ts_idx[nn] - 1;
+    const int ti = B.ib_i[bt], tj = B.ib_j[bt], tk = B.ib_k[bt];
+    const int q = K == K_P ? 3 : K >> 1;
+    const int xi = ti - (K == K_U1), xj = tj - (K == K_V1), xk = tk - (K == K_W1);
+    int ot[2][4];
+    const int n = owners(B, q, xi, xj, xk, ot);
+    int64_t best = -1;
+    double val = 0.0;
+    for (int m = 0; m < n; ++m)
+      latest_restore(B, ot[m][0], ot[m][1], ot[m][2], ot[m][3], INT64_MAX, rc, best, val);
+    if (best < 0) continue;
+    double* f = q == 0 ? B.u : q == 1 ? B.v : q == 2 ? B.w : B.p;
+    f[d.idx(xi, xj, xk)] = val;
+  }
+}
+
 // velocityBC loop 1 (x faces), src/BoundaryConditions.f90:16-40
 __global__ void k_vbc_x(DevBlock B, double deltat, double uc) {
   const Dims& d = B.d;
@@ -431,6 +625,17 @@ int launch_momentum(HostBlock* hb, double dt, double re, bool fp32) {
   else
     k_momentum<double><<<grid_for(n, 128, 1u << 20), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
   BCFD_LAUNCHED();
+  if (hb->has_body) {
+    // cells within reach of TS cells (none without surfaces 51/52), then the
+    // values the reference's loop leaves at the TS positions
+    if (fp32)
+      k_momentum_ts<float><<<grid_for(n, 128, 2048), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
+    else
+      k_momentum_ts<double><<<grid_for(n, 128, 2048), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
+    BCFD_LAUNCHED();
+    k_ts_restore<<<grid_for((int64_t)hb->d.cap_ib * 7, 128, 256), 128, 0, stream()>>>(hb->d);
+    BCFD_LAUNCHED();
+  }
   return 0;
 }
 

@@ -701,6 +701,21 @@ int launch_norm_distance(HostBlock* hb) {
   return 0;
 }
 
+// cells whose momentum stencil can read a position of a TS cell (the reach
+// of the third-order stencil plus the staggering: [-3,3]^3 around it)
+__global__ void k_ts_near(DevBlock B) {
+  const Dims& d = B.d;
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < (int64_t)nts * 343;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int nn = (int)(t / 343), o = (int)(t % 343);
+    const int bt = B.ts_idx[nn] - 1;
+    const int i = B.ib_i[bt] + o % 7 - 3, j = B.ib_j[bt] + (o / 7) % 7 - 3, k = B.ib_k[bt] + o / 49 - 3;
+    if (i < 2 || j < 2 || k < 2 || i > d.nx + 1 || j > d.ny + 1 || k > d.nz + 1) continue;
+    B.tsnear[d.idx(i, j, k)] = 1;
+  }
+}
+
 int launch_find_ts(HostBlock* hb) {
   const Dims& d = hb->d.d;
   const int64_t nint = (int64_t)d.nx * d.ny * d.nz;
@@ -709,6 +724,9 @@ int launch_find_ts(HostBlock* hb) {
   k_ts_mark<<<grid_for(hb->d.cap_ib, 256), 256, 0, stream()>>>(hb->d);
   BCFD_LAUNCHED();
   k_ts_list<<<1, 1024, 0, stream()>>>(hb->d);
+  BCFD_LAUNCHED();
+  BCFD_CUDA(cudaMemsetAsync(hb->d.tsnear, 0, d.npts(), stream()));
+  k_ts_near<<<grid_for((int64_t)hb->d.cap_ib * 343, 256, 1024), 256, 0, stream()>>>(hb->d);
   BCFD_LAUNCHED();
   return 0;
 }

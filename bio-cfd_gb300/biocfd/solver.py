@@ -235,6 +235,13 @@ class Solver:
         check(self.L.bcfd_profile_end(C.byref(r)), "profile_end")
         return {k: getattr(r, k) for k, _ in r._fields_}
 
+    def stress(self, g: int, mu_f: float, rho_f: float = 1.0) -> np.ndarray:
+        """stress_calculation (src/StressCalc.f90:14-208): viscous drag, pressure drag,
+        viscous lift, pressure lift coefficients."""
+        out = np.zeros(4, np.float64)
+        check(self.L.bcfd_stress_calculation(g, mu_f, rho_f, _pd(out)), "stress_calculation")
+        return out
+
     def stream_ptr(self) -> int:
         p = C.c_void_p()
         check(self.L.bcfd_get_stream(C.byref(p)), "get_stream")

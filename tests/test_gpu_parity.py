@@ -104,3 +104,35 @@ def test_two_block_steps():
         s.research_phase()
         compare_fields(o, s, f"step {k} research")
         compare_search(o, s, f"step {k} research")
+
+
+# the per-element contributions are the reference's expressions; only the
+# summation order differs (element order on the CPU, a fixed tree on the GPU)
+STRESS_RTOL = 1e-9
+
+
+@pytest.mark.parametrize("maker", ["sphere", "plate"])
+def test_stress_calculation(maker):
+    case = (synth.sphere_single_block(n=24, n_steps=1, diameter=0.3) if maker == "sphere"
+            else synth.plate_single_block(n=24, n_steps=1))
+    o, s = _pair(case)
+    o.step()
+    s.run(1)
+    mu_f, rho_f = 1.0 / case.re, 1.0
+    o.L.orc_stress_calculation(1, mu_f, rho_f)
+    ref = np.array([o.getf(1, k) for k in ("viscous_drag", "pressure_drag", "viscous_lift", "pressure_lift")])
+    got = s.stress(s.handles[0], mu_f, rho_f)
+    assert np.all(np.isfinite(ref)) and np.any(ref != 0.0)
+    np.testing.assert_allclose(got, ref, rtol=STRESS_RTOL, atol=1e-14 * np.max(np.abs(ref)))
+
+
+def test_steps_100_single_block_bitwise():
+    # the spec bar is rel L2 1e-8 after 100 steps; the drop-in path is bitwise
+    case = synth.sphere_single_block(n=24, n_steps=100, diameter=0.3)
+    o, s = _pair(case)
+    for _ in range(100):
+        o.step()
+    s.run(100)
+    compare_fields(o, s, "100 steps")
+    compare_iters(o, s, "100 steps")
+    compare_search(o, s, "100 steps")

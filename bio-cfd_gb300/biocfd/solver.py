@@ -86,8 +86,10 @@ class Solver:
             check(L.bcfd_interface_create(self.handles[it.a_blk - 1], self.handles[it.b_blk - 1],
                                           it.a_msh, it.b_msh, _pd(box), C.byref(h)), "interface_create")
             self.ifaces.append(h.value)
-        for g, spec in zip(self.handles, case.blocks):
-            if spec.has_body:
+        for q, (g, spec) in enumerate(zip(self.handles, case.blocks)):
+            # app/main.F90:80-85: every block g /= 1 is tagged and counted (a
+            # block without a surface is all fluid)
+            if spec.has_body or (q > 0 and case.interfaces):
                 check(L.bcfd_tagging_th(g), "tagging_th")
                 check(L.bcfd_cellcount_solid(g), "cellcount_solid")
         if case.interfaces and not case.blocks[0].has_body:
@@ -218,6 +220,9 @@ class Solver:
         d = np.zeros(2)
         check(self.L.bcfd_block_get_divergence(g, _pd(d)), "get_divergence")
         return float(d[0]), float(d[1])
+
+    def set_batching(self, on: bool):
+        check(self.L.bcfd_set_batching(int(on)), "set_batching")
 
     def set_solve_launch(self, threads: int = 0, ctas_per_sm: int = 0, fp64_sync: int = 0, block: int = None):
         for g in (self.handles if block is None else [self.handles[block]]):

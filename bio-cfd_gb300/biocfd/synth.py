@@ -257,6 +257,52 @@ def sphere_two_block(nf: int = 64, n_steps: int = 200, diameter: float = 0.5,
     return case
 
 
+def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
+                fine_boxes=(((0.5, 1.0), (0.5, 1.0), (0.5, 1.0)),
+                            ((1.5, 2.25), (0.75, 1.25), (1.0, 1.5)),
+                            ((2.375, 2.75), (1.0, 1.5), (0.375, 0.75))),
+                body: int = 0, diameter: float = 0.25, reynolds: float = 300.0, n_steps: int = 2,
+                omega: float = 1.7, pc_ita_max: int = 5000, seed: int = SEED, plate: bool = False) -> Case:
+    """A coarse block with several nested fine blocks of uneven sizes at ratio 2
+    (one interface per fine block), a stationary sphere (or, with `plate`, a
+    thin plate of surface 51) in fine block `body`.  Box edges must lie on
+    coarse faces."""
+    cnx, cny, cnz = coarse
+    L = domain
+    d = (L[0] / cnx, L[1] / cny, L[2] / cnz)
+    cs = BlockSpec(cnx, cny, cnz, uniform_faces(0, L[0], cnx), uniform_faces(0, L[1], cny),
+                   uniform_faces(0, L[2], cnz), omega=omega, is_coarse=True)
+    blocks, ifs = [cs], []
+    ratio = 2
+    for q, box in enumerate(fine_boxes):
+        n = []
+        for ax in range(3):
+            cells = (box[ax][1] - box[ax][0]) / d[ax]
+            assert abs(cells - round(cells)) < 1e-9, (box, ax)
+            n.append(int(round(cells)) * ratio)
+        fs = BlockSpec(n[0], n[1], n[2], uniform_faces(*box[0], n[0]), uniform_faces(*box[1], n[1]),
+                       uniform_faces(*box[2], n[2]), omega=omega, is_coarse=False)
+        if q == body:
+            c = np.array([0.5 * (box[a][0] + box[a][1]) for a in range(3)])
+            dxf = (box[0][1] - box[0][0]) / n[0]
+            if plate:
+                ax = np.array([0.4, 0.3, 0.1]) * diameter
+                fs.mesh = ellipsoid_plate(c, ax, 0.5 * dxf)
+                fs.search_box = search_box_for(fs, c - ax, c + ax)
+            else:
+                fs.mesh = fibonacci_sphere(c, diameter, dxf)
+                fs.search_box = search_box_for(fs, c - diameter / 2, c + diameter / 2)
+        blocks.append(fs)
+        ifs.append(InterfaceSpec(1, q + 2, 1, ratio, (box[0][0], box[0][1], box[1][0], box[1][1],
+                                                      box[2][0], box[2][1])))
+    rng = np.random.default_rng(seed)
+    dxf = d[0] / ratio
+    case = Case(name=f"multi_{len(blocks)}", blocks=blocks, interfaces=ifs, dt=0.3 * dxf,
+                re=reynolds / diameter, uc=1.0, epsi=1e-6, pc_ita_max=pc_ita_max, n_steps=n_steps)
+    case.init = [noisy_initial(b, case.uc, rng) for b in case.blocks]
+    return case
+
+
 def uniform_block(n=(384, 256, 256), lengths=(3.0, 2.0, 2.0), seed: int = SEED,
                   noise: bool = True) -> Case:
     """One body-free uniform block with the domain BCs (the coarse block of the

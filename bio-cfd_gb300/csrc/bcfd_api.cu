@@ -71,6 +71,35 @@ cudaError_t launch_coop(const void* fn, unsigned grid, unsigned block, void** ar
   return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
+int sync_block_table() {
+  Lib& L = lib();
+  const size_t n = L.blocks.size();
+  std::vector<DevBlock> cur(n);
+  for (size_t q = 0; q < n; ++q) {
+    if (L.blocks[q]) std::memcpy(&cur[q], &L.blocks[q]->d, sizeof(DevBlock));
+    else std::memset(&cur[q], 0, sizeof(DevBlock));
+  }
+  if (n > L.dtab_cap) {
+    if (L.dtab) cudaFree(L.dtab);
+    L.dtab = nullptr;
+    L.dtab_cap = 0;
+    BCFD_CUDA(cudaMalloc(&L.dtab, n * sizeof(DevBlock)));
+    L.dtab_cap = n;
+    L.htab.clear();
+    L.gen++;
+  }
+  if (cur.size() == L.htab.size() && std::memcmp(cur.data(), L.htab.data(), n * sizeof(DevBlock)) == 0)
+    return 0;
+  // a captured step must not contain this copy; the step key covers every
+  // block view, so a change always ends the capture first
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  BCFD_CUDA(cudaStreamIsCapturing(stream(), &cs));
+  if (cs != cudaStreamCaptureStatusNone) return BCFD_E_STATE;
+  L.htab = cur;
+  BCFD_CUDA(cudaMemcpyAsync(L.dtab, L.htab.data(), n * sizeof(DevBlock), cudaMemcpyHostToDevice, stream()));
+  return 0;
+}
+
 GridBar make_bar(int* err, unsigned nblocks) {
   GridBar g{};
   g.err = err;
@@ -469,6 +498,12 @@ int bcfd_init(int device) {
   return 0;
 }
 
+int bcfd_set_batching(int on) {
+  LOCK();
+  lib().batch = on != 0;
+  return 0;
+}
+
 int bcfd_finalize(void) {
   LOCK();
   Lib& L = lib();
@@ -490,6 +525,10 @@ int bcfd_finalize(void) {
       delete it;
     }
   L.blocks.clear();
+  if (L.dtab) cudaFree(L.dtab);
+  L.dtab = nullptr;
+  L.dtab_cap = 0;
+  L.htab.clear();
   L.ifs.clear();
   cudaStreamDestroy(L.s);
   L.s = nullptr;
@@ -589,6 +628,7 @@ int bcfd_block_create(int64_t nx, int64_t ny, int64_t nz, const double* x1, cons
   hb->dx = hb->dxa[1];
   hb->dy = hb->dya[1];
   hb->dz = hb->dza[1];
+  hb->index = (int)lib().blocks.size();
   lib().blocks.push_back(hb);
   *out = (bcfd_handle)lib().blocks.size();
   BCFD_CUDA(cudaStreamSynchronize(stream()));

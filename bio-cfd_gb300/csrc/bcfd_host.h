@@ -9,10 +9,12 @@
 #include <vector>
 
 #include "bcfd_internal.cuh"
+#include "bcfd_batch.cuh"
 
 namespace bcfd {
 
 struct HostBlock {
+  int index = -1;                  // registration order (device table slot)
   DevBlock d{};
   std::vector<void*> allocs;  // device allocations owned by the block
   // host copies of the 1-D grids (1-based meaning, v[i-1])
@@ -85,6 +87,11 @@ struct Lib {
   // bumped whenever a scratch buffer that captured kernels point at is
   // (re)allocated, so a captured step graph is rebuilt
   uint64_t gen = 0;
+  // device table of all blocks' views for batched launches
+  bool batch = true;                 // phases over several blocks in one launch
+  DevBlock* dtab = nullptr;
+  size_t dtab_cap = 0;
+  std::vector<DevBlock> htab;        // what the device table holds
   // captured time step (bcfd_run_steps with use_graph)
   cudaGraphExec_t step_graph = nullptr;
   std::vector<unsigned char> step_key;  // what the capture depends on
@@ -110,6 +117,16 @@ int take_block_error(HostBlock* hb);
 int launch_compute_div(HostBlock* hb);
 int launch_correct_pressure(HostBlock* hb);
 int launch_correct_velocity(HostBlock* hb, double dt);
+// the same phases over several blocks (one launch per phase when batching)
+int launch_compute_div(const std::vector<HostBlock*>& hbs);
+int launch_correct_pressure(const std::vector<HostBlock*>& hbs);
+int launch_correct_velocity(const std::vector<HostBlock*>& hbs, double dt);
+int launch_steady_state(const std::vector<HostBlock*>& hbs, double dt);
+int launch_max_div(const std::vector<HostBlock*>& hbs, bool tfield);
+int launch_copy_t_to_n(const std::vector<HostBlock*>& hbs);
+int launch_momentum(const std::vector<HostBlock*>& hbs, double dt, double re, bool fp32);
+int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double epsi, double res_tol);
+int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double div_tol);
 // res_tol > 0: stop on the FP64 residual dt*max|b/dt - A pc| <= res_tol
 int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol = 0.0);
 int launch_zero_poisson(HostBlock* hb);
@@ -151,5 +168,48 @@ int launch_fine_update_mv(HostInterface* it);
 // k_stress.cu
 int launch_stress(HostBlock* hb, double mu_f, double rho_f, double* out_host);
 int launch_stress_noalloc(HostBlock* hb, double mu_f, double rho_f, double* out_host);
+
+// Refresh the device table of block views (no copy when unchanged, so a
+// captured step contains none).
+int sync_block_table();
+
+enum class Extent { Interior, Points };
+
+inline int64_t op_cells(const HostBlock* hb, Extent e) {
+  const Dims& d = hb->d.d;
+  return e == Extent::Interior ? (int64_t)d.nx * d.ny * d.nz : d.npts();
+}
+
+// One phase operation over the given blocks: one launch per block, or, with
+// batching on and several blocks, one launch per group of up to kMaxBatch
+// blocks.  `cap` bounds the CTAs of one block.
+template <class Op, int NT>
+int launch_op(const std::vector<HostBlock*>& hbs, const Op& op, Extent ext, unsigned cap) {
+  if (hbs.empty()) return 0;
+  if (hbs.size() == 1 || !lib().batch) {
+    for (HostBlock* hb : hbs) {
+      k_one<Op, NT><<<grid_for(op_cells(hb, ext), NT, cap), NT, 0, stream()>>>(hb->d, op);
+      if (int r = note_launch()) return r;
+    }
+    return 0;
+  }
+  if (int r = sync_block_table()) return r;
+  for (size_t g0 = 0; g0 < hbs.size(); g0 += kMaxBatch) {
+    BlockSet S{};
+    S.tab = lib().dtab;
+    S.nb = (int)std::min<size_t>(kMaxBatch, hbs.size() - g0);
+    int grid = 0;
+    for (int m = 0; m < S.nb; ++m) {
+      const HostBlock* hb = hbs[g0 + m];
+      S.ids[m] = hb->index;
+      S.cta_off[m] = grid;
+      grid += (int)grid_for(op_cells(hb, ext), NT, cap);
+    }
+    S.cta_off[S.nb] = grid;
+    k_set<Op, NT><<<grid, NT, 0, stream()>>>(S, op);
+    if (int r = note_launch()) return r;
+  }
+  return 0;
+}
 
 }  // namespace bcfd

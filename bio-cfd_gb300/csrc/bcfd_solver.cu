@@ -159,40 +159,44 @@ int sor(HostBlock* hb, const SolveCfg& c) {
   return launch_sor(hb, c.itmax, c.dt, c.epsi);
 }
 
+// the same dispatch over several blocks (one batched launch when batching)
+int sor_set(const std::vector<HostBlock*>& v, const SolveCfg& c) {
+  if (c.precision == 1) return launch_sor_mixed_set(v, c.itmax, c.dt, c.div_tol);
+  if (c.precision == 2) return launch_sor_set(v, c.itmax, c.dt, c.epsi, c.div_tol);
+  return launch_sor_set(v, c.itmax, c.dt, c.epsi, 0.0);
+}
+
 // poissonSolver, src/PcorVcor.F90:22-220, over the blocks with 1-based
-// registration index in [start, finish] by step; no host round trip.
+// registration index in [start, finish] by step; no host round trip.  The
+// blocks are independent between the interface updates, so each per-block
+// phase runs over all of them at once (the reference's per-block loops of
+// :86-129 and :160-214 in one launch per phase).
 int poisson(const SolveCfg& c, int start, int finish, int step) {
   auto all = blocks();
   auto in = [&](bcfd_handle g) { return g >= start && g <= finish && (g - start) % step == 0; };
+  std::vector<HostBlock*> set, fine, first;
   for (auto& [g, hb] : all)
-    if (in(g)) TRY(launch_zero_poisson(hb));
+    if (in(g)) {
+      set.push_back(hb);
+      (g == 1 ? first : fine).push_back(hb);
+    }
+  for (HostBlock* hb : set) TRY(launch_zero_poisson(hb));
   TRY(fine_update_newv_bd());
   TRY(coarse_update_newv());
-  for (auto& [g, hb] : all)
-    if (in(g)) {
-      TRY(launch_compute_div(hb));
-      if (g != 1) TRY(sor(hb, c));
-    }
+  TRY(launch_compute_div(set));
+  TRY(sor_set(fine, c));
   TRY(coarse_update_pc());
-  for (auto& [g, hb] : all)
-    if (in(g) && g == 1) TRY(sor(hb, c));
+  TRY(sor_set(first, c));
   TRY(fine_update_pc_bd());
-  for (auto& [g, hb] : all)
-    if (in(g) && g != 1) TRY(sor(hb, c));
+  TRY(sor_set(fine, c));
   TRY(coarse_update_pc());
-  for (auto& [g, hb] : all)
-    if (in(g)) {
-      TRY(launch_correct_pressure(hb));
-      TRY(launch_correct_velocity(hb, c.dt));
-      // the divergence the solve leaves behind (measurement, not in the reference)
-      TRY(launch_max_div(hb, true));
-    }
-  for (auto& [g, hb] : all)
-    if (in(g) && g == 1) TRY(launch_velocity_bc(hb, c.dt, c.uc));
-  for (auto& [g, hb] : all)
-    if (in(g)) TRY(launch_steady_state(hb, c.dt));
-  for (auto& [g, hb] : all)
-    if (in(g)) TRY(launch_copy_t_to_n(hb));
+  TRY(launch_correct_pressure(set));
+  TRY(launch_correct_velocity(set, c.dt));
+  // the divergence the solve leaves behind (measurement, not in the reference)
+  TRY(launch_max_div(set, true));
+  for (HostBlock* hb : first) TRY(launch_velocity_bc(hb, c.dt, c.uc));
+  TRY(launch_steady_state(set, c.dt));
+  TRY(launch_copy_t_to_n(set));
   for (HostInterface* it : lib().ifs)
     if (it && get_block(it->b)) TRY(fine_update_bd_mv(it));
   TRY(coarse_update());
@@ -208,8 +212,11 @@ int poisson(const SolveCfg& c, int start, int finish, int step) {
 int step_once(const bcfd_step_config& cfg) {
   SolveCfg c{cfg.pc_ita_max, cfg.epsi, cfg.deltat, cfg.uc, cfg.precision, cfg.div_tol};
   auto all = blocks();
+  std::vector<HostBlock*> every;
+  for (auto& [g, hb] : all) every.push_back(hb);
+  // nsMomentum2order of every block in one launch (blocks are independent)
+  TRY(launch_momentum(every, cfg.deltat, cfg.re, cfg.precision == 1));
   for (auto& [g, hb] : all) {
-    TRY(launch_momentum(hb, cfg.deltat, cfg.re, cfg.precision == 1));
     if (hb->is_coarse) TRY(launch_velocity_bc(hb, cfg.deltat, cfg.uc));
     if (hb->has_body) {
       TRY(launch_solid_bc(hb, false));
@@ -259,6 +266,7 @@ std::vector<unsigned char> step_key(const bcfd_step_config& c) {
   put(&c.div_tol, sizeof c.div_tol);
   const Lib& L = lib();
   put(&L.gen, sizeof L.gen);
+  put(&L.batch, sizeof L.batch);
   for (const HostBlock* hb : L.blocks) {
     const unsigned char none = 0;
     if (!hb) { put(&none, 1); continue; }

@@ -335,21 +335,18 @@ __device__ __forceinline__ void momentum_cell(const DevBlock& B, const MomArgs& 
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128) k_momentum(DevBlock B, MomArgs a) {
-  const Dims& d = B.d;
-  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
-  const PlainReader rd{{B.u, B.v, B.w, B.p}};
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = 2 + (int)(t % d.nx);
-    const int64_t r = t / d.nx;
-    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
-    const int64_t c = d.idx(i, j, k);
-    if (B.cell[c] != 0) continue;
-    if (B.tsnear[c]) continue;  // done by k_momentum_ts
-    momentum_cell<T>(B, a, i, j, k, c, rd);
+struct MomentumOp {
+  MomArgs a;
+  __device__ void run(const DevBlock& B, int cta, int ncta) const {
+    const PlainReader rd{{B.u, B.v, B.w, B.p}};
+    FOR_INTERIOR(B, cta, ncta) {
+      INTERIOR_CELL(B);
+      if (B.cell[c] != 0) continue;
+      if (B.tsnear[c]) continue;  // done by MomentumTsOp
+      momentum_cell<T>(B, a, i, j, k, c, rd);
+    }
   }
-}
+};
 
 // ---------------------------------------------------------------------------
 // Thin-surface overlay.  Every position the reference substitutes or
@@ -488,16 +485,13 @@ __device__ void own_substitution(const DevBlock& B, int i, int j, int k, int nts
 }
 
 template <typename T>
-__global__ void __launch_bounds__(128) k_momentum_ts(DevBlock B, MomArgs a) {
+struct MomentumTsOp {
+  MomArgs a;
+  __device__ void run(const DevBlock& B, int cta, int ncta) const {
   const Dims& d = B.d;
-  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
   const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = 2 + (int)(t % d.nx);
-    const int64_t r = t / d.nx;
-    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
-    const int64_t c = d.idx(i, j, k);
+  FOR_INTERIOR(B, cta, ncta) {
+    INTERIOR_CELL(B);
     if (B.cell[c] != 0 || !B.tsnear[c]) continue;
     TsReader rd;
     rd.B = &B;
@@ -515,15 +509,17 @@ __global__ void __launch_bounds__(128) k_momentum_ts(DevBlock B, MomArgs a) {
     }
     momentum_cell<T>(B, a, i, j, k, c, rd);
   }
-}
+  }
+};
 
 // u,v,w,p at TS positions after the loop: the restore of the latest restorer
-__global__ void k_ts_restore(DevBlock B) {
+struct TsRestoreOp {
+  __device__ void run(const DevBlock& B, int cta, int ncta) const {
   const Dims& d = B.d;
   const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
   double rc[N_KIND];
   restore_consts(B, nts, rc);
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nts * N_KIND; t += gridDim.x * blockDim.x) {
+  for (int t = cta * blockDim.x + threadIdx.x; t < nts * N_KIND; t += ncta * blockDim.x) {
     const int nn = t / N_KIND, K = t % N_KIND;
     const int bt = B.ts_idx[nn] - 1;
     const int ti = B.ib_i[bt], tj = B.ib_j[bt], tk = B.ib_k[bt];
@@ -539,7 +535,8 @@ __global__ void k_ts_restore(DevBlock B) {
     double* f = q == 0 ? B.u : q == 1 ? B.v : q == 2 ? B.w : B.p;
     f[d.idx(xi, xj, xk)] = val;
   }
-}
+  }
+};
 
 // velocityBC loop 1 (x faces), src/BoundaryConditions.f90:16-40
 __global__ void k_vbc_x(DevBlock B, double deltat, double uc) {
@@ -618,25 +615,30 @@ __global__ void k_solid_bc(DevBlock B, int move) {
 
 }  // namespace
 
-int launch_momentum(HostBlock* hb, double dt, double re, bool fp32) {
-  const int64_t n = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-  if (fp32)
-    k_momentum<float><<<grid_for(n, 128, 1u << 20), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
-  else
-    k_momentum<double><<<grid_for(n, 128, 1u << 20), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
-  BCFD_LAUNCHED();
-  if (hb->has_body) {
-    // cells within reach of TS cells (none without surfaces 51/52), then the
-    // values the reference's loop leaves at the TS positions
-    if (fp32)
-      k_momentum_ts<float><<<grid_for(n, 128, 2048), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
-    else
-      k_momentum_ts<double><<<grid_for(n, 128, 2048), 128, 0, stream()>>>(hb->d, MomArgs{dt, re});
-    BCFD_LAUNCHED();
-    k_ts_restore<<<grid_for((int64_t)hb->d.cap_ib * 7, 128, 256), 128, 0, stream()>>>(hb->d);
+int launch_momentum(const std::vector<HostBlock*>& hbs, double dt, double re, bool fp32) {
+  const MomArgs a{dt, re};
+  const unsigned cap = 1u << 20;
+  if (fp32) TRY_R((launch_op<MomentumOp<float>, 128>(hbs, MomentumOp<float>{a}, Extent::Interior, cap)));
+  else TRY_R((launch_op<MomentumOp<double>, 128>(hbs, MomentumOp<double>{a}, Extent::Interior, cap)));
+  // cells within reach of TS cells (none without surfaces 51/52), then the
+  // values the reference's loop leaves at the TS positions
+  std::vector<HostBlock*> body;
+  for (HostBlock* hb : hbs)
+    if (hb->has_body) body.push_back(hb);
+  if (body.empty()) return 0;
+  if (fp32) TRY_R((launch_op<MomentumTsOp<float>, 128>(body, MomentumTsOp<float>{a}, Extent::Interior, 2048)));
+  else TRY_R((launch_op<MomentumTsOp<double>, 128>(body, MomentumTsOp<double>{a}, Extent::Interior, 2048)));
+  // up to 7 positions per TS cell: cap_ib * 7 items bound the grid
+  std::vector<HostBlock*> one(1);
+  for (HostBlock* hb : body) {
+    k_one<TsRestoreOp, 128><<<grid_for((int64_t)hb->d.cap_ib * 7, 128, 256), 128, 0, stream()>>>(hb->d, TsRestoreOp{});
     BCFD_LAUNCHED();
   }
   return 0;
+}
+
+int launch_momentum(HostBlock* hb, double dt, double re, bool fp32) {
+  return launch_momentum(std::vector<HostBlock*>{hb}, dt, re, fp32);
 }
 
 int launch_velocity_bc(HostBlock* hb, double dt, double uc) {

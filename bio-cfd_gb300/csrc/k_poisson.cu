@@ -30,22 +30,19 @@ struct RowMap {
 
 // computeDiv (src/PcorVcor.F90:222-243) over the fluid cells; b lands in the
 // packed layout.  Non-fluid cells keep the zero of the start of the solve.
-__global__ void k_div(DevBlock B) {
-  const Dims& d = B.d;
-  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = 2 + (int)(t % d.nx);
-    const int64_t r = t / d.nx;
-    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
-    const int64_t c = d.idx(i, j, k);
-    if (B.cell[c] != 0) continue;
-    const double bv = (B.ut[c] - B.ut[c - 1]) / B.dxa[i - 1] +
-                      (B.vt[c] - B.vt[c - d.NX]) / B.dya[j - 1] +
-                      (B.wt[c] - B.wt[c - (int64_t)d.NX * d.NY]) / B.dza[k - 1];
-    B.bpk[colour_of(i, j, k)][d.pidx(i, j, k)] = bv;
+struct DivOp {
+  __device__ void run(const DevBlock& B, int cta, int ncta) const {
+    const Dims& d = B.d;
+    FOR_INTERIOR(B, cta, ncta) {
+      INTERIOR_CELL(B);
+      if (B.cell[c] != 0) continue;
+      const double bv = (B.ut[c] - B.ut[c - 1]) / B.dxa[i - 1] +
+                        (B.vt[c] - B.vt[c - d.NX]) / B.dya[j - 1] +
+                        (B.wt[c] - B.wt[c - (int64_t)d.NX * d.NY]) / B.dza[k - 1];
+      B.bpk[colour_of(i, j, k)][d.pidx(i, j, k)] = bv;
+    }
   }
-}
+};
 
 // rhs = b / deltat, once per solve (the reference divides inside every sweep;
 // the quotient is the same IEEE value)
@@ -90,10 +87,10 @@ struct Tile {
   int a, b;            // tile coordinates
 };
 
-__device__ __forceinline__ Tile my_tile(const Dims& d, const TileMap& tm) {
+__device__ __forceinline__ Tile my_tile(const Dims& d, const TileMap& tm, int cta) {
   Tile t;
-  t.a = blockIdx.x % tm.ntj;
-  t.b = blockIdx.x / tm.ntj;
+  t.a = cta % tm.ntj;
+  t.b = cta / tm.ntj;
   t.j0 = 2 + t.a * tm.tj;
   t.k0 = 2 + t.b * tm.tk;
   t.nj = min(tm.tj, d.ny + 2 - t.j0);
@@ -314,9 +311,9 @@ __device__ __forceinline__ void log_solve(int64_t* log, int64_t sweeps, int64_t 
 // The three stop-test slots rotate: slot c % 3 collects check c; after the
 // grid barrier of check c every CTA has read check c-1, so slot (c+2) % 3 is
 // cleared for check c+2 by CTA 0.
-__device__ __forceinline__ double take_slot(BlockStats* st, int c) {
+__device__ __forceinline__ double take_slot(BlockStats* st, int c, int cta) {
   const double v = *((volatile double*)&st->slot[c % 3]);
-  if (blockIdx.x == 0 && threadIdx.x == 0) st->slot[(c + 2) % 3] = 0.0;
+  if (cta == 0 && threadIdx.x == 0) st->slot[(c + 2) % 3] = 0.0;
   return v;
 }
 
@@ -324,9 +321,12 @@ __device__ __forceinline__ double take_slot(BlockStats* st, int c) {
 // nIterPcor continues from stats->niter (the fine blocks accumulate it over
 // two solves per step, :78, :98, :116) and the stop test runs whenever the
 // accumulated count is a multiple of 5, exactly as the reference does.
-__global__ void __launch_bounds__(kSolveMaxThreads, 2) k_sor64(DevBlock B, SorArgs a, GridBar gb, TileMap tm) {
+// `cta` is this CTA's index among the block's CTAs (a batched launch runs
+// several blocks' solves side by side, each with its own barrier and tiles)
+__device__ __forceinline__ void sor64_body(const DevBlock& B, const SorArgs& a, const GridBar& gb,
+                                           const TileMap& tm, int cta) {
   __shared__ double sh[32];
-  const Tile t = my_tile(B.d, tm);
+  const Tile t = my_tile(B.d, tm, cta);
   BlockStats* st = B.stats;
   const int64_t it0 = st->niter;
   // every CTA has read niter before CTA 0 may rewrite it at the end
@@ -357,13 +357,13 @@ __global__ void __launch_bounds__(kSolveMaxThreads, 2) k_sor64(DevBlock B, SorAr
       const double m = block_max(lmax, sh);
       if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[check % 3], m);
       if (!grid_sync(gb)) { ok = false; break; }
-      derr4 = take_slot(st, check);
+      derr4 = take_slot(st, check, cta);
       ++check;
     }
     if (a.res_tol > 0.0 ? (derr4 <= a.res_tol) : (derr4 < a.epsi)) break;
     if (it > a.itmax) break;
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (cta == 0 && threadIdx.x == 0) {
     log_solve(a.log, it - it0, 0, B.cnt[C_FLUID], 0);
     st->niter = it;
     st->derr2 = derr4;
@@ -543,9 +543,10 @@ __device__ __forceinline__ void tile_apply4(const DevBlock& B, const Tile& t) {
   }
 }
 
-__global__ void __launch_bounds__(kDcThreads, 3) k_sor_dc(DevBlock B, DcArgs a, GridBar gb, TileMap tm) {
+__device__ __forceinline__ void sor_dc_body(const DevBlock& B, const DcArgs& a, const GridBar& gb,
+                                            const TileMap& tm, int cta) {
   __shared__ double sh[32];
-  const Tile t = my_tile(B.d, tm);
+  const Tile t = my_tile(B.d, tm, cta);
   BlockStats* st = B.stats;
   int64_t sweeps = 0;
   double res = 0.0;
@@ -558,7 +559,7 @@ __global__ void __launch_bounds__(kDcThreads, 3) k_sor_dc(DevBlock B, DcArgs a, 
     m = block_max(m, sh);
     if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[outer % 3], m);
     if (!grid_sync(gb)) return;
-    res = take_slot(st, outer);
+    res = take_slot(st, outer, cta);
     if (a.dt * res <= a.div_tol || outer >= a.max_outer || !(res == res)) break;
     for (int it = 0; it < a.inner; ++it) {
       if (!tile_wait(tm, gb, t, ph)) return;
@@ -574,13 +575,67 @@ __global__ void __launch_bounds__(kDcThreads, 3) k_sor_dc(DevBlock B, DcArgs a, 
     tile_apply4<0>(B, t);
     tile_publish(tm, t, ++ph);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (cta == 0 && threadIdx.x == 0) {
     log_solve(a.log, sweeps, outer + 1, B.cnt[C_FLUID], 1);
     st->niter = st->niter + sweeps;
     st->derr2 = a.dt * res;
     st->pad[1] = a.dt * res;  // the residual this solve leaves behind
     if (!(res == res)) set_err(B.err, BCFD_E_NONFINITE);
   }
+}
+
+__global__ void __launch_bounds__(kSolveMaxThreads, 2) k_sor64(DevBlock B, SorArgs a, GridBar gb, TileMap tm) {
+  sor64_body(B, a, gb, tm, (int)blockIdx.x);
+}
+
+__global__ void __launch_bounds__(kDcThreads, 3) k_sor_dc(DevBlock B, DcArgs a, GridBar gb, TileMap tm) {
+  sor_dc_body(B, a, gb, tm, (int)blockIdx.x);
+}
+
+// Several blocks' solves in one cooperative launch: member m owns CTAs
+// [cta0, cta0 + its tile count) and has its own barrier, tiles and slots.
+constexpr int kMaxSolveBatch = 16;
+template <class Args>
+struct SolveEntry {
+  Args a;
+  GridBar gb;
+  TileMap tm;
+  int id;    // device table index
+  int cta0;  // first CTA
+};
+template <class Args>
+struct SolveSet {
+  const DevBlock* tab;
+  int nb;
+  SolveEntry<Args> e[kMaxSolveBatch];
+};
+
+template <class Args>
+__device__ __forceinline__ int solve_member(const SolveSet<Args>& S) {
+  int m = 0;
+  for (int q = 1; q < S.nb; ++q)
+    if (S.e[q].cta0 <= (int)blockIdx.x) m = q;
+  return m;
+}
+
+__global__ void __launch_bounds__(kSolveMaxThreads, 2) k_sor64_set(SolveSet<SorArgs> S) {
+  __shared__ unsigned long long raw[(sizeof(DevBlock) + 7) / 8];
+  const int m = solve_member(S);
+  BlockSet bs;
+  bs.tab = S.tab;
+  bs.ids[0] = S.e[m].id;
+  const DevBlock& B = stage_block(bs, 0, raw);
+  sor64_body(B, S.e[m].a, S.e[m].gb, S.e[m].tm, (int)blockIdx.x - S.e[m].cta0);
+}
+
+__global__ void __launch_bounds__(kDcThreads, 3) k_sor_dc_set(SolveSet<DcArgs> S) {
+  __shared__ unsigned long long raw[(sizeof(DevBlock) + 7) / 8];
+  const int m = solve_member(S);
+  BlockSet bs;
+  bs.tab = S.tab;
+  bs.ids[0] = S.e[m].id;
+  const DevBlock& B = stage_block(bs, 0, raw);
+  sor_dc_body(B, S.e[m].a, S.e[m].gb, S.e[m].tm, (int)blockIdx.x - S.e[m].cta0);
 }
 
 // dt * max over fluid cells of |b/dt - A pc| (FP64, measurement) -> stats->pad[1]
@@ -593,98 +648,92 @@ __global__ void k_resid(DevBlock B, double dt) {
 }
 
 // correctPressure (src/PcorVcor.F90:245-259)
-__global__ void k_correct_p(DevBlock B) {
-  const Dims& d = B.d;
-  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = 2 + (int)(t % d.nx);
-    const int64_t r = t / d.nx;
-    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
-    const int64_t c = d.idx(i, j, k);
-    if (B.cell[c] != 0) continue;
-    B.p[c] = B.p[c] + B.pc[colour_of(i, j, k)][d.pidx(i, j, k)];
+struct CorrectPOp {
+  __device__ void run(const DevBlock& B, int cta, int ncta) const {
+    const Dims& d = B.d;
+    FOR_INTERIOR(B, cta, ncta) {
+      INTERIOR_CELL(B);
+      if (B.cell[c] != 0) continue;
+      B.p[c] = B.p[c] + B.pc[colour_of(i, j, k)][d.pidx(i, j, k)];
+    }
   }
-}
+};
 
 __device__ __forceinline__ double pc_at(const DevBlock& B, int i, int j, int k) {
   return B.pc[colour_of(i, j, k)][B.d.pidx(i, j, k)];
 }
 
 // correctVelocity (src/PcorVcor.F90:261-286)
-__global__ void k_correct_v(DevBlock B, double dt) {
-  const Dims& d = B.d;
-  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = 2 + (int)(t % d.nx);
-    const int64_t r = t / d.nx;
-    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
-    const int64_t c = d.idx(i, j, k);
-    if (B.cell[c] != 0) continue;
-    const double p0 = pc_at(B, i, j, k);
-    B.ut[c] = B.ut[c] - dt / (0.5 * (B.dxa[i] + B.dxa[i - 1])) * (pc_at(B, i + 1, j, k) - p0);
-    B.vt[c] = B.vt[c] - dt / (0.5 * (B.dya[j] + B.dya[j - 1])) * (pc_at(B, i, j + 1, k) - p0);
-    B.wt[c] = B.wt[c] - dt / (0.5 * (B.dza[k] + B.dza[k - 1])) * (pc_at(B, i, j, k + 1) - p0);
+struct CorrectVOp {
+  double dt;
+  __device__ void run(const DevBlock& B, int cta, int ncta) const {
+    FOR_INTERIOR(B, cta, ncta) {
+      INTERIOR_CELL(B);
+      if (B.cell[c] != 0) continue;
+      const double p0 = pc_at(B, i, j, k);
+      B.ut[c] = B.ut[c] - dt / (0.5 * (B.dxa[i] + B.dxa[i - 1])) * (pc_at(B, i + 1, j, k) - p0);
+      B.vt[c] = B.vt[c] - dt / (0.5 * (B.dya[j] + B.dya[j - 1])) * (pc_at(B, i, j + 1, k) - p0);
+      B.wt[c] = B.wt[c] - dt / (0.5 * (B.dza[k] + B.dza[k - 1])) * (pc_at(B, i, j, k + 1) - p0);
+    }
   }
-}
+};
 
 // steady-state error max |ut - u| / dt over the fluid cells (src/PcorVcor.F90:135-153)
-__global__ void k_steady(DevBlock B, double dt) {
-  __shared__ double sh[32];
-  const Dims& d = B.d;
-  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
-  double m = 0.0;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = 2 + (int)(t % d.nx);
-    const int64_t r = t / d.nx;
-    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
-    const int64_t c = d.idx(i, j, k);
-    if (B.cell[c] != 0) continue;
-    const double eu = fabs((B.ut[c] - B.u[c])) / dt;
-    const double ev = fabs((B.vt[c] - B.v[c])) / dt;
-    const double ew = fabs((B.wt[c] - B.w[c])) / dt;
-    m = fmax(fmax(fmax(m, eu), ev), ew);
+struct SteadyOp {
+  double dt;
+  __device__ void run(const DevBlock& B, int cta, int ncta) const {
+    __shared__ double sh[32];
+    double m = 0.0;
+    FOR_INTERIOR(B, cta, ncta) {
+      INTERIOR_CELL(B);
+      if (B.cell[c] != 0) continue;
+      const double eu = fabs((B.ut[c] - B.u[c])) / dt;
+      const double ev = fabs((B.vt[c] - B.v[c])) / dt;
+      const double ew = fabs((B.wt[c] - B.w[c])) / dt;
+      m = fmax(fmax(fmax(m, eu), ev), ew);
+    }
+    m = block_max(m, sh);
+    if (threadIdx.x == 0) atomic_max_nonneg(&B.stats->derr_std_st, m);
   }
-  m = block_max(m, sh);
-  if (threadIdx.x == 0) atomic_max_nonneg(&B.stats->derr_std_st, m);
-}
+};
 
 // max |div| over the fluid cells of (u,v,w) (slot maxdiv) or, right after
-// the velocity correction, of (ut,vt,wt) (slot derr_pad[0]); FP64
-__global__ void k_maxdiv(DevBlock B, int tfield) {
-  __shared__ double sh[32];
-  const Dims& d = B.d;
-  const double* U = tfield ? B.ut : B.u;
-  const double* V = tfield ? B.vt : B.v;
-  const double* W = tfield ? B.wt : B.w;
-  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
-  double m = 0.0;
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int i = 2 + (int)(t % d.nx);
-    const int64_t r = t / d.nx;
-    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
-    const int64_t c = d.idx(i, j, k);
-    if (B.cell[c] != 0) continue;
-    const double dv = (U[c] - U[c - 1]) / B.dxa[i - 1] + (V[c] - V[c - d.NX]) / B.dya[j - 1] +
-                      (W[c] - W[c - (int64_t)d.NX * d.NY]) / B.dza[k - 1];
-    m = fmax(m, fabs(dv));
+// the velocity correction, of (ut,vt,wt) (slot pad[0]); FP64
+struct MaxDivOp {
+  int tfield;
+  __device__ void run(const DevBlock& B, int cta, int ncta) const {
+    __shared__ double sh[32];
+    const Dims& d = B.d;
+    const double* U = tfield ? B.ut : B.u;
+    const double* V = tfield ? B.vt : B.v;
+    const double* W = tfield ? B.wt : B.w;
+    double m = 0.0;
+    FOR_INTERIOR(B, cta, ncta) {
+      INTERIOR_CELL(B);
+      if (B.cell[c] != 0) continue;
+      const double dv = (U[c] - U[c - 1]) / B.dxa[i - 1] + (V[c] - V[c - d.NX]) / B.dya[j - 1] +
+                        (W[c] - W[c - (int64_t)d.NX * d.NY]) / B.dza[k - 1];
+      m = fmax(m, fabs(dv));
+    }
+    m = block_max(m, sh);
+    if (threadIdx.x == 0) atomic_max_nonneg(tfield ? &B.stats->pad[0] : &B.stats->maxdiv, m);
   }
-  m = block_max(m, sh);
-  if (threadIdx.x == 0) atomic_max_nonneg(tfield ? &B.stats->pad[0] : &B.stats->maxdiv, m);
-}
+};
 
-__global__ void k_copy3(double* a, double* b, double* c, const double* x, const double* y,
-                        const double* z, int64_t n) {
-  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    a[t] = x[t];
-    b[t] = y[t];
-    c[t] = z[t];
+// u <- ut (to_n) or ut <- u over every point (src/PcorVcor.F90:212-214, 379-397)
+struct CopyOp {
+  int to_n;
+  __device__ void run(const DevBlock& B, int cta, int ncta) const {
+    const int64_t n = B.d.npts();
+    double *a = to_n ? B.u : B.ut, *b = to_n ? B.v : B.vt, *e = to_n ? B.w : B.wt;
+    const double *x = to_n ? B.ut : B.u, *y = to_n ? B.vt : B.v, *z = to_n ? B.wt : B.w;
+    for (int64_t t = (int64_t)cta * blockDim.x + threadIdx.x; t < n; t += (int64_t)ncta * blockDim.x) {
+      a[t] = x[t];
+      b[t] = y[t];
+      e[t] = z[t];
+    }
   }
-}
+};
 
 // SOR update masks from the cell tags (the red/black lists of cellCount_solid)
 __global__ void k_masks(DevBlock B) {
@@ -727,25 +776,23 @@ __global__ void k_unpack(DevBlock B, const double* p0, const double* p1, double*
 
 }  // namespace
 
-int launch_compute_div(HostBlock* hb) {
-  const int64_t n = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-  k_div<<<grid_for(n, 256), 256, 0, stream()>>>(hb->d);
-  BCFD_LAUNCHED();
-  return 0;
-}
+constexpr unsigned kCellCap = 152u * 32u;
 
-int launch_correct_pressure(HostBlock* hb) {
-  const int64_t n = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-  k_correct_p<<<grid_for(n, 256), 256, 0, stream()>>>(hb->d);
-  BCFD_LAUNCHED();
-  return 0;
+int launch_compute_div(const std::vector<HostBlock*>& hbs) {
+  return launch_op<DivOp, 256>(hbs, DivOp{}, Extent::Interior, kCellCap);
 }
+int launch_compute_div(HostBlock* hb) { return launch_compute_div(std::vector<HostBlock*>{hb}); }
 
+int launch_correct_pressure(const std::vector<HostBlock*>& hbs) {
+  return launch_op<CorrectPOp, 256>(hbs, CorrectPOp{}, Extent::Interior, kCellCap);
+}
+int launch_correct_pressure(HostBlock* hb) { return launch_correct_pressure(std::vector<HostBlock*>{hb}); }
+
+int launch_correct_velocity(const std::vector<HostBlock*>& hbs, double dt) {
+  return launch_op<CorrectVOp, 256>(hbs, CorrectVOp{dt}, Extent::Interior, kCellCap);
+}
 int launch_correct_velocity(HostBlock* hb, double dt) {
-  const int64_t n = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-  k_correct_v<<<grid_for(n, 256), 256, 0, stream()>>>(hb->d, dt);
-  BCFD_LAUNCHED();
-  return 0;
+  return launch_correct_velocity(std::vector<HostBlock*>{hb}, dt);
 }
 
 int launch_zero_poisson(HostBlock* hb) {
@@ -769,11 +816,9 @@ static int launch_residual(HostBlock* hb, double dt) {
 
 // Tiles for a tiled persistent solve: the smallest tiles (most CTAs) whose
 // count fits the co-resident capacity of `fn`, squarest among equal areas.
-static TileMap choose_tiles(HostBlock* hb, const void* fn, int threads, int global) {
+static TileMap tiles_within(HostBlock* hb, unsigned cap, int global) {
   const Dims& d = hb->d.d;
-  unsigned cap = coop_grid(fn, threads, 0, 0xffffffffu);
-  if (hb->solve_ctas_per_sm > 0) cap = std::min<unsigned>(cap, (unsigned)(hb->solve_ctas_per_sm * num_sms()));
-  cap = std::min<unsigned>(cap, kMaxTiles);
+  cap = std::max(1u, std::min<unsigned>(cap, kMaxTiles));
   TileMap best{d.ny, d.nz, 1, 1, hb->prog, global};
   long barea = (long)d.ny * d.nz, bper = d.ny + d.nz;
   for (int tk = 1; tk <= d.nz; ++tk) {
@@ -790,6 +835,12 @@ static TileMap choose_tiles(HostBlock* hb, const void* fn, int threads, int glob
     }
   }
   return best;
+}
+
+static TileMap choose_tiles(HostBlock* hb, const void* fn, int threads, int global) {
+  unsigned cap = coop_grid(fn, threads, 0, 0xffffffffu);
+  if (hb->solve_ctas_per_sm > 0) cap = std::min<unsigned>(cap, (unsigned)(hb->solve_ctas_per_sm * num_sms()));
+  return tiles_within(hb, cap, global);
 }
 
 // zeroed progress counters, stop-test slots and barrier word for one launch
@@ -860,37 +911,137 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   return 0;
 }
 
-int launch_steady_state(HostBlock* hb, double dt) {
-  const int64_t n = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-  BCFD_CUDA(cudaMemsetAsync(&hb->d.stats->derr_std_st, 0, sizeof(double), stream()));
-  k_steady<<<grid_for(n, 256, 1024), 256, 0, stream()>>>(hb->d, dt);
-  BCFD_LAUNCHED();
+// One cooperative launch for the solves of several blocks (batching on, more
+// than one block): the co-resident CTAs are shared out in proportion to the
+// blocks' cell counts; each block keeps its own tiles, barrier and slots.
+// make(hb, args) fills a block's arguments; returns nonzero to solve that
+// block alone (then solo(hb) runs).
+template <class Args, class Make, class Solo>
+static int launch_solve_set(const std::vector<HostBlock*>& hbs, const void* fn, int threads, int global,
+                            Make make, Solo solo) {
+  std::vector<HostBlock*> group;
+  for (HostBlock* hb : hbs) {
+    Args a{};
+    if (make(hb, a)) TRY_R(solo(hb));
+    else group.push_back(hb);
+  }
+  if (group.size() == 1 || (!group.empty() && !lib().batch)) {
+    for (HostBlock* hb : group) TRY_R(solo(hb));
+    return 0;
+  }
+  if (group.empty()) return 0;
+  TRY_R(sync_block_table());
+  const unsigned cap_all = std::min<unsigned>(coop_grid(fn, threads, 0, 0xffffffffu), 0x7fffffffu);
+  for (size_t g0 = 0; g0 < group.size(); g0 += kMaxSolveBatch) {
+    const int nb = (int)std::min<size_t>(kMaxSolveBatch, group.size() - g0);
+    double cells = 0;
+    for (int m = 0; m < nb; ++m) {
+      const Dims& d = group[g0 + m]->d.d;
+      cells += (double)d.nx * d.ny * d.nz;
+    }
+    SolveSet<Args> S{};
+    S.tab = lib().dtab;
+    S.nb = nb;
+    unsigned grid = 0;
+    // every member needs at least one CTA: share what is left after that
+    const unsigned spare = cap_all > (unsigned)nb ? cap_all - (unsigned)nb : 0u;
+    for (int m = 0; m < nb; ++m) {
+      HostBlock* hb = group[g0 + m];
+      const Dims& d = hb->d.d;
+      unsigned cap = 1u + (unsigned)(spare * ((double)d.nx * d.ny * d.nz / cells));
+      if (hb->solve_ctas_per_sm > 0) cap = std::min<unsigned>(cap, (unsigned)(hb->solve_ctas_per_sm * num_sms()));
+      TileMap tm = tiles_within(hb, cap, global);
+      TRY_R(reset_solve_state(hb, tm));
+      SolveEntry<Args>& e = S.e[m];
+      make(hb, e.a);
+      e.tm = tm;
+      e.gb = make_bar(hb->d.err, (unsigned)(tm.ntj * tm.ntk));
+      e.gb.ctr = reinterpret_cast<unsigned long long*>(hb->bar);
+      e.id = hb->index;
+      e.cta0 = (int)grid;
+      grid += (unsigned)(tm.ntj * tm.ntk);
+    }
+    void* args[] = {(void*)&S};
+    prof_mark(true);
+    BCFD_CUDA(launch_coop(fn, grid, threads, args));
+    prof_mark(false);
+    BCFD_LAUNCHED();
+  }
   return 0;
 }
 
-int launch_max_div(HostBlock* hb, bool tfield) {
-  const int64_t n = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-  double* slot = tfield ? &hb->d.stats->pad[0] : &hb->d.stats->maxdiv;
-  BCFD_CUDA(cudaMemsetAsync(slot, 0, sizeof(double), stream()));
-  k_maxdiv<<<grid_for(n, 256, 1024), 256, 0, stream()>>>(hb->d, tfield ? 1 : 0);
-  BCFD_LAUNCHED();
+int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double epsi, double res_tol) {
+  if (hbs.size() <= 1 || !lib().batch) {
+    for (HostBlock* hb : hbs) TRY_R(launch_sor(hb, itmax, dt, epsi, res_tol));
+    return 0;
+  }
+  const int threads = 512;
+  for (HostBlock* hb : hbs) {
+    k_rhs<<<grid_for(hb->d.d.npacked(), 256), 256, 0, stream()>>>(hb->d, dt);
+    BCFD_LAUNCHED();
+  }
+  auto make = [&](HostBlock* hb, SorArgs& a) -> int {
+    a = SorArgs{itmax, epsi, hb->omega, prof_log(), res_tol, dt};
+    // blocks with their own launch shape keep their own launch
+    return hb->solve_threads > 0 || hb->solve_sync != 0;
+  };
+  // a block solved alone goes through launch_sor (which recomputes b/dt)
+  auto solo = [&](HostBlock* hb) -> int { return launch_sor(hb, itmax, dt, epsi, res_tol); };
+  TRY_R(launch_solve_set<SorArgs>(hbs, (const void*)k_sor64_set, threads, 0, make, solo));
+  for (HostBlock* hb : hbs) TRY_R(launch_residual(hb, dt));
   return 0;
 }
 
-int launch_copy_t_to_n(HostBlock* hb) {
-  const int64_t n = hb->d.d.npts();
-  k_copy3<<<grid_for(n, 256), 256, 0, stream()>>>(hb->d.u, hb->d.v, hb->d.w, hb->d.ut, hb->d.vt,
-                                                   hb->d.wt, n);
-  BCFD_LAUNCHED();
-  return 0;
+int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double div_tol) {
+  if (hbs.size() <= 1 || !lib().batch) {
+    for (HostBlock* hb : hbs) TRY_R(launch_sor_mixed(hb, itmax, dt, div_tol));
+    return 0;
+  }
+  const int threads = kDcThreads;
+  for (HostBlock* hb : hbs) {
+    if (hb->dc_variant == 2 || hb->solve_threads > 0) continue;
+    for (int c = 0; c < 2; ++c)
+      BCFD_CUDA(cudaMemsetAsync(hb->d.pcf[c], 0, hb->d.d.npacked() * sizeof(float), stream()));
+  }
+  auto make = [&](HostBlock* hb, DcArgs& a) -> int {
+    const Dims& d = hb->d.d;
+    const int nmax = std::max(d.nx, std::max(d.ny, d.nz));
+    a.inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
+    const double om = hb->dc_omega > 0 ? hb->dc_omega : 2.0 / (1.0 + std::sin(3.14159265358979323846 / nmax));
+    a.omega = (float)std::min(1.97, std::max(1.0, om));
+    a.max_outer = itmax / a.inner + 1;
+    a.dt = dt;
+    a.inv_dt = 1.0 / dt;
+    a.div_tol = div_tol;
+    a.log = prof_log();
+    return hb->dc_variant == 2 || hb->dc_variant == 3 || hb->solve_threads > 0;
+  };
+  auto solo = [&](HostBlock* hb) -> int { return launch_sor_mixed(hb, itmax, dt, div_tol); };
+  return launch_solve_set<DcArgs>(hbs, (const void*)k_sor_dc_set, threads, 1, make, solo);
 }
 
+int launch_steady_state(const std::vector<HostBlock*>& hbs, double dt) {
+  for (HostBlock* hb : hbs)
+    BCFD_CUDA(cudaMemsetAsync(&hb->d.stats->derr_std_st, 0, sizeof(double), stream()));
+  return launch_op<SteadyOp, 256>(hbs, SteadyOp{dt}, Extent::Interior, 1024);
+}
+int launch_steady_state(HostBlock* hb, double dt) { return launch_steady_state(std::vector<HostBlock*>{hb}, dt); }
+
+int launch_max_div(const std::vector<HostBlock*>& hbs, bool tfield) {
+  for (HostBlock* hb : hbs) {
+    double* slot = tfield ? &hb->d.stats->pad[0] : &hb->d.stats->maxdiv;
+    BCFD_CUDA(cudaMemsetAsync(slot, 0, sizeof(double), stream()));
+  }
+  return launch_op<MaxDivOp, 256>(hbs, MaxDivOp{tfield ? 1 : 0}, Extent::Interior, 1024);
+}
+int launch_max_div(HostBlock* hb, bool tfield) { return launch_max_div(std::vector<HostBlock*>{hb}, tfield); }
+
+int launch_copy_t_to_n(const std::vector<HostBlock*>& hbs) {
+  return launch_op<CopyOp, 256>(hbs, CopyOp{1}, Extent::Points, kCellCap);
+}
+int launch_copy_t_to_n(HostBlock* hb) { return launch_copy_t_to_n(std::vector<HostBlock*>{hb}); }
 int launch_copy_n_to_t(HostBlock* hb) {
-  const int64_t n = hb->d.d.npts();
-  k_copy3<<<grid_for(n, 256), 256, 0, stream()>>>(hb->d.ut, hb->d.vt, hb->d.wt, hb->d.u, hb->d.v,
-                                                   hb->d.w, n);
-  BCFD_LAUNCHED();
-  return 0;
+  return launch_op<CopyOp, 256>(std::vector<HostBlock*>{hb}, CopyOp{0}, Extent::Points, kCellCap);
 }
 
 int launch_update_masks(HostBlock* hb) {

@@ -52,6 +52,11 @@ int bcfd_get_stream(void** stream);
 const char* bcfd_status_string(int status);
 /* number of kernels this library has launched since bcfd_init */
 int64_t bcfd_kernel_launches(void);
+/* 1 (default): the per-block phases of a time step (momentum, divergence,
+ * corrections, reductions, copies, and the Poisson solves of the blocks that
+ * are solved together) run over all blocks in one launch per phase, driven by
+ * a device table of block views; 0: one launch per block.  Same results. */
+int bcfd_set_batching(int on);
 
 /* ---- block registration and host mirrors (src/Blocks.f90:13-81) --------- */
 /* Allocates the per-block device arrays of src/AllocateArrays.f90:15-57 and

@@ -143,7 +143,9 @@ class Oracle:
         for it in case.interfaces:
             L.orc_interface_new(it.a_blk, it.b_blk, it.a_msh, it.b_msh, *it.box)
         for g, spec in enumerate(case.blocks, 1):
-            if spec.has_body:
+            # app/main.F90:80-85: every block g /= 1 is tagged and counted (a
+            # block without a surface is all fluid)
+            if spec.has_body or (g != 1 and case.interfaces):
                 L.orc_tagging_th_core(g)
                 L.orc_cellcount_solid(g)
         if case.interfaces and not case.blocks[0].has_body:

@@ -226,6 +226,52 @@ def sweep_roofline(torch, local, hbm, block=(384, 256, 256), fp32_pairs=40, fp64
     return out
 
 
+def twelve_block(torch, local, steps=10, warmup=3, fp64_steps=2):
+    """Twelve uneven blocks (coarse 256x192x192 + 11 fine blocks, 13.3M cells,
+    stationary thin plate): mixed-path time per step with the batched launches
+    and with one launch per block, and the plain FP64 path to the same residual.
+    The working set (> 2 GB) is far above L2, so no flush is needed."""
+    from biocfd import synth
+    from biocfd.solver import Solver
+    case = synth.twelve_block(n_steps=steps + warmup + 2)
+    out = {"workload": "12 blocks: coarse 256x192x192 over 8x6x6 + 11 fine blocks at ratio 2 "
+                       "(160x96x96 with a plate 0.5x0.125x0.0125, 2x128x64x64, 2x96x64x64, "
+                       "2x64x48x48, 2x48^3, 2x32^3), 13.3M cells, Re 500",
+           "div_tol": DIV_TOL}
+    arms = (("mixed_batched", 1, True, steps), ("mixed_per_block", 1, False, steps),
+            ("fp64_batched", 2, True, fp64_steps))
+    for key, prec, batching, n in arms:
+        if n <= 0:
+            continue
+        s = Solver(case, device=local)
+        s.set_batching(batching)
+        s.setup()
+        stream = torch.cuda.ExternalStream(s.stream_ptr())
+        for _ in range(warmup if prec == 1 else 1):
+            s.run(1, precision=prec, div_tol=DIV_TOL, use_graph=1)
+        ts = []
+        k0 = s.kernel_launches()
+        for _ in range(n):
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.run(1, precision=prec, div_tol=DIV_TOL, use_graph=1)
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        res = max(s.divergence(g)[1] for g in s.handles)
+        ms = statistics.mean(ts)
+        out[key] = {"ms_per_step": ms, "steps_per_s": 1000.0 / ms, "steps": n, "div_residual": res,
+                    "launches_per_step": (s.kernel_launches() - k0) / n,
+                    "cell_updates_per_s": 13328384 * 1000.0 / ms}
+        s.close()
+    if "fp64_batched" in out:
+        out["speedup_mixed_vs_fp64"] = out["fp64_batched"]["ms_per_step"] / out["mixed_batched"]["ms_per_step"]
+    out["speedup_batched_vs_per_block"] = (out["mixed_per_block"]["ms_per_step"] /
+                                           out["mixed_batched"]["ms_per_step"])
+    return out
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -342,6 +388,8 @@ def run_gpu(args):
     }
     if not args.no_sweep_roofline:
         line["sweep_roofline"] = sweep_roofline(torch, local, hbm)
+    if not args.no_twelve_block:
+        line["twelve_block"] = twelve_block(torch, local)
     if rank == 0 and not args.no_cpu_baseline:
         sps, secs = oracle_steps(case, 1)
         line["cpu_baseline"] = {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
@@ -359,11 +407,18 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sweep-roofline", action="store_true")
+    ap.add_argument("--no-twelve-block", action="store_true")
+    ap.add_argument("--twelve-only", action="store_true",
+                    help="only the twelve-block measurement (batched vs per-block launches)")
     ap.add_argument("--mixed-only", action="store_true",
                     help="time only the flagship arm and print a short line (profiler captures)")
     ap.add_argument("--sweep-only", default="",
                     help="nx,ny,nz[,fp32_pairs[,fp64_pairs]]: only the Poisson sweep measurement on that block")
     args = ap.parse_args()
+    if args.twelve_only:
+        import torch
+        print(json.dumps(twelve_block(torch, 0, args.steps, args.warmup)), flush=True)
+        return
     if args.sweep_only:
         import torch
         v = [int(x) for x in args.sweep_only.split(",")]

@@ -262,7 +262,8 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
                             ((1.5, 2.25), (0.75, 1.25), (1.0, 1.5)),
                             ((2.375, 2.75), (1.0, 1.5), (0.375, 0.75))),
                 body: int = 0, diameter: float = 0.25, reynolds: float = 300.0, n_steps: int = 2,
-                omega: float = 1.7, pc_ita_max: int = 5000, seed: int = SEED, plate: bool = False) -> Case:
+                omega: float = 1.7, pc_ita_max: int = 5000, seed: int = SEED, plate: bool = False,
+                plate_axes=None) -> Case:
     """A coarse block with several nested fine blocks of uneven sizes at ratio 2
     (one interface per fine block), a stationary sphere (or, with `plate`, a
     thin plate of surface 51) in fine block `body`.  Box edges must lie on
@@ -286,7 +287,7 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
             c = np.array([0.5 * (box[a][0] + box[a][1]) for a in range(3)])
             dxf = (box[0][1] - box[0][0]) / n[0]
             if plate:
-                ax = np.array([0.4, 0.3, 0.1]) * diameter
+                ax = np.array([0.4, 0.3, 0.1]) * diameter if plate_axes is None else np.asarray(plate_axes)
                 fs.mesh = ellipsoid_plate(c, ax, 0.5 * dxf)
                 fs.search_box = search_box_for(fs, c - ax, c + ax)
             else:
@@ -301,6 +302,32 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
                 re=reynolds / diameter, uc=1.0, epsi=1e-6, pc_ita_max=pc_ita_max, n_steps=n_steps)
     case.init = [noisy_initial(b, case.uc, rng) for b in case.blocks]
     return case
+
+
+# the 12-block layout: a coarse 256x192x192 block over 8x6x6 (dx 1/32) with 11
+# fine blocks at ratio 2 in the sizes 160x96x96, 128x64x64, 96x64x64,
+# 64x48x48, 48^3, 32^3 and repeats of the last five (13.3M cells in all)
+TWELVE_BLOCK_BOXES = (
+    ((0.5, 3.0), (0.5, 2.0), (0.5, 2.0)),      # 160x96x96, holds the plate
+    ((3.5, 5.5), (0.5, 1.5), (0.5, 1.5)),      # 128x64x64
+    ((6.0, 7.5), (0.5, 1.5), (0.5, 1.5)),      # 96x64x64
+    ((3.5, 4.5), (2.0, 2.75), (0.5, 1.25)),    # 64x48x48
+    ((5.0, 5.75), (2.0, 2.75), (0.5, 1.25)),   # 48^3
+    ((6.5, 7.0), (2.25, 2.75), (0.5, 1.0)),    # 32^3
+    ((0.5, 2.5), (0.5, 1.5), (3.0, 4.0)),      # 128x64x64
+    ((3.0, 4.5), (0.5, 1.5), (3.0, 4.0)),      # 96x64x64
+    ((5.0, 6.0), (0.5, 1.25), (3.0, 3.75)),    # 64x48x48
+    ((6.5, 7.25), (0.5, 1.25), (3.0, 3.75)),   # 48^3
+    ((0.5, 1.0), (3.0, 3.5), (3.0, 3.5)),      # 32^3
+)
+
+
+def twelve_block(n_steps: int = 10, seed: int = SEED) -> Case:
+    """Twelve blocks of uneven sizes around a stationary rigid ellipsoidal
+    plate (semi-axes 0.5 x 0.125 x 0.0125, surface 51), Re = 500 on the chord."""
+    return multi_block(coarse=(256, 192, 192), domain=(8.0, 6.0, 6.0), fine_boxes=TWELVE_BLOCK_BOXES,
+                       body=0, diameter=1.0, reynolds=500.0, n_steps=n_steps, seed=seed, plate=True,
+                       plate_axes=(0.5, 0.125, 0.0125))
 
 
 def uniform_block(n=(384, 256, 256), lengths=(3.0, 2.0, 2.0), seed: int = SEED,

@@ -42,6 +42,8 @@ _SIGS = {
     "bcfd_block_set_mixed_params": [c_i64, c_i64, c_double, c_int],
     "bcfd_block_set_solve_launch": [c_i64, c_int, c_int, c_int],
     "bcfd_set_batching": [c_int],
+    "bcfd_block_get_solve_launch": [c_i64, C.POINTER(c_int)],
+    "bcfd_autotune": [C.POINTER(c_i64)],
     "bcfd_block_sor_sweeps": [c_i64, c_i64, c_int],
     "bcfd_profile_begin": [],
     "bcfd_profile_end": [C.POINTER(ProfileReport)],

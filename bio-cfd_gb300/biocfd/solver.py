@@ -221,6 +221,18 @@ class Solver:
         check(self.L.bcfd_block_get_divergence(g, _pd(d)), "get_divergence")
         return float(d[0]), float(d[1])
 
+    def autotune(self) -> int:
+        """Time the candidate launch shapes of the Poisson solves and keep the fastest."""
+        n = C.c_int64()
+        check(self.L.bcfd_autotune(C.byref(n)), "autotune")
+        return n.value
+
+    def solve_launch(self, g: int) -> dict:
+        a = (C.c_int * 6)()
+        check(self.L.bcfd_block_get_solve_launch(g, a), "get_solve_launch")
+        return dict(zip(("fp64_threads", "fp64_ctas_per_sm", "fp64_sync", "fp32_threads", "fp32_ctas_per_sm",
+                         "fp32_variant"), list(a)))
+
     def set_batching(self, on: bool):
         check(self.L.bcfd_set_batching(int(on)), "set_batching")
 

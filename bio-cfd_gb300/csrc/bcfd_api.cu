@@ -1013,6 +1013,18 @@ int bcfd_block_set_solve_launch(bcfd_handle h, int threads, int ctas_per_sm, int
   hb->solve_threads = threads;
   hb->solve_ctas_per_sm = ctas_per_sm;
   hb->solve_sync = fp64_sync;
+  hb->dc_threads = threads > 256 ? 256 : threads;
+  hb->dc_ctas_per_sm = ctas_per_sm;
+  return 0;
+}
+
+int bcfd_block_get_solve_launch(bcfd_handle h, int* out) {
+  LOCK();
+  GETB(h);
+  if (!out) return BCFD_E_ARG;
+  const int v[6] = {hb->solve_threads, hb->solve_ctas_per_sm, hb->solve_sync,
+                    hb->dc_threads,    hb->dc_ctas_per_sm,    hb->dc_variant};
+  std::memcpy(out, v, sizeof v);
   return 0;
 }
 

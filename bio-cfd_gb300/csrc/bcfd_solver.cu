@@ -272,7 +272,8 @@ std::vector<unsigned char> step_key(const bcfd_step_config& c) {
     if (!hb) { put(&none, 1); continue; }
     put(&hb->d, sizeof hb->d);
     const int sw[11] = {hb->is_coarse, hb->has_body, hb->move_check, hb->blk_mv_tag, hb->dc_inner,
-                        hb->dc_variant, hb->solve_threads, hb->solve_ctas_per_sm, hb->solve_sync, 0, 0};
+                        hb->dc_variant, hb->solve_threads, hb->solve_ctas_per_sm, hb->solve_sync,
+                        hb->dc_threads, hb->dc_ctas_per_sm};
     put(sw, sizeof sw);
     put(&hb->dc_omega, sizeof hb->dc_omega);
     put(&hb->omega, sizeof hb->omega);

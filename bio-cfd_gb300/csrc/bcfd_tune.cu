@@ -1,0 +1,177 @@
+// Autotuner of the tiled Poisson solves' launch shape.  For each block it
+// times short solves (a fixed number of sweep pairs, stop test off) under
+// every candidate shape and keeps the fastest: threads per CTA, the cap on
+// co-resident CTAs per SM (which sets the tile shape through choose_tiles)
+// and the phase synchronisation (grid barrier or neighbour tiles).  None of
+// these changes the arithmetic, so the tuned solver computes exactly what the
+// untuned one does.  The block's solve state is saved before the trials and
+// restored after them; results are cached per block shape.
+#include <cstring>
+#include <map>
+#include <tuple>
+
+#include "bcfd_host.h"
+
+namespace bcfd {
+namespace {
+
+struct Shape {
+  int threads, ctas_per_sm, sync;  // sync: FP64 0 neighbour / 1 grid; FP32 variant 1 grid / 3 neighbour
+};
+struct Tuned {
+  Shape fp64, fp32;
+};
+std::map<std::tuple<int, int, int>, Tuned>& cache() {
+  static std::map<std::tuple<int, int, int>, Tuned> c;
+  return c;
+}
+
+// device copies of what a trial solve overwrites
+struct Saved {
+  void* buf = nullptr;
+  size_t off[5] = {0, 0, 0, 0, 0};
+};
+
+int save_state(HostBlock* hb, Saved& s, bool restore) {
+  const size_t np = (size_t)hb->d.d.npacked();
+  const size_t d8 = np * sizeof(double), f4 = np * sizeof(float);
+  // pc[2], rhs[2] (FP64), pcf[2], rhsf[2] (FP32), stats
+  const size_t total = 4 * d8 + 4 * f4 + sizeof(BlockStats);
+  if (!restore) BCFD_CUDA(cudaMalloc(&s.buf, total));
+  char* b = static_cast<char*>(s.buf);
+  auto cp = [&](void* dev, size_t at, size_t n) -> int {
+    if (restore) BCFD_CUDA(cudaMemcpyAsync(dev, b + at, n, cudaMemcpyDeviceToDevice, stream()));
+    else BCFD_CUDA(cudaMemcpyAsync(b + at, dev, n, cudaMemcpyDeviceToDevice, stream()));
+    return 0;
+  };
+  size_t at = 0;
+  for (int c = 0; c < 2; ++c) {
+    TRY_R(cp(hb->d.pc[c], at, d8));
+    at += d8;
+    TRY_R(cp(hb->d.rhs[c], at, d8));
+    at += d8;
+    TRY_R(cp(hb->d.pcf[c], at, f4));
+    at += f4;
+    TRY_R(cp(hb->d.rhsf[c], at, f4));
+    at += f4;
+  }
+  TRY_R(cp(hb->d.stats, at, sizeof(BlockStats)));
+  return 0;
+}
+
+// milliseconds of one trial solve (the best of two after a warm-up run)
+int time_trial(HostBlock* hb, bool fp32, int pairs, float* ms) {
+  cudaEvent_t e0, e1;
+  BCFD_CUDA(cudaEventCreate(&e0));
+  BCFD_CUDA(cudaEventCreate(&e1));
+  float best = 1e30f;
+  int r = 0;
+  for (int rep = 0; rep < 3 && !r; ++rep) {
+    cudaEventRecord(e0, stream());
+    if (fp32) {
+      const int keep = hb->dc_inner;
+      hb->dc_inner = pairs;
+      r = launch_sor_mixed(hb, 0, 1.0, -1.0);
+      hb->dc_inner = keep;
+    } else {
+      if (cudaMemsetAsync(&hb->d.stats->niter, 0, sizeof(int64_t), stream()) != cudaSuccess) r = BCFD_E_CUDA;
+      if (!r) r = launch_sor(hb, pairs - 1, 1.0, -1.0);
+    }
+    cudaEventRecord(e1, stream());
+    if (cudaEventSynchronize(e1) != cudaSuccess) r = BCFD_E_CUDA;
+    float t = 0.f;
+    if (!r && rep > 0 && cudaEventElapsedTime(&t, e0, e1) == cudaSuccess) best = std::min(best, t);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = best;
+  return r;
+}
+
+void apply(HostBlock* hb, const Shape& s, bool fp32) {
+  if (fp32) {
+    hb->dc_threads = s.threads;
+    hb->dc_ctas_per_sm = s.ctas_per_sm;
+    hb->dc_variant = s.sync;
+  } else {
+    hb->solve_threads = s.threads;
+    hb->solve_ctas_per_sm = s.ctas_per_sm;
+    hb->solve_sync = s.sync;
+  }
+}
+
+int tune_block(HostBlock* hb, Tuned* out) {
+  static const Shape c64[] = {{256, 0, 0}, {512, 0, 0}, {256, 0, 1}, {512, 0, 1}, {512, 1, 0}};
+  static const Shape c32[] = {{128, 0, 1}, {256, 0, 1}, {128, 0, 3}, {256, 0, 3}, {256, 2, 1}, {256, 1, 1}};
+  Saved sv;
+  TRY_R(save_state(hb, sv, false));
+  const int t0 = hb->solve_threads, c0 = hb->solve_ctas_per_sm, s0 = hb->solve_sync, v0 = hb->dc_variant,
+            dt0 = hb->dc_threads, dc0 = hb->dc_ctas_per_sm;
+  int r = 0;
+  float best = 1e30f;
+  Shape b64 = c64[0], b32 = c32[0];
+  for (const Shape& s : c64) {
+    apply(hb, s, false);
+    float ms = 0;
+    if ((r = time_trial(hb, false, 5, &ms))) break;
+    if (ms < best) best = ms, b64 = s;
+  }
+  best = 1e30f;
+  for (const Shape& s : c32) {
+    if (r) break;
+    apply(hb, s, true);
+    float ms = 0;
+    if ((r = time_trial(hb, true, 16, &ms))) break;
+    if (ms < best) best = ms, b32 = s;
+  }
+  hb->solve_threads = t0;
+  hb->solve_ctas_per_sm = c0;
+  hb->solve_sync = s0;
+  hb->dc_variant = v0;
+  hb->dc_threads = dt0;
+  hb->dc_ctas_per_sm = dc0;
+  const int rr = save_state(hb, sv, true);
+  cudaStreamSynchronize(stream());
+  cudaFree(sv.buf);
+  if (r) return r;
+  if (rr) return rr;
+  out->fp64 = b64;
+  out->fp32 = b32;
+  return 0;
+}
+
+}  // namespace
+}  // namespace bcfd
+
+using namespace bcfd;
+
+extern "C" int bcfd_autotune(int64_t* n_tuned) {
+  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  if (!lib().ready) return BCFD_E_STATE;
+  // blocks solved together in one batched launch share that launch's shape;
+  // tune the ones solved alone: the first block, and the others when they
+  // are not batched (batching off, or a single other block)
+  int others = 0;
+  for (size_t q = 1; q < lib().blocks.size(); ++q) others += lib().blocks[q] != nullptr;
+  int64_t n = 0;
+  for (size_t q = 0; q < lib().blocks.size(); ++q) {
+    HostBlock* hb = lib().blocks[q];
+    if (!hb || !hb->d.Acx || !hb->d.Acxf) continue;
+    if (q > 0 && lib().batch && others > 1) continue;
+    const Dims& d = hb->d.d;
+    const auto key = std::make_tuple(d.nx, d.ny, d.nz);
+    auto it = cache().find(key);
+    Tuned t;
+    if (it != cache().end()) {
+      t = it->second;
+    } else {
+      TRY_R(tune_block(hb, &t));
+      cache()[key] = t;
+      ++n;
+    }
+    apply(hb, t.fp64, false);
+    apply(hb, t.fp32, true);
+  }
+  if (n_tuned) *n_tuned = n;
+  return 0;
+}

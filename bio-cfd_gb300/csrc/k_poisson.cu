@@ -837,9 +837,9 @@ static TileMap tiles_within(HostBlock* hb, unsigned cap, int global) {
   return best;
 }
 
-static TileMap choose_tiles(HostBlock* hb, const void* fn, int threads, int global) {
+static TileMap choose_tiles(HostBlock* hb, const void* fn, int threads, int global, int ctas_per_sm) {
   unsigned cap = coop_grid(fn, threads, 0, 0xffffffffu);
-  if (hb->solve_ctas_per_sm > 0) cap = std::min<unsigned>(cap, (unsigned)(hb->solve_ctas_per_sm * num_sms()));
+  if (ctas_per_sm > 0) cap = std::min<unsigned>(cap, (unsigned)(ctas_per_sm * num_sms()));
   return tiles_within(hb, cap, global);
 }
 
@@ -857,7 +857,7 @@ int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_
   k_rhs<<<grid_for(np, 256), 256, 0, stream()>>>(B, dt);
   BCFD_LAUNCHED();
   const int threads = hb->solve_threads > 0 ? hb->solve_threads : 512;
-  TileMap tm = choose_tiles(hb, (const void*)k_sor64, threads, hb->solve_sync == 1 ? 1 : 0);
+  TileMap tm = choose_tiles(hb, (const void*)k_sor64, threads, hb->solve_sync == 1 ? 1 : 0, hb->solve_ctas_per_sm);
   TRY_R(reset_solve_state(hb, tm));
   const unsigned grid = (unsigned)(tm.ntj * tm.ntk);
   SorArgs a{itmax, epsi, hb->omega, prof_log(), res_tol, dt};
@@ -885,9 +885,10 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
     return launch_residual(hb, dt);
   }
   for (int c = 0; c < 2; ++c) BCFD_CUDA(cudaMemsetAsync(B.pcf[c], 0, np * sizeof(float), stream()));
-  const int threads = hb->solve_threads > 0 ? std::min(hb->solve_threads, kDcThreads) : kDcThreads;
+  const int threads = hb->dc_threads > 0 ? std::min(hb->dc_threads, kDcThreads) : kDcThreads;
   // variant 3: point-to-point tile sync; otherwise grid-wide phase barriers
-  TileMap tm = choose_tiles(hb, (const void*)k_sor_dc, threads, hb->dc_variant == 3 ? 0 : 1);
+  TileMap tm = choose_tiles(hb, (const void*)k_sor_dc, threads, hb->dc_variant == 3 ? 0 : 1,
+                            hb->dc_ctas_per_sm);
   TRY_R(reset_solve_state(hb, tm));
   const unsigned grid = (unsigned)(tm.ntj * tm.ntk);
   const int nmax = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
@@ -983,7 +984,7 @@ int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt,
   auto make = [&](HostBlock* hb, SorArgs& a) -> int {
     a = SorArgs{itmax, epsi, hb->omega, prof_log(), res_tol, dt};
     // blocks with their own launch shape keep their own launch
-    return hb->solve_threads > 0 || hb->solve_sync != 0;
+    return hb->solve_threads > 0 || hb->solve_sync != 0 || hb->solve_ctas_per_sm > 0;
   };
   // a block solved alone goes through launch_sor (which recomputes b/dt)
   auto solo = [&](HostBlock* hb) -> int { return launch_sor(hb, itmax, dt, epsi, res_tol); };
@@ -999,7 +1000,7 @@ int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, doub
   }
   const int threads = kDcThreads;
   for (HostBlock* hb : hbs) {
-    if (hb->dc_variant == 2 || hb->solve_threads > 0) continue;
+    if (hb->dc_variant == 2 || hb->dc_variant == 3 || hb->dc_threads > 0 || hb->dc_ctas_per_sm > 0) continue;
     for (int c = 0; c < 2; ++c)
       BCFD_CUDA(cudaMemsetAsync(hb->d.pcf[c], 0, hb->d.d.npacked() * sizeof(float), stream()));
   }
@@ -1014,7 +1015,7 @@ int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, doub
     a.inv_dt = 1.0 / dt;
     a.div_tol = div_tol;
     a.log = prof_log();
-    return hb->dc_variant == 2 || hb->dc_variant == 3 || hb->solve_threads > 0;
+    return hb->dc_variant == 2 || hb->dc_variant == 3 || hb->dc_threads > 0 || hb->dc_ctas_per_sm > 0;
   };
   auto solo = [&](HostBlock* hb) -> int { return launch_sor_mixed(hb, itmax, dt, div_tol); };
   return launch_solve_set<DcArgs>(hbs, (const void*)k_sor_dc_set, threads, 1, make, solo);

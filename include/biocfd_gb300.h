@@ -227,6 +227,16 @@ int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omeg
  * on co-resident CTAs per SM (0 = occupancy limit), and the FP64 solve's
  * phase sync (0 point-to-point between neighbour tiles, 1 grid-wide) */
 int bcfd_block_set_solve_launch(bcfd_handle h, int threads, int ctas_per_sm, int fp64_sync);
+/* out[6] = FP64 solve threads, CTAs/SM cap, sync; FP32 correction threads,
+ * CTAs/SM cap, variant (0 = library default) */
+int bcfd_block_get_solve_launch(bcfd_handle h, int* out);
+/* Autotuner (no counterpart in the reference): for every block solved alone,
+ * times short solves under each candidate launch shape of the FP64 solve and
+ * of the FP32 correction (threads per CTA, CTAs per SM, which sets the tile
+ * shape, and the phase synchronisation) and keeps the fastest; results are
+ * cached per block shape.  None of these changes the arithmetic.  The block's
+ * solve state is restored afterwards.  *n_tuned = shapes newly timed. */
+int bcfd_autotune(int64_t* n_tuned);
 /* measurement: exactly n_pairs red-black sweep pairs of the block's Poisson
  * system b = the current computeDiv result (deltat = 1), stop test disabled.
  * precision 0: the FP64 reference sweeps on pc; 1: one FP32 correction of

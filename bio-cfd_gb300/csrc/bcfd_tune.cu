@@ -102,7 +102,9 @@ void apply(HostBlock* hb, const Shape& s, bool fp32) {
 
 int tune_block(HostBlock* hb, Tuned* out) {
   static const Shape c64[] = {{256, 0, 0}, {512, 0, 0}, {256, 0, 1}, {512, 0, 1}, {512, 1, 0}};
-  static const Shape c32[] = {{128, 0, 1}, {256, 0, 1}, {128, 0, 3}, {256, 0, 3}, {256, 2, 1}, {256, 1, 1}};
+  // {256, 4, *} selects the 64-register instantiation of the FP32 solve
+  static const Shape c32[] = {{128, 0, 1}, {256, 0, 1}, {128, 0, 3}, {256, 0, 3},
+                              {256, 2, 1}, {256, 1, 1}, {256, 4, 1}, {256, 4, 3}};
   Saved sv;
   TRY_R(save_state(hb, sv, false));
   const int t0 = hb->solve_threads, c0 = hb->solve_ctas_per_sm, s0 = hb->solve_sync, v0 = hb->dc_variant,

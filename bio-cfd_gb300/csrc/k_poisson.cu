@@ -588,7 +588,10 @@ __global__ void __launch_bounds__(kSolveMaxThreads, 2) k_sor64(DevBlock B, SorAr
   sor64_body(B, a, gb, tm, (int)blockIdx.x);
 }
 
-__global__ void __launch_bounds__(kDcThreads, 3) k_sor_dc(DevBlock B, DcArgs a, GridBar gb, TileMap tm) {
+// MINB CTAs of 256 threads per SM: 3 (80 registers, no spill) or 4 (64
+// registers, a few spilled: more warps, so more loads in flight on large blocks)
+template <int MINB>
+__global__ void __launch_bounds__(kDcThreads, MINB) k_sor_dc(DevBlock B, DcArgs a, GridBar gb, TileMap tm) {
   sor_dc_body(B, a, gb, tm, (int)blockIdx.x);
 }
 
@@ -887,8 +890,9 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   for (int c = 0; c < 2; ++c) BCFD_CUDA(cudaMemsetAsync(B.pcf[c], 0, np * sizeof(float), stream()));
   const int threads = hb->dc_threads > 0 ? std::min(hb->dc_threads, kDcThreads) : kDcThreads;
   // variant 3: point-to-point tile sync; otherwise grid-wide phase barriers
-  TileMap tm = choose_tiles(hb, (const void*)k_sor_dc, threads, hb->dc_variant == 3 ? 0 : 1,
-                            hb->dc_ctas_per_sm);
+  // four CTAs per SM asked for: the 64-register instantiation
+  const void* fn = hb->dc_ctas_per_sm == 4 ? (const void*)k_sor_dc<4> : (const void*)k_sor_dc<3>;
+  TileMap tm = choose_tiles(hb, fn, threads, hb->dc_variant == 3 ? 0 : 1, hb->dc_ctas_per_sm);
   TRY_R(reset_solve_state(hb, tm));
   const unsigned grid = (unsigned)(tm.ntj * tm.ntk);
   const int nmax = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
@@ -905,7 +909,7 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   gb.ctr = reinterpret_cast<unsigned long long*>(hb->bar);
   void* args[] = {(void*)&B, (void*)&a, (void*)&gb, (void*)&tm};
   prof_mark(true);
-  BCFD_CUDA(launch_coop((const void*)k_sor_dc, grid, threads, args));
+  BCFD_CUDA(launch_coop(fn, grid, threads, args));
   prof_mark(false);
   BCFD_LAUNCHED();
   // k_sor_dc records the residual it leaves (stats pad[1]) itself

@@ -79,6 +79,13 @@ class Solver:
                 check(L.bcfd_block_set_surface(g, len(tri), len(xs), _pi(e1), _pi(e2), _pi(e3), _pi(sid),
                                                _pd(xs), _pd(ys), _pd(zs)), "set_surface")
                 check(L.bcfd_block_set_search_box(g, *spec.search_box), "set_search_box")
+                if spec.motion is not None:
+                    # app/main.F90:64-69: the nodes above are the body frame
+                    mo, mi = spec.motion, case.motion
+                    p = np.array([mo.a0_deg, mo.bfreq, mo.yamp, *mo.shift], dtype=np.float64)
+                    check(L.bcfd_block_set_body_motion(g, _pd(p)), "set_body_motion")
+                    check(L.bcfd_shift_surface_nodes_initial(g, mi.aoa_deg, mi.piv_pt, 0, case.dt, mi.dxmin, 0.0),
+                          "shift_surface_nodes_initial")
                 check(L.bcfd_compute_surface_norm(g, m.inor), "compute_surface_norm")
         for it in case.interfaces:
             box = np.asarray(it.box, dtype=np.float64)
@@ -105,6 +112,12 @@ class Solver:
             check(L.bcfd_coefficient_matrix(g, int(spec.is_coarse)), "coefficient_matrix")
         for g in self.handles:
             check(L.bcfd_non_uni_coeff(g), "non_uni_coeff")
+        # app/main.F90:45-46, 119: ita = 0 and totime = deltat when the loop starts
+        mi = case.motion
+        inor = next((b.mesh.inor for b in case.blocks if b.mesh is not None), 1)
+        check(L.bcfd_set_motion_inputs((mi.phase_deg * np.pi / 180.0) if mi else 0.0, mi.piv_pt if mi else 0.0,
+                                       mi.freq if mi else 0.0, mi.dxmin if mi else 0.0, inor, 0, case.dt),
+              "set_motion_inputs")
         self.sync()
 
     def upload_fields(self, g: int, ini: dict):
@@ -132,10 +145,19 @@ class Solver:
                                          len(self.handles), 1), "poisson_solver")
 
     def research_phase(self):
-        L = self.L
+        L, c = self.L, self.case
         for g, spec in zip(self.handles, self.case.blocks):
             if spec.has_body:
                 check(L.bcfd_pressure_forcing1(g), "pressure_forcing1")
+        # app/main.F90:169-176, 213-215: moving bodies
+        if c.motion is not None:
+            ita, tt = self.time()
+            for g, spec in zip(self.handles, self.case.blocks):
+                if spec.motion is not None:
+                    mi = c.motion
+                    check(L.bcfd_compute_surface_variables(g, mi.phase_deg * np.pi / 180.0, mi.piv_pt, ita, c.dt,
+                                                           mi.dxmin, mi.freq, tt), "compute_surface_variables")
+                    check(L.bcfd_compute_surface_norm(g, spec.mesh.inor), "compute_surface_norm")
         for g, spec in zip(self.handles, self.case.blocks):
             if not spec.has_body:
                 continue
@@ -151,7 +173,25 @@ class Solver:
             check(L.bcfd_velocity_forcing_ghost(g), "velocity_forcing_ghost")
             check(L.bcfd_pressure_forcing_ghost(g), "pressure_forcing_ghost")
 
+    def kinematic(self, g: int, name: str) -> float:
+        """A kinematic scalar of a block (xdot, ydot, yddot, thetaDot1, ..., piv_z)."""
+        return float(self.read(g, name, 1)[0])
+
+    def time(self):
+        """(ita, totime) of the native driver's loop (app/main.F90:130-131)."""
+        ita, tt = C.c_int64(), C.c_double()
+        check(self.L.bcfd_get_time(C.byref(ita), C.byref(tt)), "get_time")
+        return ita.value, tt.value
+
     def step(self):
+        # advance the loop counters as the native driver does
+        ita, tt = self.time()
+        mi = self.case.motion
+        inor = next((b.mesh.inor for b in self.case.blocks if b.mesh is not None), 1)
+        check(self.L.bcfd_set_motion_inputs((mi.phase_deg * np.pi / 180.0) if mi else 0.0,
+                                            mi.piv_pt if mi else 0.0, mi.freq if mi else 0.0,
+                                            mi.dxmin if mi else 0.0, inor, ita + 1, tt + self.case.dt),
+              "set_motion_inputs")
         self.momentum_phase()
         self.poisson_phase()
         self.research_phase()

@@ -35,6 +35,29 @@ class Mesh:
 
 
 @dataclass
+class Motion:
+    """Rigid-body motion of a block's surface (Block_t members read by
+    src/Search.F90:49-208): pitch amplitude a0 in degrees, heave frequency and
+    amplitude, body placement.  With a motion the mesh nodes are in the body
+    frame."""
+    a0_deg: float = 0.0
+    bfreq: float = 0.0
+    yamp: float = 0.0
+    shift: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+
+
+@dataclass
+class MotionInputs:
+    """The app/main.F90 inputs of the motion: initial angle of attack (deg),
+    phase angle (deg), pivot offset, pitch frequency, dxmin."""
+    aoa_deg: float = 0.0
+    phase_deg: float = 0.0
+    piv_pt: float = 0.0
+    freq: float = 0.0
+    dxmin: float = 0.0
+
+
+@dataclass
 class BlockSpec:
     nx: int
     ny: int
@@ -51,6 +74,7 @@ class BlockSpec:
     ydot: float = 0.0
     yddot: float = 0.0
     piv: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    motion: Optional["Motion"] = None
 
     @property
     def has_body(self) -> bool:
@@ -88,6 +112,7 @@ class Case:
     pc_ita_max: int = 5000
     n_steps: int = 1
     init: List[dict] = field(default_factory=list)   # per block: {"u","v","w","p"} arrays
+    motion: Optional["MotionInputs"] = None
 
     @property
     def n_interior(self) -> int:
@@ -215,6 +240,31 @@ def plate_single_block(n: int = 32, n_steps: int = 2, semi_axes=(0.25, 0.125, 0.
     chord = 2.0 * semi_axes[0]
     case = Case(name=f"plate{n}", blocks=[spec], dt=0.3 * dx, re=reynolds / chord, uc=1.0, epsi=1e-6,
                 pc_ita_max=pc_ita_max, n_steps=n_steps)
+    case.init = [noisy_initial(spec, case.uc, rng)]
+    return case
+
+
+def moving_plate_single_block(n: int = 32, n_steps: int = 3, semi_axes=(0.25, 0.125, 0.0125),
+                              center=(0.45, 0.5, 0.5), a0_deg: float = 10.0, yamp: float = 0.05,
+                              freq: float = 0.25, phase_deg: float = 90.0, reynolds: float = 300.0,
+                              seed: int = SEED) -> Case:
+    """The plate of plate_single_block heaving (yamp sin(2 pi freq t)) and
+    pitching about x (a0 sin(2 pi freq t + phase)), towed in -x by the
+    reference's fixed 0.05 dxmin per step (src/Search.F90:12)."""
+    f = uniform_faces(0.0, 1.0, n)
+    dx = 1.0 / n
+    spec = BlockSpec(n, n, n, f, f.copy(), f.copy(), omega=1.7, is_coarse=True)
+    spec.mesh = ellipsoid_plate((0.0, 0.0, 0.0), semi_axes, 0.5 * dx, surf_id=51)
+    spec.motion = Motion(a0_deg=a0_deg, bfreq=freq, yamp=yamp, shift=tuple(center))
+    c = np.asarray(center)
+    ax = np.asarray(semi_axes)
+    reach = np.array([0.0, yamp + ax[1], ax[1]]) + ax
+    spec.search_box = search_box_for(spec, c - reach, c + reach)
+    rng = np.random.default_rng(seed)
+    chord = 2.0 * semi_axes[0]
+    case = Case(name=f"moving_plate{n}", blocks=[spec], dt=0.3 * dx, re=reynolds / chord, uc=1.0,
+                epsi=1e-6, pc_ita_max=5000, n_steps=n_steps)
+    case.motion = MotionInputs(aoa_deg=0.0, phase_deg=phase_deg, piv_pt=0.0, freq=freq, dxmin=dx)
     case.init = [noisy_initial(spec, case.uc, rng)]
     return case
 

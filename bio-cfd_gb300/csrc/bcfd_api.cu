@@ -703,6 +703,7 @@ int bcfd_block_set_surface(bcfd_handle h, int64_t n_elems, int64_t n_nodes, cons
   }
   if (n_elems)
     BCFD_CUDA(cudaMemcpyAsync((void*)hb->d.elp1, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, stream()));
+  hb->elem_host = ids;
   hb->has_body = n_elems > 0;
   BCFD_CUDA(cudaStreamSynchronize(stream()));
   return bcfd_block_set_nodes(h, xnode1, ynode1, znode1);
@@ -725,6 +726,106 @@ int bcfd_block_set_nodes(bcfd_handle h, const double* x, const double* y, const 
   for (int q = 0; q < nn; ++q)
     r2 = std::max(r2, (x[q] - cx) * (x[q] - cx) + (y[q] - cy) * (y[q] - cy) + (z[q] - cz) * (z[q] - cz));
   hb->node_rmax = std::sqrt(r2);
+  return 0;
+}
+
+// node surface ids from the elements (src/ReadInput.f90:403-420): 50 by
+// default; nodes of surface-51/52 elements take that id, then nodes of
+// surface-50 elements are set back to 50
+static std::vector<int8_t> node_ids(const HostBlock* hb) {
+  const int nn = hb->d.nn, ne = hb->d.ne;
+  std::vector<int8_t> id((size_t)nn, 50);
+  const std::vector<int>& e = hb->elem_host;
+  for (int q = 0; q < ne; ++q) {
+    const int s = e[3 * (size_t)ne + q];
+    if (s == 51 || s == 52)
+      for (int c = 0; c < 3; ++c) id[(size_t)e[c * (size_t)ne + q] - 1] = (int8_t)s;
+  }
+  for (int q = 0; q < ne; ++q)
+    if (e[3 * (size_t)ne + q] == 50)
+      for (int c = 0; c < 3; ++c) id[(size_t)e[c * (size_t)ne + q] - 1] = 50;
+  return id;
+}
+
+int bcfd_block_set_body_motion(bcfd_handle h, const double* p) {
+  LOCK();
+  GETB(h);
+  if (!p || hb->d.nn <= 0) return BCFD_E_ARG;
+  BodyMotion& m = hb->motion;
+  m = BodyMotion{};
+  m.on = true;
+  m.a0 = p[0];
+  m.bfreq = p[1];
+  m.yamp = p[2];
+  m.xshift = p[3];
+  m.yshift = p[4];
+  m.zshift = p[5];
+  const int nn = hb->d.nn;
+  if (!hb->d.xnode0) {
+    double* f;
+    TRY(dalloc(hb, &f, (size_t)nn * 3));
+    hb->d.xnode0 = f;
+    hb->d.ynode0 = f + nn;
+    hb->d.znode0 = f + 2 * (size_t)nn;
+    int8_t* id;
+    TRY(dalloc(hb, &id, (size_t)nn));
+    hb->d.node_id = id;
+  }
+  // the nodes given with the surface are the body frame
+  BCFD_CUDA(cudaMemcpyAsync((void*)hb->d.xnode0, hb->d.xnode1, nn * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
+  BCFD_CUDA(cudaMemcpyAsync((void*)hb->d.ynode0, hb->d.ynode1, nn * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
+  BCFD_CUDA(cudaMemcpyAsync((void*)hb->d.znode0, hb->d.znode1, nn * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
+  const std::vector<int8_t> id = node_ids(hb);
+  BCFD_CUDA(cudaMemcpyAsync((void*)hb->d.node_id, id.data(), id.size(), cudaMemcpyHostToDevice, stream()));
+  // bound on the moving nodes' distance from the block centre: body-frame
+  // radius, the rotation about the pivot line, and the largest translation
+  double r0 = 0.0;
+  {
+    std::vector<double> x(nn), y(nn), z(nn);
+    BCFD_CUDA(cudaMemcpyAsync(x.data(), hb->d.xnode0, nn * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaMemcpyAsync(y.data(), hb->d.ynode0, nn * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaMemcpyAsync(z.data(), hb->d.znode0, nn * sizeof(double), cudaMemcpyDeviceToHost, stream()));
+    BCFD_CUDA(cudaStreamSynchronize(stream()));
+    for (int q = 0; q < nn; ++q) r0 = std::max(r0, std::sqrt(x[q] * x[q] + y[q] * y[q] + z[q] * z[q]));
+  }
+  hb->motion_r0 = r0;
+  return 0;
+}
+
+int bcfd_shift_surface_nodes_initial(bcfd_handle h, double aoa, double piv_pt, int64_t ita, double deltat,
+                                     double dxmin, double totime) {
+  LOCK();
+  GETB(h);
+  if (!hb->motion.on) return BCFD_E_STATE;
+  return shift_surface_nodes_initial(hb, aoa, piv_pt, ita, deltat, dxmin, totime);
+}
+
+int bcfd_compute_surface_variables(bcfd_handle h, double phase_angle, double piv_pt, int64_t ita,
+                                   double deltat, double dxmin, double freq, double totime) {
+  LOCK();
+  GETB(h);
+  if (!hb->motion.on) return BCFD_E_STATE;
+  return compute_surface_variables(hb, phase_angle, piv_pt, ita, deltat, dxmin, freq, totime);
+}
+
+int bcfd_set_motion_inputs(double phase_angle, double piv_pt, double freq, double dxmin, int64_t inor,
+                           int64_t ita, double totime) {
+  LOCK();
+  Lib& L = lib();
+  L.phase_angle = phase_angle;
+  L.piv_pt = piv_pt;
+  L.freq = freq;
+  L.dxmin = dxmin;
+  L.inor = inor;
+  L.ita = ita;
+  L.totime = totime;
+  return 0;
+}
+
+int bcfd_get_time(int64_t* ita, double* totime) {
+  LOCK();
+  if (ita) *ita = lib().ita;
+  if (totime) *totime = lib().totime;
   return 0;
 }
 

@@ -13,8 +13,21 @@
 
 namespace bcfd {
 
+// rigid-body motion state of a block's surface (Block_t members used by
+// src/Search.F90:49-208)
+struct BodyMotion {
+  bool on = false;
+  double a0 = 0, bfreq = 0, yamp = 0, xshift = 0, yshift = 0, zshift = 0;
+  double xpth1 = 0, xpth2 = 0, ypth2 = 0, xchg = 0, ychg = 0, xmove = 0, ymove = 0, zmove = 0;
+  double xt = 0, yt = 0, inity_cent = 0, nxty_cent = 0, initx_cent = 0, nxtx_cent = 0,
+         initz_cent = 0, nxtz_cent = 0;
+};
+
 struct HostBlock {
   int index = -1;                  // registration order (device table slot)
+  BodyMotion motion;
+  double motion_r0 = 0.0;          // largest body-frame node radius
+  std::vector<int> elem_host;      // elp1 | elp2 | elp3 | surf_id, as uploaded
   DevBlock d{};
   std::vector<void*> allocs;  // device allocations owned by the block
   // host copies of the 1-D grids (1-based meaning, v[i-1])
@@ -94,6 +107,11 @@ struct Lib {
   DevBlock* dtab = nullptr;
   size_t dtab_cap = 0;
   std::vector<DevBlock> htab;        // what the device table holds
+  // time and motion inputs of the native driver (app/main.F90 variables)
+  int64_t ita = 0;
+  double totime = 0.0;
+  double phase_angle = 0.0, piv_pt = 0.0, freq = 0.0, dxmin = 0.0;
+  int64_t inor = 1;
   // captured time step (bcfd_run_steps with use_graph)
   cudaGraphExec_t step_graph = nullptr;
   std::vector<unsigned char> step_key;  // what the capture depends on
@@ -169,6 +187,11 @@ int launch_restrict(HostInterface* it, int comp, int which);
 int launch_fine_update_mv(HostInterface* it);
 // k_stress.cu
 int launch_stress(HostBlock* hb, double mu_f, double rho_f, double* out_host);
+// k_motion.cu
+int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_t ita, double deltat,
+                                double dxmin, double totime);
+int compute_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, int64_t ita, double deltat,
+                              double dxmin, double freq, double totime);
 int launch_stress_noalloc(HostBlock* hb, double mu_f, double rho_f, double* out_host);
 
 // Refresh the device table of block views (no copy when unchanged, so a

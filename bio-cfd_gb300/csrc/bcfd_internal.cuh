@@ -109,6 +109,9 @@ struct DevBlock {
   // surface
   int ne, nn;
   const double *xnode1, *ynode1, *znode1;
+  // body-frame nodes and node surface ids (moving bodies only)
+  const double *xnode0, *ynode0, *znode0;
+  const int8_t* node_id;
   const int *elp1, *elp2, *elp3, *surf_id;
   double *xcent, *ycent, *zcent, *cosA, *cosB, *cosG, *elen;
   // IB / TS lists (capacity cap_ib), counts in cnt[]

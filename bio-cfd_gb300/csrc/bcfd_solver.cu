@@ -209,9 +209,19 @@ int poisson(const SolveCfg& c, int start, int finish, int step) {
 // get pressureForcing1 and the per-step re-Search of main.F90:232-263.  The
 // body is stationary: the kinematics / block-move stage of main.F90:169-230
 // leaves the geometry unchanged and is not run.
+bool any_motion() {
+  for (HostBlock* hb : lib().blocks)
+    if (hb && hb->motion.on) return true;
+  return false;
+}
+
 int step_once(const bcfd_step_config& cfg) {
   SolveCfg c{cfg.pc_ita_max, cfg.epsi, cfg.deltat, cfg.uc, cfg.precision, cfg.div_tol};
   auto all = blocks();
+  Lib& L = lib();
+  // app/main.F90:130-131
+  L.ita = L.ita + 1;
+  L.totime = L.totime + cfg.deltat;
   std::vector<HostBlock*> every;
   for (auto& [g, hb] : all) every.push_back(hb);
   // nsMomentum2order of every block in one launch (blocks are independent)
@@ -227,6 +237,15 @@ int step_once(const bcfd_step_config& cfg) {
   TRY(poisson(c, 1, (int)lib().blocks.size(), 1));
   for (auto& [g, hb] : all)
     if (hb->has_body) TRY(launch_forcing_pressure(hb, 0));
+  // moving bodies (app/main.F90:169-176, 213-215): kinematics and node
+  // positions, then the surface normals of the moved nodes.  The fine blocks
+  // do not move (block_move_check's margins must hold for the motion).
+  for (auto& [g, hb] : all)
+    if (hb->motion.on) {
+      hb->blk_mv_tag = 0;
+      TRY(compute_surface_variables(hb, L.phase_angle, L.piv_pt, L.ita, cfg.deltat, L.dxmin, L.freq, L.totime));
+      TRY(launch_surface_norm(hb, L.inor));
+    }
   for (auto& [g, hb] : all) {
     if (!hb->has_body) continue;
     hb->blk_mv_tag = 0;
@@ -428,7 +447,9 @@ int bcfd_poisson_solver(int64_t pc_ita_max, double epsi, int64_t ita, double del
 int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps) {
   LOCK();
   if (!cfg || n_steps < 0) return BCFD_E_ARG;
-  if (cfg->use_graph && !lib().prof_on) {
+  // a moving body changes the kernels' arguments every step: issue those
+  // steps eagerly
+  if (cfg->use_graph && !lib().prof_on && !any_motion()) {
     TRY(run_steps_graph(*cfg, n_steps));
   } else {
     for (int64_t s = 0; s < n_steps; ++s) TRY(step_once(*cfg));
@@ -483,6 +504,23 @@ int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64
     if (!r) r = dcopy(tmp, d.npts());
     cudaFree(tmp);
     return r;
+  }
+  if (s == "xnode1") return dcopy(D.xnode1, D.nn);
+  if (s == "ynode1") return dcopy(D.ynode1, D.nn);
+  if (s == "znode1") return dcopy(D.znode1, D.nn);
+  {
+    // kinematic scalars the forcing routines read
+    const char* kn[10] = {"xdot", "ydot", "yddot", "thetaDot1", "thetaDDot1", "thetaDot2", "thetaDDot2",
+                          "piv_x", "piv_y", "piv_z"};
+    const double kv[10] = {D.xdot, D.ydot, D.yddot, D.thetaDot1, D.thetaDDot1, D.thetaDot2, D.thetaDDot2,
+                           D.piv_x, D.piv_y, D.piv_z};
+    for (int q = 0; q < 10; ++q)
+      if (s == kn[q]) {
+        if (n < 1) return BCFD_E_ARG;
+        static_cast<double*>(out)[0] = kv[q];
+        if (written) *written = 1;
+        return 0;
+      }
   }
   const char* fnames[7] = {"xcent", "ycent", "zcent", "cosAlpha", "cosBeta", "cosGamma", "element_length"};
   double* fptr[7] = {D.xcent, D.ycent, D.zcent, D.cosA, D.cosB, D.cosG, D.elen};

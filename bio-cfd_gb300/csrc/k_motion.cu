@@ -1,0 +1,131 @@
+// Rigid-body motion of a block's surface: the initial placement
+// shiftSurfaceNodesInitial (src/Search.F90:49-124) and the per-step
+// kinematics and node positions computeSurfaceVariables
+// (src/Search.F90:126-208).  The kinematic scalars and the rotation's
+// cos/sin are evaluated on the host with the reference's expressions (one
+// value per step, so the host and the oracle give identical bits); one kernel
+// moves the nodes: rotation of surface-51 (+angle) and -52 (-angle) nodes
+// about the x axis through z = piv_pt, then the translation.
+#include <cmath>
+
+#include "bcfd_host.h"
+
+namespace bcfd {
+namespace {
+
+constexpr double kXfact = 0.05;  // src/Search.F90:12
+
+struct Place {
+  double c1, s1, c2, s2, piv_pt;
+  double tx, ty1, ty2, tz1, tz2;
+  int two;  // 1: y = (yr1 + ty1) + ty2, z = (zr1 + tz1) + tz2; 0: one term
+};
+
+__global__ void k_place_nodes(DevBlock B, Place P) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.nn; i += gridDim.x * blockDim.x) {
+    const int id = B.node_id[i];
+    const double x = B.xnode0[i], y = B.ynode0[i], z = B.znode0[i];
+    double xr1 = x, yr1 = y, zr1 = z;
+    if (id == 51 || id == 52) {
+      const double c = id == 51 ? P.c1 : P.c2, s = id == 51 ? P.s1 : P.s2;
+      zr1 = z * c + y * s + P.piv_pt - P.piv_pt * c;
+      yr1 = -(z * s) + y * c + P.piv_pt * s;
+    }
+    double* xn = const_cast<double*>(B.xnode1);
+    double* yn = const_cast<double*>(B.ynode1);
+    double* zn = const_cast<double*>(B.znode1);
+    xn[i] = xr1 + P.tx;
+    yn[i] = P.two ? (yr1 + P.ty1) + P.ty2 : yr1 + P.ty1;
+    zn[i] = P.two ? (zr1 + P.tz1) + P.tz2 : zr1 + P.tz1;
+  }
+}
+
+// the nearest-element search's bound on node distances from the block centre
+// after a move: translation + body-frame radius + the rotation about the pivot
+// line (a rotation about an axis at distance |piv_pt| from the origin moves a
+// point by at most 2|piv_pt| more than its radius)
+void update_node_rmax(HostBlock* hb, double piv_pt, double tx, double ty, double tz) {
+  const Dims& d = hb->d.d;
+  const double cx = 0.5 * (hb->x1[0] + hb->x1[d.nx + 2]), cy = 0.5 * (hb->y1[0] + hb->y1[d.ny + 2]),
+               cz = 0.5 * (hb->z1[0] + hb->z1[d.nz + 2]);
+  const double ax = tx - cx, ay = ty - cy, az = tz - cz;
+  hb->node_rmax = std::sqrt(ax * ax + ay * ay + az * az) + hb->motion_r0 + 2.0 * std::fabs(piv_pt) + 1e-9;
+}
+
+int place_nodes(HostBlock* hb, double aoa1, double piv_pt, double tx, double ty1, double ty2, double tz1,
+                double tz2, int two) {
+  if (hb->d.nn <= 0) return 0;
+  update_node_rmax(hb, piv_pt, tx, ty1 + ty2, tz1 + tz2);
+  const double aoa2 = -aoa1;
+  Place P{std::cos(aoa1), std::sin(aoa1), std::cos(aoa2), std::sin(aoa2), piv_pt, tx, ty1, ty2, tz1, tz2, two};
+  k_place_nodes<<<grid_for(hb->d.nn, 128), 128, 0, stream()>>>(hb->d, P);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+}  // namespace
+
+int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_t ita, double deltat,
+                                double dxmin, double totime) {
+  BodyMotion& m = hb->motion;
+  const double pi = 4.0 * std::atan(1.0);
+  const double aoa1 = aoa * pi / 180.0;
+  const double bdfr = 15, bdy = 15 * dxmin;
+  m.xmove = m.ymove = m.zmove = 0.0;
+  m.a0 = m.a0 * pi / 180.0;
+  const double angt = 2.0 * pi * m.bfreq;
+  m.xpth1 = m.xshift - ((double)ita * dxmin * kXfact);
+  m.xpth2 = m.xshift - ((double)ita * dxmin * kXfact);
+  m.ypth2 = (m.yamp) * std::sin(angt * m.xshift);
+  DevBlock& D = hb->d;
+  D.piv_x = m.xshift;
+  D.piv_y = m.yshift;
+  D.piv_z = m.zshift;
+  D.thetaDot1 = D.thetaDot2 = D.alphaDot = 0.0;
+  D.thetaDDot1 = D.thetaDDot2 = 0.0;
+  m.yt = bdy * std::sin(2 * pi * bdfr * totime);
+  D.ydot = angt * bdy * std::cos(2 * pi * bdfr * totime);
+  D.yddot = -(angt * angt * bdy * std::sin(2 * pi * bdfr * totime));
+  m.xt = m.xshift - ((double)ita * dxmin * kXfact);
+  D.xdot = -(dxmin * kXfact) / deltat;
+  m.inity_cent = m.nxty_cent = m.yshift;
+  m.initx_cent = m.nxtx_cent = m.xshift;
+  m.initz_cent = m.nxtz_cent = m.zshift;
+  return place_nodes(hb, aoa1, piv_pt, m.xshift, m.yshift, 0.0, m.zshift, 0.0, 0);
+}
+
+int compute_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, int64_t ita, double deltat,
+                              double dxmin, double freq, double totime) {
+  BodyMotion& m = hb->motion;
+  DevBlock& D = hb->d;
+  const double pi = 4.0 * std::atan(1.0);
+  const double aoa1 = (m.a0) * std::sin(2.0 * pi * freq * (totime + deltat) + phase_angle);
+  const double ang_theta = 2.0 * pi * freq;
+  const double bdfr = m.bfreq, bdy = m.yamp;
+  const double angt = 2.0 * pi * bdfr;
+  m.xpth2 = m.xshift - ((double)ita * dxmin * kXfact);
+  m.ypth2 = (m.yamp) * std::sin(angt * m.xpth2);
+  m.xchg = m.xpth2 - m.xpth1;
+  m.xpth1 = m.xpth2;
+  D.thetaDot1 = ang_theta * m.a0 * std::cos(2.0 * pi * freq * (totime + deltat) + phase_angle);
+  D.thetaDDot1 = -(ang_theta * ang_theta * m.a0 * std::sin(2.0 * pi * freq * (totime + deltat) + phase_angle));
+  D.thetaDot2 = -D.thetaDot1;
+  D.thetaDDot2 = -D.thetaDDot1;
+  m.yt = bdy * std::sin(angt * (totime));
+  D.ydot = angt * bdy * std::cos(angt * (totime));
+  D.yddot = -(angt * angt * bdy * std::sin(angt * (totime)));
+  m.xt = m.xpth2;
+  D.xdot = -(dxmin * kXfact) / deltat;
+  m.ychg = m.yt - bdy * std::sin(angt * (totime - deltat));
+  m.ymove = m.yt;
+  m.xmove = m.xchg;
+  m.zmove = 0.0;
+  D.piv_y = D.piv_y + m.ychg;
+  D.piv_x = D.piv_x + m.xmove;
+  D.piv_z = D.piv_z + m.zmove;
+  m.nxty_cent = m.nxty_cent + m.ychg;
+  m.nxtx_cent = m.nxtx_cent + m.xmove;
+  return place_nodes(hb, aoa1, piv_pt, m.xpth2, m.yshift, m.ymove, m.zshift, m.zmove, 1);
+}
+
+}  // namespace bcfd

@@ -131,6 +131,24 @@ int bcfd_pressure_forcing_ghost(bcfd_handle h);  /* src/Forcing.f90:362-448  */
 
 /* ---- Search / tagging ---------------------------------------------------- */
 int bcfd_compute_surface_norm(bcfd_handle h, int64_t inor); /* src/Search.F90:210-258  */
+
+/* ---- rigid-body motion of a block's surface (src/Search.F90:49-208) ---- */
+/* p[6] = a0 (pitch amplitude in degrees, as read), bfreq (heave frequency),
+ * yamp (heave amplitude), xshift, yshift, zshift (body placement).  The nodes
+ * set with the surface become the body frame (xnode of Block_t); node surface
+ * ids follow src/ReadInput.f90:403-420. */
+int bcfd_block_set_body_motion(bcfd_handle h, const double* p);
+int bcfd_shift_surface_nodes_initial(bcfd_handle h, double aoa, double piv_pt, int64_t ita,
+                                     double deltat, double dxmin, double totime); /* src/Search.F90:49-124 */
+int bcfd_compute_surface_variables(bcfd_handle h, double phase_angle, double piv_pt, int64_t ita,
+                                   double deltat, double dxmin, double freq,
+                                   double totime);                             /* src/Search.F90:126-208 */
+/* inputs of app/main.F90 the native driver needs for moving bodies (phase
+ * angle in radians) and its time counters ita / totime, which bcfd_run_steps
+ * advances like main.F90:130-131 */
+int bcfd_set_motion_inputs(double phase_angle, double piv_pt, double freq, double dxmin, int64_t inor,
+                           int64_t ita, double totime);
+int bcfd_get_time(int64_t* ita, double* totime);
 int bcfd_tagging_th(bcfd_handle h);                         /* src/Search.F90:260-413  */
 int bcfd_selective_retagging_th(bcfd_handle h);             /* src/Search.F90:520-651  */
 int bcfd_cellcount_solid(bcfd_handle h);                    /* src/Search.F90:653-741  */

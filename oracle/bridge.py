@@ -47,6 +47,9 @@ def lib(checked: bool = True) -> C.CDLL:
             "orc_pressure_forcing1": [_i64], "orc_velocity_forcing_field": [_i64],
             "orc_pressure_forcing_field": [_i64], "orc_velocity_forcing_ghost": [_i64],
             "orc_pressure_forcing_ghost": [_i64], "orc_compute_surface_norm": [_i64, _i64],
+            "orc_node_ids_from_elements": [_i64],
+            "orc_shift_surface_nodes_initial": [_i64, _f64, _f64, _i64, _f64, _f64, _f64],
+            "orc_compute_surface_variables": [_i64, _f64, _f64, _i64, _f64, _f64, _f64, _f64],
             "orc_tagging_th_core": [_i64], "orc_selective_retagging": [_i64],
             "orc_cellcount_solid": [_i64], "orc_cellcount_solid_coarse": [_i64],
             "orc_compute_norm_distance": [_i64], "orc_find_ts_cells": [_i64],
@@ -135,6 +138,17 @@ class Oracle:
                 self.arr(g, "ibElP2")[:] = m.tris[:, 1]
                 self.arr(g, "ibElP3")[:] = m.tris[:, 2]
                 self.arr(g, "ibSurfId")[:] = m.surf_id
+                if spec.motion is not None:
+                    # app/main.F90:64-69: body-frame nodes, initial placement
+                    mo, mi = spec.motion, case.motion
+                    self.arr(g, "xnode")[:] = m.nodes[:, 0]
+                    self.arr(g, "ynode")[:] = m.nodes[:, 1]
+                    self.arr(g, "znode")[:] = m.nodes[:, 2]
+                    L.orc_node_ids_from_elements(g)
+                    for nm, v in (("a0", mo.a0_deg), ("bfreq", mo.bfreq), ("yamp", mo.yamp),
+                                  ("xshift", mo.shift[0]), ("yshift", mo.shift[1]), ("zshift", mo.shift[2])):
+                        self.setf(g, nm, v)
+                    L.orc_shift_surface_nodes_initial(g, mi.aoa_deg, mi.piv_pt, 0, case.dt, mi.dxmin, 0.0)
                 for nm, v in zip(("i_startSearch", "i_endSearch", "j_startSearch", "j_endSearch",
                                   "k_startSearch", "k_endSearch"), spec.search_box):
                     self.seti(g, nm, v)
@@ -164,6 +178,9 @@ class Oracle:
             L.orc_coefficient_matrix(g, 1 if spec.is_coarse else 0)
         for g in range(1, self.nblocks + 1):
             L.orc_non_uni_coeff(g)
+        # app/main.F90:45-46, 119: the time counters of the loop
+        self.ita = 0
+        self.totime = case.dt
 
     # ---- one time step, the phase order of app/main.F90:129-265 ------------
     def momentum_phase(self):
@@ -183,10 +200,18 @@ class Oracle:
         self.L.orc_poisson_solver(c.pc_ita_max, c.epsi, c.dt, c.uc)
 
     def research_phase(self):
-        L = self.L
+        L, c = self.L, self.case
         for g, spec in enumerate(self.case.blocks, 1):
             if spec.has_body:
                 L.orc_pressure_forcing1(g)
+        # app/main.F90:169-176, 213-215: moving bodies
+        for g, spec in enumerate(self.case.blocks, 1):
+            if spec.motion is not None:
+                mi = c.motion
+                self.seti(g, "blk_mv_tag", 0)
+                L.orc_compute_surface_variables(g, mi.phase_deg * np.pi / 180.0, mi.piv_pt, self.ita, c.dt,
+                                                mi.dxmin, mi.freq, self.totime)
+                L.orc_compute_surface_norm(g, spec.mesh.inor)
         for g, spec in enumerate(self.case.blocks, 1):
             if not spec.has_body:
                 continue
@@ -204,6 +229,9 @@ class Oracle:
             L.orc_pressure_forcing_ghost(g)
 
     def step(self):
+        # app/main.F90:130-131
+        self.ita += 1
+        self.totime += self.case.dt
         self.momentum_phase()
         self.poisson_phase()
         self.research_phase()

@@ -16,7 +16,7 @@ F1* f1_of(Block& b, const std::string& n) {
   M(element_length) M(pNormDis) M(u1NormDis) M(u2NormDis) M(v1NormDis) M(v2NormDis)
   M(w1NormDis) M(w2NormDis) M(p_ghost) M(pt_ghost) M(u2_ghost) M(u2t_ghost) M(v2_ghost)
   M(v2t_ghost) M(w2_ghost) M(w2t_ghost) M(u1_ghost) M(u1t_ghost) M(v1_ghost) M(v1t_ghost)
-  M(w1_ghost) M(w1t_ghost) M(xnode1) M(ynode1) M(znode1)
+  M(w1_ghost) M(w1t_ghost) M(xnode1) M(ynode1) M(znode1) M(xnode) M(ynode) M(znode)
 #undef M
   return nullptr;
 }
@@ -49,7 +49,7 @@ A2<double>* f2_of(Block& b, const std::string& n) {
 I1* i1_of(Block& b, const std::string& n) {
 #define M(x) if (n == #x) return &b.x;
   M(nelp) M(nelu1) M(nelu2) M(nelv1) M(nelv2) M(nelw1) M(nelw2) M(index_ts) M(ibSurfId)
-  M(ibElP1) M(ibElP2) M(ibElP3)
+  M(ibElP1) M(ibElP2) M(ibElP3) M(ibNodeId)
 #undef M
   return nullptr;
 }
@@ -58,6 +58,8 @@ double* fs_of(Block& b, const std::string& n) {
   M(dx) M(dy) M(dz) M(omega) M(derr1) M(derr2) M(derrStdSt) M(xdot) M(ydot) M(yddot)
   M(thetaDot) M(thetaDDot) M(thetaDot1) M(thetaDDot1) M(thetaDot2) M(thetaDDot2) M(alphaDot)
   M(piv_x) M(piv_y) M(piv_z) M(viscous_drag) M(pressure_drag) M(viscous_lift) M(pressure_lift)
+  M(a0) M(bfreq) M(yamp) M(xshift) M(yshift) M(zshift) M(xpth1) M(xpth2) M(ypth2) M(xchg) M(ychg)
+  M(xmove) M(ymove) M(zmove) M(xt) M(yt) M(inity_cent) M(nxty_cent) M(initx_cent) M(nxtx_cent)
 #undef M
   return nullptr;
 }
@@ -100,7 +102,8 @@ void orc_alloc_surface(int64_t g, int64_t n_elems, int64_t n_nodes) {
                 &b.element_length})
     a->alloc(n_elems);
   for (I1* a : {&b.ibSurfId, &b.ibElP1, &b.ibElP2, &b.ibElP3}) a->alloc(n_elems);
-  for (F1* a : {&b.xnode1, &b.ynode1, &b.znode1}) a->alloc(n_nodes);
+  for (F1* a : {&b.xnode1, &b.ynode1, &b.znode1, &b.xnode, &b.ynode, &b.znode}) a->alloc(n_nodes);
+  b.ibNodeId.alloc(n_nodes);
 }
 
 // Pointer to the storage of a named array; *n = element count, dims = extents
@@ -165,6 +168,15 @@ void orc_pressure_forcing_field(int64_t g) { pressure_forcing_field(blk_of(g)); 
 void orc_velocity_forcing_ghost(int64_t g) { velocity_forcing_ghost(blk_of(g)); }
 void orc_pressure_forcing_ghost(int64_t g) { pressure_forcing_ghost(blk_of(g)); }
 void orc_compute_surface_norm(int64_t g, int64_t inor) { compute_surface_norm(blk_of(g), inor); }
+void orc_node_ids_from_elements(int64_t g) { node_ids_from_elements(blk_of(g)); }
+void orc_shift_surface_nodes_initial(int64_t g, double aoa, double piv_pt, int64_t ita, double deltat,
+                                     double dxmin, double totime) {
+  shift_surface_nodes_initial(blk_of(g), aoa, piv_pt, ita, deltat, dxmin, totime);
+}
+void orc_compute_surface_variables(int64_t g, double phase_angle, double piv_pt, int64_t ita,
+                                   double deltat, double dxmin, double freq, double totime) {
+  compute_surface_variables(blk_of(g), phase_angle, piv_pt, ita, deltat, dxmin, freq, totime);
+}
 void orc_tagging_th_core(int64_t g) { tagging_th_core(blk_of(g)); }
 void orc_selective_retagging(int64_t g) { selective_retagging_th(blk_of(g)); }
 void orc_cellcount_solid(int64_t g) { cellcount_solid(blk_of(g)); }

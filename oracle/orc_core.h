@@ -140,6 +140,14 @@ struct Block {
       v1t_ghost, w1_ghost, w1t_ghost;
   I1 ibSurfId, ibElP1, ibElP2, ibElP3;
   F1 xnode1, ynode1, znode1;
+  // body-frame nodes and their surface ids (src/ReadInput.f90:376-420), and the
+  // rigid-body motion state of src/Search.F90:49-208
+  F1 xnode, ynode, znode;
+  I1 ibNodeId;
+  double a0 = 0, bfreq = 0, yamp = 0, xshift = 0, yshift = 0, zshift = 0;
+  double xpth1 = 0, xpth2 = 0, ypth2 = 0, xchg = 0, ychg = 0, xmove = 0, ymove = 0, zmove = 0;
+  double xt = 0, yt = 0, inity_cent = 0, nxty_cent = 0, initx_cent = 0, nxtx_cent = 0,
+         initz_cent = 0, nxtz_cent = 0;
   // drag/lift from the stress integration (src/StressCalc.f90)
   double viscous_drag = 0, pressure_drag = 0, viscous_lift = 0, pressure_lift = 0;
   // first error raised by a routine on this block (0 = none); the reference
@@ -206,6 +214,12 @@ void coarse_update_newv();
 void coarse_update_pc();
 void fine_update_mv(int64_t g);
 void stress_calculation(Block& b, double mu_f, double rho_f);
+// rigid-body motion (src/Search.F90:49-208, src/ReadInput.f90:403-420)
+void node_ids_from_elements(Block& b);
+void shift_surface_nodes_initial(Block& b, double aoa, double piv_pt, int64_t ita, double deltat,
+                                 double dxmin, double totime);
+void compute_surface_variables(Block& b, double phase_angle, double piv_pt, int64_t ita,
+                               double deltat, double dxmin, double freq, double totime);
 
 // interpolation primitives (src/Interpolation.f90:16-42)
 double linear_interpolation(double x, double x0, double x1, double y0, double y1);

@@ -1,0 +1,127 @@
+// Rigid-body motion of a block's surface, restated from the reference (test
+// infrastructure only): node surface ids (src/ReadInput.f90:403-420), the
+// initial placement shiftSurfaceNodesInitial (src/Search.F90:49-124) and the
+// per-step kinematics and node positions computeSurfaceVariables
+// (src/Search.F90:126-208).  Expressions keep the reference's evaluation
+// order; pi is modGlobal's 4*atan(1).
+#include <cmath>
+
+#include "orc_core.h"
+
+namespace orc {
+namespace {
+const double kPi = 4.0 * std::atan(1.0);
+const double kXfact = 0.05;  // src/Search.F90:12
+
+// rotation of a surface-51/52 node about the x axis through z = piv_pt
+void place(Block& b, int64_t i, double aoa1, double aoa2, double piv_pt, double& xr1, double& yr1,
+           double& zr1) {
+  const int64_t id = b.ibNodeId(i);
+  if (id == 51 || id == 52) {
+    const double a = id == 51 ? aoa1 : aoa2;
+    xr1 = b.xnode(i);
+    zr1 = b.znode(i) * std::cos(a) + b.ynode(i) * std::sin(a) + piv_pt - piv_pt * std::cos(a);
+    yr1 = -(b.znode(i) * std::sin(a)) + b.ynode(i) * std::cos(a) + piv_pt * std::sin(a);
+  } else {
+    xr1 = b.xnode(i);
+    zr1 = b.znode(i);
+    yr1 = b.ynode(i);
+  }
+}
+}  // namespace
+
+void node_ids_from_elements(Block& b) {
+  b.ibNodeId.alloc(b.ibNodes);
+  for (int64_t i = 1; i <= b.ibNodes; ++i) b.ibNodeId(i) = 50;
+  for (int64_t n = 1; n <= b.ibElems; ++n) {
+    const int64_t s = b.ibSurfId(n);
+    if (s == 51 || s == 52) {
+      b.ibNodeId(b.ibElP1(n)) = s;
+      b.ibNodeId(b.ibElP2(n)) = s;
+      b.ibNodeId(b.ibElP3(n)) = s;
+    }
+  }
+  for (int64_t n = 1; n <= b.ibElems; ++n)
+    if (b.ibSurfId(n) == 50) {
+      b.ibNodeId(b.ibElP1(n)) = 50;
+      b.ibNodeId(b.ibElP2(n)) = 50;
+      b.ibNodeId(b.ibElP3(n)) = 50;
+    }
+}
+
+void shift_surface_nodes_initial(Block& b, double aoa, double piv_pt, int64_t ita, double deltat,
+                                 double dxmin, double totime) {
+  const double aoa1 = aoa * kPi / 180.0, aoa2 = -aoa1;
+  const double bdfr = 15, bdy = 15 * dxmin;
+  b.xmove = 0.0;
+  b.ymove = 0.0;
+  b.zmove = 0.0;
+  b.a0 = b.a0 * kPi / 180.0;
+  const double angt = 2.0 * kPi * b.bfreq;
+  b.xpth1 = b.xshift - ((double)ita * dxmin * kXfact);
+  b.xpth2 = b.xshift - ((double)ita * dxmin * kXfact);
+  b.ypth2 = (b.yamp) * std::sin(angt * b.xshift);
+  b.piv_x = b.xshift;
+  b.piv_y = b.yshift;
+  b.piv_z = b.zshift;
+  b.thetaDot = b.thetaDDot = b.thetaDot1 = b.thetaDot2 = b.alphaDot = 0.0;
+  b.thetaDDot1 = b.thetaDDot2 = 0.0;
+  b.yt = bdy * std::sin(2 * kPi * bdfr * totime);
+  b.ydot = angt * bdy * std::cos(2 * kPi * bdfr * totime);
+  b.yddot = -(angt * angt * bdy * std::sin(2 * kPi * bdfr * totime));
+  b.xt = b.xshift - ((double)ita * dxmin * kXfact);
+  b.xdot = -(dxmin * kXfact) / deltat;
+  b.inity_cent = b.yshift;
+  b.nxty_cent = b.yshift;
+  b.initx_cent = b.xshift;
+  b.nxtx_cent = b.xshift;
+  b.initz_cent = b.zshift;
+  b.nxtz_cent = b.zshift;
+  for (int64_t i = 1; i <= b.ibNodes; ++i) {
+    double xr1, yr1, zr1;
+    place(b, i, aoa1, aoa2, piv_pt, xr1, yr1, zr1);
+    b.xnode1(i) = xr1 + b.xshift;
+    b.ynode1(i) = yr1 + b.yshift;
+    b.znode1(i) = zr1 + b.zshift;
+  }
+}
+
+void compute_surface_variables(Block& b, double phase_angle, double piv_pt, int64_t ita,
+                               double deltat, double dxmin, double freq, double totime) {
+  const double aoa1 = (b.a0) * std::sin(2.0 * kPi * freq * (totime + deltat) + phase_angle);
+  const double aoa2 = -aoa1;
+  const double ang_theta = 2.0 * kPi * freq;
+  const double bdfr = b.bfreq, bdy = b.yamp;
+  const double angt = 2.0 * kPi * bdfr;
+  b.xpth2 = b.xshift - ((double)ita * dxmin * kXfact);
+  b.ypth2 = (b.yamp) * std::sin(angt * b.xpth2);
+  b.xchg = b.xpth2 - b.xpth1;
+  b.xpth1 = b.xpth2;
+  b.thetaDot1 = ang_theta * b.a0 * std::cos(2.0 * kPi * freq * (totime + deltat) + phase_angle);
+  b.thetaDDot1 = -(ang_theta * ang_theta * b.a0 * std::sin(2.0 * kPi * freq * (totime + deltat) + phase_angle));
+  b.thetaDot2 = -b.thetaDot1;
+  b.thetaDDot2 = -b.thetaDDot1;
+  b.yt = bdy * std::sin(angt * (totime));
+  b.ydot = angt * bdy * std::cos(angt * (totime));
+  b.yddot = -(angt * angt * bdy * std::sin(angt * (totime)));
+  b.xt = b.xpth2;
+  b.xdot = -(dxmin * kXfact) / deltat;
+  b.ychg = b.yt - bdy * std::sin(angt * (totime - deltat));
+  b.ymove = b.yt;
+  b.xmove = b.xchg;
+  b.zmove = 0.0;
+  b.piv_y = b.piv_y + b.ychg;
+  b.piv_x = b.piv_x + b.xmove;
+  b.piv_z = b.piv_z + b.zmove;
+  b.nxty_cent = b.nxty_cent + b.ychg;
+  b.nxtx_cent = b.nxtx_cent + b.xmove;
+  for (int64_t i = 1; i <= b.ibNodes; ++i) {
+    double xr1, yr1, zr1;
+    place(b, i, aoa1, aoa2, piv_pt, xr1, yr1, zr1);
+    b.xnode1(i) = xr1 + b.xpth2;
+    b.ynode1(i) = yr1 + b.yshift + b.ymove;
+    b.znode1(i) = zr1 + b.zshift + b.zmove;
+  }
+}
+
+}  // namespace orc

@@ -226,17 +226,22 @@ def sweep_roofline(torch, local, hbm, block=(384, 256, 256), fp32_pairs=40, fp64
     return out
 
 
-def twelve_block(torch, local, steps=10, warmup=3, fp64_steps=2):
+def twelve_block(torch, local, steps=10, warmup=3, fp64_steps=2, moving=False):
     """Twelve uneven blocks (coarse 256x192x192 + 11 fine blocks, 13.3M cells,
     stationary thin plate): mixed-path time per step with the batched launches
     and with one launch per block, and the plain FP64 path to the same residual.
     The working set (> 2 GB) is far above L2, so no flush is needed."""
     from biocfd import synth
     from biocfd.solver import Solver
-    case = synth.twelve_block(n_steps=steps + warmup + 2)
+    case = synth.twelve_block(n_steps=steps + warmup + 2, moving=moving)
+    ncells = sum(b.nx * b.ny * b.nz for b in case.blocks)
+    body = case.blocks[1]
     out = {"workload": "12 blocks: coarse 256x192x192 over 8x6x6 + 11 fine blocks at ratio 2 "
-                       "(160x96x96 with a plate 0.5x0.125x0.0125, 2x128x64x64, 2x96x64x64, "
-                       "2x64x48x48, 2x48^3, 2x32^3), 13.3M cells, Re 500",
+                       f"({body.nx}x{body.ny}x{body.nz} with a plate 0.5x0.125x0.0125, 2x128x64x64, 2x96x64x64, "
+                       f"2x64x48x48, 2x48^3, 2x32^3), {ncells / 1e6:.1f}M cells, Re 500" +
+                       (", plate heaving 0.5 sin(2 pi 0.25 t) and pitching 30 deg sin(2 pi 0.25 t + 90 deg), "
+                        "Search every step, steps issued kernel by kernel" if moving else
+                        ", stationary plate, graph replay"),
            "div_tol": DIV_TOL}
     arms = (("mixed_batched", 1, True, steps), ("mixed_per_block", 1, False, steps),
             ("fp64_batched", 2, True, fp64_steps))
@@ -264,7 +269,7 @@ def twelve_block(torch, local, steps=10, warmup=3, fp64_steps=2):
         ms = statistics.mean(ts)
         out[key] = {"ms_per_step": ms, "steps_per_s": 1000.0 / ms, "steps": n, "div_residual": res,
                     "launches_per_step": (s.kernel_launches() - k0) / n,
-                    "cell_updates_per_s": 13328384 * 1000.0 / ms}
+                    "cell_updates_per_s": ncells * 1000.0 / ms}
         s.close()
     if "fp64_batched" in out:
         out["speedup_mixed_vs_fp64"] = out["fp64_batched"]["ms_per_step"] / out["mixed_batched"]["ms_per_step"]
@@ -394,6 +399,7 @@ def run_gpu(args):
         line["sweep_roofline"] = sweep_roofline(torch, local, hbm)
     if not args.no_twelve_block:
         line["twelve_block"] = twelve_block(torch, local)
+        line["twelve_block_moving"] = twelve_block(torch, local, steps=5, fp64_steps=1, moving=True)
     if rank == 0 and not args.no_cpu_baseline:
         sps, secs = oracle_steps(case, 1)
         line["cpu_baseline"] = {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
@@ -422,6 +428,7 @@ def main():
     if args.twelve_only:
         import torch
         print(json.dumps(twelve_block(torch, 0, args.steps, args.warmup)), flush=True)
+        print(json.dumps(twelve_block(torch, 0, args.steps, args.warmup, fp64_steps=1, moving=True)), flush=True)
         return
     if args.sweep_only:
         import torch

@@ -313,7 +313,8 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
                             ((2.375, 2.75), (1.0, 1.5), (0.375, 0.75))),
                 body: int = 0, diameter: float = 0.25, reynolds: float = 300.0, n_steps: int = 2,
                 omega: float = 1.7, pc_ita_max: int = 5000, seed: int = SEED, plate: bool = False,
-                plate_axes=None) -> Case:
+                plate_axes=None, motion: Optional[Motion] = None,
+                motion_inputs: Optional[MotionInputs] = None) -> Case:
     """A coarse block with several nested fine blocks of uneven sizes at ratio 2
     (one interface per fine block), a stationary sphere (or, with `plate`, a
     thin plate of surface 51) in fine block `body`.  Box edges must lie on
@@ -338,8 +339,16 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
             dxf = (box[0][1] - box[0][0]) / n[0]
             if plate:
                 ax = np.array([0.4, 0.3, 0.1]) * diameter if plate_axes is None else np.asarray(plate_axes)
-                fs.mesh = ellipsoid_plate(c, ax, 0.5 * dxf)
-                fs.search_box = search_box_for(fs, c - ax, c + ax)
+                if motion is not None:
+                    # body-frame mesh placed by the motion; the search box
+                    # covers the heave and the pitch
+                    fs.mesh = ellipsoid_plate((0.0, 0.0, 0.0), ax, 0.5 * dxf)
+                    fs.motion = dataclasses.replace(motion, shift=tuple(c))
+                    reach = ax + np.array([0.0, motion.yamp + ax[1], ax[1]])
+                    fs.search_box = search_box_for(fs, c - reach, c + reach)
+                else:
+                    fs.mesh = ellipsoid_plate(c, ax, 0.5 * dxf)
+                    fs.search_box = search_box_for(fs, c - ax, c + ax)
             else:
                 fs.mesh = fibonacci_sphere(c, diameter, dxf)
                 fs.search_box = search_box_for(fs, c - diameter / 2, c + diameter / 2)
@@ -350,6 +359,7 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
     dxf = d[0] / ratio
     case = Case(name=f"multi_{len(blocks)}", blocks=blocks, interfaces=ifs, dt=0.3 * dxf,
                 re=reynolds / diameter, uc=1.0, epsi=1e-6, pc_ita_max=pc_ita_max, n_steps=n_steps)
+    case.motion = motion_inputs
     case.init = [noisy_initial(b, case.uc, rng) for b in case.blocks]
     return case
 
@@ -372,12 +382,22 @@ TWELVE_BLOCK_BOXES = (
 )
 
 
-def twelve_block(n_steps: int = 10, seed: int = SEED) -> Case:
-    """Twelve blocks of uneven sizes around a stationary rigid ellipsoidal
-    plate (semi-axes 0.5 x 0.125 x 0.0125, surface 51), Re = 500 on the chord."""
-    return multi_block(coarse=(256, 192, 192), domain=(8.0, 6.0, 6.0), fine_boxes=TWELVE_BLOCK_BOXES,
+def twelve_block(n_steps: int = 10, seed: int = SEED, moving: bool = False) -> Case:
+    """Twelve blocks of uneven sizes around a rigid ellipsoidal plate (semi-axes
+    0.5 x 0.125 x 0.0125, surface 51), Re = 500 on the chord.  With `moving`
+    the plate heaves h(t) = 0.5 sin(2 pi 0.25 t) and pitches about x
+    theta(t) = 30 deg sin(2 pi 0.25 t + 90 deg) (plus the reference's fixed
+    tow); its block is then 160x144x96, tall enough that the heave stays inside
+    the reference's block-move margins (src/Search.F90:1010-1024)."""
+    boxes = list(TWELVE_BLOCK_BOXES)
+    motion = inputs = None
+    if moving:
+        boxes[0] = ((0.5, 3.0), (0.25, 2.5), (0.5, 2.0))
+        motion = Motion(a0_deg=30.0, bfreq=0.25, yamp=0.5)
+        inputs = MotionInputs(aoa_deg=0.0, phase_deg=90.0, piv_pt=0.0, freq=0.25, dxmin=1.0 / 64.0)
+    return multi_block(coarse=(256, 192, 192), domain=(8.0, 6.0, 6.0), fine_boxes=tuple(boxes),
                        body=0, diameter=1.0, reynolds=500.0, n_steps=n_steps, seed=seed, plate=True,
-                       plate_axes=(0.5, 0.125, 0.0125))
+                       plate_axes=(0.5, 0.125, 0.0125), motion=motion, motion_inputs=inputs)
 
 
 def uniform_block(n=(384, 256, 256), lengths=(3.0, 2.0, 2.0), seed: int = SEED,

@@ -42,6 +42,8 @@ _SIGS = {
     "bcfd_block_set_mixed_params": [c_i64, c_i64, c_double, c_int],
     "bcfd_block_set_solve_launch": [c_i64, c_int, c_int, c_int],
     "bcfd_set_batching": [c_int],
+    "bcfd_poisson_solve_zero_bc": [c_i64, P_d, P_d, c_double, c_i64],
+    "bcfd_poisson_solve_adjoint": [c_i64, P_d, P_d, c_double, c_i64],
     "bcfd_block_set_body_motion": [c_i64, P_d],
     "bcfd_shift_surface_nodes_initial": [c_i64, c_double, c_double, c_i64, c_double, c_double, c_double],
     "bcfd_compute_surface_variables": [c_i64, c_double, c_double, c_i64, c_double, c_double, c_double,

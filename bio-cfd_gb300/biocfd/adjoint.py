@@ -1,0 +1,55 @@
+"""Adjoint of the pressure Poisson solve as a torch.autograd.Function.
+
+forward:  x = A^{-1} r      (bcfd_poisson_solve_zero_bc)
+backward: r_bar = A^{-T} x_bar (bcfd_poisson_solve_adjoint: the same SOR kernel
+          with the transposed line tables and reversed colour order)
+
+A is the Poisson operator of one block restricted to its fluid cells (zero
+data on the other cells).  Arrays are natural-layout (nx+2, ny+2, nz+2) FP64,
+x-fastest, like the block's fields.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from ._lib import check
+
+
+def _solve(solver, g: int, r: np.ndarray, tol: float, itmax: int, adjoint: bool) -> np.ndarray:
+    r = np.asfortranarray(r, dtype=np.float64)
+    x = np.zeros_like(r, order="F")
+    fn = solver.L.bcfd_poisson_solve_adjoint if adjoint else solver.L.bcfd_poisson_solve_zero_bc
+    check(fn(g, r.ctypes.data_as(C.POINTER(C.c_double)), x.ctypes.data_as(C.POINTER(C.c_double)), tol, itmax),
+          "poisson_solve_adjoint" if adjoint else "poisson_solve_zero_bc")
+    return x
+
+
+def poisson_solve(solver, g: int, r: np.ndarray, tol: float = 1e-12, itmax: int = 200000) -> np.ndarray:
+    """x = A^{-1} r on block g (FP64 SOR to max|r - A x| <= tol)."""
+    return _solve(solver, g, r, tol, itmax, False)
+
+
+def poisson_solve_adjoint(solver, g: int, r: np.ndarray, tol: float = 1e-12, itmax: int = 200000) -> np.ndarray:
+    """x = A^{-T} r on block g."""
+    return _solve(solver, g, r, tol, itmax, True)
+
+
+def poisson_function(solver, g: int, tol: float = 1e-12, itmax: int = 200000):
+    """A torch.autograd.Function applying A^{-1} of block g to a float64 tensor
+    of the block's point shape; its backward applies A^{-T}."""
+    import torch
+
+    class PoissonSolve(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, r):
+            x = poisson_solve(solver, g, r.detach().cpu().numpy(), tol, itmax)
+            return torch.from_numpy(np.ascontiguousarray(x)).to(r)
+
+        @staticmethod
+        def backward(ctx, gx):
+            gr = poisson_solve_adjoint(solver, g, gx.detach().cpu().numpy(), tol, itmax)
+            return torch.from_numpy(np.ascontiguousarray(gr)).to(gx)
+
+    return PoissonSolve

@@ -1,0 +1,106 @@
+// Adjoint of the pressure Poisson solve.  The solve of src/PcorVcor.F90
+// (REDBLACKSOR_linear) inverts A restricted to the fluid cells, where row
+// (i,j,k) of A is the 7-point stencil of the Acx/Acy/Acz line tables
+// (src/CoefficientMatrix.f90:10-71).  A is not symmetric on a stretched grid
+// or with the coarse block's boundary folding, but its transpose is again a
+// 7-point operator of three line tables: in row i the coefficient of i-1 is
+// row i-1's right coefficient and that of i+1 is row i+1's left coefficient;
+// the diagonal is unchanged.  So the adjoint solve A^T x = r is the same
+// persistent red-black SOR kernel run with the transposed tables and the
+// colour sweeps in reverse order (black first).  Non-fluid cells are zero
+// Dirichlet data for both solves (the adjoint of the boundary coupling is not
+// part of this entry point).
+#include <cstring>
+
+#include "bcfd_host.h"
+
+namespace bcfd {
+namespace {
+
+// transpose of one (n,3) line table
+std::vector<double> transpose_line(const std::vector<double>& A, int n) {
+  std::vector<double> T(3 * (size_t)n, 0.0);
+  for (int i = 2; i <= n + 1; ++i) {
+    T[(i - 2)] = i >= 3 ? A[(i - 3) + 2 * (size_t)n] : 0.0;
+    T[(i - 2) + n] = A[(i - 2) + (size_t)n];
+    T[(i - 2) + 2 * (size_t)n] = i <= n ? A[(i - 1)] : 0.0;
+  }
+  return T;
+}
+
+int solve_zero_bc(HostBlock* hb, const double* r, double* x, double tol, int64_t itmax, bool transpose) {
+  DevBlock& D = hb->d;
+  const Dims& d = D.d;
+  if (!D.Acx || hb->Acx.empty()) return BCFD_E_STATE;
+  const double* keep[3] = {D.Acx, D.Acy, D.Acz};
+  const int keep_rev = hb->sor_rev;
+  double* tab = nullptr;
+  double* nat = nullptr;
+  int rc = 0;
+  const size_t np = (size_t)d.npts();
+  if (cudaMalloc(&nat, np * sizeof(double)) != cudaSuccess) return BCFD_E_NOMEM;
+  if (transpose) {
+    const std::vector<double> tx = transpose_line(hb->Acx, d.nx), ty = transpose_line(hb->Acy, d.ny),
+                              tz = transpose_line(hb->Acz, d.nz);
+    std::vector<double> all(tx);
+    all.insert(all.end(), ty.begin(), ty.end());
+    all.insert(all.end(), tz.begin(), tz.end());
+    if (cudaMalloc(&tab, all.size() * sizeof(double)) != cudaSuccess) {
+      cudaFree(nat);
+      return BCFD_E_NOMEM;
+    }
+    if (cudaMemcpy(tab, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) rc = BCFD_E_CUDA;
+    D.Acx = tab;
+    D.Acy = tab + tx.size();
+    D.Acz = tab + tx.size() + ty.size();
+    hb->sor_rev = 1;
+  }
+  const size_t pbytes = (size_t)d.npacked() * sizeof(double);
+  for (int c = 0; c < 2 && !rc; ++c) {
+    if (cudaMemsetAsync(D.pc[c], 0, pbytes, stream()) != cudaSuccess) rc = BCFD_E_CUDA;
+    if (!rc && cudaMemsetAsync(D.bpk[c], 0, pbytes, stream()) != cudaSuccess) rc = BCFD_E_CUDA;
+  }
+  if (!rc && cudaMemsetAsync(&D.stats->niter, 0, sizeof(int64_t), stream()) != cudaSuccess) rc = BCFD_E_CUDA;
+  if (!rc && cudaMemcpyAsync(nat, r, np * sizeof(double), cudaMemcpyHostToDevice, stream()) != cudaSuccess)
+    rc = BCFD_E_CUDA;
+  if (!rc) rc = launch_pack(hb, nat, D.bpk);
+  // residual-target FP64 solve of A x = r (deltat = 1)
+  if (!rc) rc = launch_sor(hb, itmax, 1.0, 0.0, tol);
+  if (!rc) rc = launch_unpack(hb, D.pc, nat);
+  if (!rc && cudaMemcpyAsync(x, nat, np * sizeof(double), cudaMemcpyDeviceToHost, stream()) != cudaSuccess)
+    rc = BCFD_E_CUDA;
+  if (!rc && cudaStreamSynchronize(stream()) != cudaSuccess) rc = BCFD_E_CUDA;
+  D.Acx = keep[0];
+  D.Acy = keep[1];
+  D.Acz = keep[2];
+  hb->sor_rev = keep_rev;
+  cudaFree(tab);
+  cudaFree(nat);
+  if (rc) return rc;
+  return take_block_error(hb);
+}
+
+}  // namespace
+}  // namespace bcfd
+
+using namespace bcfd;
+
+extern "C" {
+
+int bcfd_poisson_solve_zero_bc(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax) {
+  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  HostBlock* hb = get_block(h);
+  if (!hb) return BCFD_E_HANDLE;
+  if (!r || !x || !(tol > 0.0) || itmax < 1) return BCFD_E_ARG;
+  return solve_zero_bc(hb, r, x, tol, itmax, false);
+}
+
+int bcfd_poisson_solve_adjoint(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax) {
+  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  HostBlock* hb = get_block(h);
+  if (!hb) return BCFD_E_HANDLE;
+  if (!r || !x || !(tol > 0.0) || itmax < 1) return BCFD_E_ARG;
+  return solve_zero_bc(hb, r, x, tol, itmax, true);
+}
+
+}  // extern "C"

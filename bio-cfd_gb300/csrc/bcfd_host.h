@@ -57,6 +57,7 @@ struct HostBlock {
   int solve_threads = 0;           // threads per CTA of the tiled solves (0: 256)
   int solve_ctas_per_sm = 0;       // co-resident CTAs per SM cap (0: occupancy limit)
   int solve_sync = 0;              // FP64 solve: 0 point-to-point, 1 grid-wide phase barriers
+  int sor_rev = 0;                 // FP64 solve: black half-sweep first (adjoint solves)
   int dc_threads = 0;              // FP32 correction: threads per CTA (0: 256)
   int dc_ctas_per_sm = 0;          // FP32 correction: CTAs per SM cap (0: occupancy limit)
   // largest distance of a surface node from the block centre (for the FP32

@@ -292,6 +292,7 @@ struct SorArgs {
   double res_tol; // > 0: stop on dt * max|b/dt - A pc| <= res_tol instead of
                   // the reference's increment test (same check cadence)
   double dt;
+  int rev;        // 1: black half-sweep first (the adjoint solve's order)
 };
 
 // append {sweep pairs, FP64 residual passes, fluid cells, precision}
@@ -342,10 +343,12 @@ __device__ __forceinline__ void sor64_body(const DevBlock& B, const SorArgs& a, 
     if (++r5 == 5) r5 = 0;
     double lmax = 0.0;
     if (!tile_wait(tm, gb, t, ph)) { ok = false; break; }
-    tile_half64<1>(B, t, a.omega, lmax);
+    if (a.rev) tile_half64<0>(B, t, a.omega, lmax);
+    else tile_half64<1>(B, t, a.omega, lmax);
     tile_publish(tm, t, ++ph);
     if (!tile_wait(tm, gb, t, ph)) { ok = false; break; }
-    tile_half64<0>(B, t, a.omega, lmax);
+    if (a.rev) tile_half64<1>(B, t, a.omega, lmax);
+    else tile_half64<0>(B, t, a.omega, lmax);
     tile_publish(tm, t, ++ph);
     if (r5 == 0) {
       if (a.res_tol > 0.0) {
@@ -863,7 +866,7 @@ int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_
   TileMap tm = choose_tiles(hb, (const void*)k_sor64, threads, hb->solve_sync == 1 ? 1 : 0, hb->solve_ctas_per_sm);
   TRY_R(reset_solve_state(hb, tm));
   const unsigned grid = (unsigned)(tm.ntj * tm.ntk);
-  SorArgs a{itmax, epsi, hb->omega, prof_log(), res_tol, dt};
+  SorArgs a{itmax, epsi, hb->omega, prof_log(), res_tol, dt, hb->sor_rev};
   GridBar gb = make_bar(B.err, grid);
   gb.ctr = reinterpret_cast<unsigned long long*>(hb->bar);
   void* args[] = {(void*)&B, (void*)&a, (void*)&gb, (void*)&tm};
@@ -986,7 +989,7 @@ int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt,
     BCFD_LAUNCHED();
   }
   auto make = [&](HostBlock* hb, SorArgs& a) -> int {
-    a = SorArgs{itmax, epsi, hb->omega, prof_log(), res_tol, dt};
+    a = SorArgs{itmax, epsi, hb->omega, prof_log(), res_tol, dt, hb->sor_rev};
     // blocks with their own launch shape keep their own launch
     return hb->solve_threads > 0 || hb->solve_sync != 0 || hb->solve_ctas_per_sm > 0;
   };

@@ -188,6 +188,16 @@ int bcfd_coarse_update_newv(void);             /* src/CoarseInterp.f90:206-346  
 int bcfd_coarse_update_pc(void);               /* src/CoarseInterp.f90:347-437      */
 int bcfd_fine_update_mv(bcfd_handle it);       /* src/FineInterp.f90:10-281         */
 
+/* ---- adjoint of the pressure Poisson solve (no counterpart in the reference) --
+ * Both solve on the fluid cells of a block with zero boundary data, FP64
+ * red-black SOR to max|r - A x| <= tol (at most itmax sweep pairs); r and x
+ * are natural-layout (nx+2)(ny+2)(nz+2) arrays, x is 0 off the fluid cells.
+ * The adjoint runs the same solve kernel with the transposed line tables of
+ * A and the colour sweeps in reverse order.  They use the block's Poisson
+ * arrays as scratch (call between time steps). */
+int bcfd_poisson_solve_zero_bc(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax);
+int bcfd_poisson_solve_adjoint(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax);
+
 /* ---- drag / lift (src/StressCalc.f90:14-208, FP64, deterministic order) --- */
 /* out[4] = viscous drag, pressure drag, viscous lift, pressure lift coefficients */
 int bcfd_stress_calculation(bcfd_handle h, double mu_f, double rho_f, double* out);

@@ -118,6 +118,30 @@ def dist_env():
         int(os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(values):
+    """Each value's maximum over the ranks of the process group (the values of
+    this process when no group is initialised).  Replicas only: this all-reduce
+    of a few timings is the sole collective."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(x) for x in t]
+
+
+def rank_barrier(torch):
+    """Barrier over the replicas (when a group exists) and a device synchronize."""
+    import torch.distributed as dist
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+    if dist.is_available() and dist.is_initialized():
+        dist.barrier()
+    if torch.cuda.is_available():
+        torch.cuda.synchronize()
+
+
 def oracle_steps(case, n_steps: int):
     """Serial FP64 oracle (CPU): steps/s over n_steps steps after set-up."""
     from oracle.bridge import Oracle
@@ -163,6 +187,7 @@ def time_path(solver, torch, flush, stream, steps: int, warmup: int, precision: 
     times, divs, res, iters = [], [], [], []
     ctx = clocks if clocks is not None else _Null()
     k0 = solver.kernel_launches()
+    rank_barrier(torch)
     with ctx:
         for _ in range(steps):
             with torch.cuda.stream(stream):
@@ -178,6 +203,7 @@ def time_path(solver, torch, flush, stream, steps: int, warmup: int, precision: 
             divs.append(max(x[0] for x in d))
             res.append(max(x[1] for x in d))
             iters.append([solver.sor_stats(g)[0] for g in solver.handles])
+    rank_barrier(torch)
     launches = solver.kernel_launches() - k0
     solver.profile_begin()
     solver.run(1, precision=precision, div_tol=div_tol)
@@ -348,11 +374,7 @@ def run_gpu(args):
     ms0 = statistics.mean(t0_)
     msmx = statistics.mean(tmx)
     e2e_s = statistics.mean(e2e_times)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([msmx, ms64, e2e_s], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        msmx, ms64, e2e_s = (float(x) for x in t)
+    msmx, ms64, ms0, e2e_s = max_over_ranks([msmx, ms64, ms0, e2e_s])
     nfluid = sum(s.counts(g)["fluidCellCount"] for g in s.handles)
     hbm, peak_kind = peaks()
     achieved = profmx["sor_bytes"] / (profmx["sor_ms"] * 1e-3) / 1e9 if profmx["sor_ms"] > 0 else 0.0

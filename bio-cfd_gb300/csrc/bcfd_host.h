@@ -186,6 +186,8 @@ int launch_forcing_pressure(HostBlock* hb, int mode);
 int launch_face_fill(HostInterface* it, int comp, int which);  // which: 0 t-fields, 1 pc, 2 n-fields
 int launch_restrict(HostInterface* it, int comp, int which);
 int launch_fine_update_mv(HostInterface* it);
+// op 0: face fill P, 1: P^T (accumulates), 2: restriction R, 3: R^T (accumulates)
+int coupling_apply(HostInterface* it, int comp, int op, const double* in, double* out);
 // k_stress.cu
 int launch_stress(HostBlock* hb, double mu_f, double rho_f, double* out_host);
 // k_motion.cu

@@ -409,6 +409,36 @@ int bcfd_interface_table(bcfd_handle h, const char* name, int64_t* out, int64_t 
   return BCFD_E_ARG;
 }
 
+int bcfd_coupling_apply(bcfd_handle h, int comp, int op, const double* in, double* out) {
+  LOCK();
+  HostInterface* it = get_iface(h);
+  if (!it) return BCFD_E_HANDLE;
+  if (!in || !out || comp < 0 || comp > 3 || op < 0 || op > 3) return BCFD_E_ARG;
+  HostBlock* a = get_block(it->a);
+  HostBlock* b = get_block(it->b);
+  if (!a || !b) return BCFD_E_HANDLE;
+  // 0 P (coarse -> fine), 1 P^T (fine -> coarse), 2 R (fine -> coarse),
+  // 3 R^T (coarse -> fine)
+  const size_t na = (size_t)a->d.d.npts(), nb = (size_t)b->d.d.npts();
+  const size_t nin = (op == 0 || op == 3) ? na : nb, nout = (op == 0 || op == 3) ? nb : na;
+  double *din = nullptr, *dout = nullptr;
+  BCFD_CUDA(cudaMalloc(&din, nin * sizeof(double)));
+  if (cudaMalloc(&dout, nout * sizeof(double)) != cudaSuccess) {
+    cudaFree(din);
+    return BCFD_E_NOMEM;
+  }
+  int r = 0;
+  if (cudaMemcpy(din, in, nin * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
+      cudaMemcpy(dout, out, nout * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+    r = BCFD_E_CUDA;
+  if (!r) r = coupling_apply(it, comp, op, din, dout);
+  if (!r && cudaStreamSynchronize(stream()) != cudaSuccess) r = BCFD_E_CUDA;
+  if (!r && cudaMemcpy(out, dout, nout * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) r = BCFD_E_CUDA;
+  cudaFree(din);
+  cudaFree(dout);
+  return r;
+}
+
 int bcfd_fine_update_pc_bd(void) { LOCK(); return fine_update_pc_bd(); }
 int bcfd_fine_update_newv_bd(void) { LOCK(); return fine_update_newv_bd(); }
 int bcfd_fine_update_bd_mv(bcfd_handle h) {

@@ -129,6 +129,127 @@ __global__ void k_restrict(Dims da, Dims db, FaceArgs a, int ci) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoints of the coupling (transposed trilinear interpolation).
+// ---------------------------------------------------------------------------
+// the trilinear weights of k_face for target (x,y,z): corner q = a + 2b + 4c
+// of the donor box (a: x+1, b: y+1, c: z+1), in the forward's algebra
+__device__ __forceinline__ void face_weights(double x, double y, double z, double x1, double x2, double y1,
+                                             double y2, double z1, double z2, double* w) {
+  const double den = (x2 - x1) * (y2 - y1);
+  const double b00 = (x2 - x) * (y2 - y) / den, b10 = (x - x1) * (y2 - y) / den,
+               b01 = (x2 - x) * (y - y1) / den, b11 = (x - x1) * (y - y1) / den;
+  const double tz = (z - z1) / (z2 - z1);
+  const double za = 1.0 - tz;
+  w[0] = b00 * za; w[1] = b10 * za; w[2] = b01 * za; w[3] = b11 * za;
+  w[4] = b00 * tz; w[5] = b10 * tz; w[6] = b01 * tz; w[7] = b11 * tz;
+}
+
+// Face-fill adjoint, stage 1: every entry triple on the shell (first or last
+// entry along some axis: the face passes visit exactly these) sums its
+// targets' adjoints times their weights per donor corner, in a fixed order.
+// Each target belongs to exactly one entry triple, so it is counted once,
+// although the forward's face passes may write it twice (with one value).
+__global__ void k_face_adj1(Dims db, FaceArgs a, const double* gbar, double* part) {
+  const int cx = a.tx.c, cy = a.ty.c, cz = a.tz.c;
+  const int n = cx * cy * cz;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int ei = 1 + t % cx, ej = 1 + (t / cx) % cy, ek = 1 + t / (cx * cy);
+    double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    const bool shell = ei == 1 || ei == cx || ej == 1 || ej == cy || ek == 1 || ek == cz;
+    if (shell) {
+      const int i = a.tx.at(1, ei), j = a.ty.at(1, ej), k = a.tz.at(1, ek);
+      const double x1 = a.ga.x[i - 2], x2 = a.ga.x[i], y1 = a.ga.y[j - 2], y2 = a.ga.y[j],
+                   z1 = a.ga.z[k - 2], z2 = a.ga.z[k];
+      for (int tz = a.tz.at(2, ek); tz <= a.tz.at(3, ek); ++tz)
+        for (int ty = a.ty.at(2, ej); ty <= a.ty.at(3, ej); ++ty)
+          for (int tx = a.tx.at(2, ei); tx <= a.tx.at(3, ei); ++tx) {
+            double w[8];
+            face_weights(a.gb.x[tx - 1], a.gb.y[ty - 1], a.gb.z[tz - 1], x1, x2, y1, y2, z1, z2, w);
+            const int ox = tx - (a.comp == 1), oy = ty - (a.comp == 2), oz = tz - (a.comp == 3);
+            const double g = gbar[db.idx(ox, oy, oz)];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc[q] += w[q] * g;
+          }
+    }
+#pragma unroll
+    for (int q = 0; q < 8; ++q) part[8 * (int64_t)t + q] = acc[q];
+  }
+}
+
+// inverse of an interface table: coarse index -> entry (1-based), 0 if none
+__device__ __forceinline__ int entry_of(const Tab& tb, int ci) {
+  int lo = 1, hi = tb.c;
+  while (lo <= hi) {
+    const int mid = (lo + hi) >> 1;
+    const int v = tb.at(1, mid);
+    if (v == ci) return mid;
+    if (v < ci) lo = mid + 1;
+    else hi = mid - 1;
+  }
+  return 0;
+}
+
+// Face-fill adjoint, stage 2: each coarse point of the donor range gathers
+// the partial sums of the (<= 8) entries whose donor box has it as a corner,
+// in a fixed corner order, and adds them to cbar.
+__global__ void k_face_adj2(Dims da, FaceArgs a, const double* part, double* cbar) {
+  const int sh = (a.comp == 1) ? -1 : 0, shy = (a.comp == 2) ? -1 : 0, shz = (a.comp == 3) ? -1 : 0;
+  // donor coarse indices span [first centre - 1, last centre + 1]
+  const int i0 = a.tx.at(1, 1) + sh - 1, i1 = a.tx.at(1, a.tx.c) + sh + 1;
+  const int j0 = a.ty.at(1, 1) + shy - 1, j1 = a.ty.at(1, a.ty.c) + shy + 1;
+  const int k0 = a.tz.at(1, 1) + shz - 1, k1 = a.tz.at(1, a.tz.c) + shz + 1;
+  const int nx = i1 - i0 + 1, ny = j1 - j0 + 1, nz = k1 - k0 + 1;
+  const int cx = a.tx.c, cy = a.ty.c;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nx * ny * nz; t += gridDim.x * blockDim.x) {
+    const int di = i0 + t % nx, dj = j0 + (t / nx) % ny, dk = k0 + t / (nx * ny);
+    if (di < 1 || dj < 1 || dk < 1 || di > da.NX || dj > da.NY || dk > da.NZ) continue;
+    double s = 0.0;
+    bool any = false;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      // donor corner q of centre v is v + (2a-1, 2b-1, 2c-1)
+      const int vi = di - (2 * (q & 1) - 1), vj = dj - (2 * ((q >> 1) & 1) - 1), vk = dk - (2 * (q >> 2) - 1);
+      const int ei = entry_of(a.tx, vi - sh), ej = entry_of(a.ty, vj - shy), ek = entry_of(a.tz, vk - shz);
+      if (!ei || !ej || !ek) continue;
+      s += part[8 * ((int64_t)(ei - 1) + (int64_t)cx * ((ej - 1) + (int64_t)cy * (ek - 1))) + q];
+      any = true;
+    }
+    if (any) cbar[da.idx(di, dj, dk)] += s;
+  }
+}
+
+// Restriction adjoint: the donor boxes of different coarse targets are
+// disjoint (ratio 2: the donors of entry e lie in its own fine range), so
+// the transpose is a plain scatter: fbar[donor] += weight * cbar[target].
+__global__ void k_restrict_adj(Dims da, Dims db, FaceArgs a, int ci, const double* cbar, double* fbar) {
+  const int nxs = a.tx.c - 2 * ci + 1, nys = a.ty.c - 2 * ci + 1, nzs = a.tz.c - 2 * ci + 1;
+  if (nxs <= 0 || nys <= 0 || nzs <= 0) return;
+  const int n = nxs * nys * nzs;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+    const int ei = ci + t % nxs, ej = ci + (t / nxs) % nys, ek = ci + t / (nxs * nys);
+    const int tx = a.tx.at(1, ei), ty = a.ty.at(1, ej), tz = a.tz.at(1, ek);
+    int lx = (a.tx.at(2, ei) + a.tx.at(3, ei) - 1) / 2;
+    int ly = (a.ty.at(2, ej) + a.ty.at(3, ej) - 1) / 2;
+    int lz = (a.tz.at(2, ek) + a.tz.at(3, ek) - 1) / 2;
+    if (a.comp == 1) lx = a.tx.at(3, ei);
+    if (a.comp == 2) ly = a.ty.at(3, ej);
+    if (a.comp == 3) lz = a.tz.at(3, ek);
+    int ii = lx, jj = ly, kk = lz, vi = lx, vj = ly, vk = lz;
+    if (a.comp == 1) { ii = lx - 1; vi = lx - 2; }
+    if (a.comp == 2) { jj = ly - 1; vj = ly - 2; }
+    if (a.comp == 3) { kk = lz - 1; vk = lz - 2; }
+    const double x = a.ga.x[tx - 1], y = a.ga.y[ty - 1], z = a.ga.z[tz - 1];
+    double w[8];
+    face_weights(x, y, z, a.gb.x[ii - 1], a.gb.x[ii], a.gb.y[jj - 1], a.gb.y[jj], a.gb.z[kk - 1], a.gb.z[kk], w);
+    const int ox = tx - (a.comp == 1), oy = ty - (a.comp == 2), oz = tz - (a.comp == 3);
+    const double c = cbar[da.idx(ox, oy, oz)];
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+      fbar[db.idx(vi + (q & 1), vj + ((q >> 1) & 1), vk + (q >> 2))] += w[q] * c;
+  }
+}
+
 // fineUpdate_mv (src/FineInterp.f90:10-281): fine points with cell_n /= 1
 __global__ void k_fine_mv(Dims da, Dims db, FaceArgs a, const int8_t* cell_n) {
   const int nxs = a.tx.c - 2, nys = a.ty.c - 2, nzs = a.tz.c - 2;
@@ -250,4 +371,48 @@ int launch_fine_update_mv(HostInterface* it) {
   return 0;
 }
 
+// Forward and adjoint coupling maps on caller arrays (natural layout, device
+// pointers): the face fill f = P c of one component (all three face passes)
+// and its transpose c += P^T f; the restriction c = R f and f += R^T c.
+int coupling_apply(HostInterface* it, int comp, int op, const double* in, double* out) {
+  HostBlock* a = get_block(it->a);
+  HostBlock* b = get_block(it->b);
+  if (!a || !b) return BCFD_E_HANDLE;
+  FaceArgs f = make_args(it, a, b, comp);
+  f.dst2 = Field{nullptr, nullptr, nullptr};
+  const int n = f.tx.c * f.ty.c * f.tz.c;
+  if (op == 0) {  // face fill: coarse in -> fine out
+    f.src = Field{const_cast<double*>(in), nullptr, nullptr};
+    f.dst = Field{out, nullptr, nullptr};
+    for (int axis = 1; axis <= 3; ++axis) {
+      f.axis = axis;
+      k_face<<<grid_for(n, 128), 128, 0, stream()>>>(a->d.d, b->d.d, f);
+      BCFD_LAUNCHED();
+    }
+  } else if (op == 1) {  // face-fill transpose: fine in -> coarse out (+=)
+    double* part = nullptr;
+    BCFD_CUDA(cudaMalloc(&part, (size_t)n * 8 * sizeof(double)));
+    k_face_adj1<<<grid_for(n, 128), 128, 0, stream()>>>(b->d.d, f, in, part);
+    int r = note_launch();
+    if (!r) {
+      k_face_adj2<<<grid_for((int64_t)(f.tx.c + 4) * (f.ty.c + 4) * (f.tz.c + 4), 128), 128, 0, stream()>>>(
+          a->d.d, f, part, out);
+      r = note_launch();
+    }
+    cudaStreamSynchronize(stream());
+    cudaFree(part);
+    return r;
+  } else if (op == 2) {  // restriction: fine in -> coarse out
+    f.src = Field{const_cast<double*>(in), nullptr, nullptr};
+    f.dst = Field{out, nullptr, nullptr};
+    k_restrict<<<grid_for(n, 128), 128, 0, stream()>>>(a->d.d, b->d.d, f, 3);
+    BCFD_LAUNCHED();
+  } else {  // restriction transpose: coarse in -> fine out (+=)
+    k_restrict_adj<<<grid_for(n, 128), 128, 0, stream()>>>(a->d.d, b->d.d, f, 3, in, out);
+    BCFD_LAUNCHED();
+  }
+  return 0;
+}
+
 }  // namespace bcfd
+

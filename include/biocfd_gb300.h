@@ -197,6 +197,15 @@ int bcfd_fine_update_mv(bcfd_handle it);       /* src/FineInterp.f90:10-281     
  * arrays as scratch (call between time steps). */
 int bcfd_poisson_solve_zero_bc(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax);
 int bcfd_poisson_solve_adjoint(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax);
+/* ---- coupling maps and their transposes (no counterpart in the reference) --
+ * Interface h, component comp (0 p, 1 u, 2 v, 3 w), natural-layout host
+ * arrays of the coarse (a) and fine (b) blocks:
+ *   op 0: out(fine)   = P in(coarse)   the face fill of src/FineInterp_bound.f90
+ *   op 1: out(coarse) += P^T in(fine)  deterministic gather per coarse donor
+ *   op 2: out(coarse) = R in(fine)     the restriction of src/CoarseInterp.f90
+ *   op 3: out(fine)   += R^T in(coarse) scatter (donor boxes are disjoint)
+ * ops 0 and 2 overwrite only the points they fill. */
+int bcfd_coupling_apply(bcfd_handle h, int comp, int op, const double* in, double* out);
 
 /* ---- drag / lift (src/StressCalc.f90:14-208, FP64, deterministic order) --- */
 /* out[4] = viscous drag, pressure drag, viscous lift, pressure lift coefficients */

@@ -103,3 +103,37 @@ def test_autograd_gradcheck():
     loss = lambda rr: (f.apply(rr * mask) * w).sum()
     assert torch.autograd.gradcheck(loss, (r,), eps=1e-6, atol=1e-7, rtol=1e-6)
     s.close()
+
+
+def _coupling(s, it, comp, op, x, out_shape):
+    import ctypes as C
+    from biocfd._lib import check
+    x = np.asfortranarray(x, dtype=np.float64)
+    out = np.zeros(out_shape, order="F")
+    check(s.L.bcfd_coupling_apply(it, comp, op, x.ctypes.data_as(C.POINTER(C.c_double)),
+                                  out.ctypes.data_as(C.POINTER(C.c_double))), "coupling_apply")
+    return out
+
+
+@pytest.mark.parametrize("comp", [0, 1, 2, 3])
+def test_coupling_transposes_dot_product(comp):
+    # <P c, f> = <c, P^T f> for the face fill, <R f, c> = <f, R^T c> for the
+    # restriction (each map's transpose is a separate kernel)
+    case = synth.small_two_block(n_steps=1)
+    s = Solver(case)
+    s.setup()
+    it = s.ifaces[0]
+    A, B = case.blocks[0].shape, case.blocks[1].shape
+    rng = np.random.default_rng(7 + comp)
+    c, f = rng.standard_normal(A), rng.standard_normal(B)
+    Pc = _coupling(s, it, comp, 0, c, B)
+    PTf = _coupling(s, it, comp, 1, f, A)
+    assert np.count_nonzero(Pc) > 0 and np.count_nonzero(PTf) > 0
+    lhs, rhs = np.vdot(Pc, f), np.vdot(c, PTf)
+    assert abs(lhs - rhs) <= 1e-12 * np.sqrt(np.vdot(Pc, Pc) * np.vdot(f, f)), (lhs, rhs)
+    Rf = _coupling(s, it, comp, 2, f, A)
+    RTc = _coupling(s, it, comp, 3, c, B)
+    assert np.count_nonzero(Rf) > 0 and np.count_nonzero(RTc) > 0
+    lhs, rhs = np.vdot(Rf, c), np.vdot(f, RTc)
+    assert abs(lhs - rhs) <= 1e-12 * np.sqrt(np.vdot(Rf, Rf) * np.vdot(c, c)), (lhs, rhs)
+    s.close()

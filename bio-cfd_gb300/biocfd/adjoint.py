@@ -53,3 +53,20 @@ def poisson_function(solver, g: int, tol: float = 1e-12, itmax: int = 200000):
             return torch.from_numpy(np.ascontiguousarray(gr)).to(gx)
 
     return PoissonSolve
+
+
+def momentum_tangent(solver, g: int, du, dv, dw, dp, dt: float | None = None, re: float | None = None):
+    """Tangent-linear model of nsMomentum2order on block g at its current
+    (u, v, w, p): returns (ut, vt, wt) -- bitwise the FP64 predictor -- and
+    (dut, dvt, dwt), the predictor's derivative along (du, dv, dw, dp).
+    Arrays are natural-layout FP64 of the block's point shape; only fluid
+    interior cells (cell == 0) are written, the rest stay zero."""
+    c = solver.case
+    dt = c.dt if dt is None else dt
+    re = c.re if re is None else re
+    ins = [np.asfortranarray(a, dtype=np.float64) for a in (du, dv, dw, dp)]
+    outs = [np.zeros_like(ins[0], order="F") for _ in range(6)]
+    P = C.POINTER(C.c_double)
+    check(solver.L.bcfd_momentum_tangent(g, dt, re, *(a.ctypes.data_as(P) for a in ins),
+                                         *(a.ctypes.data_as(P) for a in outs)), "momentum_tangent")
+    return tuple(outs[:3]), tuple(outs[3:])

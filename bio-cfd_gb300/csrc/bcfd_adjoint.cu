@@ -95,6 +95,45 @@ int bcfd_poisson_solve_zero_bc(bcfd_handle h, const double* r, double* x, double
   return solve_zero_bc(hb, r, x, tol, itmax, false);
 }
 
+int bcfd_momentum_tangent(bcfd_handle h, double deltat, double re, const double* du, const double* dv,
+                          const double* dw, const double* dp, double* ut, double* vt, double* wt, double* dut,
+                          double* dvt, double* dwt) {
+  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  HostBlock* hb = get_block(h);
+  if (!hb) return BCFD_E_HANDLE;
+  const double* in[4] = {du, dv, dw, dp};
+  double* outh[6] = {ut, vt, wt, dut, dvt, dwt};
+  for (const double* p : in)
+    if (!p) return BCFD_E_ARG;
+  for (double* p : outh)
+    if (!p) return BCFD_E_ARG;
+  if (!hb->d.ca[0]) return BCFD_E_STATE;
+  const size_t np = (size_t)hb->d.d.npts();
+  double* buf = nullptr;
+  if (cudaMalloc(&buf, 10 * np * sizeof(double)) != cudaSuccess) return BCFD_E_NOMEM;
+  int r = 0;
+  const double* din[4];
+  double* dval[3];
+  double* dtan[3];
+  for (int q = 0; q < 4 && !r; ++q) {
+    din[q] = buf + q * np;
+    if (cudaMemcpy((void*)din[q], in[q], np * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) r = BCFD_E_CUDA;
+  }
+  for (int q = 0; q < 3; ++q) {
+    dval[q] = buf + (4 + q) * np;
+    dtan[q] = buf + (7 + q) * np;
+  }
+  if (!r && cudaMemset(buf + 4 * np, 0, 6 * np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
+  if (!r) r = launch_momentum_tangent(hb, deltat, re, din, dval, dtan);
+  if (!r && cudaStreamSynchronize(stream()) != cudaSuccess) r = BCFD_E_CUDA;
+  for (int q = 0; q < 6 && !r; ++q)
+    if (cudaMemcpy(outh[q], buf + (4 + q) * np, np * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+      r = BCFD_E_CUDA;
+  cudaFree(buf);
+  if (r) return r;
+  return take_block_error(hb);
+}
+
 int bcfd_poisson_solve_adjoint(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax) {
   std::lock_guard<std::recursive_mutex> lk(lib().mu);
   HostBlock* hb = get_block(h);

@@ -168,6 +168,8 @@ int cluster_solve_fits(HostBlock* hb);
 int launch_sor_cluster(HostBlock* hb, int64_t itmax, double dt, double div_tol, int inner, float omega);
 // k_momentum.cu
 int launch_momentum(HostBlock* hb, double dt, double re, bool fp32);
+int launch_momentum_tangent(HostBlock* hb, double dt, double re, const double* const du[4], double* const val[3],
+                            double* const tan[3]);
 int launch_velocity_bc(HostBlock* hb, double dt, double uc);
 int launch_solid_bc(HostBlock* hb, bool move);
 // k_search.cu

@@ -11,6 +11,8 @@
 // every other cell reads the fields directly.  FP64, compiled without FMA
 // contraction, expressions in the reference's evaluation order (T = double);
 // the same stencil in FP32 arithmetic serves the mixed-precision path.
+#include <type_traits>
+
 #include "bcfd_host.h"
 
 namespace bcfd {
@@ -35,12 +37,51 @@ __device__ __forceinline__ bool adj_ok(const int8_t* c, const Dims& d, bool big,
   return true;
 }
 
-// a grid / coefficient value as T: the FP64 table or its FP32 copy
+// a grid / coefficient value as T: the FP32 copy for T = float, else the FP64 table
 template <typename T>
 __device__ __forceinline__ T grid_t(const double* d64, const float* f32, int q) {
-  if constexpr (sizeof(T) == 8) return d64[q];
-  else return f32[q];
+  if constexpr (std::is_same<T, float>::value) return f32[q];
+  else return T(d64[q]);
 }
+
+// Forward-mode dual number (value, tangent): the stencil evaluated in it gives
+// the reference's FP64 value (the value part performs exactly the double
+// operations) and the exact derivative of the discrete stencil along the
+// input tangent (the tangent-linear model).
+struct Dual {
+  double v, d;
+  __device__ Dual() : v(0.0), d(0.0) {}
+  __device__ Dual(double x) : v(x), d(0.0) {}
+  __device__ Dual(double x, double dx) : v(x), d(dx) {}
+};
+__device__ __forceinline__ Dual operator+(Dual a, Dual b) { return Dual(a.v + b.v, a.d + b.d); }
+__device__ __forceinline__ Dual operator-(Dual a, Dual b) { return Dual(a.v - b.v, a.d - b.d); }
+__device__ __forceinline__ Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
+__device__ __forceinline__ Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
+__device__ __forceinline__ Dual operator/(Dual a, Dual b) {
+  const double q = a.v / b.v;
+  return Dual(q, (a.d - q * b.d) / b.v);
+}
+// |x| with the derivative of the branch the value takes (sign(0) = +); the
+// global float/double overloads stay visible next to it
+using ::fabs;
+__device__ __forceinline__ Dual fabs(Dual a) { return a.v < 0.0 ? -a : a; }
+
+// where a stencil's three results go
+struct StoreOut {
+  double *ut, *vt, *wt;
+  template <typename T>
+  __device__ __forceinline__ void put(int q, int64_t c, T val) const {
+    (q == 0 ? ut : q == 1 ? vt : wt)[c] = (double)val;
+  }
+};
+struct DualOut {
+  double *ut, *vt, *wt, *dut, *dvt, *dwt;
+  __device__ __forceinline__ void put(int q, int64_t c, Dual val) const {
+    (q == 0 ? ut : q == 1 ? vt : wt)[c] = val.v;
+    (q == 0 ? dut : q == 1 ? dvt : dwt)[c] = val.d;
+  }
+};
 
 // Field reads of the stencil: field f (0 u, 1 v, 2 w, 3 p) at cell (a,b,e),
 // linear index x.  The plain reader loads the array.
@@ -53,9 +94,9 @@ struct PlainReader {
 // arithmetic (bit-exact drop-in).  T = float: the FP32 momentum stencil of the
 // mixed-precision path (fields stay FP64 in HBM; stencil values are rounded to
 // FP32 on load, ut/vt/wt stored back as FP64).
-template <typename T, class Rd>
+template <typename T, class Rd, class Out>
 __device__ __forceinline__ void momentum_cell(const DevBlock& B, const MomArgs& a, int i, int j, int k,
-                                              int64_t c, const Rd& rd) {
+                                              int64_t c, const Rd& rd, const Out& out) {
   const T Q25 = T(0.25), HALF = T(0.5), TWO = T(2.0), ONE = T(1.0);
   const Dims& d = B.d;
   const T alpha = ONE;
@@ -200,7 +241,7 @@ __device__ __forceinline__ void momentum_cell(const DevBlock& B, const MomArgs& 
           (TWO / (HALF * (dz2zt + dz2zb))) * ((-u12 / (HALF * dz2zt)) + (u10 / (HALF * dz2zb)));
       const T xtt2 = (d2udx2 + d2udy2 + d2udz2) / re;
       const T residu = (-duudx - dvudy - dwudz + xtt2);
-      B.ut[c] = (double)(u(0, 0, 0) + deltat * (residu + dpdx));
+      out.put(0, c, u(0, 0, 0) + deltat * (residu + dpdx));
     }
     // ---------------- V momentum ----------------
     {
@@ -260,7 +301,7 @@ __device__ __forceinline__ void momentum_cell(const DevBlock& B, const MomArgs& 
           (TWO / (HALF * (dz2zt + dz2zb))) * ((-v14 / (HALF * dz2zt)) + (v12 / (HALF * dz2zb)));
       const T ytt2 = (d2vdx2 + d2vdy2 + d2vdz2) / re;
       const T residv = (-duvdx - dvvdy - dwvdz + ytt2);
-      B.vt[c] = (double)(v(0, 0, 0) + deltat * (residv + dpdy));
+      out.put(1, c, v(0, 0, 0) + deltat * (residv + dpdy));
     }
     // ---------------- W momentum ----------------
     {
@@ -320,7 +361,7 @@ __device__ __forceinline__ void momentum_cell(const DevBlock& B, const MomArgs& 
       const T d2wdz2 = (TWO / dz2zt) * ((-w16 / dzt) + (w14 / dz));
       const T ztt2 = (d2wdx2 + d2wdy2 + d2wdz2) / re;
       const T residw = (-duwdx - dvwdy - dwwdz + ztt2);
-      B.wt[c] = (double)(w(0, 0, 0) + deltat * (residw + dpdz));
+      out.put(2, c, w(0, 0, 0) + deltat * (residw + dpdz));
     }
 #undef u
 #undef v
@@ -343,7 +384,7 @@ struct MomentumOp {
       INTERIOR_CELL(B);
       if (B.cell[c] != 0) continue;
       if (B.tsnear[c]) continue;  // done by MomentumTsOp
-      momentum_cell<T>(B, a, i, j, k, c, rd);
+      momentum_cell<T>(B, a, i, j, k, c, rd, StoreOut{B.ut, B.vt, B.wt});
     }
   }
 };
@@ -507,8 +548,36 @@ struct MomentumTsOp {
 #pragma unroll
       for (int K = 0; K < N_KIND; ++K) rd.last[K] = -1;
     }
-    momentum_cell<T>(B, a, i, j, k, c, rd);
+    momentum_cell<T>(B, a, i, j, k, c, rd, StoreOut{B.ut, B.vt, B.wt});
   }
+  }
+};
+
+// tangent-linear stencil: reads (u,v,w,p) and their tangents
+struct DualReader {
+  const double* f[4];
+  const double* df[4];
+  __device__ __forceinline__ Dual get(int q, int, int, int, int64_t x) const {
+    return Dual(__ldg(f[q] + x), __ldg(df[q] + x));
+  }
+};
+
+struct MomentumTlmOp {
+  MomArgs a;
+  const double* du[4];
+  double *ut, *vt, *wt, *dut, *dvt, *dwt;
+  __device__ void run(const DevBlock& B, int cta, int ncta) const {
+    const DualReader rd{{B.u, B.v, B.w, B.p}, {du[0], du[1], du[2], du[3]}};
+    const DualOut out{ut, vt, wt, dut, dvt, dwt};
+    FOR_INTERIOR(B, cta, ncta) {
+      INTERIOR_CELL(B);
+      if (B.cell[c] != 0) continue;
+      if (B.tsnear[c]) {
+        set_err(B.err, BCFD_E_STATE);  // the thin-surface overlay has no tangent model
+        continue;
+      }
+      momentum_cell<Dual>(B, a, i, j, k, c, rd, out);
+    }
   }
 };
 
@@ -659,4 +728,17 @@ int launch_solid_bc(HostBlock* hb, bool move) {
   return 0;
 }
 
+// tangent-linear model of nsMomentum2order at the block's current (u,v,w,p):
+// val = the predictor's ut,vt,wt (bitwise the FP64 stencil), tan = its
+// derivative along (du,dv,dw,dp); device arrays of the block's point count
+int launch_momentum_tangent(HostBlock* hb, double dt, double re, const double* const du[4], double* const val[3],
+                            double* const tan[3]) {
+  MomentumTlmOp op{MomArgs{dt, re}, {du[0], du[1], du[2], du[3]}, val[0], val[1], val[2], tan[0], tan[1], tan[2]};
+  k_one<MomentumTlmOp, 128><<<grid_for((int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz, 128, 1u << 20), 128, 0,
+                              stream()>>>(hb->d, op);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
 }  // namespace bcfd
+

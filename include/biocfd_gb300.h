@@ -197,6 +197,16 @@ int bcfd_fine_update_mv(bcfd_handle it);       /* src/FineInterp.f90:10-281     
  * arrays as scratch (call between time steps). */
 int bcfd_poisson_solve_zero_bc(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax);
 int bcfd_poisson_solve_adjoint(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax);
+/* tangent-linear model of nsMomentum2order (no counterpart in the reference):
+ * at the block's current u,v,w,p, (ut,vt,wt) = the predictor's values (bitwise
+ * those of bcfd_ns_momentum_2order; the block's own ut,vt,wt are untouched)
+ * and (dut,dvt,dwt) = its exact derivative along (du,dv,dw,dp); natural-layout
+ * host arrays, outputs 0 off the fluid cells.  Not for cells within reach of
+ * thin-surface cells (BCFD_E_STATE). */
+int bcfd_momentum_tangent(bcfd_handle h, double deltat, double re, const double* du, const double* dv,
+                          const double* dw, const double* dp, double* ut, double* vt, double* wt, double* dut,
+                          double* dvt, double* dwt);
+
 /* ---- coupling maps and their transposes (no counterpart in the reference) --
  * Interface h, component comp (0 p, 1 u, 2 v, 3 w), natural-layout host
  * arrays of the coarse (a) and fine (b) blocks:

@@ -70,3 +70,18 @@ def momentum_tangent(solver, g: int, du, dv, dw, dp, dt: float | None = None, re
     check(solver.L.bcfd_momentum_tangent(g, dt, re, *(a.ctypes.data_as(P) for a in ins),
                                          *(a.ctypes.data_as(P) for a in outs)), "momentum_tangent")
     return tuple(outs[:3]), tuple(outs[3:])
+
+
+def momentum_adjoint(solver, g: int, utb, vtb, wtb, dt: float | None = None, re: float | None = None):
+    """Adjoint of nsMomentum2order on block g at its current (u, v, w, p):
+    returns (ub, vb, wb, pb) = J^T (utb, vtb, wtb), the transpose of
+    momentum_tangent (seeds off the fluid cells are ignored)."""
+    c = solver.case
+    dt = c.dt if dt is None else dt
+    re = c.re if re is None else re
+    ins = [np.asfortranarray(a, dtype=np.float64) for a in (utb, vtb, wtb)]
+    outs = [np.zeros_like(ins[0], order="F") for _ in range(4)]
+    P = C.POINTER(C.c_double)
+    check(solver.L.bcfd_momentum_adjoint(g, dt, re, *(a.ctypes.data_as(P) for a in ins),
+                                         *(a.ctypes.data_as(P) for a in outs)), "momentum_adjoint")
+    return tuple(outs)

@@ -134,6 +134,39 @@ int bcfd_momentum_tangent(bcfd_handle h, double deltat, double re, const double*
   return take_block_error(hb);
 }
 
+int bcfd_momentum_adjoint(bcfd_handle h, double deltat, double re, const double* utb, const double* vtb,
+                          const double* wtb, double* ub, double* vb, double* wb, double* pb) {
+  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  HostBlock* hb = get_block(h);
+  if (!hb) return BCFD_E_HANDLE;
+  const double* in[3] = {utb, vtb, wtb};
+  double* outh[4] = {ub, vb, wb, pb};
+  for (const double* p : in)
+    if (!p) return BCFD_E_ARG;
+  for (double* p : outh)
+    if (!p) return BCFD_E_ARG;
+  if (!hb->d.ca[0]) return BCFD_E_STATE;
+  const size_t np = (size_t)hb->d.d.npts();
+  double* buf = nullptr;
+  // 3 seeds, 4 adjoints, then the 16-word footprint
+  if (cudaMalloc(&buf, 7 * np * sizeof(double) + 64) != cudaSuccess) return BCFD_E_NOMEM;
+  int r = 0;
+  const double* dsb[3];
+  double* dab[4];
+  for (int q = 0; q < 3 && !r; ++q) {
+    dsb[q] = buf + q * np;
+    if (cudaMemcpy((void*)dsb[q], in[q], np * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) r = BCFD_E_CUDA;
+  }
+  for (int q = 0; q < 4; ++q) dab[q] = buf + (3 + q) * np;
+  if (!r) r = launch_momentum_adjoint(hb, deltat, re, dsb, dab, (uint32_t*)(buf + 7 * np));
+  if (!r && cudaStreamSynchronize(stream()) != cudaSuccess) r = BCFD_E_CUDA;
+  for (int q = 0; q < 4 && !r; ++q)
+    if (cudaMemcpy(outh[q], dab[q], np * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) r = BCFD_E_CUDA;
+  cudaFree(buf);
+  if (r) return r;
+  return take_block_error(hb);
+}
+
 int bcfd_poisson_solve_adjoint(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax) {
   std::lock_guard<std::recursive_mutex> lk(lib().mu);
   HostBlock* hb = get_block(h);

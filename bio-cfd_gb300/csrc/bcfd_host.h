@@ -170,6 +170,8 @@ int launch_sor_cluster(HostBlock* hb, int64_t itmax, double dt, double div_tol, 
 int launch_momentum(HostBlock* hb, double dt, double re, bool fp32);
 int launch_momentum_tangent(HostBlock* hb, double dt, double re, const double* const du[4], double* const val[3],
                             double* const tan[3]);
+int launch_momentum_adjoint(HostBlock* hb, double dt, double re, const double* const sb[3], double* const ab[4],
+                            uint32_t* foot);
 int launch_velocity_bc(HostBlock* hb, double dt, double uc);
 int launch_solid_bc(HostBlock* hb, bool move);
 // k_search.cu

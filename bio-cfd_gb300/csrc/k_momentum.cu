@@ -581,6 +581,111 @@ struct MomentumTlmOp {
   }
 };
 
+// ---------------------------------------------------------------------------
+// Adjoint (reverse mode) of the predictor, as a gather: the adjoint of input
+// position X of field f is  sum over fluid cells C that read X, over the
+// three outputs q, of  seed_q(C) * dF_q(C)/dX_f.  Each partial is the tangent
+// of the dual-number stencil at C seeded with 1 at (f, X), so it is the exact
+// transpose of the tangent-linear model, summed in a fixed order (footprint
+// offsets ascending, outputs U,V,W): deterministic, no atomics.
+// The footprint (the (field, offset) pairs the stencil reads, offsets in
+// [-2,2]^3) is collected once per call from the block's own branches.
+// ---------------------------------------------------------------------------
+constexpr int kFootWords = 16;  // 4 fields x 125 offsets, 4 words per field
+
+struct FootReader {
+  const double* f[4];
+  uint32_t* m;  // per-thread mask
+  int ci, cj, ck;
+  int* err;
+  __device__ __forceinline__ double get(int q, int ii, int jj, int kk, int64_t x) const {
+    const int a = ii - ci, b = jj - cj, e = kk - ck;
+    if (a < -2 || a > 2 || b < -2 || b > 2 || e < -2 || e > 2) {
+      set_err(err, BCFD_E_STATE);  // a read outside [-2,2]^3 (none in the stencil)
+    } else {
+      const int o = (a + 2) + 5 * (b + 2) + 25 * (e + 2);
+      m[4 * q + (o >> 5)] |= 1u << (o & 31);
+    }
+    return __ldg(f[q] + x);
+  }
+};
+struct NullOut {
+  template <typename T>
+  __device__ __forceinline__ void put(int, int64_t, T) const {}
+};
+
+__global__ void k_mom_footprint(DevBlock B, MomArgs a, uint32_t* foot) {
+  uint32_t m[kFootWords];
+#pragma unroll
+  for (int w = 0; w < kFootWords; ++w) m[w] = 0u;
+  const Dims& d = B.d;
+  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(t % d.nx);
+    const int64_t r = t / d.nx;
+    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
+    const int64_t c = d.idx(i, j, k);
+    if (B.cell[c] != 0 || B.tsnear[c]) continue;
+    const FootReader rd{{B.u, B.v, B.w, B.p}, m, i, j, k, B.err};
+    momentum_cell<double>(B, a, i, j, k, c, rd, NullOut{});
+  }
+#pragma unroll
+  for (int w = 0; w < kFootWords; ++w) {
+    uint32_t v = m[w];
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) v |= __shfl_xor_sync(0xffffffffu, v, s);
+    if ((threadIdx.x & 31) == 0 && v) atomicOr(foot + w, v);
+  }
+}
+
+// dual reader seeded with 1 at (field sf, linear index sx)
+struct SeedReader {
+  const double* f[4];
+  int sf;
+  int64_t sx;
+  __device__ __forceinline__ Dual get(int q, int, int, int, int64_t x) const {
+    return Dual(__ldg(f[q] + x), (q == sf && x == sx) ? 1.0 : 0.0);
+  }
+};
+struct AdjOut {
+  const double* sb[3];
+  double* acc;
+  __device__ __forceinline__ void put(int q, int64_t c, Dual val) const { *acc += __ldg(sb[q] + c) * val.d; }
+};
+
+__global__ void __launch_bounds__(128) k_mom_adjoint(DevBlock B, MomArgs a, const uint32_t* __restrict__ foot,
+                                                     const double* ubar_t, const double* vbar_t,
+                                                     const double* wbar_t, double* ub, double* vb, double* wb,
+                                                     double* pb) {
+  const Dims& d = B.d;
+  const int64_t n = d.npts();
+  uint32_t m[kFootWords];
+#pragma unroll
+  for (int w = 0; w < kFootWords; ++w) m[w] = __ldg(foot + w);
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const int xi = 1 + (int)(x % d.NX);
+    const int64_t r = x / d.NX;
+    const int xj = 1 + (int)(r % d.NY), xk = 1 + (int)(r / d.NY);
+    for (int f = 0; f < 4; ++f) {
+      double acc = 0.0;
+      for (int o = 0; o < 125; ++o) {
+        if (!((m[4 * f + (o >> 5)] >> (o & 31)) & 1u)) continue;
+        const int ci = xi - (o % 5 - 2), cj = xj - ((o / 5) % 5 - 2), ck = xk - (o / 25 - 2);
+        if (ci < 2 || ci > d.nx + 1 || cj < 2 || cj > d.ny + 1 || ck < 2 || ck > d.nz + 1) continue;
+        const int64_t c = d.idx(ci, cj, ck);
+        if (B.cell[c] != 0) continue;
+        if (B.tsnear[c]) {
+          set_err(B.err, BCFD_E_STATE);  // the thin-surface overlay has no adjoint
+          continue;
+        }
+        const SeedReader rd{{B.u, B.v, B.w, B.p}, f, x};
+        momentum_cell<Dual>(B, a, ci, cj, ck, c, rd, AdjOut{{ubar_t, vbar_t, wbar_t}, &acc});
+      }
+      (f == 0 ? ub : f == 1 ? vb : f == 2 ? wb : pb)[x] = acc;
+    }
+  }
+}
+
 // u,v,w,p at TS positions after the loop: the restore of the latest restorer
 struct TsRestoreOp {
   __device__ void run(const DevBlock& B, int cta, int ncta) const {
@@ -736,6 +841,23 @@ int launch_momentum_tangent(HostBlock* hb, double dt, double re, const double* c
   MomentumTlmOp op{MomArgs{dt, re}, {du[0], du[1], du[2], du[3]}, val[0], val[1], val[2], tan[0], tan[1], tan[2]};
   k_one<MomentumTlmOp, 128><<<grid_for((int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz, 128, 1u << 20), 128, 0,
                               stream()>>>(hb->d, op);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+
+// adjoint of nsMomentum2order at the block's current (u,v,w,p): (ub,vb,wb,pb)
+// = J^T (ubar_t, vbar_t, wbar_t), J the predictor's Jacobian on fluid cells;
+// foot is 16 words of device scratch
+int launch_momentum_adjoint(HostBlock* hb, double dt, double re, const double* const sb[3], double* const ab[4],
+                            uint32_t* foot) {
+  const MomArgs a{dt, re};
+  BCFD_CUDA(cudaMemsetAsync(foot, 0, kFootWords * sizeof(uint32_t), stream()));
+  const int64_t ni = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
+  k_mom_footprint<<<grid_for(ni, 128, 1u << 16), 128, 0, stream()>>>(hb->d, a, foot);
+  BCFD_LAUNCHED();
+  k_mom_adjoint<<<grid_for(hb->d.d.npts(), 128, 1u << 20), 128, 0, stream()>>>(hb->d, a, foot, sb[0], sb[1], sb[2],
+                                                                               ab[0], ab[1], ab[2], ab[3]);
   BCFD_LAUNCHED();
   return 0;
 }

@@ -206,6 +206,13 @@ int bcfd_poisson_solve_adjoint(bcfd_handle h, const double* r, double* x, double
 int bcfd_momentum_tangent(bcfd_handle h, double deltat, double re, const double* du, const double* dv,
                           const double* dw, const double* dp, double* ut, double* vt, double* wt, double* dut,
                           double* dvt, double* dwt);
+/* adjoint of nsMomentum2order (no counterpart in the reference): at the
+ * block's current u,v,w,p, (ub,vb,wb,pb) = J^T (utb,vtb,wtb) with J the
+ * Jacobian of the predictor's fluid-cell outputs (the transpose of
+ * bcfd_momentum_tangent), accumulated per input point in a fixed order
+ * (deterministic).  Natural-layout host arrays; same thin-surface limit. */
+int bcfd_momentum_adjoint(bcfd_handle h, double deltat, double re, const double* utb, const double* vtb,
+                          const double* wtb, double* ub, double* vb, double* wb, double* pb);
 
 /* ---- coupling maps and their transposes (no counterpart in the reference) --
  * Interface h, component comp (0 p, 1 u, 2 v, 3 w), natural-layout host

@@ -1,15 +1,16 @@
-"""Tangent-linear model of the momentum predictor (nsMomentum2order in dual
-numbers): its value part is bitwise the FP64 predictor the drop-in path
-computes, and its tangent matches central finite differences of that
-predictor along a random direction (the stencil is quadratic in (u,v,w) and
-linear in p, so central differences are exact up to round-off away from
-upwind switches)."""
+"""Tangent-linear model and adjoint of the momentum predictor
+(nsMomentum2order in dual numbers).  The tangent's value part is bitwise the
+FP64 predictor the drop-in path computes, and its tangent matches central
+finite differences of that predictor along a random direction (the stencil
+is quadratic in (u,v,w) and linear in p, so central differences are exact up
+to round-off away from upwind switches).  The adjoint is the transpose of the
+tangent: <J d, s> = <d, J^T s> field by field."""
 import numpy as np
 import pytest
 
 from biocfd import synth
 from biocfd._lib import BcfdError, check
-from biocfd.adjoint import momentum_tangent
+from biocfd.adjoint import momentum_adjoint, momentum_tangent
 from biocfd.solver import Solver
 
 pytestmark = pytest.mark.gpu
@@ -97,3 +98,46 @@ def test_tangent_refuses_thin_surface_cells():
     z = np.zeros(case.blocks[0].shape, order="F")
     with pytest.raises(BcfdError):
         momentum_tangent(s, g, z, z, z, z)
+
+
+@pytest.mark.parametrize("field", [0, 1, 2, 3])
+def test_adjoint_is_transpose_of_tangent(field):
+    s, case, g = _sphere()
+    spec = case.blocks[0]
+    rng = np.random.default_rng(100 + field)
+    z = np.zeros(spec.shape, order="F")
+    d = [z, z, z, z]
+    d[field] = np.asfortranarray(rng.normal(size=spec.shape))
+    seeds = [np.asfortranarray(rng.normal(size=spec.shape)) for _ in range(3)]
+    _, tan = momentum_tangent(s, g, *d)
+    adj = momentum_adjoint(s, g, *seeds)
+    m = _mask(s, g, spec)
+    lhs = sum(float(np.sum(tan[q][m] * seeds[q][m])) for q in range(3))
+    rhs = float(np.sum(d[field] * adj[field]))
+    scale = sum(float(np.sum(np.abs(tan[q][m] * seeds[q][m]))) for q in range(3))
+    assert abs(lhs - rhs) <= 1e-12 * scale, (lhs, rhs, scale)
+    # the adjoint is deterministic
+    adj2 = momentum_adjoint(s, g, *seeds)
+    for a, b in zip(adj, adj2):
+        np.testing.assert_array_equal(a, b)
+
+
+def test_adjoint_unit_columns():
+    """J^T e_C at one fluid cell C equals the row of J read off by unit
+    tangents at every input point of its stencil."""
+    s, case, g = _sphere()
+    spec = case.blocks[0]
+    C = (6, 7, 8)  # natural-layout index of an interior fluid cell
+    assert _mask(s, g, spec)[C]
+    z = np.zeros(spec.shape, order="F")
+    e = z.copy(order="F")
+    e[C] = 1.0
+    adj = momentum_adjoint(s, g, e, z, z)  # gradient of ut(C)
+    for f in range(4):
+        for off in ((0, 0, 0), (1, 0, 0), (-1, 0, 0), (2, 0, 0), (0, -1, 0), (1, -1, 0), (0, 0, 2)):
+            X = tuple(c + o for c, o in zip(C, off))
+            d = [z, z, z, z]
+            d[f] = z.copy(order="F")
+            d[f][X] = 1.0
+            _, tan = momentum_tangent(s, g, *d)
+            assert tan[0][C] == adj[f][X], (f, off, tan[0][C], adj[f][X])

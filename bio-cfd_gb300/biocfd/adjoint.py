@@ -85,3 +85,34 @@ def momentum_adjoint(solver, g: int, utb, vtb, wtb, dt: float | None = None, re:
     check(solver.L.bcfd_momentum_adjoint(g, dt, re, *(a.ctypes.data_as(P) for a in ins),
                                          *(a.ctypes.data_as(P) for a in outs)), "momentum_adjoint")
     return tuple(outs)
+
+
+def adjoint_run(solver, weights: dict, n_steps: int, every: int = 20, uc: float | None = None,
+                gradient: bool = True, adj_tol: float = 1e-13, adj_itmax: int = 200000):
+    """Discrete adjoint of n_steps FP64 time steps of the solver's single
+    body-free block, checkpointing every `every` steps.
+
+    J = (1/N) sum_{n=1..N} <W, x^n> with W = weights {"u","v","w","p"}
+    (natural-layout arrays; missing fields weigh 0).  Returns J, or with
+    `gradient` (J, dJ/duc, {"u","v","w","p"}: dJ/dx^0).  The block advances
+    by n_steps, exactly as solver.run(n_steps) would advance it."""
+    c = solver.case
+    g = solver.handles[0]
+    shape = c.blocks[0].shape
+    W = [np.asfortranarray(weights.get(k, np.zeros(shape)), dtype=np.float64) for k in ("u", "v", "w", "p")]
+    cfg = solver.config(0)
+    if uc is not None:
+        cfg.uc = uc
+    P = C.POINTER(C.c_double)
+    J = C.c_double()
+    duc = C.c_double()
+    grads = [np.zeros(shape, order="F") for _ in range(4)] if gradient else None
+    null = C.cast(None, P)
+    check(solver.L.bcfd_adjoint_run(g, C.byref(cfg), n_steps, every, *(w.ctypes.data_as(P) for w in W),
+                                    adj_tol, adj_itmax, C.byref(J),
+                                    C.byref(duc) if gradient else null,
+                                    *((a.ctypes.data_as(P) for a in grads) if gradient else (null,) * 4)),
+          "adjoint_run")
+    if not gradient:
+        return J.value
+    return J.value, duc.value, dict(zip(("u", "v", "w", "p"), grads))

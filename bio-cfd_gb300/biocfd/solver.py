@@ -102,6 +102,11 @@ class Solver:
         if case.interfaces and not case.blocks[0].has_body:
             check(L.bcfd_fine_block_cell(), "fine_block_cell")
             check(L.bcfd_cellcount_solid_coarse(self.handles[0]), "cellcount_solid_coarse")
+        if not case.interfaces and not case.blocks[0].has_body:
+            # a lone block without a body (not a configuration main.F90
+            # builds): tagged all fluid and counted like a fine block
+            check(L.bcfd_tagging_th(self.handles[0]), "tagging_th")
+            check(L.bcfd_cellcount_solid(self.handles[0]), "cellcount_solid")
         if with_fields:
             for g, ini in zip(self.handles, case.init):
                 self.upload_fields(g, ini)

@@ -28,28 +28,25 @@ std::vector<double> transpose_line(const std::vector<double>& A, int n) {
   return T;
 }
 
-int solve_zero_bc(HostBlock* hb, const double* r, double* x, double tol, int64_t itmax, bool transpose) {
+}  // namespace
+
+// x = A^{-1} r (or A^{-T} r) on the fluid cells, device natural-layout arrays
+int solve_zero_bc_dev(HostBlock* hb, const double* r, double* x, double tol, int64_t itmax, bool transpose) {
   DevBlock& D = hb->d;
   const Dims& d = D.d;
   if (!D.Acx || hb->Acx.empty()) return BCFD_E_STATE;
   const double* keep[3] = {D.Acx, D.Acy, D.Acz};
   const int keep_rev = hb->sor_rev;
   double* tab = nullptr;
-  double* nat = nullptr;
   int rc = 0;
-  const size_t np = (size_t)d.npts();
-  if (cudaMalloc(&nat, np * sizeof(double)) != cudaSuccess) return BCFD_E_NOMEM;
   if (transpose) {
     const std::vector<double> tx = transpose_line(hb->Acx, d.nx), ty = transpose_line(hb->Acy, d.ny),
                               tz = transpose_line(hb->Acz, d.nz);
     std::vector<double> all(tx);
     all.insert(all.end(), ty.begin(), ty.end());
     all.insert(all.end(), tz.begin(), tz.end());
-    if (cudaMalloc(&tab, all.size() * sizeof(double)) != cudaSuccess) {
-      cudaFree(nat);
-      return BCFD_E_NOMEM;
-    }
-    if (cudaMemcpy(tab, all.data(), all.size() * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) rc = BCFD_E_CUDA;
+    if (cudaMalloc(&tab, all.size() * sizeof(double)) != cudaSuccess) return BCFD_E_NOMEM;
+    if (h2d(tab, all.data(), all.size() * sizeof(double)) != cudaSuccess) rc = BCFD_E_CUDA;
     D.Acx = tab;
     D.Acy = tab + tx.size();
     D.Acz = tab + tx.size() + ty.size();
@@ -61,23 +58,32 @@ int solve_zero_bc(HostBlock* hb, const double* r, double* x, double tol, int64_t
     if (!rc && cudaMemsetAsync(D.bpk[c], 0, pbytes, stream()) != cudaSuccess) rc = BCFD_E_CUDA;
   }
   if (!rc && cudaMemsetAsync(&D.stats->niter, 0, sizeof(int64_t), stream()) != cudaSuccess) rc = BCFD_E_CUDA;
-  if (!rc && cudaMemcpyAsync(nat, r, np * sizeof(double), cudaMemcpyHostToDevice, stream()) != cudaSuccess)
-    rc = BCFD_E_CUDA;
-  if (!rc) rc = launch_pack(hb, nat, D.bpk);
+  if (!rc) rc = launch_pack(hb, r, D.bpk);
   // residual-target FP64 solve of A x = r (deltat = 1)
   if (!rc) rc = launch_sor(hb, itmax, 1.0, 0.0, tol);
-  if (!rc) rc = launch_unpack(hb, D.pc, nat);
-  if (!rc && cudaMemcpyAsync(x, nat, np * sizeof(double), cudaMemcpyDeviceToHost, stream()) != cudaSuccess)
-    rc = BCFD_E_CUDA;
+  if (!rc) rc = launch_unpack(hb, D.pc, x);
   if (!rc && cudaStreamSynchronize(stream()) != cudaSuccess) rc = BCFD_E_CUDA;
   D.Acx = keep[0];
   D.Acy = keep[1];
   D.Acz = keep[2];
   hb->sor_rev = keep_rev;
   cudaFree(tab);
-  cudaFree(nat);
   if (rc) return rc;
   return take_block_error(hb);
+}
+
+namespace {
+
+int solve_zero_bc(HostBlock* hb, const double* r, double* x, double tol, int64_t itmax, bool transpose) {
+  const size_t np = (size_t)hb->d.d.npts();
+  double* buf = nullptr;
+  if (cudaMalloc(&buf, 2 * np * sizeof(double)) != cudaSuccess) return BCFD_E_NOMEM;
+  int rc = 0;
+  if (h2d(buf, r, np * sizeof(double)) != cudaSuccess) rc = BCFD_E_CUDA;
+  if (!rc) rc = solve_zero_bc_dev(hb, buf, buf + np, tol, itmax, transpose);
+  if (!rc && d2h(x, buf + np, np * sizeof(double)) != cudaSuccess) rc = BCFD_E_CUDA;
+  cudaFree(buf);
+  return rc;
 }
 
 }  // namespace
@@ -117,17 +123,17 @@ int bcfd_momentum_tangent(bcfd_handle h, double deltat, double re, const double*
   double* dtan[3];
   for (int q = 0; q < 4 && !r; ++q) {
     din[q] = buf + q * np;
-    if (cudaMemcpy((void*)din[q], in[q], np * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) r = BCFD_E_CUDA;
+    if (h2d((void*)din[q], in[q], np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
   }
   for (int q = 0; q < 3; ++q) {
     dval[q] = buf + (4 + q) * np;
     dtan[q] = buf + (7 + q) * np;
   }
-  if (!r && cudaMemset(buf + 4 * np, 0, 6 * np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
+  if (!r && cudaMemsetAsync(buf + 4 * np, 0, 6 * np * sizeof(double), stream()) != cudaSuccess) r = BCFD_E_CUDA;
   if (!r) r = launch_momentum_tangent(hb, deltat, re, din, dval, dtan);
   if (!r && cudaStreamSynchronize(stream()) != cudaSuccess) r = BCFD_E_CUDA;
   for (int q = 0; q < 6 && !r; ++q)
-    if (cudaMemcpy(outh[q], buf + (4 + q) * np, np * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+    if (d2h(outh[q], buf + (4 + q) * np, np * sizeof(double)) != cudaSuccess)
       r = BCFD_E_CUDA;
   cudaFree(buf);
   if (r) return r;
@@ -155,13 +161,14 @@ int bcfd_momentum_adjoint(bcfd_handle h, double deltat, double re, const double*
   double* dab[4];
   for (int q = 0; q < 3 && !r; ++q) {
     dsb[q] = buf + q * np;
-    if (cudaMemcpy((void*)dsb[q], in[q], np * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess) r = BCFD_E_CUDA;
+    if (h2d((void*)dsb[q], in[q], np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
   }
   for (int q = 0; q < 4; ++q) dab[q] = buf + (3 + q) * np;
+  if (!r && cudaMemsetAsync(buf + 3 * np, 0, 4 * np * sizeof(double), stream()) != cudaSuccess) r = BCFD_E_CUDA;
   if (!r) r = launch_momentum_adjoint(hb, deltat, re, dsb, dab, (uint32_t*)(buf + 7 * np));
   if (!r && cudaStreamSynchronize(stream()) != cudaSuccess) r = BCFD_E_CUDA;
   for (int q = 0; q < 4 && !r; ++q)
-    if (cudaMemcpy(outh[q], dab[q], np * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) r = BCFD_E_CUDA;
+    if (d2h(outh[q], dab[q], np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
   cudaFree(buf);
   if (r) return r;
   return take_block_error(hb);

@@ -1166,10 +1166,10 @@ int bcfd_profile_end(bcfd_profile_report* out) {
     out->sor_launches++;
   }
   int64_t n = 0;
-  BCFD_CUDA(cudaMemcpy(&n, L.prof_dev, sizeof(int64_t), cudaMemcpyDeviceToHost));
+  BCFD_CUDA(d2h(&n, L.prof_dev, sizeof(int64_t)));
   n = std::min<int64_t>(n, (int64_t)kProfLogCap);
   std::vector<int64_t> e(4 * (size_t)std::max<int64_t>(n, 1));
-  if (n) BCFD_CUDA(cudaMemcpy(e.data(), L.prof_dev + 1, 4 * n * sizeof(int64_t), cudaMemcpyDeviceToHost));
+  if (n) BCFD_CUDA(d2h(e.data(), L.prof_dev + 1, 4 * n * sizeof(int64_t)));
   for (int64_t q = 0; q < n; ++q) {
     const double sw = (double)e[4 * q], rp = (double)e[4 * q + 1], fl = (double)e[4 * q + 2];
     out->sor_sweeps += e[4 * q];

@@ -130,6 +130,17 @@ int note_launch(cudaError_t e = cudaGetLastError());
 #define BCFD_CUDA(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { ::bcfd::report_cuda(_e, #x, __FILE__, __LINE__); return BCFD_E_CUDA; } } while (0)
 void report_cuda(cudaError_t e, const char* what, const char* file, int line);
 
+// host <-> device copies ordered on the library stream (a non-blocking
+// stream: plain cudaMemcpy / cudaMemset on the legacy stream would race with
+// its kernels); d2h returns once the data is on the host
+inline cudaError_t h2d(void* dst, const void* src, size_t bytes) {
+  return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream());
+}
+inline cudaError_t d2h(void* dst, const void* src, size_t bytes) {
+  const cudaError_t e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream());
+  return e != cudaSuccess ? e : cudaStreamSynchronize(stream());
+}
+
 // read and clear a block's device error word (synchronises)
 int take_block_error(HostBlock* hb);
 
@@ -170,6 +181,8 @@ int launch_sor_cluster(HostBlock* hb, int64_t itmax, double dt, double div_tol, 
 int launch_momentum(HostBlock* hb, double dt, double re, bool fp32);
 int launch_momentum_tangent(HostBlock* hb, double dt, double re, const double* const du[4], double* const val[3],
                             double* const tan[3]);
+int solve_zero_bc_dev(HostBlock* hb, const double* r, double* x, double tol, int64_t itmax, bool transpose);
+int run_one_step(const bcfd_step_config& cfg);
 int launch_momentum_adjoint(HostBlock* hb, double dt, double re, const double* const sb[3], double* const ab[4],
                             uint32_t* foot);
 int launch_velocity_bc(HostBlock* hb, double dt, double uc);

@@ -351,6 +351,9 @@ int run_steps_graph(const bcfd_step_config& cfg, int64_t n) {
 }
 
 }  // namespace
+
+int run_one_step(const bcfd_step_config& cfg) { return step_once(cfg); }
+
 }  // namespace bcfd
 
 using namespace bcfd;
@@ -428,12 +431,12 @@ int bcfd_coupling_apply(bcfd_handle h, int comp, int op, const double* in, doubl
     return BCFD_E_NOMEM;
   }
   int r = 0;
-  if (cudaMemcpy(din, in, nin * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess ||
-      cudaMemcpy(dout, out, nout * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+  if (h2d(din, in, nin * sizeof(double)) != cudaSuccess ||
+      h2d(dout, out, nout * sizeof(double)) != cudaSuccess)
     r = BCFD_E_CUDA;
   if (!r) r = coupling_apply(it, comp, op, din, dout);
   if (!r && cudaStreamSynchronize(stream()) != cudaSuccess) r = BCFD_E_CUDA;
-  if (!r && cudaMemcpy(out, dout, nout * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess) r = BCFD_E_CUDA;
+  if (!r && d2h(out, dout, nout * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
   cudaFree(din);
   cudaFree(dout);
   return r;
@@ -628,7 +631,7 @@ int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64
     int r = launch_build_list(hb, which, buf, cap, &m);
     std::vector<int> t(3 * (size_t)cap);
     if (!r) {
-      BCFD_CUDA(cudaMemcpy(t.data(), buf, 3 * cap * sizeof(int), cudaMemcpyDeviceToHost));
+      BCFD_CUDA(d2h(t.data(), buf, 3 * cap * sizeof(int)));
     }
     cudaFree(buf);
     if (r) return r;

@@ -681,7 +681,7 @@ __global__ void __launch_bounds__(128) k_mom_adjoint(DevBlock B, MomArgs a, cons
         const SeedReader rd{{B.u, B.v, B.w, B.p}, f, x};
         momentum_cell<Dual>(B, a, ci, cj, ck, c, rd, AdjOut{{ubar_t, vbar_t, wbar_t}, &acc});
       }
-      (f == 0 ? ub : f == 1 ? vb : f == 2 ? wb : pb)[x] = acc;
+      (f == 0 ? ub : f == 1 ? vb : f == 2 ? wb : pb)[x] += acc;
     }
   }
 }
@@ -847,7 +847,7 @@ int launch_momentum_tangent(HostBlock* hb, double dt, double re, const double* c
 
 
 // adjoint of nsMomentum2order at the block's current (u,v,w,p): (ub,vb,wb,pb)
-// = J^T (ubar_t, vbar_t, wbar_t), J the predictor's Jacobian on fluid cells;
+// += J^T (ubar_t, vbar_t, wbar_t), J the predictor's Jacobian on fluid cells;
 // foot is 16 words of device scratch
 int launch_momentum_adjoint(HostBlock* hb, double dt, double re, const double* const sb[3], double* const ab[4],
                             uint32_t* foot) {

@@ -165,6 +165,11 @@ class Oracle:
         if case.interfaces and not case.blocks[0].has_body:
             L.orc_fine_block_cell()
             L.orc_cellcount_solid_coarse(1)
+        if not case.interfaces and not case.blocks[0].has_body:
+            # a lone block without a body (not a configuration main.F90
+            # builds): tagged all fluid and counted like a fine block
+            L.orc_tagging_th_core(1)
+            L.orc_cellcount_solid(1)
         if with_fields:
             for g, ini in enumerate(case.init, 1):
                 for nm in ("u", "v", "w", "p"):

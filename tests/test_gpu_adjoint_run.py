@@ -1,0 +1,119 @@
+"""Discrete adjoint of whole FP64 time steps with checkpointing, on a
+body-free block with the domain boundary conditions.
+
+J = (1/N) sum_n <W, x^n>: a momentum flux through a mid plane plus the
+pressure difference across a control volume.  Its adjoint gradients with
+respect to the inflow velocity uc and to the initial state are checked against
+central finite differences at a 1e-4 relative perturbation (bar: 1e-4
+relative), the gradients are independent of the checkpoint spacing (bitwise:
+recomputation reproduces the forward run exactly), and the block ends at the
+state an ordinary run leaves."""
+import numpy as np
+import pytest
+
+from biocfd import synth
+from biocfd.adjoint import adjoint_run
+from biocfd.solver import Solver
+
+pytestmark = pytest.mark.gpu
+
+N_STEPS = 12
+
+
+def _case():
+    case = synth.uniform_block(n=(24, 16, 16), lengths=(3.0, 2.0, 2.0))
+    return synth.replace(case, epsi=1e-14, pc_ita_max=50000)
+
+
+def _solver(case, init=None):
+    if init is not None:
+        case = synth.replace(case, init=[init])
+    s = Solver(case)
+    s.setup()
+    return s
+
+
+def _weights(case):
+    spec = case.blocks[0]
+    shp = spec.shape
+    nx, ny, nz = spec.nx, spec.ny, spec.nz
+    wu = np.zeros(shp, order="F")
+    wu[nx // 2, 1:ny + 1, 1:nz + 1] = 1.0 / (ny * nz)  # mean u through a mid plane
+    wp = np.zeros(shp, order="F")
+    box = (slice(5, 9), slice(5, 11))
+    wp[8, box[0], box[1]] = 1.0 / 24.0  # upstream face of a control volume
+    wp[14, box[0], box[1]] = -1.0 / 24.0  # downstream face
+    return {"u": wu, "p": wp}
+
+
+def test_adjoint_gradient_uc_and_initial_state_vs_fd():
+    case = _case()
+    W = _weights(case)
+    s = _solver(case)
+    J, duc, g = adjoint_run(s, W, N_STEPS, every=5)
+    assert np.isfinite(J) and abs(duc) > 0.0
+
+    # dJ/duc: central differences at 1e-4 relative
+    h = 1e-4 * case.uc
+    jp = adjoint_run(_solver(case), W, N_STEPS, every=5, uc=case.uc + h, gradient=False)
+    jm = adjoint_run(_solver(case), W, N_STEPS, every=5, uc=case.uc - h, gradient=False)
+    fd = (jp - jm) / (2 * h)
+    assert abs(fd - duc) <= 1e-4 * abs(fd), (fd, duc)
+
+    # dJ/dx0 along a random direction on the interior (1e-4 relative size)
+    init = case.init[0]
+    rng = np.random.default_rng(7)
+    spec = case.blocks[0]
+    m = np.zeros(spec.shape, bool, order="F")
+    m[1:-1, 1:-1, 1:-1] = True
+    # each field's direction scaled to the field's own size (p starts at 0):
+    # a 1e-4 relative step stays clear of the upwind switches of v and w
+    scale = {k: max(float(np.sqrt(np.mean(init[k] ** 2))), 1e-3) if k != "p" else 1.0 for k in ("u", "v", "w", "p")}
+    d = {k: np.asfortranarray(rng.normal(size=spec.shape) * m * scale[k]) for k in ("u", "v", "w", "p")}
+    eps = 1e-4
+    xp = {k: init[k] + eps * d[k] for k in d}
+    xm = {k: init[k] - eps * d[k] for k in d}
+    jp = adjoint_run(_solver(case, xp), W, N_STEPS, every=5, gradient=False)
+    jm = adjoint_run(_solver(case, xm), W, N_STEPS, every=5, gradient=False)
+    fd = (jp - jm) / (2 * eps)
+    ad = sum(float(np.sum(g[k] * d[k])) for k in d)
+    assert abs(fd - ad) <= 1e-4 * abs(fd), (fd, ad)
+
+
+def test_checkpoint_spacing_does_not_change_the_gradient():
+    case = _case()
+    W = _weights(case)
+    out = [adjoint_run(_solver(case), W, N_STEPS, every=k) for k in (1, 5, N_STEPS)]
+    J0, d0, g0 = out[0]
+    for J, duc, g in out[1:]:
+        assert J == J0 and duc == d0
+        for k in g0:
+            np.testing.assert_array_equal(g[k], g0[k])
+
+
+def test_block_left_at_forward_final_state():
+    case = _case()
+    W = _weights(case)
+    s = _solver(case)
+    J = adjoint_run(s, W, N_STEPS, every=4)[0]
+    fa = s.fields(s.handles[0])
+    r = _solver(case)
+    acc = 0.0
+    g = r.handles[0]
+    for _ in range(N_STEPS):
+        r.run(1)
+        f = r.fields(g)
+        acc += sum(float(np.sum(W[k] * f[k])) for k in W)
+    fb = r.fields(g)
+    for k in ("u", "v", "w", "p"):
+        np.testing.assert_array_equal(fa[k], fb[k])
+    assert abs(J - acc / N_STEPS) <= 1e-12 * abs(J)
+
+
+def test_refuses_blocks_with_a_body():
+    case = synth.sphere_single_block(n=24, n_steps=1, diameter=0.3)
+    s = Solver(case)
+    s.setup()
+    from biocfd._lib import BcfdError
+    with pytest.raises(BcfdError):
+        adjoint_run(s, {"u": np.zeros(case.blocks[0].shape)}, 2, every=1)

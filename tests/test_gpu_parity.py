@@ -136,3 +136,15 @@ def test_steps_100_single_block_bitwise():
     compare_fields(o, s, "100 steps")
     compare_iters(o, s, "100 steps")
     compare_search(o, s, "100 steps")
+
+
+def test_steps_body_free_block():
+    """A lone block with the domain BCs and no body (tagged all fluid and
+    counted): three drop-in steps bitwise against the oracle."""
+    case = synth.replace(synth.uniform_block(n=(24, 16, 16), lengths=(3.0, 2.0, 2.0)), n_steps=3, epsi=1e-8)
+    o, s = _pair(case)
+    for _ in range(3):
+        o.step()
+    s.run(3)
+    compare_fields(o, s, "3 steps, body-free block")
+    compare_iters(o, s, "3 steps, body-free block")

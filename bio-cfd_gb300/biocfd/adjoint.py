@@ -88,14 +88,18 @@ def momentum_adjoint(solver, g: int, utb, vtb, wtb, dt: float | None = None, re:
 
 
 def adjoint_run(solver, weights: dict, n_steps: int, every: int = 20, uc: float | None = None,
-                gradient: bool = True, adj_tol: float = 1e-13, adj_itmax: int = 200000):
+                gradient: bool = True, adj_tol: float = 1e-13, adj_itmax: int = 200000,
+                stress_seed=None, mu_f: float = 1.0, rho_f: float = 1.0):
     """Discrete adjoint of n_steps FP64 time steps of the solver's single
-    body-free block, checkpointing every `every` steps.
+    block (domain BCs, optionally a stationary body), checkpointing every
+    `every` steps.
 
-    J = (1/N) sum_{n=1..N} <W, x^n> with W = weights {"u","v","w","p"}
-    (natural-layout arrays; missing fields weigh 0).  Returns J, or with
-    `gradient` (J, dJ/duc, {"u","v","w","p"}: dJ/dx^0).  The block advances
-    by n_steps, exactly as solver.run(n_steps) would advance it."""
+    J = (1/N) sum_{n=1..N} (<W, x^n> + sum_t stress_seed[t] C_t(x^n)) with
+    W = weights {"u","v","w","p"} (natural-layout arrays; missing fields weigh
+    0) and C_t the four drag/lift coefficients of stress_calculation(mu_f,
+    rho_f) (e.g. stress_seed = (1, 1, 0, 0) for the total drag coefficient).
+    Returns J, or with `gradient` (J, dJ/duc, {"u","v","w","p"}: dJ/dx^0).
+    The block advances by n_steps, exactly as solver.run(n_steps) would."""
     c = solver.case
     g = solver.handles[0]
     shape = c.blocks[0].shape
@@ -108,7 +112,9 @@ def adjoint_run(solver, weights: dict, n_steps: int, every: int = 20, uc: float 
     duc = C.c_double()
     grads = [np.zeros(shape, order="F") for _ in range(4)] if gradient else None
     null = C.cast(None, P)
+    seed = None if stress_seed is None else np.ascontiguousarray(stress_seed, dtype=np.float64)
     check(solver.L.bcfd_adjoint_run(g, C.byref(cfg), n_steps, every, *(w.ctypes.data_as(P) for w in W),
+                                    null if seed is None else seed.ctypes.data_as(P), mu_f, rho_f,
                                     adj_tol, adj_itmax, C.byref(J),
                                     C.byref(duc) if gradient else null,
                                     *((a.ctypes.data_as(P) for a in grads) if gradient else (null,) * 4)),

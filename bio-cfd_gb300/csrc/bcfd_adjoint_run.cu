@@ -169,26 +169,52 @@ __global__ void k_div_adj(DevBlock B, double dt, const double* y, double* ut_b, 
   }
 }
 
-// the work arrays start as ut = u: positions the predictor does not write
-// pass their adjoint to the state; p' = p + pc passes p's adjoint through
-__global__ void k_pass_adj(DevBlock B, const double* ut_b, const double* vt_b, const double* wt_b,
-                           const double* p_b, Fields4 s) {
-  const Dims& d = B.d;
-  const int64_t n = d.npts();
+// u = ut (updateVelocity, all points) transposed: the adjoint of u moves to ut
+__global__ void k_copy_adj(int64_t n, double* ub, double* vb, double* wb, double* utb, double* vtb, double* wtb) {
   for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
-    const int i = 1 + (int)(x % d.NX);
-    const int64_t r = x / d.NX;
-    const int j = 1 + (int)(r % d.NY), k = 1 + (int)(r / d.NY);
-    if (!fluid_at(B, i, j, k)) {
-      s.u[x] += ut_b[x];
-      s.v[x] += vt_b[x];
-      s.w[x] += wt_b[x];
-    }
-    s.p[x] += p_b[x];
+    utb[x] += ub[x];
+    vtb[x] += vb[x];
+    wtb[x] += wb[x];
+    ub[x] = 0.0;
+    vb[x] = 0.0;
+    wb[x] = 0.0;
   }
 }
 
-// y = x + a * w over 4 consecutive fields
+// solidCellBC transposed: ut, vt, wt and p are overwritten with 0 at solid cells
+__global__ void k_solid_adj(DevBlock B, double* utb, double* vtb, double* wtb, double* pb) {
+  const Dims& d = B.d;
+  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(t % d.nx);
+    const int64_t r = t / d.nx;
+    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
+    const int64_t c = d.idx(i, j, k);
+    if (B.cell[c] != 1) continue;
+    utb[c] = 0.0;
+    vtb[c] = 0.0;
+    wtb[c] = 0.0;
+    pb[c] = 0.0;
+  }
+}
+
+// the predictor overwrote ut, vt, wt on the fluid cells
+__global__ void k_zero_fluid(DevBlock B, double* utb, double* vtb, double* wtb) {
+  const Dims& d = B.d;
+  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(t % d.nx);
+    const int64_t r = t / d.nx;
+    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
+    const int64_t c = d.idx(i, j, k);
+    if (B.cell[c] != 0 || B.tsnear[c]) continue;
+    utb[c] = 0.0;
+    vtb[c] = 0.0;
+    wtb[c] = 0.0;
+  }
+}
+
+// y += a * w over n values
 __global__ void k_axpy(const double* w, double a, double* y, int64_t n) {
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x)
     y[t] += a * w[t];
@@ -220,27 +246,37 @@ __global__ void __launch_bounds__(kDotThreads) k_dot_acc(const double* w, Fields
     if ((x) != cudaSuccess) return BCFD_E_CUDA; \
   } while (0)
 
+// the step state: u, v, w, p and the work arrays ut, vt, wt (with a body the
+// work arrays differ from u, v, w between steps at the forced faces)
+constexpr int kStateFields = 7;
+
+double* const* state_arrays(HostBlock* hb, double* out[kStateFields]) {
+  DevBlock& D = hb->d;
+  out[0] = D.u;
+  out[1] = D.v;
+  out[2] = D.w;
+  out[3] = D.p;
+  out[4] = D.ut;
+  out[5] = D.vt;
+  out[6] = D.wt;
+  return out;
+}
+
 int save_state(HostBlock* hb, double* slot) {
   const size_t np = (size_t)hb->d.d.npts(), b = np * sizeof(double);
-  DevBlock& D = hb->d;
-  ACK(cudaMemcpyAsync(slot, D.u, b, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(slot + np, D.v, b, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(slot + 2 * np, D.w, b, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(slot + 3 * np, D.p, b, cudaMemcpyDeviceToDevice, stream()));
+  double* f[kStateFields];
+  state_arrays(hb, f);
+  for (int q = 0; q < kStateFields; ++q)
+    ACK(cudaMemcpyAsync(slot + q * np, f[q], b, cudaMemcpyDeviceToDevice, stream()));
   return 0;
 }
 
-// the state into the block, with ut = u (the invariant at a step's start)
 int load_state(HostBlock* hb, const double* slot) {
   const size_t np = (size_t)hb->d.d.npts(), b = np * sizeof(double);
-  DevBlock& D = hb->d;
-  ACK(cudaMemcpyAsync(D.u, slot, b, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(D.v, slot + np, b, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(D.w, slot + 2 * np, b, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(D.p, slot + 3 * np, b, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(D.ut, slot, b, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(D.vt, slot + np, b, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(D.wt, slot + 2 * np, b, cudaMemcpyDeviceToDevice, stream()));
+  double* f[kStateFields];
+  state_arrays(hb, f);
+  for (int q = 0; q < kStateFields; ++q)
+    ACK(cudaMemcpyAsync(f[q], slot + q * np, b, cudaMemcpyDeviceToDevice, stream()));
   return 0;
 }
 
@@ -256,37 +292,56 @@ int launch_vbc_adj(HostBlock* hb, double dt, double uc, double* tb[3], const Fie
 }
 
 struct AdjBuffers {
-  double* lam;   // adjoint of the step's output state (4 fields)
-  double* acc;   // adjoint of the step's input state (4 fields)
-  double* tb;    // adjoint of ut,vt,wt (3 fields)
+  double* A;     // adjoint of the 7 state arrays (kept in place through the step)
   double* pcb;   // adjoint of pc
   double* y;     // A^{-T} pcb
   double* ucl;   // dJ/duc per x-face line
   uint32_t* foot;
+  ForceCoef fc;  // forcing coefficients (blocks with a body)
 };
 
-// one reverse step: lam (adjoint of x^n) -> acc (adjoint of x^{n-1}); the
-// block holds x^{n-1}
+// One step transposed, in place on the adjoint arrays (the block holds the
+// step's input state; tags, IB lists and probes are those of the run, which a
+// stationary body keeps).  The forward order is that of the native step:
+// predictor, velocityBC, [solidCellBC, velocityForcing1], velocityBC, the
+// Poisson phase (div, solve, correctPressure, correctVelocity, velocityBC,
+// ut -> u), [pressureForcing1, velocityForcingField, pressureForcingField].
 int adjoint_step(HostBlock* hb, const bcfd_step_config& c, const AdjBuffers& a, double tol, int64_t itmax) {
   const int64_t np = hb->d.d.npts();
-  const size_t b = (size_t)np * sizeof(double);
-  double* tb[3] = {a.tb, a.tb + np, a.tb + 2 * np};
-  const double* pb = a.lam + 3 * np;
-  const Fields4 s{a.acc, a.acc + np, a.acc + 2 * np, a.acc + 3 * np};
-  ACK(cudaMemcpyAsync(a.tb, a.lam, 3 * b, cudaMemcpyDeviceToDevice, stream()));  // S11
-  ACK(cudaMemsetAsync(a.acc, 0, 4 * b, stream()));
-  TRY_R(launch_vbc_adj(hb, c.deltat, c.uc, tb, s, a.ucl));  // S9
-  k_correct_adj<<<grid_for(np, 256), 256, 0, stream()>>>(hb->d, c.deltat, tb[0], tb[1], tb[2], pb, a.pcb);  // S7, S6
+  double* A[kStateFields];
+  for (int q = 0; q < kStateFields; ++q) A[q] = a.A + q * np;
+  double* tb[3] = {A[4], A[5], A[6]};
+  const Fields4 s{A[0], A[1], A[2], A[3]};
+  const bool body = hb->has_body && hb->d.ne > 0;
+  if (body) {
+    const AdjPtrs pin{{A[3], A[1], A[2], A[3]}, {A[3], A[1], A[2], A[3]}};
+    const AdjPtrs field{{A[3], A[0], A[1], A[2]}, {A[3], A[4], A[5], A[6]}};
+    TRY_R(launch_forcing_adjoint(hb, 1, 0, pin, a.fc));    // pressureForcingField
+    TRY_R(launch_forcing_adjoint(hb, 1, 1, field, a.fc));  // velocityForcingField: reads ut, writes u
+    TRY_R(launch_forcing_adjoint(hb, 0, 0, pin, a.fc));    // pressureForcing1
+  }
+  k_copy_adj<<<grid_for(np, 256), 256, 0, stream()>>>(np, A[0], A[1], A[2], A[4], A[5], A[6]);
   BCFD_LAUNCHED();
-  TRY_R(solve_zero_bc_dev(hb, a.pcb, a.y, tol, itmax, true));  // S5
-  k_div_adj<<<grid_for(np, 256), 256, 0, stream()>>>(hb->d, c.deltat, a.y, tb[0], tb[1], tb[2]);  // S4
+  TRY_R(launch_vbc_adj(hb, c.deltat, c.uc, tb, s, a.ucl));
+  k_correct_adj<<<grid_for(np, 256), 256, 0, stream()>>>(hb->d, c.deltat, tb[0], tb[1], tb[2], A[3], a.pcb);
   BCFD_LAUNCHED();
-  TRY_R(launch_vbc_adj(hb, c.deltat, c.uc, tb, s, a.ucl));  // S3
-  TRY_R(launch_vbc_adj(hb, c.deltat, c.uc, tb, s, a.ucl));  // S2
+  TRY_R(solve_zero_bc_dev(hb, a.pcb, a.y, tol, itmax, true));
+  k_div_adj<<<grid_for(np, 256), 256, 0, stream()>>>(hb->d, c.deltat, a.y, tb[0], tb[1], tb[2]);
+  BCFD_LAUNCHED();
+  TRY_R(launch_vbc_adj(hb, c.deltat, c.uc, tb, s, a.ucl));
+  if (body) {
+    const AdjPtrs vin{{A[3], A[4], A[5], A[6]}, {A[3], A[4], A[5], A[6]}};
+    TRY_R(launch_forcing_adjoint(hb, 0, 1, vin, a.fc));  // velocityForcing1, in place on ut
+    const int64_t ni = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
+    k_solid_adj<<<grid_for(ni, 256), 256, 0, stream()>>>(hb->d, A[4], A[5], A[6], A[3]);
+    BCFD_LAUNCHED();
+  }
+  TRY_R(launch_vbc_adj(hb, c.deltat, c.uc, tb, s, a.ucl));
   const double* sb[3] = {tb[0], tb[1], tb[2]};
-  double* ab[4] = {s.u, s.v, s.w, s.p};
-  TRY_R(launch_momentum_adjoint(hb, c.deltat, c.re, sb, ab, a.foot));  // S1
-  k_pass_adj<<<grid_for(np, 256), 256, 0, stream()>>>(hb->d, tb[0], tb[1], tb[2], pb, s);
+  double* ab[4] = {A[0], A[1], A[2], A[3]};
+  TRY_R(launch_momentum_adjoint(hb, c.deltat, c.re, sb, ab, a.foot));
+  const int64_t ni = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
+  k_zero_fluid<<<grid_for(ni, 256), 256, 0, stream()>>>(hb->d, tb[0], tb[1], tb[2]);
   BCFD_LAUNCHED();
   return 0;
 }
@@ -299,7 +354,7 @@ struct DevMem {
   template <typename T>
   T* get(size_t n) {
     void* p = nullptr;
-    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) return nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
     ptrs.push_back(p);
     return static_cast<T*>(p);
   }
@@ -313,8 +368,9 @@ using namespace bcfd;
 extern "C" {
 
 int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps, int64_t every, const double* wu,
-                     const double* wv, const double* ww, const double* wp, double adj_tol, int64_t adj_itmax,
-                     double* J, double* dj_duc, double* gu, double* gv, double* gw, double* gp) {
+                     const double* wv, const double* ww, const double* wp, const double* stress_seed, double mu_f,
+                     double rho_f, double adj_tol, int64_t adj_itmax, double* J, double* dj_duc, double* gu,
+                     double* gv, double* gw, double* gp) {
   std::lock_guard<std::recursive_mutex> lk(lib().mu);
   HostBlock* hb = get_block(h);
   if (!hb) return BCFD_E_HANDLE;
@@ -324,22 +380,27 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   for (HostBlock* b : lib().blocks) live += b != nullptr;
   for (HostInterface* it : lib().ifs)
     if (it) return BCFD_E_STATE;
-  if (live != 1 || !hb->is_coarse || hb->has_body || hb->motion.on || cfg->precision != 0) return BCFD_E_STATE;
+  if (live != 1 || !hb->is_coarse || hb->motion.on || cfg->precision != 0) return BCFD_E_STATE;
   if (!hb->d.ca[0] || !hb->d.Acx) return BCFD_E_STATE;
+  const bool body = hb->has_body && hb->d.ne > 0;
+  const bool use_stress = stress_seed && body;
+  if (stress_seed && !body) return BCFD_E_STATE;
+  if (body && hb->d.ne > BCFD_STRESS_NOALLOC_MAX_ELEMS) return BCFD_E_CAPACITY;
   const bool grad = dj_duc || gu || gv || gw || gp;
   const Dims& d = hb->d.d;
   const int64_t np = d.npts();
   const size_t fb = (size_t)np * sizeof(double);
   const int64_t K = std::min(every, n_steps);
   const int64_t ncp = (n_steps + K - 1) / K;  // checkpoints at 0, K, 2K, ... < N
+  const size_t S = (size_t)kStateFields * np;
   DevMem mem;
   double* W = mem.get<double>(4 * np);
-  double* cps = mem.get<double>((size_t)ncp * 4 * np);
-  double* fin = mem.get<double>(4 * np);
+  double* cps = mem.get<double>((size_t)ncp * S);
+  double* fin = mem.get<double>(S);
   double* part = mem.get<double>(kDotCtas);
   if (!W || !cps || !fin || !part) return BCFD_E_NOMEM;
   const double* wh[4] = {wu, wv, ww, wp};
-  for (int q = 0; q < 4; ++q) ACK(cudaMemcpyAsync(W + q * np, wh[q], fb, cudaMemcpyHostToDevice, stream()));
+  for (int q = 0; q < 4; ++q) ACK(h2d(W + q * np, wh[q], fb));
   ACK(cudaMemsetAsync(part, 0, kDotCtas * sizeof(double), stream()));
   Lib& L = lib();
   const int64_t ita0 = L.ita;
@@ -348,76 +409,102 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   c.use_graph = 0;
   const Fields4 bx{hb->d.u, hb->d.v, hb->d.w, hb->d.p};
 
-  // forward: checkpoints, objective
+  // forward: the work arrays start equal to u, v, w; checkpoints; objective
+  ACK(cudaMemcpyAsync(hb->d.ut, hb->d.u, fb, cudaMemcpyDeviceToDevice, stream()));
+  ACK(cudaMemcpyAsync(hb->d.vt, hb->d.v, fb, cudaMemcpyDeviceToDevice, stream()));
+  ACK(cudaMemcpyAsync(hb->d.wt, hb->d.w, fb, cudaMemcpyDeviceToDevice, stream()));
   TRY_R(save_state(hb, cps));
-  TRY_R(load_state(hb, cps));
+  // the transpose assumes the tags the run starts with hold throughout
+  // (a stationary body: the per-step re-Search reproduces them)
+  std::vector<int8_t> tags0((size_t)np), tags1((size_t)np);
+  ACK(d2h(tags0.data(), hb->d.cell, (size_t)np));
+  double jstress = 0.0;
   for (int64_t n = 1; n <= n_steps; ++n) {
     TRY_R(run_one_step(c));
     k_dot_acc<<<kDotCtas, kDotThreads, 0, stream()>>>(W, bx, np, part);
     BCFD_LAUNCHED();
-    if (n % K == 0 && n < n_steps) TRY_R(save_state(hb, cps + (size_t)(n / K) * 4 * np));
+    if (use_stress) {
+      double co[4];
+      TRY_R(launch_stress_noalloc(hb, mu_f, rho_f, co));
+      for (int t = 0; t < 4; ++t) jstress += stress_seed[t] * co[t];
+    }
+    if (n % K == 0 && n < n_steps) TRY_R(save_state(hb, cps + (size_t)(n / K) * S));
   }
   TRY_R(save_state(hb, fin));
   std::vector<double> ph(kDotCtas);
-  ACK(cudaMemcpyAsync(ph.data(), part, kDotCtas * sizeof(double), cudaMemcpyDeviceToHost, stream()));
-  ACK(cudaStreamSynchronize(stream()));
+  ACK(d2h(ph.data(), part, kDotCtas * sizeof(double)));
   double jsum = 0.0;
   for (double v : ph) jsum += v;
-  *J = jsum / (double)n_steps;
+  *J = (jsum + jstress) / (double)n_steps;
   int err = take_block_error(hb);
+  ACK(d2h(tags1.data(), hb->d.cell, (size_t)np));
+  if (!err && tags0 != tags1) err = BCFD_E_STATE;
   if (err || !grad) {
     L.ita = ita0 + n_steps;
     L.totime = tot0 + n_steps * cfg->deltat;
     return err;
   }
 
+  // objective weights per step: W plus the stress coefficients' weights
+  if (use_stress) {
+    double* sd = mem.get<double>(4);
+    double* ss = mem.get<double>(8 + 64 * (size_t)hb->d.ne);
+    if (!sd || !ss) return BCFD_E_NOMEM;
+    ACK(h2d(sd, stress_seed, 4 * sizeof(double)));
+    TRY_R(launch_stress_weights(hb, mu_f, rho_f, sd, W, ss));
+  }
   // reverse: recompute each segment from its checkpoint, then step back
-  double* tape = mem.get<double>((size_t)K * 4 * np);
+  double* tape = mem.get<double>((size_t)K * S);
   AdjBuffers a;
-  a.lam = mem.get<double>(4 * np);
-  a.acc = mem.get<double>(4 * np);
-  a.tb = mem.get<double>(3 * np);
+  a.A = mem.get<double>(S);
   a.pcb = mem.get<double>(np);
   a.y = mem.get<double>(np);
   a.ucl = mem.get<double>((size_t)d.ny * d.nz);
   a.foot = mem.get<uint32_t>(16);
-  if (!tape || !a.lam || !a.acc || !a.tb || !a.pcb || !a.y || !a.ucl || !a.foot) return BCFD_E_NOMEM;
+  const size_t ntask = 6 * (size_t)hb->d.cap_ib;
+  a.fc.tgt = mem.get<int64_t>(body ? ntask : 1);
+  a.fc.axis = mem.get<int>(body ? ntask : 1);
+  a.fc.pos = mem.get<int64_t>(body ? 8 * ntask : 1);
+  a.fc.coef = mem.get<double>(body ? 8 * ntask : 1);
+  if (!tape || !a.A || !a.pcb || !a.y || !a.ucl || !a.foot || !a.fc.tgt || !a.fc.axis || !a.fc.pos || !a.fc.coef)
+    return BCFD_E_NOMEM;
   ACK(cudaMemsetAsync(a.ucl, 0, (size_t)d.ny * d.nz * sizeof(double), stream()));
-  ACK(cudaMemsetAsync(a.lam, 0, 4 * fb, stream()));
+  ACK(cudaMemsetAsync(a.A, 0, S * sizeof(double), stream()));
   const double wn = 1.0 / (double)n_steps;
-  k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, a.lam, 4 * np);
+  k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, a.A, 4 * np);
   BCFD_LAUNCHED();
   for (int64_t m = ncp - 1; m >= 0; --m) {
     const int64_t n0 = m * K, n1 = std::min(n0 + K, n_steps);
-    const double* cp = cps + (size_t)m * 4 * np;
-    ACK(cudaMemcpyAsync(tape, cp, 4 * fb, cudaMemcpyDeviceToDevice, stream()));
+    const double* cp = cps + (size_t)m * S;
+    ACK(cudaMemcpyAsync(tape, cp, S * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
     TRY_R(load_state(hb, cp));
     L.ita = ita0 + n0;
     L.totime = tot0 + n0 * cfg->deltat;
     for (int64_t n = n0 + 1; n < n1; ++n) {
       TRY_R(run_one_step(c));
-      TRY_R(save_state(hb, tape + (size_t)(n - n0) * 4 * np));
+      TRY_R(save_state(hb, tape + (size_t)(n - n0) * S));
     }
     for (int64_t n = n1; n > n0; --n) {
-      TRY_R(load_state(hb, tape + (size_t)(n - 1 - n0) * 4 * np));
+      TRY_R(load_state(hb, tape + (size_t)(n - 1 - n0) * S));
       TRY_R(adjoint_step(hb, c, a, adj_tol, adj_itmax));
-      std::swap(a.lam, a.acc);
       if (n - 1 >= 1) {
-        k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, a.lam, 4 * np);
+        k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, a.A, 4 * np);
         BCFD_LAUNCHED();
       }
     }
   }
-  // leave the block at x^N, as the forward run left it
+  // leave the block at the forward run's final state
   TRY_R(load_state(hb, fin));
   L.ita = ita0 + n_steps;
   L.totime = tot0 + n_steps * cfg->deltat;
+  // the run started from ut = u, vt = v, wt = w: their adjoints add up
+  k_axpy<<<grid_for(3 * np, 256), 256, 0, stream()>>>(a.A + 4 * np, 1.0, a.A, 3 * np);
+  BCFD_LAUNCHED();
   double* gh[4] = {gu, gv, gw, gp};
   for (int q = 0; q < 4; ++q)
-    if (gh[q]) ACK(cudaMemcpyAsync(gh[q], a.lam + q * np, fb, cudaMemcpyDeviceToHost, stream()));
+    if (gh[q]) ACK(cudaMemcpyAsync(gh[q], a.A + q * np, fb, cudaMemcpyDeviceToHost, stream()));
   std::vector<double> ul((size_t)d.ny * d.nz);
-  ACK(cudaMemcpyAsync(ul.data(), a.ucl, ul.size() * sizeof(double), cudaMemcpyDeviceToHost, stream()));
-  ACK(cudaStreamSynchronize(stream()));
+  ACK(d2h(ul.data(), a.ucl, ul.size() * sizeof(double)));
   if (dj_duc) {
     double sum = 0.0;
     for (double v : ul) sum += v;

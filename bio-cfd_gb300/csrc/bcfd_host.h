@@ -213,6 +213,21 @@ int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_
 int compute_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, int64_t ita, double deltat,
                               double dxmin, double freq, double totime);
 int launch_stress_noalloc(HostBlock* hb, double mu_f, double rho_f, double* out_host);
+// adjoint of the forcing loops (k_forcing.cu): per-task coefficient scratch
+// (capacity 6 * cap_ib tasks) and the adjoint arrays by axis (0 p, 1 u, 2 v, 3 w)
+struct ForceCoef {
+  int64_t* tgt;
+  int* axis;
+  int64_t* pos;
+  double* coef;
+};
+struct AdjPtrs {
+  double* tgt[4];
+  double* src[4];
+};
+int launch_forcing_adjoint(HostBlock* hb, int mode, int vel, const AdjPtrs& a, const ForceCoef& fc);
+int launch_stress_weights(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double* w,
+                          double* scratch);
 
 // Refresh the device table of block views (no copy when unchanged, so a
 // captured step contains none).

@@ -428,7 +428,69 @@ __global__ void k_p_ghost(DevBlock B) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of the forcing loops.  With the geometry fixed every task is affine
+// in its 8 stencil values (interpolation, derivative and the quadratic fit are
+// linear in them; the surface velocity and dp/dn are constants), so its
+// coefficients are reconstruct(e_q) - reconstruct(0).  The reference's loops
+// run the tasks in list order, in place; their transpose runs them in reverse
+// order on the adjoint arrays: take the target's adjoint, zero it (the target
+// was overwritten), add coefficient x adjoint to each stencil point.  A read
+// of a value an earlier task wrote becomes an add that the earlier task picks
+// up when its turn comes, which is exactly the chain rule through the serial
+// order.  One thread runs the reverse sweep, so the sums have a fixed order.
+// ---------------------------------------------------------------------------
+__global__ void k_force_coef(DevBlock B, int mode, int vel, ForceCoef fc) {
+  const int nib = (int)min(B.cnt[C_IB], (int64_t)B.cap_ib);
+  const int nt = vel ? 6 * nib : nib;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+    const int n = vel ? t / 6 : t, comp = vel ? t % 6 : -1;
+    const Probe P = make_probe(B, mode, comp, n);
+    double f[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) f[q] = 0.0;
+    const double r0 = reconstruct(B, mode, comp, P, f);
+    for (int q = 0; q < 8; ++q) {
+      f[q] = 1.0;
+      fc.coef[8 * (int64_t)t + q] = reconstruct(B, mode, comp, P, f) - r0;
+      f[q] = 0.0;
+      fc.pos[8 * (int64_t)t + q] = B.d.idx(P.ii + (q & 1), P.jj + ((q >> 1) & 1), P.kk + (q >> 2));
+    }
+    fc.tgt[t] = B.d.idx(P.ti, P.tj, P.tk);
+    fc.axis[t] = P.axis;
+  }
+}
+
+__global__ void k_force_rev(DevBlock B, int vel, ForceCoef fc, AdjPtrs a) {
+  if (blockIdx.x || threadIdx.x) return;
+  const int nib = (int)min(B.cnt[C_IB], (int64_t)B.cap_ib);
+  const int nt = vel ? 6 * nib : nib;
+  for (int t = nt - 1; t >= 0; --t) {
+    const int ax = fc.axis[t];
+    double* T = a.tgt[ax];
+    double* S = a.src[ax];
+    const double o = T[fc.tgt[t]];
+    T[fc.tgt[t]] = 0.0;
+    for (int q = 0; q < 8; ++q) S[fc.pos[8 * (int64_t)t + q]] += fc.coef[8 * (int64_t)t + q] * o;
+  }
+}
+
 }  // namespace
+
+// transpose of launch_forcing_velocity / launch_forcing_pressure (modes 0 and
+// 1) on adjoint arrays indexed by axis (0 p, 1 u, 2 v, 3 w): a.tgt holds the
+// adjoint of the written arrays, a.src that of the read ones (the same arrays
+// for the in-place loops; ut/vt/wt's for velocityForcingField, which reads ut
+// and writes u)
+int launch_forcing_adjoint(HostBlock* hb, int mode, int vel, const AdjPtrs& a, const ForceCoef& fc) {
+  if (hb->d.ne <= 0) return 0;
+  const int64_t cap = (vel ? 6 : 1) * (int64_t)hb->d.cap_ib;
+  k_force_coef<<<grid_for(cap, 128, 2048), 128, 0, stream()>>>(hb->d, mode, vel, fc);
+  BCFD_LAUNCHED();
+  k_force_rev<<<1, 32, 0, stream()>>>(hb->d, vel, fc, a);
+  BCFD_LAUNCHED();
+  return 0;
+}
 
 static DagScratch& dag_scratch(HostBlock* hb, int* status) {
   *status = 0;

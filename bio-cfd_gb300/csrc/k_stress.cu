@@ -34,17 +34,26 @@ __device__ __forceinline__ double der(double x, double x2, double x1, double p_x
   return (h1 * h1 * p_x2 - h2 * h2 * p_x1 + (h2 * h2 - h1 * h1) * p_x) / (h1 * h2 * (h1 + h2) + 1e-16);
 }
 
-// compute_value_and_derivatives with the find_index ranges 2..n+1 of StressCalc
-__device__ void vad(const DevBlock& B, double x, double y, double z, const double* xg, int nxg,
-                    const double* yg, int nyg, const double* zg, int nzg, int off, const double* var,
-                    double& val, double d3[3]) {
+// compute_value_and_derivatives with the find_index ranges 2..n+1 of
+// StressCalc, split into the bracket search (the 8 stencil points) and the
+// evaluation on the 8 values
+__device__ void vad_find(const DevBlock& B, double x, double y, double z, const double* xg, int nxg,
+                         const double* yg, int nyg, const double* zg, int nzg, int off, int ijk[3],
+                         int64_t pos[8]) {
   const Dims& d = B.d;
   const int i = fidx(B, x, xg, nxg, 2, d.nx + 1), j = fidx(B, y, yg, nyg, 2, d.ny + 1),
             k = fidx(B, z, zg, nzg, 2, d.nz + 1);
   const int ii = i - (off == 1), jj = j - (off == 2), kk = k - (off == 3);
-  double f[8];
 #pragma unroll
-  for (int q = 0; q < 8; ++q) f[q] = var[d.idx(ii + (q & 1), jj + ((q >> 1) & 1), kk + (q >> 2))];
+  for (int q = 0; q < 8; ++q) pos[q] = d.idx(ii + (q & 1), jj + ((q >> 1) & 1), kk + (q >> 2));
+  ijk[0] = i;
+  ijk[1] = j;
+  ijk[2] = k;
+}
+
+__device__ void vad_eval(double x, double y, double z, const double* xg, const double* yg, const double* zg,
+                         const int ijk[3], const double f[8], double& val, double d3[3]) {
+  const int i = ijk[0], j = ijk[1], k = ijk[2];
   const double yj = yg[j - 1], yj1 = yg[j], zk = zg[k - 1], zk1 = zg[k], xi = xg[i - 1], xi1 = xg[i];
   const double t11 = bil(y, z, yj, yj1, zk, zk1, f[0], f[2], f[4], f[6]);
   const double t12 = bil(y, z, yj, yj1, zk, zk1, f[1], f[3], f[5], f[7]);
@@ -58,55 +67,140 @@ __device__ void vad(const DevBlock& B, double x, double y, double z, const doubl
   d3[2] = der(z, zk1, zk, val, t32, t31);
 }
 
-// per element: [viscous drag, pressure drag, viscous lift, pressure lift, area, a_xz, a_yz]
-__global__ void k_stress_elem(DevBlock B, double mu_f, double rho_f, double* part) {
+// probe point and stencils of one element (fields u, v, w, p)
+struct ElemStencil {
+  double px, py, pz, diag;
+  int ijk[4][3];
+  int64_t pos[4][8];
+};
+
+__device__ ElemStencil elem_stencil(const DevBlock& B, int e) {
   const Dims& d = B.d;
+  ElemStencil S;
+  const int ic = fidx(B, B.xcent[e], B.x1, d.NX + 1, 2, d.nx + 1);
+  const int jc = fidx(B, B.ycent[e], B.y1, d.NY + 1, 2, d.ny + 1);
+  const int kc = fidx(B, B.zcent[e], B.z1, d.NZ + 1, 2, d.nz + 1);
+  const double dX = B.x1[ic] - B.x1[ic - 1], dY = B.y1[jc] - B.y1[jc - 1], dZ = B.z1[kc] - B.z1[kc - 1];
+  S.diag = sqrt(dX * dX + dY * dY + dZ * dZ);
+  const double nd = S.diag;
+  S.px = B.xcent[e] + nd * B.cosA[e];
+  S.py = B.ycent[e] + nd * B.cosB[e];
+  S.pz = B.zcent[e] + nd * B.cosG[e];
+  vad_find(B, S.px, S.py, S.pz, B.xu, d.NX + 1, B.yu, d.NY, B.zu, d.NZ, 1, S.ijk[0], S.pos[0]);
+  vad_find(B, S.px, S.py, S.pz, B.xv, d.NX, B.yv, d.NY + 1, B.zv, d.NZ, 2, S.ijk[1], S.pos[1]);
+  vad_find(B, S.px, S.py, S.pz, B.xw, d.NX, B.yw, d.NY, B.zw, d.NZ + 1, 3, S.ijk[2], S.pos[2]);
+  vad_find(B, S.px, S.py, S.pz, B.xp, d.NX, B.yp, d.NY, B.zp, d.NZ, 0, S.ijk[3], S.pos[3]);
+  return S;
+}
+
+// per element: [viscous drag, pressure drag, viscous lift, pressure lift, area, a_xz, a_yz]
+// from the element's 4 x 8 stencil values f (u, v, w, p)
+__device__ void elem_terms(const DevBlock& B, int e, double mu_f, double rho_f, const ElemStencil& S,
+                           const double f[4][8], double o[7]) {
+  const double nrm[3] = {B.cosA[e], B.cosB[e], B.cosG[e]};
+  const double nd = S.diag, diag = S.diag;
+  const double px = S.px, py = S.py, pz = S.pz;
+  const int sid = B.surf_id[e];
+  const double td = sid == 51 ? B.thetaDot1 : (sid == 52 ? B.thetaDot2 : 0.0);
+  const double tdd = sid == 51 ? B.thetaDDot1 : (sid == 52 ? B.thetaDDot2 : 0.0);
+  const double us = B.xdot;
+  const double vs = -td * (B.zcent[e] - B.piv_z) + B.ydot;
+  const double ws = td * (B.ycent[e] - B.piv_y);
+  const double ac_z = -(td * td) * (B.zcent[e] - B.piv_z);
+  const double ac_y = -(td * td) * (B.ycent[e] - B.piv_y);
+  const double at_z = tdd * (B.ycent[e] - B.piv_y);
+  const double at_y = -tdd * (B.zcent[e] - B.piv_z);
+  const double dpdn = -((ac_z + at_z) * B.cosG[e] + (ac_y + at_y) * B.cosB[e]) - B.yddot * B.cosB[e];
+  double val, g[3], ddn[3];
+  vad_eval(px, py, pz, B.xu, B.yu, B.zu, S.ijk[0], f[0], val, g);
+  ddn[0] = (2.0 / nd) * (val - us) - (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]);
+  vad_eval(px, py, pz, B.xv, B.yv, B.zv, S.ijk[1], f[1], val, g);
+  ddn[1] = (2.0 / nd) * (val - vs) - (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]);
+  vad_eval(px, py, pz, B.xw, B.yw, B.zw, S.ijk[2], f[2], val, g);
+  ddn[2] = (2.0 / nd) * (val - ws) - (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]);
+  const double alen = B.elen[e];
+  const double area = alen / 2.0;
+  const double a_yz = 0.5 * fabs(alen * nrm[0]);
+  const double a_xz = 0.5 * fabs(alen * nrm[1]);
+  const double dd = ddn[0] * nrm[0] + ddn[1] * nrm[1] + ddn[2] * nrm[2];
+  const double sh0 = (ddn[0] - dd * nrm[0]) * mu_f * area;
+  const double sh1 = (ddn[1] - dd * nrm[1]) * mu_f * area;
+  vad_eval(px, py, pz, B.xp, B.yp, B.zp, S.ijk[3], f[3], val, g);
+  const double dpdn_e = g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2];
+  const double cval = val - (dpdn_e + dpdn) * diag * 0.5;
+  o[0] = sh0;
+  o[1] = -cval * area * nrm[0] * rho_f;
+  o[2] = sh1;
+  o[3] = -cval * area * nrm[1] * rho_f;
+  o[4] = area;
+  o[5] = a_xz;
+  o[6] = a_yz;
+}
+
+__global__ void k_stress_elem(DevBlock B, double mu_f, double rho_f, double* part) {
+  const double* arr[4] = {B.u, B.v, B.w, B.p};
   for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B.ne; e += gridDim.x * blockDim.x) {
-    const double nrm[3] = {B.cosA[e], B.cosB[e], B.cosG[e]};
-    const int ic = fidx(B, B.xcent[e], B.x1, d.NX + 1, 2, d.nx + 1);
-    const int jc = fidx(B, B.ycent[e], B.y1, d.NY + 1, 2, d.ny + 1);
-    const int kc = fidx(B, B.zcent[e], B.z1, d.NZ + 1, 2, d.nz + 1);
-    const double dX = B.x1[ic] - B.x1[ic - 1], dY = B.y1[jc] - B.y1[jc - 1], dZ = B.z1[kc] - B.z1[kc - 1];
-    const double diag = sqrt(dX * dX + dY * dY + dZ * dZ);
-    const double nd = diag;
-    const double px = B.xcent[e] + nd * nrm[0], py = B.ycent[e] + nd * nrm[1], pz = B.zcent[e] + nd * nrm[2];
-    const int sid = B.surf_id[e];
-    const double td = sid == 51 ? B.thetaDot1 : (sid == 52 ? B.thetaDot2 : 0.0);
-    const double tdd = sid == 51 ? B.thetaDDot1 : (sid == 52 ? B.thetaDDot2 : 0.0);
-    const double us = B.xdot;
-    const double vs = -td * (B.zcent[e] - B.piv_z) + B.ydot;
-    const double ws = td * (B.ycent[e] - B.piv_y);
-    const double ac_z = -(td * td) * (B.zcent[e] - B.piv_z);
-    const double ac_y = -(td * td) * (B.ycent[e] - B.piv_y);
-    const double at_z = tdd * (B.ycent[e] - B.piv_y);
-    const double at_y = -tdd * (B.zcent[e] - B.piv_z);
-    const double dpdn = -((ac_z + at_z) * B.cosG[e] + (ac_y + at_y) * B.cosB[e]) - B.yddot * B.cosB[e];
-    double val, g[3], ddn[3];
-    vad(B, px, py, pz, B.xu, d.NX + 1, B.yu, d.NY, B.zu, d.NZ, 1, B.u, val, g);
-    ddn[0] = (2.0 / nd) * (val - us) - (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]);
-    vad(B, px, py, pz, B.xv, d.NX, B.yv, d.NY + 1, B.zv, d.NZ, 2, B.v, val, g);
-    ddn[1] = (2.0 / nd) * (val - vs) - (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]);
-    vad(B, px, py, pz, B.xw, d.NX, B.yw, d.NY, B.zw, d.NZ + 1, 3, B.w, val, g);
-    ddn[2] = (2.0 / nd) * (val - ws) - (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]);
-    const double alen = B.elen[e];
-    const double area = alen / 2.0;
-    const double a_yz = 0.5 * fabs(alen * nrm[0]);
-    const double a_xz = 0.5 * fabs(alen * nrm[1]);
-    const double dd = ddn[0] * nrm[0] + ddn[1] * nrm[1] + ddn[2] * nrm[2];
-    const double sh0 = (ddn[0] - dd * nrm[0]) * mu_f * area;
-    const double sh1 = (ddn[1] - dd * nrm[1]) * mu_f * area;
-    vad(B, px, py, pz, B.xp, d.NX, B.yp, d.NY, B.zp, d.NZ, 0, B.p, val, g);
-    const double dpdn_e = g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2];
-    const double cval = val - (dpdn_e + dpdn) * diag * 0.5;
-    double* o = part + 7 * (int64_t)e;
-    o[0] = sh0;
-    o[1] = -cval * area * nrm[0] * rho_f;
-    o[2] = sh1;
-    o[3] = -cval * area * nrm[1] * rho_f;
-    o[4] = area;
-    o[5] = a_xz;
-    o[6] = a_yz;
+    const ElemStencil S = elem_stencil(B, e);
+    double f[4][8];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) f[c][q] = arr[c][S.pos[c][q]];
+    elem_terms(B, e, mu_f, rho_f, S, f, part + 7 * (int64_t)e);
   }
+}
+
+// Weights of a fixed linear combination of the 4 coefficients as a function
+// of (u, v, w, p): the element terms are affine in the 32 stencil values, so
+// the partial of term q in value c is term(e_c) - term(0).  coef[e][32] and
+// pos[e][32] per element; the accumulation is done in element order.
+__global__ void k_stress_coef(DevBlock B, double mu_f, double rho_f, const double* scale, double* coef,
+                              int64_t* pos) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B.ne; e += gridDim.x * blockDim.x) {
+    const ElemStencil S = elem_stencil(B, e);
+    double f[4][8];
+    for (int c = 0; c < 4; ++c)
+      for (int q = 0; q < 8; ++q) f[c][q] = 0.0;
+    double o0[7], o1[7];
+    elem_terms(B, e, mu_f, rho_f, S, f, o0);
+    for (int c = 0; c < 4; ++c)
+      for (int q = 0; q < 8; ++q) {
+        f[c][q] = 1.0;
+        elem_terms(B, e, mu_f, rho_f, S, f, o1);
+        f[c][q] = 0.0;
+        double w = 0.0;
+        for (int t = 0; t < 4; ++t) w += scale[t] * (o1[t] - o0[t]);
+        coef[32 * (int64_t)e + 8 * c + q] = w;
+        pos[32 * (int64_t)e + 8 * c + q] = S.pos[c][q];
+      }
+  }
+}
+
+// scale[t] = seed[t] * 2 / aS (aS from the element areas, as k_stress_sum)
+__global__ void k_stress_scale(DevBlock B, const double* seed, double* scale) {
+  if (blockIdx.x || threadIdx.x) return;
+  double sx = 0.0, sy = 0.0;
+  for (int e = 0; e < B.ne; ++e) {
+    const double alen = B.elen[e];
+    sx += 0.5 * fabs(alen * B.cosB[e]);
+    sy += 0.5 * fabs(alen * B.cosA[e]);
+  }
+  const double aSx = 0.5 * sx, aSy = 0.5 * sy;
+  scale[0] = seed[0] * 2.0 / aSx;
+  scale[1] = seed[1] * 2.0 / aSy;
+  scale[2] = seed[2] * 2.0 / aSx;
+  scale[3] = seed[3] * 2.0 / aSy;
+}
+
+// w[c][pos] += coef over all elements, in element order (one thread)
+__global__ void k_stress_accum(int ne, const double* coef, const int64_t* pos, double* w, int64_t np) {
+  if (blockIdx.x || threadIdx.x) return;
+  for (int e = 0; e < ne; ++e)
+    for (int c = 0; c < 4; ++c)
+      for (int q = 0; q < 8; ++q) {
+        const int64_t r = 32 * (int64_t)e + 8 * c + q;
+        w[c * np + pos[r]] += coef[r];
+      }
 }
 
 // fixed-order pairwise reduction by one CTA
@@ -133,6 +227,25 @@ __global__ void k_stress_sum(const double* part, int ne, double* out) {
 }
 
 }  // namespace
+
+// w (4 fields, natural layout) += the gradient of sum_t seed[t] * coefficient t
+// with respect to (u, v, w, p) at the block's geometry (the coefficients are
+// affine in the fields); scratch: 2 * 32 * ne + 8 doubles
+int launch_stress_weights(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double* w,
+                          double* scratch) {
+  const int ne = hb->d.ne;
+  if (ne <= 0) return BCFD_E_STATE;
+  double* scale = scratch;
+  double* coef = scratch + 8;
+  int64_t* pos = reinterpret_cast<int64_t*>(coef + 32 * (size_t)ne);
+  k_stress_scale<<<1, 32, 0, stream()>>>(hb->d, seed_dev, scale);
+  TRY_R(note_launch());
+  k_stress_coef<<<grid_for(ne, 64), 64, 0, stream()>>>(hb->d, mu_f, rho_f, scale, coef, pos);
+  TRY_R(note_launch());
+  k_stress_accum<<<1, 32, 0, stream()>>>(ne, coef, pos, w, hb->d.d.npts());
+  TRY_R(note_launch());
+  return 0;
+}
 
 int launch_stress(HostBlock* hb, double mu_f, double rho_f, double* out_host) {
   const int ne = hb->d.ne;

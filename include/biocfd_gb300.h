@@ -263,18 +263,24 @@ typedef struct bcfd_step_config {
 int bcfd_block_set_role(bcfd_handle h, int is_coarse, int has_body);
 int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps);
 /* Discrete adjoint of n_steps whole time steps (no counterpart in the
- * reference).  Scope: one registered block with the domain BCs, no body and
- * no interfaces, FP64 drop-in steps (cfg->precision 0).  Runs the steps
- * forward, checkpointing the state (u,v,w,p) every `every` steps in HBM, and
- * returns J = (1/N) sum_{n=1..N} <W, x^n> for the natural-layout weights
- * (wu,wv,ww,wp).  When any gradient output is non-null it then runs the
- * reverse pass, recomputing each segment from its checkpoint, and returns
- * dJ/duc and dJ/d(u,v,w,p)^0; the adjoint Poisson solves run to
- * max|r - A^T y| <= adj_tol (at most adj_itmax iterations).  The block is left
- * at the forward run's final state. */
+ * reference).  Scope: one registered block with the domain BCs, no
+ * interfaces, FP64 drop-in steps (cfg->precision 0), with or without a
+ * stationary immersed body.  Runs the steps forward from the block's state
+ * with ut,vt,wt = u,v,w, checkpointing (u,v,w,p,ut,vt,wt) every `every` steps
+ * in HBM, and returns
+ *   J = (1/N) sum_{n=1..N} ( <W, x^n> + sum_t stress_seed[t] * C_t(x^n) )
+ * for natural-layout weights W = (wu,wv,ww,wp) over (u,v,w,p) and, when
+ * stress_seed (4 values) is non-null, the drag/lift coefficients C_t of
+ * bcfd_stress_calculation with (mu_f, rho_f) (a body is required).  When any
+ * gradient output is non-null it then runs the reverse pass, recomputing each
+ * segment from its checkpoint, and returns dJ/duc and dJ/d(u,v,w,p)^0; the
+ * adjoint Poisson solves run to max|r - A^T y| <= adj_tol (at most adj_itmax
+ * iterations).  The tags must not change during the run (BCFD_E_STATE
+ * otherwise).  The block is left at the forward run's final state. */
 int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps, int64_t every, const double* wu,
-                     const double* wv, const double* ww, const double* wp, double adj_tol, int64_t adj_itmax,
-                     double* J, double* dj_duc, double* gu, double* gv, double* gw, double* gp);
+                     const double* wv, const double* ww, const double* wp, const double* stress_seed, double mu_f,
+                     double rho_f, double adj_tol, int64_t adj_itmax, double* J, double* dj_duc, double* gu,
+                     double* gv, double* gw, double* gp);
 /* max over fluid cells of |div u| of the current u,v,w (FP64) */
 int bcfd_max_divergence(bcfd_handle h, double* out);
 /* out[0] = max over fluid cells of |div ut| right after the last velocity

@@ -1,13 +1,14 @@
-"""Discrete adjoint of whole FP64 time steps with checkpointing, on a
-body-free block with the domain boundary conditions.
+"""Discrete adjoint of whole FP64 time steps with checkpointing.
 
-J = (1/N) sum_n <W, x^n>: a momentum flux through a mid plane plus the
-pressure difference across a control volume.  Its adjoint gradients with
-respect to the inflow velocity uc and to the initial state are checked against
-central finite differences at a 1e-4 relative perturbation (bar: 1e-4
-relative), the gradients are independent of the checkpoint spacing (bitwise:
-recomputation reproduces the forward run exactly), and the block ends at the
-state an ordinary run leaves."""
+Body-free block with the domain BCs: J = (1/N) sum_n <W, x^n>, a momentum flux
+through a mid plane plus the pressure difference across a control volume.
+Stationary sphere (IB forcing in the step): J = the time-averaged drag
+coefficient (viscous + pressure) of stress_calculation.  The adjoint
+gradients with respect to the inflow velocity uc and to the initial state are
+checked against central finite differences at a 1e-4 relative perturbation
+(bar: 1e-4 relative), the gradients are independent of the checkpoint spacing
+(bitwise: recomputation reproduces the forward run exactly), and the block
+ends at the state an ordinary run leaves."""
 import numpy as np
 import pytest
 
@@ -110,13 +111,12 @@ def test_block_left_at_forward_final_state():
     assert abs(J - acc / N_STEPS) <= 1e-12 * abs(J)
 
 
-def test_refuses_blocks_with_a_body():
-    case = synth.sphere_single_block(n=24, n_steps=1, diameter=0.3)
-    s = Solver(case)
-    s.setup()
+def test_refuses_a_stress_objective_without_a_body():
+    case = _case()
+    s = _solver(case)
     from biocfd._lib import BcfdError
     with pytest.raises(BcfdError):
-        adjoint_run(s, {"u": np.zeros(case.blocks[0].shape)}, 2, every=1)
+        adjoint_run(s, {}, 2, every=1, stress_seed=(1.0, 1.0, 0.0, 0.0))
 
 
 @pytest.mark.parametrize("field", ["u", "v", "w", "p"])
@@ -138,3 +138,73 @@ def test_initial_state_gradient_per_field(field):
     fd = (jp - jm) / (2 * eps)
     ad = float(np.sum(g[field] * d))
     assert abs(fd - ad) <= 1e-4 * abs(fd), (field, fd, ad)
+
+
+
+# ---- stationary sphere: drag objective through the IB forcing ---------------
+
+SPHERE_STEPS = 6
+DRAG = (1.0, 1.0, 0.0, 0.0)
+
+
+def _sphere_case():
+    case = synth.sphere_single_block(n=24, n_steps=1, diameter=0.3)
+    return synth.replace(case, epsi=1e-14, pc_ita_max=50000)
+
+
+def _sphere_solver(case, state=None):
+    s = Solver(case)
+    s.setup()
+    s.run(1)  # the per-step re-Search settles the tags of the set-up
+    if state is not None:
+        s.upload_fields(s.handles[0], state)
+    return s
+
+
+def _drag_run(s, case, **kw):
+    return adjoint_run(s, {}, SPHERE_STEPS, every=kw.pop("every", 2), stress_seed=DRAG,
+                       mu_f=1.0 / case.re, rho_f=1.0, **kw)
+
+
+def test_sphere_drag_gradient_uc_vs_fd():
+    case = _sphere_case()
+    J, duc, g = _drag_run(_sphere_solver(case), case)
+    assert np.isfinite(J) and J != 0.0
+    h = 1e-4 * case.uc
+    jp = _drag_run(_sphere_solver(case), case, uc=case.uc + h, gradient=False)
+    jm = _drag_run(_sphere_solver(case), case, uc=case.uc - h, gradient=False)
+    fd = (jp - jm) / (2 * h)
+    assert abs(fd - duc) <= 1e-4 * abs(fd), (fd, duc)
+
+
+@pytest.mark.parametrize("field", ["u", "v", "w", "p"])
+def test_sphere_drag_gradient_state_vs_fd(field):
+    case = _sphere_case()
+    s0 = _sphere_solver(case)
+    g0 = s0.handles[0]
+    state = {k: v.copy(order="F") for k, v in s0.fields(g0).items() if k in ("u", "v", "w", "p")}
+    J, duc, g = _drag_run(s0, case)
+    spec = case.blocks[0]
+    cell = s0.tags(g0)["cell"]
+    m = np.zeros(spec.shape, bool, order="F")
+    m[1:-1, 1:-1, 1:-1] = True
+    m &= cell == 0
+    rng = np.random.default_rng(21)
+    scale = max(float(np.sqrt(np.mean(state[field] ** 2))), 1e-3)
+    d = np.asfortranarray(rng.normal(size=spec.shape) * m * scale)
+    eps = 1e-4
+    jp = _drag_run(_sphere_solver(case, {**state, field: state[field] + eps * d}), case, gradient=False)
+    jm = _drag_run(_sphere_solver(case, {**state, field: state[field] - eps * d}), case, gradient=False)
+    fd = (jp - jm) / (2 * eps)
+    ad = float(np.sum(g[field] * d))
+    assert abs(fd - ad) <= 1e-4 * abs(fd), (field, fd, ad)
+
+
+def test_sphere_checkpoint_spacing_does_not_change_the_gradient():
+    case = _sphere_case()
+    out = [_drag_run(_sphere_solver(case), case, every=k) for k in (1, 3, SPHERE_STEPS)]
+    J0, d0, g0 = out[0]
+    for J, duc, g in out[1:]:
+        assert J == J0 and duc == d0
+        for k in g0:
+            np.testing.assert_array_equal(g[k], g0[k])

@@ -48,7 +48,7 @@ _SIGS = {
     "bcfd_momentum_tangent": [c_i64, c_double, c_double, P_d, P_d, P_d, P_d, P_d, P_d, P_d, P_d, P_d, P_d],
     "bcfd_momentum_adjoint": [c_i64, c_double, c_double, P_d, P_d, P_d, P_d, P_d, P_d, P_d],
     "bcfd_adjoint_run": [c_i64, C.POINTER(StepConfig), c_i64, c_i64, P_d, P_d, P_d, P_d, P_d, c_double, c_double,
-                         c_double, c_i64, P_d, P_d, P_d, P_d, P_d, P_d],
+                         c_double, c_i64, P_d, P_d, P_d, P_d, P_d, P_d, P_d],
     "bcfd_block_set_body_motion": [c_i64, P_d],
     "bcfd_shift_surface_nodes_initial": [c_i64, c_double, c_double, c_i64, c_double, c_double, c_double],
     "bcfd_compute_surface_variables": [c_i64, c_double, c_double, c_i64, c_double, c_double, c_double,

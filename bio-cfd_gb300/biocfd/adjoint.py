@@ -98,8 +98,11 @@ def adjoint_run(solver, weights: dict, n_steps: int, every: int = 20, uc: float 
     W = weights {"u","v","w","p"} (natural-layout arrays; missing fields weigh
     0) and C_t the four drag/lift coefficients of stress_calculation(mu_f,
     rho_f) (e.g. stress_seed = (1, 1, 0, 0) for the total drag coefficient).
-    Returns J, or with `gradient` (J, dJ/duc, {"u","v","w","p"}: dJ/dx^0).
-    The block advances by n_steps, exactly as solver.run(n_steps) would."""
+    Returns J, or with `gradient` (J, dJ/duc, {"u","v","w","p"}: dJ/dx^0,
+    "kin": dJ/d(xdot, ydot, yddot, thetaDot1, thetaDDot1, thetaDot2,
+    thetaDDot2, alphaDot)} with the body's kinematic scalars constant and its
+    geometry fixed).  The block advances by n_steps, exactly as
+    solver.run(n_steps) would."""
     c = solver.case
     g = solver.handles[0]
     shape = c.blocks[0].shape
@@ -111,14 +114,18 @@ def adjoint_run(solver, weights: dict, n_steps: int, every: int = 20, uc: float 
     J = C.c_double()
     duc = C.c_double()
     grads = [np.zeros(shape, order="F") for _ in range(4)] if gradient else None
+    kin = np.zeros(8)
     null = C.cast(None, P)
     seed = None if stress_seed is None else np.ascontiguousarray(stress_seed, dtype=np.float64)
     check(solver.L.bcfd_adjoint_run(g, C.byref(cfg), n_steps, every, *(w.ctypes.data_as(P) for w in W),
                                     null if seed is None else seed.ctypes.data_as(P), mu_f, rho_f,
                                     adj_tol, adj_itmax, C.byref(J),
                                     C.byref(duc) if gradient else null,
+                                    kin.ctypes.data_as(P) if gradient else null,
                                     *((a.ctypes.data_as(P) for a in grads) if gradient else (null,) * 4)),
           "adjoint_run")
     if not gradient:
         return J.value
-    return J.value, duc.value, dict(zip(("u", "v", "w", "p"), grads))
+    out = dict(zip(("u", "v", "w", "p"), grads))
+    out["kin"] = kin
+    return J.value, duc.value, out

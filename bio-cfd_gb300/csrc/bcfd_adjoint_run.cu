@@ -369,8 +369,8 @@ extern "C" {
 
 int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps, int64_t every, const double* wu,
                      const double* wv, const double* ww, const double* wp, const double* stress_seed, double mu_f,
-                     double rho_f, double adj_tol, int64_t adj_itmax, double* J, double* dj_duc, double* gu,
-                     double* gv, double* gw, double* gp) {
+                     double rho_f, double adj_tol, int64_t adj_itmax, double* J, double* dj_duc,
+                     double* dj_dkin, double* gu, double* gv, double* gw, double* gp) {
   std::lock_guard<std::recursive_mutex> lk(lib().mu);
   HostBlock* hb = get_block(h);
   if (!hb) return BCFD_E_HANDLE;
@@ -386,7 +386,7 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   const bool use_stress = stress_seed && body;
   if (stress_seed && !body) return BCFD_E_STATE;
   if (body && hb->d.ne > BCFD_STRESS_NOALLOC_MAX_ELEMS) return BCFD_E_CAPACITY;
-  const bool grad = dj_duc || gu || gv || gw || gp;
+  const bool grad = dj_duc || dj_dkin || gu || gv || gw || gp;
   const Dims& d = hb->d.d;
   const int64_t np = d.npts();
   const size_t fb = (size_t)np * sizeof(double);
@@ -446,12 +446,18 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   }
 
   // objective weights per step: W plus the stress coefficients' weights
+  bool kin_stress = false;
+  double* stress_seed_dev = nullptr;
+  double* stress_scratch = nullptr;
   if (use_stress) {
     double* sd = mem.get<double>(4);
     double* ss = mem.get<double>(8 + 64 * (size_t)hb->d.ne);
     if (!sd || !ss) return BCFD_E_NOMEM;
     ACK(h2d(sd, stress_seed, 4 * sizeof(double)));
     TRY_R(launch_stress_weights(hb, mu_f, rho_f, sd, W, ss));
+    kin_stress = true;
+    stress_seed_dev = sd;
+    stress_scratch = ss;
   }
   // reverse: recompute each segment from its checkpoint, then step back
   double* tape = mem.get<double>((size_t)K * S);
@@ -466,8 +472,15 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   a.fc.axis = mem.get<int>(body ? ntask : 1);
   a.fc.pos = mem.get<int64_t>(body ? 8 * ntask : 1);
   a.fc.coef = mem.get<double>(body ? 8 * ntask : 1);
-  if (!tape || !a.A || !a.pcb || !a.y || !a.ucl || !a.foot || !a.fc.tgt || !a.fc.axis || !a.fc.pos || !a.fc.coef)
+  a.fc.kc = mem.get<double>(body ? 8 * ntask : 1);
+  a.fc.gk = mem.get<double>(8);
+  if (!tape || !a.A || !a.pcb || !a.y || !a.ucl || !a.foot || !a.fc.tgt || !a.fc.axis || !a.fc.pos || !a.fc.coef ||
+      !a.fc.kc || !a.fc.gk)
     return BCFD_E_NOMEM;
+  ACK(cudaMemsetAsync(a.fc.gk, 0, 8 * sizeof(double), stream()));
+  // the coefficients' own dependence on the kinematic scalars (the same at
+  // every step: (1/N) * N times)
+  if (kin_stress) TRY_R(launch_stress_kin(hb, mu_f, rho_f, stress_seed_dev, a.fc.gk, stress_scratch));
   ACK(cudaMemsetAsync(a.ucl, 0, (size_t)d.ny * d.nz * sizeof(double), stream()));
   ACK(cudaMemsetAsync(a.A, 0, S * sizeof(double), stream()));
   const double wn = 1.0 / (double)n_steps;
@@ -505,6 +518,7 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
     if (gh[q]) ACK(cudaMemcpyAsync(gh[q], a.A + q * np, fb, cudaMemcpyDeviceToHost, stream()));
   std::vector<double> ul((size_t)d.ny * d.nz);
   ACK(d2h(ul.data(), a.ucl, ul.size() * sizeof(double)));
+  if (dj_dkin) ACK(d2h(dj_dkin, a.fc.gk, 8 * sizeof(double)));
   if (dj_duc) {
     double sum = 0.0;
     for (double v : ul) sum += v;

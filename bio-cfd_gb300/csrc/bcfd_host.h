@@ -220,11 +220,28 @@ struct ForceCoef {
   int* axis;
   int64_t* pos;
   double* coef;
+  double* kc;  // per task, d(output)/d(kinematic scalar p), p = 0..7 (the order of bcfd_block_set_kinematics)
+  double* gk;  // 8 accumulators: dJ/d(kinematic scalar p)
 };
+// the 8 rigid-body kinematic scalars of a block, in bcfd_block_set_kinematics order
+__host__ __device__ inline double& kin_scalar(DevBlock& B, int p) {
+  switch (p) {
+    case 0: return B.xdot;
+    case 1: return B.ydot;
+    case 2: return B.yddot;
+    case 3: return B.thetaDot1;
+    case 4: return B.thetaDDot1;
+    case 5: return B.thetaDot2;
+    case 6: return B.thetaDDot2;
+    default: return B.alphaDot;
+  }
+}
 struct AdjPtrs {
   double* tgt[4];
   double* src[4];
 };
+int launch_stress_kin(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double* gk,
+                      double* scratch);
 int launch_forcing_adjoint(HostBlock* hb, int mode, int vel, const AdjPtrs& a, const ForceCoef& fc);
 int launch_stress_weights(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double* w,
                           double* scratch);

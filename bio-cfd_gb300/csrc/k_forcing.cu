@@ -458,6 +458,15 @@ __global__ void k_force_coef(DevBlock B, int mode, int vel, ForceCoef fc) {
     }
     fc.tgt[t] = B.d.idx(P.ti, P.tj, P.tk);
     fc.axis[t] = P.axis;
+    // kinematic sensitivities at f = 0: the output is at most quadratic in
+    // each scalar (centripetal terms), so the central difference with unit
+    // steps is its derivative
+    for (int p = 0; p < 8; ++p) {
+      DevBlock Bp = B, Bm = B;
+      kin_scalar(Bp, p) += 1.0;
+      kin_scalar(Bm, p) -= 1.0;
+      fc.kc[8 * (int64_t)t + p] = 0.5 * (reconstruct(Bp, mode, comp, P, f) - reconstruct(Bm, mode, comp, P, f));
+    }
   }
 }
 
@@ -472,6 +481,7 @@ __global__ void k_force_rev(DevBlock B, int vel, ForceCoef fc, AdjPtrs a) {
     const double o = T[fc.tgt[t]];
     T[fc.tgt[t]] = 0.0;
     for (int q = 0; q < 8; ++q) S[fc.pos[8 * (int64_t)t + q]] += fc.coef[8 * (int64_t)t + q] * o;
+    for (int p = 0; p < 8; ++p) fc.gk[p] += fc.kc[8 * (int64_t)t + p] * o;
   }
 }
 

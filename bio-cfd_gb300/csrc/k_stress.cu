@@ -176,6 +176,31 @@ __global__ void k_stress_coef(DevBlock B, double mu_f, double rho_f, const doubl
   }
 }
 
+// gk[p] += d/d(kinematic scalar p) of sum_t scale[t] * sum_e term_t(e) at
+// the current fields (the terms are affine in the fields and at most quadratic
+// in each scalar); one thread, element order
+__global__ void k_stress_kin(DevBlock B, double mu_f, double rho_f, const double* scale, double* gk) {
+  if (blockIdx.x || threadIdx.x) return;
+  const double* arr[4] = {B.u, B.v, B.w, B.p};
+  for (int p = 0; p < 8; ++p) {
+    DevBlock Bp = B, Bm = B;
+    kin_scalar(Bp, p) += 1.0;
+    kin_scalar(Bm, p) -= 1.0;
+    double acc = 0.0;
+    for (int e = 0; e < B.ne; ++e) {
+      const ElemStencil S = elem_stencil(B, e);
+      double f[4][8];
+      for (int c = 0; c < 4; ++c)
+        for (int q = 0; q < 8; ++q) f[c][q] = arr[c][S.pos[c][q]];
+      double op[7], om[7];
+      elem_terms(Bp, e, mu_f, rho_f, S, f, op);
+      elem_terms(Bm, e, mu_f, rho_f, S, f, om);
+      for (int t = 0; t < 4; ++t) acc += scale[t] * 0.5 * (op[t] - om[t]);
+    }
+    gk[p] += acc;
+  }
+}
+
 // scale[t] = seed[t] * 2 / aS (aS from the element areas, as k_stress_sum)
 __global__ void k_stress_scale(DevBlock B, const double* seed, double* scale) {
   if (blockIdx.x || threadIdx.x) return;
@@ -243,6 +268,18 @@ int launch_stress_weights(HostBlock* hb, double mu_f, double rho_f, const double
   k_stress_coef<<<grid_for(ne, 64), 64, 0, stream()>>>(hb->d, mu_f, rho_f, scale, coef, pos);
   TRY_R(note_launch());
   k_stress_accum<<<1, 32, 0, stream()>>>(ne, coef, pos, w, hb->d.d.npts());
+  TRY_R(note_launch());
+  return 0;
+}
+
+// gk[8] += the kinematic derivative of sum_t seed[t] * coefficient t at the
+// block's current fields; scratch: 8 doubles
+int launch_stress_kin(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double* gk,
+                      double* scratch) {
+  if (hb->d.ne <= 0) return BCFD_E_STATE;
+  k_stress_scale<<<1, 32, 0, stream()>>>(hb->d, seed_dev, scratch);
+  TRY_R(note_launch());
+  k_stress_kin<<<1, 32, 0, stream()>>>(hb->d, mu_f, rho_f, scratch, gk);
   TRY_R(note_launch());
   return 0;
 }

@@ -273,14 +273,19 @@ int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps);
  * stress_seed (4 values) is non-null, the drag/lift coefficients C_t of
  * bcfd_stress_calculation with (mu_f, rho_f) (a body is required).  When any
  * gradient output is non-null it then runs the reverse pass, recomputing each
- * segment from its checkpoint, and returns dJ/duc and dJ/d(u,v,w,p)^0; the
+ * segment from its checkpoint, and returns dJ/duc, dJ/d(u,v,w,p)^0 and
+ * dj_dkin[8], the derivative with respect to the body's rigid-body kinematic
+ * scalars in bcfd_block_set_kinematics order (xdot, ydot, yddot, thetaDot1,
+ * thetaDDot1, thetaDot2, thetaDDot2, alphaDot) held constant over the run
+ * with the geometry fixed (the body's surface velocity and acceleration in
+ * the forcing and in the coefficients); the
  * adjoint Poisson solves run to max|r - A^T y| <= adj_tol (at most adj_itmax
  * iterations).  The tags must not change during the run (BCFD_E_STATE
  * otherwise).  The block is left at the forward run's final state. */
 int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps, int64_t every, const double* wu,
                      const double* wv, const double* ww, const double* wp, const double* stress_seed, double mu_f,
-                     double rho_f, double adj_tol, int64_t adj_itmax, double* J, double* dj_duc, double* gu,
-                     double* gv, double* gw, double* gp);
+                     double rho_f, double adj_tol, int64_t adj_itmax, double* J, double* dj_duc,
+                     double* dj_dkin, double* gu, double* gv, double* gw, double* gp);
 /* max over fluid cells of |div u| of the current u,v,w (FP64) */
 int bcfd_max_divergence(bcfd_handle h, double* out);
 /* out[0] = max over fluid cells of |div ut| right after the last velocity

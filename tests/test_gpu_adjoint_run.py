@@ -208,3 +208,33 @@ def test_sphere_checkpoint_spacing_does_not_change_the_gradient():
         assert J == J0 and duc == d0
         for k in g0:
             np.testing.assert_array_equal(g[k], g0[k])
+
+
+KIN0 = np.array([0.05, 0.1, 0.2, 0.0, 0.0, 0.0, 0.0, 0.0])
+
+
+def _set_kin(s, case, kin):
+    import ctypes as C
+    spec = case.blocks[0]
+    full = np.ascontiguousarray(np.concatenate([kin, np.asarray(spec.piv, dtype=np.float64)]))
+    check = __import__("biocfd._lib", fromlist=["check"]).check
+    check(s.L.bcfd_block_set_kinematics(s.handles[0], full.ctypes.data_as(C.POINTER(C.c_double))), "kin")
+
+
+@pytest.mark.parametrize("p", [0, 1, 2])
+def test_sphere_drag_gradient_kinematics_vs_fd(p):
+    """dJ/d(xdot, ydot, yddot): the sphere's surface translating (and
+    accelerating) at constant rates with its geometry fixed."""
+    case = _sphere_case()
+
+    def run(kin, gradient):
+        s = _sphere_solver(case)
+        _set_kin(s, case, kin)
+        return _drag_run(s, case, gradient=gradient)
+
+    J, duc, g = run(KIN0, True)
+    h = 1e-4 * max(abs(KIN0[p]), 1.0)
+    e = np.zeros(8)
+    e[p] = h
+    fd = (run(KIN0 + e, False) - run(KIN0 - e, False)) / (2 * h)
+    assert abs(fd - g["kin"][p]) <= 1e-4 * abs(fd), (p, fd, g["kin"][p])

@@ -382,6 +382,19 @@ int upload_coefs(HostBlock* hb) {
       foff.push_back(f.size());
       for (double x : (t < N_TAB ? hb->ca[t] : hb->ck[t - N_TAB])) f.push_back((float)x);
     }
+    // the x coefficients per float4 run and x-parity, 16-byte aligned
+    while (f.size() % 4) f.push_back(0.0f);
+    const size_t axr_off = f.size();
+    {
+      const int nx = hb->d.d.nx, nq = hb->d.d.NXH / 4;
+      for (int par = 0; par < 2; ++par)
+        for (int col = 0; col < 3; ++col)
+          for (int run = 0; run < nq; ++run)
+            for (int u = 0; u < 4; ++u) {
+              const int ic = std::min(std::max(2 * (4 * run + u) + 1 + par, 2), nx + 1);
+              f.push_back((float)hb->Acx[(size_t)(ic - 2) + (size_t)col * nx]);
+            }
+    }
     if (hb->coef_f32) {
       cudaFree(hb->coef_f32);
       hb->allocs.erase(std::remove(hb->allocs.begin(), hb->allocs.end(), (void*)hb->coef_f32), hb->allocs.end());
@@ -393,6 +406,7 @@ int upload_coefs(HostBlock* hb) {
     hb->d.Acxf = hb->coef_f32;
     hb->d.Acyf = hb->coef_f32 + hb->Acx.size();
     hb->d.Aczf = hb->coef_f32 + hb->Acx.size() + hb->Acy.size();
+    hb->d.axr = reinterpret_cast<const float4*>(hb->coef_f32 + axr_off);
     for (int t = 0; t < N_TAB; ++t) {
       hb->d.caf[t] = hb->coef_f32 + foff[t];
       hb->d.ckf[t] = hb->coef_f32 + foff[N_TAB + t];

@@ -92,6 +92,10 @@ struct DevBlock {
   const double *Acx, *Acy, *Acz;
   // the same coefficients rounded to FP32 (mixed-precision sweeps)
   const float *Acxf, *Acyf, *Aczf;
+  // Acxf laid out per packed float4 run of the FP32 half-sweep:
+  // axr[(3 * par + col) * (NXH / 4) + run] holds column col of the run's 4
+  // cells i = 2(4 run + u) + 1 + par (clamped to 2..nx+1)
+  const float4* axr;
   // momentum tables ca/ck(6, n+2), column-major
   const double *ca[N_TAB], *ck[N_TAB];
   // FP32 copies of dxa/dya/dza and ca/ck (FP32 momentum stencil)

@@ -429,6 +429,12 @@ __device__ __forceinline__ void tile_half32(const DevBlock& B, const Tile& t, fl
     const float ox = par ? o[pi + 4] : o[pi - 1];
     const float ay1 = B.Acyf[j - 2], ay2 = B.Acyf[j - 2 + d.ny], ay3 = B.Acyf[j - 2 + 2 * d.ny];
     const float az1 = B.Aczf[k - 2], az2 = B.Aczf[k - 2 + d.nz], az3 = B.Aczf[k - 2 + 2 * d.nz];
+    // the run's x coefficients: three float4 loads of a small table (the
+    // same FP32 values as Acxf at the run's cells)
+    const float4* __restrict__ ar = B.axr + (int64_t)(3 * par) * nq + w.a;
+    const float4 c1 = ar[0], c2 = ar[nq], c3 = ar[2 * nq];
+    const float axv1[4] = {c1.x, c1.y, c1.z, c1.w}, axv2[4] = {c2.x, c2.y, c2.z, c2.w},
+                axv3[4] = {c3.x, c3.y, c3.z, c3.w};
     const float oxs[6] = {par ? oc.x : ox, oc.x, oc.y, oc.z, oc.w, par ? ox : oc.w};
     const float sv[4] = {os.x, os.y, os.z, os.w}, nv4[4] = {on.x, on.y, on.z, on.w};
     const float bv[4] = {ob.x, ob.y, ob.z, ob.w}, tv[4] = {ot.x, ot.y, ot.z, ot.w};
@@ -442,8 +448,7 @@ __device__ __forceinline__ void tile_half32(const DevBlock& B, const Tile& t, fl
       // local memory)
       const float left = par ? oxs[u + 1] : oxs[u];
       const float right = par ? oxs[u + 2] : oxs[u + 1];
-      const int ic = min(max(2 * (h0 + u) + 1 + par, 2), d.nx + 1);
-      const float ax1 = B.Acxf[ic - 2], ax2 = B.Acxf[ic - 2 + d.nx], ax3 = B.Acxf[ic - 2 + 2 * d.nx];
+      const float ax1 = axv1[u], ax2 = axv2[u], ax3 = axv3[u];
       float s = rv[u];
       s = __fmaf_rn(-ax1, left, s);
       s = __fmaf_rn(-ax3, right, s);

@@ -236,18 +236,29 @@ def sweep_roofline(torch, local, hbm, block=(384, 256, 256), fp32_pairs=40, fp64
     check(s.L.bcfd_cellcount_solid(g), "cellcount_solid")
     check(s.L.bcfd_compute_div(g), "compute_div")
     check(s.L.bcfd_block_sor_sweeps(g, 2, 1), "sor_sweeps")
+    s.autotune()  # the launch shapes a user gets after bcfd_autotune
     cells = block[0] * block[1] * block[2]
     out = {"block": "x".join(map(str, block)) + f" ({cells / 1e6:.1f}M cells), no body",
-           "l2": f"FP32 working set {17 * cells / 1e6:.0f} MB vs 129 MB L2"}
+           "l2": f"FP32 working set {17 * cells / 1e6:.0f} MB vs 129 MB L2",
+           "solve_launch": s.solve_launch(g)}
     for prec, pairs, key in ((1, fp32_pairs, "fp32"), (0, fp64_pairs, "fp64")):
         if pairs <= 0:
             continue
-        s.profile_begin()
-        check(s.L.bcfd_block_sor_sweeps(g, pairs, prec), "sor_sweeps")
-        p = s.profile_end()
+        runs = {}
+        for n in (pairs, 2 * pairs):
+            s.profile_begin()
+            check(s.L.bcfd_block_sor_sweeps(g, n, prec), "sor_sweeps")
+            runs[n] = s.profile_end()
+        p = runs[pairs]
         gbs = p["sor_bytes"] / (p["sor_ms"] * 1e-3) / 1e9
+        # the sweep pairs alone: the difference between the 2P and P launches
+        # (the residual, update and launch costs cancel)
+        q = runs[2 * pairs]
+        mgbs = (q["sor_bytes"] - p["sor_bytes"]) / ((q["sor_ms"] - p["sor_ms"]) * 1e-3) / 1e9
         out[key] = {"sweep_pairs": pairs, "ms": p["sor_ms"], "gbs": gbs, "frac_of_measured_hbm": gbs / hbm,
-                    "bytes": p["sor_bytes"]}
+                    "bytes": p["sor_bytes"], "sweep_pair_gbs_marginal": mgbs,
+                    "sweep_pair_frac_of_measured_hbm": mgbs / hbm,
+                    "half_sweep_us": (q["sor_ms"] - p["sor_ms"]) * 1e3 / (2 * pairs)}
     s.close()
     return out
 

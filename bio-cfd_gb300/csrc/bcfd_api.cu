@@ -395,6 +395,14 @@ int upload_coefs(HostBlock* hb) {
               f.push_back((float)hb->Acx[(size_t)(ic - 2) + (size_t)col * nx]);
             }
     }
+    const size_t ayr_off = f.size();
+    for (int j = 0; j < hb->d.d.ny; ++j)
+      for (int col = 0; col < 4; ++col)
+        f.push_back(col < 3 ? (float)hb->Acy[(size_t)j + (size_t)col * hb->d.d.ny] : 0.0f);
+    const size_t azr_off = f.size();
+    for (int k = 0; k < hb->d.d.nz; ++k)
+      for (int col = 0; col < 4; ++col)
+        f.push_back(col < 3 ? (float)hb->Acz[(size_t)k + (size_t)col * hb->d.d.nz] : 0.0f);
     if (hb->coef_f32) {
       cudaFree(hb->coef_f32);
       hb->allocs.erase(std::remove(hb->allocs.begin(), hb->allocs.end(), (void*)hb->coef_f32), hb->allocs.end());
@@ -407,6 +415,8 @@ int upload_coefs(HostBlock* hb) {
     hb->d.Acyf = hb->coef_f32 + hb->Acx.size();
     hb->d.Aczf = hb->coef_f32 + hb->Acx.size() + hb->Acy.size();
     hb->d.axr = reinterpret_cast<const float4*>(hb->coef_f32 + axr_off);
+    hb->d.ayr = reinterpret_cast<const float4*>(hb->coef_f32 + ayr_off);
+    hb->d.azr = reinterpret_cast<const float4*>(hb->coef_f32 + azr_off);
     for (int t = 0; t < N_TAB; ++t) {
       hb->d.caf[t] = hb->coef_f32 + foff[t];
       hb->d.ckf[t] = hb->coef_f32 + foff[N_TAB + t];

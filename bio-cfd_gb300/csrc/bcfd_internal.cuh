@@ -96,6 +96,8 @@ struct DevBlock {
   // axr[(3 * par + col) * (NXH / 4) + run] holds column col of the run's 4
   // cells i = 2(4 run + u) + 1 + par (clamped to 2..nx+1)
   const float4* axr;
+  // Acyf / Aczf rows as {a1, a2, a3, 0} (one float4 load per run)
+  const float4 *ayr, *azr;
   // momentum tables ca/ck(6, n+2), column-major
   const double *ca[N_TAB], *ck[N_TAB];
   // FP32 copies of dxa/dya/dza and ca/ck (FP32 momentum stencil)

@@ -427,8 +427,9 @@ __device__ __forceinline__ void tile_half32(const DevBlock& B, const Tile& t, fl
     const float4 e4 = *reinterpret_cast<const float4*>(own + pi);
     // the one x-neighbour outside the centre float4 (in range: row +- 1)
     const float ox = par ? o[pi + 4] : o[pi - 1];
-    const float ay1 = B.Acyf[j - 2], ay2 = B.Acyf[j - 2 + d.ny], ay3 = B.Acyf[j - 2 + 2 * d.ny];
-    const float az1 = B.Aczf[k - 2], az2 = B.Aczf[k - 2 + d.nz], az3 = B.Aczf[k - 2 + 2 * d.nz];
+    const float4 cy = B.ayr[j - 2], cz = B.azr[k - 2];
+    const float ay1 = cy.x, ay2 = cy.y, ay3 = cy.z;
+    const float az1 = cz.x, az2 = cz.y, az3 = cz.z;
     // the run's x coefficients: three float4 loads of a small table (the
     // same FP32 values as Acxf at the run's cells)
     const float4* __restrict__ ar = B.axr + (int64_t)(3 * par) * nq + w.a;

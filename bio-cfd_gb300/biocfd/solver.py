@@ -188,6 +188,16 @@ class Solver:
         check(self.L.bcfd_get_time(C.byref(ita), C.byref(tt)), "get_time")
         return ita.value, tt.value
 
+    def set_time(self, ita: int, totime: float):
+        """Set the native driver's loop counters (a restart: lastConditions'
+        ita and totime, then totime + deltat as app/main.F90:116 does)."""
+        mi = self.case.motion
+        inor = next((b.mesh.inor for b in self.case.blocks if b.mesh is not None), 1)
+        check(self.L.bcfd_set_motion_inputs((mi.phase_deg * np.pi / 180.0) if mi else 0.0,
+                                            mi.piv_pt if mi else 0.0, mi.freq if mi else 0.0,
+                                            mi.dxmin if mi else 0.0, inor, int(ita), float(totime)),
+              "set_motion_inputs")
+
     def step(self):
         # advance the loop counters as the native driver does
         ita, tt = self.time()

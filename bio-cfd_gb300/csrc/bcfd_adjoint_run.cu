@@ -21,6 +21,8 @@
 // transposed line tables, colours reversed) and the momentum adjoint at the
 // step's own input state, recomputed from the nearest checkpoint.  Each
 // adjoint value is a sum in a fixed order: the result is deterministic.
+#include <array>
+
 #include "bcfd_host.h"
 
 namespace bcfd {
@@ -120,8 +122,10 @@ __global__ void k_vbc_z_adj(DevBlock B, double* ut_b, double* vt_b, double* wt_b
   }
 }
 
-// correctVelocity and correctPressure transposed: pcb = adjoint of pc (zero
-// off the fluid cells, where pc is held at zero)
+// correctVelocity and correctPressure transposed: pcb = adjoint of pc at every
+// position the corrections read (the fluid cells, and the non-fluid neighbours
+// whose pc is boundary data of the solve: fine-block ghosts, coarse cells
+// under a fine block)
 __global__ void k_correct_adj(DevBlock B, double dt, const double* ut_b, const double* vt_b, const double* wt_b,
                               const double* p_b, double* pcb) {
   const Dims& d = B.d;
@@ -130,19 +134,59 @@ __global__ void k_correct_adj(DevBlock B, double dt, const double* ut_b, const d
     const int i = 1 + (int)(x % d.NX);
     const int64_t r = x / d.NX;
     const int j = 1 + (int)(r % d.NY), k = 1 + (int)(r / d.NY);
-    if (!fluid_at(B, i, j, k)) {
-      pcb[x] = 0.0;
-      continue;
+    double g = 0.0;
+    if (fluid_at(B, i, j, k)) {
+      g = p_b[x];
+      g += dt / (0.5 * (B.dxa[i] + B.dxa[i - 1])) * ut_b[x];
+      g += dt / (0.5 * (B.dya[j] + B.dya[j - 1])) * vt_b[x];
+      g += dt / (0.5 * (B.dza[k] + B.dza[k - 1])) * wt_b[x];
     }
-    double g = p_b[x];
-    g += dt / (0.5 * (B.dxa[i] + B.dxa[i - 1])) * ut_b[x];
-    g += dt / (0.5 * (B.dya[j] + B.dya[j - 1])) * vt_b[x];
-    g += dt / (0.5 * (B.dza[k] + B.dza[k - 1])) * wt_b[x];
     if (fluid_at(B, i - 1, j, k)) g -= dt / (0.5 * (B.dxa[i - 1] + B.dxa[i - 2])) * ut_b[x - 1];
     if (fluid_at(B, i, j - 1, k)) g -= dt / (0.5 * (B.dya[j - 1] + B.dya[j - 2])) * vt_b[x - sy];
     if (fluid_at(B, i, j, k - 1)) g -= dt / (0.5 * (B.dza[k - 1] + B.dza[k - 2])) * wt_b[x - sz];
     pcb[x] = g;
   }
+}
+
+// The solve with boundary data: on the fluid cells A_ff pc = b/dt - A_fn g,
+// g the pc held at non-fluid neighbours.  Given y = A_ff^{-T} pcb_f, the
+// adjoint of g is pcb_g - A_fn^T y (pc at a non-fluid position also passes
+// through unchanged); the fluid cells' incoming pc (the initial guess) has
+// no influence at convergence.  A_fn's entries are the line-table
+// coefficients of the fluid row for that neighbour.
+__global__ void k_dirichlet_adj(DevBlock B, const double* y, double* pcb) {
+  const Dims& d = B.d;
+  const int64_t n = d.npts(), sy = d.NX, sz = (int64_t)d.NX * d.NY;
+  const int nx = d.nx, ny = d.ny, nz = d.nz;
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(x % d.NX);
+    const int64_t r = x / d.NX;
+    const int j = 1 + (int)(r % d.NY), k = 1 + (int)(r / d.NY);
+    if (fluid_at(B, i, j, k)) {
+      pcb[x] = 0.0;
+      continue;
+    }
+    double s = 0.0;
+    // x is the left neighbour of (i+1) and the right neighbour of (i-1), ...
+    if (fluid_at(B, i + 1, j, k)) s += B.Acx[(i + 1) - 2] * y[x + 1];
+    if (fluid_at(B, i - 1, j, k)) s += B.Acx[(i - 1) - 2 + 2 * nx] * y[x - 1];
+    if (fluid_at(B, i, j + 1, k)) s += B.Acy[(j + 1) - 2] * y[x + sy];
+    if (fluid_at(B, i, j - 1, k)) s += B.Acy[(j - 1) - 2 + 2 * ny] * y[x - sy];
+    if (fluid_at(B, i, j, k + 1)) s += B.Acz[(k + 1) - 2] * y[x + sz];
+    if (fluid_at(B, i, j, k - 1)) s += B.Acz[(k - 1) - 2 + 2 * nz] * y[x - sz];
+    pcb[x] -= s;
+  }
+}
+
+// a[x] = 0 where mask[x] != 0 (positions a coupling map overwrote)
+__global__ void k_zero_masked(int64_t n, double* a, const double* mask) {
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
+    if (mask[x] != 0.0) a[x] = 0.0;
+}
+
+__global__ void k_fill(int64_t n, double* a, double v) {
+  for (int64_t x = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; x < n; x += (int64_t)gridDim.x * blockDim.x)
+    a[x] = v;
 }
 
 // computeDiv transposed with the solve's 1/deltat: ut_b += D^T (y / deltat)
@@ -291,59 +335,156 @@ int launch_vbc_adj(HostBlock* hb, double dt, double uc, double* tb[3], const Fie
   return 0;
 }
 
-struct AdjBuffers {
-  double* A;     // adjoint of the 7 state arrays (kept in place through the step)
-  double* pcb;   // adjoint of pc
-  double* y;     // A^{-T} pcb
-  double* ucl;   // dJ/duc per x-face line
-  uint32_t* foot;
-  ForceCoef fc;  // forcing coefficients (blocks with a body)
+// per block: the adjoint arrays and scratch
+struct AdjBlock {
+  HostBlock* hb = nullptr;
+  double* A = nullptr;     // adjoint of the 7 state arrays, in place through a step
+  double* pcb = nullptr;   // adjoint of pc
+  double* y = nullptr;     // A_ff^{-T} pcb
+  double* bb = nullptr;    // accumulated y of the block's solves (adjoint of b, times deltat)
+  uint32_t* foot = nullptr;
+  ForceCoef fc{};          // forcing coefficients and kinematic accumulators (body blocks)
+  double* ucl = nullptr;   // dJ/duc per x-face line (coarse block)
+  bool body = false;
+  int64_t np = 0;
+  double* F(int q) const { return A + q * np; }
 };
 
-// One step transposed, in place on the adjoint arrays (the block holds the
-// step's input state; tags, IB lists and probes are those of the run, which a
-// stationary body keeps).  The forward order is that of the native step:
-// predictor, velocityBC, [solidCellBC, velocityForcing1], velocityBC, the
-// Poisson phase (div, solve, correctPressure, correctVelocity, velocityBC,
-// ut -> u), [pressureForcing1, velocityForcingField, pressureForcingField].
-int adjoint_step(HostBlock* hb, const bcfd_step_config& c, const AdjBuffers& a, double tol, int64_t itmax) {
-  const int64_t np = hb->d.d.npts();
-  double* A[kStateFields];
-  for (int q = 0; q < kStateFields; ++q) A[q] = a.A + q * np;
-  double* tb[3] = {A[4], A[5], A[6]};
-  const Fields4 s{A[0], A[1], A[2], A[3]};
-  const bool body = hb->has_body && hb->d.ne > 0;
-  if (body) {
-    const AdjPtrs pin{{A[3], A[1], A[2], A[3]}, {A[3], A[1], A[2], A[3]}};
-    const AdjPtrs field{{A[3], A[0], A[1], A[2]}, {A[3], A[4], A[5], A[6]}};
-    TRY_R(launch_forcing_adjoint(hb, 1, 0, pin, a.fc));    // pressureForcingField
-    TRY_R(launch_forcing_adjoint(hb, 1, 1, field, a.fc));  // velocityForcingField: reads ut, writes u
-    TRY_R(launch_forcing_adjoint(hb, 0, 0, pin, a.fc));    // pressureForcing1
-  }
-  k_copy_adj<<<grid_for(np, 256), 256, 0, stream()>>>(np, A[0], A[1], A[2], A[4], A[5], A[6]);
-  BCFD_LAUNCHED();
-  TRY_R(launch_vbc_adj(hb, c.deltat, c.uc, tb, s, a.ucl));
-  k_correct_adj<<<grid_for(np, 256), 256, 0, stream()>>>(hb->d, c.deltat, tb[0], tb[1], tb[2], A[3], a.pcb);
-  BCFD_LAUNCHED();
-  TRY_R(solve_zero_bc_dev(hb, a.pcb, a.y, tol, itmax, true));
-  k_div_adj<<<grid_for(np, 256), 256, 0, stream()>>>(hb->d, c.deltat, a.y, tb[0], tb[1], tb[2]);
-  BCFD_LAUNCHED();
-  TRY_R(launch_vbc_adj(hb, c.deltat, c.uc, tb, s, a.ucl));
-  if (body) {
-    const AdjPtrs vin{{A[3], A[4], A[5], A[6]}, {A[3], A[4], A[5], A[6]}};
-    TRY_R(launch_forcing_adjoint(hb, 0, 1, vin, a.fc));  // velocityForcing1, in place on ut
-    const int64_t ni = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-    k_solid_adj<<<grid_for(ni, 256), 256, 0, stream()>>>(hb->d, A[4], A[5], A[6], A[3]);
-    BCFD_LAUNCHED();
-  }
-  TRY_R(launch_vbc_adj(hb, c.deltat, c.uc, tb, s, a.ucl));
-  const double* sb[3] = {tb[0], tb[1], tb[2]};
-  double* ab[4] = {A[0], A[1], A[2], A[3]};
-  TRY_R(launch_momentum_adjoint(hb, c.deltat, c.re, sb, ab, a.foot));
-  const int64_t ni = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-  k_zero_fluid<<<grid_for(ni, 256), 256, 0, stream()>>>(hb->d, tb[0], tb[1], tb[2]);
+// positions a coupling map overwrites, per interface and component: the fine
+// block's face-fill targets and the coarse block's restriction targets
+struct IfaceMasks {
+  HostInterface* it = nullptr;
+  AdjBlock* a = nullptr;   // coarse
+  AdjBlock* b = nullptr;   // fine
+  double* face[4] = {nullptr, nullptr, nullptr, nullptr};
+  double* restr[4] = {nullptr, nullptr, nullptr, nullptr};
+};
+
+// f = P c (face fill into the fine block) transposed: c_bar += P^T f_bar on
+// the written positions, then f_bar = 0 there
+int face_fill_adj(IfaceMasks& m, int comp, double* fine_bar, double* coarse_bar) {
+  TRY_R(coupling_apply(m.it, comp, 1, fine_bar, coarse_bar));
+  k_zero_masked<<<grid_for(m.b->np, 256), 256, 0, stream()>>>(m.b->np, fine_bar, m.face[comp]);
   BCFD_LAUNCHED();
   return 0;
+}
+
+// c = R f (restriction into the coarse block) transposed
+int restrict_adj(IfaceMasks& m, int comp, double* coarse_bar, double* fine_bar) {
+  TRY_R(coupling_apply(m.it, comp, 3, coarse_bar, fine_bar));
+  k_zero_masked<<<grid_for(m.a->np, 256), 256, 0, stream()>>>(m.a->np, coarse_bar, m.restr[comp]);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+// solve transposed: y = A_ff^{-T} pcb, bb += y, pcb -> adjoint of the boundary data
+int solve_adj(AdjBlock& a, double tol, int64_t itmax) {
+  TRY_R(solve_zero_bc_dev(a.hb, a.pcb, a.y, tol, itmax, true));
+  k_axpy<<<grid_for(a.np, 256), 256, 0, stream()>>>(a.y, 1.0, a.bb, a.np);
+  BCFD_LAUNCHED();
+  k_dirichlet_adj<<<grid_for(a.np, 256), 256, 0, stream()>>>(a.hb->d, a.y, a.pcb);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+// One whole step transposed, in place on every block's adjoint arrays (each
+// block holds the step's input state).  The forward order is that of the
+// native step (app/main.F90:129-265 with poissonSolver, PcorVcor.F90:22-220):
+//   predictor (all blocks); per block: velocityBC (coarse), solidCellBC and
+//   velocityForcing1 (body), velocityBC (coarse);
+//   Poisson: fineUpdate_newv_bd (ut faces), coarseUpdate_newv, div, solve
+//   fine, coarseUpdate_pc, solve coarse, fineUpdate_pc_bd, solve fine,
+//   coarseUpdate_pc, correctPressure, correctVelocity, velocityBC (block 1),
+//   ut -> u, fineUpdate_bd_mv (u, v, w, p faces), coarseUpdate (u, v, w, p);
+//   pressureForcing1; velocityForcingField, pressureForcingField (body).
+int adjoint_step(std::vector<AdjBlock>& B, std::vector<IfaceMasks>& M, const bcfd_step_config& c, double tol,
+                 int64_t itmax) {
+  std::vector<AdjBlock*> fine, first;
+  for (AdjBlock& a : B) (a.hb->is_coarse ? first : fine).push_back(&a);
+  auto tb = [](AdjBlock& a) {
+    return std::array<double*, 3>{a.F(4), a.F(5), a.F(6)};
+  };
+  // pressureForcingField, velocityForcingField, pressureForcing1
+  for (AdjBlock& a : B) {
+    if (!a.body) continue;
+    const AdjPtrs pin{{a.F(3), a.F(1), a.F(2), a.F(3)}, {a.F(3), a.F(1), a.F(2), a.F(3)}};
+    const AdjPtrs field{{a.F(3), a.F(0), a.F(1), a.F(2)}, {a.F(3), a.F(4), a.F(5), a.F(6)}};
+    TRY_R(launch_forcing_adjoint(a.hb, 1, 0, pin, a.fc));
+    TRY_R(launch_forcing_adjoint(a.hb, 1, 1, field, a.fc));
+    TRY_R(launch_forcing_adjoint(a.hb, 0, 0, pin, a.fc));
+  }
+  // coarseUpdate (u,v,w,p) and fineUpdate_bd_mv (u,v,w,p), reversed
+  const int f_of[4] = {3, 0, 1, 2};  // comp 0 p, 1 u, 2 v, 3 w -> state field
+  for (auto m = M.rbegin(); m != M.rend(); ++m)
+    for (int comp = 3; comp >= 0; --comp) TRY_R(restrict_adj(*m, comp, m->a->F(f_of[comp]), m->b->F(f_of[comp])));
+  for (auto m = M.rbegin(); m != M.rend(); ++m)
+    for (int comp = 3; comp >= 0; --comp) TRY_R(face_fill_adj(*m, comp, m->b->F(f_of[comp]), m->a->F(f_of[comp])));
+  // ut -> u, velocityBC of block 1, the corrections
+  for (AdjBlock& a : B) {
+    k_copy_adj<<<grid_for(a.np, 256), 256, 0, stream()>>>(a.np, a.F(0), a.F(1), a.F(2), a.F(4), a.F(5), a.F(6));
+    BCFD_LAUNCHED();
+  }
+  for (AdjBlock* a : first) {
+    auto t = tb(*a);
+    double* tt[3] = {t[0], t[1], t[2]};
+    TRY_R(launch_vbc_adj(a->hb, c.deltat, c.uc, tt, Fields4{a->F(0), a->F(1), a->F(2), a->F(3)}, a->ucl));
+  }
+  for (AdjBlock& a : B) {
+    k_correct_adj<<<grid_for(a.np, 256), 256, 0, stream()>>>(a.hb->d, c.deltat, a.F(4), a.F(5), a.F(6), a.F(3), a.pcb);
+    BCFD_LAUNCHED();
+    ACK(cudaMemsetAsync(a.bb, 0, a.np * sizeof(double), stream()));
+  }
+  // coarseUpdate_pc, solve fine, fineUpdate_pc_bd, solve coarse, coarseUpdate_pc, solve fine
+  for (auto m = M.rbegin(); m != M.rend(); ++m) TRY_R(restrict_adj(*m, 0, m->a->pcb, m->b->pcb));
+  for (AdjBlock* a : fine) TRY_R(solve_adj(*a, tol, itmax));
+  for (auto m = M.rbegin(); m != M.rend(); ++m) TRY_R(face_fill_adj(*m, 0, m->b->pcb, m->a->pcb));
+  for (AdjBlock* a : first) TRY_R(solve_adj(*a, tol, itmax));
+  for (auto m = M.rbegin(); m != M.rend(); ++m) TRY_R(restrict_adj(*m, 0, m->a->pcb, m->b->pcb));
+  for (AdjBlock* a : fine) TRY_R(solve_adj(*a, tol, itmax));
+  // div (with the solves' 1/deltat), coarseUpdate_newv, fineUpdate_newv_bd
+  for (AdjBlock& a : B) {
+    auto t = tb(a);
+    k_div_adj<<<grid_for(a.np, 256), 256, 0, stream()>>>(a.hb->d, c.deltat, a.bb, t[0], t[1], t[2]);
+    BCFD_LAUNCHED();
+  }
+  for (auto m = M.rbegin(); m != M.rend(); ++m)
+    for (int comp = 3; comp >= 1; --comp) TRY_R(restrict_adj(*m, comp, m->a->F(3 + comp), m->b->F(3 + comp)));
+  for (auto m = M.rbegin(); m != M.rend(); ++m)
+    for (int comp = 3; comp >= 1; --comp) TRY_R(face_fill_adj(*m, comp, m->b->F(3 + comp), m->a->F(3 + comp)));
+  // per block: velocityBC, [velocityForcing1, solidCellBC], velocityBC, reversed
+  for (AdjBlock& a : B) {
+    auto t = tb(a);
+    double* tt[3] = {t[0], t[1], t[2]};
+    const Fields4 s{a.F(0), a.F(1), a.F(2), a.F(3)};
+    if (a.hb->is_coarse) TRY_R(launch_vbc_adj(a.hb, c.deltat, c.uc, tt, s, a.ucl));
+    if (a.body) {
+      const AdjPtrs vin{{a.F(3), a.F(4), a.F(5), a.F(6)}, {a.F(3), a.F(4), a.F(5), a.F(6)}};
+      TRY_R(launch_forcing_adjoint(a.hb, 0, 1, vin, a.fc));
+      const int64_t ni = (int64_t)a.hb->d.d.nx * a.hb->d.d.ny * a.hb->d.d.nz;
+      k_solid_adj<<<grid_for(ni, 256), 256, 0, stream()>>>(a.hb->d, a.F(4), a.F(5), a.F(6), a.F(3));
+      BCFD_LAUNCHED();
+    }
+    if (a.hb->is_coarse) TRY_R(launch_vbc_adj(a.hb, c.deltat, c.uc, tt, s, a.ucl));
+  }
+  // the predictor
+  for (AdjBlock& a : B) {
+    auto t = tb(a);
+    const double* sb[3] = {t[0], t[1], t[2]};
+    double* ab[4] = {a.F(0), a.F(1), a.F(2), a.F(3)};
+    TRY_R(launch_momentum_adjoint(a.hb, c.deltat, c.re, sb, ab, a.foot));
+    const int64_t ni = (int64_t)a.hb->d.d.nx * a.hb->d.d.ny * a.hb->d.d.nz;
+    k_zero_fluid<<<grid_for(ni, 256), 256, 0, stream()>>>(a.hb->d, t[0], t[1], t[2]);
+    BCFD_LAUNCHED();
+  }
+  return 0;
+}
+
+// the registered blocks in registration order
+std::vector<std::pair<bcfd_handle, HostBlock*>> registered_blocks() {
+  std::vector<std::pair<bcfd_handle, HostBlock*>> v;
+  for (size_t q = 0; q < lib().blocks.size(); ++q)
+    if (lib().blocks[q]) v.push_back({(bcfd_handle)(q + 1), lib().blocks[q]});
+  return v;
 }
 
 struct DevMem {
@@ -376,23 +517,38 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   if (!hb) return BCFD_E_HANDLE;
   if (!cfg || n_steps < 1 || every < 1 || !wu || !wv || !ww || !wp || !J || !(adj_tol > 0.0) || adj_itmax < 1)
     return BCFD_E_ARG;
-  int live = 0;
-  for (HostBlock* b : lib().blocks) live += b != nullptr;
+  if (cfg->precision != 0) return BCFD_E_STATE;
+  // the blocks: block 1 with the domain BCs, the others fine blocks coupled
+  // to it by interfaces; no moving bodies, no thin-surface cells
+  auto all = registered_blocks();
+  if (all.empty() || !all.front().second->is_coarse) return BCFD_E_STATE;
+  for (auto& [g, b] : all) {
+    if (b->motion.on || !b->d.ca[0] || !b->d.Acx) return BCFD_E_STATE;
+    if (g != all.front().first && b->is_coarse) return BCFD_E_STATE;
+    if (b->has_body && b->d.ne > BCFD_STRESS_NOALLOC_MAX_ELEMS) return BCFD_E_CAPACITY;
+  }
+  std::vector<HostInterface*> ifs;
   for (HostInterface* it : lib().ifs)
-    if (it) return BCFD_E_STATE;
-  if (live != 1 || !hb->is_coarse || hb->motion.on || cfg->precision != 0) return BCFD_E_STATE;
-  if (!hb->d.ca[0] || !hb->d.Acx) return BCFD_E_STATE;
+    if (it) ifs.push_back(it);
+  if (all.size() > 1 && ifs.empty()) return BCFD_E_STATE;
   const bool body = hb->has_body && hb->d.ne > 0;
-  const bool use_stress = stress_seed && body;
   if (stress_seed && !body) return BCFD_E_STATE;
-  if (body && hb->d.ne > BCFD_STRESS_NOALLOC_MAX_ELEMS) return BCFD_E_CAPACITY;
+  const bool use_stress = stress_seed != nullptr;
   const bool grad = dj_duc || dj_dkin || gu || gv || gw || gp;
-  const Dims& d = hb->d.d;
-  const int64_t np = d.npts();
+  const int nb = (int)all.size();
+  int hidx = -1;
+  for (int q = 0; q < nb; ++q)
+    if (all[q].second == hb) hidx = q;
+  std::vector<int64_t> npb(nb), off(nb + 1, 0);
+  for (int q = 0; q < nb; ++q) {
+    npb[q] = all[q].second->d.d.npts();
+    off[q + 1] = off[q] + kStateFields * npb[q];
+  }
+  const size_t S = (size_t)off[nb];  // doubles of one state of all blocks
+  const int64_t np = hb->d.d.npts();
   const size_t fb = (size_t)np * sizeof(double);
   const int64_t K = std::min(every, n_steps);
-  const int64_t ncp = (n_steps + K - 1) / K;  // checkpoints at 0, K, 2K, ... < N
-  const size_t S = (size_t)kStateFields * np;
+  const int64_t ncp = (n_steps + K - 1) / K;
   DevMem mem;
   double* W = mem.get<double>(4 * np);
   double* cps = mem.get<double>((size_t)ncp * S);
@@ -402,6 +558,14 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   const double* wh[4] = {wu, wv, ww, wp};
   for (int q = 0; q < 4; ++q) ACK(h2d(W + q * np, wh[q], fb));
   ACK(cudaMemsetAsync(part, 0, kDotCtas * sizeof(double), stream()));
+  auto save_all = [&](double* slot) -> int {
+    for (int q = 0; q < nb; ++q) TRY_R(save_state(all[q].second, slot + off[q]));
+    return 0;
+  };
+  auto load_all = [&](const double* slot) -> int {
+    for (int q = 0; q < nb; ++q) TRY_R(load_state(all[q].second, slot + off[q]));
+    return 0;
+  };
   Lib& L = lib();
   const int64_t ita0 = L.ita;
   const double tot0 = L.totime;
@@ -410,14 +574,20 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   const Fields4 bx{hb->d.u, hb->d.v, hb->d.w, hb->d.p};
 
   // forward: the work arrays start equal to u, v, w; checkpoints; objective
-  ACK(cudaMemcpyAsync(hb->d.ut, hb->d.u, fb, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(hb->d.vt, hb->d.v, fb, cudaMemcpyDeviceToDevice, stream()));
-  ACK(cudaMemcpyAsync(hb->d.wt, hb->d.w, fb, cudaMemcpyDeviceToDevice, stream()));
-  TRY_R(save_state(hb, cps));
+  for (auto& [g, b] : all) {
+    const size_t bytes = (size_t)b->d.d.npts() * sizeof(double);
+    ACK(cudaMemcpyAsync(b->d.ut, b->d.u, bytes, cudaMemcpyDeviceToDevice, stream()));
+    ACK(cudaMemcpyAsync(b->d.vt, b->d.v, bytes, cudaMemcpyDeviceToDevice, stream()));
+    ACK(cudaMemcpyAsync(b->d.wt, b->d.w, bytes, cudaMemcpyDeviceToDevice, stream()));
+  }
+  TRY_R(save_all(cps));
   // the transpose assumes the tags the run starts with hold throughout
-  // (a stationary body: the per-step re-Search reproduces them)
-  std::vector<int8_t> tags0((size_t)np), tags1((size_t)np);
-  ACK(d2h(tags0.data(), hb->d.cell, (size_t)np));
+  // (stationary bodies: the per-step re-Search reproduces them)
+  std::vector<std::vector<int8_t>> tags0(nb);
+  for (int q = 0; q < nb; ++q) {
+    tags0[q].resize((size_t)npb[q]);
+    ACK(d2h(tags0[q].data(), all[q].second->d.cell, (size_t)npb[q]));
+  }
   double jstress = 0.0;
   for (int64_t n = 1; n <= n_steps; ++n) {
     TRY_R(run_one_step(c));
@@ -428,103 +598,145 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
       TRY_R(launch_stress_noalloc(hb, mu_f, rho_f, co));
       for (int t = 0; t < 4; ++t) jstress += stress_seed[t] * co[t];
     }
-    if (n % K == 0 && n < n_steps) TRY_R(save_state(hb, cps + (size_t)(n / K) * S));
+    if (n % K == 0 && n < n_steps) TRY_R(save_all(cps + (size_t)(n / K) * S));
   }
-  TRY_R(save_state(hb, fin));
+  TRY_R(save_all(fin));
   std::vector<double> ph(kDotCtas);
   ACK(d2h(ph.data(), part, kDotCtas * sizeof(double)));
   double jsum = 0.0;
   for (double v : ph) jsum += v;
   *J = (jsum + jstress) / (double)n_steps;
-  int err = take_block_error(hb);
-  ACK(d2h(tags1.data(), hb->d.cell, (size_t)np));
-  if (!err && tags0 != tags1) err = BCFD_E_STATE;
+  int err = 0;
+  for (int q = 0; q < nb && !err; ++q) {
+    err = take_block_error(all[q].second);
+    std::vector<int8_t> t1((size_t)npb[q]);
+    ACK(d2h(t1.data(), all[q].second->d.cell, (size_t)npb[q]));
+    if (!err && t1 != tags0[q]) err = BCFD_E_STATE;
+  }
   if (err || !grad) {
     L.ita = ita0 + n_steps;
     L.totime = tot0 + n_steps * cfg->deltat;
     return err;
   }
 
-  // objective weights per step: W plus the stress coefficients' weights
-  bool kin_stress = false;
-  double* stress_seed_dev = nullptr;
-  double* stress_scratch = nullptr;
+  // per-block adjoint buffers
+  std::vector<AdjBlock> AB(nb);
+  for (int q = 0; q < nb; ++q) {
+    AdjBlock& a = AB[q];
+    a.hb = all[q].second;
+    a.np = npb[q];
+    a.body = a.hb->has_body && a.hb->d.ne > 0;
+    a.A = mem.get<double>(kStateFields * a.np);
+    a.pcb = mem.get<double>(a.np);
+    a.y = mem.get<double>(a.np);
+    a.bb = mem.get<double>(a.np);
+    a.foot = mem.get<uint32_t>(16);
+    a.ucl = mem.get<double>((size_t)a.hb->d.d.ny * a.hb->d.d.nz);
+    const size_t ntask = a.body ? 6 * (size_t)a.hb->d.cap_ib : 1;
+    a.fc.tgt = mem.get<int64_t>(ntask);
+    a.fc.axis = mem.get<int>(ntask);
+    a.fc.pos = mem.get<int64_t>(8 * ntask);
+    a.fc.coef = mem.get<double>(8 * ntask);
+    a.fc.kc = mem.get<double>(8 * ntask);
+    a.fc.gk = mem.get<double>(8);
+    if (!a.A || !a.pcb || !a.y || !a.bb || !a.foot || !a.ucl || !a.fc.tgt || !a.fc.axis || !a.fc.pos ||
+        !a.fc.coef || !a.fc.kc || !a.fc.gk)
+      return BCFD_E_NOMEM;
+    ACK(cudaMemsetAsync(a.A, 0, kStateFields * a.np * sizeof(double), stream()));
+    ACK(cudaMemsetAsync(a.ucl, 0, (size_t)a.hb->d.d.ny * a.hb->d.d.nz * sizeof(double), stream()));
+    ACK(cudaMemsetAsync(a.fc.gk, 0, 8 * sizeof(double), stream()));
+  }
+  // coupling masks: the positions each map writes (the maps are partitions of
+  // unity, so a field of ones maps to ones exactly there)
+  std::vector<IfaceMasks> M;
+  for (HostInterface* it : ifs) {
+    IfaceMasks m;
+    m.it = it;
+    for (int q = 0; q < nb; ++q) {
+      if (all[q].first == it->a) m.a = &AB[q];
+      if (all[q].first == it->b) m.b = &AB[q];
+    }
+    if (!m.a || !m.b) return BCFD_E_STATE;
+    double* ones_a = mem.get<double>(m.a->np);
+    double* ones_b = mem.get<double>(m.b->np);
+    if (!ones_a || !ones_b) return BCFD_E_NOMEM;
+    k_fill<<<grid_for(m.a->np, 256), 256, 0, stream()>>>(m.a->np, ones_a, 1.0);
+    BCFD_LAUNCHED();
+    k_fill<<<grid_for(m.b->np, 256), 256, 0, stream()>>>(m.b->np, ones_b, 1.0);
+    BCFD_LAUNCHED();
+    for (int comp = 0; comp < 4; ++comp) {
+      m.face[comp] = mem.get<double>(m.b->np);
+      m.restr[comp] = mem.get<double>(m.a->np);
+      if (!m.face[comp] || !m.restr[comp]) return BCFD_E_NOMEM;
+      ACK(cudaMemsetAsync(m.face[comp], 0, m.b->np * sizeof(double), stream()));
+      ACK(cudaMemsetAsync(m.restr[comp], 0, m.a->np * sizeof(double), stream()));
+      TRY_R(coupling_apply(it, comp, 0, ones_a, m.face[comp]));
+      TRY_R(coupling_apply(it, comp, 2, ones_b, m.restr[comp]));
+    }
+    M.push_back(m);
+  }
+  // objective weights per step on block h: W plus the coefficients' weights
+  AdjBlock& ah = AB[hidx];
   if (use_stress) {
     double* sd = mem.get<double>(4);
     double* ss = mem.get<double>(8 + 64 * (size_t)hb->d.ne);
     if (!sd || !ss) return BCFD_E_NOMEM;
     ACK(h2d(sd, stress_seed, 4 * sizeof(double)));
     TRY_R(launch_stress_weights(hb, mu_f, rho_f, sd, W, ss));
-    kin_stress = true;
-    stress_seed_dev = sd;
-    stress_scratch = ss;
+    // the coefficients' own dependence on the kinematic scalars (the same at
+    // every step: (1/N) * N times)
+    TRY_R(launch_stress_kin(hb, mu_f, rho_f, sd, ah.fc.gk, ss));
   }
-  // reverse: recompute each segment from its checkpoint, then step back
   double* tape = mem.get<double>((size_t)K * S);
-  AdjBuffers a;
-  a.A = mem.get<double>(S);
-  a.pcb = mem.get<double>(np);
-  a.y = mem.get<double>(np);
-  a.ucl = mem.get<double>((size_t)d.ny * d.nz);
-  a.foot = mem.get<uint32_t>(16);
-  const size_t ntask = 6 * (size_t)hb->d.cap_ib;
-  a.fc.tgt = mem.get<int64_t>(body ? ntask : 1);
-  a.fc.axis = mem.get<int>(body ? ntask : 1);
-  a.fc.pos = mem.get<int64_t>(body ? 8 * ntask : 1);
-  a.fc.coef = mem.get<double>(body ? 8 * ntask : 1);
-  a.fc.kc = mem.get<double>(body ? 8 * ntask : 1);
-  a.fc.gk = mem.get<double>(8);
-  if (!tape || !a.A || !a.pcb || !a.y || !a.ucl || !a.foot || !a.fc.tgt || !a.fc.axis || !a.fc.pos || !a.fc.coef ||
-      !a.fc.kc || !a.fc.gk)
-    return BCFD_E_NOMEM;
-  ACK(cudaMemsetAsync(a.fc.gk, 0, 8 * sizeof(double), stream()));
-  // the coefficients' own dependence on the kinematic scalars (the same at
-  // every step: (1/N) * N times)
-  if (kin_stress) TRY_R(launch_stress_kin(hb, mu_f, rho_f, stress_seed_dev, a.fc.gk, stress_scratch));
-  ACK(cudaMemsetAsync(a.ucl, 0, (size_t)d.ny * d.nz * sizeof(double), stream()));
-  ACK(cudaMemsetAsync(a.A, 0, S * sizeof(double), stream()));
+  if (!tape) return BCFD_E_NOMEM;
   const double wn = 1.0 / (double)n_steps;
-  k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, a.A, 4 * np);
+  k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, ah.A, 4 * np);
   BCFD_LAUNCHED();
   for (int64_t m = ncp - 1; m >= 0; --m) {
     const int64_t n0 = m * K, n1 = std::min(n0 + K, n_steps);
     const double* cp = cps + (size_t)m * S;
     ACK(cudaMemcpyAsync(tape, cp, S * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
-    TRY_R(load_state(hb, cp));
+    TRY_R(load_all(cp));
     L.ita = ita0 + n0;
     L.totime = tot0 + n0 * cfg->deltat;
     for (int64_t n = n0 + 1; n < n1; ++n) {
       TRY_R(run_one_step(c));
-      TRY_R(save_state(hb, tape + (size_t)(n - n0) * S));
+      TRY_R(save_all(tape + (size_t)(n - n0) * S));
     }
     for (int64_t n = n1; n > n0; --n) {
-      TRY_R(load_state(hb, tape + (size_t)(n - 1 - n0) * S));
-      TRY_R(adjoint_step(hb, c, a, adj_tol, adj_itmax));
+      TRY_R(load_all(tape + (size_t)(n - 1 - n0) * S));
+      TRY_R(adjoint_step(AB, M, c, adj_tol, adj_itmax));
       if (n - 1 >= 1) {
-        k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, a.A, 4 * np);
+        k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, ah.A, 4 * np);
         BCFD_LAUNCHED();
       }
     }
   }
-  // leave the block at the forward run's final state
-  TRY_R(load_state(hb, fin));
+  // leave the blocks at the forward run's final state
+  TRY_R(load_all(fin));
   L.ita = ita0 + n_steps;
   L.totime = tot0 + n_steps * cfg->deltat;
   // the run started from ut = u, vt = v, wt = w: their adjoints add up
-  k_axpy<<<grid_for(3 * np, 256), 256, 0, stream()>>>(a.A + 4 * np, 1.0, a.A, 3 * np);
+  k_axpy<<<grid_for(3 * np, 256), 256, 0, stream()>>>(ah.A + 4 * np, 1.0, ah.A, 3 * np);
   BCFD_LAUNCHED();
   double* gh[4] = {gu, gv, gw, gp};
   for (int q = 0; q < 4; ++q)
-    if (gh[q]) ACK(cudaMemcpyAsync(gh[q], a.A + q * np, fb, cudaMemcpyDeviceToHost, stream()));
-  std::vector<double> ul((size_t)d.ny * d.nz);
-  ACK(d2h(ul.data(), a.ucl, ul.size() * sizeof(double)));
-  if (dj_dkin) ACK(d2h(dj_dkin, a.fc.gk, 8 * sizeof(double)));
-  if (dj_duc) {
-    double sum = 0.0;
-    for (double v : ul) sum += v;
-    *dj_duc = sum;
+    if (gh[q]) ACK(cudaMemcpyAsync(gh[q], ah.A + q * np, fb, cudaMemcpyDeviceToHost, stream()));
+  if (dj_dkin) ACK(d2h(dj_dkin, ah.fc.gk, 8 * sizeof(double)));
+  double duc = 0.0;
+  for (AdjBlock& a : AB) {
+    if (!a.hb->is_coarse) continue;
+    std::vector<double> ul((size_t)a.hb->d.d.ny * a.hb->d.d.nz);
+    ACK(d2h(ul.data(), a.ucl, ul.size() * sizeof(double)));
+    for (double v : ul) duc += v;
   }
-  return take_block_error(hb);
+  if (dj_duc) *dj_duc = duc;
+  ACK(cudaStreamSynchronize(stream()));
+  for (auto& [g, b] : all) {
+    const int e = take_block_error(b);
+    if (e) return e;
+  }
+  return 0;
 }
 
 }  // extern "C"

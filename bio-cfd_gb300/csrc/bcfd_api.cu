@@ -1156,7 +1156,7 @@ int bcfd_block_get_solve_launch(bcfd_handle h, int* out) {
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant) {
   LOCK();
   GETB(h);
-  if (inner_sweeps < 0 || inner_sweeps > 100000 || omega < 0.0 || omega >= 2.0 || variant < 0 || variant > 3)
+  if (inner_sweeps < 0 || inner_sweeps > 100000 || omega < 0.0 || omega >= 2.0 || variant < 0 || variant > 4)
     return BCFD_E_ARG;
   hb->dc_inner = (int)inner_sweeps;
   hb->dc_omega = omega;

@@ -44,6 +44,7 @@ struct HostBlock {
   double* coef_buf = nullptr;      // device Acx/Acy/Acz + ca/ck tables
   float* grid_f32 = nullptr;       // device dxa/dya/dza rounded to FP32
   float* coef_f32 = nullptr;       // device Acx/Acy/Acz rounded to FP32
+  float* pcf2 = nullptr;           // second FP32 correction buffer (both colours) of the temporal-blocked sweeps
   int surf_cap_e = 0, surf_cap_n = 0;
   // per-block barrier words for persistent kernels: [count, gen]
   unsigned* bar = nullptr;
@@ -158,6 +159,7 @@ int launch_max_div(const std::vector<HostBlock*>& hbs, bool tfield);
 int launch_copy_t_to_n(const std::vector<HostBlock*>& hbs);
 int launch_momentum(const std::vector<HostBlock*>& hbs, double dt, double re, bool fp32);
 int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double epsi, double res_tol);
+bool tb_solve_fits(HostBlock* hb);
 int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double div_tol);
 // res_tol > 0: stop on the FP64 residual dt*max|b/dt - A pc| <= res_tol
 int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol = 0.0);

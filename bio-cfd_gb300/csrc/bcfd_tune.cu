@@ -103,8 +103,9 @@ void apply(HostBlock* hb, const Shape& s, bool fp32) {
 int tune_block(HostBlock* hb, Tuned* out) {
   static const Shape c64[] = {{256, 0, 0}, {512, 0, 0}, {256, 0, 1}, {512, 0, 1}, {512, 1, 0}};
   // {256, 4, *} selects the 64-register instantiation of the FP32 solve
+  // {512, 0, 4}: the temporal-blocked sweeps (small blocks)
   static const Shape c32[] = {{128, 0, 1}, {256, 0, 1}, {128, 0, 3}, {256, 0, 3},
-                              {256, 2, 1}, {256, 1, 1}, {256, 4, 1}, {256, 4, 3}};
+                              {256, 2, 1}, {256, 1, 1}, {256, 4, 1}, {256, 4, 3}, {512, 0, 4}};
   Saved sv;
   TRY_R(save_state(hb, sv, false));
   const int t0 = hb->solve_threads, c0 = hb->solve_ctas_per_sm, s0 = hb->solve_sync, v0 = hb->dc_variant,
@@ -121,6 +122,7 @@ int tune_block(HostBlock* hb, Tuned* out) {
   best = 1e30f;
   for (const Shape& s : c32) {
     if (r) break;
+    if (s.sync == 4 && !tb_solve_fits(hb)) continue;
     apply(hb, s, true);
     float ms = 0;
     if ((r = time_trial(hb, true, 16, &ms))) break;

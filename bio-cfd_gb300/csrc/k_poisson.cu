@@ -604,6 +604,254 @@ __global__ void __launch_bounds__(kDcThreads, MINB) k_sor_dc(DevBlock B, DcArgs 
   sor_dc_body(B, a, gb, tm, (int)blockIdx.x);
 }
 
+// ---------------------------------------------------------------------------
+// Temporal-blocked FP32 sweeps (variant 4): one grid barrier per sweep pair
+// instead of two.  Each CTA copies the rows of its tile plus two halo rows on
+// each side in j and k (both colours of the correction e, the right-hand side
+// and the masks) into shared memory, runs the red half-sweep over the tile
+// grown by one row and the black half-sweep over the tile, and writes the
+// tile's rows to the other of two e buffers.  The halo's red values are
+// recomputed from the inputs the owning CTA uses, with the same operations,
+// so every cell gets exactly the values of the two-barrier sweep (bitwise);
+// the second buffer keeps a round's reads of the neighbours' rows from racing
+// with their writes.  Small blocks only: the halo'd tile has to fit in
+// shared memory (18 bytes per packed cell position).
+// ---------------------------------------------------------------------------
+constexpr int kTbThreads = 512;
+constexpr int kTbPad = 4;  // floats before and after each shared row (zero)
+
+struct TbSmem {
+  int rj, rk, pitch;  // rows along j and k incl. halo, row pitch in floats
+  float* e;           // [2 colours][rk][rj][pitch]
+  float* r;
+  uint8_t* m;
+  __device__ __forceinline__ int rows() const { return rj * rk; }
+  __device__ __forceinline__ int off(int c, int jj, int kk) const {
+    return (c * rows() + kk * rj + jj) * pitch + kTbPad;
+  }
+};
+
+__device__ __forceinline__ TbSmem tb_smem(float* base, const TileMap& tm, const Dims& d) {
+  TbSmem s;
+  s.rj = tm.tj + 4;
+  s.rk = tm.tk + 4;
+  s.pitch = d.NXH + 2 * kTbPad;
+  const int n = 2 * s.rj * s.rk * s.pitch;
+  s.e = base;
+  s.r = base + n;
+  s.m = reinterpret_cast<uint8_t*>(base + 2 * n);
+  return s;
+}
+
+// asynchronous global -> shared copies (cp.async): a thread issues all its
+// copies before waiting once, so the few CTAs of this variant keep many
+// loads in flight
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.commit_group;\n\tcp.async.wait_group 0;" ::: "memory");
+}
+
+// copy the halo'd rows of e (both colours; and of r and the masks when
+// `inputs`) from global memory; rows outside the arrays read as zero.  The
+// caller synchronises the CTA afterwards.
+__device__ __forceinline__ void tb_load(const DevBlock& B, const Tile& t, const TbSmem& s, const float* const E[2],
+                                        bool inputs) {
+  const Dims& d = B.d;
+  const int nq = d.NXH >> 2;
+  const int64_t sz = (int64_t)d.NXH * d.NY;
+  const int n = s.rows() * nq;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int a = q % nq, rr = q / nq;
+    const int jj = rr % s.rj, kk = rr / s.rj;
+    const int j = t.j0 - 2 + jj, k = t.k0 - 2 + kk;
+    const bool in = j >= 1 && j <= d.NY && k >= 1 && k <= d.NZ;
+    const int64_t pi = (int64_t)d.NXH * (j - 1) + sz * (k - 1) + 4 * a;
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      const int o = s.off(c, jj, kk) + 4 * a;
+      if (in) {
+        cp_async16(s.e + o, E[c] + pi);
+        if (inputs) {
+          cp_async16(s.r + o, B.rhsf[c] + pi);
+          cp_async4(s.m + o, B.upd[c] + pi);
+        }
+      } else {
+        *reinterpret_cast<float4*>(s.e + o) = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (inputs) {
+          *reinterpret_cast<float4*>(s.r + o) = make_float4(0.f, 0.f, 0.f, 0.f);
+          *reinterpret_cast<uchar4*>(s.m + o) = make_uchar4(0, 0, 0, 0);
+        }
+      }
+    }
+  }
+  cp_async_wait_all();
+}
+
+// zero the row pads once (the x-neighbour of a row's first/last run reads a
+// pad; those cells are never updated)
+__device__ __forceinline__ void tb_zero_pads(const TbSmem& s) {
+  const int n = 2 * s.rows();
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int c = q / s.rows(), rr = q % s.rows();
+    const int o = s.off(c, rr % s.rj, rr / s.rj);
+    for (int u = 1; u <= kTbPad; ++u) {
+      s.e[o - u] = 0.f;
+      s.e[o + (s.pitch - 2 * kTbPad) + u - 1] = 0.f;
+    }
+  }
+}
+
+// one half-sweep of colour C over the rows lo .. rj-1-lo (j) and lo .. rk-1-lo
+// (k) of the shared tile: the arithmetic of tile_half32
+template <int C>
+__device__ __forceinline__ void tb_half(const DevBlock& B, const Tile& t, const TbSmem& s, int lo, float omega) {
+  const Dims& d = B.d;
+  const int nq = d.NXH >> 2;
+  const int wj = s.rj - 2 * lo, wk = s.rk - 2 * lo;
+  const int n = wj * wk * nq;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int a = q % nq, rr = q / nq;
+    const int jj = lo + rr % wj, kk = lo + rr / wj;
+    const int j = t.j0 - 2 + jj, k = t.k0 - 2 + kk;
+    if (j < 2 || j > d.ny + 1 || k < 2 || k > d.nz + 1) continue;  // ghost rows hold no updated cell
+    const int oo = s.off(1 - C, jj, kk) + 4 * a, ow = s.off(C, jj, kk) + 4 * a;
+    const int sy = s.pitch, sz = s.rj * s.pitch;
+    const uchar4 m = *reinterpret_cast<const uchar4*>(s.m + ow);
+    const int par = ((1 + j + k) & 1) != C;
+    const float4 oc = *reinterpret_cast<const float4*>(s.e + oo);
+    const float4 os = *reinterpret_cast<const float4*>(s.e + oo - sy);
+    const float4 on = *reinterpret_cast<const float4*>(s.e + oo + sy);
+    const float4 ob = *reinterpret_cast<const float4*>(s.e + oo - sz);
+    const float4 ot = *reinterpret_cast<const float4*>(s.e + oo + sz);
+    const float4 r4 = *reinterpret_cast<const float4*>(s.r + ow);
+    const float4 e4 = *reinterpret_cast<const float4*>(s.e + ow);
+    const float ox = par ? s.e[oo + 4] : s.e[oo - 1];
+    const float4 cy = B.ayr[j - 2], cz = B.azr[k - 2];
+    const float ay1 = cy.x, ay2 = cy.y, ay3 = cy.z;
+    const float az1 = cz.x, az2 = cz.y, az3 = cz.z;
+    const float4* __restrict__ ar = B.axr + (int64_t)(3 * par) * nq + a;
+    const float4 c1 = ar[0], c2 = ar[nq], c3 = ar[2 * nq];
+    const float axv1[4] = {c1.x, c1.y, c1.z, c1.w}, axv2[4] = {c2.x, c2.y, c2.z, c2.w},
+                axv3[4] = {c3.x, c3.y, c3.z, c3.w};
+    const float oxs[6] = {par ? oc.x : ox, oc.x, oc.y, oc.z, oc.w, par ? ox : oc.w};
+    const float sv[4] = {os.x, os.y, os.z, os.w}, nv4[4] = {on.x, on.y, on.z, on.w};
+    const float bv[4] = {ob.x, ob.y, ob.z, ob.w}, tv[4] = {ot.x, ot.y, ot.z, ot.w};
+    const float rv[4] = {r4.x, r4.y, r4.z, r4.w};
+    float ev[4] = {e4.x, e4.y, e4.z, e4.w};
+    const unsigned char mv[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float left = par ? oxs[u + 1] : oxs[u];
+      const float right = par ? oxs[u + 2] : oxs[u + 1];
+      const float ax1 = axv1[u], ax2 = axv2[u], ax3 = axv3[u];
+      float sm = rv[u];
+      sm = __fmaf_rn(-ax1, left, sm);
+      sm = __fmaf_rn(-ax3, right, sm);
+      sm = __fmaf_rn(-ay1, sv[u], sm);
+      sm = __fmaf_rn(-ay3, nv4[u], sm);
+      sm = __fmaf_rn(-az1, bv[u], sm);
+      sm = __fmaf_rn(-az3, tv[u], sm);
+      const float nvv = __fmaf_rn(omega, __fdividef(sm, ax2 + ay2 + az2) - ev[u], ev[u]);
+      ev[u] = mv[u] ? nvv : ev[u];
+    }
+    *reinterpret_cast<float4*>(s.e + ow) = make_float4(ev[0], ev[1], ev[2], ev[3]);
+  }
+}
+
+// the tile's own rows (both colours) from shared memory to E
+__device__ __forceinline__ void tb_store(const DevBlock& B, const Tile& t, const TbSmem& s, float* const E[2]) {
+  const Dims& d = B.d;
+  const int nq = d.NXH >> 2;
+  const int64_t sz = (int64_t)d.NXH * d.NY;
+  const int n = t.nj * t.nk * nq;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int a = q % nq, rr = q / nq;
+    const int jj = 2 + rr % t.nj, kk = 2 + rr / t.nj;
+    const int j = t.j0 - 2 + jj, k = t.k0 - 2 + kk;
+    const int64_t pi = (int64_t)d.NXH * (j - 1) + sz * (k - 1) + 4 * a;
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+      *reinterpret_cast<float4*>(E[c] + pi) = *reinterpret_cast<const float4*>(s.e + s.off(c, jj, kk) + 4 * a);
+  }
+}
+
+// the tile's rows of E copied to the canonical buffer (an odd sweep count
+// leaves the correction in the second buffer)
+__device__ __forceinline__ void tb_copy_back(const DevBlock& B, const Tile& t, const float* const E2[2]) {
+  const Dims& d = B.d;
+  const int nq = d.NXH >> 2;
+  const int64_t sz = (int64_t)d.NXH * d.NY;
+  const int n = t.nj * t.nk * nq;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int a = q % nq, rr = q / nq;
+    const int64_t pi = (int64_t)d.NXH * (t.j0 + rr % t.nj - 1) + sz * (t.k0 + rr / t.nj - 1) + 4 * a;
+#pragma unroll
+    for (int c = 0; c < 2; ++c)
+      *reinterpret_cast<float4*>(B.pcf[c] + pi) = *reinterpret_cast<const float4*>(E2[c] + pi);
+  }
+}
+
+__global__ void __launch_bounds__(kTbThreads, 1) k_sor_tb(DevBlock B, DcArgs a, GridBar gb, TileMap tm, float* e2) {
+  extern __shared__ float4 tb_raw[];
+  __shared__ double sh[32];
+  const int cta = (int)blockIdx.x;
+  const Tile t = my_tile(B.d, tm, cta);
+  const TbSmem s = tb_smem(reinterpret_cast<float*>(tb_raw), tm, B.d);
+  const int64_t np = B.d.npacked();
+  float* const E0[2] = {B.pcf[0], B.pcf[1]};
+  float* const E1[2] = {e2, e2 + np};
+  BlockStats* st = B.stats;
+  tb_zero_pads(s);
+  int64_t sweeps = 0;
+  double res = 0.0;
+  int outer = 0;
+  for (;; ++outer) {
+    double m = fmax(tile_residual64v<1>(B, t, a.inv_dt), tile_residual64v<0>(B, t, a.inv_dt));
+    m = block_max(m, sh);
+    if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[outer % 3], m);
+    if (!grid_sync(gb)) return;
+    res = take_slot(st, outer, cta);
+    if (a.dt * res <= a.div_tol || outer >= a.max_outer || !(res == res)) break;
+    int cur = 0;
+    for (int it = 0; it < a.inner; ++it) {
+      const float* const* src = cur ? E1 : E0;
+      const float* srcc[2] = {src[0], src[1]};
+      tb_load(B, t, s, srcc, it == 0);
+      __syncthreads();
+      tb_half<1>(B, t, s, 1, a.omega);
+      __syncthreads();
+      tb_half<0>(B, t, s, 2, a.omega);
+      __syncthreads();
+      tb_store(B, t, s, cur ? E0 : E1);
+      cur ^= 1;
+      if (!grid_sync(gb)) return;
+    }
+    sweeps += a.inner;
+    if (cur) {
+      const float* e1c[2] = {E1[0], E1[1]};
+      tb_copy_back(B, t, e1c);
+      __syncthreads();
+    }
+    tile_apply4<1>(B, t);
+    tile_apply4<0>(B, t);
+    if (!grid_sync(gb)) return;
+  }
+  if (cta == 0 && threadIdx.x == 0) {
+    log_solve(a.log, sweeps, outer + 1, B.cnt[C_FLUID], 1);
+    st->niter = st->niter + sweeps;
+    st->derr2 = a.dt * res;
+    st->pad[1] = a.dt * res;
+    if (!(res == res)) set_err(B.err, BCFD_E_NONFINITE);
+  }
+}
+
 // Several blocks' solves in one cooperative launch: member m owns CTAs
 // [cta0, cta0 + its tile count) and has its own barrier, tiles and slots.
 constexpr int kMaxSolveBatch = 16;
@@ -883,6 +1131,76 @@ int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_
   return launch_residual(hb, dt);
 }
 
+// Temporal-blocked solve: tiles of tj x tk rows with their two halo rows per
+// side in shared memory, one CTA of 512 threads per tile, all co-resident.
+static size_t tb_bytes(const Dims& d, int tj, int tk) {
+  return (size_t)(tj + 4) * (tk + 4) * (d.NXH + 2 * kTbPad) * 18;
+}
+
+// the smallest square-ish tiles (the most CTAs, for loads in flight) whose
+// count fits one CTA per SM and whose halo'd rows fit in shared memory; 0 when
+// the block is too large for this variant
+static int tb_tiles(HostBlock* hb, int* tj, int* tk) {
+  const Dims& d = hb->d.d;
+  int dev = lib().device, smem_max = 0, nsm = num_sms();
+  if (cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) return 0;
+  const size_t cap = (size_t)smem_max - 1024;  // static shared memory of the kernel
+  for (int s = 2; s <= 32; ++s) {
+    const int a = std::min(s, d.ny), b = std::min(s, d.nz);
+    const int n = ((d.ny + a - 1) / a) * ((d.nz + b - 1) / b);
+    if (tb_bytes(d, a, b) <= cap && n <= nsm) {
+      *tj = a;
+      *tk = b;
+      return 1;
+    }
+  }
+  return 0;
+}
+
+bool tb_solve_fits(HostBlock* hb) {
+  int a, b;
+  return tb_tiles(hb, &a, &b) != 0;
+}
+
+static int launch_sor_tb(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
+  DevBlock& B = hb->d;
+  const int64_t np = B.d.npacked();
+  if (!hb->pcf2) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, 2 * (size_t)np * sizeof(float)) != cudaSuccess) return BCFD_E_NOMEM;
+    hb->allocs.push_back(p);
+    hb->pcf2 = static_cast<float*>(p);
+    BCFD_CUDA(cudaMemsetAsync(hb->pcf2, 0, 2 * (size_t)np * sizeof(float), stream()));
+    lib().gen++;
+  }
+  int tj = 0, tk = 0;
+  if (!tb_tiles(hb, &tj, &tk)) return BCFD_E_STATE;
+  TileMap tm{tj, tk, (B.d.ny + tj - 1) / tj, (B.d.nz + tk - 1) / tk, hb->prog, 1};
+  TRY_R(reset_solve_state(hb, tm));
+  const size_t smem = tb_bytes(B.d, tj, tk);
+  BCFD_CUDA(cudaFuncSetAttribute((const void*)k_sor_tb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const unsigned grid = (unsigned)(tm.ntj * tm.ntk);
+  const int nmax = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
+  DcArgs a;
+  a.inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
+  double om = hb->dc_omega > 0 ? hb->dc_omega : 2.0 / (1.0 + std::sin(3.14159265358979323846 / nmax));
+  a.omega = (float)std::min(1.97, std::max(1.0, om));
+  a.max_outer = itmax / a.inner + 1;
+  a.dt = dt;
+  a.inv_dt = 1.0 / dt;
+  a.div_tol = div_tol;
+  a.log = prof_log();
+  GridBar gb = make_bar(B.err, grid);
+  gb.ctr = reinterpret_cast<unsigned long long*>(hb->bar);
+  float* e2 = hb->pcf2;
+  void* args[] = {(void*)&B, (void*)&a, (void*)&gb, (void*)&tm, (void*)&e2};
+  prof_mark(true);
+  BCFD_CUDA(launch_coop((const void*)k_sor_tb, grid, kTbThreads, args, smem));
+  prof_mark(false);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
 int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   DevBlock& B = hb->d;
   const int64_t np = B.d.npacked();
@@ -897,6 +1215,7 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
     return launch_residual(hb, dt);
   }
   for (int c = 0; c < 2; ++c) BCFD_CUDA(cudaMemsetAsync(B.pcf[c], 0, np * sizeof(float), stream()));
+  if (hb->dc_variant == 4 && tb_solve_fits(hb)) return launch_sor_tb(hb, itmax, dt, div_tol);
   const int threads = hb->dc_threads > 0 ? std::min(hb->dc_threads, kDcThreads) : kDcThreads;
   // variant 3: point-to-point tile sync; otherwise grid-wide phase barriers
   // four CTAs per SM asked for: the 64-register instantiation
@@ -1013,7 +1332,7 @@ int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, doub
   }
   const int threads = kDcThreads;
   for (HostBlock* hb : hbs) {
-    if (hb->dc_variant == 2 || hb->dc_variant == 3 || hb->dc_threads > 0 || hb->dc_ctas_per_sm > 0) continue;
+    if (hb->dc_variant >= 2 || hb->dc_threads > 0 || hb->dc_ctas_per_sm > 0) continue;
     for (int c = 0; c < 2; ++c)
       BCFD_CUDA(cudaMemsetAsync(hb->d.pcf[c], 0, hb->d.d.npacked() * sizeof(float), stream()));
   }
@@ -1028,7 +1347,7 @@ int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, doub
     a.inv_dt = 1.0 / dt;
     a.div_tol = div_tol;
     a.log = prof_log();
-    return hb->dc_variant == 2 || hb->dc_variant == 3 || hb->dc_threads > 0 || hb->dc_ctas_per_sm > 0;
+    return hb->dc_variant >= 2 || hb->dc_threads > 0 || hb->dc_ctas_per_sm > 0;
   };
   auto solo = [&](HostBlock* hb) -> int { return launch_sor_mixed(hb, itmax, dt, div_tol); };
   return launch_solve_set<DcArgs>(hbs, (const void*)k_sor_dc_set, threads, 1, make, solo);

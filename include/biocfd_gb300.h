@@ -297,7 +297,10 @@ int bcfd_block_get_divergence(bcfd_handle h, double* out);
  * their relaxation factor (0 selects the defaults) and the kernel variant
  * (0: the library's choice, 1: tiled cooperative with grid-wide phase
  * barriers, 2: cluster-resident when the block fits in one 16-CTA cluster,
- * else 1, 3: tiled cooperative with point-to-point neighbour sync) */
+ * else 1, 3: tiled cooperative with point-to-point neighbour sync, 4:
+ * temporal-blocked sweeps, one grid barrier per sweep pair, when the block's
+ * halo'd tiles fit in shared memory, else 1; 1, 3 and 4 give bitwise the
+ * same corrections) */
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant);
 /* launch shape of a block's tiled Poisson solves (the autotuner's knobs; no
  * effect on results): threads per CTA (0 = the default: 512 for the FP64

@@ -48,3 +48,21 @@ def test_mixed_cluster_variant_on_64_block():
     assert max(rc) <= TOL * (1 + 1e-9) and max(rg) <= TOL * (1 + 1e-9)
     for nm in ("u", "v", "w", "p"):
         assert rel_l2(fg[0][nm], fc[0][nm]) < FIELD_TOL
+
+
+@pytest.mark.parametrize("variant", [1, 3, 4])
+def test_mixed_reaches_tolerance_odd_block(variant):
+    # odd sizes: padded colour rows and ragged tiles in every solve variant
+    case = synth.uniform_block(n=(23, 17, 13), lengths=(3.0, 2.0, 2.0))
+    f1, r1 = _run(case, 1, 2, variant)
+    assert max(r1) <= TOL * (1 + 1e-9), r1
+    f2, r2 = _run(case, 2, 2)
+    for b1, b2 in zip(f1, f2):
+        # v and w are O(1e-3) noise here: measure every velocity component
+        # against the flow's scale |u|.  The pressure is not compared: on
+        # this body-free block it is small and the residual target does not
+        # bound its smooth, nearly singular mode (which the velocity
+        # correction, a gradient, hardly sees)
+        for nm in ("u", "v", "w"):
+            e = np.linalg.norm(b2[nm] - b1[nm]) / np.linalg.norm(b1["u"])
+            assert e < FIELD_TOL, (nm, e)

@@ -138,10 +138,12 @@ def test_steps_100_single_block_bitwise():
     compare_search(o, s, "100 steps")
 
 
-def test_steps_body_free_block():
+@pytest.mark.parametrize("n", [(24, 16, 16), (23, 17, 13), (5, 4, 3)])
+def test_steps_body_free_block(n):
     """A lone block with the domain BCs and no body (tagged all fluid and
-    counted): three drop-in steps bitwise against the oracle."""
-    case = synth.replace(synth.uniform_block(n=(24, 16, 16), lengths=(3.0, 2.0, 2.0)), n_steps=3, epsi=1e-8)
+    counted): three drop-in steps bitwise against the oracle, on even, odd
+    (padded colour rows, ragged tiles) and minimal block sizes."""
+    case = synth.replace(synth.uniform_block(n=n, lengths=(3.0, 2.0, 2.0)), n_steps=3, epsi=1e-8)
     o, s = _pair(case)
     for _ in range(3):
         o.step()

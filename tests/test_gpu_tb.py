@@ -25,9 +25,10 @@ def _pc(case, variant, pairs):
     return out
 
 
-@pytest.mark.parametrize("pairs", [7, 16])
-def test_tb_sweeps_bitwise_equal_to_tiled(pairs):
-    case = synth.small_two_block(n_steps=1)
+@pytest.mark.parametrize("pairs,odd", [(7, False), (16, False), (5, True)])
+def test_tb_sweeps_bitwise_equal_to_tiled(pairs, odd):
+    case = (synth.uniform_block(n=(23, 17, 13), lengths=(3.0, 2.0, 2.0)) if odd
+            else synth.small_two_block(n_steps=1))
     ref = _pc(case, 1, pairs)
     got = _pc(case, 4, pairs)
     for a, b in zip(ref, got):

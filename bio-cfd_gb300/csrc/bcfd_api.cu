@@ -730,6 +730,28 @@ int bcfd_block_set_surface(bcfd_handle h, int64_t n_elems, int64_t n_nodes, cons
   hb->elem_host = ids;
   hb->has_body = n_elems > 0;
   BCFD_CUDA(cudaStreamSynchronize(stream()));
+  // findDistnode (src/Search.F90:21-47) on the nodes as given, with the node
+  // tags readSurfaceMeshGmsh derives from the elements (51/52 first, then 50):
+  // mk is the last surface-51 node whose |z| exceeds the running value,
+  // mkx1 / mkx2 those of |x| below / above theirs; the running values keep
+  // the signed coordinate, as the reference does
+  {
+    std::vector<int> nid((size_t)n_nodes, 50);
+    for (int64_t e = 0; e < n_elems; ++e)
+      if (surf_id[e] == 51 || surf_id[e] == 52)
+        for (const int64_t* p : {elp1, elp2, elp3}) nid[(size_t)p[e] - 1] = (int)surf_id[e];
+    for (int64_t e = 0; e < n_elems; ++e)
+      if (surf_id[e] == 50)
+        for (const int64_t* p : {elp1, elp2, elp3}) nid[(size_t)p[e] - 1] = 50;
+    double dist = 0.0, dist1 = 999999.0, dist2 = 0.0;
+    hb->mk = hb->mkx1 = hb->mkx2 = 0;
+    for (int64_t i = 0; i < n_nodes; ++i) {
+      if (nid[(size_t)i] != 51) continue;
+      if (std::fabs(znode1[i]) > dist) dist = znode1[i], hb->mk = i + 1;
+      if (std::fabs(xnode1[i]) < dist1) dist1 = xnode1[i], hb->mkx1 = i + 1;
+      if (std::fabs(xnode1[i]) > dist2) dist2 = xnode1[i], hb->mkx2 = i + 1;
+    }
+  }
   return bcfd_block_set_nodes(h, xnode1, ynode1, znode1);
 }
 

@@ -44,7 +44,8 @@ struct HostBlock {
   double* coef_buf = nullptr;      // device Acx/Acy/Acz + ca/ck tables
   float* grid_f32 = nullptr;       // device dxa/dya/dza rounded to FP32
   float* coef_f32 = nullptr;       // device Acx/Acy/Acz rounded to FP32
-  float* pcf2 = nullptr;           // second FP32 correction buffer (both colours) of the temporal-blocked sweeps
+  float* pcf2 = nullptr;
+  int64_t mk = 0, mkx1 = 0, mkx2 = 0;  // findDistnode's extreme surface nodes (1-based)           // second FP32 correction buffer (both colours) of the temporal-blocked sweeps
   int surf_cap_e = 0, surf_cap_n = 0;
   // per-block barrier words for persistent kernels: [count, gen]
   unsigned* bar = nullptr;

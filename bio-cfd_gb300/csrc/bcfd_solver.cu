@@ -538,6 +538,12 @@ int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64
     cudaFree(tmp);
     return r;
   }
+  if (s == "mk" || s == "mkx1" || s == "mkx2") {
+    if (n < 1) return BCFD_E_ARG;
+    *(int64_t*)out = s == "mk" ? hb->mk : s == "mkx1" ? hb->mkx1 : hb->mkx2;
+    if (written) *written = 1;
+    return 0;
+  }
   if (s == "xnode1") return dcopy(D.xnode1, D.nn);
   if (s == "ynode1") return dcopy(D.ynode1, D.nn);
   if (s == "znode1") return dcopy(D.znode1, D.nn);

@@ -48,6 +48,7 @@ def lib(checked: bool = True) -> C.CDLL:
             "orc_pressure_forcing_field": [_i64], "orc_velocity_forcing_ghost": [_i64],
             "orc_pressure_forcing_ghost": [_i64], "orc_compute_surface_norm": [_i64, _i64],
             "orc_node_ids_from_elements": [_i64],
+            "orc_find_dist_node": [_i64],
             "orc_shift_surface_nodes_initial": [_i64, _f64, _f64, _i64, _f64, _f64, _f64],
             "orc_compute_surface_variables": [_i64, _f64, _f64, _i64, _f64, _f64, _f64, _f64],
             "orc_tagging_th_core": [_i64], "orc_selective_retagging": [_i64],
@@ -145,6 +146,7 @@ class Oracle:
                     self.arr(g, "ynode")[:] = m.nodes[:, 1]
                     self.arr(g, "znode")[:] = m.nodes[:, 2]
                     L.orc_node_ids_from_elements(g)
+                    L.orc_find_dist_node(g)
                     for nm, v in (("a0", mo.a0_deg), ("bfreq", mo.bfreq), ("yamp", mo.yamp),
                                   ("xshift", mo.shift[0]), ("yshift", mo.shift[1]), ("zshift", mo.shift[2])):
                         self.setf(g, nm, v)

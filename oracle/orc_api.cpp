@@ -68,7 +68,7 @@ int64_t* is_of(Block& b, const std::string& n) {
   M(nx) M(ny) M(nz) M(nIterPcor) M(cintp) M(i_startSearch) M(i_endSearch) M(j_startSearch)
   M(j_endSearch) M(k_startSearch) M(k_endSearch) M(ibCellCount) M(solidCellCount)
   M(fluidCellCount) M(redCellCount) M(blackCellCount) M(TSCellCount) M(ibElems) M(ibNodes)
-  M(move_check) M(blk_mv_tag)
+  M(move_check) M(blk_mv_tag) M(mk) M(mkx1) M(mkx2)
 #undef M
   return nullptr;
 }
@@ -169,6 +169,7 @@ void orc_velocity_forcing_ghost(int64_t g) { velocity_forcing_ghost(blk_of(g)); 
 void orc_pressure_forcing_ghost(int64_t g) { pressure_forcing_ghost(blk_of(g)); }
 void orc_compute_surface_norm(int64_t g, int64_t inor) { compute_surface_norm(blk_of(g), inor); }
 void orc_node_ids_from_elements(int64_t g) { node_ids_from_elements(blk_of(g)); }
+void orc_find_dist_node(int64_t g) { find_dist_node(blk_of(g)); }
 void orc_shift_surface_nodes_initial(int64_t g, double aoa, double piv_pt, int64_t ita, double deltat,
                                      double dxmin, double totime) {
   shift_surface_nodes_initial(blk_of(g), aoa, piv_pt, ita, deltat, dxmin, totime);

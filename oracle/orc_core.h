@@ -119,6 +119,7 @@ struct Block {
           blackCellCount = 0, TSCellCount = 0;
   int64_t ibElems = 0, ibNodes = 0;
   int64_t move_check = 0, blk_mv_tag = 0;
+  int64_t mk = 0, mkx1 = 0, mkx2 = 0;  // findDistnode's extreme surface nodes
   // kinematics read by the forcing routines
   double xdot = 0, ydot = 0, yddot = 0;
   double thetaDot = 0, thetaDDot = 0, thetaDot1 = 0, thetaDDot1 = 0, thetaDot2 = 0,
@@ -216,6 +217,7 @@ void fine_update_mv(int64_t g);
 void stress_calculation(Block& b, double mu_f, double rho_f);
 // rigid-body motion (src/Search.F90:49-208, src/ReadInput.f90:403-420)
 void node_ids_from_elements(Block& b);
+void find_dist_node(Block& b);
 void shift_surface_nodes_initial(Block& b, double aoa, double piv_pt, int64_t ita, double deltat,
                                  double dxmin, double totime);
 void compute_surface_variables(Block& b, double phase_angle, double piv_pt, int64_t ita,

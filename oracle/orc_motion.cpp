@@ -30,6 +30,29 @@ void place(Block& b, int64_t i, double aoa1, double aoa2, double piv_pt, double&
 }
 }  // namespace
 
+// findDistnode (src/Search.F90:21-47): over the nodes of surface 51, mk is
+// the last node whose |z| exceeds the running value, mkx1 / mkx2 those of
+// |x| below / above theirs.  The running values take the signed
+// coordinate while the tests compare its magnitude, as the reference does.
+void find_dist_node(Block& b) {
+  double dist = 0.0, dist1 = 999999.0, dist2 = 0.0;
+  for (int64_t i = 1; i <= b.ibNodes; ++i) {
+    if (b.ibNodeId(i) != 51) continue;
+    if (std::fabs(b.znode(i)) > dist) {
+      dist = b.znode(i);
+      b.mk = i;
+    }
+    if (std::fabs(b.xnode(i)) < dist1) {
+      dist1 = b.xnode(i);
+      b.mkx1 = i;
+    }
+    if (std::fabs(b.xnode(i)) > dist2) {
+      dist2 = b.xnode(i);
+      b.mkx2 = i;
+    }
+  }
+}
+
 void node_ids_from_elements(Block& b) {
   b.ibNodeId.alloc(b.ibNodes);
   for (int64_t i = 1; i <= b.ibNodes; ++i) b.ibNodeId(i) = 50;

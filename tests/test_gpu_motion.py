@@ -35,6 +35,9 @@ def test_moving_plate_setup_and_steps():
     case = synth.moving_plate_single_block(n=32, n_steps=4)
     o, s = _pair(case)
     _nodes(o, s, "setup")
+    # findDistnode's extreme nodes (the block-move checks read them)
+    for nm in ("mk", "mkx1", "mkx2"):
+        assert int(s.read(s.handles[0], nm, 1, np.int64)[0]) == o.geti(1, nm) > 0, nm
     compare_search(o, s, "setup")
     for q in range(4):
         o.step()

@@ -72,3 +72,20 @@ def test_update_velocity_newv_noop_without_move():
     o.arr(g, "ut")[...] = 4
     o.L.orc_update_velocity_newv(g)
     assert np.all(o.arr(g, "ut") == 4)
+
+
+def test_find_dist_node_kat():
+    # test/test_search.f90:47-54: six surface-51 nodes with x = y = z =
+    # (0, -7, -4, 1, -10, 8) -> mk = 6 (the running value keeps the signed z)
+    o = Oracle()
+    g = o.L.orc_block_new(5, 5, 5)
+    o.L.orc_alloc_surface(g, 1, 6)  # 1 element, 6 nodes
+    vals = np.array([0.0, -7.0, -4.0, 1.0, -10.0, 8.0])
+    for nm in ("xnode", "ynode", "znode"):
+        o.arr(g, nm)[:] = vals
+    o.arr(g, "ibNodeId")[:] = 51
+    o.L.orc_find_dist_node(g)
+    assert o.geti(g, "mk") == 6
+    # the same rule for x: mkx1 follows |x| below the signed running value,
+    # mkx2 above it
+    assert o.geti(g, "mkx1") == 1 and o.geti(g, "mkx2") == 6

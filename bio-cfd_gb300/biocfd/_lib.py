@@ -105,6 +105,8 @@ _SIGS = {
     "bcfd_stress_calculation": [c_i64, c_double, c_double, P_d],
     "bcfd_stress_calculation_noalloc": [c_i64, c_double, c_double, P_d],
     "bcfd_run_steps": [C.POINTER(StepConfig), c_i64],
+    "bcfd_block_move_stage": [P_i64],
+    "bcfd_tagging_th_move": [c_i64],
     "bcfd_max_divergence": [c_i64, P_d],
 }
 

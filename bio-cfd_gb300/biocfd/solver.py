@@ -154,23 +154,36 @@ class Solver:
         for g, spec in zip(self.handles, self.case.blocks):
             if spec.has_body:
                 check(L.bcfd_pressure_forcing1(g), "pressure_forcing1")
-        # app/main.F90:169-176, 213-215: moving bodies
+        # app/main.F90:169-230: moving bodies, the fine-block moves, the
+        # surface normals, the re-tagging of moved blocks
         if c.motion is not None:
             ita, tt = self.time()
             for g, spec in zip(self.handles, self.case.blocks):
                 if spec.motion is not None:
                     mi = c.motion
+                    check(L.bcfd_block_set_flags(g, -1, 0), "set_flags")
                     check(L.bcfd_compute_surface_variables(g, mi.phase_deg * np.pi / 180.0, mi.piv_pt, ita, c.dt,
                                                            mi.dxmin, mi.freq, tt), "compute_surface_variables")
+            if c.interfaces:
+                moved = np.zeros(1, np.int64)
+                check(L.bcfd_block_move_stage(_pi(moved)), "block_move_stage")
+            for g, spec in zip(self.handles, self.case.blocks):
+                if spec.motion is not None:
                     check(L.bcfd_compute_surface_norm(g, spec.mesh.inor), "compute_surface_norm")
+            if c.interfaces:
+                for g in self.handles[1:]:
+                    check(L.bcfd_tagging_th_move(g), "tagging_th_move")
         for g, spec in zip(self.handles, self.case.blocks):
             if not spec.has_body:
                 continue
-            check(L.bcfd_block_set_flags(g, 0, 0), "set_flags")
+            # main.F90:238-249: blk_mv_tag clears after the re-tagging,
+            # move_check after the moved block's solid cells and ut = u
             check(L.bcfd_selective_retagging_th(g), "selective_retagging_th")
+            check(L.bcfd_block_set_flags(g, -1, 0), "set_flags")
             check(L.bcfd_cellcount_solid(g), "cellcount_solid")
             check(L.bcfd_solid_cell_bc_move(g), "solid_cell_bc_move")
             check(L.bcfd_update_velocity_newv(g), "update_velocity_newv")
+            check(L.bcfd_block_set_flags(g, 0, -1), "set_flags")
             check(L.bcfd_compute_norm_distance(g), "compute_norm_distance")
             check(L.bcfd_find_ts_cells(g), "find_ts_cells")
             check(L.bcfd_velocity_forcing_field(g), "velocity_forcing_field")

@@ -364,6 +364,19 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
     return case
 
 
+def moving_plate_block_move(n_steps: int = 3, seed: int = SEED) -> Case:
+    """A coarse 48x32x32 block over 1.5x1x1 (dx 1/32) with one fine block at
+    ratio 2 around a heaving, pitching, towed plate, sized so that the
+    reference's block-move margins (src/Search.F90:1013-1040: 4.5, 5 and 1.52
+    times 3 coarse cells in x, y and z) hold from the first step: the fine
+    block moves by whole cells every step."""
+    mo = Motion(a0_deg=10.0, bfreq=0.25, yamp=0.02)
+    mi = MotionInputs(aoa_deg=0.0, phase_deg=90.0, piv_pt=0.0, freq=0.25, dxmin=1.0 / 64)
+    return multi_block(coarse=(48, 32, 32), domain=(1.5, 1.0, 1.0),
+                       fine_boxes=(((0.25, 1.0), (0.25, 0.75), (0.25, 0.75)),), body=0, plate=True,
+                       plate_axes=(0.1, 0.075, 0.02), motion=mo, motion_inputs=mi, n_steps=n_steps, seed=seed)
+
+
 # the 12-block layout: a coarse 256x192x192 block over 8x6x6 (dx 1/32) with 11
 # fine blocks at ratio 2 in the sizes 160x96x96, 128x64x64, 96x64x64,
 # 64x48x48, 48^3, 32^3 and repeats of the last five (13.3M cells in all)

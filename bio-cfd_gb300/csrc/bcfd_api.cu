@@ -497,6 +497,19 @@ int block_sync_err(HostBlock* hb) {
 }
 
 }  // namespace
+
+// change_block_coords (src/Search.F90:1208-1264): the faces move by whole
+// cells, the staggered and centre coordinates follow, the spacings stay
+int shift_block_grid(HostBlock* hb, double cx, double cy, double cz) {
+  // the search's bound on |node - block centre| holds for the moved centre
+  // after growing by the shift (triangle inequality)
+  if (hb->node_rmax > 0.0) hb->node_rmax += std::sqrt(cx * cx + cy * cy + cz * cz);
+  for (double& x : hb->x1) x = x + cx;
+  for (double& y : hb->y1) y = y + cy;
+  for (double& z : hb->z1) z = z + cz;
+  derive_staggered(hb);
+  return upload_grids(hb);
+}
 }  // namespace bcfd
 
 using namespace bcfd;
@@ -897,8 +910,8 @@ int bcfd_block_set_kinematics(bcfd_handle h, const double* k) {
 int bcfd_block_set_flags(bcfd_handle h, int64_t move_check, int64_t blk_mv_tag) {
   LOCK();
   GETB(h);
-  hb->move_check = move_check;
-  hb->blk_mv_tag = blk_mv_tag;
+  if (move_check >= 0) hb->move_check = move_check;
+  if (blk_mv_tag >= 0) hb->blk_mv_tag = blk_mv_tag;
   return 0;
 }
 

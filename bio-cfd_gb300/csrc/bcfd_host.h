@@ -45,7 +45,13 @@ struct HostBlock {
   float* grid_f32 = nullptr;       // device dxa/dya/dza rounded to FP32
   float* coef_f32 = nullptr;       // device Acx/Acy/Acz rounded to FP32
   float* pcf2 = nullptr;
-  int64_t mk = 0, mkx1 = 0, mkx2 = 0;  // findDistnode's extreme surface nodes (1-based)           // second FP32 correction buffer (both colours) of the temporal-blocked sweeps
+  int64_t mk = 0, mkx1 = 0, mkx2 = 0;  // findDistnode's extreme surface nodes (1-based)
+  // fine-block moves (src/Search.F90:997-1370): the last move and the index
+  // ranges of the old (cpy) and new (cpy_mv) positions of the moved data,
+  // which keep their values when a search finds no index, as the reference's
+  double* mv_dum = nullptr;  // u, v, w, p before the move
+  int64_t move_amt[3] = {0, 0, 0};
+  int64_t cpy[6] = {0, 0, 0, 0, 0, 0}, cpy_mv[6] = {0, 0, 0, 0, 0, 0};           // second FP32 correction buffer (both colours) of the temporal-blocked sweeps
   int surf_cap_e = 0, surf_cap_n = 0;
   // per-block barrier words for persistent kernels: [count, gen]
   unsigned* bar = nullptr;
@@ -198,6 +204,11 @@ int launch_cellcount(HostBlock* hb, bool coarse);
 int launch_norm_distance(HostBlock* hb);
 int launch_find_ts(HostBlock* hb);
 int launch_fine_block_cell(HostBlock* a, HostInterface* it, bool first);
+// fine-block moves: grid shift (host grids, derived grids, upload), the
+// cell_n marks of the data the block keeps, the moved fields
+int shift_block_grid(HostBlock* hb, double cx, double cy, double cz);
+int launch_mark_cell_n(HostBlock* hb, const double box_new[6]);
+int launch_move_fields(HostBlock* hb, const double* dum);
 int launch_build_list(HostBlock* hb, int which, int* out_ijk, int64_t cap, int64_t* count_host);
 // k_forcing.cu
 int launch_forcing_velocity(HostBlock* hb, int mode);  // 0 forcing1, 1 field, 2 ghost

@@ -209,6 +209,143 @@ int poisson(const SolveCfg& c, int start, int finish, int step) {
 // get pressureForcing1 and the per-step re-Search of main.F90:232-263.  The
 // body is stationary: the kinematics / block-move stage of main.F90:169-230
 // leaves the geometry unchanged and is not run.
+// ---------------------------------------------------------------------------
+// Fine-block moves (app/main.F90:178-230 with src/Search.F90:916-1461): a
+// fine block whose moving surface comes within fixed margins of its
+// interface box shifts by whole cells, a multiple of the refinement factor.
+// The scalar decisions run on the host as the reference's do; the fields,
+// tags and lists move on the device.
+// ---------------------------------------------------------------------------
+int64_t round_move(int64_t m, int64_t factor) {
+  if (std::llabs(m) < factor) return m < 0 ? -factor : factor;
+  if (m < 0) return m + std::llabs(m) % factor;
+  return m - std::llabs(m) % factor;
+}
+
+// first 1-based index i in [from, n] with v(i) > s; `keep` when there is none
+int64_t first_above(const std::vector<double>& v, int64_t from, int64_t n, double s, int64_t keep) {
+  for (int64_t i = std::max<int64_t>(from, 1); i <= n; ++i)
+    if (v[(size_t)i - 1] > s) return i;
+  return keep;
+}
+
+// block_move_check, change_block_coords, change_block_coords_interfaces,
+// change_block_interface, fine_block_cell and cellCount_solid_coarse_mv
+int block_move_stage() {
+  HostBlock* c = get_block(1);
+  if (!c) return 0;
+  int64_t flag = 0;
+  struct Moved {
+    HostInterface* it;
+    HostBlock* fb;
+    double box_new[6];
+  };
+  std::vector<Moved> moved;
+  for (HostInterface* it : lib().ifs) {
+    if (!it) continue;
+    HostBlock* fb = get_block(it->b);
+    if (!fb || !fb->motion.on || fb->mk < 1 || fb->mkx1 < 1) continue;
+    BodyMotion& m = fb->motion;
+    const double mg1 = 3.0 * c->dx;  // cintp * block(1)%dx
+    const double marginx = 4.5 * mg1, marginy = 5 * mg1, marginz = 1.52 * mg1;
+    const int64_t factor = it->b_msh / it->a_msh;
+    double ymk = 0.0, xmk1 = 0.0;
+    BCFD_CUDA(d2h(&ymk, fb->d.ynode1 + (fb->mk - 1), sizeof(double)));
+    BCFD_CUDA(d2h(&xmk1, fb->d.xnode1 + (fb->mkx1 - 1), sizeof(double)));
+    const double yval_up = std::fmax(ymk, m.nxty_cent + 0.02), yval_dw = std::fmin(ymk, m.nxty_cent - 0.02);
+    const double piv_z = fb->d.piv_z;
+    double* box = it->box;  // xs, xe, ys, ye, zs, ze
+    int64_t* amt = fb->move_amt;
+    amt[0] = amt[1] = amt[2] = 0;
+    const bool ytrig = std::fabs(yval_dw - box[2]) <= marginy || std::fabs(yval_up - box[3]) <= marginy;
+    const bool trig = std::fabs(xmk1 - box[0]) <= marginx || std::fabs(piv_z - box[4]) <= marginz ||
+                      std::fabs(piv_z - box[5]) <= marginz || ytrig;
+    if (!trig) continue;
+    fb->move_check = 1;
+    fb->blk_mv_tag = 1;
+    flag = 1;
+    if (ytrig) {
+      amt[1] = round_move((int64_t)std::floor((m.nxty_cent - m.inity_cent) / fb->dy), factor);
+      m.inity_cent = m.nxty_cent;
+    }
+    if (std::fabs(xmk1 - box[0]) < marginx) {
+      amt[0] = round_move((int64_t)std::floor((m.nxtx_cent - m.initx_cent) / fb->dx) - factor, factor);
+      m.initx_cent = m.nxtx_cent;
+    }
+    if (std::fabs(piv_z - box[4]) < (0.500 - 0.410 - mg1) || std::fabs(piv_z - box[5]) < (0.600 - 0.500 - mg1)) {
+      amt[2] = round_move((int64_t)std::floor((m.nxtz_cent - m.initz_cent) / fb->dz), factor);
+      m.initz_cent = m.nxtz_cent;
+    }
+    const double ch[3] = {amt[0] * fb->dx, amt[1] * fb->dy, amt[2] * fb->dz};
+    Moved mv{it, fb, {0, 0, 0, 0, 0, 0}};
+    for (int a = 0; a < 3; ++a) {
+      mv.box_new[2 * a] = std::fmax(box[2 * a], box[2 * a] + ch[a]);
+      mv.box_new[2 * a + 1] = std::fmin(box[2 * a + 1], box[2 * a + 1] + ch[a]);
+      box[2 * a] = box[2 * a] + ch[a];
+      box[2 * a + 1] = box[2 * a + 1] + ch[a];
+    }
+    // the old indices whose centres lie in the overlap of the old and new boxes
+    const std::vector<double>* cen[3] = {&fb->xp, &fb->yp, &fb->zp};
+    const int64_t npa[3] = {fb->d.d.NX, fb->d.d.NY, fb->d.d.NZ};
+    for (int a = 0; a < 3; ++a) {
+      fb->cpy[2 * a] = first_above(*cen[a], 1, npa[a], mv.box_new[2 * a], fb->cpy[2 * a]);
+      fb->cpy[2 * a + 1] =
+          first_above(*cen[a], fb->cpy[2 * a], npa[a], mv.box_new[2 * a + 1], fb->cpy[2 * a + 1] + 1) - 1;
+    }
+    const size_t np = (size_t)fb->d.d.npts();
+    if (!fb->mv_dum) {
+      void* p = nullptr;
+      if (cudaMalloc(&p, 4 * np * sizeof(double)) != cudaSuccess) return BCFD_E_NOMEM;
+      fb->allocs.push_back(p);
+      fb->mv_dum = static_cast<double*>(p);
+      lib().gen++;
+    }
+    const double* src[4] = {fb->d.u, fb->d.v, fb->d.w, fb->d.p};
+    for (int q = 0; q < 4; ++q)
+      BCFD_CUDA(cudaMemcpyAsync(fb->mv_dum + q * np, src[q], np * sizeof(double), cudaMemcpyDeviceToDevice,
+                                stream()));
+    moved.push_back(mv);
+  }
+  if (!flag) return 0;
+  // change_block_coords
+  for (Moved& mv : moved)
+    TRY(shift_block_grid(mv.fb, mv.fb->move_amt[0] * mv.fb->dx, mv.fb->move_amt[1] * mv.fb->dy,
+                         mv.fb->move_amt[2] * mv.fb->dz));
+  // change_block_coords_interfaces: cell_n, the new index ranges, the fields
+  for (Moved& mv : moved) {
+    HostBlock* fb = mv.fb;
+    TRY(launch_mark_cell_n(fb, mv.box_new));
+    const std::vector<double>* cen[3] = {&fb->xp, &fb->yp, &fb->zp};
+    const int64_t npa[3] = {fb->d.d.NX, fb->d.d.NY, fb->d.d.NZ};
+    for (int a = 0; a < 3; ++a) {
+      fb->cpy_mv[2 * a] = first_above(*cen[a], 1, npa[a], mv.box_new[2 * a], fb->cpy_mv[2 * a]);
+      fb->cpy_mv[2 * a + 1] =
+          first_above(*cen[a], fb->cpy_mv[2 * a], npa[a], mv.box_new[2 * a + 1], fb->cpy_mv[2 * a + 1] + 1) - 1;
+    }
+    TRY(launch_move_fields(fb, fb->mv_dum));
+  }
+  // change_block_interface: the coarse indices of the tables shift by the
+  // move in coarse cells
+  for (Moved& mv : moved) {
+    HostInterface* it = mv.it;
+    const int64_t factor = it->b_msh / it->a_msh;
+    for (int t = 0; t < 12; ++t) {
+      const int64_t inc = mv.fb->move_amt[t % 3] / factor;
+      for (int64_t q = 0; q < it->counter[t]; ++q) it->tab[t][(size_t)(3 * q)] += inc;
+    }
+    HostBlock* A = get_block(it->a);
+    if (!A || !iface_in_bounds(it, A, mv.fb)) return BCFD_E_STATE;  // moved out of the coarse block
+    TRY(upload_iface(it));
+  }
+  // fine_block_cell and cellCount_solid_coarse_mv (the coarse tags are the
+  // same as before when nothing moved, so both run only after a move)
+  TRY(launch_fine_block_cell(c, nullptr, true));
+  for (HostInterface* it : lib().ifs)
+    if (it && it->a == 1) TRY(launch_fine_block_cell(c, it, false));
+  TRY(launch_cellcount(c, true));
+  return 0;
+}
+
 bool any_motion() {
   for (HostBlock* hb : lib().blocks)
     if (hb && hb->motion.on) return true;
@@ -240,16 +377,36 @@ int step_once(const bcfd_step_config& cfg) {
   // moving bodies (app/main.F90:169-176, 213-215): kinematics and node
   // positions, then the surface normals of the moved nodes.  The fine blocks
   // do not move (block_move_check's margins must hold for the motion).
+  bool moving = false;
   for (auto& [g, hb] : all)
     if (hb->motion.on) {
       hb->blk_mv_tag = 0;
       TRY(compute_surface_variables(hb, L.phase_angle, L.piv_pt, L.ita, cfg.deltat, L.dxmin, L.freq, L.totime));
-      TRY(launch_surface_norm(hb, L.inor));
+      moving = true;
+    }
+  // the fine-block moves (main.F90:178-211), then the normals, then the
+  // re-tagging of the moved blocks (tagging_th_move, :226-230)
+  bool ifaces = false;
+  for (HostInterface* it : L.ifs) ifaces |= it != nullptr;
+  if (moving && ifaces) TRY(block_move_stage());
+  for (auto& [g, hb] : all)
+    if (hb->motion.on) TRY(launch_surface_norm(hb, L.inor));
+  if (moving && ifaces)
+    for (auto& [g, hb] : all) {
+      if (g == 1 || hb->move_check != 1) continue;
+      TRY(launch_tagging(hb));
+      for (HostInterface* it : L.ifs)
+        if (it && it->b == g) {
+          TRY(launch_fine_update_mv(it));
+          TRY(fine_update_bd_mv(it));
+        }
     }
   for (auto& [g, hb] : all) {
     if (!hb->has_body) continue;
+    // app/main.F90:238-239: a block that moved this step was re-tagged whole
+    // (blk_mv_tag = 1 skips the selective pass), then the tag is cleared
+    if (hb->blk_mv_tag == 0) TRY(launch_retagging(hb));
     hb->blk_mv_tag = 0;
-    TRY(launch_retagging(hb));
     TRY(launch_cellcount(hb, false));
     if (hb->move_check == 1) {
       TRY(launch_solid_bc(hb, true));
@@ -475,6 +632,32 @@ int bcfd_poisson_solver(int64_t pc_ita_max, double epsi, int64_t ita, double del
       if (total_time) *total_time = totime + *total_time;
     }
   return err;
+}
+
+int bcfd_block_move_stage(int64_t* moved) {
+  LOCK();
+  std::vector<int64_t> before;
+  for (HostBlock* hb : lib().blocks) before.push_back(hb ? hb->move_check : 0);
+  TRY(block_move_stage());
+  int64_t any = 0;
+  for (size_t q = 0; q < lib().blocks.size(); ++q)
+    if (lib().blocks[q] && lib().blocks[q]->move_check == 1 && before[q] != 1) any = 1;
+  if (moved) *moved = any;
+  return 0;
+}
+
+int bcfd_tagging_th_move(bcfd_handle h) {
+  LOCK();
+  HostBlock* hb = get_block(h);
+  if (!hb) return BCFD_E_HANDLE;
+  if (hb->move_check != 1) return 0;
+  TRY(launch_tagging(hb));
+  for (HostInterface* it : lib().ifs)
+    if (it && it->b == h) {
+      TRY(launch_fine_update_mv(it));
+      TRY(fine_update_bd_mv(it));
+    }
+  return 0;
 }
 
 int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps) {

@@ -94,6 +94,73 @@ int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_
   return place_nodes(hb, aoa1, piv_pt, m.xshift, m.yshift, 0.0, m.zshift, 0.0, 0);
 }
 
+namespace {
+
+// change_block_coords_interfaces (src/Search.F90:1269-1370), device part:
+// cell_n = 1 where the moved block keeps old data (centres strictly inside
+// the overlap of the old and new boxes, one cell in from its faces)
+__global__ void k_mark_cell_n(DevBlock B, double xs, double xe, double ys, double ye, double zs, double ze,
+                              double dx, double dy, double dz) {
+  const Dims& d = B.d;
+  const int64_t n = d.npts();
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 1 + (int)(t % d.NX);
+    const int64_t r = t / d.NX;
+    const int j = 1 + (int)(r % d.NY), k = 1 + (int)(r / d.NY);
+    const double x = B.xp[i - 1], y = B.yp[j - 1], z = B.zp[k - 1];
+    B.cell_n[t] = (x > xs + dx && x < xe - dx && z > zs + dz && z < ze - dz && y > ys + dy && y < ye - dy) ? 1 : 0;
+  }
+}
+
+// the moved fields: u,v,w,p at the new indices [cpy_mv] from the old indices
+// [cpy] (zero elsewhere), one thread per target point
+__global__ void k_move_fields(DevBlock B, const double* dum, int64_t x0, int64_t y0, int64_t z0, int64_t nx,
+                              int64_t ny, int64_t nz, int64_t ox, int64_t oy, int64_t oz) {
+  const Dims& d = B.d;
+  const int64_t np = d.npts(), n = nx * ny * nz;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = t % nx, r = t / nx;
+    const int64_t b = r % ny, c = r / ny;
+    const int64_t dst = d.idx((int)(x0 + a), (int)(y0 + b), (int)(z0 + c));
+    const int64_t src = d.idx((int)(ox + a), (int)(oy + b), (int)(oz + c));
+    B.u[dst] = dum[src];
+    B.v[dst] = dum[np + src];
+    B.w[dst] = dum[2 * np + src];
+    B.p[dst] = dum[3 * np + src];
+  }
+}
+
+}  // namespace
+
+int launch_mark_cell_n(HostBlock* hb, const double box_new[6]) {
+  k_mark_cell_n<<<grid_for(hb->d.d.npts(), 256), 256, 0, stream()>>>(hb->d, box_new[0], box_new[1], box_new[2],
+                                                                        box_new[3], box_new[4], box_new[5], hb->dx,
+                                                                        hb->dy, hb->dz);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+// u,v,w,p = 0, then the kept data at its new indices; the index ranges must
+// lie inside the block (the reference would read outside otherwise)
+int launch_move_fields(HostBlock* hb, const double* dum) {
+  const Dims& d = hb->d.d;
+  const size_t b = (size_t)d.npts() * sizeof(double);
+  for (double* f : {hb->d.u, hb->d.v, hb->d.w, hb->d.p}) BCFD_CUDA(cudaMemsetAsync(f, 0, b, stream()));
+  const int64_t* c = hb->cpy;
+  const int64_t* m = hb->cpy_mv;
+  const int64_t nx = m[1] - m[0] + 1, ny = m[3] - m[2] + 1, nz = m[5] - m[4] + 1;
+  if (nx <= 0 || ny <= 0 || nz <= 0) return 0;
+  const int64_t hi[3] = {d.NX, d.NY, d.NZ};
+  for (int a = 0; a < 3; ++a) {
+    const int64_t n = a == 0 ? nx : a == 1 ? ny : nz;
+    if (m[2 * a] < 1 || m[2 * a] + n - 1 > hi[a] || c[2 * a] < 1 || c[2 * a] + n - 1 > hi[a]) return BCFD_E_STATE;
+  }
+  k_move_fields<<<grid_for(nx * ny * nz, 256), 256, 0, stream()>>>(hb->d, dum, m[0], m[2], m[4], nx, ny, nz, c[0],
+                                                                    c[2], c[4]);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
 int compute_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, int64_t ita, double deltat,
                               double dxmin, double freq, double totime) {
   BodyMotion& m = hb->motion;

@@ -85,7 +85,7 @@ int bcfd_block_set_nodes(bcfd_handle h, const double* xnode1, const double* ynod
  * {xdot, ydot, yddot, thetaDot1, thetaDDot1, thetaDot2, thetaDDot2, alphaDot,
  *  piv_x, piv_y, piv_z} */
 int bcfd_block_set_kinematics(bcfd_handle h, const double* kin);
-/* Block_t move_check / blk_mv_tag */
+/* Block_t move_check / blk_mv_tag (a negative value leaves that flag as it is) */
 int bcfd_block_set_flags(bcfd_handle h, int64_t move_check, int64_t blk_mv_tag);
 /* fields (nx+2,ny+2,nz+2); any pointer may be NULL */
 int bcfd_block_upload_fields(bcfd_handle h, const double* u, const double* v, const double* w,
@@ -262,6 +262,16 @@ typedef struct bcfd_step_config {
  * per-block roles set by bcfd_block_set_role (domain BCs / immersed body). */
 int bcfd_block_set_role(bcfd_handle h, int is_coarse, int has_body);
 int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps);
+/* the fine-block moves of app/main.F90:178-211 after computeSurfaceVariables:
+ * block_move_check, change_block_coords, change_block_coords_interfaces,
+ * change_block_interface (src/Search.F90:997-1461), then fine_block_cell and
+ * cellCount_solid_coarse_mv (:863-995) when a block moved; *moved = 1 then.
+ * Only blocks with body motion are checked.  BCFD_E_STATE when a move would
+ * take a fine block's coupling stencils outside the coarse block. */
+int bcfd_block_move_stage(int64_t* moved);
+/* tagging_th_move (src/Search.F90:415-432): a block that moved is re-tagged
+ * and refilled from the coarse block (fineUpdate_mv, fineUpdate_bd_mv) */
+int bcfd_tagging_th_move(bcfd_handle h);
 /* Discrete adjoint of n_steps whole time steps (no counterpart in the
  * reference).  Scope: one registered block with the domain BCs, no
  * interfaces, FP64 drop-in steps (cfg->precision 0), with or without a

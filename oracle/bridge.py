@@ -49,6 +49,8 @@ def lib(checked: bool = True) -> C.CDLL:
             "orc_pressure_forcing_ghost": [_i64], "orc_compute_surface_norm": [_i64, _i64],
             "orc_node_ids_from_elements": [_i64],
             "orc_find_dist_node": [_i64],
+            "orc_block_move_stage": [],
+            "orc_tagging_th_move": [_i64],
             "orc_shift_surface_nodes_initial": [_i64, _f64, _f64, _i64, _f64, _f64, _f64],
             "orc_compute_surface_variables": [_i64, _f64, _f64, _i64, _f64, _f64, _f64, _f64],
             "orc_tagging_th_core": [_i64], "orc_selective_retagging": [_i64],
@@ -211,19 +213,30 @@ class Oracle:
         for g, spec in enumerate(self.case.blocks, 1):
             if spec.has_body:
                 L.orc_pressure_forcing1(g)
-        # app/main.F90:169-176, 213-215: moving bodies
+        # app/main.F90:169-230: moving bodies, the fine-block moves, the
+        # surface normals, the re-tagging of moved blocks
         for g, spec in enumerate(self.case.blocks, 1):
             if spec.motion is not None:
                 mi = c.motion
                 self.seti(g, "blk_mv_tag", 0)
                 L.orc_compute_surface_variables(g, mi.phase_deg * np.pi / 180.0, mi.piv_pt, self.ita, c.dt,
                                                 mi.dxmin, mi.freq, self.totime)
+        moving = c.motion is not None and any(s.motion is not None for s in self.case.blocks)
+        if moving and c.interfaces:
+            L.orc_block_move_stage()
+        for g, spec in enumerate(self.case.blocks, 1):
+            if spec.motion is not None:
                 L.orc_compute_surface_norm(g, spec.mesh.inor)
+        if moving and c.interfaces:
+            for g in range(2, self.nblocks + 1):
+                L.orc_tagging_th_move(g)
         for g, spec in enumerate(self.case.blocks, 1):
             if not spec.has_body:
                 continue
-            self.seti(g, "blk_mv_tag", 0)
+            # app/main.F90:238-239: a block that moved this step was re-tagged
+            # whole by tagging_th_move (blk_mv_tag = 1 skips the selective pass)
             L.orc_selective_retagging(g)
+            self.seti(g, "blk_mv_tag", 0)
             L.orc_cellcount_solid(g)
             L.orc_solid_cell_bc_move(g)
             L.orc_update_velocity_newv(g)

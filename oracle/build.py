@@ -18,7 +18,7 @@ from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
 SOURCES = ["orc_navier.cpp", "orc_forcing.cpp", "orc_pcor.cpp", "orc_search.cpp",
-           "orc_interp.cpp", "orc_stress.cpp", "orc_motion.cpp", "orc_api.cpp"]
+           "orc_interp.cpp", "orc_stress.cpp", "orc_motion.cpp", "orc_blockmove.cpp", "orc_api.cpp"]
 
 
 def lib_path(checked: bool = True) -> Path:

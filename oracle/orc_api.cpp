@@ -68,7 +68,7 @@ int64_t* is_of(Block& b, const std::string& n) {
   M(nx) M(ny) M(nz) M(nIterPcor) M(cintp) M(i_startSearch) M(i_endSearch) M(j_startSearch)
   M(j_endSearch) M(k_startSearch) M(k_endSearch) M(ibCellCount) M(solidCellCount)
   M(fluidCellCount) M(redCellCount) M(blackCellCount) M(TSCellCount) M(ibElems) M(ibNodes)
-  M(move_check) M(blk_mv_tag) M(mk) M(mkx1) M(mkx2)
+  M(move_check) M(blk_mv_tag) M(mk) M(mkx1) M(mkx2) M(move_amtx) M(move_amty) M(move_amtz)
 #undef M
   return nullptr;
 }
@@ -170,6 +170,20 @@ void orc_pressure_forcing_ghost(int64_t g) { pressure_forcing_ghost(blk_of(g)); 
 void orc_compute_surface_norm(int64_t g, int64_t inor) { compute_surface_norm(blk_of(g), inor); }
 void orc_node_ids_from_elements(int64_t g) { node_ids_from_elements(blk_of(g)); }
 void orc_find_dist_node(int64_t g) { find_dist_node(blk_of(g)); }
+// the block-move stage of app/main.F90:178-230 after computeSurfaceVariables:
+// block_move_check, change_block_coords, change_block_coords_interfaces,
+// change_block_interface, fine_block_cell + cellCount_solid_coarse_mv (the
+// caller runs computeSurfaceNorm next, then orc_tagging_th_move)
+void orc_block_move_stage() {
+  int64_t flag = 0;
+  block_move_check(flag);
+  for (size_t g = 1; g < g_blocks.size(); ++g) change_block_coords(*g_blocks[g]);
+  for (Interface* it : g_interfaces) change_block_coords_interfaces(*it, blk_of(it->b_blk));
+  for (Interface* it : g_interfaces) change_block_interface(*it, blk_of(it->a_blk), blk_of(it->b_blk));
+  fine_block_cell();
+  cellcount_solid_coarse_mv(flag);
+}
+void orc_tagging_th_move(int64_t g) { tagging_th_move(blk_of(g), g); }
 void orc_shift_surface_nodes_initial(int64_t g, double aoa, double piv_pt, int64_t ita, double deltat,
                                      double dxmin, double totime) {
   shift_surface_nodes_initial(blk_of(g), aoa, piv_pt, ita, deltat, dxmin, totime);

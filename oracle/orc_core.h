@@ -120,6 +120,11 @@ struct Block {
   int64_t ibElems = 0, ibNodes = 0;
   int64_t move_check = 0, blk_mv_tag = 0;
   int64_t mk = 0, mkx1 = 0, mkx2 = 0;  // findDistnode's extreme surface nodes
+  // block move (src/Search.F90:997-1370)
+  int64_t move_amtx = 0, move_amty = 0, move_amtz = 0;
+  int64_t cpy_x_start = 0, cpy_x_end = 0, cpy_y_start = 0, cpy_y_end = 0, cpy_z_start = 0, cpy_z_end = 0;
+  int64_t cpy_x_start_mv = 0, cpy_x_end_mv = 0, cpy_y_start_mv = 0, cpy_y_end_mv = 0, cpy_z_start_mv = 0,
+          cpy_z_end_mv = 0;
   // kinematics read by the forcing routines
   double xdot = 0, ydot = 0, yddot = 0;
   double thetaDot = 0, thetaDDot = 0, thetaDot1 = 0, thetaDDot1 = 0, thetaDot2 = 0,
@@ -131,6 +136,7 @@ struct Block {
       ck_vu, ca_vw, ck_vw, ca_wu, ck_wu, ca_wv, ck_wv;
   A2<double> Acx, Acy, Acz;
   F3 b, u, ut, v, vt, w, wt, p, pc, pco;
+  F3 u_dum, v_dum, w_dum, p_dum;
   I3 cell, cell2, cell_n, cell_pr, nodeIdTag;
   I2 fluidIndexPtr, redCellIndexPtr, blackCellIndexPtr, TSIndexPtr, interceptedIndexPtr,
       solidIndexPtr;
@@ -161,6 +167,8 @@ struct Interface {
   I2 px, ux, vx, wx, py, uy, vy, wy, pz, uz, vz, wz;  // (3, n) tables
   double xintf_start = 0, xintf_end = 0, yintf_start = 0, yintf_end = 0, zintf_start = 0,
          zintf_end = 0;
+  double xintf_st_new = 0, xintf_en_new = 0, yintf_st_new = 0, yintf_en_new = 0, zintf_st_new = 0,
+         zintf_en_new = 0;
   int64_t a_blk = 1, b_blk = 2;
   int64_t a_msh = 1, b_msh = 2;
   int64_t cxu = 0, cyu = 0, cxp = 0, cyp = 0, cxv = 0, cyv = 0, cxw = 0, cyw = 0, czu = 0,
@@ -218,6 +226,12 @@ void stress_calculation(Block& b, double mu_f, double rho_f);
 // rigid-body motion (src/Search.F90:49-208, src/ReadInput.f90:403-420)
 void node_ids_from_elements(Block& b);
 void find_dist_node(Block& b);
+void block_move_check(int64_t& coarse_flcnt_check);
+void change_block_coords(Block& b);
+void change_block_coords_interfaces(Interface& it, Block& b);
+void change_block_interface(Interface& it, Block& a, Block& b);
+void cellcount_solid_coarse_mv(int64_t& coarse_flcnt_check);
+void tagging_th_move(Block& b, int64_t id);
 void shift_surface_nodes_initial(Block& b, double aoa, double piv_pt, int64_t ita, double deltat,
                                  double dxmin, double totime);
 void compute_surface_variables(Block& b, double phase_angle, double piv_pt, int64_t ita,

@@ -12,7 +12,8 @@ std::vector<Interface*> g_interfaces;
 // src/AllocateArrays.f90:15-57 (+ the grid arrays of src/ReadInput.f90:206-225)
 void allocate_arrays(Block& b) {
   const int64_t nx = b.nx, ny = b.ny, nz = b.nz;
-  for (F3* f : {&b.u, &b.ut, &b.v, &b.vt, &b.w, &b.wt, &b.p, &b.b, &b.pc, &b.pco})
+  for (F3* f : {&b.u, &b.ut, &b.v, &b.vt, &b.w, &b.wt, &b.p, &b.b, &b.pc, &b.pco, &b.u_dum, &b.v_dum, &b.w_dum,
+                &b.p_dum})
     f->alloc(nx + 2, ny + 2, nz + 2);
   b.cell.alloc(nx + 2, ny + 2, nz + 2);
   b.cell_n.alloc(nx + 2, ny + 2, nz + 2);

@@ -647,12 +647,15 @@ int bcfd_block_create(int64_t nx, int64_t ny, int64_t nz, const double* x1, cons
   A(&D.stats, 1);
   A(&hb->bar, 2);
   A(&hb->prog, (size_t)kMaxTiles * kTileStride);
+  A(&hb->kin_dev, 1);
+  A(&hb->stage_dev, 1);
   if (r) {
     for (void* p : hb->allocs) cudaFree(p);
     delete hb;
     return r;
   }
   hb->stats = D.stats;
+  D.kin = hb->kin_dev;
   for (int q = 0; q < 6; ++q) D.box[q] = q & 1 ? -1 : 0;
   hb->x1.assign(x1, x1 + nx + 3);
   hb->y1.assign(y1, y1 + ny + 3);
@@ -846,7 +849,11 @@ int bcfd_block_set_body_motion(bcfd_handle h, const double* p) {
     BCFD_CUDA(cudaMemcpyAsync(z.data(), hb->d.znode0, nn * sizeof(double), cudaMemcpyDeviceToHost, stream()));
     BCFD_CUDA(cudaStreamSynchronize(stream()));
     for (int q = 0; q < nn; ++q) r0 = std::max(r0, std::sqrt(x[q] * x[q] + y[q] * y[q] + z[q] * z[q]));
+    hb->node0[0] = std::move(x);
+    hb->node0[1] = std::move(y);
+    hb->node0[2] = std::move(z);
   }
+  hb->node_id_host = id;
   hb->motion_r0 = r0;
   return 0;
 }
@@ -892,7 +899,7 @@ int bcfd_block_set_kinematics(bcfd_handle h, const double* k) {
   LOCK();
   GETB(h);
   if (!k) return BCFD_E_ARG;
-  DevBlock& D = hb->d;
+  Kin& D = hb->kin;
   D.xdot = k[0];
   D.ydot = k[1];
   D.yddot = k[2];
@@ -904,7 +911,7 @@ int bcfd_block_set_kinematics(bcfd_handle h, const double* k) {
   D.piv_x = k[8];
   D.piv_y = k[9];
   D.piv_z = k[10];
-  return 0;
+  return upload_kin(hb);
 }
 
 int bcfd_block_set_flags(bcfd_handle h, int64_t move_check, int64_t blk_mv_tag) {

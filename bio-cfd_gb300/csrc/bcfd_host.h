@@ -23,10 +23,51 @@ struct BodyMotion {
          initz_cent = 0, nxtz_cent = 0;
 };
 
+// Node placement of one step (computeSurfaceVariables): the rotation's
+// cos/sin for surface-51 (+angle) and -52 (-angle) nodes about the x axis
+// through z = piv_pt, then the translation
+struct Place {
+  double c1, s1, c2, s2, piv_pt;
+  double tx, ty1, ty2, tz1, tz2;
+  int two;  // 1: y = (yr1 + ty1) + ty2, z = (zr1 + tz1) + tz2; 0: one term
+};
+
+// one node moved by a Place, in the reference's evaluation order (the same
+// expression on the host and the device)
+__host__ __device__ inline void place_node(const Place& P, int id, double x, double y, double z, double* xo,
+                                           double* yo, double* zo) {
+  double xr1 = x, yr1 = y, zr1 = z;
+  if (id == 51 || id == 52) {
+    const double c = id == 51 ? P.c1 : P.c2, s = id == 51 ? P.s1 : P.s2;
+    zr1 = z * c + y * s + P.piv_pt - P.piv_pt * c;
+    yr1 = -(z * s) + y * c + P.piv_pt * s;
+  }
+  *xo = xr1 + P.tx;
+  *yo = P.two ? (yr1 + P.ty1) + P.ty2 : yr1 + P.ty1;
+  *zo = P.two ? (zr1 + P.tz1) + P.tz2 : zr1 + P.tz1;
+}
+
+// What a moving block's step needs from the host, uploaded in one copy: the
+// kinematics that take effect when the nodes move, the placement, and the
+// search origin/radius of the moved surface
+struct MotionStage {
+  Kin kin;
+  Place place;
+  float org[4];
+};
+
 struct HostBlock {
   int index = -1;                  // registration order (device table slot)
   BodyMotion motion;
   double motion_r0 = 0.0;          // largest body-frame node radius
+  Kin kin{};                       // host copy of the device kinematics (d.kin)
+  Kin* kin_dev = nullptr;          // the device kinematics the kernels read
+  MotionStage* stage_dev = nullptr;
+  MotionStage stage{};             // last staged placement
+  bool staged = false;             // a step's motion is staged but not applied
+  // body-frame nodes and surface ids on the host (moving blocks)
+  std::vector<double> node0[3];
+  std::vector<int8_t> node_id_host;
   std::vector<int> elem_host;      // elp1 | elp2 | elp3 | surf_id, as uploaded
   DevBlock d{};
   std::vector<void*> allocs;  // device allocations owned by the block
@@ -124,6 +165,7 @@ struct Lib {
   // captured time step (bcfd_run_steps with use_graph)
   cudaGraphExec_t step_graph = nullptr;
   std::vector<unsigned char> step_key;  // what the capture depends on
+  std::vector<unsigned char> eager_key; // the key left by the last eager step
   int64_t step_kernels = 0;              // kernels in the captured step
 };
 
@@ -226,6 +268,19 @@ int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_
                                 double dxmin, double totime);
 int compute_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, int64_t ita, double deltat,
                               double dxmin, double freq, double totime);
+// computeSurfaceVariables in two halves: the host's kinematics and the
+// staged upload (outside a captured step), then the node kernel that applies
+// them (inside it)
+int stage_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, int64_t ita, double deltat,
+                            double dxmin, double freq, double totime);
+int apply_surface_variables(HostBlock* hb);
+// a node's position under the staged placement (host, the kernel's arithmetic)
+void staged_node(const HostBlock* hb, int64_t node, double* x, double* y, double* z);
+// the device kinematics from the host copy (set_kinematics, set-up)
+int upload_kin(HostBlock* hb);
+// k_search.cu: the search origin/radius for the block's current grid and
+// node bound, recorded as the device's value (the caller puts it there)
+int search_origin_stage(HostBlock* hb, float h[4], float** dev);
 int launch_stress_noalloc(HostBlock* hb, double mu_f, double rho_f, double* out_host);
 // adjoint of the forcing loops (k_forcing.cu): per-task coefficient scratch
 // (capacity 6 * cap_ib tasks) and the adjoint arrays by axis (0 p, 1 u, 2 v, 3 w)
@@ -238,16 +293,16 @@ struct ForceCoef {
   double* gk;  // 8 accumulators: dJ/d(kinematic scalar p)
 };
 // the 8 rigid-body kinematic scalars of a block, in bcfd_block_set_kinematics order
-__host__ __device__ inline double& kin_scalar(DevBlock& B, int p) {
+__host__ __device__ inline double& kin_scalar(Kin& K, int p) {
   switch (p) {
-    case 0: return B.xdot;
-    case 1: return B.ydot;
-    case 2: return B.yddot;
-    case 3: return B.thetaDot1;
-    case 4: return B.thetaDDot1;
-    case 5: return B.thetaDot2;
-    case 6: return B.thetaDDot2;
-    default: return B.alphaDot;
+    case 0: return K.xdot;
+    case 1: return K.ydot;
+    case 2: return K.yddot;
+    case 3: return K.thetaDot1;
+    case 4: return K.thetaDDot1;
+    case 5: return K.thetaDot2;
+    case 6: return K.thetaDDot2;
+    default: return K.alphaDot;
   }
 }
 struct AdjPtrs {

@@ -82,6 +82,12 @@ struct Walk3 {
 // Momentum coefficient tables, order of src/NavierStokes.f90:32-40
 enum CoefTab { T_UU = 0, T_VV, T_WW, T_UV, T_UW, T_VU, T_VW, T_WU, T_WV, N_TAB };
 
+// Rigid-body kinematic scalars of a block's surface (Block_t's xdot, ydot,
+// yddot, thetaDot1/2, thetaDDot1/2, alphaDot and the pivot piv_x/y/z).
+struct Kin {
+  double xdot, ydot, yddot, thetaDot1, thetaDDot1, thetaDot2, thetaDDot2, alphaDot, piv_x, piv_y, piv_z;
+};
+
 // Device view of one block (passed by value to kernels).
 struct DevBlock {
   Dims d;
@@ -131,9 +137,9 @@ struct DevBlock {
   int64_t* cnt;         // device counts: [0] ib, [1] solid, [2] fluid, [3] red, [4] black, [5] ts
   // search box (tagging_th_core)
   int box[6];
-  // kinematics (the forcing routines read them)
-  double xdot, ydot, yddot, thetaDot1, thetaDDot1, thetaDot2, thetaDDot2, alphaDot, piv_x, piv_y,
-      piv_z;
+  // kinematics of the block's body (the forcing and stress routines read
+  // them); device-resident so that a captured step reads each step's values
+  const struct Kin* kin;
   int* err;             // device error word of this block (first error wins)
   double* scratch;      // per-block reduction scratch
   double* bpk[2];       // colour-packed divergence b (the reference's Block_t%b)

@@ -229,6 +229,44 @@ int64_t first_above(const std::vector<double>& v, int64_t from, int64_t n, doubl
   return keep;
 }
 
+// block_move_check's trigger (src/Search.F90:1020-1030): the moving surface
+// within the margins of its fine block's interface box.  The surface nodes
+// mk and mkx1 are evaluated on the host from the staged placement (the node
+// kernel's own arithmetic), so the decision needs no device read.
+bool move_triggered(const HostBlock* c, const HostInterface* it, const HostBlock* fb, double* xmk1_out,
+                    bool* ytrig_out) {
+  const BodyMotion& m = fb->motion;
+  const double mg1 = 3.0 * c->dx;  // cintp * block(1)%dx
+  const double marginx = 4.5 * mg1, marginy = 5 * mg1, marginz = 1.52 * mg1;
+  double xq, yq, zq, ymk, xmk1;
+  staged_node(fb, fb->mk, &xq, &ymk, &zq);
+  staged_node(fb, fb->mkx1, &xmk1, &yq, &zq);
+  const double yval_up = std::fmax(ymk, m.nxty_cent + 0.02), yval_dw = std::fmin(ymk, m.nxty_cent - 0.02);
+  const double piv_z = fb->kin.piv_z;
+  const double* box = it->box;  // xs, xe, ys, ye, zs, ze
+  const bool ytrig = std::fabs(yval_dw - box[2]) <= marginy || std::fabs(yval_up - box[3]) <= marginy;
+  if (xmk1_out) *xmk1_out = xmk1;
+  if (ytrig_out) *ytrig_out = ytrig;
+  return std::fabs(xmk1 - box[0]) <= marginx || std::fabs(piv_z - box[4]) <= marginz ||
+         std::fabs(piv_z - box[5]) <= marginz || ytrig;
+}
+
+bool movable(const HostBlock* fb) {
+  return fb && fb->motion.on && fb->mk >= 1 && fb->mkx1 >= 1 && !fb->node_id_host.empty();
+}
+
+// a staged step that will move a fine block (such a step runs eagerly)
+bool any_move_pending() {
+  HostBlock* c = get_block(1);
+  if (!c) return false;
+  for (HostInterface* it : lib().ifs) {
+    if (!it) continue;
+    HostBlock* fb = get_block(it->b);
+    if (movable(fb) && move_triggered(c, it, fb, nullptr, nullptr)) return true;
+  }
+  return false;
+}
+
 // block_move_check, change_block_coords, change_block_coords_interfaces,
 // change_block_interface, fine_block_cell and cellCount_solid_coarse_mv
 int block_move_stage() {
@@ -244,23 +282,18 @@ int block_move_stage() {
   for (HostInterface* it : lib().ifs) {
     if (!it) continue;
     HostBlock* fb = get_block(it->b);
-    if (!fb || !fb->motion.on || fb->mk < 1 || fb->mkx1 < 1) continue;
+    if (!movable(fb)) continue;
     BodyMotion& m = fb->motion;
     const double mg1 = 3.0 * c->dx;  // cintp * block(1)%dx
-    const double marginx = 4.5 * mg1, marginy = 5 * mg1, marginz = 1.52 * mg1;
+    const double marginx = 4.5 * mg1;
     const int64_t factor = it->b_msh / it->a_msh;
-    double ymk = 0.0, xmk1 = 0.0;
-    BCFD_CUDA(d2h(&ymk, fb->d.ynode1 + (fb->mk - 1), sizeof(double)));
-    BCFD_CUDA(d2h(&xmk1, fb->d.xnode1 + (fb->mkx1 - 1), sizeof(double)));
-    const double yval_up = std::fmax(ymk, m.nxty_cent + 0.02), yval_dw = std::fmin(ymk, m.nxty_cent - 0.02);
-    const double piv_z = fb->d.piv_z;
+    const double piv_z = fb->kin.piv_z;
     double* box = it->box;  // xs, xe, ys, ye, zs, ze
     int64_t* amt = fb->move_amt;
     amt[0] = amt[1] = amt[2] = 0;
-    const bool ytrig = std::fabs(yval_dw - box[2]) <= marginy || std::fabs(yval_up - box[3]) <= marginy;
-    const bool trig = std::fabs(xmk1 - box[0]) <= marginx || std::fabs(piv_z - box[4]) <= marginz ||
-                      std::fabs(piv_z - box[5]) <= marginz || ytrig;
-    if (!trig) continue;
+    double xmk1 = 0.0;
+    bool ytrig = false;
+    if (!move_triggered(c, it, fb, &xmk1, &ytrig)) continue;
     fb->move_check = 1;
     fb->blk_mv_tag = 1;
     flag = 1;
@@ -346,19 +379,27 @@ int block_move_stage() {
   return 0;
 }
 
-bool any_motion() {
-  for (HostBlock* hb : lib().blocks)
-    if (hb && hb->motion.on) return true;
-  return false;
+// The host part of a step, run before its launches (and outside a captured
+// step): app/main.F90:130-131, then the kinematics of every moving body,
+// staged in device memory for the step's node kernel.  The kinematics depend
+// only on the loop counters, never on the flow, so evaluating them before the
+// step's first half gives the values the reference computes after it.
+int step_begin(const bcfd_step_config& cfg) {
+  Lib& L = lib();
+  L.ita = L.ita + 1;
+  L.totime = L.totime + cfg.deltat;
+  for (auto& [g, hb] : blocks())
+    if (hb->motion.on)
+      TRY(stage_surface_variables(hb, L.phase_angle, L.piv_pt, L.ita, cfg.deltat, L.dxmin, L.freq, L.totime));
+  return 0;
 }
 
-int step_once(const bcfd_step_config& cfg) {
+// The device part of a step (everything a captured step holds); a step whose
+// staged motion moves a fine block runs it eagerly.
+int step_body(const bcfd_step_config& cfg) {
   SolveCfg c{cfg.pc_ita_max, cfg.epsi, cfg.deltat, cfg.uc, cfg.precision, cfg.div_tol};
   auto all = blocks();
   Lib& L = lib();
-  // app/main.F90:130-131
-  L.ita = L.ita + 1;
-  L.totime = L.totime + cfg.deltat;
   std::vector<HostBlock*> every;
   for (auto& [g, hb] : all) every.push_back(hb);
   // nsMomentum2order of every block in one launch (blocks are independent)
@@ -374,14 +415,13 @@ int step_once(const bcfd_step_config& cfg) {
   TRY(poisson(c, 1, (int)lib().blocks.size(), 1));
   for (auto& [g, hb] : all)
     if (hb->has_body) TRY(launch_forcing_pressure(hb, 0));
-  // moving bodies (app/main.F90:169-176, 213-215): kinematics and node
-  // positions, then the surface normals of the moved nodes.  The fine blocks
-  // do not move (block_move_check's margins must hold for the motion).
+  // moving bodies (app/main.F90:169-176, 213-215): the staged kinematics
+  // take effect and the nodes move
   bool moving = false;
   for (auto& [g, hb] : all)
     if (hb->motion.on) {
       hb->blk_mv_tag = 0;
-      TRY(compute_surface_variables(hb, L.phase_angle, L.piv_pt, L.ita, cfg.deltat, L.dxmin, L.freq, L.totime));
+      TRY(apply_surface_variables(hb));
       moving = true;
     }
   // the fine-block moves (main.F90:178-211), then the normals, then the
@@ -421,6 +461,11 @@ int step_once(const bcfd_step_config& cfg) {
     TRY(launch_forcing_pressure(hb, 2));
   }
   return 0;
+}
+
+int step_once(const bcfd_step_config& cfg) {
+  TRY(step_begin(cfg));
+  return step_body(cfg);
 }
 
 // Everything a captured step's launches depend on: the step configuration,
@@ -464,6 +509,7 @@ std::vector<unsigned char> step_key(const bcfd_step_config& c) {
     put(&it->dtab, sizeof it->dtab);
     put(it->counter, sizeof it->counter);
     put(it->off, sizeof it->off);
+    put(it->box, sizeof it->box);
   }
   return k;
 }
@@ -473,36 +519,45 @@ std::vector<unsigned char> step_key(const bcfd_step_config& c) {
 // happen there, outside any capture), then one step is captured, not run.
 int run_steps_graph(const bcfd_step_config& cfg, int64_t n) {
   Lib& L = lib();
-  int64_t done = 0;
-  if (!L.step_graph || step_key(cfg) != L.step_key) {
-    if (L.step_graph) cudaGraphExecDestroy(L.step_graph);
-    L.step_graph = nullptr;
-    L.step_key.clear();
-    if (n == 0) return 0;
-    TRY(step_once(cfg));
-    done = 1;
-    if (done == n) return 0;
-    const std::vector<unsigned char> key = step_key(cfg);
-    cudaGraph_t g = nullptr;
-    const int64_t k0 = L.launches;
-    BCFD_CUDA(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeRelaxed));
-    const int r = step_once(cfg);
-    const cudaError_t e = cudaStreamEndCapture(stream(), &g);
-    if (r) {
-      if (g) cudaGraphDestroy(g);
-      return r;
+  for (int64_t done = 0; done < n; ++done) {
+    TRY(step_begin(cfg));
+    // a fine-block move changes grids, tables and launch shapes: eager
+    if (any_move_pending()) {
+      TRY(step_body(cfg));
+      continue;
     }
-    BCFD_CUDA(e);
-    const cudaError_t ei = cudaGraphInstantiate(&L.step_graph, g, 0);
-    cudaGraphDestroy(g);
-    BCFD_CUDA(ei);
-    L.step_kernels = L.launches - k0;
-    L.launches = k0;
-    L.step_key = key;
-  }
-  for (; done < n; ++done) {
+    const std::vector<unsigned char> key = step_key(cfg);
+    if (!L.step_graph || key != L.step_key) {
+      if (L.step_graph) cudaGraphExecDestroy(L.step_graph);
+      L.step_graph = nullptr;
+      L.step_key.clear();
+      if (key != L.eager_key) {
+        // the first step under a new key runs eagerly (one-time allocations);
+        // the key it leaves is the one captured next
+        TRY(step_body(cfg));
+        L.eager_key = step_key(cfg);
+        continue;
+      }
+      cudaGraph_t g = nullptr;
+      const int64_t k0 = L.launches;
+      BCFD_CUDA(cudaStreamBeginCapture(stream(), cudaStreamCaptureModeRelaxed));
+      const int r = step_body(cfg);
+      const cudaError_t e = cudaStreamEndCapture(stream(), &g);
+      if (r) {
+        if (g) cudaGraphDestroy(g);
+        return r;
+      }
+      BCFD_CUDA(e);
+      const cudaError_t ei = cudaGraphInstantiate(&L.step_graph, g, 0);
+      cudaGraphDestroy(g);
+      BCFD_CUDA(ei);
+      L.step_kernels = L.launches - k0;
+      L.launches = k0;
+      L.step_key = key;
+    }
     BCFD_CUDA(cudaGraphLaunch(L.step_graph, stream()));
     L.launches += L.step_kernels;
+    for (auto& [g, hb] : blocks()) hb->staged = false;  // applied by the replay
   }
   return 0;
 }
@@ -663,9 +718,7 @@ int bcfd_tagging_th_move(bcfd_handle h) {
 int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps) {
   LOCK();
   if (!cfg || n_steps < 0) return BCFD_E_ARG;
-  // a moving body changes the kernels' arguments every step: issue those
-  // steps eagerly
-  if (cfg->use_graph && !lib().prof_on && !any_motion()) {
+  if (cfg->use_graph && !lib().prof_on) {
     TRY(run_steps_graph(*cfg, n_steps));
   } else {
     for (int64_t s = 0; s < n_steps; ++s) TRY(step_once(*cfg));
@@ -734,8 +787,9 @@ int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64
     // kinematic scalars the forcing routines read
     const char* kn[10] = {"xdot", "ydot", "yddot", "thetaDot1", "thetaDDot1", "thetaDot2", "thetaDDot2",
                           "piv_x", "piv_y", "piv_z"};
-    const double kv[10] = {D.xdot, D.ydot, D.yddot, D.thetaDot1, D.thetaDDot1, D.thetaDot2, D.thetaDDot2,
-                           D.piv_x, D.piv_y, D.piv_z};
+    const Kin& K = hb->kin;
+    const double kv[10] = {K.xdot, K.ydot, K.yddot, K.thetaDot1, K.thetaDDot1, K.thetaDot2, K.thetaDDot2,
+                           K.piv_x, K.piv_y, K.piv_z};
     for (int q = 0; q < 10; ++q)
       if (s == kn[q]) {
         if (n < 1) return BCFD_E_ARG;

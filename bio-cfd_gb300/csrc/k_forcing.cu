@@ -182,19 +182,19 @@ __device__ __forceinline__ double dotn(const DevBlock& B, int e, const double d[
 // the `0 + ydot` forms of Forcing.f90:237 and :551 are kept (they map -0 to +0)
 __device__ double surf_velocity(const DevBlock& B, int e, int comp, int mode) {
   const int sid = B.surf_id[e];
-  if (comp == CU2 || comp == CU1) return B.xdot;
+  if (comp == CU2 || comp == CU1) return B.kin->xdot;
   if (comp == CV2 || comp == CV1) {
     if (sid == 50) {
       const bool plus0 = (comp == CV1 && mode == 0) || (comp == CV2 && mode == 2);
-      return plus0 ? 0.0 + B.ydot : B.ydot;
+      return plus0 ? 0.0 + B.kin->ydot : B.kin->ydot;
     }
-    const double td = sid == 51 ? B.thetaDot1 : B.thetaDot2;
-    if (mode == 0) return -td * (B.zcent[e] - B.piv_z) + B.ydot;
-    return -td * (B.zcent[e] - B.piv_z) + (-B.alphaDot) * (B.xcent[e] - B.piv_x) + B.ydot;
+    const double td = sid == 51 ? B.kin->thetaDot1 : B.kin->thetaDot2;
+    if (mode == 0) return -td * (B.zcent[e] - B.kin->piv_z) + B.kin->ydot;
+    return -td * (B.zcent[e] - B.kin->piv_z) + (-B.kin->alphaDot) * (B.xcent[e] - B.kin->piv_x) + B.kin->ydot;
   }
   if (sid == 50) return 0.0;
-  const double td = sid == 51 ? B.thetaDot1 : B.thetaDot2;
-  return td * (B.ycent[e] - B.piv_y);
+  const double td = sid == 51 ? B.kin->thetaDot1 : B.kin->thetaDot2;
+  return td * (B.ycent[e] - B.kin->piv_y);
 }
 
 __device__ __forceinline__ double vel_quad(double pos_val, double surf, double dn, double n1,
@@ -210,16 +210,16 @@ __device__ double dpdn_body(const DevBlock& B, int e, int mode) {
   const int sid = B.surf_id[e];
   double ac_y = 0, ac_z = 0, at_y = 0, at_z = 0;
   if (sid == 51 || sid == 52) {
-    const double td = sid == 51 ? B.thetaDot1 : B.thetaDot2;
-    const double tdd = sid == 51 ? B.thetaDDot1 : B.thetaDDot2;
-    ac_z = -(td * td) * (B.zcent[e] - B.piv_z);
-    ac_y = -(td * td) * (B.ycent[e] - B.piv_y);
-    at_z = tdd * (B.ycent[e] - B.piv_y);
-    at_y = -tdd * (B.zcent[e] - B.piv_z);
+    const double td = sid == 51 ? B.kin->thetaDot1 : B.kin->thetaDot2;
+    const double tdd = sid == 51 ? B.kin->thetaDDot1 : B.kin->thetaDDot2;
+    ac_z = -(td * td) * (B.zcent[e] - B.kin->piv_z);
+    ac_y = -(td * td) * (B.ycent[e] - B.kin->piv_y);
+    at_z = tdd * (B.ycent[e] - B.kin->piv_y);
+    at_y = -tdd * (B.zcent[e] - B.kin->piv_z);
   }
   if (mode == 2)
-    return ((ac_z + at_z) * B.cosG[e] + (ac_y + at_y) * B.cosB[e]) + (B.yddot * (B.cosB[e]));
-  return -((ac_z + at_z) * B.cosG[e] + (ac_y + at_y) * B.cosB[e]) - B.yddot * B.cosB[e];
+    return ((ac_z + at_z) * B.cosG[e] + (ac_y + at_y) * B.cosB[e]) + (B.kin->yddot * (B.cosB[e]));
+  return -((ac_z + at_z) * B.cosG[e] + (ac_y + at_y) * B.cosB[e]) - B.kin->yddot * B.cosB[e];
 }
 
 // value of one reconstruction from its 8 stencil values
@@ -462,9 +462,12 @@ __global__ void k_force_coef(DevBlock B, int mode, int vel, ForceCoef fc) {
     // each scalar (centripetal terms), so the central difference with unit
     // steps is its derivative
     for (int p = 0; p < 8; ++p) {
+      Kin kp = *B.kin, km = *B.kin;
+      kin_scalar(kp, p) += 1.0;
+      kin_scalar(km, p) -= 1.0;
       DevBlock Bp = B, Bm = B;
-      kin_scalar(Bp, p) += 1.0;
-      kin_scalar(Bm, p) -= 1.0;
+      Bp.kin = &kp;
+      Bm.kin = &km;
       fc.kc[8 * (int64_t)t + p] = 0.5 * (reconstruct(Bp, mode, comp, P, f) - reconstruct(Bm, mode, comp, P, f));
     }
   }

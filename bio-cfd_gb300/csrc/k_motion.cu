@@ -3,9 +3,12 @@
 // kinematics and node positions computeSurfaceVariables
 // (src/Search.F90:126-208).  The kinematic scalars and the rotation's
 // cos/sin are evaluated on the host with the reference's expressions (one
-// value per step, so the host and the oracle give identical bits); one kernel
+// value per step, so the host and the oracle give identical bits) and staged
+// in device memory with one copy; one kernel then makes them current and
 // moves the nodes: rotation of surface-51 (+angle) and -52 (-angle) nodes
-// about the x axis through z = piv_pt, then the translation.
+// about the x axis through z = piv_pt, then the translation.  Staging runs
+// before a captured step is launched, the kernel inside it, so a step with a
+// moving body replays from a CUDA graph.
 #include <cmath>
 
 #include "bcfd_host.h"
@@ -15,29 +18,21 @@ namespace {
 
 constexpr double kXfact = 0.05;  // src/Search.F90:12
 
-struct Place {
-  double c1, s1, c2, s2, piv_pt;
-  double tx, ty1, ty2, tz1, tz2;
-  int two;  // 1: y = (yr1 + ty1) + ty2, z = (zr1 + tz1) + tz2; 0: one term
-};
-
-__global__ void k_place_nodes(DevBlock B, Place P) {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < B.nn; i += gridDim.x * blockDim.x) {
-    const int id = B.node_id[i];
-    const double x = B.xnode0[i], y = B.ynode0[i], z = B.znode0[i];
-    double xr1 = x, yr1 = y, zr1 = z;
-    if (id == 51 || id == 52) {
-      const double c = id == 51 ? P.c1 : P.c2, s = id == 51 ? P.s1 : P.s2;
-      zr1 = z * c + y * s + P.piv_pt - P.piv_pt * c;
-      yr1 = -(z * s) + y * c + P.piv_pt * s;
-    }
-    double* xn = const_cast<double*>(B.xnode1);
-    double* yn = const_cast<double*>(B.ynode1);
-    double* zn = const_cast<double*>(B.znode1);
-    xn[i] = xr1 + P.tx;
-    yn[i] = P.two ? (yr1 + P.ty1) + P.ty2 : yr1 + P.ty1;
-    zn[i] = P.two ? (zr1 + P.tz1) + P.tz2 : zr1 + P.tz1;
+// the staged step: the kinematics take effect, the search origin of the
+// moved surface is set, the nodes move
+__global__ void k_place_nodes(DevBlock B, const MotionStage* S, Kin* kin, float* org) {
+  const int t0 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t0 == 0) {
+    *kin = S->kin;
+    if (org)
+      for (int q = 0; q < 4; ++q) org[q] = S->org[q];
   }
+  const Place P = S->place;
+  double* xn = const_cast<double*>(B.xnode1);
+  double* yn = const_cast<double*>(B.ynode1);
+  double* zn = const_cast<double*>(B.znode1);
+  for (int i = t0; i < B.nn; i += gridDim.x * blockDim.x)
+    place_node(P, B.node_id[i], B.xnode0[i], B.ynode0[i], B.znode0[i], xn + i, yn + i, zn + i);
 }
 
 // the nearest-element search's bound on node distances from the block centre
@@ -52,17 +47,48 @@ void update_node_rmax(HostBlock* hb, double piv_pt, double tx, double ty, double
   hb->node_rmax = std::sqrt(ax * ax + ay * ay + az * az) + hb->motion_r0 + 2.0 * std::fabs(piv_pt) + 1e-9;
 }
 
-int place_nodes(HostBlock* hb, double aoa1, double piv_pt, double tx, double ty1, double ty2, double tz1,
+// stage a placement: the node bound, the search origin, one upload of the
+// kinematics/placement/origin (a pageable source is staged by the copy call,
+// so the host struct may change right after)
+int stage_place(HostBlock* hb, double aoa1, double piv_pt, double tx, double ty1, double ty2, double tz1,
                 double tz2, int two) {
   if (hb->d.nn <= 0) return 0;
   update_node_rmax(hb, piv_pt, tx, ty1 + ty2, tz1 + tz2);
   const double aoa2 = -aoa1;
-  Place P{std::cos(aoa1), std::sin(aoa1), std::cos(aoa2), std::sin(aoa2), piv_pt, tx, ty1, ty2, tz1, tz2, two};
-  k_place_nodes<<<grid_for(hb->d.nn, 128), 128, 0, stream()>>>(hb->d, P);
+  MotionStage& S = hb->stage;
+  S.kin = hb->kin;
+  S.place = Place{std::cos(aoa1), std::sin(aoa1), std::cos(aoa2), std::sin(aoa2), piv_pt, tx, ty1, ty2, tz1, tz2, two};
+  float* dev = nullptr;
+  TRY_R(search_origin_stage(hb, S.org, &dev));
+  BCFD_CUDA(cudaMemcpyAsync(hb->stage_dev, &S, sizeof(S), cudaMemcpyHostToDevice, stream()));
+  hb->staged = true;
+  return 0;
+}
+
+}  // namespace
+
+int apply_surface_variables(HostBlock* hb) {
+  if (hb->d.nn <= 0) return upload_kin(hb);
+  if (!hb->staged) return BCFD_E_STATE;
+  hb->staged = false;
+  float* dev = nullptr;
+  TRY_R(search_origin_stage(hb, nullptr, &dev));
+  k_place_nodes<<<grid_for(hb->d.nn, 128), 128, 0, stream()>>>(hb->d, hb->stage_dev, hb->kin_dev, dev);
   BCFD_LAUNCHED();
   return 0;
 }
 
+void staged_node(const HostBlock* hb, int64_t node, double* x, double* y, double* z) {
+  const size_t q = (size_t)(node - 1);
+  place_node(hb->stage.place, hb->node_id_host[q], hb->node0[0][q], hb->node0[1][q], hb->node0[2][q], x, y, z);
+}
+
+int upload_kin(HostBlock* hb) {
+  BCFD_CUDA(cudaMemcpyAsync(hb->kin_dev, &hb->kin, sizeof(Kin), cudaMemcpyHostToDevice, stream()));
+  return 0;
+}
+
+namespace {
 }  // namespace
 
 int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_t ita, double deltat,
@@ -77,7 +103,7 @@ int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_
   m.xpth1 = m.xshift - ((double)ita * dxmin * kXfact);
   m.xpth2 = m.xshift - ((double)ita * dxmin * kXfact);
   m.ypth2 = (m.yamp) * std::sin(angt * m.xshift);
-  DevBlock& D = hb->d;
+  Kin& D = hb->kin;
   D.piv_x = m.xshift;
   D.piv_y = m.yshift;
   D.piv_z = m.zshift;
@@ -91,7 +117,8 @@ int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_
   m.inity_cent = m.nxty_cent = m.yshift;
   m.initx_cent = m.nxtx_cent = m.xshift;
   m.initz_cent = m.nxtz_cent = m.zshift;
-  return place_nodes(hb, aoa1, piv_pt, m.xshift, m.yshift, 0.0, m.zshift, 0.0, 0);
+  TRY_R(stage_place(hb, aoa1, piv_pt, m.xshift, m.yshift, 0.0, m.zshift, 0.0, 0));
+  return apply_surface_variables(hb);
 }
 
 namespace {
@@ -163,8 +190,14 @@ int launch_move_fields(HostBlock* hb, const double* dum) {
 
 int compute_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, int64_t ita, double deltat,
                               double dxmin, double freq, double totime) {
+  TRY_R(stage_surface_variables(hb, phase_angle, piv_pt, ita, deltat, dxmin, freq, totime));
+  return apply_surface_variables(hb);
+}
+
+int stage_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, int64_t ita, double deltat,
+                            double dxmin, double freq, double totime) {
   BodyMotion& m = hb->motion;
-  DevBlock& D = hb->d;
+  Kin& D = hb->kin;
   const double pi = 4.0 * std::atan(1.0);
   const double aoa1 = (m.a0) * std::sin(2.0 * pi * freq * (totime + deltat) + phase_angle);
   const double ang_theta = 2.0 * pi * freq;
@@ -192,7 +225,7 @@ int compute_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, 
   D.piv_z = D.piv_z + m.zmove;
   m.nxty_cent = m.nxty_cent + m.ychg;
   m.nxtx_cent = m.nxtx_cent + m.xmove;
-  return place_nodes(hb, aoa1, piv_pt, m.xpth2, m.yshift, m.ymove, m.zshift, m.zmove, 1);
+  return stage_place(hb, aoa1, piv_pt, m.xpth2, m.yshift, m.ymove, m.zshift, m.zmove, 1);
 }
 
 }  // namespace bcfd

@@ -541,7 +541,7 @@ void free_search_scratch(HostBlock* hb) {
   hb->search_scratch = nullptr;
 }
 
-static int ensure_scratch(HostBlock* hb) {
+static int ensure_alloc(HostBlock* hb) {
   SearchScratch& s = scratch_of(hb);
   const int64_t np = hb->d.d.npts();
   if (s.npts != np) {
@@ -566,21 +566,46 @@ static int ensure_scratch(HostBlock* hb) {
     s.cap_e = hb->d.ne;
     lib().gen++;
   }
-  // origin: centre of the block; R: half diagonal of the padded block
+  return 0;
+}
+
+// origin: centre of the block; R: half diagonal of the padded block
+static void origin_of(const HostBlock* hb, float h[4]) {
   const Dims& d = hb->d.d;
   const double x0 = hb->x1[0], x1 = hb->x1[d.nx + 2], y0 = hb->y1[0], y1 = hb->y1[d.ny + 2],
                z0 = hb->z1[0], z1 = hb->z1[d.nz + 2];
-  float h[4] = {(float)(0.5 * (x0 + x1)), (float)(0.5 * (y0 + y1)), (float)(0.5 * (z0 + z1)), 0.f};
+  h[0] = (float)(0.5 * (x0 + x1));
+  h[1] = (float)(0.5 * (y0 + y1));
+  h[2] = (float)(0.5 * (z0 + z1));
   const double R = 0.5 * std::sqrt((x1 - x0) * (x1 - x0) + (y1 - y0) * (y1 - y0) + (z1 - z0) * (z1 - z0));
   // bound on |query - origin| and |centroid - origin| (centroids lie inside
   // the hull of the nodes)
   h[3] = (float)(1.01 * std::max(R, hb->node_rmax) + 1e-6);
+}
+
+static int ensure_scratch(HostBlock* hb) {
+  TRY_R(ensure_alloc(hb));
+  SearchScratch& s = scratch_of(hb);
+  float h[4];
+  origin_of(hb, h);
   // upload only when it changes (a captured step contains no host copies)
   if (!s.org_set || std::memcmp(h, s.org_host, sizeof(h)) != 0) {
     std::memcpy(s.org_host, h, sizeof(h));
     BCFD_CUDA(cudaMemcpyAsync(s.org, s.org_host, sizeof(h), cudaMemcpyHostToDevice, stream()));
     s.org_set = true;
   }
+  return 0;
+}
+
+int search_origin_stage(HostBlock* hb, float h[4], float** dev) {
+  TRY_R(ensure_alloc(hb));
+  SearchScratch& s = scratch_of(hb);
+  if (h) {
+    origin_of(hb, h);
+    std::memcpy(s.org_host, h, 4 * sizeof(float));
+    s.org_set = true;
+  }
+  *dev = s.org;
   return 0;
 }
 

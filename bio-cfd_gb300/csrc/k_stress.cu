@@ -101,16 +101,16 @@ __device__ void elem_terms(const DevBlock& B, int e, double mu_f, double rho_f, 
   const double nd = S.diag, diag = S.diag;
   const double px = S.px, py = S.py, pz = S.pz;
   const int sid = B.surf_id[e];
-  const double td = sid == 51 ? B.thetaDot1 : (sid == 52 ? B.thetaDot2 : 0.0);
-  const double tdd = sid == 51 ? B.thetaDDot1 : (sid == 52 ? B.thetaDDot2 : 0.0);
-  const double us = B.xdot;
-  const double vs = -td * (B.zcent[e] - B.piv_z) + B.ydot;
-  const double ws = td * (B.ycent[e] - B.piv_y);
-  const double ac_z = -(td * td) * (B.zcent[e] - B.piv_z);
-  const double ac_y = -(td * td) * (B.ycent[e] - B.piv_y);
-  const double at_z = tdd * (B.ycent[e] - B.piv_y);
-  const double at_y = -tdd * (B.zcent[e] - B.piv_z);
-  const double dpdn = -((ac_z + at_z) * B.cosG[e] + (ac_y + at_y) * B.cosB[e]) - B.yddot * B.cosB[e];
+  const double td = sid == 51 ? B.kin->thetaDot1 : (sid == 52 ? B.kin->thetaDot2 : 0.0);
+  const double tdd = sid == 51 ? B.kin->thetaDDot1 : (sid == 52 ? B.kin->thetaDDot2 : 0.0);
+  const double us = B.kin->xdot;
+  const double vs = -td * (B.zcent[e] - B.kin->piv_z) + B.kin->ydot;
+  const double ws = td * (B.ycent[e] - B.kin->piv_y);
+  const double ac_z = -(td * td) * (B.zcent[e] - B.kin->piv_z);
+  const double ac_y = -(td * td) * (B.ycent[e] - B.kin->piv_y);
+  const double at_z = tdd * (B.ycent[e] - B.kin->piv_y);
+  const double at_y = -tdd * (B.zcent[e] - B.kin->piv_z);
+  const double dpdn = -((ac_z + at_z) * B.cosG[e] + (ac_y + at_y) * B.cosB[e]) - B.kin->yddot * B.cosB[e];
   double val, g[3], ddn[3];
   vad_eval(px, py, pz, B.xu, B.yu, B.zu, S.ijk[0], f[0], val, g);
   ddn[0] = (2.0 / nd) * (val - us) - (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]);
@@ -183,9 +183,12 @@ __global__ void k_stress_kin(DevBlock B, double mu_f, double rho_f, const double
   if (blockIdx.x || threadIdx.x) return;
   const double* arr[4] = {B.u, B.v, B.w, B.p};
   for (int p = 0; p < 8; ++p) {
+    Kin kp = *B.kin, km = *B.kin;
+    kin_scalar(kp, p) += 1.0;
+    kin_scalar(km, p) -= 1.0;
     DevBlock Bp = B, Bm = B;
-    kin_scalar(Bp, p) += 1.0;
-    kin_scalar(Bm, p) -= 1.0;
+    Bp.kin = &kp;
+    Bm.kin = &km;
     double acc = 0.0;
     for (int e = 0; e < B.ne; ++e) {
       const ElemStencil S = elem_stencil(B, e);

@@ -39,6 +39,10 @@ void block_move_check(int64_t& coarse_flcnt_check) {
   for (Interface* itp : g_interfaces) {
     Interface& it = *itp;
     Block& fb = blk_of(it.b_blk);
+    // the reference reads ynode1(mk) and xnode1(mkx1) of every fine block;
+    // a block without a moving plate has no such nodes (mk = 0, an
+    // out-of-bounds read there) and is skipped, as the library does
+    if (fb.mk < 1 || fb.mkx1 < 1) continue;
     const double mg1 = (double)fb.cintp * blk_of(1).dx;
     const double marginx = 4.5 * mg1, marginy = 5 * mg1, marginz = 1.52 * mg1;
     const int64_t factor = it.b_msh / it.a_msh;

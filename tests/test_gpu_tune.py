@@ -27,7 +27,7 @@ def test_tuned_equals_untuned(precision):
     case = synth.small_two_block(n_steps=2)
     a, _, _ = _run(case, precision, False)
     b, n, shapes = _run(case, precision, True)
-    assert all(sh["fp64_threads"] > 0 and sh["fp32_variant"] in (1, 3) for sh in shapes), shapes
+    assert all(sh["fp64_threads"] > 0 and sh["fp32_variant"] in (1, 3, 4) for sh in shapes), shapes
     for q, ((fa, ia), (fb, ib)) in enumerate(zip(a, b)):
         for k in ("u", "v", "w", "p"):
             assert_bitwise(f"block {q + 1} {k}", fa[k], fb[k])

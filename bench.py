@@ -277,7 +277,7 @@ def twelve_block(torch, local, steps=10, warmup=3, fp64_steps=2, moving=False):
                        f"({body.nx}x{body.ny}x{body.nz} with a plate 0.5x0.125x0.0125, 2x128x64x64, 2x96x64x64, "
                        f"2x64x48x48, 2x48^3, 2x32^3), {ncells / 1e6:.1f}M cells, Re 500" +
                        (", plate heaving 0.5 sin(2 pi 0.25 t) and pitching 30 deg sin(2 pi 0.25 t + 90 deg), "
-                        "Search every step, steps issued kernel by kernel" if moving else
+                        "Search every step, graph replay (each step's kinematics staged before its launch)" if moving else
                         ", stationary plate, graph replay"),
            "div_tol": DIV_TOL}
     arms = (("mixed_batched", 1, True, steps), ("mixed_per_block", 1, False, steps),

@@ -780,6 +780,18 @@ int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64
     if (written) *written = 1;
     return 0;
   }
+  {
+    // the block-move switches and amounts of Block_t
+    const char* fn[5] = {"move_check", "blk_mv_tag", "move_amtx", "move_amty", "move_amtz"};
+    const int64_t fv[5] = {hb->move_check, hb->blk_mv_tag, hb->move_amt[0], hb->move_amt[1], hb->move_amt[2]};
+    for (int q = 0; q < 5; ++q)
+      if (s == fn[q]) {
+        if (n < 1) return BCFD_E_ARG;
+        static_cast<int64_t*>(out)[0] = fv[q];
+        if (written) *written = 1;
+        return 0;
+      }
+  }
   if (s == "xnode1") return dcopy(D.xnode1, D.nn);
   if (s == "ynode1") return dcopy(D.ynode1, D.nn);
   if (s == "znode1") return dcopy(D.znode1, D.nn);

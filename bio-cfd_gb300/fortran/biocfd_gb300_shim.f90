@@ -309,3 +309,209 @@ contains
     call bcfd_call(blk, c_update_newv, 'updateVelocity_newv')
   end subroutine
 end module biocfd_pcor_vcor
+
+module biocfd_forcing
+  use biocfd_block_type, only: Block_t
+  use biocfd_gb300_c
+  use biocfd_gb300_glue
+  implicit none
+  private
+  public :: velocityForcing1, pressureForcing1, velocityForcingField, pressureForcingField, &
+            velocityForcingGhost, pressureForcingGhost
+  interface
+    integer(c_int) function c_vf1(h) bind(C, name="bcfd_velocity_forcing1")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_pf1(h) bind(C, name="bcfd_pressure_forcing1")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_vff(h) bind(C, name="bcfd_velocity_forcing_field")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_pff(h) bind(C, name="bcfd_pressure_forcing_field")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_vfg(h) bind(C, name="bcfd_velocity_forcing_ghost")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_pfg(h) bind(C, name="bcfd_pressure_forcing_ghost")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+  end interface
+contains
+  subroutine velocityForcing1(blk)                  ! src/Forcing.f90:92-360
+    type(Block_t), intent(inout) :: blk
+    call bcfd_call(blk, c_vf1, 'velocityForcing1')
+  end subroutine
+  subroutine pressureForcing1(blk)                  ! src/Forcing.f90:14-90
+    type(Block_t), intent(inout) :: blk
+    call bcfd_call(blk, c_pf1, 'pressureForcing1')
+  end subroutine
+  subroutine velocityForcingField(blk)              ! src/Forcing.f90:813-1075
+    type(Block_t), intent(inout) :: blk
+    call bcfd_call(blk, c_vff, 'velocityForcingField')
+  end subroutine
+  subroutine pressureForcingField(blk)              ! src/Forcing.f90:737-811
+    type(Block_t), intent(inout) :: blk
+    call bcfd_call(blk, c_pff, 'pressureForcingField')
+  end subroutine
+  subroutine velocityForcingGhost(blk)              ! src/Forcing.f90:450-734
+    type(Block_t), intent(inout) :: blk
+    call bcfd_call(blk, c_vfg, 'velocityForcingGhost')
+  end subroutine
+  subroutine pressureForcingGhost(blk)              ! src/Forcing.f90:362-448
+    type(Block_t), intent(inout) :: blk
+    call bcfd_call(blk, c_pfg, 'pressureForcingGhost')
+  end subroutine
+end module biocfd_forcing
+
+! Search routines of app/main.F90:169-263.  The fine-block move runs whole in
+! block_move_check (bcfd_block_move_stage); change_block_coords,
+! change_block_coords_interfaces, change_block_interface and
+! cellCount_solid_coarse_mv then only refresh the host mirrors.
+module biocfd_search
+  use, intrinsic :: iso_fortran_env, only: dp => real64, int64
+  use global, only: block
+  use biocfd_block_type, only: Block_t
+  use biocfd_gb300_c
+  use biocfd_gb300_glue
+  implicit none
+  private
+  public :: computeSurfaceVariables, computeSurfaceNorm, block_move_check, change_block_coords, &
+            change_block_coords_interfaces, change_block_interface, fine_block_cell, &
+            cellCount_solid_coarse_mv, tagging_th_move, selectiveRetagging_th, cellCount_solid, &
+            computeNormDistance, findTScells
+  interface
+    integer(c_int) function c_csv(h, phase, piv, ita, dt, dxmin, freq, totime) &
+         bind(C, name="bcfd_compute_surface_variables")
+      import :: c_int, c_int64_t, c_double
+      integer(c_int64_t), value :: h, ita
+      real(c_double), value :: phase, piv, dt, dxmin, freq, totime
+    end function
+    integer(c_int) function c_csn(h, inor) bind(C, name="bcfd_compute_surface_norm")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h, inor
+    end function
+    integer(c_int) function c_move(moved) bind(C, name="bcfd_block_move_stage")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), intent(out) :: moved
+    end function
+    integer(c_int) function c_tag_move(h) bind(C, name="bcfd_tagging_th_move")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_retag(h) bind(C, name="bcfd_selective_retagging_th")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_count(h) bind(C, name="bcfd_cellcount_solid")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_nd(h) bind(C, name="bcfd_compute_norm_distance")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_ts(h) bind(C, name="bcfd_find_ts_cells")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_read(h, name, out, n, written) bind(C, name="bcfd_block_read")
+      import :: c_int, c_int64_t, c_char, c_ptr
+      integer(c_int64_t), value :: h, n
+      character(kind=c_char), intent(in) :: name(*)
+      type(c_ptr), value :: out
+      integer(c_int64_t), intent(out) :: written
+    end function
+  end interface
+contains
+  subroutine computeSurfaceVariables(blk, g, phase_angle, piv_pt, ita, deltat, dxmin, freq, re, totime)
+    ! src/Search.F90:126-208 (re is not used by the routine)
+    type(Block_t), intent(inout) :: blk
+    integer(int64), intent(in) :: g, ita
+    real(dp), intent(in) :: phase_angle, piv_pt, deltat, dxmin, freq, re, totime
+    call bcfd_ensure(blk)
+    call bcfd_check(bcfd_block_set_flags(blk%bcfd, -1_c_int64_t, int(blk%blk_mv_tag, c_int64_t)), 'set_flags')
+    call bcfd_check(c_csv(blk%bcfd, phase_angle, piv_pt, ita, deltat, dxmin, freq, totime), &
+         'computeSurfaceVariables')
+  end subroutine
+  subroutine computeSurfaceNorm(blk, inor)          ! src/Search.F90:210-258
+    type(Block_t), intent(inout) :: blk
+    integer(int64), intent(in) :: inor
+    call bcfd_ensure(blk)
+    call bcfd_check(c_csn(blk%bcfd, inor), 'computeSurfaceNorm')
+  end subroutine
+  subroutine block_move_check(coarse_flcnt_check)   ! src/Search.F90:997-1203, with :1208-1461
+    integer(int64), intent(inout) :: coarse_flcnt_check
+    integer(c_int64_t) :: moved, w
+    integer(int64), target :: f(1)
+    integer :: g
+    call bcfd_check(c_move(moved), 'block_move_check')
+    coarse_flcnt_check = moved
+    ! the switches a moved block carries into the re-tagging (Block_t copies)
+    do g = 2, size(block)
+      if (block(g)%bcfd == 0) cycle
+      call bcfd_check(c_read(block(g)%bcfd, 'move_check'//char(0), c_loc(f), 1_c_int64_t, w), 'read')
+      block(g)%move_check = f(1)
+      call bcfd_check(c_read(block(g)%bcfd, 'blk_mv_tag'//char(0), c_loc(f), 1_c_int64_t, w), 'read')
+      block(g)%blk_mv_tag = real(f(1), dp)
+    end do
+  end subroutine
+  subroutine change_block_coords(blk)               ! src/Search.F90:1208-1264 (done in block_move_check)
+    type(Block_t), intent(inout), target :: blk
+    integer(c_int64_t) :: w
+    if (blk%bcfd == 0 .or. blk%move_check /= 1) return
+    call bcfd_check(c_read(blk%bcfd, 'x1'//char(0), c_loc(blk%x1), size(blk%x1, kind=c_int64_t), w), 'x1')
+    call bcfd_check(c_read(blk%bcfd, 'y1'//char(0), c_loc(blk%y1), size(blk%y1, kind=c_int64_t), w), 'y1')
+    call bcfd_check(c_read(blk%bcfd, 'z1'//char(0), c_loc(blk%z1), size(blk%z1, kind=c_int64_t), w), 'z1')
+  end subroutine
+  subroutine change_block_coords_interfaces(intf, blk)  ! :1269-1370 (done in block_move_check)
+    class(*), intent(inout) :: intf
+    type(Block_t), intent(inout) :: blk
+    if (blk%bcfd /= 0 .and. blk%move_check == 1 .and. bcfd_host_mirror) call bcfd_pull(blk)
+  end subroutine
+  subroutine change_block_interface(intf, a, b)    ! :1372-1461 (done in block_move_check)
+    class(*), intent(inout) :: intf
+    type(Block_t), intent(inout) :: a, b
+  end subroutine
+  subroutine fine_block_cell                       ! :863-914 (done in block_move_check)
+  end subroutine
+  subroutine cellCount_solid_coarse_mv(coarse_flcnt_check)  ! :916-995 (done in block_move_check)
+    integer(int64), intent(inout) :: coarse_flcnt_check
+    coarse_flcnt_check = 0
+  end subroutine
+  subroutine tagging_th_move(blk, id)               ! src/Search.F90:415-432
+    type(Block_t), intent(inout) :: blk
+    integer(int64), intent(in) :: id
+    call bcfd_call(blk, c_tag_move, 'tagging_th_move')
+  end subroutine
+  subroutine selectiveRetagging_th(blk)             ! src/Search.F90:520-651
+    type(Block_t), intent(inout) :: blk
+    call bcfd_call(blk, c_retag, 'selectiveRetagging_th')
+  end subroutine
+  subroutine cellCount_solid(blk, g)                ! src/Search.F90:653-741
+    type(Block_t), intent(inout) :: blk
+    integer(int64), intent(in) :: g
+    ! main.F90 has cleared blk_mv_tag on the host by now
+    call bcfd_ensure(blk)
+    call bcfd_check(bcfd_block_set_flags(blk%bcfd, -1_c_int64_t, int(blk%blk_mv_tag, c_int64_t)), 'set_flags')
+    call bcfd_call(blk, c_count, 'cellCount_solid')
+  end subroutine
+  subroutine computeNormDistance(blk)               ! src/Search.F90:743-861
+    type(Block_t), intent(inout) :: blk
+    ! main.F90 has cleared move_check on the host by now
+    call bcfd_ensure(blk)
+    call bcfd_check(bcfd_block_set_flags(blk%bcfd, blk%move_check, -1_c_int64_t), 'set_flags')
+    call bcfd_call(blk, c_nd, 'computeNormDistance')
+  end subroutine
+  subroutine findTScells(blk)                       ! src/Search.F90:434-518
+    type(Block_t), intent(inout) :: blk
+    call bcfd_call(blk, c_ts, 'findTScells')
+  end subroutine
+end module biocfd_search

@@ -107,7 +107,8 @@ int bcfd_block_set_sor_iter(bcfd_handle h, int64_t n_iter);
 /* named host read-back of any other device array, in the reference layout:
  * "pc", "b", "xcent", ..., "pNormDis", "nelp", "p_ghost", "fluidIndexPtr",
  * "interceptedIndexPtr", "solidIndexPtr", "redCellIndexPtr", "TSIndexPtr",
- * "index_ts", "Acx", "ca_uu", ...  (reals as double, integers as int64);
+ * "index_ts", "Acx", "ca_uu", "x1", "xnode1", "xdot", ..., "mk", "move_check",
+ * "blk_mv_tag", "move_amtx", ...  (reals as double, integers as int64);
  * n = capacity in elements, *written = elements written */
 int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64_t* written);
 
@@ -273,11 +274,12 @@ int bcfd_block_move_stage(int64_t* moved);
  * and refilled from the coarse block (fineUpdate_mv, fineUpdate_bd_mv) */
 int bcfd_tagging_th_move(bcfd_handle h);
 /* Discrete adjoint of n_steps whole time steps (no counterpart in the
- * reference).  Scope: one registered block with the domain BCs, no
- * interfaces, FP64 drop-in steps (cfg->precision 0), with or without a
- * stationary immersed body.  Runs the steps forward from the block's state
- * with ut,vt,wt = u,v,w, checkpointing (u,v,w,p,ut,vt,wt) every `every` steps
- * in HBM, and returns
+ * reference).  Scope: block 1 with the domain BCs plus fine blocks coupled to
+ * it by interfaces, FP64 drop-in steps (cfg->precision 0), stationary immersed
+ * bodies without thin-surface cells (BCFD_E_STATE for body motion).  The
+ * objective and the returned gradients refer to block h.  Runs the steps
+ * forward from the blocks' state with ut,vt,wt = u,v,w, checkpointing
+ * (u,v,w,p,ut,vt,wt of every block) every `every` steps in HBM, and returns
  *   J = (1/N) sum_{n=1..N} ( <W, x^n> + sum_t stress_seed[t] * C_t(x^n) )
  * for natural-layout weights W = (wu,wv,ww,wp) over (u,v,w,p) and, when
  * stress_seed (4 values) is non-null, the drag/lift coefficients C_t of
@@ -291,7 +293,7 @@ int bcfd_tagging_th_move(bcfd_handle h);
  * the forcing and in the coefficients); the
  * adjoint Poisson solves run to max|r - A^T y| <= adj_tol (at most adj_itmax
  * iterations).  The tags must not change during the run (BCFD_E_STATE
- * otherwise).  The block is left at the forward run's final state. */
+ * otherwise).  The blocks are left at the forward run's final state. */
 int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps, int64_t every, const double* wu,
                      const double* wv, const double* ww, const double* wp, const double* stress_seed, double mu_f,
                      double rho_f, double adj_tol, int64_t adj_itmax, double* J, double* dj_duc,

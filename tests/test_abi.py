@@ -41,3 +41,16 @@ def test_step_config_layout_matches_header():
     from biocfd._lib import StepConfig
     # deltat, re, uc, epsi (4 doubles) + pc_ita_max + precision(int, padded) + div_tol + use_graph
     assert C.sizeof(StepConfig) == 8 * 4 + 8 + 8 + 8 + 8
+
+
+def test_fortran_shim_binds_only_declared_symbols():
+    """Every C name the Fortran shim binds (bind(C, name=...)) is declared in
+    the header, so the shim links against the library's exports."""
+    shim = (ROOT / "bio-cfd_gb300" / "fortran" / "biocfd_gb300_shim.f90").read_text()
+    bound = sorted(set(re.findall(r'name="(bcfd_[a-z0-9_]+)"', shim)))
+    assert len(bound) > 30
+    missing = [s for s in bound if s not in declared_symbols()]
+    assert not missing, missing
+    # the Search module carries the fine-block move sequence of app/main.F90
+    for routine in ("block_move_check", "tagging_th_move", "selectiveRetagging_th", "computeSurfaceVariables"):
+        assert re.search(rf"subroutine {routine}\b", shim), routine

@@ -315,6 +315,39 @@ def twelve_block(torch, local, steps=10, warmup=3, fp64_steps=2, moving=False):
     return out
 
 
+def adjoint_bench(torch, local, steps=4, every=2):
+    """Discrete adjoint of whole FP64 steps on the 64^3 sphere block (D = 0.25,
+    Re 100): time per step of forward + checkpointed reverse pass for the
+    objective "time-averaged drag + lift coefficients", with the adjoint
+    Poisson solves in FP64 SOR and in FP32 sweeps + FP64 defect correction
+    (both to the same FP64 residual)."""
+    import time
+    from biocfd import synth
+    from biocfd.adjoint import adjoint_run
+    from biocfd.solver import Solver
+    case = synth.sphere_single_block(n=64, n_steps=steps + 2)
+    out = {"workload": f"64^3 sphere block (D=0.25, Re 100), {steps} FP64 steps, checkpoint every {every}, "
+                       "objective mean of drag + lift coefficients, gradients in uc, u,v,w,p^0 and the "
+                       "body's kinematic scalars", "adj_tol": 1e-13}
+    for key, prec in (("adjoint_fp64_solves", 0), ("adjoint_mixed_solves", 1)):
+        s = Solver(case, device=local)
+        s.setup()
+        s.run(1)  # the per-step re-Search settles the tags of the set-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        J, duc, g = adjoint_run(s, {}, steps, every=every, stress_seed=(1.0, 1.0, 0.0, 0.0),
+                                mu_f=1.0 / case.re, rho_f=1.0, adj_tol=1e-13, solve_precision=prec)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        out[key] = {"ms_per_step": 1000.0 * secs / steps, "J": J, "dJ_duc": duc}
+        s.close()
+    out["speedup_mixed_solves"] = (out["adjoint_fp64_solves"]["ms_per_step"] /
+                                   out["adjoint_mixed_solves"]["ms_per_step"])
+    out["dJ_duc_rel_diff"] = abs(out["adjoint_fp64_solves"]["dJ_duc"] - out["adjoint_mixed_solves"]["dJ_duc"]) / \
+        abs(out["adjoint_fp64_solves"]["dJ_duc"])
+    return out
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -433,6 +466,8 @@ def run_gpu(args):
     if not args.no_twelve_block:
         line["twelve_block"] = twelve_block(torch, local)
         line["twelve_block_moving"] = twelve_block(torch, local, steps=5, fp64_steps=1, moving=True)
+    if not args.no_adjoint:
+        line["adjoint"] = adjoint_bench(torch, local)
     if rank == 0 and not args.no_cpu_baseline:
         sps, secs = oracle_steps(case, 1)
         line["cpu_baseline"] = {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
@@ -451,6 +486,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-sweep-roofline", action="store_true")
     ap.add_argument("--no-twelve-block", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint timing")
     ap.add_argument("--twelve-only", action="store_true",
                     help="only the twelve-block measurement (batched vs per-block launches)")
     ap.add_argument("--mixed-only", action="store_true",
@@ -458,6 +495,11 @@ def main():
     ap.add_argument("--sweep-only", default="",
                     help="nx,ny,nz[,fp32_pairs[,fp64_pairs]]: only the Poisson sweep measurement on that block")
     args = ap.parse_args()
+    if args.adjoint_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(adjoint_bench(torch, 0)), flush=True)
+        return
     if args.twelve_only:
         import torch
         print(json.dumps(twelve_block(torch, 0, args.steps, args.warmup)), flush=True)

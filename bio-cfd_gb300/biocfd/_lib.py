@@ -42,6 +42,7 @@ _SIGS = {
     "bcfd_block_set_mixed_params": [c_i64, c_i64, c_double, c_int],
     "bcfd_block_set_solve_launch": [c_i64, c_int, c_int, c_int],
     "bcfd_set_batching": [c_int],
+    "bcfd_adjoint_set_solver": [c_int],
     "bcfd_poisson_solve_zero_bc": [c_i64, P_d, P_d, c_double, c_i64],
     "bcfd_poisson_solve_adjoint": [c_i64, P_d, P_d, c_double, c_i64],
     "bcfd_coupling_apply": [c_i64, c_int, c_int, P_d, P_d],

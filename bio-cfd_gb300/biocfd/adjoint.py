@@ -89,7 +89,7 @@ def momentum_adjoint(solver, g: int, utb, vtb, wtb, dt: float | None = None, re:
 
 def adjoint_run(solver, weights: dict, n_steps: int, every: int = 20, uc: float | None = None,
                 gradient: bool = True, adj_tol: float = 1e-13, adj_itmax: int = 200000,
-                stress_seed=None, mu_f: float = 1.0, rho_f: float = 1.0):
+                stress_seed=None, mu_f: float = 1.0, rho_f: float = 1.0, solve_precision: int | None = None):
     """Discrete adjoint of n_steps FP64 time steps of the solver's single
     block (domain BCs, optionally a stationary body), checkpointing every
     `every` steps.
@@ -102,10 +102,14 @@ def adjoint_run(solver, weights: dict, n_steps: int, every: int = 20, uc: float 
     "kin": dJ/d(xdot, ydot, yddot, thetaDot1, thetaDDot1, thetaDot2,
     thetaDDot2, alphaDot)} with the body's kinematic scalars constant and its
     geometry fixed).  The block advances by n_steps, exactly as
-    solver.run(n_steps) would."""
+    solver.run(n_steps) would.  `solve_precision` selects the adjoint Poisson
+    solver (0 FP64 SOR, 1 FP32 sweeps with FP64 defect correction; both to
+    adj_tol), None keeps the library's setting."""
     c = solver.case
     g = solver.handles[0]
     shape = c.blocks[0].shape
+    if solve_precision is not None:
+        check(solver.L.bcfd_adjoint_set_solver(int(solve_precision)), "adjoint_set_solver")
     W = [np.asfortranarray(weights.get(k, np.zeros(shape)), dtype=np.float64) for k in ("u", "v", "w", "p")]
     cfg = solver.config(0)
     if uc is not None:

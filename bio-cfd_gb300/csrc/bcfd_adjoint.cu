@@ -30,14 +30,18 @@ std::vector<double> transpose_line(const std::vector<double>& A, int n) {
 
 }  // namespace
 
-// x = A^{-1} r (or A^{-T} r) on the fluid cells, device natural-layout arrays
+// x = A^{-1} r (or A^{-T} r) on the fluid cells, device natural-layout arrays,
+// to max|r - A x| <= tol: FP64 SOR, or (lib().adj_precision == 1) FP32 SOR
+// sweeps with FP64 defect correction to the same FP64 residual target
 int solve_zero_bc_dev(HostBlock* hb, const double* r, double* x, double tol, int64_t itmax, bool transpose) {
   DevBlock& D = hb->d;
   const Dims& d = D.d;
   if (!D.Acx || hb->Acx.empty()) return BCFD_E_STATE;
-  const double* keep[3] = {D.Acx, D.Acy, D.Acz};
+  const bool mixed = lib().adj_precision == 1;
+  const DevBlock keep = D;
   const int keep_rev = hb->sor_rev;
   double* tab = nullptr;
+  float* tabf = nullptr;
   int rc = 0;
   if (transpose) {
     const std::vector<double> tx = transpose_line(hb->Acx, d.nx), ty = transpose_line(hb->Acy, d.ny),
@@ -51,6 +55,23 @@ int solve_zero_bc_dev(HostBlock* hb, const double* r, double* x, double tol, int
     D.Acy = tab + tx.size();
     D.Acz = tab + tx.size() + ty.size();
     hb->sor_rev = 1;
+    if (mixed && !rc) {
+      // the FP32 line and sweep tables of the transposed operator
+      std::vector<float> f;
+      for (double v : all) f.push_back((float)v);
+      size_t ox, oy, oz;
+      append_sweep_tables(d, tx, ty, tz, f, &ox, &oy, &oz);
+      if (cudaMalloc(&tabf, f.size() * sizeof(float)) != cudaSuccess) rc = BCFD_E_NOMEM;
+      if (!rc && h2d(tabf, f.data(), f.size() * sizeof(float)) != cudaSuccess) rc = BCFD_E_CUDA;
+      if (!rc) {
+        D.Acxf = tabf;
+        D.Acyf = tabf + tx.size();
+        D.Aczf = tabf + tx.size() + ty.size();
+        D.axr = reinterpret_cast<const float4*>(tabf + ox);
+        D.ayr = reinterpret_cast<const float4*>(tabf + oy);
+        D.azr = reinterpret_cast<const float4*>(tabf + oz);
+      }
+    }
   }
   const size_t pbytes = (size_t)d.npacked() * sizeof(double);
   for (int c = 0; c < 2 && !rc; ++c) {
@@ -59,15 +80,22 @@ int solve_zero_bc_dev(HostBlock* hb, const double* r, double* x, double tol, int
   }
   if (!rc && cudaMemsetAsync(&D.stats->niter, 0, sizeof(int64_t), stream()) != cudaSuccess) rc = BCFD_E_CUDA;
   if (!rc) rc = launch_pack(hb, r, D.bpk);
-  // residual-target FP64 solve of A x = r (deltat = 1)
-  if (!rc) rc = launch_sor(hb, itmax, 1.0, 0.0, tol);
+  // residual-target solve of A x = r (deltat = 1)
+  if (!rc) rc = mixed ? launch_sor_mixed(hb, itmax, 1.0, tol) : launch_sor(hb, itmax, 1.0, 0.0, tol);
   if (!rc) rc = launch_unpack(hb, D.pc, x);
   if (!rc && cudaStreamSynchronize(stream()) != cudaSuccess) rc = BCFD_E_CUDA;
-  D.Acx = keep[0];
-  D.Acy = keep[1];
-  D.Acz = keep[2];
+  D.Acx = keep.Acx;
+  D.Acy = keep.Acy;
+  D.Acz = keep.Acz;
+  D.Acxf = keep.Acxf;
+  D.Acyf = keep.Acyf;
+  D.Aczf = keep.Aczf;
+  D.axr = keep.axr;
+  D.ayr = keep.ayr;
+  D.azr = keep.azr;
   hb->sor_rev = keep_rev;
   cudaFree(tab);
+  cudaFree(tabf);
   if (rc) return rc;
   return take_block_error(hb);
 }
@@ -92,6 +120,13 @@ int solve_zero_bc(HostBlock* hb, const double* r, double* x, double tol, int64_t
 using namespace bcfd;
 
 extern "C" {
+
+int bcfd_adjoint_set_solver(int precision) {
+  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  if (precision != 0 && precision != 1) return BCFD_E_ARG;
+  lib().adj_precision = precision;
+  return 0;
+}
 
 int bcfd_poisson_solve_zero_bc(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax) {
   std::lock_guard<std::recursive_mutex> lk(lib().mu);

@@ -128,6 +128,30 @@ int take_block_error(HostBlock* hb) {
   return e;
 }
 
+// The FP32 sweep tables of line tables Ax/Ay/Az (n,3): the x coefficients
+// per float4 run and x-parity, then one float4 (3 coefficients + 0) per y row
+// and per z row; 16-byte aligned offsets into f
+void append_sweep_tables(const Dims& d, const std::vector<double>& Ax, const std::vector<double>& Ay,
+                         const std::vector<double>& Az, std::vector<float>& f, size_t* axr_off, size_t* ayr_off,
+                         size_t* azr_off) {
+  while (f.size() % 4) f.push_back(0.0f);
+  *axr_off = f.size();
+  const int nx = d.nx, nq = d.NXH / 4;
+  for (int par = 0; par < 2; ++par)
+    for (int col = 0; col < 3; ++col)
+      for (int run = 0; run < nq; ++run)
+        for (int u = 0; u < 4; ++u) {
+          const int ic = std::min(std::max(2 * (4 * run + u) + 1 + par, 2), nx + 1);
+          f.push_back((float)Ax[(size_t)(ic - 2) + (size_t)col * nx]);
+        }
+  *ayr_off = f.size();
+  for (int j = 0; j < d.ny; ++j)
+    for (int col = 0; col < 4; ++col) f.push_back(col < 3 ? (float)Ay[(size_t)j + (size_t)col * d.ny] : 0.0f);
+  *azr_off = f.size();
+  for (int k = 0; k < d.nz; ++k)
+    for (int col = 0; col < 4; ++col) f.push_back(col < 3 ? (float)Az[(size_t)k + (size_t)col * d.nz] : 0.0f);
+}
+
 namespace {
 
 template <class T>
@@ -382,27 +406,8 @@ int upload_coefs(HostBlock* hb) {
       foff.push_back(f.size());
       for (double x : (t < N_TAB ? hb->ca[t] : hb->ck[t - N_TAB])) f.push_back((float)x);
     }
-    // the x coefficients per float4 run and x-parity, 16-byte aligned
-    while (f.size() % 4) f.push_back(0.0f);
-    const size_t axr_off = f.size();
-    {
-      const int nx = hb->d.d.nx, nq = hb->d.d.NXH / 4;
-      for (int par = 0; par < 2; ++par)
-        for (int col = 0; col < 3; ++col)
-          for (int run = 0; run < nq; ++run)
-            for (int u = 0; u < 4; ++u) {
-              const int ic = std::min(std::max(2 * (4 * run + u) + 1 + par, 2), nx + 1);
-              f.push_back((float)hb->Acx[(size_t)(ic - 2) + (size_t)col * nx]);
-            }
-    }
-    const size_t ayr_off = f.size();
-    for (int j = 0; j < hb->d.d.ny; ++j)
-      for (int col = 0; col < 4; ++col)
-        f.push_back(col < 3 ? (float)hb->Acy[(size_t)j + (size_t)col * hb->d.d.ny] : 0.0f);
-    const size_t azr_off = f.size();
-    for (int k = 0; k < hb->d.d.nz; ++k)
-      for (int col = 0; col < 4; ++col)
-        f.push_back(col < 3 ? (float)hb->Acz[(size_t)k + (size_t)col * hb->d.d.nz] : 0.0f);
+    size_t axr_off, ayr_off, azr_off;
+    append_sweep_tables(hb->d.d, hb->Acx, hb->Acy, hb->Acz, f, &axr_off, &ayr_off, &azr_off);
     if (hb->coef_f32) {
       cudaFree(hb->coef_f32);
       hb->allocs.erase(std::remove(hb->allocs.begin(), hb->allocs.end(), (void*)hb->coef_f32), hb->allocs.end());

@@ -166,6 +166,7 @@ struct Lib {
   cudaGraphExec_t step_graph = nullptr;
   std::vector<unsigned char> step_key;  // what the capture depends on
   std::vector<unsigned char> eager_key; // the key left by the last eager step
+  int adj_precision = 1;  // zero-BC and adjoint solves: 0 FP64 SOR, 1 FP32 sweeps + FP64 correction
   int64_t step_kernels = 0;              // kernels in the captured step
 };
 
@@ -278,6 +279,10 @@ int apply_surface_variables(HostBlock* hb);
 void staged_node(const HostBlock* hb, int64_t node, double* x, double* y, double* z);
 // the device kinematics from the host copy (set_kinematics, set-up)
 int upload_kin(HostBlock* hb);
+// bcfd_api.cu: the FP32 sweep tables (axr | ayr | azr) of three line tables
+void append_sweep_tables(const Dims& d, const std::vector<double>& Ax, const std::vector<double>& Ay,
+                         const std::vector<double>& Az, std::vector<float>& f, size_t* axr_off, size_t* ayr_off,
+                         size_t* azr_off);
 // k_search.cu: the search origin/radius for the block's current grid and
 // node bound, recorded as the device's value (the caller puts it there)
 int search_origin_stage(HostBlock* hb, float h[4], float** dev);

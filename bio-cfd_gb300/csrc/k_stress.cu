@@ -176,31 +176,47 @@ __global__ void k_stress_coef(DevBlock B, double mu_f, double rho_f, const doubl
   }
 }
 
-// gk[p] += d/d(kinematic scalar p) of sum_t scale[t] * sum_e term_t(e) at
-// the current fields (the terms are affine in the fields and at most quadratic
-// in each scalar); one thread, element order
-__global__ void k_stress_kin(DevBlock B, double mu_f, double rho_f, const double* scale, double* gk) {
-  if (blockIdx.x || threadIdx.x) return;
+// part[8e + p] = d/d(kinematic scalar p) of sum_t scale[t] * term_t(e) at the
+// current fields (the terms are affine in the fields and at most quadratic in
+// each scalar, so the central difference with unit steps is exact)
+__global__ void k_stress_kin_elem(DevBlock B, double mu_f, double rho_f, const double* scale, double* part) {
   const double* arr[4] = {B.u, B.v, B.w, B.p};
-  for (int p = 0; p < 8; ++p) {
-    Kin kp = *B.kin, km = *B.kin;
-    kin_scalar(kp, p) += 1.0;
-    kin_scalar(km, p) -= 1.0;
-    DevBlock Bp = B, Bm = B;
-    Bp.kin = &kp;
-    Bm.kin = &km;
-    double acc = 0.0;
-    for (int e = 0; e < B.ne; ++e) {
-      const ElemStencil S = elem_stencil(B, e);
-      double f[4][8];
-      for (int c = 0; c < 4; ++c)
-        for (int q = 0; q < 8; ++q) f[c][q] = arr[c][S.pos[c][q]];
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B.ne; e += gridDim.x * blockDim.x) {
+    const ElemStencil S = elem_stencil(B, e);
+    double f[4][8];
+    for (int c = 0; c < 4; ++c)
+      for (int q = 0; q < 8; ++q) f[c][q] = arr[c][S.pos[c][q]];
+    for (int p = 0; p < 8; ++p) {
+      Kin kp = *B.kin, km = *B.kin;
+      kin_scalar(kp, p) += 1.0;
+      kin_scalar(km, p) -= 1.0;
+      DevBlock Bp = B, Bm = B;
+      Bp.kin = &kp;
+      Bm.kin = &km;
       double op[7], om[7];
       elem_terms(Bp, e, mu_f, rho_f, S, f, op);
       elem_terms(Bm, e, mu_f, rho_f, S, f, om);
+      double acc = 0.0;
       for (int t = 0; t < 4; ++t) acc += scale[t] * 0.5 * (op[t] - om[t]);
+      part[8 * (int64_t)e + p] = acc;
     }
-    gk[p] += acc;
+  }
+}
+
+// gk[p] += sum_e part[8e + p]: fixed-order reduction by one CTA of 256 threads
+__global__ void k_stress_kin_sum(const double* part, int ne, double* gk) {
+  __shared__ double s[256];
+  for (int p = 0; p < 8; ++p) {
+    double acc = 0.0;
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) acc += part[8 * (int64_t)e + p];
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+      if ((int)threadIdx.x < h) s[threadIdx.x] += s[threadIdx.x + h];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) gk[p] += s[0];
+    __syncthreads();
   }
 }
 
@@ -276,13 +292,16 @@ int launch_stress_weights(HostBlock* hb, double mu_f, double rho_f, const double
 }
 
 // gk[8] += the kinematic derivative of sum_t seed[t] * coefficient t at the
-// block's current fields; scratch: 8 doubles
+// block's current fields; scratch: 8 + 8 ne doubles
 int launch_stress_kin(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double* gk,
                       double* scratch) {
   if (hb->d.ne <= 0) return BCFD_E_STATE;
   k_stress_scale<<<1, 32, 0, stream()>>>(hb->d, seed_dev, scratch);
   TRY_R(note_launch());
-  k_stress_kin<<<1, 32, 0, stream()>>>(hb->d, mu_f, rho_f, scratch, gk);
+  // per-element partials after the 8 scale slots (the scratch holds 8 + 64 ne doubles)
+  k_stress_kin_elem<<<grid_for(hb->d.ne, 128), 128, 0, stream()>>>(hb->d, mu_f, rho_f, scratch, scratch + 8);
+  TRY_R(note_launch());
+  k_stress_kin_sum<<<1, 256, 0, stream()>>>(scratch + 8, hb->d.ne, gk);
   TRY_R(note_launch());
   return 0;
 }

@@ -196,6 +196,11 @@ int bcfd_fine_update_mv(bcfd_handle it);       /* src/FineInterp.f90:10-281     
  * The adjoint runs the same solve kernel with the transposed line tables of
  * A and the colour sweeps in reverse order.  They use the block's Poisson
  * arrays as scratch (call between time steps). */
+/* the solver of bcfd_poisson_solve_zero_bc / _adjoint and of the adjoint
+ * solves in bcfd_adjoint_run (no counterpart in the reference): 0 FP64 SOR,
+ * 1 (default) FP32 red-black sweeps with FP64 defect correction; both stop at
+ * the same FP64 residual target */
+int bcfd_adjoint_set_solver(int precision);
 int bcfd_poisson_solve_zero_bc(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax);
 int bcfd_poisson_solve_adjoint(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax);
 /* tangent-linear model of nsMomentum2order (no counterpart in the reference):

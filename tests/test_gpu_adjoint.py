@@ -62,8 +62,11 @@ def _interior(spec, rng):
     return r
 
 
-def test_adjoint_solve_against_dense_transpose():
+@pytest.mark.parametrize("precision", [0, 1])
+def test_adjoint_solve_against_dense_transpose(precision):
+    # 0: FP64 SOR; 1: FP32 sweeps (transposed FP32 tables) + FP64 correction
     s, g, spec = _block(6, 5, 4)
+    s.L.bcfd_adjoint_set_solver(precision)
     A = _dense(s, g, spec)
     assert np.abs(A - A.T).max() > 1e-3 * np.abs(A).max()  # genuinely non-symmetric
     rng = np.random.default_rng(11)
@@ -74,6 +77,7 @@ def test_adjoint_solve_against_dense_transpose():
     xr, yr = np.linalg.solve(A, rv), np.linalg.solve(A.T, rv)
     assert np.linalg.norm(x - xr) <= 1e-9 * np.linalg.norm(xr)
     assert np.linalg.norm(y - yr) <= 1e-9 * np.linalg.norm(yr)
+    s.L.bcfd_adjoint_set_solver(1)
     s.close()
 
 

@@ -329,3 +329,18 @@ def test_two_block_checkpoint_spacing_does_not_change_the_gradient():
     assert J0 == J1 and d0 == d1
     for k in g0:
         np.testing.assert_array_equal(g0[k], g1[k])
+
+
+def test_adjoint_solver_precision_agrees():
+    """The adjoint Poisson solves in FP64 SOR and in FP32 sweeps with FP64
+    defect correction stop at the same FP64 residual target, so the
+    gradients agree far inside the finite-difference bar."""
+    case = _sphere_case()
+    out = [_drag_run(_sphere_solver(case), case, solve_precision=sp) for sp in (0, 1)]
+    (j0, d0, g0), (j1, d1, g1) = out
+    assert j0 == j1  # the forward steps are the same FP64 steps
+    assert abs(d0 - d1) <= 1e-8 * abs(d0), (d0, d1)
+    for k in ("u", "v", "w", "p"):
+        n = np.linalg.norm(g0[k])
+        assert np.linalg.norm(g1[k] - g0[k]) <= 1e-8 * max(n, 1e-30), k
+    assert np.allclose(g0["kin"], g1["kin"], rtol=1e-8, atol=1e-12 * np.abs(g0["kin"]).max())

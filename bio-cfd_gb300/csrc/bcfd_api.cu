@@ -750,6 +750,48 @@ int bcfd_block_set_surface(bcfd_handle h, int64_t n_elems, int64_t n_nodes, cons
     BCFD_CUDA(cudaMemcpyAsync((void*)hb->d.elp1, ids.data(), ids.size() * sizeof(int), cudaMemcpyHostToDevice, stream()));
   hb->elem_host = ids;
   hb->has_body = n_elems > 0;
+  // the search's element order: Morton order of the centroids (30-bit code
+  // on the centroids' bounding box, ties by index), so that runs of 32
+  // consecutive elements are spatially compact; only the pruning of the
+  // nearest-element queries depends on it, never a result
+  {
+    std::vector<double> cx((size_t)n_elems), cy((size_t)n_elems), cz((size_t)n_elems);
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300};
+    for (int64_t e = 0; e < n_elems; ++e) {
+      const int64_t a0 = elp1[e] - 1, a1 = elp2[e] - 1, a2 = elp3[e] - 1;
+      cx[e] = (xnode1[a0] + xnode1[a1] + xnode1[a2]) / 3.0;
+      cy[e] = (ynode1[a0] + ynode1[a1] + ynode1[a2]) / 3.0;
+      cz[e] = (znode1[a0] + znode1[a1] + znode1[a2]) / 3.0;
+      const double c3[3] = {cx[e], cy[e], cz[e]};
+      for (int q = 0; q < 3; ++q) {
+        lo[q] = std::min(lo[q], c3[q]);
+        hi[q] = std::max(hi[q], c3[q]);
+      }
+    }
+    auto spread = [](uint32_t v) {  // 10 bits -> every third bit
+      v &= 0x3ffu;
+      v = (v | (v << 16)) & 0x30000ffu;
+      v = (v | (v << 8)) & 0x300f00fu;
+      v = (v | (v << 4)) & 0x30c30c3u;
+      v = (v | (v << 2)) & 0x9249249u;
+      return v;
+    };
+    std::vector<std::pair<uint32_t, int>> key((size_t)n_elems);
+    for (int64_t e = 0; e < n_elems; ++e) {
+      const double c3[3] = {cx[e], cy[e], cz[e]};
+      uint32_t g[3];
+      for (int q = 0; q < 3; ++q) {
+        const double span = hi[q] - lo[q];
+        const double t = span > 0.0 ? (c3[q] - lo[q]) / span : 0.0;
+        g[q] = (uint32_t)std::min(1023.0, std::max(0.0, std::floor(t * 1023.0)));
+      }
+      key[(size_t)e] = {spread(g[0]) | (spread(g[1]) << 1) | (spread(g[2]) << 2), (int)e};
+    }
+    std::sort(key.begin(), key.end());
+    hb->elem_perm.resize((size_t)n_elems);
+    for (int64_t q = 0; q < n_elems; ++q) hb->elem_perm[(size_t)q] = key[(size_t)q].second;
+    hb->elem_perm_gen++;
+  }
   BCFD_CUDA(cudaStreamSynchronize(stream()));
   // findDistnode (src/Search.F90:21-47) on the nodes as given, with the node
   // tags readSurfaceMeshGmsh derives from the elements (51/52 first, then 50):

@@ -69,6 +69,8 @@ struct HostBlock {
   std::vector<double> node0[3];
   std::vector<int8_t> node_id_host;
   std::vector<int> elem_host;      // elp1 | elp2 | elp3 | surf_id, as uploaded
+  std::vector<int> elem_perm;      // search order -> element index (Morton order of the centroids)
+  int elem_perm_gen = 0;           // bumped when elem_perm changes
   DevBlock d{};
   std::vector<void*> allocs;  // device allocations owned by the block
   // host copies of the 1-D grids (1-based meaning, v[i-1])

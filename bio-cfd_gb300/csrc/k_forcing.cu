@@ -9,9 +9,10 @@
 //   * for every stencil point the task finds the latest task before it that
 //     writes that point (a u point u(a,b,c) is written by the U2 task of cell
 //     (a,b,c) and the U1 task of cell (a+1,b,c), the later one winning);
-//   * tasks are levelled (level = 1 + max level of their dependencies) and
-//     evaluated level by level, reading each stencil value either from the
-//     unmodified array or from the dependency's output slot;
+//   * tasks are evaluated in rounds: in each round every task whose
+//     dependencies finished in earlier rounds runs, reading each stencil
+//     value either from the unmodified array or from the dependency's output
+//     slot (rounds = dependency depth + 1, one grid barrier each);
 //   * last writers scatter their outputs into the array at the end.
 // Everything runs in one cooperative launch with bounded grid barriers.  The
 // Field / Ghost velocity variants read ut and write u (or ghost arrays) and
@@ -255,8 +256,8 @@ __device__ __forceinline__ double* comp_array(const DevBlock& B, int axis, bool 
 struct DagScratch {
   double* out;    // per task output
   int* dep;       // per task 8 dependency task ids (-1: read the array)
-  int* level;     // per task level
-  int* flag;      // [0..1] changed flags, [2] max level, [3] rounds
+  int* level;     // per task: the round it finished in (0: not yet)
+  int* flag;      // [0..2] "work left" flags of the rounds
 };
 
 struct DagArgs {
@@ -302,54 +303,38 @@ __global__ void __launch_bounds__(256) k_forcing_dag(DevBlock B, DagArgs g, DagS
   for (int t = tid; t < nt; t += nthr) {
     const int n = g.vel ? t / 6 : t, comp = g.vel ? t % 6 : -1;
     const Probe P = make_probe(B, g.mode, comp, n);
-    int lv = 0;
 #pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int w = last_writer(B, g, P.axis, P.ii + (q & 1), P.jj + ((q >> 1) & 1), P.kk + (q >> 2), t);
-      s.dep[8 * t + q] = w;
-      if (w >= 0) lv = 1;
-    }
-    s.level[t] = lv;
+    for (int q = 0; q < 8; ++q)
+      s.dep[8 * t + q] = last_writer(B, g, P.axis, P.ii + (q & 1), P.jj + ((q >> 1) & 1), P.kk + (q >> 2), t);
+    s.level[t] = 0;
   }
   if (!grid_sync(gb)) return;
-  // phase 2: levels by monotone relaxation (bounded by the task count)
+  // phase 2: evaluate in rounds: in round r every task whose dependencies all
+  // finished in earlier rounds computes its output (done = r + 1).  A task
+  // finishes in round (its level), so the rounds are the dependency depth
+  // plus one, one grid barrier each; the "work left" flag is triple-buffered
+  // (set in round r, read after its barrier, cleared for round r + 2).
+  int* done = s.level;
   for (int round = 0;; ++round) {
-    __shared__ int s_changed;
-    if (threadIdx.x == 0) s_changed = 0;
+    __shared__ int s_left;
+    if (threadIdx.x == 0) s_left = 0;
     __syncthreads();
-    int changed = 0, mx = 0;
+    int left = 0;
     for (int t = tid; t < nt; t += nthr) {
-      int lv = 0;
+      if (__ldcg(done + t) != 0) continue;
+      bool can = true;
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const int w = s.dep[8 * t + q];
-        if (w >= 0) lv = max(lv, __ldcg(s.level + w) + 1);
+        if (w >= 0) {
+          const int dw = __ldcg(done + w);
+          if (dw == 0 || dw > round) can = false;
+        }
       }
-      if (lv != __ldcg(s.level + t)) {
-        __stcg(s.level + t, lv);
-        changed = 1;
+      if (!can) {
+        left = 1;
+        continue;
       }
-      mx = max(mx, lv);
-    }
-    if (changed) atomicOr(&s_changed, 1);
-    if (mx) atomicMax(&s.flag[2], mx);
-    __syncthreads();
-    if (threadIdx.x == 0 && s_changed) atomicOr(&s.flag[round & 1], 1);
-    if (!grid_sync(gb)) return;
-    const int any = *((volatile int*)&s.flag[round & 1]);
-    if (blockIdx.x == 0 && threadIdx.x == 0) s.flag[(round + 1) & 1] = 0;
-    if (!any) break;
-    if (round > nt + 2) {  // cannot happen for a DAG; guard the loop anyway
-      if (threadIdx.x == 0) set_err(B.err, BCFD_E_TIMEOUT);
-      return;
-    }
-    if (!grid_sync(gb)) return;
-  }
-  const int maxl = *((volatile int*)&s.flag[2]);
-  // phase 3: evaluate level by level
-  for (int L = 0; L <= maxl; ++L) {
-    for (int t = tid; t < nt; t += nthr) {
-      if (__ldcg(s.level + t) != L) continue;
       const int n = g.vel ? t / 6 : t, comp = g.vel ? t % 6 : -1;
       const Probe P = make_probe(B, g.mode, comp, n);
       const double* arr = comp_array(B, P.axis, g.vel != 0);
@@ -361,8 +346,19 @@ __global__ void __launch_bounds__(256) k_forcing_dag(DevBlock B, DagArgs g, DagS
                       : arr[B.d.idx(P.ii + (q & 1), P.jj + ((q >> 1) & 1), P.kk + (q >> 2))];
       }
       __stcg(s.out + t, reconstruct(B, g.mode, comp, P, f));
+      __stcg(done + t, round + 1);
     }
+    if (left) atomicOr(&s_left, 1);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_left) atomicOr(&s.flag[round % 3], 1);
     if (!grid_sync(gb)) return;
+    const int any = *((volatile int*)&s.flag[round % 3]);
+    if (blockIdx.x == 0 && threadIdx.x == 0) s.flag[(round + 2) % 3] = 0;
+    if (!any) break;
+    if (round > nt + 2) {  // cannot happen for a DAG; guard the loop anyway
+      if (threadIdx.x == 0) set_err(B.err, BCFD_E_TIMEOUT);
+      return;
+    }
   }
   // phase 4: scatter the final values
   for (int t = tid; t < nt; t += nthr) {

@@ -21,16 +21,42 @@ namespace {
 constexpr int kWarps = 8;  // warps per CTA in the query kernels
 
 struct QueryCtx {
-  const float4* cf;  // element centroids relative to origin, FP32
+  const float4* cf;   // element centroids relative to origin, FP32, in search order
+  const int* perm;    // search order -> element index
+  const float4* box;  // per chunk of 32 search positions: lo, hi of its FP32 centroids
+  int nch;            // chunks
   const double *xc, *yc, *zc;
   int ne;
   double ox, oy, oz;
-  float R;           // bound on |coordinate - origin| of queries and centroids
+  float R;            // bound on |coordinate - origin| of queries and centroids
 };
+
+constexpr float kFInf = 3.0e38f;
+
+__device__ __forceinline__ float fdist2(float dx, float dy, float dz) {
+  return __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
+}
+
+// lower bound of fdist2(q - e) over the centroids e of a chunk box [lo, hi]:
+// per axis the gap to the box is at most |q - e| in FP32 (rounding is
+// monotone), and the same fused squares and sums keep the order
+__device__ __forceinline__ float box_lb(const float (&q)[3], float4 lo, float4 hi) {
+  const float gx = fmaxf(fmaxf(lo.x - q[0], q[0] - hi.x), 0.0f);
+  const float gy = fmaxf(fmaxf(lo.y - q[1], q[1] - hi.y), 0.0f);
+  const float gz = fmaxf(fmaxf(lo.z - q[2], q[2] - hi.z), 0.0f);
+  return fdist2(gx, gy, gz);
+}
 
 __device__ __forceinline__ double sq3(double a, double b, double c) { return a * a + b * b + c * c; }
 
-// Q simultaneous nearest-element queries by one warp; out[q] = 1-based element
+// Q simultaneous nearest-element queries by one warp; out[q] = 1-based element.
+// Pass 1 finds each query's minimum FP32 distance d_f over all elements,
+// pass 2 re-evaluates in FP64 every element whose FP32 distance lies within
+// a rounding bound of d_f.  Both passes visit only the chunks of 32 elements
+// (search order) whose box lower bound can matter: a skipped chunk's elements
+// have FP32 distances above the running minimum (pass 1) or above the bound
+// (pass 2), so d_f, the candidate set and the FP64 argmin (lowest element
+// index on ties) are exactly those of the brute-force loops.
 template <int Q>
 __device__ void warp_nearest(const QueryCtx& C, const double (&q)[Q][3], int (&out)[Q]) {
   const int lane = threadIdx.x & 31;
@@ -41,30 +67,79 @@ __device__ void warp_nearest(const QueryCtx& C, const double (&q)[Q][3], int (&o
     qf[s][1] = (float)(q[s][1] - C.oy);
     qf[s][2] = (float)(q[s][2] - C.oz);
   }
+  // pass 1, seeds: per query the chunk of least lower bound (lane = chunk)
   float mf[Q];
+  int seed[Q];
 #pragma unroll
-  for (int s = 0; s < Q; ++s) mf[s] = 3.0e38f;
-  for (int m = lane; m < C.ne; m += 32) {
-    const float4 e = __ldg(C.cf + m);
+  for (int s = 0; s < Q; ++s) {
+    mf[s] = kFInf;
+    seed[s] = 0;
+  }
+  for (int cb = 0; cb < C.nch; cb += 32) {
+    const int c = cb + lane;
+    if (c < C.nch) {
+      const float4 lo = __ldg(C.box + 2 * c), hi = __ldg(C.box + 2 * c + 1);
+#pragma unroll
+      for (int s = 0; s < Q; ++s) {
+        const float lb = box_lb(qf[s], lo, hi);
+        if (lb < mf[s]) {
+          mf[s] = lb;
+          seed[s] = c;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < Q; ++s) {
+    float v = mf[s];
+    int c = seed[s];
+    for (int o = 16; o > 0; o >>= 1) {
+      const float ov = __shfl_xor_sync(0xffffffffu, v, o);
+      const int oc = __shfl_xor_sync(0xffffffffu, c, o);
+      if (ov < v || (ov == v && oc < c)) {
+        v = ov;
+        c = oc;
+      }
+    }
+    seed[s] = c;
+    mf[s] = kFInf;
+  }
+  // one chunk: every query's minimum over its elements (warp-uniform result)
+  auto visit1 = [&](int c) {
+    const int pos = 32 * c + lane;
+    float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool in = pos < C.ne;
+    if (in) e = __ldg(C.cf + pos);
 #pragma unroll
     for (int s = 0; s < Q; ++s) {
-      const float dx = qf[s][0] - e.x, dy = qf[s][1] - e.y, dz = qf[s][2] - e.z;
-      const float dd = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-      mf[s] = fminf(mf[s], dd);
+      float v = in ? fdist2(qf[s][0] - e.x, qf[s][1] - e.y, qf[s][2] - e.z) : kFInf;
+      for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+      mf[s] = fminf(mf[s], v);
     }
+  };
+#pragma unroll
+  for (int s = 0; s < Q; ++s) visit1(seed[s]);
+  for (int cb = 0; cb < C.nch; cb += 32) {
+    const int c = cb + lane;
+    bool need = false;
+    if (c < C.nch) {
+      const float4 lo = __ldg(C.box + 2 * c), hi = __ldg(C.box + 2 * c + 1);
+#pragma unroll
+      for (int s = 0; s < Q; ++s) need |= box_lb(qf[s], lo, hi) <= mf[s];
+    }
+    for (unsigned m = __ballot_sync(0xffffffffu, need); m; m &= m - 1) visit1(cb + __ffs(m) - 1);
   }
   float thr[Q];
 #pragma unroll
   for (int s = 0; s < Q; ++s) {
-    float v = mf[s];
-    for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
     // |d_f - d| <= (3.5 R + 4 d) 2^-24 for coordinates rounded to FP32;
     // keep everything within 8x that bound (plus an absolute floor)
-    const float d = sqrtf(v);
+    const float d = sqrtf(mf[s]);
     const float tau = 8.0f * (3.5f * C.R + 4.0f * d + 1e-3f) * 5.9604645e-8f + 1e-12f;
     const float lim = d + 2.0f * tau;
     thr[s] = lim * lim * (1.0f + 1e-6f);
   }
+  // pass 2: FP64 distances of the candidates (lowest index on ties)
   double best[Q];
   int bm[Q];
 #pragma unroll
@@ -72,17 +147,28 @@ __device__ void warp_nearest(const QueryCtx& C, const double (&q)[Q][3], int (&o
     best[s] = 1e300;
     bm[s] = 0x7fffffff;
   }
-  for (int m = lane; m < C.ne; m += 32) {
-    const float4 e = __ldg(C.cf + m);
+  for (int cb = 0; cb < C.nch; cb += 32) {
+    const int c = cb + lane;
+    bool need = false;
+    if (c < C.nch) {
+      const float4 lo = __ldg(C.box + 2 * c), hi = __ldg(C.box + 2 * c + 1);
 #pragma unroll
-    for (int s = 0; s < Q; ++s) {
-      const float dx = qf[s][0] - e.x, dy = qf[s][1] - e.y, dz = qf[s][2] - e.z;
-      const float dd = __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)));
-      if (dd <= thr[s]) {
-        const double d64 = sq3(q[s][0] - __ldg(C.xc + m), q[s][1] - __ldg(C.yc + m), q[s][2] - __ldg(C.zc + m));
-        if (d64 < best[s]) {  // lanes visit m in increasing order: ties keep the lower index
-          best[s] = d64;
-          bm[s] = m;
+      for (int s = 0; s < Q; ++s) need |= box_lb(qf[s], lo, hi) <= thr[s];
+    }
+    for (unsigned msk = __ballot_sync(0xffffffffu, need); msk; msk &= msk - 1) {
+      const int pos = 32 * (cb + __ffs(msk) - 1) + lane;
+      if (pos >= C.ne) continue;
+      const float4 e = __ldg(C.cf + pos);
+      const int m = __ldg(C.perm + pos);
+#pragma unroll
+      for (int s = 0; s < Q; ++s) {
+        const float dd = fdist2(qf[s][0] - e.x, qf[s][1] - e.y, qf[s][2] - e.z);
+        if (dd <= thr[s]) {
+          const double d64 = sq3(q[s][0] - __ldg(C.xc + m), q[s][1] - __ldg(C.yc + m), q[s][2] - __ldg(C.zc + m));
+          if (d64 < best[s] || (d64 == best[s] && m < bm[s])) {
+            best[s] = d64;
+            bm[s] = m;
+          }
         }
       }
     }
@@ -103,9 +189,20 @@ __device__ void warp_nearest(const QueryCtx& C, const double (&q)[Q][3], int (&o
   }
 }
 
-__device__ __forceinline__ QueryCtx qctx(const DevBlock& B, const float4* cf, const float* org) {
+struct SearchView {
+  const float4* cf;
+  const int* perm;
+  const float4* box;
+  const float* org;
+};
+
+__device__ __forceinline__ QueryCtx qctx(const DevBlock& B, const SearchView& V) {
+  const float* org = V.org;
   QueryCtx C;
-  C.cf = cf;
+  C.cf = V.cf;
+  C.perm = V.perm;
+  C.box = V.box;
+  C.nch = (B.ne + 31) / 32;
   C.xc = B.xcent;
   C.yc = B.ycent;
   C.zc = B.zcent;
@@ -117,8 +214,8 @@ __device__ __forceinline__ QueryCtx qctx(const DevBlock& B, const float4* cf, co
   return C;
 }
 
-// computeSurfaceNorm, src/Search.F90:210-258, plus the FP32 centroid copy
-__global__ void k_surface_norm(DevBlock B, double fin, float4* cf, const float* org) {
+// computeSurfaceNorm, src/Search.F90:210-258
+__global__ void k_surface_norm(DevBlock B, double fin) {
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < B.ne; n += gridDim.x * blockDim.x) {
     const int a = B.elp1[n] - 1, b = B.elp2[n] - 1, c = B.elp3[n] - 1;
     const double p1x = B.xnode1[a], p1y = B.ynode1[a], p1z = B.znode1[a];
@@ -137,8 +234,39 @@ __global__ void k_surface_norm(DevBlock B, double fin, float4* cf, const float* 
     B.cosA[n] = fin * ca / len;
     B.cosB[n] = fin * cb / len;
     B.cosG[n] = fin * cg / len;
-    cf[n] = make_float4((float)(xc - (double)org[0]), (float)(yc - (double)org[1]),
-                        (float)(zc - (double)org[2]), 0.0f);
+  }
+}
+
+// the search's FP32 centroid copies relative to the origin, in search order,
+// and the box of each chunk of 32 (one warp per chunk)
+__global__ void k_cf_chunks(DevBlock B, float4* cf, const int* perm, float4* box, const float* org) {
+  const int lane = threadIdx.x & 31;
+  const int nch = (B.ne + 31) / 32;
+  const double ox = org[0], oy = org[1], oz = org[2];
+  for (int c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; c < nch; c += (gridDim.x * blockDim.x) >> 5) {
+    const int pos = 32 * c + lane;
+    float4 e = make_float4(0.f, 0.f, 0.f, 0.f);
+    float lx = kFInf, ly = kFInf, lz = kFInf, hx = -kFInf, hy = -kFInf, hz = -kFInf;
+    if (pos < B.ne) {
+      const int n = perm[pos];
+      e = make_float4((float)(B.xcent[n] - ox), (float)(B.ycent[n] - oy), (float)(B.zcent[n] - oz), 0.0f);
+      cf[pos] = e;
+      lx = hx = e.x;
+      ly = hy = e.y;
+      lz = hz = e.z;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      lx = fminf(lx, __shfl_xor_sync(0xffffffffu, lx, o));
+      ly = fminf(ly, __shfl_xor_sync(0xffffffffu, ly, o));
+      lz = fminf(lz, __shfl_xor_sync(0xffffffffu, lz, o));
+      hx = fmaxf(hx, __shfl_xor_sync(0xffffffffu, hx, o));
+      hy = fmaxf(hy, __shfl_xor_sync(0xffffffffu, hy, o));
+      hz = fmaxf(hz, __shfl_xor_sync(0xffffffffu, hz, o));
+    }
+    if (lane == 0) {
+      box[2 * c] = make_float4(lx, ly, lz, 0.0f);
+      box[2 * c + 1] = make_float4(hx, hy, hz, 0.0f);
+    }
   }
 }
 
@@ -164,8 +292,8 @@ __device__ void tag_cell_warp(const DevBlock& B, const QueryCtx& C, int i, int j
 }
 
 // tagging_th_core loop 1 over the search box (one warp per cell)
-__global__ void k_tag_box(DevBlock B, const float4* cf, const float* org) {
-  const QueryCtx C = qctx(B, cf, org);
+__global__ void k_tag_box(DevBlock B, SearchView V) {
+  const QueryCtx C = qctx(B, V);
   const int bx = B.box[1] - B.box[0] + 1, by = B.box[3] - B.box[2] + 1, bz = B.box[5] - B.box[4] + 1;
   const int64_t n = (int64_t)bx * by * bz;
   const int64_t warp = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
@@ -240,9 +368,9 @@ __device__ __forceinline__ void lin_to_ijk(const Dims& d, int64_t t, int& i, int
   k = 1 + (int)(r / d.NY);
 }
 
-__global__ void k_retag_cells(DevBlock B, const float4* cf, const float* org, const int* list,
+__global__ void k_retag_cells(DevBlock B, SearchView V, const int* list,
                               const int* count) {
-  const QueryCtx C = qctx(B, cf, org);
+  const QueryCtx C = qctx(B, V);
   const int n = min(*count, (int)B.d.npts());
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -399,8 +527,8 @@ __global__ void k_fill_int(int* a, int64_t n, int v) {
 }
 
 // computeNormDistance, src/Search.F90:743-861 (one warp per IB cell)
-__global__ void k_norm_distance(DevBlock B, const float4* cf, const float* org) {
-  const QueryCtx C = qctx(B, cf, org);
+__global__ void k_norm_distance(DevBlock B, SearchView V) {
+  const QueryCtx C = qctx(B, V);
   const int nib = (int)min(B.cnt[C_IB], (int64_t)B.cap_ib);
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -516,7 +644,10 @@ __global__ void k_fine_block_cell(DevBlock A, FbcArgs f, double dx, double dy, d
 // per-block search scratch: FP32 centroids, origin/radius, marks, lists
 // ---------------------------------------------------------------------------
 struct SearchScratch {
-  float4* cf = nullptr;
+  float4* cf = nullptr;   // FP32 centroids in search order
+  int* perm = nullptr;    // search order -> element index
+  float4* box = nullptr;  // chunk boxes (lo, hi)
+  int perm_gen = -1;      // elem_perm_gen of the uploaded perm
   float* org = nullptr;   // [ox, oy, oz, R] on device
   uint8_t* mark = nullptr;
   int* list = nullptr;
@@ -535,7 +666,8 @@ static SearchScratch& scratch_of(HostBlock* hb) {
 void free_search_scratch(HostBlock* hb) {
   if (!hb->search_scratch) return;
   SearchScratch* s = static_cast<SearchScratch*>(hb->search_scratch);
-  for (void* p : {(void*)s->cf, (void*)s->org, (void*)s->mark, (void*)s->list, (void*)s->count, (void*)s->cta})
+  for (void* p : {(void*)s->cf, (void*)s->perm, (void*)s->box, (void*)s->org, (void*)s->mark, (void*)s->list,
+                  (void*)s->count, (void*)s->cta})
     if (p) cudaFree(p);
   delete s;
   hb->search_scratch = nullptr;
@@ -560,14 +692,32 @@ static int ensure_alloc(HostBlock* hb) {
     s.org_set = false;
     lib().gen++;
   }
-  if (s.cap_e < hb->d.ne) {
+  if (s.cap_e < hb->d.ne || !s.cf) {
     if (s.cf) cudaFree(s.cf);
-    BCFD_CUDA(cudaMalloc(&s.cf, (size_t)std::max(hb->d.ne, 1) * sizeof(float4)));
+    if (s.perm) cudaFree(s.perm);
+    if (s.box) cudaFree(s.box);
+    const size_t ne = (size_t)std::max(hb->d.ne, 1), nch = (ne + 31) / 32;
+    BCFD_CUDA(cudaMalloc(&s.cf, ne * sizeof(float4)));
+    BCFD_CUDA(cudaMalloc(&s.perm, ne * sizeof(int)));
+    BCFD_CUDA(cudaMalloc(&s.box, 2 * nch * sizeof(float4)));
     s.cap_e = hb->d.ne;
+    s.perm_gen = -1;
     lib().gen++;
+  }
+  if (s.perm_gen != hb->elem_perm_gen) {
+    // the search order (identity when none was set with the surface)
+    std::vector<int> perm(hb->elem_perm);
+    if ((int)perm.size() != hb->d.ne) {
+      perm.resize((size_t)std::max(hb->d.ne, 0));
+      for (int q = 0; q < hb->d.ne; ++q) perm[(size_t)q] = q;
+    }
+    if (!perm.empty()) BCFD_CUDA(h2d(s.perm, perm.data(), perm.size() * sizeof(int)));
+    s.perm_gen = hb->elem_perm_gen;
   }
   return 0;
 }
+
+static SearchView view_of(const SearchScratch& s) { return SearchView{s.cf, s.perm, s.box, s.org}; }
 
 // origin: centre of the block; R: half diagonal of the padded block
 static void origin_of(const HostBlock* hb, float h[4]) {
@@ -613,7 +763,10 @@ int launch_surface_norm(HostBlock* hb, int64_t inor) {
   if (int r = ensure_scratch(hb)) return r;
   SearchScratch& s = scratch_of(hb);
   if (hb->d.ne <= 0) return 0;
-  k_surface_norm<<<grid_for(hb->d.ne, 128), 128, 0, stream()>>>(hb->d, (double)inor, s.cf, s.org);
+  k_surface_norm<<<grid_for(hb->d.ne, 128), 128, 0, stream()>>>(hb->d, (double)inor);
+  BCFD_LAUNCHED();
+  const int64_t nch = (hb->d.ne + 31) / 32;
+  k_cf_chunks<<<grid_for(nch * 32, 256), 256, 0, stream()>>>(hb->d, s.cf, s.perm, s.box, s.org);
   BCFD_LAUNCHED();
   return 0;
 }
@@ -628,7 +781,7 @@ int launch_tagging(HostBlock* hb) {
   const int* b = hb->d.box;
   const int64_t n = (int64_t)(b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1);
   if (n <= 0 || hb->d.ne <= 0) return 0;
-  k_tag_box<<<grid_for(n * 32, 32 * kWarps, 152u * 64u), 32 * kWarps, 0, stream()>>>(hb->d, s.cf, s.org);
+  k_tag_box<<<grid_for(n * 32, 32 * kWarps, 152u * 64u), 32 * kWarps, 0, stream()>>>(hb->d, view_of(s));
   BCFD_LAUNCHED();
   k_solid_box<<<grid_for(n, 256), 256, 0, stream()>>>(hb->d);
   BCFD_LAUNCHED();
@@ -650,7 +803,7 @@ int launch_retagging(HostBlock* hb) {
                                                                    (int)d.npts());
   BCFD_LAUNCHED();
   if (hb->d.ne > 0) {
-    k_retag_cells<<<152 * 16, 32 * kWarps, 0, stream()>>>(hb->d, s.cf, s.org, s.list, s.count);
+    k_retag_cells<<<152 * 16, 32 * kWarps, 0, stream()>>>(hb->d, view_of(s), s.list, s.count);
     BCFD_LAUNCHED();
   }
   k_retag_solid<<<grid_for(d.npts(), 256), 256, 0, stream()>>>(hb->d, s.list, s.count);
@@ -721,7 +874,7 @@ int launch_norm_distance(HostBlock* hb) {
   if (int r = ensure_scratch(hb)) return r;
   SearchScratch& s = scratch_of(hb);
   if (hb->d.ne <= 0) return 0;
-  k_norm_distance<<<152 * 8, 32 * kWarps, 0, stream()>>>(hb->d, s.cf, s.org);
+  k_norm_distance<<<152 * 8, 32 * kWarps, 0, stream()>>>(hb->d, view_of(s));
   BCFD_LAUNCHED();
   return 0;
 }

@@ -261,6 +261,8 @@ int launch_forcing_pressure(HostBlock* hb, int mode);
 // k_interp.cu
 int launch_face_fill(HostInterface* it, int comp, int which);  // which: 0 t-fields, 1 pc, 2 n-fields
 int launch_restrict(HostInterface* it, int comp, int which);
+int launch_face_fill_set(HostInterface* it, const int* comps, int nc, int which);
+int launch_restrict_set(HostInterface* it, const int* comps, int nc, int which);
 int launch_fine_update_mv(HostInterface* it);
 // op 0: face fill P, 1: P^T (accumulates), 2: restriction R, 3: R^T (accumulates)
 int coupling_apply(HostInterface* it, int comp, int op, const double* in, double* out);

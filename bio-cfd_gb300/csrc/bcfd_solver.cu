@@ -108,13 +108,12 @@ std::vector<std::pair<bcfd_handle, HostBlock*>> blocks() {
   return v;
 }
 
+constexpr int kUVW[3] = {1, 2, 3};
+constexpr int kPUVW[4] = {0, 1, 2, 3};
+
 int fine_update_newv_bd() {
   for (HostInterface* it : lib().ifs)
-    if (it) {
-      TRY(launch_face_fill(it, 1, 0));
-      TRY(launch_face_fill(it, 2, 0));
-      TRY(launch_face_fill(it, 3, 0));
-    }
+    if (it) TRY(launch_face_fill_set(it, kUVW, 3, 0));
   return 0;
 }
 int fine_update_pc_bd() {
@@ -122,20 +121,15 @@ int fine_update_pc_bd() {
     if (it) TRY(launch_face_fill(it, 0, 1));
   return 0;
 }
-int fine_update_bd_mv(HostInterface* it) {
-  for (int c = 0; c < 4; ++c) TRY(launch_face_fill(it, c, 2));
-  return 0;
-}
+int fine_update_bd_mv(HostInterface* it) { return launch_face_fill_set(it, kPUVW, 4, 2); }
 int coarse_update() {
   for (HostInterface* it : lib().ifs)
-    if (it)
-      for (int c = 0; c < 4; ++c) TRY(launch_restrict(it, c, 2));
+    if (it) TRY(launch_restrict_set(it, kPUVW, 4, 2));
   return 0;
 }
 int coarse_update_newv() {
   for (HostInterface* it : lib().ifs)
-    if (it)
-      for (int c = 1; c < 4; ++c) TRY(launch_restrict(it, c, 0));
+    if (it) TRY(launch_restrict_set(it, kUVW, 3, 0));
   return 0;
 }
 int coarse_update_pc() {

@@ -57,8 +57,14 @@ struct FaceArgs {
   int axis;          // face pass 1..3
 };
 
+// the components of one coupling call, each its own arrays (one launch per
+// face pass instead of one per component)
+struct FaceSet {
+  FaceArgs f[4];
+};
+
 // trilinear_interpolation of src/FineInterp_bound.f90:554-603 (donors loc+-1)
-__global__ void k_face(Dims da, Dims db, FaceArgs a) {
+__device__ __forceinline__ void face_body(const Dims& da, const Dims& db, const FaceArgs& a) {
   const int sx = a.axis == 1 ? a.tx.c - 1 : 1, sy = a.axis == 2 ? a.ty.c - 1 : 1,
             sz = a.axis == 3 ? a.tz.c - 1 : 1;
   const int nxs = (a.tx.c - 1) / sx + 1, nys = (a.ty.c - 1) / sy + 1, nzs = (a.tz.c - 1) / sz + 1;
@@ -93,10 +99,19 @@ __global__ void k_face(Dims da, Dims db, FaceArgs a) {
   }
 }
 
+__global__ void k_face(Dims da, Dims db, FaceArgs a) { face_body(da, db, a); }
+
+// face pass `axis` of the components S.f[blockIdx.y]
+__global__ void k_face_set(Dims da, Dims db, FaceSet S, int axis) {
+  FaceArgs a = S.f[blockIdx.y];
+  a.axis = axis;
+  face_body(da, db, a);
+}
+
 // trilinear_interpolation of src/CoarseInterp.f90:447-502 (adjacent donors);
 // the target coarse point of entry i is det(1,i); the donor index is the
 // middle fine index (start+end-1)/2, or `end` along the staggered axis.
-__global__ void k_restrict(Dims da, Dims db, FaceArgs a, int ci) {
+__device__ __forceinline__ void restrict_body(const Dims& da, const Dims& db, const FaceArgs& a, int ci) {
   const int nxs = a.tx.c - 2 * ci + 1, nys = a.ty.c - 2 * ci + 1, nzs = a.tz.c - 2 * ci + 1;
   if (nxs <= 0 || nys <= 0 || nzs <= 0) return;
   const int n = nxs * nys * nzs;
@@ -128,6 +143,9 @@ __global__ void k_restrict(Dims da, Dims db, FaceArgs a, int ci) {
     if (a.dst2.nat || a.dst2.pk0) fset(da, a.dst2, ox, oy, oz, r);
   }
 }
+
+__global__ void k_restrict(Dims da, Dims db, FaceArgs a, int ci) { restrict_body(da, db, a, ci); }
+__global__ void k_restrict_set(Dims da, Dims db, FaceSet S, int ci) { restrict_body(da, db, S.f[blockIdx.y], ci); }
 
 // ---------------------------------------------------------------------------
 // Adjoints of the coupling (transposed trilinear interpolation).
@@ -339,6 +357,54 @@ int launch_face_fill(HostInterface* it, int comp, int which) {
     k_face<<<grid_for(n, 128), 128, 0, stream()>>>(a->d.d, b->d.d, f);
     BCFD_LAUNCHED();
   }
+  return 0;
+}
+
+// the face fill of several components: one launch per face pass (the
+// components write different arrays and read the coarse block only; the
+// passes keep their order, so points two passes write get the later value)
+int launch_face_fill_set(HostInterface* it, const int* comps, int nc, int which) {
+  HostBlock* a = get_block(it->a);
+  HostBlock* b = get_block(it->b);
+  if (!a || !b) return BCFD_E_HANDLE;
+  if (nc < 1 || nc > 4) return BCFD_E_ARG;
+  FaceSet S{};
+  int n = 0;
+  for (int q = 0; q < nc; ++q) {
+    FaceArgs& f = S.f[q];
+    f = make_args(it, a, b, comps[q]);
+    f.src = field_of(a->d, comps[q], which);
+    f.dst = field_of(b->d, comps[q], which);
+    f.dst2 = Field{nullptr, nullptr, nullptr};
+    n = std::max(n, f.tx.c * f.ty.c * f.tz.c);
+  }
+  for (int axis = 1; axis <= 3; ++axis) {
+    const dim3 grid(grid_for(n, 128), (unsigned)nc);
+    k_face_set<<<grid, 128, 0, stream()>>>(a->d.d, b->d.d, S, axis);
+    BCFD_LAUNCHED();
+  }
+  return 0;
+}
+
+// the restriction of several components in one launch (different arrays)
+int launch_restrict_set(HostInterface* it, const int* comps, int nc, int which) {
+  HostBlock* a = get_block(it->a);
+  HostBlock* b = get_block(it->b);
+  if (!a || !b) return BCFD_E_HANDLE;
+  if (nc < 1 || nc > 4) return BCFD_E_ARG;
+  FaceSet S{};
+  int n = 0;
+  for (int q = 0; q < nc; ++q) {
+    FaceArgs& f = S.f[q];
+    f = make_args(it, a, b, comps[q]);
+    f.src = field_of(b->d, comps[q], which);
+    f.dst = field_of(a->d, comps[q], which);
+    f.dst2 = Field{nullptr, nullptr, nullptr};
+    n = std::max(n, f.tx.c * f.ty.c * f.tz.c);
+  }
+  const dim3 grid(grid_for(n, 128), (unsigned)nc);
+  k_restrict_set<<<grid, 128, 0, stream()>>>(a->d.d, b->d.d, S, 3);
+  BCFD_LAUNCHED();
   return 0;
 }
 

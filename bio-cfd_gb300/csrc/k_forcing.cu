@@ -43,10 +43,18 @@ __device__ __forceinline__ Grid3 comp_grid(const DevBlock& B, int axis) {
 // find_index_in_array (src/Forcing.f90:1165-1183): first i in [s, f] with
 // a(i) <= v < a(i+1).  Indices outside the array are skipped; when no
 // bracket exists the error word is set and a clamped start index returned.
+// The grid coordinates are non-decreasing, so a bracket is unique and a
+// binary search for the last i with a(i) <= v finds the scan's answer.
 __device__ int find_index(const DevBlock& B, double v, const double* a, int len, int s, int f) {
-  for (int i = s; i <= f; ++i) {
-    if (i < 1 || i + 1 > len) continue;
-    if (v >= a[i - 1] && v < a[i]) return i;
+  const int lo = max(s, 1), hi = min(f, len - 1);
+  if (lo <= hi && v >= a[lo - 1]) {
+    int L = lo, H = hi;
+    while (L < H) {
+      const int m = (L + H + 1) >> 1;
+      if (a[m - 1] <= v) L = m;
+      else H = m - 1;
+    }
+    if (v < a[L]) return L;
   }
   set_err(B.err, BCFD_E_NOTFOUND);
   int r = s < 1 ? 1 : s;

@@ -12,10 +12,18 @@ namespace bcfd {
 
 namespace {
 
+// first i in [s, f] with a(i) <= v < a(i+1); on the non-decreasing grid
+// coordinates the bracket is unique, so a binary search finds the scan's i
 __device__ int fidx(const DevBlock& B, double v, const double* a, int len, int s, int f) {
-  for (int i = s; i <= f; ++i) {
-    if (i < 1 || i + 1 > len) continue;
-    if (v >= a[i - 1] && v < a[i]) return i;
+  const int lo = max(s, 1), hi = min(f, len - 1);
+  if (lo <= hi && v >= a[lo - 1]) {
+    int L = lo, H = hi;
+    while (L < H) {
+      const int m = (L + H + 1) >> 1;
+      if (a[m - 1] <= v) L = m;
+      else H = m - 1;
+    }
+    if (v < a[L]) return L;
   }
   set_err(B.err, BCFD_E_NOTFOUND);
   return max(1, min(s, len - 1));

@@ -150,3 +150,22 @@ def test_steps_body_free_block(n):
     s.run(3)
     compare_fields(o, s, "3 steps, body-free block")
     compare_iters(o, s, "3 steps, body-free block")
+
+
+@pytest.mark.parametrize("workload", ["sphere_64", "two_block_bench"])
+def test_full_size_steps_bitwise(workload):
+    """The workloads at their full sizes: the 64^3 sphere block (D = 0.25 at
+    (0.4, 0.5, 0.5), Re 100) and the bench's coarse 96x64x64 + fine 64^3
+    two-block sphere (D = 0.5, Re 300).  Two drop-in steps bitwise against
+    the oracle: fields, SOR iteration counts and Search tags."""
+    if workload == "sphere_64":
+        case = synth.sphere_single_block(n=64, n_steps=2)
+    else:
+        case = synth.sphere_two_block(n_steps=2)
+    o, s = _pair(case)
+    for _ in range(2):
+        o.step()
+    s.run(2)
+    compare_fields(o, s, f"{workload}, 2 steps")
+    compare_iters(o, s, f"{workload}, 2 steps")
+    compare_search(o, s, f"{workload}, 2 steps")

@@ -259,8 +259,8 @@ int launch_build_list(HostBlock* hb, int which, int* out_ijk, int64_t cap, int64
 int launch_forcing_velocity(HostBlock* hb, int mode);  // 0 forcing1, 1 field, 2 ghost
 int launch_forcing_pressure(HostBlock* hb, int mode);
 // k_interp.cu
-int launch_face_fill(HostInterface* it, int comp, int which);  // which: 0 t-fields, 1 pc, 2 n-fields
-int launch_restrict(HostInterface* it, int comp, int which);
+// the face fill / restriction of components comps[0..nc) of an interface
+// (which: 0 t-fields, 1 pc, 2 n-fields)
 int launch_face_fill_set(HostInterface* it, const int* comps, int nc, int which);
 int launch_restrict_set(HostInterface* it, const int* comps, int nc, int which);
 int launch_fine_update_mv(HostInterface* it);

@@ -116,9 +116,11 @@ int fine_update_newv_bd() {
     if (it) TRY(launch_face_fill_set(it, kUVW, 3, 0));
   return 0;
 }
+constexpr int kP[1] = {0};
+
 int fine_update_pc_bd() {
   for (HostInterface* it : lib().ifs)
-    if (it) TRY(launch_face_fill(it, 0, 1));
+    if (it) TRY(launch_face_fill_set(it, kP, 1, 1));
   return 0;
 }
 int fine_update_bd_mv(HostInterface* it) { return launch_face_fill_set(it, kPUVW, 4, 2); }
@@ -134,7 +136,7 @@ int coarse_update_newv() {
 }
 int coarse_update_pc() {
   for (HostInterface* it : lib().ifs)
-    if (it) TRY(launch_restrict(it, 0, 1));
+    if (it) TRY(launch_restrict_set(it, kP, 1, 1));
   return 0;
 }
 

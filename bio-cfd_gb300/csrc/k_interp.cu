@@ -63,13 +63,22 @@ struct FaceSet {
   FaceArgs f[4];
 };
 
-// trilinear_interpolation of src/FineInterp_bound.f90:554-603 (donors loc+-1)
+// trilinear_interpolation of src/FineInterp_bound.f90:554-603 (donors loc+-1).
+// SUB: eight threads per table entry, each taking every second fine point
+// along each axis of the entry's target range (the points are independent;
+// a thread's chain of FP64 divisions is an eighth as long)
+template <bool SUB>
 __device__ __forceinline__ void face_body(const Dims& da, const Dims& db, const FaceArgs& a) {
   const int sx = a.axis == 1 ? a.tx.c - 1 : 1, sy = a.axis == 2 ? a.ty.c - 1 : 1,
             sz = a.axis == 3 ? a.tz.c - 1 : 1;
   const int nxs = (a.tx.c - 1) / sx + 1, nys = (a.ty.c - 1) / sy + 1, nzs = (a.tz.c - 1) / sz + 1;
   const int n = nxs * nys * nzs;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x) {
+  const int per = SUB ? 8 : 1;
+  for (int64_t tt = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; tt < (int64_t)n * per;
+       tt += (int64_t)gridDim.x * blockDim.x) {
+    const int t = (int)(tt / per), sub = (int)(tt % per);
+    const int ox0 = SUB ? (sub & 1) : 0, oy0 = SUB ? ((sub >> 1) & 1) : 0, oz0 = SUB ? (sub >> 2) : 0;
+    const int st = SUB ? 2 : 1;
     const int ei = 1 + (t % nxs) * sx, ej = 1 + ((t / nxs) % nys) * sy, ek = 1 + (t / (nxs * nys)) * sz;
     const int vx1 = a.tx.at(2, ei), vx2 = a.tx.at(3, ei);
     const int vy1 = a.ty.at(2, ej), vy2 = a.ty.at(3, ej);
@@ -85,9 +94,9 @@ __device__ __forceinline__ void face_body(const Dims& da, const Dims& db, const 
                  f2 = fget(da, a.src, vi - 1, vj + 1, vk - 1), f3 = fget(da, a.src, vi + 1, vj + 1, vk - 1);
     const double g0 = fget(da, a.src, vi - 1, vj - 1, vk + 1), g1 = fget(da, a.src, vi + 1, vj - 1, vk + 1),
                  g2 = fget(da, a.src, vi - 1, vj + 1, vk + 1), g3 = fget(da, a.src, vi + 1, vj + 1, vk + 1);
-    for (int tz = vz1; tz <= vz2; ++tz)
-      for (int ty = vy1; ty <= vy2; ++ty)
-        for (int tx = vx1; tx <= vx2; ++tx) {
+    for (int tz = vz1 + oz0; tz <= vz2; tz += st)
+      for (int ty = vy1 + oy0; ty <= vy2; ty += st)
+        for (int tx = vx1 + ox0; tx <= vx2; tx += st) {
           const double x = a.gb.x[tx - 1], y = a.gb.y[ty - 1], z = a.gb.z[tz - 1];
           const double za = bilinear(x, y, x1, x2, y1, y2, f0, f1, f2, f3);
           const double zb = bilinear(x, y, x1, x2, y1, y2, g0, g1, g2, g3);
@@ -99,13 +108,13 @@ __device__ __forceinline__ void face_body(const Dims& da, const Dims& db, const 
   }
 }
 
-__global__ void k_face(Dims da, Dims db, FaceArgs a) { face_body(da, db, a); }
+__global__ void k_face(Dims da, Dims db, FaceArgs a) { face_body<false>(da, db, a); }
 
 // face pass `axis` of the components S.f[blockIdx.y]
 __global__ void k_face_set(Dims da, Dims db, FaceSet S, int axis) {
   FaceArgs a = S.f[blockIdx.y];
   a.axis = axis;
-  face_body(da, db, a);
+  face_body<true>(da, db, a);
 }
 
 // trilinear_interpolation of src/CoarseInterp.f90:447-502 (adjacent donors);
@@ -343,22 +352,6 @@ FaceArgs make_args(HostInterface* it, HostBlock* a, HostBlock* b, int comp) {
 
 }  // namespace
 
-int launch_face_fill(HostInterface* it, int comp, int which) {
-  HostBlock* a = get_block(it->a);
-  HostBlock* b = get_block(it->b);
-  if (!a || !b) return BCFD_E_HANDLE;
-  FaceArgs f = make_args(it, a, b, comp);
-  f.src = field_of(a->d, comp, which);
-  f.dst = field_of(b->d, comp, which);
-  f.dst2 = Field{nullptr, nullptr, nullptr};  // pco aliases pc in the packed layout
-  for (int axis = 1; axis <= 3; ++axis) {
-    f.axis = axis;
-    const int n = f.tx.c * f.ty.c * f.tz.c;
-    k_face<<<grid_for(n, 128), 128, 0, stream()>>>(a->d.d, b->d.d, f);
-    BCFD_LAUNCHED();
-  }
-  return 0;
-}
 
 // the face fill of several components: one launch per face pass (the
 // components write different arrays and read the coarse block only; the
@@ -379,7 +372,7 @@ int launch_face_fill_set(HostInterface* it, const int* comps, int nc, int which)
     n = std::max(n, f.tx.c * f.ty.c * f.tz.c);
   }
   for (int axis = 1; axis <= 3; ++axis) {
-    const dim3 grid(grid_for(n, 128), (unsigned)nc);
+    const dim3 grid(grid_for(8 * (int64_t)n, 128), (unsigned)nc);
     k_face_set<<<grid, 128, 0, stream()>>>(a->d.d, b->d.d, S, axis);
     BCFD_LAUNCHED();
   }
@@ -408,19 +401,6 @@ int launch_restrict_set(HostInterface* it, const int* comps, int nc, int which) 
   return 0;
 }
 
-int launch_restrict(HostInterface* it, int comp, int which) {
-  HostBlock* a = get_block(it->a);
-  HostBlock* b = get_block(it->b);
-  if (!a || !b) return BCFD_E_HANDLE;
-  FaceArgs f = make_args(it, a, b, comp);
-  f.src = field_of(b->d, comp, which);
-  f.dst = field_of(a->d, comp, which);
-  f.dst2 = Field{nullptr, nullptr, nullptr};
-  const int n = f.tx.c * f.ty.c * f.tz.c;
-  k_restrict<<<grid_for(n, 128), 128, 0, stream()>>>(a->d.d, b->d.d, f, 3);
-  BCFD_LAUNCHED();
-  return 0;
-}
 
 int launch_fine_update_mv(HostInterface* it) {
   HostBlock* a = get_block(it->a);

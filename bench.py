@@ -315,6 +315,82 @@ def twelve_block(torch, local, steps=10, warmup=3, fp64_steps=2, moving=False):
     return out
 
 
+def tandem(torch, local, steps=5, warmup=2, cmp_steps=2):
+    """Two stationary plates in tandem on the 45M-cell layout (coarse 384x256x256
+    + two fine 256x192x192 blocks): time per step of the mixed path to the
+    divergence residual 1e-6, of the plain FP64 path with the input's omega 1.7
+    (which stops at pcItaMax = 5000 iterations per solve on the 384-cell block,
+    short of 1e-6) and of the plain FP64 path relaxing with the mixed path's
+    factor (which reaches 1e-6); and the mixed path's error against both FP64
+    runs after `cmp_steps` steps from the same initial state (relative L2 of
+    u, v, w, p per block; the drag and lift coefficients of each plate)."""
+    import numpy as np
+    from biocfd import synth
+    from biocfd.solver import Solver
+    assert cmp_steps >= 2
+    case = synth.tandem_plates(n_steps=steps + warmup + cmp_steps + 2)
+    ncells = sum(b.nx * b.ny * b.nz for b in case.blocks)
+    out = {"workload": "tandem plates: coarse 384x256x256 over 6x4x4 + two fine 256x192x192 at ratio 2, "
+                       f"{ncells / 1e6:.1f}M cells, stationary plates 0.5x0.125x0.0125 with centres 2.5 apart "
+                       "(1.5 chords), Re 1000, graph replay", "div_tol": DIV_TOL}
+    mu_f = 1.0 / case.re
+    snaps = {}
+    case_om = synth.with_mixed_omega(case)
+    for key, prec, n_timed, arm_case in (("mixed", 1, steps, case), ("fp64", 2, 1, case),
+                                         ("fp64_mixed_omega", 2, 1, case_om)):
+        s = Solver(arm_case, device=local)
+        s.setup()
+        s.autotune()
+        stream = torch.cuda.ExternalStream(s.stream_ptr())
+        # mixed: cmp_steps, warm-up, then the timed steps; FP64: cmp_steps, the
+        # last of them (a graph replay) timed
+        n_pre = cmp_steps + warmup if prec == 1 else cmp_steps - 1
+        ts = []
+        k0 = 0
+        for it in range(n_pre + n_timed):
+            timed = it >= n_pre
+            if it == n_pre:
+                k0 = s.kernel_launches()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            s.run(1, precision=prec, div_tol=DIV_TOL, use_graph=1)
+            e1.record(stream)
+            e1.synchronize()
+            if timed:
+                ts.append(e0.elapsed_time(e1))
+            if it == cmp_steps - 1:
+                snaps[key] = ([s.fields(g) for g in s.handles],
+                              [s.stress(g, mu_f).tolist() for g in s.handles[1:]])
+        res = max(s.divergence(g)[1] for g in s.handles)
+        ms = statistics.mean(ts)
+        out[key] = {"ms_per_step": ms, "steps_per_s": 1000.0 / ms, "steps": len(ts), "div_residual": res,
+                    "launches_per_step": (s.kernel_launches() - k0) / len(ts),
+                    "cell_updates_per_s": ncells * 1000.0 / ms}
+        s.close()
+    out["fp64"]["omega"] = [b.omega for b in case.blocks]
+    out["fp64_mixed_omega"]["omega"] = [b.omega for b in case_om.blocks]
+    out["speedup_mixed_vs_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    out["speedup_mixed_vs_fp64_mixed_omega"] = (out["fp64_mixed_omega"]["ms_per_step"] /
+                                                out["mixed"]["ms_per_step"])
+    fm, sm = snaps["mixed"]
+    for ref in ("fp64_mixed_omega", "fp64"):
+        fd, sd = snaps[ref]
+        err = {}
+        for q in range(len(fm)):
+            for k in ("u", "v", "w", "p"):
+                a, b = fm[q][k], fd[q][k]
+                if k == "p":  # pressure is defined up to a constant per solve: compare about the mean
+                    a, b = a - a.mean(), b - b.mean()
+                err[f"block{q + 1}_{k}"] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+        out[f"error_vs_{ref}"] = {"after_steps": cmp_steps, "field_rel_l2": err,
+                                  "coefficients": "viscous drag, pressure drag, viscous lift, pressure lift",
+                                  "plates_mixed": sm, f"plates_{ref}": sd,
+                                  "coef_rel": [[abs(x - y) / max(abs(y), 1e-300) for x, y in zip(a, b)]
+                                               for a, b in zip(sm, sd)]}
+    return out
+
+
 def adjoint_bench(torch, local, steps=4, every=2):
     """Discrete adjoint of whole FP64 steps on the 64^3 sphere block (D = 0.25,
     Re 100): time per step of forward + checkpointed reverse pass for the
@@ -376,10 +452,10 @@ def run_gpu(args):
         s.close()
         return
 
-    def arm(precision, clocks=None):
+    def arm(precision, clocks=None, arm_case=None):
         nonlocal s, stream
         s.close()
-        s = Solver(case, device=local)
+        s = Solver(case if arm_case is None else arm_case, device=local)
         s.setup()
         s.autotune()  # launch shapes of the solves; results do not depend on them
         stream = torch.cuda.ExternalStream(s.stream_ptr())
@@ -389,6 +465,9 @@ def run_gpu(args):
     t0_, div0, res0, it0, prof0 = arm(0)
     # plain FP64 SOR run to the same FP64 residual target as the mixed path
     t64, div64, res64, it64, prof64 = arm(2)
+    # the same, relaxing with the mixed path's factor instead of the input's 1.7
+    case_om = synth.with_mixed_omega(case)
+    t64o, _, res64o, it64o, _ = arm(2, arm_case=case_om)
     # flagship: FP32 momentum + FP32 SOR with FP64 defect correction
     clocks = Clocks(local)
     tmx, divmx, resmx, itmx, profmx = arm(1, clocks)
@@ -415,10 +494,11 @@ def run_gpu(args):
         e2e_times.append(time.perf_counter() - t0)
 
     ms64 = statistics.mean(t64)
+    ms64o = statistics.mean(t64o)
     ms0 = statistics.mean(t0_)
     msmx = statistics.mean(tmx)
     e2e_s = statistics.mean(e2e_times)
-    msmx, ms64, ms0, e2e_s = max_over_ranks([msmx, ms64, ms0, e2e_s])
+    msmx, ms64, ms0, e2e_s, ms64o = max_over_ranks([msmx, ms64, ms0, e2e_s, ms64o])
     nfluid = sum(s.counts(g)["fluidCellCount"] for g in s.handles)
     hbm, peak_kind = peaks()
     achieved = profmx["sor_bytes"] / (profmx["sor_ms"] * 1e-3) / 1e9 if profmx["sor_ms"] > 0 else 0.0
@@ -448,6 +528,11 @@ def run_gpu(args):
                         "sor_iters_last_step": it0[-1]},
         "mixed": {"steps_per_s": 1000.0 / msmx, "ms_per_step": msmx, "div_residual": max(resmx),
                   "div_tol": tol, "max_div_after_correction": max(divmx), "fp32_sweeps_last_step": itmx[-1]},
+        "fp64_mixed_omega": {"steps_per_s": 1000.0 / ms64o, "ms_per_step": ms64o, "div_residual": max(res64o),
+                             "omega": [b.omega for b in case_om.blocks], "sor_iters_last_step": it64o[-1],
+                             "speedup_mixed_vs_this": ms64o / msmx,
+                             "note": "plain FP64 SOR relaxing with the mixed path's default factor "
+                                     "2/(1+sin(pi/n_max)) instead of the input's 1.7"},
         "speedup_vs_fp64": ms64 / msmx,
         "cell_updates_per_s": world * nfluid * 1000.0 / msmx,
         "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
@@ -468,6 +553,8 @@ def run_gpu(args):
         line["twelve_block_moving"] = twelve_block(torch, local, steps=5, fp64_steps=1, moving=True)
     if not args.no_adjoint:
         line["adjoint"] = adjoint_bench(torch, local)
+    if not args.no_tandem:
+        line["tandem"] = tandem(torch, local)
     if rank == 0 and not args.no_cpu_baseline:
         sps, secs = oracle_steps(case, 1)
         line["cpu_baseline"] = {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
@@ -487,6 +574,9 @@ def main():
     ap.add_argument("--no-sweep-roofline", action="store_true")
     ap.add_argument("--no-twelve-block", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-tandem", action="store_true")
+    ap.add_argument("--tandem-only", action="store_true",
+                    help="only the 45M-cell tandem-plate measurement (mixed vs FP64, error vs FP64)")
     ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint timing")
     ap.add_argument("--twelve-only", action="store_true",
                     help="only the twelve-block measurement (batched vs per-block launches)")
@@ -499,6 +589,11 @@ def main():
         import torch
         torch.cuda.set_device(0)
         print(json.dumps(adjoint_bench(torch, 0)), flush=True)
+        return
+    if args.tandem_only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(tandem(torch, 0)), flush=True)
         return
     if args.twelve_only:
         import torch

@@ -311,14 +311,16 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
                 fine_boxes=(((0.5, 1.0), (0.5, 1.0), (0.5, 1.0)),
                             ((1.5, 2.25), (0.75, 1.25), (1.0, 1.5)),
                             ((2.375, 2.75), (1.0, 1.5), (0.375, 0.75))),
-                body: int = 0, diameter: float = 0.25, reynolds: float = 300.0, n_steps: int = 2,
+                body=0, diameter: float = 0.25, reynolds: float = 300.0, n_steps: int = 2,
                 omega: float = 1.7, pc_ita_max: int = 5000, seed: int = SEED, plate: bool = False,
                 plate_axes=None, motion: Optional[Motion] = None,
                 motion_inputs: Optional[MotionInputs] = None) -> Case:
     """A coarse block with several nested fine blocks of uneven sizes at ratio 2
     (one interface per fine block), a stationary sphere (or, with `plate`, a
-    thin plate of surface 51) in fine block `body`.  Box edges must lie on
-    coarse faces."""
+    thin plate of surface 51) centred in fine block `body` (an index, or a
+    tuple of indices for one body in each of several blocks).  Box edges must
+    lie on coarse faces."""
+    bodies = (body,) if isinstance(body, int) else tuple(body)
     cnx, cny, cnz = coarse
     L = domain
     d = (L[0] / cnx, L[1] / cny, L[2] / cnz)
@@ -334,7 +336,7 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
             n.append(int(round(cells)) * ratio)
         fs = BlockSpec(n[0], n[1], n[2], uniform_faces(*box[0], n[0]), uniform_faces(*box[1], n[1]),
                        uniform_faces(*box[2], n[2]), omega=omega, is_coarse=False)
-        if q == body:
+        if q in bodies:
             c = np.array([0.5 * (box[a][0] + box[a][1]) for a in range(3)])
             dxf = (box[0][1] - box[0][0]) / n[0]
             if plate:
@@ -413,10 +415,23 @@ def twelve_block(n_steps: int = 10, seed: int = SEED, moving: bool = False) -> C
                        plate_axes=(0.5, 0.125, 0.0125), motion=motion, motion_inputs=inputs)
 
 
+def tandem_plates(n_steps: int = 2, seed: int = SEED) -> Case:
+    """Two thin plates in tandem on the 45M-cell layout: a coarse 384x256x256
+    block over 6x4x4 (dx 1/64) and two fine 256x192x192 blocks at ratio 2
+    (dx 1/128), each holding a stationary rigid ellipsoidal plate of semi-axes
+    0.5 x 0.125 x 0.0125 (surface 51) at its centre; the plates are 1.5 chords
+    apart (centres at x = 1.75 and 4.25), Re = 1000 on the chord."""
+    boxes = (((0.75, 2.75), (1.25, 2.75), (1.25, 2.75)),
+             ((3.25, 5.25), (1.25, 2.75), (1.25, 2.75)))
+    return multi_block(coarse=(384, 256, 256), domain=(6.0, 4.0, 4.0), fine_boxes=boxes, body=(0, 1),
+                       diameter=1.0, reynolds=1000.0, n_steps=n_steps, seed=seed, plate=True,
+                       plate_axes=(0.5, 0.125, 0.0125))
+
+
 def uniform_block(n=(384, 256, 256), lengths=(3.0, 2.0, 2.0), seed: int = SEED,
                   noise: bool = True) -> Case:
-    """One body-free uniform block with the domain BCs (the coarse block of the
-    tandem-plate workload is 384x256x256 over 3x2x2); used to measure the
+    """One body-free uniform block with the domain BCs (384x256x256 is the
+    coarse block size of the tandem-plate workload); used to measure the
     Poisson sweeps at sizes far above the 129 MB L2."""
     nx, ny, nz = n
     spec = BlockSpec(nx, ny, nz, uniform_faces(0, lengths[0], nx), uniform_faces(0, lengths[1], ny),
@@ -436,6 +451,16 @@ def small_two_block(n_steps: int = 2, seed: int = SEED) -> Case:
     return sphere_two_block(nf=16, n_steps=n_steps, diameter=0.5, coarse=(24, 16, 16),
                             domain=(3.0, 2.0, 2.0), fine_box=((1.0, 2.0), (0.5, 1.5), (0.5, 1.5)),
                             pc_ita_max=2000, seed=seed)
+
+
+def with_mixed_omega(case: Case) -> Case:
+    """A copy of `case` whose blocks relax with the factor the mixed path's FP32
+    sweeps use by default, 2 / (1 + sin(pi / n_max)) for the block's largest
+    extent n_max, instead of the input's omega: the plain FP64 solve at the same
+    relaxation separates the gain of the precision from that of the factor."""
+    blocks = [dataclasses.replace(b, omega=2.0 / (1.0 + np.sin(np.pi / max(b.nx, b.ny, b.nz))))
+              for b in case.blocks]
+    return dataclasses.replace(case, blocks=blocks)
 
 
 def replace(case: Case, **kw) -> Case:

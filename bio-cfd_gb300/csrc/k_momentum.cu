@@ -67,6 +67,48 @@ __device__ __forceinline__ Dual operator/(Dual a, Dual b) {
 using ::fabs;
 __device__ __forceinline__ Dual fabs(Dual a) { return a.v < 0.0 ? -a : a; }
 
+// The same with four tangents: one evaluation carries the derivatives along
+// four seeds at once.  Each tangent lane performs exactly the operations of
+// Dual's tangent on the same operands, so lane l equals the Dual tangent of
+// seed l bit for bit.
+struct Dual4 {
+  double v, d[4];
+  __device__ Dual4() : v(0.0), d{0.0, 0.0, 0.0, 0.0} {}
+  __device__ Dual4(double x) : v(x), d{0.0, 0.0, 0.0, 0.0} {}
+};
+__device__ __forceinline__ Dual4 operator+(const Dual4& a, const Dual4& b) {
+  Dual4 r(a.v + b.v);
+#pragma unroll
+  for (int l = 0; l < 4; ++l) r.d[l] = a.d[l] + b.d[l];
+  return r;
+}
+__device__ __forceinline__ Dual4 operator-(const Dual4& a, const Dual4& b) {
+  Dual4 r(a.v - b.v);
+#pragma unroll
+  for (int l = 0; l < 4; ++l) r.d[l] = a.d[l] - b.d[l];
+  return r;
+}
+__device__ __forceinline__ Dual4 operator-(const Dual4& a) {
+  Dual4 r(-a.v);
+#pragma unroll
+  for (int l = 0; l < 4; ++l) r.d[l] = -a.d[l];
+  return r;
+}
+__device__ __forceinline__ Dual4 operator*(const Dual4& a, const Dual4& b) {
+  Dual4 r(a.v * b.v);
+#pragma unroll
+  for (int l = 0; l < 4; ++l) r.d[l] = a.d[l] * b.v + a.v * b.d[l];
+  return r;
+}
+__device__ __forceinline__ Dual4 operator/(const Dual4& a, const Dual4& b) {
+  const double q = a.v / b.v;
+  Dual4 r(q);
+#pragma unroll
+  for (int l = 0; l < 4; ++l) r.d[l] = (a.d[l] - q * b.d[l]) / b.v;
+  return r;
+}
+__device__ __forceinline__ Dual4 fabs(const Dual4& a) { return a.v < 0.0 ? -a : a; }
+
 // where a stencil's three results go
 struct StoreOut {
   double *ut, *vt, *wt;
@@ -638,21 +680,34 @@ __global__ void k_mom_footprint(DevBlock B, MomArgs a, uint32_t* foot) {
   }
 }
 
-// dual reader seeded with 1 at (field sf, linear index sx)
-struct SeedReader {
+// four-lane dual reader: lane f carries the seed 1 at (field f, linear index sx)
+struct SeedReader4 {
   const double* f[4];
-  int sf;
   int64_t sx;
-  __device__ __forceinline__ Dual get(int q, int, int, int, int64_t x) const {
-    return Dual(__ldg(f[q] + x), (q == sf && x == sx) ? 1.0 : 0.0);
+  __device__ __forceinline__ Dual4 get(int q, int, int, int, int64_t x) const {
+    Dual4 r(__ldg(f[q] + x));
+    if (x == sx) r.d[q] = 1.0;
+    return r;
   }
 };
-struct AdjOut {
+// adds seed_q(C) * dF_q(C)/dX_f to field f's sum, for the fields whose
+// footprint holds this offset (the others' partials are zero)
+struct AdjOut4 {
   const double* sb[3];
   double* acc;
-  __device__ __forceinline__ void put(int q, int64_t c, Dual val) const { *acc += __ldg(sb[q] + c) * val.d; }
+  unsigned fmask;
+  __device__ __forceinline__ void put(int q, int64_t c, const Dual4& val) const {
+    const double s = __ldg(sb[q] + c);
+#pragma unroll
+    for (int f = 0; f < 4; ++f)
+      if ((fmask >> f) & 1u) acc[f] += s * val.d[f];
+  }
 };
 
+// One dual evaluation per (point, footprint offset) gives the partials of all
+// four fields at that point; each field's sum takes the offsets in ascending
+// order and, within one, the outputs U, V, W: the order of one evaluation per
+// field and offset, so the sums are those of four single-seed gathers.
 __global__ void __launch_bounds__(128) k_mom_adjoint(DevBlock B, MomArgs a, const uint32_t* __restrict__ foot,
                                                      const double* ubar_t, const double* vbar_t,
                                                      const double* wbar_t, double* ub, double* vb, double* wb,
@@ -666,23 +721,27 @@ __global__ void __launch_bounds__(128) k_mom_adjoint(DevBlock B, MomArgs a, cons
     const int xi = 1 + (int)(x % d.NX);
     const int64_t r = x / d.NX;
     const int xj = 1 + (int)(r % d.NY), xk = 1 + (int)(r / d.NY);
-    for (int f = 0; f < 4; ++f) {
-      double acc = 0.0;
-      for (int o = 0; o < 125; ++o) {
-        if (!((m[4 * f + (o >> 5)] >> (o & 31)) & 1u)) continue;
-        const int ci = xi - (o % 5 - 2), cj = xj - ((o / 5) % 5 - 2), ck = xk - (o / 25 - 2);
-        if (ci < 2 || ci > d.nx + 1 || cj < 2 || cj > d.ny + 1 || ck < 2 || ck > d.nz + 1) continue;
-        const int64_t c = d.idx(ci, cj, ck);
-        if (B.cell[c] != 0) continue;
-        if (B.tsnear[c]) {
-          set_err(B.err, BCFD_E_STATE);  // the thin-surface overlay has no adjoint
-          continue;
-        }
-        const SeedReader rd{{B.u, B.v, B.w, B.p}, f, x};
-        momentum_cell<Dual>(B, a, ci, cj, ck, c, rd, AdjOut{{ubar_t, vbar_t, wbar_t}, &acc});
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int o = 0; o < 125; ++o) {
+      unsigned fmask = 0u;
+#pragma unroll
+      for (int f = 0; f < 4; ++f) fmask |= ((m[4 * f + (o >> 5)] >> (o & 31)) & 1u) << f;
+      if (!fmask) continue;
+      const int ci = xi - (o % 5 - 2), cj = xj - ((o / 5) % 5 - 2), ck = xk - (o / 25 - 2);
+      if (ci < 2 || ci > d.nx + 1 || cj < 2 || cj > d.ny + 1 || ck < 2 || ck > d.nz + 1) continue;
+      const int64_t c = d.idx(ci, cj, ck);
+      if (B.cell[c] != 0) continue;
+      if (B.tsnear[c]) {
+        set_err(B.err, BCFD_E_STATE);  // the thin-surface overlay has no adjoint
+        continue;
       }
-      (f == 0 ? ub : f == 1 ? vb : f == 2 ? wb : pb)[x] += acc;
+      const SeedReader4 rd{{B.u, B.v, B.w, B.p}, x};
+      momentum_cell<Dual4>(B, a, ci, cj, ck, c, rd, AdjOut4{{ubar_t, vbar_t, wbar_t}, acc, fmask});
     }
+    ub[x] += acc[0];
+    vb[x] += acc[1];
+    wb[x] += acc[2];
+    pb[x] += acc[3];
   }
 }
 

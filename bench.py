@@ -539,7 +539,7 @@ def run_gpu(args):
                 "d2h_bytes_per_step": nbytes},
         "gpu_launches": profmx["timed_launches"],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic, "kernel": "k_sor_dc (mixed Poisson solve)",
+                     "frac": achieved / hbm, "traffic": traffic, "kernel": "mixed Poisson solve (k_sor_dc or k_sor_tb, as autotuned)",
                      "peak_source": peak_kind,
                      "note": "algorithmic bytes: 17 B per cell per FP32 sweep pair + FP64 residual/update passes; "
                              "the 64^3 and 96x64x64 blocks are L2-resident during a solve"},

@@ -415,17 +415,25 @@ def twelve_block(n_steps: int = 10, seed: int = SEED, moving: bool = False) -> C
                        plate_axes=(0.5, 0.125, 0.0125), motion=motion, motion_inputs=inputs)
 
 
-def tandem_plates(n_steps: int = 2, seed: int = SEED) -> Case:
+def tandem_plates(n_steps: int = 2, seed: int = SEED, moving: bool = False) -> Case:
     """Two thin plates in tandem on the 45M-cell layout: a coarse 384x256x256
     block over 6x4x4 (dx 1/64) and two fine 256x192x192 blocks at ratio 2
-    (dx 1/128), each holding a stationary rigid ellipsoidal plate of semi-axes
+    (dx 1/128), each holding a rigid ellipsoidal plate of semi-axes
     0.5 x 0.125 x 0.0125 (surface 51) at its centre; the plates are 1.5 chords
-    apart (centres at x = 1.75 and 4.25), Re = 1000 on the chord."""
+    apart (centres at x = 1.75 and 4.25), Re = 1000 on the chord.  With
+    `moving` both plates heave 0.125 sin(2 pi 0.25 t) and pitch about x
+    15 deg sin(2 pi 0.25 t + 90 deg) (one phase angle for every body, as the
+    reference's kinematics take it), amplitudes that keep each plate inside
+    its block's move margins (src/Search.F90:1010-1040)."""
     boxes = (((0.75, 2.75), (1.25, 2.75), (1.25, 2.75)),
              ((3.25, 5.25), (1.25, 2.75), (1.25, 2.75)))
+    motion = inputs = None
+    if moving:
+        motion = Motion(a0_deg=15.0, bfreq=0.25, yamp=0.125)
+        inputs = MotionInputs(aoa_deg=0.0, phase_deg=90.0, piv_pt=0.0, freq=0.25, dxmin=1.0 / 128.0)
     return multi_block(coarse=(384, 256, 256), domain=(6.0, 4.0, 4.0), fine_boxes=boxes, body=(0, 1),
                        diameter=1.0, reynolds=1000.0, n_steps=n_steps, seed=seed, plate=True,
-                       plate_axes=(0.5, 0.125, 0.0125))
+                       plate_axes=(0.5, 0.125, 0.0125), motion=motion, motion_inputs=inputs)
 
 
 def uniform_block(n=(384, 256, 256), lengths=(3.0, 2.0, 2.0), seed: int = SEED,

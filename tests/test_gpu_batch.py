@@ -28,6 +28,24 @@ def test_multi_block_parity_vs_oracle(plate):
     compare_search(o, s, "2 steps")
 
 
+@pytest.mark.parametrize("plate", [False, True])
+def test_two_bodies_parity_vs_oracle(plate):
+    # a body in each of two fine blocks (the tandem-plate layout in small):
+    # fields, SOR iteration counts and every Search output bitwise after 2 steps
+    case = synth.multi_block(n_steps=2, plate=plate, body=(0, 1))
+    assert sum(b.has_body for b in case.blocks) == 2
+    o = Oracle()
+    o.setup(case)
+    s = Solver(case)
+    s.setup()
+    for _ in range(2):
+        o.step()
+    s.run(2)
+    compare_fields(o, s, "2 steps")
+    compare_iters(o, s, "2 steps")
+    compare_search(o, s, "2 steps")
+
+
 def _run(case, precision, batching, steps):
     s = Solver(case)
     s.set_batching(batching)

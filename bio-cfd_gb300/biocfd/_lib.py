@@ -24,6 +24,19 @@ class BcfdError(RuntimeError):
     pass
 
 
+# bcfd_status of include/biocfd_gb300.h
+BCFD_OK = 0
+BCFD_E_HANDLE = -1
+BCFD_E_NOMEM = -2
+BCFD_E_NONFINITE = -3
+BCFD_E_NOTFOUND = -4
+BCFD_E_TIMEOUT = -5
+BCFD_E_ARG = -6
+BCFD_E_CUDA = -7
+BCFD_E_STATE = -8
+BCFD_E_CAPACITY = -9
+
+
 class StepConfig(C.Structure):
     """bcfd_step_config of include/biocfd_gb300.h."""
     _fields_ = [("deltat", c_double), ("re", c_double), ("uc", c_double), ("epsi", c_double),
@@ -42,6 +55,9 @@ _SIGS = {
     "bcfd_block_set_mixed_params": [c_i64, c_i64, c_double, c_int],
     "bcfd_block_set_solve_launch": [c_i64, c_int, c_int, c_int],
     "bcfd_set_batching": [c_int],
+    "bcfd_set_wait_limit_ns": [c_i64],
+    "bcfd_check_wait_limit": [C.POINTER(c_int), P_d],
+    "bcfd_block_set_list_capacity": [c_i64, c_i64],
     "bcfd_adjoint_set_solver": [c_int],
     "bcfd_poisson_solve_zero_bc": [c_i64, P_d, P_d, c_double, c_i64],
     "bcfd_poisson_solve_adjoint": [c_i64, P_d, P_d, c_double, c_i64],
@@ -52,6 +68,7 @@ _SIGS = {
                          c_double, c_i64, P_d, P_d, P_d, P_d, P_d, P_d, P_d],
     "bcfd_block_set_body_motion": [c_i64, P_d],
     "bcfd_shift_surface_nodes_initial": [c_i64, c_double, c_double, c_i64, c_double, c_double, c_double],
+    "bcfd_block_set_body_lag": [c_i64, c_double, c_double],
     "bcfd_compute_surface_variables": [c_i64, c_double, c_double, c_i64, c_double, c_double, c_double,
                                        c_double],
     "bcfd_set_motion_inputs": [c_double, c_double, c_double, c_double, c_i64, c_i64, c_double],

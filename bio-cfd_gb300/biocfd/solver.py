@@ -84,6 +84,9 @@ class Solver:
                     mo, mi = spec.motion, case.motion
                     p = np.array([mo.a0_deg, mo.bfreq, mo.yamp, *mo.shift], dtype=np.float64)
                     check(L.bcfd_block_set_body_motion(g, _pd(p)), "set_body_motion")
+                    if mo.lag_deg != 0.0:
+                        check(L.bcfd_block_set_body_lag(g, mo.lag_deg * np.pi / 180.0, mi.phase_deg * np.pi / 180.0),
+                              "set_body_lag")
                     check(L.bcfd_shift_surface_nodes_initial(g, mi.aoa_deg, mi.piv_pt, 0, case.dt, mi.dxmin, 0.0),
                           "shift_surface_nodes_initial")
                 check(L.bcfd_compute_surface_norm(g, m.inor), "compute_surface_norm")

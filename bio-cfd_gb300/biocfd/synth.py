@@ -44,6 +44,9 @@ class Motion:
     bfreq: float = 0.0
     yamp: float = 0.0
     shift: Tuple[float, float, float] = (0.0, 0.0, 0.0)
+    # phase lag (degrees) of this body's heave and pitch behind the shared
+    # kinematics (bcfd_block_set_body_lag); 0 = the reference's kinematics
+    lag_deg: float = 0.0
 
 
 @dataclass
@@ -314,12 +317,13 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
                 body=0, diameter: float = 0.25, reynolds: float = 300.0, n_steps: int = 2,
                 omega: float = 1.7, pc_ita_max: int = 5000, seed: int = SEED, plate: bool = False,
                 plate_axes=None, motion: Optional[Motion] = None,
-                motion_inputs: Optional[MotionInputs] = None) -> Case:
+                motion_inputs: Optional[MotionInputs] = None, lags_deg=None) -> Case:
     """A coarse block with several nested fine blocks of uneven sizes at ratio 2
     (one interface per fine block), a stationary sphere (or, with `plate`, a
     thin plate of surface 51) centred in fine block `body` (an index, or a
     tuple of indices for one body in each of several blocks).  Box edges must
-    lie on coarse faces."""
+    lie on coarse faces.  With a `motion`, `lags_deg` gives each body (in the
+    order of `body`) its phase lag behind the shared kinematics."""
     bodies = (body,) if isinstance(body, int) else tuple(body)
     cnx, cny, cnz = coarse
     L = domain
@@ -345,7 +349,8 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
                     # body-frame mesh placed by the motion; the search box
                     # covers the heave and the pitch
                     fs.mesh = ellipsoid_plate((0.0, 0.0, 0.0), ax, 0.5 * dxf)
-                    fs.motion = dataclasses.replace(motion, shift=tuple(c))
+                    lag = 0.0 if lags_deg is None else float(lags_deg[bodies.index(q)])
+                    fs.motion = dataclasses.replace(motion, shift=tuple(c), lag_deg=lag)
                     reach = ax + np.array([0.0, motion.yamp + ax[1], ax[1]])
                     fs.search_box = search_box_for(fs, c - reach, c + reach)
                 else:
@@ -415,25 +420,28 @@ def twelve_block(n_steps: int = 10, seed: int = SEED, moving: bool = False) -> C
                        plate_axes=(0.5, 0.125, 0.0125), motion=motion, motion_inputs=inputs)
 
 
-def tandem_plates(n_steps: int = 2, seed: int = SEED, moving: bool = False) -> Case:
-    """Two thin plates in tandem on the 45M-cell layout: a coarse 384x256x256
+def tandem_plates(n_steps: int = 2, seed: int = SEED, moving: bool = False, lag_deg: float = 90.0) -> Case:
+    """Two thin plates in tandem on the 44M-cell layout: a coarse 384x256x256
     block over 6x4x4 (dx 1/64) and two fine 256x192x192 blocks at ratio 2
     (dx 1/128), each holding a rigid ellipsoidal plate of semi-axes
     0.5 x 0.125 x 0.0125 (surface 51) at its centre; the plates are 1.5 chords
     apart (centres at x = 1.75 and 4.25), Re = 1000 on the chord.  With
-    `moving` both plates heave 0.125 sin(2 pi 0.25 t) and pitch about x
-    15 deg sin(2 pi 0.25 t + 90 deg) (one phase angle for every body, as the
-    reference's kinematics take it), amplitudes that keep each plate inside
-    its block's move margins (src/Search.F90:1010-1040)."""
+    `moving` the leading plate heaves 0.125 sin(2 pi 0.25 t) and pitches about
+    x 15 deg sin(2 pi 0.25 t + 90 deg), starting at its t = 0 angle of attack
+    (15 deg); the trailing plate does the same `lag_deg` behind
+    (bcfd_block_set_body_lag), starting at its own t = 0 state.  The
+    amplitudes keep each plate inside its block's move margins
+    (src/Search.F90:1010-1040)."""
     boxes = (((0.75, 2.75), (1.25, 2.75), (1.25, 2.75)),
              ((3.25, 5.25), (1.25, 2.75), (1.25, 2.75)))
     motion = inputs = None
     if moving:
         motion = Motion(a0_deg=15.0, bfreq=0.25, yamp=0.125)
-        inputs = MotionInputs(aoa_deg=0.0, phase_deg=90.0, piv_pt=0.0, freq=0.25, dxmin=1.0 / 128.0)
+        inputs = MotionInputs(aoa_deg=15.0, phase_deg=90.0, piv_pt=0.0, freq=0.25, dxmin=1.0 / 128.0)
     return multi_block(coarse=(384, 256, 256), domain=(6.0, 4.0, 4.0), fine_boxes=boxes, body=(0, 1),
                        diameter=1.0, reynolds=1000.0, n_steps=n_steps, seed=seed, plate=True,
-                       plate_axes=(0.5, 0.125, 0.0125), motion=motion, motion_inputs=inputs)
+                       plate_axes=(0.5, 0.125, 0.0125), motion=motion, motion_inputs=inputs,
+                       lags_deg=(0.0, lag_deg) if moving else None)
 
 
 def uniform_block(n=(384, 256, 256), lengths=(3.0, 2.0, 2.0), seed: int = SEED,

@@ -122,14 +122,14 @@ using namespace bcfd;
 extern "C" {
 
 int bcfd_adjoint_set_solver(int precision) {
-  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  LibLock lk;
   if (precision != 0 && precision != 1) return BCFD_E_ARG;
   lib().adj_precision = precision;
   return 0;
 }
 
 int bcfd_poisson_solve_zero_bc(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax) {
-  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  LibLock lk;
   HostBlock* hb = get_block(h);
   if (!hb) return BCFD_E_HANDLE;
   if (!r || !x || !(tol > 0.0) || itmax < 1) return BCFD_E_ARG;
@@ -139,7 +139,7 @@ int bcfd_poisson_solve_zero_bc(bcfd_handle h, const double* r, double* x, double
 int bcfd_momentum_tangent(bcfd_handle h, double deltat, double re, const double* du, const double* dv,
                           const double* dw, const double* dp, double* ut, double* vt, double* wt, double* dut,
                           double* dvt, double* dwt) {
-  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  LibLock lk;
   HostBlock* hb = get_block(h);
   if (!hb) return BCFD_E_HANDLE;
   const double* in[4] = {du, dv, dw, dp};
@@ -177,7 +177,7 @@ int bcfd_momentum_tangent(bcfd_handle h, double deltat, double re, const double*
 
 int bcfd_momentum_adjoint(bcfd_handle h, double deltat, double re, const double* utb, const double* vtb,
                           const double* wtb, double* ub, double* vb, double* wb, double* pb) {
-  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  LibLock lk;
   HostBlock* hb = get_block(h);
   if (!hb) return BCFD_E_HANDLE;
   const double* in[3] = {utb, vtb, wtb};
@@ -210,7 +210,7 @@ int bcfd_momentum_adjoint(bcfd_handle h, double deltat, double re, const double*
 }
 
 int bcfd_poisson_solve_adjoint(bcfd_handle h, const double* r, double* x, double tol, int64_t itmax) {
-  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  LibLock lk;
   HostBlock* hb = get_block(h);
   if (!hb) return BCFD_E_HANDLE;
   if (!r || !x || !(tol > 0.0) || itmax < 1) return BCFD_E_ARG;

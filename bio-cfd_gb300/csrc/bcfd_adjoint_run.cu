@@ -512,7 +512,7 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
                      const double* wv, const double* ww, const double* wp, const double* stress_seed, double mu_f,
                      double rho_f, double adj_tol, int64_t adj_itmax, double* J, double* dj_duc,
                      double* dj_dkin, double* gu, double* gv, double* gw, double* gp) {
-  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  LibLock lk;
   HostBlock* hb = get_block(h);
   if (!hb) return BCFD_E_HANDLE;
   if (!cfg || n_steps < 1 || every < 1 || !wu || !wv || !ww || !wp || !J || !(adj_tol > 0.0) || adj_itmax < 1)
@@ -525,7 +525,6 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   for (auto& [g, b] : all) {
     if (b->motion.on || !b->d.ca[0] || !b->d.Acx) return BCFD_E_STATE;
     if (g != all.front().first && b->is_coarse) return BCFD_E_STATE;
-    if (b->has_body && b->d.ne > BCFD_STRESS_NOALLOC_MAX_ELEMS) return BCFD_E_CAPACITY;
   }
   std::vector<HostInterface*> ifs;
   for (HostInterface* it : lib().ifs)
@@ -595,7 +594,12 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
     BCFD_LAUNCHED();
     if (use_stress) {
       double co[4];
-      TRY_R(launch_stress_noalloc(hb, mu_f, rho_f, co));
+      // the fixed scratch when the body fits in it (no allocation per
+      // step), else the allocating launch: same kernels, same result
+      if (hb->d.ne <= BCFD_STRESS_NOALLOC_MAX_ELEMS)
+        TRY_R(launch_stress_noalloc(hb, mu_f, rho_f, co));
+      else
+        TRY_R(launch_stress(hb, mu_f, rho_f, co));
       for (int t = 0; t < 4; ++t) jstress += stress_seed[t] * co[t];
     }
     if (n % K == 0 && n < n_steps) TRY_R(save_all(cps + (size_t)(n / K) * S));

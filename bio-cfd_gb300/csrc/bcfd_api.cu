@@ -100,10 +100,19 @@ int sync_block_table() {
   return 0;
 }
 
+namespace {
+// One grid barrier whose arrival target is one CTA more than the launch has:
+// nothing completes it, so every waiting CTA gives up after the wait limit
+// (recording BCFD_E_TIMEOUT and setting the abandon bit, which releases the
+// others at once).  Exercises the bounded-wait path of the persistent kernels.
+__global__ void k_wait_unreachable(GridBar gb) { (void)grid_sync(gb); }
+}  // namespace
+
 GridBar make_bar(int* err, unsigned nblocks) {
   GridBar g{};
   g.err = err;
   g.nblocks = nblocks;
+  g.limit_ns = lib().wait_limit_ns;
   return g;
 }
 
@@ -519,7 +528,7 @@ int shift_block_grid(HostBlock* hb, double cx, double cy, double cz) {
 
 using namespace bcfd;
 
-#define LOCK() std::lock_guard<std::recursive_mutex> _lk(lib().mu)
+#define LOCK() ::bcfd::LibLock _lk
 #define GETB(h)                      \
   HostBlock* hb = get_block(h);      \
   if (!hb) return BCFD_E_HANDLE;
@@ -537,6 +546,62 @@ int bcfd_init(int device) {
   L.device = device;
   BCFD_CUDA(cudaStreamCreateWithFlags(&L.s, cudaStreamNonBlocking));
   L.ready = true;
+  return 0;
+}
+
+int bcfd_set_wait_limit_ns(int64_t ns) {
+  LOCK();
+  if (ns < 0 || ns > 600000000000ll) return BCFD_E_ARG;
+  lib().wait_limit_ns = ns == 0 ? kBarrierLimitNs : (uint64_t)ns;
+  return 0;
+}
+
+int bcfd_check_wait_limit(int* status, double* waited_ms) {
+  LOCK();
+  if (!lib().ready) return BCFD_E_STATE;
+  if (!status) return BCFD_E_ARG;
+  // [0] arrival counter (8 bytes), [1] error word
+  unsigned long long* w = nullptr;
+  BCFD_CUDA(cudaMalloc(&w, 2 * sizeof(unsigned long long)));
+  int r = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  auto ck = [&](cudaError_t e) {
+    if (e != cudaSuccess && !r) {
+      report_cuda(e, "check_wait_limit", __FILE__, __LINE__);
+      r = BCFD_E_CUDA;
+    }
+  };
+  ck(cudaMemsetAsync(w, 0, 2 * sizeof(unsigned long long), stream()));
+  ck(cudaEventCreate(&e0));
+  ck(cudaEventCreate(&e1));
+  if (!r) {
+    const unsigned ctas = 2;
+    GridBar gb = make_bar(reinterpret_cast<int*>(w + 1), ctas + 1);
+    gb.ctr = w;
+    ck(cudaEventRecord(e0, stream()));
+    k_wait_unreachable<<<ctas, 32, 0, stream()>>>(gb);
+    r = note_launch();
+    ck(cudaEventRecord(e1, stream()));
+  }
+  int e = 0;
+  if (!r) ck(cudaMemcpyAsync(&e, w + 1, sizeof(int), cudaMemcpyDeviceToHost, stream()));
+  ck(cudaStreamSynchronize(stream()));
+  float ms = 0.0f;
+  if (!r) ck(cudaEventElapsedTime(&ms, e0, e1));
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaFree(w);
+  if (r) return r;
+  *status = e;
+  if (waited_ms) *waited_ms = ms;
+  return 0;
+}
+
+int bcfd_block_set_list_capacity(bcfd_handle h, int64_t cap) {
+  LOCK();
+  GETB(h);
+  if (cap < 0 || cap > hb->cap_ib_alloc) return BCFD_E_ARG;
+  hb->d.cap_ib = cap == 0 ? hb->cap_ib_alloc : (int)cap;
   return 0;
 }
 
@@ -641,6 +706,7 @@ int bcfd_block_create(int64_t nx, int64_t ny, int64_t nz, const double* x1, cons
   // IB / TS list capacity: every cell up to 4M cells (a list that outgrows it
   // reports BCFD_E_CAPACITY)
   D.cap_ib = (int)std::max<int64_t>(64, std::min<int64_t>((int64_t)nx * ny * nz, (int64_t)1 << 22));
+  hb->cap_ib_alloc = D.cap_ib;
   A(&D.ib_i, D.cap_ib); A(&D.ib_j, D.cap_ib); A(&D.ib_k, D.cap_ib);
   for (int q = 0; q < 7; ++q) { A(&D.nel[q], D.cap_ib); A(&D.nd[q], D.cap_ib); }
   A(&D.ts_idx, D.cap_ib);
@@ -902,6 +968,16 @@ int bcfd_block_set_body_motion(bcfd_handle h, const double* p) {
   }
   hb->node_id_host = id;
   hb->motion_r0 = r0;
+  return 0;
+}
+
+int bcfd_block_set_body_lag(bcfd_handle h, double lag, double phase_angle) {
+  LOCK();
+  GETB(h);
+  if (!hb->motion.on) return BCFD_E_STATE;
+  if (!std::isfinite(lag) || !std::isfinite(phase_angle)) return BCFD_E_ARG;
+  hb->motion.lag = lag;
+  hb->motion.lag_phase = phase_angle;
   return 0;
 }
 
@@ -1245,7 +1321,8 @@ int bcfd_block_get_solve_launch(bcfd_handle h, int* out) {
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant) {
   LOCK();
   GETB(h);
-  if (inner_sweeps < 0 || inner_sweeps > 100000 || omega < 0.0 || omega >= 2.0 || variant < 0 || variant > 4)
+  if (inner_sweeps < 0 || inner_sweeps > 100000 || omega < 0.0 || omega >= 2.0 || variant < 0 || variant > 4 ||
+      variant == 2)  // the cluster-resident variant was withdrawn
     return BCFD_E_ARG;
   hb->dc_inner = (int)inner_sweeps;
   hb->dc_omega = omega;

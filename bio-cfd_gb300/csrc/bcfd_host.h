@@ -21,6 +21,10 @@ struct BodyMotion {
   double xpth1 = 0, xpth2 = 0, ypth2 = 0, xchg = 0, ychg = 0, xmove = 0, ymove = 0, zmove = 0;
   double xt = 0, yt = 0, inity_cent = 0, nxty_cent = 0, initx_cent = 0, nxtx_cent = 0,
          initz_cent = 0, nxtz_cent = 0;
+  // phase lag of this body's heave and pitch behind the kinematics all bodies
+  // share (radians; 0 = the reference's single-phase kinematics) and the
+  // shared pitch phase angle its initial placement is taken against
+  double lag = 0, lag_phase = 0;
 };
 
 // Node placement of one step (computeSurfaceVariables): the rotation's
@@ -87,15 +91,16 @@ struct HostBlock {
   double* coef_buf = nullptr;      // device Acx/Acy/Acz + ca/ck tables
   float* grid_f32 = nullptr;       // device dxa/dya/dza rounded to FP32
   float* coef_f32 = nullptr;       // device Acx/Acy/Acz rounded to FP32
-  float* pcf2 = nullptr;
+  float* pcf2 = nullptr;           // second FP32 correction buffer (both colours) of the temporal-blocked sweeps
   int64_t mk = 0, mkx1 = 0, mkx2 = 0;  // findDistnode's extreme surface nodes (1-based)
   // fine-block moves (src/Search.F90:997-1370): the last move and the index
   // ranges of the old (cpy) and new (cpy_mv) positions of the moved data,
   // which keep their values when a search finds no index, as the reference's
   double* mv_dum = nullptr;  // u, v, w, p before the move
   int64_t move_amt[3] = {0, 0, 0};
-  int64_t cpy[6] = {0, 0, 0, 0, 0, 0}, cpy_mv[6] = {0, 0, 0, 0, 0, 0};           // second FP32 correction buffer (both colours) of the temporal-blocked sweeps
+  int64_t cpy[6] = {0, 0, 0, 0, 0, 0}, cpy_mv[6] = {0, 0, 0, 0, 0, 0};
   int surf_cap_e = 0, surf_cap_n = 0;
+  int cap_ib_alloc = 0;            // IB/TS list entries allocated (d.cap_ib may be set lower)
   // per-block barrier words for persistent kernels: [count, gen]
   unsigned* bar = nullptr;
   unsigned* prog = nullptr;        // per-tile phase counters of the tiled solves
@@ -103,7 +108,8 @@ struct HostBlock {
   // (0 = defaults chosen from the block size)
   int dc_inner = 0;
   double dc_omega = 0.0;
-  // mixed solve kernel: 0 = cluster-resident when the block fits, 1 = grid-wide
+  // mixed solve kernel: 0 = library default, 1 = grid-wide phase barriers,
+  // 3 = neighbour sync, 4 = temporal-blocked
   int dc_variant = 0;
   int solve_threads = 0;           // threads per CTA of the tiled solves (0: 256)
   int solve_ctas_per_sm = 0;       // co-resident CTAs per SM cap (0: occupancy limit)
@@ -169,10 +175,26 @@ struct Lib {
   std::vector<unsigned char> step_key;  // what the capture depends on
   std::vector<unsigned char> eager_key; // the key left by the last eager step
   int adj_precision = 1;  // zero-BC and adjoint solves: 0 FP64 SOR, 1 FP32 sweeps + FP64 correction
+  uint64_t wait_limit_ns = kBarrierLimitNs;  // longest single device-side wait
   int64_t step_kernels = 0;              // kernels in the captured step
 };
 
 Lib& lib();
+
+// Held by every entry point: serialises calls and, once bcfd_init has run,
+// makes the library's device current on the calling thread, so a host thread
+// other than the one that called bcfd_init (which starts on device 0) can
+// call in.  The calling thread's current device is left at the library's.
+struct LibLock {
+  std::lock_guard<std::recursive_mutex> g;
+  LibLock() : g(lib().mu) {
+    if (lib().ready) {
+      int cur = -1;
+      if (cudaGetDevice(&cur) != cudaSuccess || cur != lib().device) cudaSetDevice(lib().device);
+    }
+  }
+};
+
 HostBlock* get_block(bcfd_handle h);
 HostInterface* get_iface(bcfd_handle h);
 
@@ -228,9 +250,6 @@ int launch_max_div(HostBlock* hb, bool tfield);
 int64_t* prof_log();
 void prof_mark(bool begin);
 int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol);
-// k_sor_cluster.cu
-int cluster_solve_fits(HostBlock* hb);
-int launch_sor_cluster(HostBlock* hb, int64_t itmax, double dt, double div_tol, int inner, float omega);
 // k_momentum.cu
 int launch_momentum(HostBlock* hb, double dt, double re, bool fp32);
 int launch_momentum_tangent(HostBlock* hb, double dt, double re, const double* const du[4], double* const val[3],

@@ -183,6 +183,7 @@ struct GridBar {
   unsigned long long* ctr;
   int* err;          // set to BCFD_E_TIMEOUT when a wait exceeds the limit
   unsigned nblocks;
+  unsigned long long limit_ns;  // longest a single wait may last
 };
 constexpr unsigned long long kBarAbandon = 1ull << 63;
 
@@ -226,7 +227,7 @@ __device__ inline int ld_acquire_i(const int* p) {
   return v;
 }
 
-constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // 2 s per wait
+constexpr unsigned long long kBarrierLimitNs = 2000000000ull;  // default: 2 s per wait
 
 // Returns false (on every thread of the CTA) once the barrier was abandoned:
 // a wait timed out somewhere, or a CTA saw a recorded error while waiting.
@@ -254,7 +255,7 @@ __device__ inline bool grid_sync(const GridBar& gb) {
             ok = 0;
             break;
           }
-          if (globaltimer_ns() - t0 > kBarrierLimitNs) {
+          if (globaltimer_ns() - t0 > gb.limit_ns) {
             atomicCAS(gb.err, 0, BCFD_E_TIMEOUT);
             atomicOr(gb.ctr, kBarAbandon);
             ok = 0;
@@ -273,8 +274,15 @@ __device__ inline bool grid_sync(const GridBar& gb) {
 // ---------------------------------------------------------------------------
 // reductions
 // ---------------------------------------------------------------------------
+// max that propagates NaN (fmax drops a NaN operand): equal to fmax for
+// non-NaN operands, so a reduction of finite values is unchanged, while a NaN
+// anywhere reaches the result and the non-finite checks see it
+__device__ __forceinline__ double nmax(double a, double b) { return (a > b || a != a) ? a : b; }
+// true for NaN and +-Inf
+__device__ __forceinline__ bool non_finite(double x) { return !(fabs(x) <= 1.7976931348623157e308); }
+
 __device__ inline double warp_max(double v) {
-  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  for (int o = 16; o > 0; o >>= 1) v = nmax(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 // block-wide max; result valid on thread 0. `sh` needs blockDim.x/32 doubles.

@@ -484,6 +484,7 @@ std::vector<unsigned char> step_key(const bcfd_step_config& c) {
   const Lib& L = lib();
   put(&L.gen, sizeof L.gen);
   put(&L.batch, sizeof L.batch);
+  put(&L.wait_limit_ns, sizeof L.wait_limit_ns);
   for (const HostBlock* hb : L.blocks) {
     const unsigned char none = 0;
     if (!hb) { put(&none, 1); continue; }
@@ -566,7 +567,7 @@ int run_one_step(const bcfd_step_config& cfg) { return step_once(cfg); }
 
 using namespace bcfd;
 
-#define LOCK() std::lock_guard<std::recursive_mutex> _lk(lib().mu)
+#define LOCK() ::bcfd::LibLock _lk
 
 extern "C" {
 

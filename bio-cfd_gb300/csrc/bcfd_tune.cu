@@ -150,7 +150,7 @@ int tune_block(HostBlock* hb, Tuned* out) {
 using namespace bcfd;
 
 extern "C" int bcfd_autotune(int64_t* n_tuned) {
-  std::lock_guard<std::recursive_mutex> lk(lib().mu);
+  LibLock lk;
   if (!lib().ready) return BCFD_E_STATE;
   // blocks solved together in one batched launch share that launch's shape;
   // tune the ones solved alone: the first block, and the others when they

@@ -95,7 +95,15 @@ int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_
                                 double dxmin, double totime) {
   BodyMotion& m = hb->motion;
   const double pi = 4.0 * std::atan(1.0);
-  const double aoa1 = aoa * pi / 180.0;
+  // a lagging body starts where its lagged kinematics put it at t = 0 relative
+  // to the shared ones: its angle differs by the pitch's change over the lag,
+  // its heave position is yamp sin(-lag) (both 0 without a lag)
+  double aoa_b = aoa, y0 = 0.0;
+  if (m.lag != 0.0) {
+    aoa_b = aoa + m.a0 * (std::sin(m.lag_phase - m.lag) - std::sin(m.lag_phase));
+    y0 = m.yamp * std::sin(-m.lag);
+  }
+  const double aoa1 = aoa_b * pi / 180.0;
   const double bdfr = 15, bdy = 15 * dxmin;
   m.xmove = m.ymove = m.zmove = 0.0;
   m.a0 = m.a0 * pi / 180.0;
@@ -104,8 +112,9 @@ int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_
   m.xpth2 = m.xshift - ((double)ita * dxmin * kXfact);
   m.ypth2 = (m.yamp) * std::sin(angt * m.xshift);
   Kin& D = hb->kin;
+  const double ysh = m.lag != 0.0 ? m.yshift + y0 : m.yshift;
   D.piv_x = m.xshift;
-  D.piv_y = m.yshift;
+  D.piv_y = ysh;
   D.piv_z = m.zshift;
   D.thetaDot1 = D.thetaDot2 = D.alphaDot = 0.0;
   D.thetaDDot1 = D.thetaDDot2 = 0.0;
@@ -114,10 +123,10 @@ int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_
   D.yddot = -(angt * angt * bdy * std::sin(2 * pi * bdfr * totime));
   m.xt = m.xshift - ((double)ita * dxmin * kXfact);
   D.xdot = -(dxmin * kXfact) / deltat;
-  m.inity_cent = m.nxty_cent = m.yshift;
+  m.inity_cent = m.nxty_cent = ysh;
   m.initx_cent = m.nxtx_cent = m.xshift;
   m.initz_cent = m.nxtz_cent = m.zshift;
-  TRY_R(stage_place(hb, aoa1, piv_pt, m.xshift, m.yshift, 0.0, m.zshift, 0.0, 0));
+  TRY_R(stage_place(hb, aoa1, piv_pt, m.xshift, ysh, 0.0, m.zshift, 0.0, 0));
   return apply_surface_variables(hb);
 }
 
@@ -199,7 +208,10 @@ int stage_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, in
   BodyMotion& m = hb->motion;
   Kin& D = hb->kin;
   const double pi = 4.0 * std::atan(1.0);
-  const double aoa1 = (m.a0) * std::sin(2.0 * pi * freq * (totime + deltat) + phase_angle);
+  // pitch and heave phases; a lagging body subtracts its lag from both
+  double parg = 2.0 * pi * freq * (totime + deltat) + phase_angle;
+  if (m.lag != 0.0) parg = parg - m.lag;
+  const double aoa1 = (m.a0) * std::sin(parg);
   const double ang_theta = 2.0 * pi * freq;
   const double bdfr = m.bfreq, bdy = m.yamp;
   const double angt = 2.0 * pi * bdfr;
@@ -207,16 +219,21 @@ int stage_surface_variables(HostBlock* hb, double phase_angle, double piv_pt, in
   m.ypth2 = (m.yamp) * std::sin(angt * m.xpth2);
   m.xchg = m.xpth2 - m.xpth1;
   m.xpth1 = m.xpth2;
-  D.thetaDot1 = ang_theta * m.a0 * std::cos(2.0 * pi * freq * (totime + deltat) + phase_angle);
-  D.thetaDDot1 = -(ang_theta * ang_theta * m.a0 * std::sin(2.0 * pi * freq * (totime + deltat) + phase_angle));
+  D.thetaDot1 = ang_theta * m.a0 * std::cos(parg);
+  D.thetaDDot1 = -(ang_theta * ang_theta * m.a0 * std::sin(parg));
   D.thetaDot2 = -D.thetaDot1;
   D.thetaDDot2 = -D.thetaDDot1;
-  m.yt = bdy * std::sin(angt * (totime));
-  D.ydot = angt * bdy * std::cos(angt * (totime));
-  D.yddot = -(angt * angt * bdy * std::sin(angt * (totime)));
+  double h0 = angt * (totime), h1 = angt * (totime - deltat);
+  if (m.lag != 0.0) {
+    h0 = h0 - m.lag;
+    h1 = h1 - m.lag;
+  }
+  m.yt = bdy * std::sin(h0);
+  D.ydot = angt * bdy * std::cos(h0);
+  D.yddot = -(angt * angt * bdy * std::sin(h0));
   m.xt = m.xpth2;
   D.xdot = -(dxmin * kXfact) / deltat;
-  m.ychg = m.yt - bdy * std::sin(angt * (totime - deltat));
+  m.ychg = m.yt - bdy * std::sin(h1);
   m.ymove = m.yt;
   m.xmove = m.xchg;
   m.zmove = 0.0;

@@ -134,7 +134,7 @@ __device__ __forceinline__ bool tile_wait(const TileMap& tm, const GridBar& gb, 
             ok = 0;
             break;
           }
-          if (globaltimer_ns() - t0 > kBarrierLimitNs) {
+          if (globaltimer_ns() - t0 > gb.limit_ns) {
             atomicCAS(gb.err, 0, BCFD_E_TIMEOUT);
             atomicOr(gb.ctr, kBarAbandon);
             ok = 0;
@@ -213,7 +213,7 @@ __device__ __forceinline__ void tile_half64(const DevBlock& B, const Tile& t, do
     double old;
     const double nv = sor64_cell<C>(B, p, omega, old);
     own[p.pi] = nv;
-    lmax = fmax(lmax, fabs(nv - old));
+    lmax = nmax(lmax, fabs(nv - old));
   }
 }
 
@@ -249,7 +249,7 @@ __device__ __forceinline__ double tile_resid_max64(const DevBlock& B, const Tile
   w.init(threadIdx.x, blockDim.x, B.d.NXH, t.nj);
   for (int q = threadIdx.x; q < n; q += blockDim.x, w.next()) {
     const Pos p = tile_pos<C>(B, t, w, true);
-    if (p.on) m = fmax(m, fabs(resid64_cell<C>(B, p)));
+    if (p.on) m = nmax(m, fabs(resid64_cell<C>(B, p)));
   }
   return m;
 }
@@ -280,7 +280,7 @@ __device__ __forceinline__ double resid_max64(const DevBlock& B, const RowMap& r
     ax = fma(B.Acy[j - 2 + 2 * d.ny], __ldcg(o + pi + sy), ax);
     ax = fma(B.Acz[k - 2], __ldcg(o + pi - sz), ax);
     ax = fma(B.Acz[k - 2 + 2 * d.nz], __ldcg(o + pi + sz), ax);
-    m = fmax(m, fabs(B.rhs[C][pi] - ax));
+    m = nmax(m, fabs(B.rhs[C][pi] - ax));
   }
   return m;
 }
@@ -354,7 +354,7 @@ __device__ __forceinline__ void sor64_body(const DevBlock& B, const SorArgs& a, 
       if (a.res_tol > 0.0) {
         // residual-target mode: the residual needs the neighbours' sweep pair
         if (!tile_wait(tm, gb, t, ph)) { ok = false; break; }
-        lmax = fmax(tile_resid_max64<1>(B, t), tile_resid_max64<0>(B, t)) * a.dt;
+        lmax = nmax(tile_resid_max64<1>(B, t), tile_resid_max64<0>(B, t)) * a.dt;
         tile_publish(tm, t, ++ph);
       }
       const double m = block_max(lmax, sh);
@@ -364,13 +364,13 @@ __device__ __forceinline__ void sor64_body(const DevBlock& B, const SorArgs& a, 
       ++check;
     }
     if (a.res_tol > 0.0 ? (derr4 <= a.res_tol) : (derr4 < a.epsi)) break;
-    if (it > a.itmax) break;
+    if (it > a.itmax || non_finite(derr4)) break;
   }
   if (cta == 0 && threadIdx.x == 0) {
     log_solve(a.log, it - it0, 0, B.cnt[C_FLUID], 0);
     st->niter = it;
     st->derr2 = derr4;
-    if (ok && !(derr4 == derr4)) set_err(B.err, BCFD_E_NONFINITE);
+    if (ok && non_finite(derr4)) set_err(B.err, BCFD_E_NONFINITE);
   }
 }
 
@@ -516,8 +516,8 @@ __device__ __forceinline__ double tile_residual64v(const DevBlock& B, const Tile
       ax = fma(az3, u == 0 ? ot.x : ot.y, ax);
       r[u] = (u == 0 ? b2.x : b2.y) * inv_dt - ax;
     }
-    if (mk.x) m = fmax(m, fabs(r[0]));
-    if (mk.y) m = fmax(m, fabs(r[1]));
+    if (mk.x) m = nmax(m, fabs(r[0]));
+    if (mk.y) m = nmax(m, fabs(r[1]));
     *reinterpret_cast<float2*>(rf + pi) = make_float2(mk.x ? (float)r[0] : 0.0f, mk.y ? (float)r[1] : 0.0f);
   }
   return m;
@@ -563,13 +563,13 @@ __device__ __forceinline__ void sor_dc_body(const DevBlock& B, const DcArgs& a, 
   int outer = 0;
   for (;; ++outer) {
     if (!tile_wait(tm, gb, t, ph)) return;
-    double m = fmax(tile_residual64v<1>(B, t, a.inv_dt), tile_residual64v<0>(B, t, a.inv_dt));
+    double m = nmax(tile_residual64v<1>(B, t, a.inv_dt), tile_residual64v<0>(B, t, a.inv_dt));
     tile_publish(tm, t, ++ph);
     m = block_max(m, sh);
     if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[outer % 3], m);
     if (!grid_sync(gb)) return;
     res = take_slot(st, outer, cta);
-    if (a.dt * res <= a.div_tol || outer >= a.max_outer || !(res == res)) break;
+    if (a.dt * res <= a.div_tol || outer >= a.max_outer || non_finite(res)) break;
     for (int it = 0; it < a.inner; ++it) {
       if (!tile_wait(tm, gb, t, ph)) return;
       tile_half32<1>(B, t, a.omega);
@@ -589,7 +589,7 @@ __device__ __forceinline__ void sor_dc_body(const DevBlock& B, const DcArgs& a, 
     st->niter = st->niter + sweeps;
     st->derr2 = a.dt * res;
     st->pad[1] = a.dt * res;  // the residual this solve leaves behind
-    if (!(res == res)) set_err(B.err, BCFD_E_NONFINITE);
+    if (non_finite(res)) set_err(B.err, BCFD_E_NONFINITE);
   }
 }
 
@@ -813,12 +813,12 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_sor_tb(DevBlock B, DcArgs a, 
   double res = 0.0;
   int outer = 0;
   for (;; ++outer) {
-    double m = fmax(tile_residual64v<1>(B, t, a.inv_dt), tile_residual64v<0>(B, t, a.inv_dt));
+    double m = nmax(tile_residual64v<1>(B, t, a.inv_dt), tile_residual64v<0>(B, t, a.inv_dt));
     m = block_max(m, sh);
     if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[outer % 3], m);
     if (!grid_sync(gb)) return;
     res = take_slot(st, outer, cta);
-    if (a.dt * res <= a.div_tol || outer >= a.max_outer || !(res == res)) break;
+    if (a.dt * res <= a.div_tol || outer >= a.max_outer || non_finite(res)) break;
     int cur = 0;
     for (int it = 0; it < a.inner; ++it) {
       const float* const* src = cur ? E1 : E0;
@@ -848,7 +848,7 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_sor_tb(DevBlock B, DcArgs a, 
     st->niter = st->niter + sweeps;
     st->derr2 = a.dt * res;
     st->pad[1] = a.dt * res;
-    if (!(res == res)) set_err(B.err, BCFD_E_NONFINITE);
+    if (non_finite(res)) set_err(B.err, BCFD_E_NONFINITE);
   }
 }
 
@@ -903,7 +903,7 @@ __global__ void k_resid(DevBlock B, double dt) {
   __shared__ double sh[32];
   const int64_t total = (int64_t)B.d.NXH * B.d.ny * B.d.nz;
   const RowMap rm{B.d.NXH, B.d.ny};
-  const double m = block_max(fmax(resid_max64<1>(B, rm, total), resid_max64<0>(B, rm, total)), sh);
+  const double m = block_max(nmax(resid_max64<1>(B, rm, total), resid_max64<0>(B, rm, total)), sh);
   if (threadIdx.x == 0) atomic_max_nonneg(&B.stats->pad[1], m * dt);
 }
 
@@ -950,7 +950,7 @@ struct SteadyOp {
       const double eu = fabs((B.ut[c] - B.u[c])) / dt;
       const double ev = fabs((B.vt[c] - B.v[c])) / dt;
       const double ew = fabs((B.wt[c] - B.w[c])) / dt;
-      m = fmax(fmax(fmax(m, eu), ev), ew);
+      m = nmax(nmax(nmax(m, eu), ev), ew);
     }
     m = block_max(m, sh);
     if (threadIdx.x == 0) atomic_max_nonneg(&B.stats->derr_std_st, m);
@@ -973,7 +973,7 @@ struct MaxDivOp {
       if (B.cell[c] != 0) continue;
       const double dv = (U[c] - U[c - 1]) / B.dxa[i - 1] + (V[c] - V[c - d.NX]) / B.dya[j - 1] +
                         (W[c] - W[c - (int64_t)d.NX * d.NY]) / B.dza[k - 1];
-      m = fmax(m, fabs(dv));
+      m = nmax(m, fabs(dv));
     }
     m = block_max(m, sh);
     if (threadIdx.x == 0) atomic_max_nonneg(tfield ? &B.stats->pad[0] : &B.stats->maxdiv, m);
@@ -1205,15 +1205,6 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   DevBlock& B = hb->d;
   const int64_t np = B.d.npacked();
   const int nmax0 = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
-  if (hb->dc_variant == 2 && cluster_solve_fits(hb)) {
-    k_rhs<<<grid_for(np, 256), 256, 0, stream()>>>(B, dt);
-    BCFD_LAUNCHED();
-    // the whole block fits in one cluster's distributed shared memory
-    const int inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
-    const double om = hb->dc_omega > 0 ? hb->dc_omega : 2.0 / (1.0 + std::sin(3.14159265358979323846 / nmax0));
-    TRY_R(launch_sor_cluster(hb, itmax, dt, div_tol, inner, (float)std::min(1.97, std::max(1.0, om))));
-    return launch_residual(hb, dt);
-  }
   for (int c = 0; c < 2; ++c) BCFD_CUDA(cudaMemsetAsync(B.pcf[c], 0, np * sizeof(float), stream()));
   if (hb->dc_variant == 4 && tb_solve_fits(hb)) return launch_sor_tb(hb, itmax, dt, div_tol);
   const int threads = hb->dc_threads > 0 ? std::min(hb->dc_threads, kDcThreads) : kDcThreads;

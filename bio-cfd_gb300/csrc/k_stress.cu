@@ -319,8 +319,10 @@ int launch_stress(HostBlock* hb, double mu_f, double rho_f, double* out_host) {
   if (ne <= 0) return BCFD_E_STATE;
   double* part = nullptr;
   double* out = nullptr;
-  BCFD_CUDA(cudaMalloc(&part, (size_t)ne * 7 * sizeof(double)));
-  BCFD_CUDA(cudaMalloc(&out, 4 * sizeof(double)));
+  // one allocation holds the partials and the 4 coefficients, so no error
+  // path can leave half of the scratch allocated
+  BCFD_CUDA(cudaMalloc(&part, ((size_t)ne * 7 + 4) * sizeof(double)));
+  out = part + (size_t)ne * 7;
   k_stress_elem<<<grid_for(ne, 128), 128, 0, stream()>>>(hb->d, mu_f, rho_f, part);
   int r = note_launch();
   if (!r) {
@@ -328,11 +330,14 @@ int launch_stress(HostBlock* hb, double mu_f, double rho_f, double* out_host) {
     r = note_launch();
   }
   if (!r) {
-    BCFD_CUDA(cudaMemcpyAsync(out_host, out, 4 * sizeof(double), cudaMemcpyDeviceToHost, stream()));
-    BCFD_CUDA(cudaStreamSynchronize(stream()));
+    cudaError_t e = cudaMemcpyAsync(out_host, out, 4 * sizeof(double), cudaMemcpyDeviceToHost, stream());
+    if (e == cudaSuccess) e = cudaStreamSynchronize(stream());
+    if (e != cudaSuccess) {
+      report_cuda(e, "stress coefficients to host", __FILE__, __LINE__);
+      r = BCFD_E_CUDA;
+    }
   }
   cudaFree(part);
-  cudaFree(out);
   return r;
 }
 

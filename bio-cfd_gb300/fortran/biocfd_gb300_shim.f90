@@ -6,14 +6,28 @@
 ! src/CoefficientMatrix.f90, and instead of the hot-path routines of
 ! src/Search.F90 / src/FineInterp_bound.f90 / src/CoarseInterp.f90; add the
 ! component `integer(int64) :: bcfd = 0` to Block_t (src/Blocks.f90) so that
-! each block carries its device handle.  app/main.F90 relinks unchanged.
+! each block carries its device handle.  app/main.F90 relinks unchanged: every
+! name it imports from biocfd_search, biocfd_pcor_vcor,
+! biocfd_boundary_conditions, biocfd_coefficient_matrix,
+! biocfd_navier_stokes and biocfd_forcing is public here.
 !
-! Data ownership: the device arrays are authoritative.  Each routine here
-! registers a block on first sight (uploading grids, surface, fields and
-! tags), calls the C entry point and, when bcfd_host_mirror is .true. (the
-! default), copies the fields back so that host-side code (output, restart,
-! kinematics) sees current values.  Setting bcfd_host_mirror = .false. keeps
-! the data on the GPU between calls; call bcfd_pull(blk) before host reads.
+! Registration: the first call of any routine here registers every block of
+! `block` in block-number order (the library's block 1 is the coarse block)
+! with its grids, scalars, search box, surface, tags, kinematics and fields,
+! then every interface of `intfr` (the boxes read by readBlockInterface).  A
+! surface is registered with the placed nodes xnode1 when they exist, else
+! with the body-frame nodes xnode (findDistnode runs before
+! shiftSurfaceNodesInitial allocates xnode1).
+!
+! Data ownership: the device arrays are authoritative.  When bcfd_host_mirror
+! is .true. (the default) each routine uploads the block's fields before its
+! C call and downloads them after it, so host-side code (initial and restart
+! conditions, output, kinematics) and the device stay in step.  Setting
+! bcfd_host_mirror = .false. keeps the data on the GPU between calls; call
+! bcfd_push(blk) after host writes and bcfd_pull(blk) before host reads.
+! Kinematic scalars and the body's nodes belong to the library once
+! registered (computeSurfaceVariables runs there); the routines that change
+! them copy them back to the Block_t members.
 module biocfd_gb300_c
   use, intrinsic :: iso_c_binding
   implicit none
@@ -113,6 +127,31 @@ module biocfd_gb300_c
       import :: c_int, c_int64_t
       integer(c_int64_t), value :: h
     end function
+    integer(c_int) function bcfd_block_download_tags(h, cell, cell2, nid, celln, cellpr) &
+         bind(C, name="bcfd_block_download_tags")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+      integer(c_int64_t), intent(out) :: cell(*), cell2(*), nid(*), celln(*), cellpr(*)
+    end function
+    integer(c_int) function bcfd_block_read(h, name, out, n, written) bind(C, name="bcfd_block_read")
+      import :: c_int, c_int64_t, c_char, c_ptr
+      integer(c_int64_t), value :: h, n
+      character(kind=c_char), intent(in) :: name(*)
+      type(c_ptr), value :: out
+      integer(c_int64_t), intent(out) :: written
+    end function
+    integer(c_int) function bcfd_block_set_body_motion(h, p) bind(C, name="bcfd_block_set_body_motion")
+      import :: c_int, c_int64_t, c_double
+      integer(c_int64_t), value :: h
+      real(c_double), intent(in) :: p(6)
+    end function
+    integer(c_int) function bcfd_interface_create(a, b, a_msh, b_msh, box, h) &
+         bind(C, name="bcfd_interface_create")
+      import :: c_int, c_int64_t, c_double
+      integer(c_int64_t), value :: a, b, a_msh, b_msh
+      real(c_double), intent(in) :: box(6)
+      integer(c_int64_t), intent(out) :: h
+    end function
     integer(c_int) function bcfd_poisson_solver(itmax, epsi, ita, dt, totime, uc, total, s, f, st) &
          bind(C, name="bcfd_poisson_solver")
       import :: c_int, c_int64_t, c_double
@@ -137,6 +176,7 @@ module biocfd_gb300_glue
   use, intrinsic :: iso_fortran_env, only: int64, dp => real64
   use biocfd_gb300_c
   use biocfd_block_type, only: Block_t
+  use global, only: block, intfr
   implicit none
   logical :: bcfd_host_mirror = .true.
   logical, private :: ready = .false.
@@ -150,14 +190,36 @@ contains
     end if
   end subroutine
 
-  ! register a block on first sight: grids, scalars, surface, tags, fields
+  ! first call: the library, every block in block-number order, every interface
   subroutine bcfd_ensure(blk)
     type(Block_t), intent(inout) :: blk
-    integer(c_int64_t) :: h
+    integer :: g
+    integer(c_int64_t) :: hi
+    real(c_double) :: box(6)
     if (.not. ready) then
       call bcfd_check(bcfd_init(0_c_int), 'bcfd_init')
       ready = .true.
+      do g = 1, size(block)
+        call bcfd_register(block(g))
+      end do
+      if (allocated(intfr)) then
+        do g = 1, size(intfr)
+          box = [intfr(g)%xintf_start, intfr(g)%xintf_end, intfr(g)%yintf_start, &
+                 intfr(g)%yintf_end, intfr(g)%zintf_start, intfr(g)%zintf_end]
+          call bcfd_check(bcfd_interface_create(block(intfr(g)%a_blk)%bcfd, &
+               block(intfr(g)%b_blk)%bcfd, intfr(g)%a_msh, intfr(g)%b_msh, box, hi), &
+               'interface_create')
+        end do
+      end if
     end if
+    if (blk%bcfd == 0) call bcfd_register(blk)
+  end subroutine
+
+  ! one block: grids, scalars, search box, surface, tags, kinematics, fields
+  subroutine bcfd_register(blk)
+    type(Block_t), intent(inout) :: blk
+    integer(c_int64_t) :: h
+    real(dp) :: kin(11)
     if (blk%bcfd /= 0) return
     call bcfd_check(bcfd_block_create(blk%nx, blk%ny, blk%nz, blk%x1, blk%y1, blk%z1, &
          blk%deltax, blk%deltay, blk%deltaz, h), 'block_create')
@@ -166,27 +228,33 @@ contains
     call bcfd_check(bcfd_block_set_search_box(h, blk%i_startSearch, blk%i_endSearch, &
          blk%j_startSearch, blk%j_endSearch, blk%k_startSearch, blk%k_endSearch), 'set_search_box')
     if (allocated(blk%ibElP1)) then
-      call bcfd_check(bcfd_block_set_surface(h, blk%ibElems, blk%ibNodes, blk%ibElP1, blk%ibElP2, &
-           blk%ibElP3, blk%ibSurfId, blk%xnode1, blk%ynode1, blk%znode1), 'set_surface')
+      if (allocated(blk%xnode1)) then
+        call bcfd_check(bcfd_block_set_surface(h, blk%ibElems, blk%ibNodes, blk%ibElP1, blk%ibElP2, &
+             blk%ibElP3, blk%ibSurfId, blk%xnode1, blk%ynode1, blk%znode1), 'set_surface')
+      else
+        call bcfd_check(bcfd_block_set_surface(h, blk%ibElems, blk%ibNodes, blk%ibElP1, blk%ibElP2, &
+             blk%ibElP3, blk%ibSurfId, blk%xnode, blk%ynode, blk%znode), 'set_surface')
+      end if
     end if
     if (allocated(blk%cell2)) then
       call bcfd_check(bcfd_block_upload_tags(h, blk%cell, blk%cell2, blk%nodeIdTag, blk%cell_n, &
            blk%cell_pr), 'upload_tags')
     end if
+    kin = [blk%xdot, blk%ydot, blk%yddot, blk%thetaDot1, blk%thetaDDot1, blk%thetaDot2, &
+           blk%thetaDDot2, blk%alphaDot, blk%piv_x, blk%piv_y, blk%piv_z]
+    call bcfd_check(bcfd_block_set_kinematics(h, kin), 'set_kinematics')
+    call bcfd_check(bcfd_block_set_flags(h, blk%move_check, int(blk%blk_mv_tag, int64)), 'set_flags')
     call bcfd_push(blk)
   end subroutine
 
+  ! host fields -> device
   subroutine bcfd_push(blk)
     type(Block_t), intent(inout) :: blk
-    real(dp) :: kin(11)
-    kin = [blk%xdot, blk%ydot, blk%yddot, blk%thetaDot1, blk%thetaDDot1, blk%thetaDot2, &
-           blk%thetaDDot2, blk%alphaDot, blk%piv_x, blk%piv_y, blk%piv_z]
-    call bcfd_check(bcfd_block_set_kinematics(blk%bcfd, kin), 'set_kinematics')
-    call bcfd_check(bcfd_block_set_flags(blk%bcfd, blk%move_check, int(blk%blk_mv_tag, int64)), 'set_flags')
     call bcfd_check(bcfd_block_upload_fields(blk%bcfd, blk%u, blk%v, blk%w, blk%p, blk%ut, blk%vt, &
          blk%wt), 'upload_fields')
   end subroutine
 
+  ! device fields, counts and Poisson statistics -> host
   subroutine bcfd_pull(blk)
     type(Block_t), intent(inout) :: blk
     integer(c_int64_t) :: c(6)
@@ -204,8 +272,42 @@ contains
     procedure(h_routine) :: fn
     character(*), intent(in) :: what
     call bcfd_ensure(blk)
+    if (bcfd_host_mirror) call bcfd_push(blk)
     call bcfd_check(fn(blk%bcfd), what)
     if (bcfd_host_mirror) call bcfd_pull(blk)
+  end subroutine
+
+  ! one real array of the block, read back by name (bcfd_block_read)
+  subroutine bcfd_read_real(h, name, arr)
+    integer(c_int64_t), intent(in) :: h
+    character(*), intent(in) :: name
+    real(dp), intent(inout), target, contiguous :: arr(:)
+    integer(c_int64_t) :: w
+    call bcfd_check(bcfd_block_read(h, name//char(0), c_loc(arr), size(arr, kind=c_int64_t), w), name)
+  end subroutine
+
+  ! kinematic scalars and placed nodes of a moving body -> Block_t members
+  subroutine bcfd_pull_motion(blk)
+    type(Block_t), intent(inout) :: blk
+    real(dp) :: k(1)
+    integer(c_int64_t) :: h
+    h = blk%bcfd
+    if (.not. allocated(blk%xnode1)) then
+      allocate(blk%xnode1(blk%ibNodes), blk%ynode1(blk%ibNodes), blk%znode1(blk%ibNodes))
+    end if
+    call bcfd_read_real(h, 'xnode1', blk%xnode1)
+    call bcfd_read_real(h, 'ynode1', blk%ynode1)
+    call bcfd_read_real(h, 'znode1', blk%znode1)
+    call bcfd_read_real(h, 'xdot', k); blk%xdot = k(1)
+    call bcfd_read_real(h, 'ydot', k); blk%ydot = k(1)
+    call bcfd_read_real(h, 'yddot', k); blk%yddot = k(1)
+    call bcfd_read_real(h, 'thetaDot1', k); blk%thetaDot1 = k(1)
+    call bcfd_read_real(h, 'thetaDDot1', k); blk%thetaDDot1 = k(1)
+    call bcfd_read_real(h, 'thetaDot2', k); blk%thetaDot2 = k(1)
+    call bcfd_read_real(h, 'thetaDDot2', k); blk%thetaDDot2 = k(1)
+    call bcfd_read_real(h, 'piv_x', k); blk%piv_x = k(1)
+    call bcfd_read_real(h, 'piv_y', k); blk%piv_y = k(1)
+    call bcfd_read_real(h, 'piv_z', k); blk%piv_z = k(1)
   end subroutine
 end module biocfd_gb300_glue
 
@@ -255,6 +357,7 @@ contains
     type(Block_t), intent(inout) :: blk
     real(dp), intent(in) :: deltat, uc
     call bcfd_ensure(blk)
+    if (bcfd_host_mirror) call bcfd_push(blk)
     call bcfd_check(bcfd_velocity_bc(blk%bcfd, deltat, uc), 'velocityBC')
     if (bcfd_host_mirror) call bcfd_pull(blk)
   end subroutine
@@ -383,10 +486,13 @@ module biocfd_search
   use biocfd_gb300_glue
   implicit none
   private
-  public :: computeSurfaceVariables, computeSurfaceNorm, block_move_check, change_block_coords, &
-            change_block_coords_interfaces, change_block_interface, fine_block_cell, &
-            cellCount_solid_coarse_mv, tagging_th_move, selectiveRetagging_th, cellCount_solid, &
-            computeNormDistance, findTScells
+  public :: findDistnode, shiftSurfaceNodesInitial, computeSurfaceVariables, computeSurfaceNorm, &
+            tagging_th, block_move_check, change_block_coords, change_block_coords_interfaces, &
+            change_block_interface, fine_block_cell, cellCount_solid_coarse, cellCount_solid_coarse_mv, &
+            tagging_th_move, selectiveRetagging_th, cellCount_solid, computeNormDistance, findTScells
+  ! the coarse cells under the fine blocks are marked (set-up call of
+  ! fine_block_cell, or a fine-block move inside block_move_check)
+  logical :: marks_current = .false.
   interface
     integer(c_int) function c_csv(h, phase, piv, ita, dt, dxmin, freq, totime) &
          bind(C, name="bcfd_compute_surface_variables")
@@ -422,6 +528,23 @@ module biocfd_search
       import :: c_int, c_int64_t
       integer(c_int64_t), value :: h
     end function
+    integer(c_int) function c_ssni(h, aoa, piv, ita, dt, dxmin, totime) &
+         bind(C, name="bcfd_shift_surface_nodes_initial")
+      import :: c_int, c_int64_t, c_double
+      integer(c_int64_t), value :: h, ita
+      real(c_double), value :: aoa, piv, dt, dxmin, totime
+    end function
+    integer(c_int) function c_tag(h) bind(C, name="bcfd_tagging_th")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_count_coarse(h) bind(C, name="bcfd_cellcount_solid_coarse")
+      import :: c_int, c_int64_t
+      integer(c_int64_t), value :: h
+    end function
+    integer(c_int) function c_fbc() bind(C, name="bcfd_fine_block_cell")
+      import :: c_int
+    end function
     integer(c_int) function c_read(h, name, out, n, written) bind(C, name="bcfd_block_read")
       import :: c_int, c_int64_t, c_char, c_ptr
       integer(c_int64_t), value :: h, n
@@ -431,6 +554,68 @@ module biocfd_search
     end function
   end interface
 contains
+  subroutine findDistnode(blk)                      ! src/Search.F90:21-47
+    ! The library finds the extreme surface-51 nodes mk, mkx1, mkx2 of the
+    ! body frame when the block's body motion is set; the block's nodes are
+    ! the body frame here (xnode), and the motion members (a0 in degrees, as
+    ! read) are handed over with them.
+    type(Block_t), intent(inout), target :: blk
+    real(dp) :: p(6)
+    integer(int64), target :: f(1)
+    integer(c_int64_t) :: w
+    call bcfd_ensure(blk)
+    call bcfd_check(bcfd_block_set_nodes(blk%bcfd, blk%xnode, blk%ynode, blk%znode), 'set_nodes')
+    p = [blk%a0, blk%bfreq, blk%yamp, blk%xshift, blk%yshift, blk%zshift]
+    call bcfd_check(bcfd_block_set_body_motion(blk%bcfd, p), 'set_body_motion')
+    call bcfd_check(c_read(blk%bcfd, 'mk'//char(0), c_loc(f), 1_c_int64_t, w), 'mk')
+    blk%mk = f(1)
+    call bcfd_check(c_read(blk%bcfd, 'mkx1'//char(0), c_loc(f), 1_c_int64_t, w), 'mkx1')
+    blk%mkx1 = f(1)
+    call bcfd_check(c_read(blk%bcfd, 'mkx2'//char(0), c_loc(f), 1_c_int64_t, w), 'mkx2')
+    blk%mkx2 = f(1)
+  end subroutine
+  subroutine shiftSurfaceNodesInitial(blk, aoa, piv_pt, ita, deltat, dxmin, totime)  ! src/Search.F90:49-124
+    type(Block_t), intent(inout) :: blk
+    real(dp), intent(in) :: aoa, piv_pt, deltat, dxmin, totime
+    integer(int64), intent(in) :: ita
+    real(dp), parameter :: pi_ = 4.0_dp * atan(1.0_dp)
+    call bcfd_ensure(blk)
+    call bcfd_check(c_ssni(blk%bcfd, aoa, piv_pt, ita, deltat, dxmin, totime), 'shiftSurfaceNodesInitial')
+    ! the Block_t members the routine changes: the placed nodes (allocated
+    ! here, as the reference does), the kinematics and a0 in radians
+    call bcfd_pull_motion(blk)
+    blk%a0 = blk%a0 * pi_ / 180.0_dp
+  end subroutine
+  subroutine tagging_th(blk, blk_no)                ! src/Search.F90:388-413
+    ! tagging_th_core on the device, then the reference's two record files
+    ! butter_f.NNN.dat (cell, nodeIdTag per point) and butter_cellcount_f.NNN.dat
+    type(Block_t), intent(inout) :: blk
+    integer(int64), intent(in) :: blk_no
+    character(len=120) :: filename1
+    integer(int64) :: i, j, k
+    integer :: u
+    call bcfd_call(blk, c_tag, 'tagging_th')
+    call bcfd_check(bcfd_block_download_tags(blk%bcfd, blk%cell, blk%cell2, blk%nodeIdTag, blk%cell_n, &
+         blk%cell_pr), 'download_tags')
+    write(filename1, '("butter_f.",i3.3,".dat")') blk_no
+    open(newunit=u, file=filename1, status="unknown")
+    do k = 1, blk%nz + 2
+      do j = 1, blk%ny + 2
+        do i = 1, blk%nx + 2
+          write(u, *) blk%cell(i, j, k), blk%nodeIdTag(i, j, k)
+        end do
+      end do
+    end do
+    close(u)
+    write(filename1, '("butter_cellcount_f.",i3.3,".dat")') blk_no
+    open(newunit=u, file=filename1, form="formatted")
+    write(u, *) blk%solidCellCount, blk%fluidCellCount, blk%ibCellCount
+    close(u)
+  end subroutine
+  subroutine cellCount_solid_coarse(blk)            ! src/Search.F90:1463-1532
+    type(Block_t), intent(inout) :: blk
+    call bcfd_call(blk, c_count_coarse, 'cellCount_solid_coarse')
+  end subroutine
   subroutine computeSurfaceVariables(blk, g, phase_angle, piv_pt, ita, deltat, dxmin, freq, re, totime)
     ! src/Search.F90:126-208 (re is not used by the routine)
     type(Block_t), intent(inout) :: blk
@@ -440,6 +625,7 @@ contains
     call bcfd_check(bcfd_block_set_flags(blk%bcfd, -1_c_int64_t, int(blk%blk_mv_tag, c_int64_t)), 'set_flags')
     call bcfd_check(c_csv(blk%bcfd, phase_angle, piv_pt, ita, deltat, dxmin, freq, totime), &
          'computeSurfaceVariables')
+    if (bcfd_host_mirror) call bcfd_pull_motion(blk)
   end subroutine
   subroutine computeSurfaceNorm(blk, inor)          ! src/Search.F90:210-258
     type(Block_t), intent(inout) :: blk
@@ -454,6 +640,7 @@ contains
     integer :: g
     call bcfd_check(c_move(moved), 'block_move_check')
     coarse_flcnt_check = moved
+    if (moved /= 0) marks_current = .true.  ! re-marked with the move
     ! the switches a moved block carries into the re-tagging (Block_t copies)
     do g = 2, size(block)
       if (block(g)%bcfd == 0) cycle
@@ -480,7 +667,13 @@ contains
     class(*), intent(inout) :: intf
     type(Block_t), intent(inout) :: a, b
   end subroutine
-  subroutine fine_block_cell                       ! :863-914 (done in block_move_check)
+  subroutine fine_block_cell                       ! src/Search.F90:863-914
+    ! the set-up call marks the coarse cells under the fine blocks; later calls
+    ! find them current (a fine-block move re-marks inside block_move_check),
+    ! and marking them again would change nothing
+    if (marks_current) return
+    call bcfd_check(c_fbc(), 'fine_block_cell')
+    marks_current = .true.
   end subroutine
   subroutine cellCount_solid_coarse_mv(coarse_flcnt_check)  ! :916-995 (done in block_move_check)
     integer(int64), intent(inout) :: coarse_flcnt_check
@@ -515,3 +708,24 @@ contains
     call bcfd_call(blk, c_ts, 'findTScells')
   end subroutine
 end module biocfd_search
+
+! coefficientMatrix of src/CoefficientMatrix.f90:10-71: the 3-point Poisson
+! line tables Acx/Acy/Acz (coarse-block boundary folding when is_coarse)
+module biocfd_coefficient_matrix
+  use biocfd_block_type, only: Block_t
+  use biocfd_gb300_c
+  use biocfd_gb300_glue
+  implicit none
+  private
+  public :: coefficientMatrix
+contains
+  subroutine coefficientMatrix(blk, is_coarse)      ! src/CoefficientMatrix.f90:10-71
+    type(Block_t), intent(inout) :: blk
+    logical, intent(in) :: is_coarse
+    integer(c_int) :: c
+    c = 0
+    if (is_coarse) c = 1
+    call bcfd_ensure(blk)
+    call bcfd_check(bcfd_coefficient_matrix(blk%bcfd, c), 'coefficientMatrix')
+  end subroutine
+end module biocfd_coefficient_matrix

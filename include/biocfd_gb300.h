@@ -57,6 +57,24 @@ int64_t bcfd_kernel_launches(void);
  * are solved together) run over all blocks in one launch per phase, driven by
  * a device table of block views; 0: one launch per block.  Same results. */
 int bcfd_set_batching(int on);
+/* Longest time (ns) any single device-side wait of a persistent kernel (the
+ * grid barriers and the neighbour-tile waits of the Poisson solves, the
+ * forcing's level barriers) may spin before the kernel gives up: it records
+ * BCFD_E_TIMEOUT, every CTA leaves its loops and the call that launched it
+ * returns BCFD_E_TIMEOUT; the context stays usable.  0 restores the default
+ * (2 s); at most 600 s.  No counterpart in the reference (its OpenACC loops
+ * do not wait on each other). */
+int bcfd_set_wait_limit_ns(int64_t ns);
+/* Self-check of the bounded waits (no counterpart in the reference): launches
+ * one grid barrier that nothing can complete and returns in *status what the
+ * device recorded (BCFD_E_TIMEOUT once the wait limit passed) and in
+ * *waited_ms (may be NULL) the kernel's duration.  The context stays usable. */
+int bcfd_check_wait_limit(int* status, double* waited_ms);
+/* Caps the entries of a block's IB / thin-surface lists (no counterpart in
+ * the reference, whose lists are allocated to fit): 0 restores the allocated
+ * capacity, min(interior cells, 4M); a lower cap makes a list that outgrows
+ * it report BCFD_E_CAPACITY (entries beyond it are dropped, never written). */
+int bcfd_block_set_list_capacity(bcfd_handle h, int64_t cap);
 
 /* ---- block registration and host mirrors (src/Blocks.f90:13-81) --------- */
 /* Allocates the per-block device arrays of src/AllocateArrays.f90:15-57 and
@@ -139,6 +157,19 @@ int bcfd_compute_surface_norm(bcfd_handle h, int64_t inor); /* src/Search.F90:21
  * set with the surface become the body frame (xnode of Block_t); node surface
  * ids follow src/ReadInput.f90:403-420. */
 int bcfd_block_set_body_motion(bcfd_handle h, const double* p);
+/* A phase lag of this body's heave and pitch behind the kinematics that every
+ * body shares (no counterpart in the reference, whose kinematics take one
+ * phase angle for all bodies: src/Search.F90:142, app/main.F90:62,173).  With
+ * lag L (radians) the body pitches a0 sin(2 pi freq (t + dt) + phase - L) and
+ * heaves yamp sin(2 pi bfreq t - L); its initial placement
+ * (bcfd_shift_surface_nodes_initial) starts it where the lagged kinematics
+ * put it at t = 0: angle aoa + a0 (sin(phase_angle - L) - sin(phase_angle))
+ * and heave position yamp sin(-L), where phase_angle is the pitch phase the
+ * bodies share (radians).  L = 0 (the default, and what
+ * bcfd_block_set_body_motion resets to) is the reference's arithmetic bit for
+ * bit.  Call after bcfd_block_set_body_motion, before the initial placement;
+ * BCFD_E_STATE without body motion. */
+int bcfd_block_set_body_lag(bcfd_handle h, double lag, double phase_angle);
 int bcfd_shift_surface_nodes_initial(bcfd_handle h, double aoa, double piv_pt, int64_t ita,
                                      double deltat, double dxmin, double totime); /* src/Search.F90:49-124 */
 int bcfd_compute_surface_variables(bcfd_handle h, double phase_angle, double piv_pt, int64_t ita,
@@ -313,11 +344,10 @@ int bcfd_block_get_divergence(bcfd_handle h, double* out);
 /* mixed-precision solve parameters of a block: FP32 sweeps per correction,
  * their relaxation factor (0 selects the defaults) and the kernel variant
  * (0: the library's choice, 1: tiled cooperative with grid-wide phase
- * barriers, 2: cluster-resident when the block fits in one 16-CTA cluster,
- * else 1, 3: tiled cooperative with point-to-point neighbour sync, 4:
+ * barriers, 3: tiled cooperative with point-to-point neighbour sync, 4:
  * temporal-blocked sweeps, one grid barrier per sweep pair, when the block's
  * halo'd tiles fit in shared memory, else 1; 1, 3 and 4 give bitwise the
- * same corrections) */
+ * same corrections; 2 is not accepted) */
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant);
 /* launch shape of a block's tiled Poisson solves (the autotuner's knobs; no
  * effect on results): threads per CTA (0 = the default: 512 for the FP64

@@ -152,6 +152,9 @@ class Oracle:
                     for nm, v in (("a0", mo.a0_deg), ("bfreq", mo.bfreq), ("yamp", mo.yamp),
                                   ("xshift", mo.shift[0]), ("yshift", mo.shift[1]), ("zshift", mo.shift[2])):
                         self.setf(g, nm, v)
+                    if mo.lag_deg != 0.0:
+                        self.setf(g, "lag", mo.lag_deg * np.pi / 180.0)
+                        self.setf(g, "lag_phase", mi.phase_deg * np.pi / 180.0)
                     L.orc_shift_surface_nodes_initial(g, mi.aoa_deg, mi.piv_pt, 0, case.dt, mi.dxmin, 0.0)
                 for nm, v in zip(("i_startSearch", "i_endSearch", "j_startSearch", "j_endSearch",
                                   "k_startSearch", "k_endSearch"), spec.search_box):

@@ -58,7 +58,7 @@ double* fs_of(Block& b, const std::string& n) {
   M(dx) M(dy) M(dz) M(omega) M(derr1) M(derr2) M(derrStdSt) M(xdot) M(ydot) M(yddot)
   M(thetaDot) M(thetaDDot) M(thetaDot1) M(thetaDDot1) M(thetaDot2) M(thetaDDot2) M(alphaDot)
   M(piv_x) M(piv_y) M(piv_z) M(viscous_drag) M(pressure_drag) M(viscous_lift) M(pressure_lift)
-  M(a0) M(bfreq) M(yamp) M(xshift) M(yshift) M(zshift) M(xpth1) M(xpth2) M(ypth2) M(xchg) M(ychg)
+  M(lag) M(lag_phase) M(a0) M(bfreq) M(yamp) M(xshift) M(yshift) M(zshift) M(xpth1) M(xpth2) M(ypth2) M(xchg) M(ychg)
   M(xmove) M(ymove) M(zmove) M(xt) M(yt) M(inity_cent) M(nxty_cent) M(initx_cent) M(nxtx_cent)
 #undef M
   return nullptr;

@@ -152,6 +152,9 @@ struct Block {
   F1 xnode, ynode, znode;
   I1 ibNodeId;
   double a0 = 0, bfreq = 0, yamp = 0, xshift = 0, yshift = 0, zshift = 0;
+  // per-body phase lag of heave and pitch and the shared pitch phase (an
+  // extension of the reference's kinematics; 0 = the reference)
+  double lag = 0, lag_phase = 0;
   double xpth1 = 0, xpth2 = 0, ypth2 = 0, xchg = 0, ychg = 0, xmove = 0, ymove = 0, zmove = 0;
   double xt = 0, yt = 0, inity_cent = 0, nxty_cent = 0, initx_cent = 0, nxtx_cent = 0,
          initz_cent = 0, nxtz_cent = 0;

@@ -1,5 +1,6 @@
 // ORACLE -- TEST INFRASTRUCTURE ONLY (see orc_core.h).
 // Immersed-boundary forcing routines of src/Forcing.f90, restated serially.
+#include <algorithm>
 #include <cmath>
 #include "orc_core.h"
 
@@ -30,13 +31,23 @@ double compute_derivative(double x, double x2, double x1, double p_x, double p_x
 }
 
 // compute_value_and_derivatives, src/Forcing.f90:1091-1161
+// The reference reads outside `var` when a stencil corner falls off the array
+// (a probe with no bracket, or the staggered offset at index 1); the oracle
+// records ORC_E_NOTFOUND in *err and clamps the corner into the array, as the
+// GPU library does.
 void value_and_derivatives(double x, double y, double z, int64_t i, int64_t j, int64_t k,
                            const F1& xg, const F1& yg, const F1& zg, int offset_axis,
-                           const F3& var, double& val, double der[3]) {
+                           const F3& var, double& val, double der[3], int* err) {
   int64_t ii = i, jj = j, kk = k;
   if (offset_axis == 1) ii = i - 1;
   if (offset_axis == 2) jj = j - 1;
   if (offset_axis == 3) kk = k - 1;
+  if (ii < 1 || ii + 1 > var.n1 || jj < 1 || jj + 1 > var.n2 || kk < 1 || kk + 1 > var.n3) {
+    if (*err == 0) *err = ORC_E_NOTFOUND;
+    ii = std::max<int64_t>(1, std::min<int64_t>(ii, var.n1 - 1));
+    jj = std::max<int64_t>(1, std::min<int64_t>(jj, var.n2 - 1));
+    kk = std::max<int64_t>(1, std::min<int64_t>(kk, var.n3 - 1));
+  }
   double f[4];
   f[0] = var(ii, jj, kk); f[1] = var(ii, jj + 1, kk); f[2] = var(ii, jj, kk + 1); f[3] = var(ii, jj + 1, kk + 1);
   const double t11 = bilinear_interpolation(y, z, yg(j), yg(j + 1), zg(k), zg(k + 1), f);
@@ -128,7 +139,7 @@ void p_recon(Block& b, int64_t n, bool field) {
     iz = find_index(b, pz, b.zp, k - 7, k + 7);
   }
   double val, der[3];
-  value_and_derivatives(px, py, pz, ix, iy, iz, b.xp, b.yp, b.zp, 0, b.p, val, der);
+  value_and_derivatives(px, py, pz, ix, iy, iz, b.xp, b.yp, b.zp, 0, b.p, val, der, &b.err);
   const double dpdn_e = dotn(b, e, der);
   const double n1 = pt1 + s2n;
   const double bval = dpdn;
@@ -222,7 +233,7 @@ void v_recon(Block& b, int64_t n, int c, int mode) {
   F3& src = g.axis == 1 ? b.ut : (g.axis == 2 ? b.vt : b.wt);
   F3& dst = mode == 0 ? src : (g.axis == 1 ? b.u : (g.axis == 2 ? b.v : b.w));
   double val, der[3];
-  value_and_derivatives(px, py, pz, ix, iy, iz, *g.xg, *g.yg, *g.zg, g.axis, src, val, der);
+  value_and_derivatives(px, py, pz, ix, iy, iz, *g.xg, *g.yg, *g.zg, g.axis, src, val, der, &b.err);
   const double dn = dotn(b, e, der);
   const double n1 = pt1 + s2n;
   const double r = vel_quad(val, surf, dn, n1, s2n);
@@ -276,7 +287,7 @@ void pressure_forcing_ghost(Block& b) {
     const int64_t iy = find_index(b, py, b.yp, j - 7, j + 7);
     const int64_t iz = find_index(b, pz, b.zp, k - 7, k + 7);
     double val, der[3];
-    value_and_derivatives(px, py, pz, ix, iy, iz, b.xp, b.yp, b.zp, 0, b.p, val, der);
+    value_and_derivatives(px, py, pz, ix, iy, iz, b.xp, b.yp, b.zp, 0, b.p, val, der, &b.err);
     const double dpdn_e = -1.0 * dotn(b, e, der);
     const double n1 = pt1 + s2n;
     const double bval = dpdn;
@@ -312,7 +323,7 @@ void velocity_forcing_ghost(Block& b) {
       F3& src = g.axis == 1 ? b.ut : (g.axis == 2 ? b.vt : b.wt);
       F3& cur = g.axis == 1 ? b.u : (g.axis == 2 ? b.v : b.w);
       double val, der[3];
-      value_and_derivatives(px, py, pz, ix, iy, iz, *g.xg, *g.yg, *g.zg, g.axis, src, val, der);
+      value_and_derivatives(px, py, pz, ix, iy, iz, *g.xg, *g.yg, *g.zg, g.axis, src, val, der, &b.err);
       const double dn = -1.0 * dotn(b, e, der);
       const double n1 = pt1 + s2n;
       (*ghost[c])(n) = vel_quad(val, surf, dn, n1, s2n);

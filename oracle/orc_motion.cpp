@@ -74,7 +74,15 @@ void node_ids_from_elements(Block& b) {
 
 void shift_surface_nodes_initial(Block& b, double aoa, double piv_pt, int64_t ita, double deltat,
                                  double dxmin, double totime) {
-  const double aoa1 = aoa * kPi / 180.0, aoa2 = -aoa1;
+  // extension: a lagging body starts at its lagged state at t = 0 (angle and
+  // heave position); without a lag this is the reference's placement
+  double aoa_b = aoa, y0 = 0.0;
+  if (b.lag != 0.0) {
+    aoa_b = aoa + b.a0 * (std::sin(b.lag_phase - b.lag) - std::sin(b.lag_phase));
+    y0 = b.yamp * std::sin(-b.lag);
+  }
+  const double ysh = b.lag != 0.0 ? b.yshift + y0 : b.yshift;
+  const double aoa1 = aoa_b * kPi / 180.0, aoa2 = -aoa1;
   const double bdfr = 15, bdy = 15 * dxmin;
   b.xmove = 0.0;
   b.ymove = 0.0;
@@ -85,7 +93,7 @@ void shift_surface_nodes_initial(Block& b, double aoa, double piv_pt, int64_t it
   b.xpth2 = b.xshift - ((double)ita * dxmin * kXfact);
   b.ypth2 = (b.yamp) * std::sin(angt * b.xshift);
   b.piv_x = b.xshift;
-  b.piv_y = b.yshift;
+  b.piv_y = ysh;
   b.piv_z = b.zshift;
   b.thetaDot = b.thetaDDot = b.thetaDot1 = b.thetaDot2 = b.alphaDot = 0.0;
   b.thetaDDot1 = b.thetaDDot2 = 0.0;
@@ -94,8 +102,8 @@ void shift_surface_nodes_initial(Block& b, double aoa, double piv_pt, int64_t it
   b.yddot = -(angt * angt * bdy * std::sin(2 * kPi * bdfr * totime));
   b.xt = b.xshift - ((double)ita * dxmin * kXfact);
   b.xdot = -(dxmin * kXfact) / deltat;
-  b.inity_cent = b.yshift;
-  b.nxty_cent = b.yshift;
+  b.inity_cent = ysh;
+  b.nxty_cent = ysh;
   b.initx_cent = b.xshift;
   b.nxtx_cent = b.xshift;
   b.initz_cent = b.zshift;
@@ -104,14 +112,16 @@ void shift_surface_nodes_initial(Block& b, double aoa, double piv_pt, int64_t it
     double xr1, yr1, zr1;
     place(b, i, aoa1, aoa2, piv_pt, xr1, yr1, zr1);
     b.xnode1(i) = xr1 + b.xshift;
-    b.ynode1(i) = yr1 + b.yshift;
+    b.ynode1(i) = yr1 + ysh;
     b.znode1(i) = zr1 + b.zshift;
   }
 }
 
 void compute_surface_variables(Block& b, double phase_angle, double piv_pt, int64_t ita,
                                double deltat, double dxmin, double freq, double totime) {
-  const double aoa1 = (b.a0) * std::sin(2.0 * kPi * freq * (totime + deltat) + phase_angle);
+  double parg = 2.0 * kPi * freq * (totime + deltat) + phase_angle;
+  if (b.lag != 0.0) parg = parg - b.lag;  // extension: per-body lag
+  const double aoa1 = (b.a0) * std::sin(parg);
   const double aoa2 = -aoa1;
   const double ang_theta = 2.0 * kPi * freq;
   const double bdfr = b.bfreq, bdy = b.yamp;
@@ -120,16 +130,21 @@ void compute_surface_variables(Block& b, double phase_angle, double piv_pt, int6
   b.ypth2 = (b.yamp) * std::sin(angt * b.xpth2);
   b.xchg = b.xpth2 - b.xpth1;
   b.xpth1 = b.xpth2;
-  b.thetaDot1 = ang_theta * b.a0 * std::cos(2.0 * kPi * freq * (totime + deltat) + phase_angle);
-  b.thetaDDot1 = -(ang_theta * ang_theta * b.a0 * std::sin(2.0 * kPi * freq * (totime + deltat) + phase_angle));
+  b.thetaDot1 = ang_theta * b.a0 * std::cos(parg);
+  b.thetaDDot1 = -(ang_theta * ang_theta * b.a0 * std::sin(parg));
   b.thetaDot2 = -b.thetaDot1;
   b.thetaDDot2 = -b.thetaDDot1;
-  b.yt = bdy * std::sin(angt * (totime));
-  b.ydot = angt * bdy * std::cos(angt * (totime));
-  b.yddot = -(angt * angt * bdy * std::sin(angt * (totime)));
+  double h0 = angt * (totime), h1 = angt * (totime - deltat);
+  if (b.lag != 0.0) {
+    h0 = h0 - b.lag;
+    h1 = h1 - b.lag;
+  }
+  b.yt = bdy * std::sin(h0);
+  b.ydot = angt * bdy * std::cos(h0);
+  b.yddot = -(angt * angt * bdy * std::sin(h0));
   b.xt = b.xpth2;
   b.xdot = -(dxmin * kXfact) / deltat;
-  b.ychg = b.yt - bdy * std::sin(angt * (totime - deltat));
+  b.ychg = b.yt - bdy * std::sin(h1);
   b.ymove = b.yt;
   b.xmove = b.xchg;
   b.zmove = 0.0;

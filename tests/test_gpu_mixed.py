@@ -27,7 +27,7 @@ def _run(case, precision, steps, variant=0):
     return out, res
 
 
-@pytest.mark.parametrize("variant", [1, 2])
+@pytest.mark.parametrize("variant", [1, 3, 4])
 def test_mixed_reaches_tolerance_two_block(variant):
     case = synth.small_two_block(n_steps=2)
     f1, r1 = _run(case, 1, 2, variant)
@@ -38,16 +38,6 @@ def test_mixed_reaches_tolerance_two_block(variant):
         for nm in ("u", "v", "w", "p"):
             e = rel_l2(b2[nm], b1[nm])
             assert e < FIELD_TOL, (nm, e)
-
-
-def test_mixed_cluster_variant_on_64_block():
-    # a 64^3 block: the cluster-resident kernel path (16 z-slabs of 4 planes)
-    case = synth.sphere_single_block(n=64, n_steps=1)
-    fc, rc = _run(case, 1, 1, variant=2)
-    fg, rg = _run(case, 1, 1, variant=1)
-    assert max(rc) <= TOL * (1 + 1e-9) and max(rg) <= TOL * (1 + 1e-9)
-    for nm in ("u", "v", "w", "p"):
-        assert rel_l2(fg[0][nm], fc[0][nm]) < FIELD_TOL
 
 
 @pytest.mark.parametrize("variant", [1, 3, 4])

@@ -48,3 +48,24 @@ def test_moving_plate_setup_and_steps():
         compare_search(o, s, f"step {q + 1}")
     for nm in ("xdot", "ydot", "yddot", "thetaDot1", "thetaDDot1", "piv_x", "piv_y"):
         assert s.kinematic(s.handles[0], nm) == o.getf(1, nm), nm
+
+
+def test_lagging_plate_matches_oracle():
+    # a body lagging 90 deg behind the shared kinematics (the tandem plates'
+    # trailing plate): its initial placement at its own t = 0 state, then the
+    # lagged heave and pitch, bitwise against the oracle's restatement
+    case = synth.moving_plate_single_block(n=32, n_steps=3)
+    spec = case.blocks[0]
+    spec.motion = synth.dataclasses.replace(spec.motion, lag_deg=90.0)
+    o, s = _pair(case)
+    _nodes(o, s, "setup")
+    assert s.kinematic(s.handles[0], "piv_y") == o.getf(1, "piv_y") != spec.motion.shift[1]
+    for q in range(3):
+        o.step()
+        s.run(1)
+        _nodes(o, s, f"step {q + 1}")
+        compare_fields(o, s, f"step {q + 1}")
+        compare_iters(o, s, f"step {q + 1}")
+        compare_search(o, s, f"step {q + 1}")
+    for nm in ("xdot", "ydot", "yddot", "thetaDot1", "thetaDDot1", "piv_x", "piv_y"):
+        assert s.kinematic(s.handles[0], nm) == o.getf(1, nm), nm

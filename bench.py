@@ -1,24 +1,31 @@
 #!/usr/bin/env python
 """Bench: time steps/s of the Bio-CFD hot path on one GB300.
 
-Workload (one "step" = one time step of app/main.F90:129-265 over all blocks):
-the two-block refinement case -- coarse 96x64x64 over 3x2x2 plus a nested
-fine 64^3 block at ratio 2 around a stationary sphere D = 0.5, Re = 300,
-uniform inflow, seeded N(0, 1e-3) noise, dt from CFL 0.3, SOR to 1e-6.
+Headline workload (one "step" = one time step of app/main.F90:129-265 over
+all blocks): the largest single-GPU configuration, tandem flapping plates on
+44.0M cells -- a coarse 384x256x256 block over 6x4x4 plus two fine
+256x192x192 blocks at ratio 2, each holding a rigid ellipsoidal plate
+(0.5 x 0.125 x 0.0125) 1.5 chords apart, Re = 1000; the leading plate heaves
+0.125 sin(2 pi 0.25 t) and pitches 15 deg sin(2 pi 0.25 t + 90 deg), the
+trailing plate does the same 90 deg behind; Search every step; seeded
+N(0, 1e-3) noise on u = 1.
 
-Three GPU paths run on the same GPU, each from the same initial state:
-  * "fp64_dropin": FP64 red-black SOR with the reference's stop test
-    (max |pc - pco| < 1e-6 every 5th iteration), bit-identical to the
-    reference arithmetic;
-  * "fp64": plain FP64 red-black SOR (FP64 momentum) run until the FP64
-    Poisson residual in divergence units, dt * max|b/dt - A pc|, is <= 1e-6;
-  * "mixed" (the flagship, reported as `value`): FP32 momentum stencil and
-    FP32 red-black SOR inside an FP64 defect-correction loop, stopped at the
-    same FP64 residual 1e-6 (so both end at equal divergence residual).
+`value` is the flagship path: FP32 momentum stencil and FP32 red-black SOR
+inside an FP64 defect-correction loop, every solve stopped at the FP64
+Poisson residual dt * max|b/dt - A pc| <= 1e-6, each step one replay of the
+captured step CUDA graph.  Beside it, on the same GPU and workload:
+  * "fp64_fast": plain FP64 (FP64 momentum, FP64 SOR without divisions) to the
+    same residual -- the metric's FP64 denominator;
+  * "fp64": plain FP64 with the reference's sweep arithmetic to the same
+    residual; "fp64_input_omega": the same with the input omega 1.7;
+  * the per-phase split of one step, the roofline of the dominant kernel (the
+    mixed Poisson solve), and the mixed path's error against the FP64 run.
 `e2e` repeats the flagship through the C ABI with host buffers: every step
-uploads u,v,w,p of both blocks from pinned host memory and downloads them.
-The CPU baseline is the serial FP64 oracle (the reference itself is Fortran
-and no Fortran compiler exists on either machine).
+uploads u,v,w,p of all blocks from pinned host memory and downloads them.
+The CPU baseline / reference arm is the FP64 oracle on the host cores (the
+reference itself is Fortran and no Fortran compiler exists on either
+machine), timed on a bounded sample of the same workload (see
+`cpu_reference_sample`).
 """
 from __future__ import annotations
 
@@ -38,7 +45,18 @@ sys.path.insert(0, str(ROOT))
 
 DIV_TOL = 1e-6
 METRIC = "time steps/s at 1e-6 div residual: FP32+FP64-refine vs plain FP64, same GPU"
-WORKLOAD = "two-block sphere: coarse 96x64x64 over 3x2x2 + fine 64^3 at ratio 2, D=0.5, Re=300"
+WORKLOAD = ("tandem flapping plates, 44.0M cells: coarse 384x256x256 over 6x4x4 + two fine 256x192x192 at "
+            "ratio 2, plates 0.5x0.125x0.0125 1.5 chords apart heaving 0.125 sin(2 pi 0.25 t) and pitching "
+            "15 deg sin(2 pi 0.25 t + 90 deg), trailing plate 90 deg behind, Re 1000, Search every step")
+
+# Sweep pairs the reference algorithm (FP64 SOR, omega 1.7, stop when
+# max|pc - pco| < 1e-6 every 5th iteration, at most pcItaMax = 5000 per solve)
+# spends per block in the first step of the headline workload, summed over the
+# block's solve calls in the step (the coarse block is solved once, each fine
+# block twice).  Measured with the GPU drop-in path, whose iteration counts
+# equal the oracle's bit for bit; the CPU reference arm multiplies its
+# measured cost per sweep pair by these counts.
+REFERENCE_SWEEP_PAIRS = None  # filled from a measurement (see `dropin_sweep_pairs`)
 
 
 def peaks():
@@ -49,16 +67,16 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profiles():
-    """dram read+write bytes per launch of the dominant kernel, from the committed ncu summary."""
-    f = ROOT / "profiles" / "k_sor_dc_two_block.md"
+def profile_value(name: str, key: str):
+    """A `key: value` line of a committed ncu summary under profiles/."""
+    f = ROOT / "profiles" / name
     if not f.exists():
         return None
     for line in f.read_text().splitlines():
-        if line.strip().startswith("traffic_bytes_per_launch:"):
+        if line.strip().startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
+            except (ValueError, IndexError):
                 return None
     return None
 
@@ -78,7 +96,7 @@ class Clocks:
     def __enter__(self):
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "50"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -113,6 +131,17 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(self.rows)}
 
 
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+    def summary(self):
+        return None
+
+
 def dist_env():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), \
         int(os.environ.get("LOCAL_RANK", "0"))
@@ -142,16 +171,52 @@ def rank_barrier(torch):
         torch.cuda.synchronize()
 
 
-def oracle_steps(case, n_steps: int):
-    """Serial FP64 oracle (CPU): steps/s over n_steps steps after set-up."""
+# ---------------------------------------------------------------------------
+# CPU reference: the FP64 oracle (all host threads) on a bounded sample
+# ---------------------------------------------------------------------------
+
+def cpu_reference_sample(case, sweep_pairs=None, cap_pairs: int = 4):
+    """Time the oracle (the FP64 restatement of the reference; its OpenMP loops
+    use every host core) on a bounded sample of one time step of `case` and
+    return the estimated time of a whole reference step.
+
+    The sample is one full time step with every Poisson solve capped at
+    `cap_pairs` sweep pairs (pcItaMax), plus `cap_pairs` more sweep pairs of
+    each block timed alone; a whole step then costs the capped step plus, per
+    block, (the reference's sweep pairs - the capped ones) times the measured
+    cost of one pair.  `sweep_pairs` are the reference's sweep pairs per block
+    in that step (REFERENCE_SWEEP_PAIRS); without them the capped step alone
+    is reported (a lower bound)."""
+    from biocfd import synth
     from oracle.bridge import Oracle
     o = Oracle(checked=False)
-    o.setup(case)
     t0 = time.perf_counter()
-    for _ in range(n_steps):
-        o.step()
-    dt = time.perf_counter() - t0
-    return n_steps / dt, dt
+    o.setup(synth.replace(case, pc_ita_max=cap_pairs - 1))
+    t_setup = time.perf_counter() - t0
+    threads = int(o.L.orc_get_threads())
+    t0 = time.perf_counter()
+    o.step()
+    t_capped = time.perf_counter() - t0
+    nb = len(case.blocks)
+    capped_pairs = [o.geti(g, "nIterPcor") for g in range(1, nb + 1)]
+    # per-block cost of one sweep pair: the block's SOR alone for cap_pairs pairs
+    pair_s = []
+    for g in range(1, nb + 1):
+        o.seti(g, "nIterPcor", 0)
+        t0 = time.perf_counter()
+        o.L.orc_redblack_sor(g, cap_pairs - 1, case.dt, -1.0)
+        pair_s.append((time.perf_counter() - t0) / max(o.geti(g, "nIterPcor"), 1))
+    if sweep_pairs:
+        extra = sum(max(n - c, 0) * t for n, c, t in zip(sweep_pairs, capped_pairs, pair_s))
+        est = t_capped + extra
+        how = (f"one oracle step with every Poisson solve capped at {cap_pairs} sweep pairs ({t_capped:.1f} s) "
+               f"+ per block (the reference's sweep pairs {list(sweep_pairs)} - the capped ones {capped_pairs}) x "
+               f"the block's measured seconds per sweep pair {[round(x, 4) for x in pair_s]}")
+    else:
+        est = t_capped
+        how = f"one oracle step with every Poisson solve capped at {cap_pairs} sweep pairs (lower bound)"
+    return {"step_s": est, "steps_per_s": 1.0 / est, "threads": threads, "sample": how,
+            "setup_s": t_setup, "capped_step_s": t_capped, "pair_s": pair_s}
 
 
 def run_reference(args):
@@ -159,142 +224,220 @@ def run_reference(args):
     if rank != 0:
         return
     from biocfd import synth
-    case = synth.sphere_two_block(n_steps=args.steps)
-    # bounded sample: warm-up and timed steps of the serial oracle, capped so
-    # the whole run stays within a few minutes
-    k = max(1, min(args.steps, 6))
-    sps, secs = oracle_steps(case, k)
-    line = {"metric": METRIC, "value": sps, "unit": "steps/s", "n_gpus": 0, "steps": k,
-            "warmup": 0, "ms_per_step": 1000.0 / sps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, numpy default_rng 20261203)",
-            "impl": "reference",
-            "config": {"workload": WORKLOAD, "precision": "fp64 serial oracle"},
-            "cpu_baseline": {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
-                             "sample": f"{k} time steps of the workload on the serial FP64 oracle "
-                                       f"(the Fortran reference is unbuildable: no Fortran compiler), {secs:.1f} s"},
-            "e2e": {"value": sps, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    case = synth.tandem_plates(n_steps=2, moving=True)
+    r = cpu_reference_sample(case, REFERENCE_SWEEP_PAIRS)
+    # each of the K requested steps is this bounded sample; one sample
+    # stands for all of them (the oracle is deterministic)
+    line = {"metric": METRIC, "value": r["steps_per_s"], "unit": "steps/s", "n_gpus": 0, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * r["step_s"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded, numpy default_rng 20261203)", "impl": "reference",
+            "config": {"workload": WORKLOAD, "precision": "FP64, the reference's algorithm (omega 1.7, "
+                                                          "max|pc - pco| < 1e-6, pcItaMax 5000)"},
+            "cpu_baseline": {"value": r["steps_per_s"], "unit": "steps/s", "cores": r["threads"], "kind": "port",
+                             "sample": r["sample"] + "; FP64 oracle port (the Fortran reference is unbuildable "
+                                       "here: no Fortran compiler on either machine)"},
+            "e2e": {"value": r["steps_per_s"], "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
 
-def time_path(solver, torch, flush, stream, steps: int, warmup: int, precision: int, div_tol: float,
-              clocks: "Clocks | None" = None):
-    """Per-step CUDA-event timing on the library stream, L2 flushed between
-    steps; each step is a replay of the captured step graph.  One more step
-    afterwards runs inside the profiling window (kernel by kernel) for the
-    solve's device time and algorithmic bytes."""
-    for _ in range(warmup):
-        solver.run(1, precision=precision, div_tol=div_tol, use_graph=1)
-    times, divs, res, iters = [], [], [], []
-    ctx = clocks if clocks is not None else _Null()
-    k0 = solver.kernel_launches()
-    rank_barrier(torch)
-    with ctx:
+# ---------------------------------------------------------------------------
+# GPU arms
+# ---------------------------------------------------------------------------
+
+def new_solver(case, local, tune=True):
+    from biocfd.solver import Solver
+    s = Solver(case, device=local)
+    s.setup()
+    if tune:
+        s.autotune()  # launch shapes of the solves; results do not depend on them
+    return s
+
+
+def timed_steps(s, torch, steps, precision, clocks=None, graph=1):
+    """Per-step CUDA events on the library stream; returns (ms list, launches)."""
+    stream = torch.cuda.ExternalStream(s.stream_ptr())
+    ts = []
+    k0 = s.kernel_launches()
+    with (clocks if clocks is not None else _Null()):
         for _ in range(steps):
-            with torch.cuda.stream(stream):
-                flush.add_(1.0)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            solver.run(1, precision=precision, div_tol=div_tol, use_graph=1)
+            s.run(1, precision=precision, div_tol=DIV_TOL, use_graph=graph)
             e1.record(stream)
             e1.synchronize()
-            times.append(e0.elapsed_time(e1))
-            d = [solver.divergence(g) for g in solver.handles]
-            divs.append(max(x[0] for x in d))
-            res.append(max(x[1] for x in d))
-            iters.append([solver.sor_stats(g)[0] for g in solver.handles])
-    rank_barrier(torch)
-    launches = solver.kernel_launches() - k0
-    solver.profile_begin()
-    solver.run(1, precision=precision, div_tol=div_tol)
-    prof = solver.profile_end()
-    prof["timed_launches"] = launches
-    return times, divs, res, iters, prof
+            ts.append(e0.elapsed_time(e1))
+    return ts, s.kernel_launches() - k0
 
 
-class _Null:
-    def __enter__(self):
-        return self
+def profiled_step(s, precision):
+    """One eager step inside a measurement window: solve device time and
+    algorithmic bytes, kernels launched, and the per-phase device times."""
+    s.profile_begin()
+    s.run(1, precision=precision, div_tol=DIV_TOL)
+    prof = s.profile_end()
+    prof["phases_ms"] = s.profile_phases()
+    return prof
 
-    def __exit__(self, *a):
-        return False
+
+def residual_stats(s):
+    """Largest FP64 Poisson residual (divergence units) left by the last
+    solves, and each block's SOR sweep pairs in the last step."""
+    res = max(s.divergence(g)[1] for g in s.handles)
+    return res, [s.sor_stats(g)[0] for g in s.handles]
 
 
-def sweep_roofline(torch, local, hbm, block=(384, 256, 256), fp32_pairs=40, fp64_pairs=4):
-    """Poisson sweeps on one body-free 384x256x256 block (the coarse block of
-    the tandem-plate workload, ~25M cells, far above the 129 MB L2): achieved
-    GB/s of the FP32 and FP64 red-black sweep kernels, algorithmic bytes from
-    the solve log (17 B / 33 B per cell per sweep pair plus the FP64 residual
-    and update passes of the FP32 correction)."""
+def field_errors(fa, fb, sa, sb):
+    import numpy as np
+    err = {}
+    for q in range(len(fa)):
+        for k in ("u", "v", "w", "p"):
+            a, b = fa[q][k], fb[q][k]
+            if k == "p":  # pressure is defined up to a constant per solve: compare about the mean
+                a, b = a - a.mean(), b - b.mean()
+            err[f"block{q + 1}_{k}"] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+    coef = [[abs(x - y) / max(abs(y), 1e-300) for x, y in zip(a, b)] for a, b in zip(sa, sb)]
+    return err, coef
+
+
+def headline(args, torch, local, world):
+    """The flagship mixed path on the tandem-plate workload, its FP64 arms,
+    phase split, roofline and e2e."""
+    import ctypes as C
+    import numpy as np
     from biocfd import synth
-    from biocfd.solver import Solver
-    from biocfd._lib import check
-    case = synth.uniform_block(tuple(block), noise=True)
-    s = Solver(case, device=local)
-    s.setup()
-    g = s.handles[0]
-    check(s.L.bcfd_cellcount_solid(g), "cellcount_solid")
-    check(s.L.bcfd_compute_div(g), "compute_div")
-    check(s.L.bcfd_block_sor_sweeps(g, 2, 1), "sor_sweeps")
-    s.autotune()  # the launch shapes a user gets after bcfd_autotune
-    cells = block[0] * block[1] * block[2]
-    out = {"block": "x".join(map(str, block)) + f" ({cells / 1e6:.1f}M cells), no body",
-           "l2": f"FP32 working set {17 * cells / 1e6:.0f} MB vs 129 MB L2",
-           "solve_launch": s.solve_launch(g)}
-    for prec, pairs, key in ((1, fp32_pairs, "fp32"), (0, fp64_pairs, "fp64")):
-        if pairs <= 0:
-            continue
-        runs = {}
-        for n in (pairs, 2 * pairs):
-            s.profile_begin()
-            check(s.L.bcfd_block_sor_sweeps(g, n, prec), "sor_sweeps")
-            runs[n] = s.profile_end()
-        p = runs[pairs]
-        gbs = p["sor_bytes"] / (p["sor_ms"] * 1e-3) / 1e9
-        # the sweep pairs alone: the difference between the 2P and P launches
-        # (the residual, update and launch costs cancel)
-        q = runs[2 * pairs]
-        mgbs = (q["sor_bytes"] - p["sor_bytes"]) / ((q["sor_ms"] - p["sor_ms"]) * 1e-3) / 1e9
-        out[key] = {"sweep_pairs": pairs, "ms": p["sor_ms"], "gbs": gbs, "frac_of_measured_hbm": gbs / hbm,
-                    "bytes": p["sor_bytes"], "sweep_pair_gbs_marginal": mgbs,
-                    "sweep_pair_frac_of_measured_hbm": mgbs / hbm,
-                    "half_sweep_us": (q["sor_ms"] - p["sor_ms"]) * 1e3 / (2 * pairs)}
+    from biocfd._lib import P_d, check
+    hbm, peak_kind = peaks()
+    n_pre = 2  # steps every arm runs from the initial state before the compared state
+    case = synth.tandem_plates(n_steps=args.steps + args.warmup + 8, moving=True)
+    ncells = sum(b.nx * b.ny * b.nz for b in case.blocks)
+    mu_f = 1.0 / case.re
+    out = {}
+    # ---- flagship: mixed precision --------------------------------------------
+    t0 = time.perf_counter()
+    s = new_solver(case, local)
+    setup_s = time.perf_counter() - t0
+    for _ in range(n_pre):
+        s.run(1, precision=1, div_tol=DIV_TOL, use_graph=1)
+    snap_mixed = ([s.fields(g) for g in s.handles], [s.stress(g, mu_f).tolist() for g in s.handles[1:]])
+    for _ in range(args.warmup):
+        s.run(1, precision=1, div_tol=DIV_TOL, use_graph=1)
+    clocks = Clocks(local)
+    rank_barrier(torch)
+    tmx, launches = timed_steps(s, torch, args.steps, 1, clocks)
+    rank_barrier(torch)
+    res_mx, pairs_mx = residual_stats(s)
+    prof = profiled_step(s, 1)
+    nfluid = sum(s.counts(g)["fluidCellCount"] for g in s.handles)
+    # ---- e2e through the C ABI with host buffers ------------------------------
+    host = []
+    for g in s.handles:
+        f = s.fields(g)
+        host.append({k: torch.from_numpy(np.ascontiguousarray(f[k].ravel(order="F"))).pin_memory()
+                     for k in ("u", "v", "w", "p")})
+    nbytes = sum(h[k].numel() * 8 for h in host for k in ("u", "v", "w", "p"))
+    e2e_times = []
+    for _ in range(args.steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for h, g in zip(host, s.handles):
+            ptr = [C.cast(h[k].data_ptr(), P_d) for k in ("u", "v", "w", "p")]
+            check(s.L.bcfd_block_upload_fields(g, *ptr, None, None, None), "upload")
+        s.run(1, precision=1, div_tol=DIV_TOL, use_graph=1)
+        for h, g in zip(host, s.handles):
+            ptr = [C.cast(h[k].data_ptr(), P_d) for k in ("u", "v", "w", "p")]
+            check(s.L.bcfd_block_download_fields(g, *ptr, None, None, None), "download")
+        e2e_times.append(time.perf_counter() - t0)
+    solve_launch = {f"block{q + 1}": s.solve_launch(g) for q, g in enumerate(s.handles)}
     s.close()
+    msmx = statistics.mean(tmx)
+    e2e_s = statistics.mean(e2e_times)
+    msmx, e2e_s = max_over_ranks([msmx, e2e_s])
+    achieved = prof["sor_bytes"] / (prof["sor_ms"] * 1e-3) / 1e9 if prof["sor_ms"] > 0 else 0.0
+    out["mixed"] = {"ms_per_step": msmx, "steps_per_s": 1000.0 / msmx, "steps": len(tmx),
+                    "div_residual": res_mx, "sweep_pairs_last_step": pairs_mx,
+                    "cell_updates_per_s": nfluid * 1000.0 / msmx, "launches_per_step": launches / len(tmx),
+                    "setup_s": setup_s, "solve_launch": solve_launch}
+    step_ms = sum(prof["phases_ms"].values())
+    out["phases"] = {"ms": prof["phases_ms"],
+                     "share": {k: v / step_ms for k, v in prof["phases_ms"].items()} if step_ms > 0 else {},
+                     "note": "one eagerly issued step of the flagship path (CUDA events at phase boundaries on "
+                             "the library stream); its total exceeds a graph replay by the launch gaps"}
+    traffic = profile_value("k_sor_dc_set_tandem.md", "traffic_bytes_per_launch")
+    out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                       "frac": achieved / hbm, "traffic": traffic,
+                       "kernel": "mixed Poisson solve launches (k_sor_dc_set / k_sor_dc, as autotuned)",
+                       "peak_source": peak_kind,
+                       "launches": prof["sor_launches"], "ms": prof["sor_ms"], "bytes": prof["sor_bytes"],
+                       "note": "algorithmic bytes from the solve log: 17 B per cell per FP32 sweep pair, 29 B per "
+                               "FP64 residual pass, 25 B per FP64 update pass; CUDA events around each solve "
+                               "launch; working set far above the 129 MB L2"}
+    out["e2e"] = {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
+                  "d2h_bytes_per_step": nbytes}
+    out["gpu_launches"] = launches
+    out["clocks"] = clocks.summary()
+    out["nfluid"] = nfluid
+    out["ncells"] = ncells
+    # ---- FP64 arms on the same workload ---------------------------------------
+    case_om = synth.with_mixed_omega(case)
+    arms = [("fp64_fast", 3, case_om, args.fp64_steps, "FP64 momentum + FP64 SOR without divisions (fused "
+             "residual, Newton-Raphson inverse diagonal), relaxing with the mixed path's factor"),
+            ("fp64", 2, case_om, args.fp64_steps, "FP64 momentum + FP64 SOR with the reference's sweep "
+             "arithmetic (one IEEE division per update), relaxing with the mixed path's factor")]
+    if args.fp64_input_omega:
+        arms.append(("fp64_input_omega", 2, case, 1, "as fp64, relaxing with the input's omega 1.7"))
+    for key, prec, arm_case, n_timed, what in arms:
+        if n_timed <= 0:
+            continue
+        s = new_solver(arm_case, local)
+        for _ in range(n_pre):
+            s.run(1, precision=prec, div_tol=DIV_TOL, use_graph=1)
+        snap = ([s.fields(g) for g in s.handles], [s.stress(g, mu_f).tolist() for g in s.handles[1:]])
+        ts, nl = timed_steps(s, torch, n_timed, prec)
+        res, pairs = residual_stats(s)
+        s.close()
+        ms = max_over_ranks([statistics.mean(ts)])[0]
+        err, coef = field_errors(snap_mixed[0], snap[0], snap_mixed[1], snap[1])
+        out[key] = {"ms_per_step": ms, "steps_per_s": 1000.0 / ms, "steps": len(ts), "div_residual": res,
+                    "sweep_pairs_last_step": pairs, "omega": [b.omega for b in arm_case.blocks],
+                    "what": what, "speedup_mixed_vs_this": ms / msmx,
+                    "mixed_error_vs_this": {"after_steps": n_pre, "field_rel_l2": err,
+                                            "coef_rel": coef,
+                                            "coefficients": "per plate: viscous drag, pressure drag, viscous "
+                                                            "lift, pressure lift"}}
+    if args.dropin_steps > 0:
+        # the drop-in path (reference arithmetic and stop test) on the same
+        # workload: its sweep pairs are the reference's (REFERENCE_SWEEP_PAIRS)
+        s = new_solver(case, local)
+        ts, _ = timed_steps(s, torch, args.dropin_steps, 0, graph=0)
+        out["fp64_dropin"] = {"ms_per_step": statistics.mean(ts), "steps": len(ts),
+                              "sweep_pairs_per_step": [s.sor_stats(g)[0] for g in s.handles],
+                              "stop": "max|pc - pco| < 1e-6 every 5th iteration, omega 1.7, pcItaMax 5000"}
+        s.close()
     return out
 
 
-def twelve_block(torch, local, steps=10, warmup=3, fp64_steps=2, moving=False):
-    """Twelve uneven blocks (coarse 256x192x192 + 11 fine blocks, 13.3M cells,
-    stationary thin plate): mixed-path time per step with the batched launches
-    and with one launch per block, and the plain FP64 path to the same residual.
-    The working set (> 2 GB) is far above L2, so no flush is needed."""
+def two_block(torch, local, steps, warmup):
+    """The two-block sphere workload (coarse 96x64x64 over 3x2x2 + fine 64^3 at
+    ratio 2, D = 0.5, Re 300): mixed path vs the FP64 arms, L2 flushed
+    between steps (its working set fits in L2)."""
     from biocfd import synth
-    from biocfd.solver import Solver
-    case = synth.twelve_block(n_steps=steps + warmup + 2, moving=moving)
-    ncells = sum(b.nx * b.ny * b.nz for b in case.blocks)
-    body = case.blocks[1]
-    out = {"workload": "12 blocks: coarse 256x192x192 over 8x6x6 + 11 fine blocks at ratio 2 "
-                       f"({body.nx}x{body.ny}x{body.nz} with a plate 0.5x0.125x0.0125, 2x128x64x64, 2x96x64x64, "
-                       f"2x64x48x48, 2x48^3, 2x32^3), {ncells / 1e6:.1f}M cells, Re 500" +
-                       (", plate heaving 0.5 sin(2 pi 0.25 t) and pitching 30 deg sin(2 pi 0.25 t + 90 deg), "
-                        "Search every step, graph replay (each step's kinematics staged before its launch)" if moving else
-                        ", stationary plate, graph replay"),
-           "div_tol": DIV_TOL}
-    arms = (("mixed_batched", 1, True, steps), ("mixed_per_block", 1, False, steps),
-            ("fp64_batched", 2, True, fp64_steps))
-    for key, prec, batching, n in arms:
-        if n <= 0:
-            continue
-        s = Solver(case, device=local)
-        s.set_batching(batching)
-        s.setup()
-        s.autotune()
+    case = synth.sphere_two_block(n_steps=steps + warmup + 4)
+    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
+    out = {"workload": "two-block sphere: coarse 96x64x64 over 3x2x2 + fine 64^3 at ratio 2, D=0.5, Re=300",
+           "l2": "flushed between timed steps (256 MB write)"}
+    for key, prec, c in (("mixed", 1, case), ("fp64_fast", 3, synth.with_mixed_omega(case)),
+                         ("fp64", 2, synth.with_mixed_omega(case)), ("fp64_input_omega", 2, case),
+                         ("fp64_dropin", 0, case)):
+        s = new_solver(c, local)
         stream = torch.cuda.ExternalStream(s.stream_ptr())
-        for _ in range(warmup if prec == 1 else 1):
+        for _ in range(warmup):
             s.run(1, precision=prec, div_tol=DIV_TOL, use_graph=1)
         ts = []
-        k0 = s.kernel_launches()
-        for _ in range(n):
+        for _ in range(steps):
+            with torch.cuda.stream(stream):
+                flush.add_(1.0)
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
@@ -302,119 +445,118 @@ def twelve_block(torch, local, steps=10, warmup=3, fp64_steps=2, moving=False):
             e1.record(stream)
             e1.synchronize()
             ts.append(e0.elapsed_time(e1))
-        res = max(s.divergence(g)[1] for g in s.handles)
-        ms = statistics.mean(ts)
-        out[key] = {"ms_per_step": ms, "steps_per_s": 1000.0 / ms, "steps": n, "div_residual": res,
-                    "launches_per_step": (s.kernel_launches() - k0) / n,
-                    "cell_updates_per_s": ncells * 1000.0 / ms}
+        res, pairs = residual_stats(s)
         s.close()
-    if "fp64_batched" in out:
-        out["speedup_mixed_vs_fp64"] = out["fp64_batched"]["ms_per_step"] / out["mixed_batched"]["ms_per_step"]
-    out["speedup_batched_vs_per_block"] = (out["mixed_per_block"]["ms_per_step"] /
-                                           out["mixed_batched"]["ms_per_step"])
+        ms = statistics.mean(ts)
+        out[key] = {"ms_per_step": ms, "steps_per_s": 1000.0 / ms, "div_residual": res,
+                    "sweep_pairs_last_step": pairs}
+    for key in ("fp64_fast", "fp64", "fp64_input_omega"):
+        out[f"speedup_mixed_vs_{key}"] = out[key]["ms_per_step"] / out["mixed"]["ms_per_step"]
     return out
 
 
-def tandem(torch, local, steps=5, warmup=2, cmp_steps=2, moving=False):
-    """Two stationary plates in tandem on the 45M-cell layout (coarse 384x256x256
-    + two fine 256x192x192 blocks): time per step of the mixed path to the
-    divergence residual 1e-6, of the plain FP64 path with the input's omega 1.7
-    (which stops at pcItaMax = 5000 iterations per solve on the 384-cell block,
-    short of 1e-6) and of the plain FP64 path relaxing with the mixed path's
-    factor (which reaches 1e-6); and the mixed path's error against both FP64
-    runs after `cmp_steps` steps from the same initial state (relative L2 of
-    u, v, w, p per block; the drag and lift coefficients of each plate).
-    With `moving` (both plates heaving and pitching, Search every step) only
-    the mixed path and the FP64 path at the mixed path's factor run."""
-    import numpy as np
+def sweep_roofline(torch, local, hbm, block=(384, 256, 256), fp32_pairs=40, fp64_pairs=8):
+    """Poisson sweeps on one body-free 384x256x256 block (the coarse block of
+    the tandem-plate workload, ~25M cells, far above the 129 MB L2): achieved
+    GB/s of the FP32 and FP64 red-black sweep kernels, algorithmic bytes from
+    the solve log (17 B / 33 B per cell per sweep pair plus the FP64 residual
+    and update passes of the FP32 correction)."""
     from biocfd import synth
-    from biocfd.solver import Solver
-    assert cmp_steps >= 2
-    case = synth.tandem_plates(n_steps=steps + warmup + cmp_steps + 2, moving=moving)
+    from biocfd._lib import check
+    case = synth.uniform_block(tuple(block), noise=True)
+    s = new_solver(case, local, tune=False)
+    g = s.handles[0]
+    check(s.L.bcfd_cellcount_solid(g), "cellcount_solid")
+    check(s.L.bcfd_compute_div(g), "compute_div")
+    check(s.L.bcfd_block_sor_sweeps(g, 2, 1), "sor_sweeps")
+    s.autotune()
+    cells = block[0] * block[1] * block[2]
+    out = {"block": "x".join(map(str, block)) + f" ({cells / 1e6:.1f}M cells), no body",
+           "l2": f"FP32 working set {17 * cells / 1e6:.0f} MB vs 129 MB L2", "solve_launch": s.solve_launch(g)}
+    for prec, pairs, key in ((1, fp32_pairs, "fp32"), (0, fp64_pairs, "fp64_reference_sweeps"),
+                             (2, fp64_pairs, "fp64_division_free")):
+        runs = {}
+        for n in (pairs, 2 * pairs):
+            s.profile_begin()
+            check(s.L.bcfd_block_sor_sweeps(g, n, prec), "sor_sweeps")
+            runs[n] = s.profile_end()
+        p, q = runs[pairs], runs[2 * pairs]
+        gbs = p["sor_bytes"] / (p["sor_ms"] * 1e-3) / 1e9
+        # the sweep pairs alone: the difference between the 2P and P launches
+        mgbs = (q["sor_bytes"] - p["sor_bytes"]) / ((q["sor_ms"] - p["sor_ms"]) * 1e-3) / 1e9
+        pair_us = (q["sor_ms"] - p["sor_ms"]) * 1e3 / pairs
+        out[key] = {"sweep_pairs": pairs, "ms": p["sor_ms"], "gbs": gbs, "frac_of_measured_hbm": gbs / hbm,
+                    "sweep_pair_gbs_marginal": mgbs, "sweep_pair_frac_of_measured_hbm": mgbs / hbm,
+                    "sweep_pair_us": pair_us, "half_sweep_us": pair_us / 2}
+        if prec != 1:
+            # FP64 work per cell update: 7 FMA residual + reference divide (or
+            # 3 more FMA/MUL of the division-free form)
+            out[key]["cell_updates_per_s"] = cells / (pair_us * 1e-6)
+    s.close()
+    return out
+
+
+def alu_rates(local):
+    import ctypes as C
+    from biocfd._lib import check, load
+    from biocfd.solver import Solver  # noqa: F401  (initialises the library on the device)
+    L = load()
+    check(L.bcfd_init(local), "init")
+    v = (C.c_double * 3)()
+    check(L.bcfd_measure_alu_rates(v), "measure_alu_rates")
+    return {"fp64_fma_gflops": v[0], "fp64_div_gops": v[1], "fp32_fma_gflops": v[2],
+            "how": "independent FMA / divide chains on every SM (8 CTAs x 256 threads per SM), best of 3 "
+                   "CUDA-event timings, no clock changes"}
+
+
+def twelve_block(torch, local, steps=5, warmup=3, fp64_steps=1, moving=False):
+    """Twelve uneven blocks (coarse 320x224x224 + 11 fine blocks, 20.0M cells,
+    plate): mixed path batched and per block, plain FP64 to the same residual."""
+    from biocfd import synth
+    case = synth.twelve_block(n_steps=steps + warmup + 2, moving=moving)
     ncells = sum(b.nx * b.ny * b.nz for b in case.blocks)
-    out = {"workload": "tandem plates: coarse 384x256x256 over 6x4x4 + two fine 256x192x192 at ratio 2, "
-                       f"{ncells / 1e6:.1f}M cells, " +
-                       ("plates heaving 0.125 sin(2 pi 0.25 t) and pitching 15 deg sin(2 pi 0.25 t + 90 deg), "
-                        "Search every step, " if moving else "stationary ") +
-                       "plates 0.5x0.125x0.0125 with centres 2.5 apart (1.5 chords), Re 1000, graph replay",
-           "div_tol": DIV_TOL}
-    mu_f = 1.0 / case.re
-    snaps = {}
-    case_om = synth.with_mixed_omega(case)
-    arms = [("mixed", 1, steps, case), ("fp64", 2, 1, case), ("fp64_mixed_omega", 2, 1, case_om)]
-    if moving:
-        del arms[1]
-    for key, prec, n_timed, arm_case in arms:
-        s = Solver(arm_case, device=local)
+    body = case.blocks[1]
+    out = {"workload": f"12 blocks: coarse 320x224x224 over 10x7x7 + 11 fine blocks at ratio 2 "
+                       f"({body.nx}x{body.ny}x{body.nz} with a plate 0.5x0.125x0.0125, 2x128x64x64, 2x96x64x64, "
+                       f"2x64x48x48, 2x48^3, 2x32^3), {ncells / 1e6:.1f}M cells, Re 500" +
+                       (", plate heaving 0.5 sin(2 pi 0.25 t) and pitching 30 deg sin(2 pi 0.25 t + 90 deg), "
+                        "Search every step" if moving else ", stationary plate") + ", graph replay"}
+    arms = (("mixed_batched", 1, True, steps), ("mixed_per_block", 1, False, steps),
+            ("fp64_fast_batched", 3, True, fp64_steps))
+    for key, prec, batching, n in arms:
+        if n <= 0:
+            continue
+        from biocfd.solver import Solver
+        s = Solver(case if prec == 1 else synth.with_mixed_omega(case), device=local)
+        s.set_batching(batching)
         s.setup()
         s.autotune()
-        stream = torch.cuda.ExternalStream(s.stream_ptr())
-        # mixed: cmp_steps, warm-up, then the timed steps; FP64: cmp_steps, the
-        # last of them (a graph replay) timed
-        n_pre = cmp_steps + warmup if prec == 1 else cmp_steps - 1
-        ts = []
-        k0 = 0
-        for it in range(n_pre + n_timed):
-            timed = it >= n_pre
-            if it == n_pre:
-                k0 = s.kernel_launches()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
+        for _ in range(warmup if prec == 1 else 1):
             s.run(1, precision=prec, div_tol=DIV_TOL, use_graph=1)
-            e1.record(stream)
-            e1.synchronize()
-            if timed:
-                ts.append(e0.elapsed_time(e1))
-            if it == cmp_steps - 1:
-                snaps[key] = ([s.fields(g) for g in s.handles],
-                              [s.stress(g, mu_f).tolist() for g in s.handles[1:]])
-        res = max(s.divergence(g)[1] for g in s.handles)
+        ts, nl = timed_steps(s, torch, n, prec)
+        res, _ = residual_stats(s)
         ms = statistics.mean(ts)
-        out[key] = {"ms_per_step": ms, "steps_per_s": 1000.0 / ms, "steps": len(ts), "div_residual": res,
-                    "launches_per_step": (s.kernel_launches() - k0) / len(ts),
-                    "cell_updates_per_s": ncells * 1000.0 / ms}
+        out[key] = {"ms_per_step": ms, "steps_per_s": 1000.0 / ms, "steps": n, "div_residual": res,
+                    "launches_per_step": nl / n, "cell_updates_per_s": ncells * 1000.0 / ms}
         s.close()
-    out["fp64_mixed_omega"]["omega"] = [b.omega for b in case_om.blocks]
-    if "fp64" in out:
-        out["fp64"]["omega"] = [b.omega for b in case.blocks]
-        out["speedup_mixed_vs_fp64"] = out["fp64"]["ms_per_step"] / out["mixed"]["ms_per_step"]
-    out["speedup_mixed_vs_fp64_mixed_omega"] = (out["fp64_mixed_omega"]["ms_per_step"] /
-                                                out["mixed"]["ms_per_step"])
-    fm, sm = snaps["mixed"]
-    for ref in ("fp64_mixed_omega", "fp64"):
-        if ref not in snaps:
-            continue
-        fd, sd = snaps[ref]
-        err = {}
-        for q in range(len(fm)):
-            for k in ("u", "v", "w", "p"):
-                a, b = fm[q][k], fd[q][k]
-                if k == "p":  # pressure is defined up to a constant per solve: compare about the mean
-                    a, b = a - a.mean(), b - b.mean()
-                err[f"block{q + 1}_{k}"] = float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
-        out[f"error_vs_{ref}"] = {"after_steps": cmp_steps, "field_rel_l2": err,
-                                  "coefficients": "viscous drag, pressure drag, viscous lift, pressure lift",
-                                  "plates_mixed": sm, f"plates_{ref}": sd,
-                                  "coef_rel": [[abs(x - y) / max(abs(y), 1e-300) for x, y in zip(a, b)]
-                                               for a, b in zip(sm, sd)]}
+    if "fp64_fast_batched" in out:
+        out["speedup_mixed_vs_fp64_fast"] = (out["fp64_fast_batched"]["ms_per_step"] /
+                                             out["mixed_batched"]["ms_per_step"])
+    out["speedup_batched_vs_per_block"] = (out["mixed_per_block"]["ms_per_step"] /
+                                           out["mixed_batched"]["ms_per_step"])
     return out
 
 
 def adjoint_bench(torch, local, steps=4, every=2):
     """Discrete adjoint of whole FP64 steps on the 64^3 sphere block (D = 0.25,
     Re 100): time per step of forward + checkpointed reverse pass for the
-    objective "time-averaged drag + lift coefficients", with the adjoint
-    Poisson solves in FP64 SOR and in FP32 sweeps + FP64 defect correction
-    (both to the same FP64 residual)."""
-    import time
+    objective "time-averaged drag + lift coefficients"."""
     from biocfd import synth
     from biocfd.adjoint import adjoint_run
     from biocfd.solver import Solver
     case = synth.sphere_single_block(n=64, n_steps=steps + 2)
     out = {"workload": f"64^3 sphere block (D=0.25, Re 100), {steps} FP64 steps, checkpoint every {every}, "
-                       "objective mean of drag + lift coefficients, gradients in uc, u,v,w,p^0 and the "
-                       "body's kinematic scalars", "adj_tol": 1e-13}
+                       "objective mean of drag + lift coefficients", "adj_tol": 1e-13}
     for key, prec in (("adjoint_fp64_solves", 0), ("adjoint_mixed_solves", 1)):
         s = Solver(case, device=local)
         s.setup()
@@ -427,200 +569,112 @@ def adjoint_bench(torch, local, steps=4, every=2):
         secs = time.perf_counter() - t0
         out[key] = {"ms_per_step": 1000.0 * secs / steps, "J": J, "dJ_duc": duc}
         s.close()
-    out["speedup_mixed_solves"] = (out["adjoint_fp64_solves"]["ms_per_step"] /
-                                   out["adjoint_mixed_solves"]["ms_per_step"])
-    out["dJ_duc_rel_diff"] = abs(out["adjoint_fp64_solves"]["dJ_duc"] - out["adjoint_mixed_solves"]["dJ_duc"]) / \
-        abs(out["adjoint_fp64_solves"]["dJ_duc"])
     return out
 
 
 def run_gpu(args):
-    import numpy as np
     import torch
-    from biocfd import synth
-    from biocfd.solver import Solver
 
     rank, world, local = dist_env()
     torch.cuda.set_device(local)
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("gloo")
-    case = synth.sphere_two_block(n_steps=args.steps + args.warmup)
-    s = Solver(case, device=local)
-    s.setup()
-    stream = torch.cuda.ExternalStream(s.stream_ptr())
-    flush = torch.zeros(64 * 1024 * 1024, dtype=torch.float32, device=f"cuda:{local}")  # 256 MB > L2
-
-    tol = DIV_TOL
-
-    if args.mixed_only:
-        # the flagship arm alone (for profiler captures of its kernels)
-        s.autotune()
-        t, _, res, it, _ = time_path(s, torch, flush, stream, args.steps, args.warmup, 1, tol)
-        print(json.dumps({"run": "mixed arm only", "ms_per_step": statistics.mean(t), "div_residual": max(res),
-                          "fp32_sweeps_last_step": it[-1]}), flush=True)
-        s.close()
-        return
-
-    def arm(precision, clocks=None, arm_case=None):
-        nonlocal s, stream
-        s.close()
-        s = Solver(case if arm_case is None else arm_case, device=local)
-        s.setup()
-        s.autotune()  # launch shapes of the solves; results do not depend on them
-        stream = torch.cuda.ExternalStream(s.stream_ptr())
-        return time_path(s, torch, flush, stream, args.steps, args.warmup, precision, tol, clocks)
-
-    # drop-in FP64 path: the reference's stop test (max|pc - pco| < 1e-6)
-    t0_, div0, res0, it0, prof0 = arm(0)
-    # plain FP64 SOR run to the same FP64 residual target as the mixed path
-    t64, div64, res64, it64, prof64 = arm(2)
-    # the same, relaxing with the mixed path's factor instead of the input's 1.7
-    case_om = synth.with_mixed_omega(case)
-    t64o, _, res64o, it64o, _ = arm(2, arm_case=case_om)
-    # flagship: FP32 momentum + FP32 SOR with FP64 defect correction
-    clocks = Clocks(local)
-    tmx, divmx, resmx, itmx, profmx = arm(1, clocks)
-    # e2e through the C ABI with host buffers (pinned), flagship precision
-    host = []
-    for spec, g in zip(case.blocks, s.handles):
-        f = s.fields(g)
-        host.append({k: torch.from_numpy(np.ascontiguousarray(f[k].ravel(order="F"))).pin_memory()
-                     for k in ("u", "v", "w", "p")})
-    import ctypes as C
-    from biocfd._lib import P_d, check
-    nbytes = sum(h[k].numel() * 8 for h in host for k in ("u", "v", "w", "p"))
-    e2e_times = []
-    for step in range(args.steps):
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for h, g in zip(host, s.handles):
-            ptr = [C.cast(h[k].data_ptr(), P_d) for k in ("u", "v", "w", "p")]
-            check(s.L.bcfd_block_upload_fields(g, *ptr, None, None, None), "upload")
-        s.run(1, precision=1, div_tol=tol, use_graph=1)
-        for h, g in zip(host, s.handles):
-            ptr = [C.cast(h[k].data_ptr(), P_d) for k in ("u", "v", "w", "p")]
-            check(s.L.bcfd_block_download_fields(g, *ptr, None, None, None), "download")
-        e2e_times.append(time.perf_counter() - t0)
-
-    ms64 = statistics.mean(t64)
-    ms64o = statistics.mean(t64o)
-    ms0 = statistics.mean(t0_)
-    msmx = statistics.mean(tmx)
-    e2e_s = statistics.mean(e2e_times)
-    msmx, ms64, ms0, e2e_s, ms64o = max_over_ranks([msmx, ms64, ms0, e2e_s, ms64o])
-    nfluid = sum(s.counts(g)["fluidCellCount"] for g in s.handles)
     hbm, peak_kind = peaks()
-    achieved = profmx["sor_bytes"] / (profmx["sor_ms"] * 1e-3) / 1e9 if profmx["sor_ms"] > 0 else 0.0
-    ach64 = prof64["sor_bytes"] / (prof64["sor_ms"] * 1e-3) / 1e9 if prof64["sor_ms"] > 0 else 0.0
-    traffic = traffic_from_profiles()
+    t_start = time.perf_counter()
+    h = headline(args, torch, local, world)
+    mixed = h["mixed"]
+    fast = h.get("fp64_fast")
     line = {
         "metric": METRIC,
-        "value": world * 1000.0 / msmx,
+        "value": world * mixed["steps_per_s"],
         "unit": "steps/s",
         "n_gpus": world,
         "steps": args.steps,
         "warmup": args.warmup,
-        "ms_per_step": msmx,
+        "ms_per_step": mixed["ms_per_step"],
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 sweeps + f64 defect correction",
         "data": "synthetic (seeded, numpy default_rng 20261203)",
-        "config": {"workload": WORKLOAD, "blocks": "96x64x64 + 64^3", "parallelism": f"replicas x{world}",
-                   "l2": "flushed between timed steps (256 MB write)", "timed": "per-step CUDA events",
-                   "launch": "each step one replay of the captured step CUDA graph"},
-        "fp64": {"steps_per_s": 1000.0 / ms64, "ms_per_step": ms64, "div_residual": max(res64),
-                 "div_tol": tol, "max_div_after_correction": max(div64), "sor_iters_last_step": it64[-1],
-                 "solve_gbs": ach64},
-        "fp64_dropin": {"steps_per_s": 1000.0 / ms0, "ms_per_step": ms0, "div_residual": max(res0),
-                        "stop": "max|pc - pco| < epsi every 5th iteration (reference stop test)",
-                        "sor_iters_last_step": it0[-1]},
-        "mixed": {"steps_per_s": 1000.0 / msmx, "ms_per_step": msmx, "div_residual": max(resmx),
-                  "div_tol": tol, "max_div_after_correction": max(divmx), "fp32_sweeps_last_step": itmx[-1]},
-        "fp64_mixed_omega": {"steps_per_s": 1000.0 / ms64o, "ms_per_step": ms64o, "div_residual": max(res64o),
-                             "omega": [b.omega for b in case_om.blocks], "sor_iters_last_step": it64o[-1],
-                             "speedup_mixed_vs_this": ms64o / msmx,
-                             "note": "plain FP64 SOR relaxing with the mixed path's default factor "
-                                     "2/(1+sin(pi/n_max)) instead of the input's 1.7"},
-        "speedup_vs_fp64": ms64 / msmx,
-        "cell_updates_per_s": world * nfluid * 1000.0 / msmx,
-        "e2e": {"value": world / e2e_s, "unit": "steps/s", "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes},
-        "gpu_launches": profmx["timed_launches"],
-        "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                     "frac": achieved / hbm, "traffic": traffic, "kernel": "mixed Poisson solve (k_sor_dc or k_sor_tb, as autotuned)",
-                     "peak_source": peak_kind,
-                     "note": "algorithmic bytes: 17 B per cell per FP32 sweep pair + FP64 residual/update passes; "
-                             "the 64^3 and 96x64x64 blocks are L2-resident during a solve"},
-        "clocks": clocks.summary(),
-        "solve_launch": {f"block{q + 1}": s.solve_launch(g) for q, g in enumerate(s.handles)},
+        "config": {"workload": WORKLOAD, "blocks": "384x256x256 + 2 x 256x192x192",
+                   "parallelism": f"replicas x{world}",
+                   "l2": "not flushed: working set ~5 GB, far above the 129 MB L2",
+                   "timed": "per-step CUDA events on the library stream",
+                   "launch": "each step one replay of the captured step CUDA graph (each step's kinematics "
+                             "staged on the host before its replay)"},
+        "e2e": h["e2e"],
+        "gpu_launches": h["gpu_launches"],
+        "roofline": h["roofline"],
+        "clocks": h["clocks"],
+        "mixed": mixed,
+        "phases": h["phases"],
+        "cell_updates_per_s": world * mixed["cell_updates_per_s"],
     }
-    if not args.no_sweep_roofline:
+    for key in ("fp64_fast", "fp64", "fp64_input_omega", "fp64_dropin"):
+        if key in h:
+            line[key] = h[key]
+    if fast:
+        line["speedup_vs_fp64"] = fast["ms_per_step"] / mixed["ms_per_step"]
+    if not args.no_extras:
+        line["alu_rates"] = alu_rates(local)
         line["sweep_roofline"] = sweep_roofline(torch, local, hbm)
-    if not args.no_twelve_block:
-        line["twelve_block"] = twelve_block(torch, local)
-        line["twelve_block_moving"] = twelve_block(torch, local, steps=5, fp64_steps=1, moving=True)
-    if not args.no_adjoint:
+        line["two_block"] = two_block(torch, local, steps=10, warmup=3)
+        line["twelve_block_moving"] = twelve_block(torch, local, moving=True)
         line["adjoint"] = adjoint_bench(torch, local)
-    if not args.no_tandem:
-        line["tandem"] = tandem(torch, local)
-        line["tandem_moving"] = tandem(torch, local, moving=True)
     if rank == 0 and not args.no_cpu_baseline:
-        sps, secs = oracle_steps(case, 1)
-        line["cpu_baseline"] = {"value": sps, "unit": "steps/s", "cores": 1, "kind": "port",
-                                "sample": f"1 time step of the same workload on the serial FP64 oracle, {secs:.1f} s"}
+        from biocfd import synth
+        r = cpu_reference_sample(synth.tandem_plates(n_steps=2, moving=True), REFERENCE_SWEEP_PAIRS)
+        line["cpu_baseline"] = {"value": r["steps_per_s"], "unit": "steps/s", "cores": r["threads"],
+                                "kind": "port", "sample": r["sample"]}
+    line["bench_wall_s"] = time.perf_counter() - t_start
     if rank == 0:
         print(json.dumps(line), flush=True)
-    s.close()
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--fp64-steps", type=int, default=1, help="timed steps of each FP64 arm")
+    ap.add_argument("--fp64-input-omega", action="store_true",
+                    help="also run the plain FP64 arm with the input omega 1.7 (~16 s per step)")
+    ap.add_argument("--dropin-steps", type=int, default=0,
+                    help="steps of the drop-in FP64 path (reference stop test) on the headline workload")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--no-sweep-roofline", action="store_true")
-    ap.add_argument("--no-twelve-block", action="store_true")
-    ap.add_argument("--no-adjoint", action="store_true")
-    ap.add_argument("--no-tandem", action="store_true")
-    ap.add_argument("--tandem-only", action="store_true",
-                    help="only the 45M-cell tandem-plate measurement (mixed vs FP64, error vs FP64)")
-    ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint timing")
-    ap.add_argument("--twelve-only", action="store_true",
-                    help="only the twelve-block measurement (batched vs per-block launches)")
-    ap.add_argument("--mixed-only", action="store_true",
-                    help="time only the flagship arm and print a short line (profiler captures)")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the ALU rates, sweep roofline, two-block, twelve-block and adjoint keys")
     ap.add_argument("--sweep-only", default="",
                     help="nx,ny,nz[,fp32_pairs[,fp64_pairs]]: only the Poisson sweep measurement on that block")
+    ap.add_argument("--twelve-only", action="store_true", help="only the twelve-block measurement")
+    ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint timing")
+    ap.add_argument("--alu-only", action="store_true", help="only the arithmetic-rate measurement")
     args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.sweep_only:
+        import torch
+        v = [int(x) for x in args.sweep_only.split(",")]
+        hbm, _ = peaks()
+        print(json.dumps(sweep_roofline(torch, 0, hbm, v[:3], v[3] if len(v) > 3 else 40,
+                                        v[4] if len(v) > 4 else 8)), flush=True)
+        return
+    if args.twelve_only:
+        import torch
+        print(json.dumps(twelve_block(torch, 0, args.steps, args.warmup)), flush=True)
+        print(json.dumps(twelve_block(torch, 0, args.steps, args.warmup, moving=True)), flush=True)
+        return
     if args.adjoint_only:
         import torch
         torch.cuda.set_device(0)
         print(json.dumps(adjoint_bench(torch, 0)), flush=True)
         return
-    if args.tandem_only:
-        import torch
-        torch.cuda.set_device(0)
-        print(json.dumps(tandem(torch, 0)), flush=True)
-        print(json.dumps(tandem(torch, 0, moving=True)), flush=True)
+    if args.alu_only:
+        print(json.dumps(alu_rates(0)), flush=True)
         return
-    if args.twelve_only:
-        import torch
-        print(json.dumps(twelve_block(torch, 0, args.steps, args.warmup)), flush=True)
-        print(json.dumps(twelve_block(torch, 0, args.steps, args.warmup, fp64_steps=1, moving=True)), flush=True)
-        return
-    if args.sweep_only:
-        import torch
-        v = [int(x) for x in args.sweep_only.split(",")]
-        hbm, _ = peaks()
-        r = sweep_roofline(torch, 0, hbm, v[:3], v[3] if len(v) > 3 else 40, v[4] if len(v) > 4 else 4)
-        print(json.dumps(r), flush=True)
-        return
-    if args.warmup < 3:
-        args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
     else:

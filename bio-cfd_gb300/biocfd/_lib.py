@@ -78,6 +78,8 @@ _SIGS = {
     "bcfd_block_sor_sweeps": [c_i64, c_i64, c_int],
     "bcfd_profile_begin": [],
     "bcfd_profile_end": [C.POINTER(ProfileReport)],
+    "bcfd_profile_phases": [P_d, c_int],
+    "bcfd_measure_alu_rates": [P_d],
     "bcfd_init": [c_int], "bcfd_finalize": [], "bcfd_synchronize": [],
     "bcfd_get_stream": [C.POINTER(C.c_void_p)],
     "bcfd_block_create": [c_i64, c_i64, c_i64, P_d, P_d, P_d, P_d, P_d, P_d, P_i64],

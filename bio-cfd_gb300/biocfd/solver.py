@@ -323,6 +323,15 @@ class Solver:
         check(self.L.bcfd_profile_end(C.byref(r)), "profile_end")
         return {k: getattr(r, k) for k, _ in r._fields_}
 
+    PHASES = ("momentum", "forcing", "poisson_solves", "coupling", "correction", "motion_search",
+              "forcing_field")
+
+    def profile_phases(self) -> dict:
+        """Device ms per step phase of the eager steps of the last measurement window."""
+        ms = np.zeros(len(self.PHASES))
+        check(self.L.bcfd_profile_phases(_pd(ms), len(ms)), "profile_phases")
+        return {k: float(v) for k, v in zip(self.PHASES, ms)}
+
     def stress(self, g: int, mu_f: float, rho_f: float = 1.0) -> np.ndarray:
         """stress_calculation (src/StressCalc.f90:14-208): viscous drag, pressure drag,
         viscous lift, pressure lift coefficients."""

@@ -404,18 +404,21 @@ TWELVE_BLOCK_BOXES = (
 
 def twelve_block(n_steps: int = 10, seed: int = SEED, moving: bool = False) -> Case:
     """Twelve blocks of uneven sizes around a rigid ellipsoidal plate (semi-axes
-    0.5 x 0.125 x 0.0125, surface 51), Re = 500 on the chord.  With `moving`
-    the plate heaves h(t) = 0.5 sin(2 pi 0.25 t) and pitches about x
-    theta(t) = 30 deg sin(2 pi 0.25 t + 90 deg) (plus the reference's fixed
-    tow); its block is then 160x144x96, tall enough that the heave stays inside
-    the reference's block-move margins (src/Search.F90:1010-1024)."""
+    0.5 x 0.125 x 0.0125, surface 51), Re = 500 on the chord: a coarse
+    320x224x224 block over 10x7x7 (dx 1/32, 16.1M cells) and the eleven fine
+    blocks of TWELVE_BLOCK_BOXES at ratio 2 (3.9M cells), 20.0M cells in all.
+    With `moving` the plate heaves h(t) = 0.5 sin(2 pi 0.25 t) and pitches
+    about x theta(t) = 30 deg sin(2 pi 0.25 t + 90 deg) (plus the reference's
+    fixed tow); its block is then 160x144x96 (20.7M cells in all), tall enough
+    that the heave stays inside the reference's block-move margins
+    (src/Search.F90:1010-1024)."""
     boxes = list(TWELVE_BLOCK_BOXES)
     motion = inputs = None
     if moving:
         boxes[0] = ((0.5, 3.0), (0.25, 2.5), (0.5, 2.0))
         motion = Motion(a0_deg=30.0, bfreq=0.25, yamp=0.5)
         inputs = MotionInputs(aoa_deg=0.0, phase_deg=90.0, piv_pt=0.0, freq=0.25, dxmin=1.0 / 64.0)
-    return multi_block(coarse=(256, 192, 192), domain=(8.0, 6.0, 6.0), fine_boxes=tuple(boxes),
+    return multi_block(coarse=(320, 224, 224), domain=(10.0, 7.0, 7.0), fine_boxes=tuple(boxes),
                        body=0, diameter=1.0, reynolds=500.0, n_steps=n_steps, seed=seed, plate=True,
                        plate_axes=(0.5, 0.125, 0.0125), motion=motion, motion_inputs=inputs)
 

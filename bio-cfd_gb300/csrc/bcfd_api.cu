@@ -129,6 +129,21 @@ void prof_mark(bool /*begin*/) {
   cudaEventRecord(L.prof_events[L.prof_used++], stream());
 }
 
+void phase_mark(int ph) {
+  Lib& L = lib();
+  if (!L.prof_on) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream(), &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+  if (L.phase_used == L.phase_events.size()) {
+    cudaEvent_t e;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    L.phase_events.push_back(e);
+    L.phase_ids.push_back(0);
+  }
+  L.phase_ids[L.phase_used] = ph;
+  cudaEventRecord(L.phase_events[L.phase_used++], stream());
+}
+
 int take_block_error(HostBlock* hb) {
   int e = 0;
   BCFD_CUDA(cudaMemcpyAsync(&e, hb->d.err, sizeof(int), cudaMemcpyDeviceToHost, stream()));
@@ -1180,13 +1195,23 @@ int bcfd_solid_cell_bc_move(bcfd_handle h) {
   return launch_solid_bc(hb, true);
 }
 
+// The routines below can record a device status (a probe without a bracket,
+// a list over capacity, a non-finite residual, a wait that gave up); called
+// one at a time they return it, which synchronises the library stream.  The
+// whole-step driver reads the status once per step instead.
+#define RET_DEV(hb, expr) \
+  do {                    \
+    TRY(expr);            \
+    return take_block_error(hb); \
+  } while (0)
+
 // ---- forcing ----
-int bcfd_velocity_forcing1(bcfd_handle h) { LOCK(); GETB(h); return launch_forcing_velocity(hb, 0); }
-int bcfd_pressure_forcing1(bcfd_handle h) { LOCK(); GETB(h); return launch_forcing_pressure(hb, 0); }
-int bcfd_velocity_forcing_field(bcfd_handle h) { LOCK(); GETB(h); return launch_forcing_velocity(hb, 1); }
-int bcfd_pressure_forcing_field(bcfd_handle h) { LOCK(); GETB(h); return launch_forcing_pressure(hb, 1); }
-int bcfd_velocity_forcing_ghost(bcfd_handle h) { LOCK(); GETB(h); return launch_forcing_velocity(hb, 2); }
-int bcfd_pressure_forcing_ghost(bcfd_handle h) { LOCK(); GETB(h); return launch_forcing_pressure(hb, 2); }
+int bcfd_velocity_forcing1(bcfd_handle h) { LOCK(); GETB(h); RET_DEV(hb, launch_forcing_velocity(hb, 0)); }
+int bcfd_pressure_forcing1(bcfd_handle h) { LOCK(); GETB(h); RET_DEV(hb, launch_forcing_pressure(hb, 0)); }
+int bcfd_velocity_forcing_field(bcfd_handle h) { LOCK(); GETB(h); RET_DEV(hb, launch_forcing_velocity(hb, 1)); }
+int bcfd_pressure_forcing_field(bcfd_handle h) { LOCK(); GETB(h); RET_DEV(hb, launch_forcing_pressure(hb, 1)); }
+int bcfd_velocity_forcing_ghost(bcfd_handle h) { LOCK(); GETB(h); RET_DEV(hb, launch_forcing_velocity(hb, 2)); }
+int bcfd_pressure_forcing_ghost(bcfd_handle h) { LOCK(); GETB(h); RET_DEV(hb, launch_forcing_pressure(hb, 2)); }
 
 // ---- search ----
 int bcfd_compute_surface_norm(bcfd_handle h, int64_t inor) {
@@ -1200,34 +1225,34 @@ int bcfd_tagging_th(bcfd_handle h) {
   GETB(h);
   TRY(launch_tagging(hb));
   // tagging_th_core ends with the three counts (src/Search.F90:365-380)
-  return launch_cellcount(hb, false);
+  RET_DEV(hb, launch_cellcount(hb, false));
 }
 int bcfd_selective_retagging_th(bcfd_handle h) {
   LOCK();
   GETB(h);
   if (hb->blk_mv_tag != 0) return 0;
   TRY(launch_retagging(hb));
-  return launch_cellcount(hb, false);
+  RET_DEV(hb, launch_cellcount(hb, false));
 }
 int bcfd_cellcount_solid(bcfd_handle h) {
   LOCK();
   GETB(h);
-  return launch_cellcount(hb, false);
+  RET_DEV(hb, launch_cellcount(hb, false));
 }
 int bcfd_cellcount_solid_coarse(bcfd_handle h) {
   LOCK();
   GETB(h);
-  return launch_cellcount(hb, true);
+  RET_DEV(hb, launch_cellcount(hb, true));
 }
 int bcfd_compute_norm_distance(bcfd_handle h) {
   LOCK();
   GETB(h);
-  return launch_norm_distance(hb);
+  RET_DEV(hb, launch_norm_distance(hb));
 }
 int bcfd_find_ts_cells(bcfd_handle h) {
   LOCK();
   GETB(h);
-  return launch_find_ts(hb);
+  RET_DEV(hb, launch_find_ts(hb));
 }
 int bcfd_fine_block_cell(void) {
   LOCK();
@@ -1246,17 +1271,17 @@ int bcfd_correct_velocity(bcfd_handle h, double dt) { LOCK(); GETB(h); return la
 int bcfd_redblack_sor_linear(bcfd_handle h, int64_t itmax, double dt, double epsi) {
   LOCK();
   GETB(h);
-  TRY(launch_sor(hb, itmax, dt, epsi));
-  return 0;
+  RET_DEV(hb, launch_sor(hb, itmax, dt, epsi));
 }
 int bcfd_block_sor_sweeps(bcfd_handle h, int64_t n_pairs, int precision) {
   LOCK();
   GETB(h);
-  if (n_pairs < 1 || n_pairs > 1000000 || precision < 0 || precision > 1) return BCFD_E_ARG;
-  if (precision == 0) {
-    // the reference sweeps from iteration 0, stop test disabled (epsi < 0)
+  if (n_pairs < 1 || n_pairs > 1000000 || precision < 0 || precision > 2) return BCFD_E_ARG;
+  if (precision != 1) {
+    // the reference sweeps (0) or the division-free FP64 sweeps (2) from
+    // iteration 0, stop test disabled (epsi < 0)
     BCFD_CUDA(cudaMemsetAsync(&hb->d.stats->niter, 0, sizeof(int64_t), stream()));
-    TRY(launch_sor(hb, n_pairs - 1, 1.0, -1.0));
+    TRY(launch_sor(hb, n_pairs - 1, 1.0, -1.0, 0.0, precision == 2));
   } else {
     // one correction of n_pairs FP32 sweep pairs, stop test disabled
     const int keep = hb->dc_inner;
@@ -1337,8 +1362,16 @@ int bcfd_profile_begin(void) {
   if (!L.prof_dev) BCFD_CUDA(cudaMalloc(&L.prof_dev, (1 + 4 * kProfLogCap) * sizeof(int64_t)));
   BCFD_CUDA(cudaMemsetAsync(L.prof_dev, 0, sizeof(int64_t), stream()));
   L.prof_used = 0;
+  L.phase_used = 0;
   L.prof_on = true;
   L.prof_launch0 = L.launches;
+  return 0;
+}
+
+int bcfd_profile_phases(double* ms, int n) {
+  LOCK();
+  if (!ms || n < 0) return BCFD_E_ARG;
+  for (int q = 0; q < n && q < PH_COUNT; ++q) ms[q] = lib().phase_ms[q];
   return 0;
 }
 
@@ -1346,9 +1379,17 @@ int bcfd_profile_end(bcfd_profile_report* out) {
   LOCK();
   Lib& L = lib();
   if (!L.prof_on || !out) return BCFD_E_STATE;
+  // the window ends at a phase boundary so the last phase is closed
+  phase_mark(PH_COUNT);
   L.prof_on = false;
   BCFD_CUDA(cudaStreamSynchronize(stream()));
   std::memset(out, 0, sizeof(*out));
+  for (double& v : L.phase_ms) v = 0.0;
+  for (size_t q = 0; q + 1 < L.phase_used; ++q) {
+    float ms = 0.f;
+    BCFD_CUDA(cudaEventElapsedTime(&ms, L.phase_events[q], L.phase_events[q + 1]));
+    if (L.phase_ids[q] >= 0 && L.phase_ids[q] < PH_COUNT) L.phase_ms[L.phase_ids[q]] += ms;
+  }
   for (size_t q = 0; q + 1 < L.prof_used; q += 2) {
     float ms = 0.f;
     BCFD_CUDA(cudaEventElapsedTime(&ms, L.prof_events[q], L.prof_events[q + 1]));

@@ -157,6 +157,12 @@ struct Lib {
   std::vector<cudaEvent_t> prof_events;   // begin/end pairs, in order
   size_t prof_used = 0;
   int64_t prof_launch0 = 0;
+  // per-phase split of the window: an event at every phase boundary of an
+  // eagerly issued step, and the summed device time per phase of the last window
+  std::vector<cudaEvent_t> phase_events;
+  std::vector<int> phase_ids;
+  size_t phase_used = 0;
+  double phase_ms[8] = {0};
   // bumped whenever a scratch buffer that captured kernels point at is
   // (re)allocated, so a captured step graph is rebuilt
   uint64_t gen = 0;
@@ -232,11 +238,13 @@ int launch_steady_state(const std::vector<HostBlock*>& hbs, double dt);
 int launch_max_div(const std::vector<HostBlock*>& hbs, bool tfield);
 int launch_copy_t_to_n(const std::vector<HostBlock*>& hbs);
 int launch_momentum(const std::vector<HostBlock*>& hbs, double dt, double re, bool fp32);
-int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double epsi, double res_tol);
+// fast = 1 (residual-target solves only): the division-free FP64 update
+int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double epsi, double res_tol,
+                   int fast = 0);
 bool tb_solve_fits(HostBlock* hb);
 int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double div_tol);
 // res_tol > 0: stop on the FP64 residual dt*max|b/dt - A pc| <= res_tol
-int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol = 0.0);
+int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol = 0.0, int fast = 0);
 int launch_zero_poisson(HostBlock* hb);
 int launch_steady_state(HostBlock* hb, double dt);
 int launch_copy_t_to_n(HostBlock* hb);
@@ -249,6 +257,20 @@ int launch_max_div(HostBlock* hb, bool tfield);
 // events around each persistent solve launch
 int64_t* prof_log();
 void prof_mark(bool begin);
+// phases of a time step for the measurement window's split (bcfd_profile_phases)
+enum StepPhase {
+  PH_MOMENTUM = 0,   // nsMomentum2order and the domain BCs
+  PH_FORCING,        // solid-cell BCs, velocityForcing1, pressureForcing1
+  PH_SOLVE,          // the Poisson solves (incl. their right-hand sides)
+  PH_COUPLING,       // coarse/fine face fills and restrictions
+  PH_CORRECTION,     // zeroing, divergence, corrections, reductions, copies
+  PH_SEARCH,         // body motion, normals, block moves, re-Search and lists
+  PH_FORCING_FIELD,  // forcing on the re-searched geometry (Field, Ghost)
+  PH_COUNT
+};
+// marks the start of phase `ph` on the library stream (no-op outside a
+// measurement window or while a stream capture is running)
+void phase_mark(int ph);
 int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol);
 // k_momentum.cu
 int launch_momentum(HostBlock* hb, double dt, double re, bool fp32);

@@ -148,17 +148,18 @@ struct SolveCfg {
 };
 
 // precision 0: FP64, the reference's stop test (drop-in arithmetic);
-// 1: FP32 SOR + FP64 defect correction to div_tol; 2: FP64 SOR to div_tol
+// 1: FP32 SOR + FP64 defect correction to div_tol; 2: FP64 SOR (reference
+// sweeps) to div_tol; 3: division-free FP64 SOR to div_tol
 int sor(HostBlock* hb, const SolveCfg& c) {
   if (c.precision == 1) return launch_sor_mixed(hb, c.itmax, c.dt, c.div_tol);
-  if (c.precision == 2) return launch_sor(hb, c.itmax, c.dt, c.epsi, c.div_tol);
+  if (c.precision >= 2) return launch_sor(hb, c.itmax, c.dt, c.epsi, c.div_tol, c.precision == 3);
   return launch_sor(hb, c.itmax, c.dt, c.epsi);
 }
 
 // the same dispatch over several blocks (one batched launch when batching)
 int sor_set(const std::vector<HostBlock*>& v, const SolveCfg& c) {
   if (c.precision == 1) return launch_sor_mixed_set(v, c.itmax, c.dt, c.div_tol);
-  if (c.precision == 2) return launch_sor_set(v, c.itmax, c.dt, c.epsi, c.div_tol);
+  if (c.precision >= 2) return launch_sor_set(v, c.itmax, c.dt, c.epsi, c.div_tol, c.precision == 3);
   return launch_sor_set(v, c.itmax, c.dt, c.epsi, 0.0);
 }
 
@@ -176,16 +177,26 @@ int poisson(const SolveCfg& c, int start, int finish, int step) {
       set.push_back(hb);
       (g == 1 ? first : fine).push_back(hb);
     }
+  phase_mark(PH_CORRECTION);
   for (HostBlock* hb : set) TRY(launch_zero_poisson(hb));
+  phase_mark(PH_COUPLING);
   TRY(fine_update_newv_bd());
   TRY(coarse_update_newv());
+  phase_mark(PH_CORRECTION);
   TRY(launch_compute_div(set));
+  phase_mark(PH_SOLVE);
   TRY(sor_set(fine, c));
+  phase_mark(PH_COUPLING);
   TRY(coarse_update_pc());
+  phase_mark(PH_SOLVE);
   TRY(sor_set(first, c));
+  phase_mark(PH_COUPLING);
   TRY(fine_update_pc_bd());
+  phase_mark(PH_SOLVE);
   TRY(sor_set(fine, c));
+  phase_mark(PH_COUPLING);
   TRY(coarse_update_pc());
+  phase_mark(PH_CORRECTION);
   TRY(launch_correct_pressure(set));
   TRY(launch_correct_velocity(set, c.dt));
   // the divergence the solve leaves behind (measurement, not in the reference)
@@ -193,6 +204,7 @@ int poisson(const SolveCfg& c, int start, int finish, int step) {
   for (HostBlock* hb : first) TRY(launch_velocity_bc(hb, c.dt, c.uc));
   TRY(launch_steady_state(set, c.dt));
   TRY(launch_copy_t_to_n(set));
+  phase_mark(PH_COUPLING);
   for (HostInterface* it : lib().ifs)
     if (it && get_block(it->b)) TRY(fine_update_bd_mv(it));
   TRY(coarse_update());
@@ -399,18 +411,28 @@ int step_body(const bcfd_step_config& cfg) {
   std::vector<HostBlock*> every;
   for (auto& [g, hb] : all) every.push_back(hb);
   // nsMomentum2order of every block in one launch (blocks are independent)
+  phase_mark(PH_MOMENTUM);
   TRY(launch_momentum(every, cfg.deltat, cfg.re, cfg.precision == 1));
   for (auto& [g, hb] : all) {
-    if (hb->is_coarse) TRY(launch_velocity_bc(hb, cfg.deltat, cfg.uc));
+    if (hb->is_coarse) {
+      phase_mark(PH_MOMENTUM);
+      TRY(launch_velocity_bc(hb, cfg.deltat, cfg.uc));
+    }
     if (hb->has_body) {
+      phase_mark(PH_FORCING);
       TRY(launch_solid_bc(hb, false));
       TRY(launch_forcing_velocity(hb, 0));
     }
-    if (hb->is_coarse) TRY(launch_velocity_bc(hb, cfg.deltat, cfg.uc));
+    if (hb->is_coarse) {
+      phase_mark(PH_MOMENTUM);
+      TRY(launch_velocity_bc(hb, cfg.deltat, cfg.uc));
+    }
   }
   TRY(poisson(c, 1, (int)lib().blocks.size(), 1));
+  phase_mark(PH_FORCING);
   for (auto& [g, hb] : all)
     if (hb->has_body) TRY(launch_forcing_pressure(hb, 0));
+  phase_mark(PH_SEARCH);
   // moving bodies (app/main.F90:169-176, 213-215): the staged kinematics
   // take effect and the nodes move
   bool moving = false;
@@ -451,10 +473,12 @@ int step_body(const bcfd_step_config& cfg) {
     hb->move_check = 0;
     TRY(launch_norm_distance(hb));
     TRY(launch_find_ts(hb));
+    phase_mark(PH_FORCING_FIELD);
     TRY(launch_forcing_velocity(hb, 1));
     TRY(launch_forcing_pressure(hb, 1));
     TRY(launch_forcing_velocity(hb, 2));
     TRY(launch_forcing_pressure(hb, 2));
+    phase_mark(PH_SEARCH);
   }
   return 0;
 }
@@ -714,7 +738,8 @@ int bcfd_tagging_th_move(bcfd_handle h) {
 
 int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps) {
   LOCK();
-  if (!cfg || n_steps < 0) return BCFD_E_ARG;
+  if (!cfg || n_steps < 0 || cfg->precision < 0 || cfg->precision > 3) return BCFD_E_ARG;
+  if (cfg->precision >= 1 && !(cfg->div_tol > 0.0)) return BCFD_E_ARG;
   if (cfg->use_graph && !lib().prof_on) {
     TRY(run_steps_graph(*cfg, n_steps));
   } else {

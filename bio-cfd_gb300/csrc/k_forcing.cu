@@ -512,7 +512,9 @@ int launch_forcing_adjoint(HostBlock* hb, int mode, int vel, const AdjPtrs& a, c
 static DagScratch& dag_scratch(HostBlock* hb, int* status) {
   *status = 0;
   if (!hb->dag_scratch) {
-    const int64_t need = 6 * (int64_t)hb->d.cap_ib;
+    // sized for the allocated list capacity, so a cap lowered and raised
+    // again (bcfd_block_set_list_capacity) never outgrows it
+    const int64_t need = 6 * (int64_t)hb->cap_ib_alloc;
     DagScratch* s = new DagScratch{};
     if (cudaMalloc(&s->out, need * sizeof(double)) != cudaSuccess ||
         cudaMalloc(&s->dep, need * 8 * sizeof(int)) != cudaSuccess ||

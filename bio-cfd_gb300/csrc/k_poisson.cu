@@ -201,8 +201,41 @@ __device__ __forceinline__ double sor64_cell(const DevBlock& B, const Pos& p, do
 // One half-sweep of colour C over the tile, FP64, reference arithmetic; one
 // cell per pass (the FP64 sweep is bound by the FP64 divide, and the lower
 // register count keeps two CTAs of 512 threads per SM)
+// SOR update of one FP64 cell without a division, for solves that stop on
+// the FP64 residual (precision 3): r = b/dt - A_offdiag pc by fused
+// multiply-adds, then x + omega r / d.  1/d is an FP32 reciprocal refined by
+// one Newton-Raphson step in FP64 (y1 = y0 + y0 (1 - d y0)), accurate to a
+// few FP64 ulps; the iteration's fixed point A x = b does not depend on it.
 template <int C>
-__device__ __forceinline__ void tile_half64(const DevBlock& B, const Tile& t, double omega, double& lmax) {
+__device__ __forceinline__ double sor64f_cell(const DevBlock& B, const Pos& p, double omega, double& old) {
+  const Dims& d = B.d;
+  const double* __restrict__ o = B.pc[1 - C];
+  const int64_t sy = d.NXH, sz = (int64_t)d.NXH * d.NY;
+  const int i = p.ic, j = p.j, k = p.k, nx = d.nx, ny = d.ny, nz = d.nz;
+  const double pl = __ldcg(o + p.row + ((p.i - 2) >> 1));
+  const double pr = __ldcg(o + p.row + (p.i >> 1));
+  const double ps = __ldcg(o + p.pi - sy), pn = __ldcg(o + p.pi + sy);
+  const double pb = __ldcg(o + p.pi - sz), pt = __ldcg(o + p.pi + sz);
+  old = __ldcg(B.pc[C] + p.pi);
+  const double ax1 = B.Acx[i - 2], ax2 = B.Acx[i - 2 + nx], ax3 = B.Acx[i - 2 + 2 * nx];
+  const double ay1 = B.Acy[j - 2], ay2 = B.Acy[j - 2 + ny], ay3 = B.Acy[j - 2 + 2 * ny];
+  const double az1 = B.Acz[k - 2], az2 = B.Acz[k - 2 + nz], az3 = B.Acz[k - 2 + 2 * nz];
+  const double dg = ax2 + ay2 + az2;
+  double r = fma(-dg, old, B.rhs[C][p.pi]);
+  r = fma(-ax1, pl, r);
+  r = fma(-ax3, pr, r);
+  r = fma(-ay1, ps, r);
+  r = fma(-ay3, pn, r);
+  r = fma(-az1, pb, r);
+  r = fma(-az3, pt, r);
+  const double y0 = (double)__frcp_rn((float)dg);
+  const double y1 = fma(y0, fma(-dg, y0, 1.0), y0);
+  return fma(omega * y1, r, old);
+}
+
+template <int C>
+__device__ __forceinline__ void tile_half64(const DevBlock& B, const Tile& t, double omega, double& lmax,
+                                            int fast) {
   double* __restrict__ own = B.pc[C];
   const int n = B.d.NXH * t.nj * t.nk;
   Walk3 w;
@@ -211,7 +244,7 @@ __device__ __forceinline__ void tile_half64(const DevBlock& B, const Tile& t, do
     const Pos p = tile_pos<C>(B, t, w, true);
     if (!p.on) continue;
     double old;
-    const double nv = sor64_cell<C>(B, p, omega, old);
+    const double nv = fast ? sor64f_cell<C>(B, p, omega, old) : sor64_cell<C>(B, p, omega, old);
     own[p.pi] = nv;
     lmax = nmax(lmax, fabs(nv - old));
   }
@@ -293,6 +326,7 @@ struct SorArgs {
                   // the reference's increment test (same check cadence)
   double dt;
   int rev;        // 1: black half-sweep first (the adjoint solve's order)
+  int fast;       // 1: division-free update (not the reference's arithmetic)
 };
 
 // append {sweep pairs, FP64 residual passes, fluid cells, precision}
@@ -343,12 +377,12 @@ __device__ __forceinline__ void sor64_body(const DevBlock& B, const SorArgs& a, 
     if (++r5 == 5) r5 = 0;
     double lmax = 0.0;
     if (!tile_wait(tm, gb, t, ph)) { ok = false; break; }
-    if (a.rev) tile_half64<0>(B, t, a.omega, lmax);
-    else tile_half64<1>(B, t, a.omega, lmax);
+    if (a.rev) tile_half64<0>(B, t, a.omega, lmax, a.fast);
+    else tile_half64<1>(B, t, a.omega, lmax, a.fast);
     tile_publish(tm, t, ++ph);
     if (!tile_wait(tm, gb, t, ph)) { ok = false; break; }
-    if (a.rev) tile_half64<1>(B, t, a.omega, lmax);
-    else tile_half64<0>(B, t, a.omega, lmax);
+    if (a.rev) tile_half64<1>(B, t, a.omega, lmax, a.fast);
+    else tile_half64<0>(B, t, a.omega, lmax, a.fast);
     tile_publish(tm, t, ++ph);
     if (r5 == 0) {
       if (a.res_tol > 0.0) {
@@ -1111,7 +1145,7 @@ static int reset_solve_state(HostBlock* hb, const TileMap& tm) {
   return 0;
 }
 
-int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol) {
+int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol, int fast) {
   DevBlock& B = hb->d;
   const int64_t np = B.d.npacked();
   k_rhs<<<grid_for(np, 256), 256, 0, stream()>>>(B, dt);
@@ -1120,7 +1154,7 @@ int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_
   TileMap tm = choose_tiles(hb, (const void*)k_sor64, threads, hb->solve_sync == 1 ? 1 : 0, hb->solve_ctas_per_sm);
   TRY_R(reset_solve_state(hb, tm));
   const unsigned grid = (unsigned)(tm.ntj * tm.ntk);
-  SorArgs a{itmax, epsi, hb->omega, prof_log(), res_tol, dt, hb->sor_rev};
+  SorArgs a{itmax, epsi, hb->omega, prof_log(), res_tol, dt, hb->sor_rev, fast};
   GridBar gb = make_bar(B.err, grid);
   gb.ctr = reinterpret_cast<unsigned long long*>(hb->bar);
   void* args[] = {(void*)&B, (void*)&a, (void*)&gb, (void*)&tm};
@@ -1294,9 +1328,10 @@ static int launch_solve_set(const std::vector<HostBlock*>& hbs, const void* fn, 
   return 0;
 }
 
-int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double epsi, double res_tol) {
+int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double epsi, double res_tol,
+                   int fast) {
   if (hbs.size() <= 1 || !lib().batch) {
-    for (HostBlock* hb : hbs) TRY_R(launch_sor(hb, itmax, dt, epsi, res_tol));
+    for (HostBlock* hb : hbs) TRY_R(launch_sor(hb, itmax, dt, epsi, res_tol, fast));
     return 0;
   }
   const int threads = 512;
@@ -1305,12 +1340,12 @@ int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt,
     BCFD_LAUNCHED();
   }
   auto make = [&](HostBlock* hb, SorArgs& a) -> int {
-    a = SorArgs{itmax, epsi, hb->omega, prof_log(), res_tol, dt, hb->sor_rev};
+    a = SorArgs{itmax, epsi, hb->omega, prof_log(), res_tol, dt, hb->sor_rev, fast};
     // blocks with their own launch shape keep their own launch
     return hb->solve_threads > 0 || hb->solve_sync != 0 || hb->solve_ctas_per_sm > 0;
   };
   // a block solved alone goes through launch_sor (which recomputes b/dt)
-  auto solo = [&](HostBlock* hb) -> int { return launch_sor(hb, itmax, dt, epsi, res_tol); };
+  auto solo = [&](HostBlock* hb) -> int { return launch_sor(hb, itmax, dt, epsi, res_tol, fast); };
   TRY_R(launch_solve_set<SorArgs>(hbs, (const void*)k_sor64_set, threads, 0, make, solo));
   for (HostBlock* hb : hbs) TRY_R(launch_residual(hb, dt));
   return 0;

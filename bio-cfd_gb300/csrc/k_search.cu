@@ -330,7 +330,8 @@ __global__ void k_solid_box(DevBlock B) {
 
 // selectiveRetagging_th step 1: clear the IB cells
 __global__ void k_clear_ib(DevBlock B) {
-  const int nib = (int)B.cnt[C_IB];
+  // a count beyond the capacity (BCFD_E_CAPACITY recorded) reads no further
+  const int nib = (int)min(B.cnt[C_IB], (int64_t)B.cap_ib);
   for (int n = blockIdx.x * blockDim.x + threadIdx.x; n < nib; n += gridDim.x * blockDim.x)
     B.cell[B.d.idx(B.ib_i[n], B.ib_j[n], B.ib_k[n])] = 0;
 }
@@ -338,7 +339,7 @@ __global__ void k_clear_ib(DevBlock B) {
 // mark the 27-neighbourhoods of the IB cells (the union is what the
 // reference re-tags; every cell of it gets the same values from any visit)
 __global__ void k_mark_nbhd(DevBlock B, uint8_t* mark) {
-  const int nib = (int)B.cnt[C_IB];
+  const int nib = (int)min(B.cnt[C_IB], (int64_t)B.cap_ib);
   const int64_t n = (int64_t)nib * 27;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n;
        t += (int64_t)gridDim.x * blockDim.x) {

@@ -289,9 +289,12 @@ typedef struct bcfd_step_config {
   int64_t pc_ita_max;  /* SOR iteration cap                                    */
   int precision;       /* 0: FP64 reference arithmetic and stop test (drop-in);
                           1: FP32 SOR + FP64 defect correction to div_tol;
-                          2: FP64 SOR (reference sweeps) to div_tol            */
-  double div_tol;      /* precision 1/2: target FP64 Poisson residual in
-                          divergence units, deltat * max|b/deltat - A pc|      */
+                          2: FP64 SOR (reference sweeps) to div_tol;
+                          3: FP64 SOR without divisions (fused residual, the
+                             inverse diagonal by Newton-Raphson) to div_tol   */
+  double div_tol;      /* precision 1-3: target FP64 Poisson residual in
+                          divergence units, deltat * max|b/deltat - A pc|;
+                          must be > 0 (BCFD_E_ARG otherwise)                   */
   int use_graph;       /* capture the step in a CUDA graph and replay it       */
 } bcfd_step_config;
 
@@ -368,7 +371,8 @@ int bcfd_autotune(int64_t* n_tuned);
 /* measurement: exactly n_pairs red-black sweep pairs of the block's Poisson
  * system b = the current computeDiv result (deltat = 1), stop test disabled.
  * precision 0: the FP64 reference sweeps on pc; 1: one FP32 correction of
- * n_pairs sweeps (with its two FP64 residual passes and the FP64 update).
+ * n_pairs sweeps (with its two FP64 residual passes and the FP64 update);
+ * 2: the division-free FP64 sweeps of bcfd_step_config precision 3.
  * Changes pc; for timing and roofline measurement only. */
 int bcfd_block_sor_sweeps(bcfd_handle h, int64_t n_pairs, int precision);
 
@@ -384,6 +388,20 @@ typedef struct bcfd_profile_report {
 } bcfd_profile_report;
 int bcfd_profile_begin(void);
 int bcfd_profile_end(bcfd_profile_report* out);
+/* Device time (ms) per phase of the time steps issued eagerly (use_graph 0)
+ * inside the last measurement window, summed over the window's steps:
+ * ms[0] nsMomentum2order and the domain BCs, [1] solid-cell BCs,
+ * velocityForcing1 and pressureForcing1, [2] the Poisson solves, [3] the
+ * coarse/fine face fills and restrictions, [4] zeroing, divergence,
+ * pressure and velocity corrections, reductions and copies, [5] body motion,
+ * normals, fine-block moves, re-Search and index lists, [6] the forcing on
+ * the re-searched geometry (Field and Ghost variants).  n <= 7 entries. */
+int bcfd_profile_phases(double* ms, int n);
+/* Measured arithmetic rates of this GPU (no counterpart in the reference):
+ * out[0] FP64 fused multiply-add GFLOP/s (2 per FMA), out[1] FP64 IEEE
+ * divisions in G/s, out[2] FP32 fused multiply-add GFLOP/s; chains of
+ * independent operations on every SM, best of three CUDA-event timings. */
+int bcfd_measure_alu_rates(double* out);
 
 #ifdef __cplusplus
 }

@@ -35,6 +35,8 @@ def lib(checked: bool = True) -> C.CDLL:
         L.orc_get_i.restype = _i64
         L.orc_get_i.argtypes = [_i64, C.c_char_p]
         L.orc_err.argtypes = [_i64]
+        L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_get_threads.restype = C.c_int
         L.orc_interface_new.restype = _i64
         L.orc_interface_new.argtypes = [_i64, _i64, _i64, _i64] + [_f64] * 6
         L.orc_interface_table.restype = C.POINTER(_i64)

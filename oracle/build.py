@@ -1,9 +1,10 @@
 """Build recipe for the CPU oracle (test infrastructure only).
 
-Compiles the serial FP64 restatement in this directory into
+Compiles the FP64 restatement in this directory into
 ``oracle/build/liborc.so`` with ``-ffp-contract=off`` so that every
 expression rounds exactly as written (no fused multiply-adds), which is the
-arithmetic of the reference's serial CPU build.
+arithmetic of the reference's serial CPU build.  Loops whose result does not
+depend on their order run under OpenMP; the results equal the serial ones.
 
 The reference itself (Fortran 2008 + OpenACC) cannot be compiled in this
 environment -- no Fortran compiler exists on either machine -- so there is
@@ -34,7 +35,10 @@ def build(checked: bool = True, force: bool = False) -> Path:
     out.parent.mkdir(parents=True, exist_ok=True)
     objdir = out.parent / ("obj" if checked else "obj_fast")
     objdir.mkdir(exist_ok=True)
-    flags = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall"]
+    # OpenMP: the order-independent loops (sweeps of one colour, per-cell
+    # stencils without thin-surface cells, per-cell searches, maxima) run on
+    # all host cores with the serial loops' results
+    flags = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-fopenmp"]
     if not checked:
         flags.append("-DORC_NOCHECK")
     procs, objs = [], []
@@ -45,7 +49,7 @@ def build(checked: bool = True, force: bool = False) -> Path:
     if any(p.wait() != 0 for p in procs):
         raise RuntimeError("oracle compile failed")
     tmp = out.with_suffix(".so.tmp%d" % os.getpid())
-    subprocess.check_call(["g++", "-shared", "-o", str(tmp), *map(str, objs)])
+    subprocess.check_call(["g++", "-shared", "-fopenmp", "-o", str(tmp), *map(str, objs)])
     os.replace(tmp, out)
     return out
 

@@ -3,6 +3,8 @@
 // ctypes.  Arrays are exposed in place (column-major, the Fortran layout).
 #include <cstring>
 #include <string>
+#include <omp.h>
+
 #include "orc_core.h"
 
 using namespace orc;
@@ -152,6 +154,9 @@ double orc_bilinear_interpolation(double x, double y, double x1, double x2, doub
 }
 
 int orc_err(int64_t g) { return blk_of(g).err; }
+// threads of the OpenMP loops (1 = the serial loops)
+void orc_set_threads(int n) { omp_set_num_threads(n < 1 ? 1 : n); }
+int orc_get_threads(void) { return omp_get_max_threads(); }
 void orc_clear_err(int64_t g) { blk_of(g).err = 0; }
 
 void orc_derive_grids(int64_t g) { derive_grids(blk_of(g)); }

@@ -282,12 +282,16 @@ static bool check_adjacent(const I3& c, int64_t i, int64_t j, int64_t k, int64_t
 // nsMomentum2order, src/NavierStokes.f90:252-912.  Serial loop over the
 // fluid list in list order, including the in-place ghost substitution for
 // cells next to a thin-surface (TS) cell and the restore with the t-ghosts
-// of the last TS index.
+// of the last TS index.  Without TS cells (cell2 /= 2 everywhere) no cell
+// writes u, v, w or p and each writes only its own ut, vt, wt, so the loop
+// then runs in parallel (OpenMP) with the serial loop's results.
 void ns_momentum_2order(Block& b, double deltat, double re) {
   const double alpha = 1.0;
   const int64_t nx_var = b.nx, ny_var = b.ny, nz_var = b.nz;
   F3 &u = b.u, &v = b.v, &w = b.w, &p = b.p;
   I3& c2 = b.cell2;
+  const bool no_ts = b.TSCellCount == 0;
+#pragma omp parallel for schedule(dynamic, 4096) if (no_ts)
   for (int64_t n = 1; n <= b.fluidCellCount; ++n) {
     const int64_t i = b.fluidIndexPtr(n, 1), j = b.fluidIndexPtr(n, 2), k = b.fluidIndexPtr(n, 3);
     int64_t index_ip1 = 0, index_im1 = 0, index_jp1 = 0, index_jm1 = 0, index_kp1 = 0,

@@ -7,6 +7,7 @@ namespace orc {
 
 // computeDiv, src/PcorVcor.F90:222-243
 void compute_div(Block& b) {
+#pragma omp parallel for schedule(static)
   for (int64_t n = 1; n <= b.fluidCellCount; ++n) {
     const int64_t i = b.fluidIndexPtr(n, 1), j = b.fluidIndexPtr(n, 2), k = b.fluidIndexPtr(n, 3);
     b.b(i, j, k) = (b.ut(i, j, k) - b.ut(i - 1, j, k)) / b.deltax(i) +
@@ -17,6 +18,7 @@ void compute_div(Block& b) {
 
 // correctPressure, src/PcorVcor.F90:245-259
 void correct_pressure(Block& b) {
+#pragma omp parallel for schedule(static)
   for (int64_t n = 1; n <= b.fluidCellCount; ++n) {
     const int64_t i = b.fluidIndexPtr(n, 1), j = b.fluidIndexPtr(n, 2), k = b.fluidIndexPtr(n, 3);
     b.p(i, j, k) = b.p(i, j, k) + b.pc(i, j, k);
@@ -25,6 +27,7 @@ void correct_pressure(Block& b) {
 
 // correctVelocity, src/PcorVcor.F90:261-286
 void correct_velocity(Block& b, double deltat) {
+#pragma omp parallel for schedule(static)
   for (int64_t n = 1; n <= b.fluidCellCount; ++n) {
     const int64_t i = b.fluidIndexPtr(n, 1), j = b.fluidIndexPtr(n, 2), k = b.fluidIndexPtr(n, 3);
     b.ut(i, j, k) = b.ut(i, j, k) - deltat / (0.5 * (b.deltax(i + 1) + b.deltax(i))) *
@@ -39,13 +42,17 @@ void correct_velocity(Block& b, double deltat) {
 // REDBLACKSOR_linear, src/PcorVcor.F90:288-377.  The red sweep reads the old
 // iterate pco, the black sweep the updated pc; every 5th iteration the max
 // increment over the fluid cells is the stop test; pco <- pc after each sweep
-// pair.
+// pair.  Within one sweep every update reads only values that sweep does not
+// write (the other colour, pco, b), and a maximum does not depend on the
+// order of its operands, so the loops run in parallel (OpenMP) with results
+// identical to the serial order.
 void redblack_sor_linear(Block& b, int64_t pcItaMax, double deltat, double epsi) {
   const double omega = b.omega;
   double derr4 = 11111.0;
   b.derr2 = 0.0;
   for (;;) {
     b.nIterPcor = b.nIterPcor + 1;
+#pragma omp parallel for schedule(static)
     for (int64_t n = 1; n <= b.redCellCount; ++n) {
       const int64_t i = b.redCellIndexPtr(n, 1), j = b.redCellIndexPtr(n, 2),
                     k = b.redCellIndexPtr(n, 3);
@@ -57,6 +64,7 @@ void redblack_sor_linear(Block& b, int64_t pcItaMax, double deltat, double epsi)
       b.pc(i, j, k) = v;
       b.pc(i, j, k) = (1.0 - omega) * b.pco(i, j, k) + omega * b.pc(i, j, k);
     }
+#pragma omp parallel for schedule(static)
     for (int64_t n = 1; n <= b.blackCellCount; ++n) {
       const int64_t i = b.blackCellIndexPtr(n, 1), j = b.blackCellIndexPtr(n, 2),
                     k = b.blackCellIndexPtr(n, 3);
@@ -69,15 +77,23 @@ void redblack_sor_linear(Block& b, int64_t pcItaMax, double deltat, double epsi)
       b.pc(i, j, k) = (1.0 - omega) * b.pco(i, j, k) + omega * b.pc(i, j, k);
     }
     if (b.nIterPcor % 5 == 0) {
-      derr4 = 0.0;
+      double m = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : m)
       for (int64_t n = 1; n <= b.fluidCellCount; ++n) {
         const int64_t i = b.fluidIndexPtr(n, 1), j = b.fluidIndexPtr(n, 2),
                       k = b.fluidIndexPtr(n, 3);
         const double var = std::fabs(b.pc(i, j, k) - b.pco(i, j, k));
-        derr4 = std::fmax(derr4, var);
+        m = std::fmax(m, var);
       }
+      derr4 = m;
     }
-    b.pco.d = b.pc.d;
+    {
+      const size_t nd = b.pc.d.size();
+      const double* src = b.pc.d.data();
+      double* dst = b.pco.d.data();
+#pragma omp parallel for schedule(static)
+      for (size_t q = 0; q < nd; ++q) dst[q] = src[q];
+    }
     b.derr2 = derr4;
     if (derr4 < epsi || b.nIterPcor > pcItaMax) break;
   }
@@ -127,6 +143,7 @@ void poisson_solver(int64_t pcItaMax, double epsi, double deltat, double uc, int
   for (int64_t g = start; g <= finish; g += step) {
     Block& b = blk_of(g);
     double err_ds = 0.0;
+#pragma omp parallel for schedule(static) reduction(max : err_ds)
     for (int64_t n = 1; n <= b.fluidCellCount; ++n) {
       const int64_t i = b.fluidIndexPtr(n, 1), j = b.fluidIndexPtr(n, 2), k = b.fluidIndexPtr(n, 3);
       const double eu = std::fabs((b.ut(i, j, k) - b.u(i, j, k))) / deltat;

@@ -2,6 +2,8 @@
 // Marker-to-cell Search of src/Search.F90, restated serially.  The serial
 // CPU build fills every index list in (k,j,i) order; the oracle does the same.
 #include <cmath>
+#include <vector>
+
 #include "orc_core.h"
 
 namespace orc {
@@ -85,6 +87,8 @@ void tagging_th_core(Block& b) {
   b.cell.fill(0);
   b.cell2.fill(0);
   b.nodeIdTag.fill(0);
+  // each cell's tags depend only on the geometry: parallel over planes
+#pragma omp parallel for schedule(dynamic, 1)
   for (int64_t k = b.k_startSearch; k <= b.k_endSearch; ++k)
     for (int64_t j = b.j_startSearch; j <= b.j_endSearch; ++j)
       for (int64_t i = b.i_startSearch; i <= b.i_endSearch; ++i) tag_cell(b, i, j, k);
@@ -101,19 +105,39 @@ void selective_retagging_th(Block& b) {
   for (int64_t nn = 1; nn <= b.ibCellCount; ++nn)
     b.cell(b.interceptedIndexPtr(nn, 1), b.interceptedIndexPtr(nn, 2),
            b.interceptedIndexPtr(nn, 3)) = 0;
-  for (int64_t nn = 1; nn <= b.ibCellCount; ++nn)
-    for (int64_t kp = -1; kp <= 1; ++kp)
-      for (int64_t jp = -1; jp <= 1; ++jp)
-        for (int64_t ip = -1; ip <= 1; ++ip)
-          tag_cell(b, b.interceptedIndexPtr(nn, 1) + ip, b.interceptedIndexPtr(nn, 2) + jp,
-                   b.interceptedIndexPtr(nn, 3) + kp);
-  for (int64_t nn = 1; nn <= b.ibCellCount; ++nn) {
-    const int64_t i1 = b.interceptedIndexPtr(nn, 1), j1 = b.interceptedIndexPtr(nn, 2),
-                  k1 = b.interceptedIndexPtr(nn, 3);
-    for (int64_t k = k1 - 1; k <= k1 + 1; ++k)
-      for (int64_t j = j1 - 1; j <= j1 + 1; ++j)
-        for (int64_t i = i1 - 1; i <= i1 + 1; ++i)
-          if (b.cell(i, j, k) != 2) b.cell(i, j, k) = corner_sum(b, i, j, k) == 8 ? 1 : 0;
+  // The neighbourhoods of IB cells overlap; a cell's new tags depend only on
+  // the geometry and (in the second pass) on its own tag and the node tags of
+  // the first pass, so visiting each cell once, in parallel, gives the serial
+  // loops' result.
+  std::vector<int64_t> cells;
+  {
+    std::vector<uint8_t> seen((size_t)(b.nx + 2) * (b.ny + 2) * (b.nz + 2), 0);
+    for (int64_t nn = 1; nn <= b.ibCellCount; ++nn)
+      for (int64_t kp = -1; kp <= 1; ++kp)
+        for (int64_t jp = -1; jp <= 1; ++jp)
+          for (int64_t ip = -1; ip <= 1; ++ip) {
+            const int64_t i = b.interceptedIndexPtr(nn, 1) + ip, j = b.interceptedIndexPtr(nn, 2) + jp,
+                          k = b.interceptedIndexPtr(nn, 3) + kp;
+            const size_t q = (size_t)((i - 1) + (b.nx + 2) * ((j - 1) + (b.ny + 2) * (k - 1)));
+            ORC_CHECK(i >= 1 && i <= b.nx + 2 && j >= 1 && j <= b.ny + 2 && k >= 1 && k <= b.nz + 2,
+                      "retag neighbourhood");
+            if (!seen[q]) {
+              seen[q] = 1;
+              cells.push_back((int64_t)q);
+            }
+          }
+  }
+  const int64_t nc = (int64_t)cells.size(), sx = b.nx + 2, sy = b.ny + 2;
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int64_t c = 0; c < nc; ++c) {
+    const int64_t q = cells[(size_t)c];
+    tag_cell(b, 1 + q % sx, 1 + (q / sx) % sy, 1 + q / (sx * sy));
+  }
+#pragma omp parallel for schedule(static)
+  for (int64_t c = 0; c < nc; ++c) {
+    const int64_t q = cells[(size_t)c];
+    const int64_t i = 1 + q % sx, j = 1 + (q / sx) % sy, k = 1 + q / (sx * sy);
+    if (b.cell(i, j, k) != 2) b.cell(i, j, k) = corner_sum(b, i, j, k) == 8 ? 1 : 0;
   }
   count_cells(b);
 }
@@ -213,6 +237,7 @@ void compute_norm_distance(Block& b) {
                 &b.w1NormDis, &b.w2NormDis})
     a->alloc(nib);
   for (I1* a : {&b.nelp, &b.nelu1, &b.nelu2, &b.nelv1, &b.nelv2, &b.nelw1, &b.nelw2}) a->alloc(nib);
+#pragma omp parallel for schedule(dynamic, 16)
   for (int64_t k = 1; k <= nib; ++k) {
     const int64_t ci = b.interceptedIndexPtr(k, 1), cj = b.interceptedIndexPtr(k, 2),
                   ck = b.interceptedIndexPtr(k, 3);

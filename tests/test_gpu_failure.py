@@ -101,11 +101,15 @@ def test_ib_list_over_capacity_is_reported():
         nib = s.counts(g)["ibCellCount"]
         assert nib > 16
         check(s.L.bcfd_block_set_list_capacity(g, 16), "set_list_capacity")
-        assert s.L.bcfd_tagging_th(g) == 0  # tags hold no list
+        # the routine called alone, and a whole step, report the overflow
         assert s.L.bcfd_cellcount_solid(g) == BCFD_E_CAPACITY
+        assert _status(s) == BCFD_E_CAPACITY
+        # with the capacity back the lists are rebuilt whole
         check(s.L.bcfd_block_set_list_capacity(g, 0), "set_list_capacity")
+        assert s.L.bcfd_tagging_th(g) == 0
         assert s.L.bcfd_cellcount_solid(g) == 0
         assert s.counts(g)["ibCellCount"] == nib
+        assert _status(s) == 0
     finally:
         s.close()
 

@@ -56,7 +56,7 @@ WORKLOAD = ("tandem flapping plates, 44.0M cells: coarse 384x256x256 over 6x4x4 
 # block twice).  Measured with the GPU drop-in path, whose iteration counts
 # equal the oracle's bit for bit; the CPU reference arm multiplies its
 # measured cost per sweep pair by these counts.
-REFERENCE_SWEEP_PAIRS = None  # filled from a measurement (see `dropin_sweep_pairs`)
+REFERENCE_SWEEP_PAIRS = (1400, 2645, 2560)  # coarse, fine 1, fine 2 (bench.py --dropin-steps 1)
 
 
 def peaks():
@@ -572,6 +572,40 @@ def adjoint_bench(torch, local, steps=4, every=2):
     return out
 
 
+def profile_run(args):
+    """A short run for profiler captures: the chosen workload set up without
+    the autotuner, then `--profile-steps` eagerly issued steps of the mixed
+    path (one kernel launch per phase and block, as a replayed graph holds
+    them); prints the per-step time and the phase split of the last step."""
+    import torch
+    from biocfd import synth
+    torch.cuda.set_device(0)
+    if args.profile_case == "tandem":
+        case = synth.tandem_plates(n_steps=args.profile_steps + 2, moving=True)
+    else:  # one 256x192x192 block with a plate: the fine-block size, ~1 GB on the device
+        case = synth.plate_block(n=(256, 192, 192), n_steps=args.profile_steps + 2)
+    s = new_solver(case, 0, tune=False)
+    stream = torch.cuda.ExternalStream(s.stream_ptr())
+    ts = []
+    for q in range(args.profile_steps):
+        last = q == args.profile_steps - 1
+        if last:
+            s.profile_begin()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        s.run(1, precision=1, div_tol=DIV_TOL)
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1))
+        if last:
+            prof = s.profile_end()
+    print(json.dumps({"profile_case": args.profile_case, "ms_per_step": ts, "phases_ms": s.profile_phases(),
+                      "kernel_launches_last_step": prof["kernel_launches"],
+                      "counts": [s.counts(g) for g in s.handles]}), flush=True)
+    s.close()
+
+
 def run_gpu(args):
     import torch
 
@@ -652,6 +686,9 @@ def main():
     ap.add_argument("--twelve-only", action="store_true", help="only the twelve-block measurement")
     ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint timing")
     ap.add_argument("--alu-only", action="store_true", help="only the arithmetic-rate measurement")
+    ap.add_argument("--profile-steps", type=int, default=0,
+                    help="profiler mode: set up without the autotuner and run this many eager mixed steps")
+    ap.add_argument("--profile-case", default="tandem", choices=["tandem", "block256"])
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -674,6 +711,9 @@ def main():
         return
     if args.alu_only:
         print(json.dumps(alu_rates(0)), flush=True)
+        return
+    if args.profile_steps > 0:
+        profile_run(args)
         return
     if args.impl == "reference":
         run_reference(args)

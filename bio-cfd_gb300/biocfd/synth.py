@@ -447,6 +447,26 @@ def tandem_plates(n_steps: int = 2, seed: int = SEED, moving: bool = False, lag_
                        lags_deg=(0.0, lag_deg) if moving else None)
 
 
+def plate_block(n=(256, 192, 192), n_steps: int = 2, seed: int = SEED) -> Case:
+    """One block of the tandem plates' fine-block size (dx 1/128) with the
+    domain BCs and a stationary plate of semi-axes 0.5 x 0.125 x 0.0125 at its
+    centre, Re = 1000 on the chord: the momentum stencil, forcing and Search
+    of the large workload on ~1 GB of device memory (profiler captures)."""
+    nx, ny, nz = n
+    L = (nx / 128.0, ny / 128.0, nz / 128.0)
+    spec = BlockSpec(nx, ny, nz, uniform_faces(0, L[0], nx), uniform_faces(0, L[1], ny),
+                     uniform_faces(0, L[2], nz), omega=1.7, is_coarse=True)
+    c = np.array([0.5 * L[0], 0.5 * L[1], 0.5 * L[2]])
+    ax = np.array([0.5, 0.125, 0.0125])
+    dx = 1.0 / 128.0
+    spec.mesh = ellipsoid_plate(c, ax, 0.5 * dx)
+    spec.search_box = search_box_for(spec, c - ax, c + ax)
+    case = Case(name=f"plate_block{nx}", blocks=[spec], dt=0.3 * dx, re=1000.0, uc=1.0, epsi=1e-6,
+                pc_ita_max=5000, n_steps=n_steps)
+    case.init = [noisy_initial(spec, case.uc, np.random.default_rng(seed))]
+    return case
+
+
 def uniform_block(n=(384, 256, 256), lengths=(3.0, 2.0, 2.0), seed: int = SEED,
                   noise: bool = True) -> Case:
     """One body-free uniform block with the domain BCs (384x256x256 is the

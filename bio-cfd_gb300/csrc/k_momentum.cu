@@ -37,10 +37,31 @@ __device__ __forceinline__ bool adj_ok(const int8_t* c, const Dims& d, bool big,
   return true;
 }
 
-// a grid / coefficient value as T: the FP32 copy for T = float, else the FP64 table
+// FP32 number of the mixed path's momentum stencil.  Every divisor of the
+// stencil is a grid quantity (spacings, their sums, coefficient-table
+// entries, re), so the quotient is taken as a reciprocal times the dividend
+// (__fdividef, within 2 ulp of the IEEE quotient) instead of the IEEE
+// division's instruction sequence; the stencil's FP32 rounding dominates that
+// difference.  The FP64 drop-in stencil keeps IEEE division.
+struct FastF {
+  float v;
+  FastF() = default;
+  __device__ __forceinline__ constexpr FastF(float x) : v(x) {}
+  __device__ __forceinline__ explicit FastF(double x) : v((float)x) {}
+  __device__ __forceinline__ explicit operator double() const { return (double)v; }
+};
+__device__ __forceinline__ FastF operator+(FastF a, FastF b) { return FastF(a.v + b.v); }
+__device__ __forceinline__ FastF operator-(FastF a, FastF b) { return FastF(a.v - b.v); }
+__device__ __forceinline__ FastF operator-(FastF a) { return FastF(-a.v); }
+__device__ __forceinline__ FastF operator*(FastF a, FastF b) { return FastF(a.v * b.v); }
+__device__ __forceinline__ FastF operator/(FastF a, FastF b) { return FastF(__fdividef(a.v, b.v)); }
+__device__ __forceinline__ FastF fabs(FastF a) { return FastF(fabsf(a.v)); }
+
+// a grid / coefficient value as T: the FP32 copy for the FP32 stencils, else
+// the FP64 table
 template <typename T>
 __device__ __forceinline__ T grid_t(const double* d64, const float* f32, int q) {
-  if constexpr (std::is_same<T, float>::value) return f32[q];
+  if constexpr (std::is_same<T, float>::value || std::is_same<T, FastF>::value) return T(f32[q]);
   else return T(d64[q]);
 }
 
@@ -851,7 +872,7 @@ __global__ void k_solid_bc(DevBlock B, int move) {
 int launch_momentum(const std::vector<HostBlock*>& hbs, double dt, double re, bool fp32) {
   const MomArgs a{dt, re};
   const unsigned cap = 1u << 20;
-  if (fp32) TRY_R((launch_op<MomentumOp<float>, 128>(hbs, MomentumOp<float>{a}, Extent::Interior, cap)));
+  if (fp32) TRY_R((launch_op<MomentumOp<FastF>, 128>(hbs, MomentumOp<FastF>{a}, Extent::Interior, cap)));
   else TRY_R((launch_op<MomentumOp<double>, 128>(hbs, MomentumOp<double>{a}, Extent::Interior, cap)));
   // cells within reach of TS cells (none without surfaces 51/52), then the
   // values the reference's loop leaves at the TS positions

@@ -1,0 +1,95 @@
+"""Parity at the configurations' own sizes and horizons:
+
+  * the 64^3 sphere block (D = 0.25, Re 100) over 100 drop-in steps, bitwise
+    against the oracle (fields, SOR iteration counts, tags and lists);
+  * the twelve-block layout (coarse 320x224x224 + 11 fine blocks, 20.7M cells)
+    with the heaving and pitching plate, one drop-in step bitwise;
+  * the two-block sphere (coarse 96x64x64 + fine 64^3, D = 0.5, Re 300) over
+    200 steps: the FP32+FP64-refined path and the division-free FP64 path,
+    both to the FP64 Poisson residual 1e-6, against the oracle run with a far
+    tighter stop (max|pc - pco| < 1e-10) -- the error the residual target
+    leaves after the whole horizon.
+
+The oracle's OpenMP loops use every host core (results identical to its
+serial loops, tests/test_oracle_threads.py)."""
+import json
+
+import numpy as np
+import pytest
+
+from biocfd import synth
+from biocfd.solver import Solver
+from oracle.bridge import Oracle
+from parity_util import compare_fields, compare_iters, compare_search, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+def test_config1_sphere_64_cubed_100_steps_bitwise():
+    case = synth.sphere_single_block(n=64, n_steps=100)
+    o = Oracle(checked=False)
+    o.setup(case)
+    for _ in range(100):
+        o.step()
+    s = Solver(case)
+    try:
+        s.setup()
+        s.run(100)
+        compare_fields(o, s, "100 steps")
+        compare_iters(o, s, "100 steps")
+        compare_search(o, s, "100 steps")
+    finally:
+        s.close()
+
+
+def test_config3_twelve_blocks_moving_plate_one_step_bitwise():
+    case = synth.twelve_block(n_steps=1, moving=True)
+    o = Oracle(checked=False)
+    o.setup(case)
+    o.step()
+    s = Solver(case)
+    try:
+        s.setup()
+        s.run(1)
+        compare_fields(o, s, "1 step")
+        compare_iters(o, s, "1 step")
+        compare_search(o, s, "1 step")
+    finally:
+        s.close()
+
+
+# relative L2 bounds after 200 steps against the converged oracle (measured
+# values are printed; the bounds leave a margin above them)
+BOUND_VEL = 1e-4
+BOUND_P = 1e-2
+
+
+def test_config2_residual_target_paths_vs_converged_oracle_200_steps():
+    n = 200
+    case = synth.sphere_two_block(n_steps=n)
+    o = Oracle(checked=False)
+    o.setup(synth.replace(case, epsi=1e-10, pc_ita_max=50000))
+    for _ in range(n):
+        o.step()
+    report = {}
+    for name, prec, c in (("mixed", 1, case), ("fp64_division_free", 3, synth.with_mixed_omega(case))):
+        s = Solver(c)
+        try:
+            s.setup()
+            s.run(n, precision=prec, div_tol=1e-6, use_graph=1)
+            err = {}
+            for gi, g in enumerate(s.handles, 1):
+                f = s.fields(g)
+                for nm in ("u", "v", "w", "p"):
+                    a, b = f[nm], np.asarray(o.arr(gi, nm))
+                    if nm == "p":  # defined up to a constant per solve
+                        a, b = a - a.mean(), b - b.mean()
+                    err[f"block{gi}_{nm}"] = rel_l2(b, a)
+            report[name] = err
+        finally:
+            s.close()
+    print("\nconfig2_200_steps_rel_l2 " + json.dumps(report))
+    for name, err in report.items():
+        for k, e in err.items():
+            bound = BOUND_P if k.endswith("_p") else BOUND_VEL
+            assert e <= bound, f"{name} {k}: rel L2 {e:.3e} > {bound:.0e}"

@@ -245,10 +245,14 @@ def run_reference(args):
 # GPU arms
 # ---------------------------------------------------------------------------
 
-def new_solver(case, local, tune=True):
+WARM_START = True  # residual-target solves start from the last correction (--zero-start turns it off)
+
+
+def new_solver(case, local, tune=True, warm=None):
     from biocfd.solver import Solver
     s = Solver(case, device=local)
     s.setup()
+    s.set_warm_start(WARM_START if warm is None else warm)
     if tune:
         s.autotune()  # launch shapes of the solves; results do not depend on them
     return s
@@ -406,6 +410,18 @@ def headline(args, torch, local, world):
                                             "coef_rel": coef,
                                             "coefficients": "per plate: viscous drag, pressure drag, viscous "
                                                             "lift, pressure lift"}}
+    if WARM_START and args.zero_start_steps > 0:
+        # the flagship with the reference's zero start of every solve
+        s = new_solver(case, local, warm=False)
+        for _ in range(n_pre + 1):
+            s.run(1, precision=1, div_tol=DIV_TOL, use_graph=1)
+        ts, _ = timed_steps(s, torch, args.zero_start_steps, 1)
+        res, pairs = residual_stats(s)
+        s.close()
+        ms = statistics.mean(ts)
+        out["mixed_zero_start"] = {"ms_per_step": ms, "steps_per_s": 1000.0 / ms, "steps": len(ts),
+                                   "div_residual": res, "sweep_pairs_last_step": pairs,
+                                   "note": "the flagship with every solve started from pc = 0, as the reference"}
     if args.dropin_steps > 0:
         # the drop-in path (reference arithmetic and stop test) on the same
         # workload: its sweep pairs are the reference's (REFERENCE_SWEEP_PAIRS)
@@ -530,6 +546,7 @@ def twelve_block(torch, local, steps=5, warmup=3, fp64_steps=1, moving=False):
         s = Solver(case if prec == 1 else synth.with_mixed_omega(case), device=local)
         s.set_batching(batching)
         s.setup()
+        s.set_warm_start(WARM_START)
         s.autotune()
         for _ in range(warmup if prec == 1 else 1):
             s.run(1, precision=prec, div_tol=DIV_TOL, use_graph=1)
@@ -634,6 +651,9 @@ def run_gpu(args):
         "data": "synthetic (seeded, numpy default_rng 20261203)",
         "config": {"workload": WORKLOAD, "blocks": "384x256x256 + 2 x 256x192x192",
                    "parallelism": f"replicas x{world}",
+                   "solve_start": ("warm: every residual-target solve (mixed and FP64 arms alike) starts from "
+                                   "the previous step's correction at its fluid cells" if WARM_START else
+                                   "zero, as the reference"),
                    "l2": "not flushed: working set ~5 GB, far above the 129 MB L2",
                    "timed": "per-step CUDA events on the library stream",
                    "launch": "each step one replay of the captured step CUDA graph (each step's kinematics "
@@ -646,7 +666,7 @@ def run_gpu(args):
         "phases": h["phases"],
         "cell_updates_per_s": world * mixed["cell_updates_per_s"],
     }
-    for key in ("fp64_fast", "fp64", "fp64_input_omega", "fp64_dropin"):
+    for key in ("mixed_zero_start", "fp64_fast", "fp64", "fp64_input_omega", "fp64_dropin"):
         if key in h:
             line[key] = h[key]
     if fast:
@@ -686,10 +706,16 @@ def main():
     ap.add_argument("--twelve-only", action="store_true", help="only the twelve-block measurement")
     ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint timing")
     ap.add_argument("--alu-only", action="store_true", help="only the arithmetic-rate measurement")
+    ap.add_argument("--zero-start", action="store_true",
+                    help="start every residual-target solve from pc = 0 (the reference's start)")
+    ap.add_argument("--zero-start-steps", type=int, default=5,
+                    help="timed steps of the flagship with zero-started solves, beside the warm-started value")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiler mode: set up without the autotuner and run this many eager mixed steps")
     ap.add_argument("--profile-case", default="tandem", choices=["tandem", "block256"])
     args = ap.parse_args()
+    global WARM_START
+    WARM_START = not args.zero_start
     if args.warmup < 3:
         args.warmup = 3
     if args.sweep_only:

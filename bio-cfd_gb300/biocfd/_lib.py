@@ -55,6 +55,7 @@ _SIGS = {
     "bcfd_block_set_mixed_params": [c_i64, c_i64, c_double, c_int],
     "bcfd_block_set_solve_launch": [c_i64, c_int, c_int, c_int],
     "bcfd_set_batching": [c_int],
+    "bcfd_set_warm_start": [c_int],
     "bcfd_set_wait_limit_ns": [c_i64],
     "bcfd_check_wait_limit": [C.POINTER(c_int), P_d],
     "bcfd_block_set_list_capacity": [c_i64, c_i64],

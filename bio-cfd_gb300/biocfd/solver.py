@@ -307,6 +307,10 @@ class Solver:
     def set_batching(self, on: bool):
         check(self.L.bcfd_set_batching(int(on)), "set_batching")
 
+    def set_warm_start(self, on: bool):
+        """Residual-target solves start from the previous step's correction (library-wide)."""
+        check(self.L.bcfd_set_warm_start(int(on)), "set_warm_start")
+
     def set_solve_launch(self, threads: int = 0, ctas_per_sm: int = 0, fp64_sync: int = 0, block: int = None):
         for g in (self.handles if block is None else [self.handles[block]]):
             check(self.L.bcfd_block_set_solve_launch(g, threads, ctas_per_sm, fp64_sync), "set_solve_launch")

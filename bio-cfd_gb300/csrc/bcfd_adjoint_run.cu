@@ -641,14 +641,14 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
     a.fc.axis = mem.get<int>(ntask);
     a.fc.pos = mem.get<int64_t>(8 * ntask);
     a.fc.coef = mem.get<double>(8 * ntask);
-    a.fc.kc = mem.get<double>(8 * ntask);
-    a.fc.gk = mem.get<double>(8);
+    a.fc.kc = mem.get<double>(kKinScalars * ntask);
+    a.fc.gk = mem.get<double>(kKinScalars);
     if (!a.A || !a.pcb || !a.y || !a.bb || !a.foot || !a.ucl || !a.fc.tgt || !a.fc.axis || !a.fc.pos ||
         !a.fc.coef || !a.fc.kc || !a.fc.gk)
       return BCFD_E_NOMEM;
     ACK(cudaMemsetAsync(a.A, 0, kStateFields * a.np * sizeof(double), stream()));
     ACK(cudaMemsetAsync(a.ucl, 0, (size_t)a.hb->d.d.ny * a.hb->d.d.nz * sizeof(double), stream()));
-    ACK(cudaMemsetAsync(a.fc.gk, 0, 8 * sizeof(double), stream()));
+    ACK(cudaMemsetAsync(a.fc.gk, 0, kKinScalars * sizeof(double), stream()));
   }
   // coupling masks: the positions each map writes (the maps are partitions of
   // unity, so a field of ones maps to ones exactly there)
@@ -683,7 +683,7 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   AdjBlock& ah = AB[hidx];
   if (use_stress) {
     double* sd = mem.get<double>(4);
-    double* ss = mem.get<double>(8 + 64 * (size_t)hb->d.ne);
+    double* ss = mem.get<double>(8 + std::max<size_t>(64, kKinScalars) * (size_t)hb->d.ne);
     if (!sd || !ss) return BCFD_E_NOMEM;
     ACK(h2d(sd, stress_seed, 4 * sizeof(double)));
     TRY_R(launch_stress_weights(hb, mu_f, rho_f, sd, W, ss));

@@ -620,6 +620,12 @@ int bcfd_block_set_list_capacity(bcfd_handle h, int64_t cap) {
   return 0;
 }
 
+int bcfd_set_warm_start(int on) {
+  LOCK();
+  lib().warm_start = on != 0;
+  return 0;
+}
+
 int bcfd_set_batching(int on) {
   LOCK();
   lib().batch = on != 0;

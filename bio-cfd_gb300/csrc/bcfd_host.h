@@ -142,6 +142,18 @@ struct HostInterface {
 
 enum TabId { TPX = 0, TPY, TPZ, TUX, TUY, TUZ, TVX, TVY, TVZ, TWX, TWY, TWZ };
 
+// Records, during the forward recomputation of an adjoint run through moving
+// bodies, what the transposes need from each forcing call: the geometric
+// partials of every task at the stencil values it read (k_force_geo).
+struct ForceRecorder {
+  virtual ~ForceRecorder() = default;
+  // device buffer of 6 * nt doubles for call (mode, vel) of block hb in the
+  // step being recomputed (nullptr: nothing to record)
+  virtual double* slot(HostBlock* hb, int mode, int vel, int64_t nt) = 0;
+  // device scratch of 3 point arrays of the block (the pre-call copies)
+  virtual double* scratch(HostBlock* hb) = 0;
+};
+
 struct Lib {
   std::recursive_mutex mu;
   bool ready = false;
@@ -182,6 +194,8 @@ struct Lib {
   std::vector<unsigned char> eager_key; // the key left by the last eager step
   int adj_precision = 1;  // zero-BC and adjoint solves: 0 FP64 SOR, 1 FP32 sweeps + FP64 correction
   uint64_t wait_limit_ns = kBarrierLimitNs;  // longest single device-side wait
+  bool warm_start = false;  // residual-target solves start from the last correction
+  ForceRecorder* recorder = nullptr;  // set by an adjoint run while it recomputes steps
   int64_t step_kernels = 0;              // kernels in the captured step
 };
 
@@ -245,7 +259,9 @@ bool tb_solve_fits(HostBlock* hb);
 int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double div_tol);
 // res_tol > 0: stop on the FP64 residual dt*max|b/dt - A pc| <= res_tol
 int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol = 0.0, int fast = 0);
-int launch_zero_poisson(HostBlock* hb);
+// warm = true: the solve starts from the previous correction at its updated
+// cells (residual-target solves only) instead of from 0
+int launch_zero_poisson(HostBlock* hb, bool warm = false);
 int launch_steady_state(HostBlock* hb, double dt);
 int launch_copy_t_to_n(HostBlock* hb);
 int launch_copy_n_to_t(HostBlock* hb);
@@ -334,13 +350,19 @@ int search_origin_stage(HostBlock* hb, float h[4], float** dev);
 int launch_stress_noalloc(HostBlock* hb, double mu_f, double rho_f, double* out_host);
 // adjoint of the forcing loops (k_forcing.cu): per-task coefficient scratch
 // (capacity 6 * cap_ib tasks) and the adjoint arrays by axis (0 p, 1 u, 2 v, 3 w)
+// kinematic scalars the forcing and drag/lift depend on: the 8 of
+// bcfd_block_set_kinematics and the pivot (piv_x, piv_y, piv_z)
+constexpr int kKinScalars = 11;
 struct ForceCoef {
   int64_t* tgt;
   int* axis;
   int64_t* pos;
   double* coef;
-  double* kc;  // per task, d(output)/d(kinematic scalar p), p = 0..7 (the order of bcfd_block_set_kinematics)
-  double* gk;  // 8 accumulators: dJ/d(kinematic scalar p)
+  double* kc;  // per task, d(output)/d(kinematic scalar p), p < kKinScalars (bcfd_block_set_kinematics order)
+  double* gk;  // kKinScalars accumulators: dJ/d(kinematic scalar p)
+  int* elem;         // per task: its element (0-based)
+  const double* geo; // per task: 6 geometric partials recorded forward (nullptr: geometry fixed)
+  double* ge;        // per element: 6 accumulators dJ/d(centroid, unit normal) (with geo)
 };
 // the 8 rigid-body kinematic scalars of a block, in bcfd_block_set_kinematics order
 __host__ __device__ inline double& kin_scalar(Kin& K, int p) {
@@ -352,7 +374,10 @@ __host__ __device__ inline double& kin_scalar(Kin& K, int p) {
     case 4: return K.thetaDDot1;
     case 5: return K.thetaDot2;
     case 6: return K.thetaDDot2;
-    default: return K.alphaDot;
+    case 7: return K.alphaDot;
+    case 8: return K.piv_x;
+    case 9: return K.piv_y;
+    default: return K.piv_z;
   }
 }
 struct AdjPtrs {

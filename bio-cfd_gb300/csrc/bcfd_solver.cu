@@ -178,7 +178,10 @@ int poisson(const SolveCfg& c, int start, int finish, int step) {
       (g == 1 ? first : fine).push_back(hb);
     }
   phase_mark(PH_CORRECTION);
-  for (HostBlock* hb : set) TRY(launch_zero_poisson(hb));
+  // the reference starts every solve from pc = 0; a residual-target solve may
+  // start from the last correction instead (same stop, same boundary data)
+  const bool warm = lib().warm_start && c.precision >= 1;
+  for (HostBlock* hb : set) TRY(launch_zero_poisson(hb, warm));
   phase_mark(PH_COUPLING);
   TRY(fine_update_newv_bd());
   TRY(coarse_update_newv());
@@ -509,6 +512,7 @@ std::vector<unsigned char> step_key(const bcfd_step_config& c) {
   put(&L.gen, sizeof L.gen);
   put(&L.batch, sizeof L.batch);
   put(&L.wait_limit_ns, sizeof L.wait_limit_ns);
+  put(&L.warm_start, sizeof L.warm_start);
   for (const HostBlock* hb : L.blocks) {
     const unsigned char none = 0;
     if (!hb) { put(&none, 1); continue; }

@@ -18,6 +18,7 @@
 // Field / Ghost velocity variants read ut and write u (or ghost arrays) and
 // therefore run as plain data-parallel kernels.
 #include "bcfd_host.h"
+#include "bcfd_dual.cuh"
 
 namespace bcfd {
 
@@ -249,6 +250,110 @@ __device__ double reconstruct(const DevBlock& B, int mode, int comp, const Probe
   return vel_quad(val, surf_velocity(B, P.e, comp, mode), dn, n1, s2n);
 }
 
+// ---------------------------------------------------------------------------
+// Geometric partials of one reconstruction (adjoint through moving bodies):
+// the output's derivatives with respect to the centroid (lanes 0-2) and the
+// unit normal (lanes 3-5) of the task's element, at the stencil values f the
+// forward read.  The bracketing indices, the element and every branch are
+// those of the forward evaluation (the discrete choices are held fixed); the
+// normal distance s2n = (sample - centroid) . normal of computeNormDistance
+// (src/Search.F90:743-861) carries its own derivatives.
+// ---------------------------------------------------------------------------
+using G6 = DualN<6>;
+
+__device__ __forceinline__ G6 bilinear_g(const G6& x, const G6& y, double x1, double x2, double y1, double y2,
+                                         double f0, double f1, double f2, double f3) {
+  const G6 numer = f0 * (x2 - x) * (y2 - y) + f2 * (x2 - x) * (y - y1) + f1 * (x - x1) * (y2 - y) +
+                   f3 * (x - x1) * (y - y1);
+  return numer / ((x2 - x1) * (y2 - y1));
+}
+__device__ __forceinline__ G6 derivative_g(const G6& x, double x2, double x1, const G6& p_x, const G6& p_x2,
+                                           const G6& p_x1) {
+  const G6 h2 = fabs(x2 - x), h1 = fabs(x1 - x);
+  return (h1 * h1 * p_x2 - h2 * h2 * p_x1 + (h2 * h2 - h1 * h1) * p_x) / (h1 * h2 * (h1 + h2) + 1e-16);
+}
+
+// the sample point of NormDis slot `slot` of IB cell (i,j,k) (k_norm_distance)
+__device__ __forceinline__ void nd_sample(const DevBlock& B, int slot, int i, int j, int k, double q[3]) {
+  q[0] = slot == 1 ? B.x1[i - 1] : slot == 2 ? B.x1[i] : B.xp[i - 1];
+  q[1] = slot == 3 ? B.y1[j - 1] : slot == 4 ? B.y1[j] : B.yp[j - 1];
+  q[2] = slot == 5 ? B.z1[k - 1] : slot == 6 ? B.z1[k] : B.zp[k - 1];
+}
+
+__device__ G6 reconstruct_geo(const DevBlock& B, int mode, int comp, int n, const Probe& P, const double f[8]) {
+  const int ib = mode == 2 ? B.ts_idx[n] - 1 : n;
+  const int i = B.ib_i[ib], j = B.ib_j[ib], k = B.ib_k[ib];
+  const int e = P.e;
+  const G6 cx = G6::seed(B.xcent[e], 0), cy = G6::seed(B.ycent[e], 1), cz = G6::seed(B.zcent[e], 2);
+  const G6 nx = G6::seed(B.cosA[e], 3), ny = G6::seed(B.cosB[e], 4), nz = G6::seed(B.cosG[e], 5);
+  const int slot = comp < 0 ? N_P : comp + ((comp & 1) ? 0 : 2);
+  double xs[3];
+  nd_sample(B, slot, i, j, k, xs);
+  const double sg = mode == 2 ? -1.0 : 1.0;
+  G6 s2n = sg * ((xs[0] - cx) * nx + (xs[1] - cy) * ny + (xs[2] - cz) * nz);
+  s2n.v = P.s2n;  // the forward's value (its branches)
+  const G6 pt1 = 1.5 * ::sqrt(B.dxa[i - 1] * B.dxa[i - 1] + B.dya[j - 1] * B.dya[j - 1] +
+                              B.dza[k - 1] * B.dza[k - 1]) +
+                 (fabs(s2n) - s2n) * 0.5;
+  const Grid3 G = comp_grid(B, P.axis);
+  double qx = G.x[i - 1], qy = G.y[j - 1], qz = G.z[k - 1];
+  if (comp == CU2) qx = G.x[i];
+  if (comp == CV2) qy = G.y[j];
+  if (comp == CW2) qz = G.z[k];
+  const G6 x = qx + sg * (pt1 * nx), y = qy + sg * (pt1 * ny), z = qz + sg * (pt1 * nz);
+  // compute_value_and_derivatives on the forward's brackets
+  const int ii = P.ix, jj = P.iy, kk = P.iz;
+  const double yj = G.y[jj - 1], yj1 = G.y[jj], zk = G.z[kk - 1], zk1 = G.z[kk], xi = G.x[ii - 1], xi1 = G.x[ii];
+  const G6 t11 = bilinear_g(y, z, yj, yj1, zk, zk1, f[0], f[2], f[4], f[6]);
+  const G6 t12 = bilinear_g(y, z, yj, yj1, zk, zk1, f[1], f[3], f[5], f[7]);
+  const G6 t21 = bilinear_g(x, z, xi, xi1, zk, zk1, f[0], f[1], f[4], f[5]);
+  const G6 t22 = bilinear_g(x, z, xi, xi1, zk, zk1, f[2], f[3], f[6], f[7]);
+  const G6 t31 = bilinear_g(x, y, xi, xi1, yj, yj1, f[0], f[1], f[2], f[3]);
+  const G6 t32 = bilinear_g(x, y, xi, xi1, yj, yj1, f[4], f[5], f[6], f[7]);
+  const G6 val = t11 + (x - xi) * (t12 - t11) / (xi1 - xi);
+  const G6 d0 = derivative_g(x, xi1, xi, val, t12, t11);
+  const G6 d1 = derivative_g(y, yj1, yj, val, t22, t21);
+  const G6 d2 = derivative_g(z, zk1, zk, val, t32, t31);
+  const G6 dn = sg * (d0 * nx + d1 * ny + d2 * nz);
+  const G6 n1 = pt1 + s2n;
+  const Kin& K = *B.kin;
+  const int sid = B.surf_id[e];
+  if (comp < 0) {
+    G6 ac_y(0.0), ac_z(0.0), at_y(0.0), at_z(0.0);
+    if (sid == 51 || sid == 52) {
+      const double td = sid == 51 ? K.thetaDot1 : K.thetaDot2;
+      const double tdd = sid == 51 ? K.thetaDDot1 : K.thetaDDot2;
+      ac_z = -(td * td) * (cz - K.piv_z);
+      ac_y = -(td * td) * (cy - K.piv_y);
+      at_z = tdd * (cy - K.piv_y);
+      at_y = -tdd * (cz - K.piv_z);
+    }
+    const G6 dpdn = mode == 2 ? ((ac_z + at_z) * nz + (ac_y + at_y) * ny) + K.yddot * ny
+                              : -((ac_z + at_z) * nz + (ac_y + at_y) * ny) - K.yddot * ny;
+    const G6 aval = (dn - dpdn) / (2.0 * n1);
+    const G6 cval = val - (dn + dpdn) * n1 * 0.5;
+    return aval * (s2n * s2n) + dpdn * s2n + cval;
+  }
+  G6 surf(0.0);
+  if (comp == CU2 || comp == CU1) {
+    surf = G6(K.xdot);
+  } else if (comp == CV2 || comp == CV1) {
+    if (sid == 50) {
+      surf = G6(K.ydot);
+    } else {
+      const double td = sid == 51 ? K.thetaDot1 : K.thetaDot2;
+      surf = mode == 0 ? -td * (cz - K.piv_z) + K.ydot
+                       : -td * (cz - K.piv_z) + (-K.alphaDot) * (cx - K.piv_x) + K.ydot;
+    }
+  } else if (sid != 50) {
+    const double td = sid == 51 ? K.thetaDot1 : K.thetaDot2;
+    surf = td * (cy - K.piv_y);
+  }
+  const G6 bval = 2.0 / n1 * (val - surf) - dn;
+  const G6 aval = dn / n1 - (val - surf) / (n1 * n1);
+  return aval * (s2n * s2n) + bval * s2n + surf;
+}
+
 __device__ __forceinline__ double* comp_array(const DevBlock& B, int axis, bool tfield) {
   switch (axis) {
     case 1: return tfield ? B.ut : B.u;
@@ -266,6 +371,11 @@ struct DagScratch {
   int* dep;       // per task 8 dependency task ids (-1: read the array)
   int* level;     // per task: the round it finished in (0: not yet)
   int* flag;      // [0..2] "work left" flags of the rounds
+};
+
+// four read-only point arrays indexed by axis (0 p, 1 u, 2 v, 3 w)
+struct Fields4c {
+  const double* a[4];
 };
 
 struct DagArgs {
@@ -462,17 +572,19 @@ __global__ void k_force_coef(DevBlock B, int mode, int vel, ForceCoef fc) {
     }
     fc.tgt[t] = B.d.idx(P.ti, P.tj, P.tk);
     fc.axis[t] = P.axis;
+    if (fc.elem) fc.elem[t] = P.e;
     // kinematic sensitivities at f = 0: the output is at most quadratic in
     // each scalar (centripetal terms), so the central difference with unit
     // steps is its derivative
-    for (int p = 0; p < 8; ++p) {
+    for (int p = 0; p < kKinScalars; ++p) {
       Kin kp = *B.kin, km = *B.kin;
       kin_scalar(kp, p) += 1.0;
       kin_scalar(km, p) -= 1.0;
       DevBlock Bp = B, Bm = B;
       Bp.kin = &kp;
       Bm.kin = &km;
-      fc.kc[8 * (int64_t)t + p] = 0.5 * (reconstruct(Bp, mode, comp, P, f) - reconstruct(Bm, mode, comp, P, f));
+      fc.kc[kKinScalars * (int64_t)t + p] =
+          0.5 * (reconstruct(Bp, mode, comp, P, f) - reconstruct(Bm, mode, comp, P, f));
     }
   }
 }
@@ -488,11 +600,40 @@ __global__ void k_force_rev(DevBlock B, int vel, ForceCoef fc, AdjPtrs a) {
     const double o = T[fc.tgt[t]];
     T[fc.tgt[t]] = 0.0;
     for (int q = 0; q < 8; ++q) S[fc.pos[8 * (int64_t)t + q]] += fc.coef[8 * (int64_t)t + q] * o;
-    for (int p = 0; p < 8; ++p) fc.gk[p] += fc.kc[8 * (int64_t)t + p] * o;
+    for (int p = 0; p < kKinScalars; ++p) fc.gk[p] += fc.kc[kKinScalars * (int64_t)t + p] * o;
+    if (fc.geo) {
+      const int e = fc.elem[t];
+      for (int l = 0; l < 6; ++l) fc.ge[6 * (int64_t)e + l] += fc.geo[6 * (int64_t)t + l] * o;
+    }
   }
 }
 
 }  // namespace
+
+// Geometric partials of every task of one forcing call, at the stencil values
+// it read: the DAG variants read the output of the latest earlier writer, else
+// the array as it was before the call (`pre`); the others read their source
+// array, which the call does not change.
+__global__ void k_force_geo(DevBlock B, int mode, int vel, Fields4c pre, DagScratch s, int dag, double* geo) {
+  const int nib = (int)min(B.cnt[C_IB], (int64_t)B.cap_ib);
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  const int cnt = mode == 2 ? nts : nib;
+  const int nt = vel ? 6 * cnt : cnt;
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
+    const int n = vel ? t / 6 : t, comp = vel ? t % 6 : -1;
+    const Probe P = make_probe(B, mode, comp, n);
+    const double* src = pre.a[P.axis];
+    double f[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int w = dag ? s.dep[8 * t + q] : -1;
+      f[q] = w >= 0 ? s.out[w] : src[B.d.idx(P.ii + (q & 1), P.jj + ((q >> 1) & 1), P.kk + (q >> 2))];
+    }
+    const G6 r = reconstruct_geo(B, mode, comp, n, P, f);
+#pragma unroll
+    for (int l = 0; l < 6; ++l) geo[6 * (int64_t)t + l] = r.d[l];
+  }
+}
 
 // transpose of launch_forcing_velocity / launch_forcing_pressure (modes 0 and
 // 1) on adjoint arrays indexed by axis (0 p, 1 u, 2 v, 3 w): a.tgt holds the
@@ -555,25 +696,70 @@ static int launch_dag(HostBlock* hb, int mode, int vel) {
   return 0;
 }
 
-int launch_forcing_velocity(HostBlock* hb, int mode) {
-  if (hb->d.ne <= 0) return 0;
-  if (mode == 0) return launch_dag(hb, 0, 1);
-  if (mode == 1) {
-    k_vel_field<<<grid_for(6 * (int64_t)hb->d.cap_ib, 128, 2048), 128, 0, stream()>>>(hb->d);
-    BCFD_LAUNCHED();
-    return 0;
-  }
-  k_vel_ghost<<<grid_for(6 * (int64_t)hb->d.cap_ib, 128, 2048), 128, 0, stream()>>>(hb->d);
+// With a recorder (an adjoint run recomputing steps through moving bodies):
+// the pre-call copy of the arrays a DAG variant overwrites in place
+static int record_pre(HostBlock* hb, int vel, Fields4c* pre) {
+  ForceRecorder* R = lib().recorder;
+  double* sc = R->scratch(hb);
+  if (!sc) return BCFD_E_NOMEM;
+  const size_t np = (size_t)hb->d.d.npts(), b = np * sizeof(double);
+  const double* src[3] = {vel ? hb->d.ut : hb->d.p, hb->d.vt, hb->d.wt};
+  for (int q = 0; q < (vel ? 3 : 1); ++q)
+    BCFD_CUDA(cudaMemcpyAsync(sc + q * np, src[q], b, cudaMemcpyDeviceToDevice, stream()));
+  if (vel) *pre = Fields4c{{hb->d.p, sc, sc + np, sc + 2 * np}};
+  else *pre = Fields4c{{sc, hb->d.ut, hb->d.vt, hb->d.wt}};
+  return 0;
+}
+
+// ... and the tasks' geometric partials once the call has run
+static int record_geo(HostBlock* hb, int mode, int vel, const Fields4c& pre, bool dag) {
+  int64_t cnt[N_COUNT];
+  BCFD_CUDA(d2h(cnt, hb->d.cnt, sizeof(cnt)));
+  const int64_t c = std::min<int64_t>(mode == 2 ? cnt[C_TS] : cnt[C_IB], hb->d.cap_ib);
+  const int64_t nt = vel ? 6 * c : c;
+  double* geo = lib().recorder->slot(hb, mode, vel, nt);
+  if (!geo || nt == 0) return 0;
+  int st = 0;
+  DagScratch& s = dag_scratch(hb, &st);
+  if (st) return st;
+  k_force_geo<<<grid_for(nt, 128, 2048), 128, 0, stream()>>>(hb->d, mode, vel, pre, s, dag ? 1 : 0, geo);
   BCFD_LAUNCHED();
   return 0;
 }
 
+int launch_forcing_velocity(HostBlock* hb, int mode) {
+  if (hb->d.ne <= 0) return 0;
+  const bool rec = lib().recorder != nullptr;
+  const Fields4c cur{{hb->d.p, hb->d.ut, hb->d.vt, hb->d.wt}};
+  if (mode == 0) {
+    Fields4c pre = cur;
+    if (rec) TRY_R(record_pre(hb, 1, &pre));
+    TRY_R(launch_dag(hb, 0, 1));
+    return rec ? record_geo(hb, 0, 1, pre, true) : 0;
+  }
+  if (mode == 1) {
+    k_vel_field<<<grid_for(6 * (int64_t)hb->d.cap_ib, 128, 2048), 128, 0, stream()>>>(hb->d);
+    BCFD_LAUNCHED();
+    return rec ? record_geo(hb, 1, 1, cur, false) : 0;
+  }
+  k_vel_ghost<<<grid_for(6 * (int64_t)hb->d.cap_ib, 128, 2048), 128, 0, stream()>>>(hb->d);
+  BCFD_LAUNCHED();
+  return rec ? record_geo(hb, 2, 1, cur, false) : 0;
+}
+
 int launch_forcing_pressure(HostBlock* hb, int mode) {
   if (hb->d.ne <= 0) return 0;
-  if (mode == 0 || mode == 1) return launch_dag(hb, mode, 0);
+  const bool rec = lib().recorder != nullptr;
+  const Fields4c cur{{hb->d.p, hb->d.ut, hb->d.vt, hb->d.wt}};
+  if (mode == 0 || mode == 1) {
+    Fields4c pre = cur;
+    if (rec) TRY_R(record_pre(hb, 0, &pre));
+    TRY_R(launch_dag(hb, mode, 0));
+    return rec ? record_geo(hb, mode, 0, pre, true) : 0;
+  }
   k_p_ghost<<<grid_for(hb->d.cap_ib, 128, 2048), 128, 0, stream()>>>(hb->d);
   BCFD_LAUNCHED();
-  return 0;
+  return rec ? record_geo(hb, 2, 0, cur, false) : 0;
 }
 
 }  // namespace bcfd

@@ -569,21 +569,29 @@ __device__ __forceinline__ void restore_consts(const DevBlock& B, int nts, doubl
 }
 
 // sign tests of src/NavierStokes.f90:321-354 for every TS entry: the last
-// entry with a negative test, per kind
+// entry with a negative test, per kind.  The reference's loop keeps the last
+// hit, so the entries are visited from the end and each kind stops at its
+// first hit: the same entry, the same sign test arithmetic, and usually a few
+// entries instead of all of them.
 __device__ void own_substitution(const DevBlock& B, int i, int j, int k, int nts, int* last) {
   const double X[N_KIND] = {B.x1[i], B.x1[i - 1], B.xp[i - 1], B.xp[i - 1], B.xp[i - 1], B.xp[i - 1], B.xp[i - 1]};
   const double Y[N_KIND] = {B.yp[j - 1], B.yp[j - 1], B.y1[j], B.y1[j - 1], B.yp[j - 1], B.yp[j - 1], B.yp[j - 1]};
   const double Z[N_KIND] = {B.zp[k - 1], B.zp[k - 1], B.zp[k - 1], B.zp[k - 1], B.z1[k], B.z1[k - 1], B.zp[k - 1]};
 #pragma unroll
   for (int K = 0; K < N_KIND; ++K) last[K] = -1;
-  for (int nn = 0; nn < nts; ++nn) {
+  unsigned open = (1u << N_KIND) - 1u;  // kinds still without a hit
+  for (int nn = nts - 1; nn >= 0 && open; --nn) {
     const int bt = B.ts_idx[nn] - 1;
 #pragma unroll
     for (int K = 0; K < N_KIND; ++K) {
+      if (!(open & (1u << K))) continue;
       const int e = B.nel[nel_slot(K)][bt] - 1;
       const double t = (X[K] - B.xcent[e]) * B.cosA[e] + (Y[K] - B.ycent[e]) * B.cosB[e] +
                        (Z[K] - B.zcent[e]) * B.cosG[e];
-      if (t < 0) last[K] = nn;
+      if (t < 0) {
+        last[K] = nn;
+        open &= ~(1u << K);
+      }
     }
   }
 }

@@ -1089,10 +1089,25 @@ int launch_correct_velocity(HostBlock* hb, double dt) {
   return launch_correct_velocity(std::vector<HostBlock*>{hb}, dt);
 }
 
-int launch_zero_poisson(HostBlock* hb) {
+// warm start: pc keeps its values at the cells the solve updates (the last
+// step's correction there, the initial guess) and is 0 everywhere else, as
+// after the reference's zeroing (solid cells, block faces, coupling ghosts)
+__global__ void k_pc_warm(DevBlock B) {
+  const int64_t n = B.d.npacked();
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    if (!B.upd[0][t]) B.pc[0][t] = 0.0;
+    if (!B.upd[1][t]) B.pc[1][t] = 0.0;
+  }
+}
+
+int launch_zero_poisson(HostBlock* hb, bool warm) {
   const size_t bytes = (size_t)hb->d.d.npacked() * sizeof(double);
+  if (warm) {
+    k_pc_warm<<<grid_for(hb->d.d.npacked(), 256), 256, 0, stream()>>>(hb->d);
+    BCFD_LAUNCHED();
+  }
   for (int c = 0; c < 2; ++c) {
-    BCFD_CUDA(cudaMemsetAsync(hb->d.pc[c], 0, bytes, stream()));
+    if (!warm) BCFD_CUDA(cudaMemsetAsync(hb->d.pc[c], 0, bytes, stream()));
     BCFD_CUDA(cudaMemsetAsync(hb->d.bpk[c], 0, bytes, stream()));
   }
   // nIterPcor = 0, derr2 = 0, derrStdSt = 0 (src/PcorVcor.F90:78-80)

@@ -184,7 +184,7 @@ __global__ void k_stress_coef(DevBlock B, double mu_f, double rho_f, const doubl
   }
 }
 
-// part[8e + p] = d/d(kinematic scalar p) of sum_t scale[t] * term_t(e) at the
+// part[11e + p] = d/d(kinematic scalar p) of sum_t scale[t] * term_t(e) at the
 // current fields (the terms are affine in the fields and at most quadratic in
 // each scalar, so the central difference with unit steps is exact)
 __global__ void k_stress_kin_elem(DevBlock B, double mu_f, double rho_f, const double* scale, double* part) {
@@ -194,7 +194,7 @@ __global__ void k_stress_kin_elem(DevBlock B, double mu_f, double rho_f, const d
     double f[4][8];
     for (int c = 0; c < 4; ++c)
       for (int q = 0; q < 8; ++q) f[c][q] = arr[c][S.pos[c][q]];
-    for (int p = 0; p < 8; ++p) {
+    for (int p = 0; p < kKinScalars; ++p) {
       Kin kp = *B.kin, km = *B.kin;
       kin_scalar(kp, p) += 1.0;
       kin_scalar(km, p) -= 1.0;
@@ -206,17 +206,17 @@ __global__ void k_stress_kin_elem(DevBlock B, double mu_f, double rho_f, const d
       elem_terms(Bm, e, mu_f, rho_f, S, f, om);
       double acc = 0.0;
       for (int t = 0; t < 4; ++t) acc += scale[t] * 0.5 * (op[t] - om[t]);
-      part[8 * (int64_t)e + p] = acc;
+      part[kKinScalars * (int64_t)e + p] = acc;
     }
   }
 }
 
-// gk[p] += sum_e part[8e + p]: fixed-order reduction by one CTA of 256 threads
+// gk[p] += sum_e part[11e + p]: fixed-order reduction by one CTA of 256 threads
 __global__ void k_stress_kin_sum(const double* part, int ne, double* gk) {
   __shared__ double s[256];
-  for (int p = 0; p < 8; ++p) {
+  for (int p = 0; p < kKinScalars; ++p) {
     double acc = 0.0;
-    for (int e = threadIdx.x; e < ne; e += blockDim.x) acc += part[8 * (int64_t)e + p];
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) acc += part[kKinScalars * (int64_t)e + p];
     s[threadIdx.x] = acc;
     __syncthreads();
     for (int h = blockDim.x / 2; h > 0; h >>= 1) {
@@ -299,8 +299,8 @@ int launch_stress_weights(HostBlock* hb, double mu_f, double rho_f, const double
   return 0;
 }
 
-// gk[8] += the kinematic derivative of sum_t seed[t] * coefficient t at the
-// block's current fields; scratch: 8 + 8 ne doubles
+// gk[kKinScalars] += the kinematic derivative of sum_t seed[t] * coefficient
+// t at the block's current fields; scratch: 8 + kKinScalars ne doubles
 int launch_stress_kin(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double* gk,
                       double* scratch) {
   if (hb->d.ne <= 0) return BCFD_E_STATE;

@@ -57,6 +57,15 @@ int64_t bcfd_kernel_launches(void);
  * are solved together) run over all blocks in one launch per phase, driven by
  * a device table of block views; 0: one launch per block.  Same results. */
 int bcfd_set_batching(int on);
+/* 1: the Poisson solves of the residual-target precisions (1-3 of
+ * bcfd_step_config) start from the previous step's correction pc at the cells
+ * they update instead of from pc = 0 (no counterpart in the reference, which
+ * zeroes pc before every poissonSolver, src/PcorVcor.F90:74-80).  The stop
+ * test, the operator and the boundary data (0 at solid cells and faces, the
+ * coupling ghosts) are unchanged, so each solve still ends at the requested
+ * residual; only its starting point differs.  0 (default): zero start.  The
+ * drop-in precision 0 always starts from 0. */
+int bcfd_set_warm_start(int on);
 /* Longest time (ns) any single device-side wait of a persistent kernel (the
  * grid barriers and the neighbour-tile waits of the Poisson solves, the
  * forcing's level barriers) may spin before the kernel gives up: it records

@@ -12,6 +12,7 @@ pytestmark = pytest.mark.gpu
 
 TOL = 1e-6          # FP64 Poisson residual target in divergence units
 FIELD_TOL = 2e-5    # rel L2 between solutions that each meet TOL
+P_TOL = 1e-4        # the same for the pressure of differently started solves
 
 
 def _run(case, precision, steps, variant=0):
@@ -69,3 +70,33 @@ def test_division_free_fp64_reaches_tolerance_two_block():
         for nm in ("u", "v", "w", "p"):
             e = rel_l2(b2[nm], b3[nm])
             assert e < FIELD_TOL, (nm, e)
+
+
+@pytest.mark.parametrize("precision", [1, 3])
+def test_warm_start_reaches_tolerance_and_agrees(precision):
+    # the residual-target solves started from the previous correction stop at
+    # the same FP64 residual and give the zero-start fields within the tolerance
+    case = synth.small_two_block(n_steps=4)
+    if precision == 3:
+        case = synth.with_mixed_omega(case)
+    s = Solver(case)
+    s.setup()
+    s.set_warm_start(True)
+    try:
+        res = []
+        for _ in range(4):
+            s.run(1, precision=precision, div_tol=TOL)
+            res.append(max(s.divergence(g)[1] for g in s.handles))
+        fw = [s.fields(g) for g in s.handles]
+    finally:
+        s.set_warm_start(False)
+        s.close()
+    assert 0.0 < max(res) <= TOL * (1 + 1e-9), res
+    fz, _ = _run(case, precision, 4)
+    for bw, bz in zip(fw, fz):
+        for nm in ("u", "v", "w", "p"):
+            # the residual target bounds the divergence the correction leaves,
+            # not the pressure's smooth mode, which the starting point shifts
+            # further than the velocities
+            e = rel_l2(bz[nm], bw[nm])
+            assert e < (P_TOL if nm == "p" else FIELD_TOL), (nm, e)

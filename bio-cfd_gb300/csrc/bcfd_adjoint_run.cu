@@ -397,21 +397,47 @@ int solve_adj(AdjBlock& a, double tol, int64_t itmax) {
 //   coarseUpdate_pc, correctPressure, correctVelocity, velocityBC (block 1),
 //   ut -> u, fineUpdate_bd_mv (u, v, w, p faces), coarseUpdate (u, v, w, p);
 //   pressureForcing1; velocityForcingField, pressureForcingField (body).
-int adjoint_step(std::vector<AdjBlock>& B, std::vector<IfaceMasks>& M, const bcfd_step_config& c, double tol,
-                 int64_t itmax) {
+// The recorded geometric partials of the forcing calls of the step being
+// transposed (moving bodies; nullptr with the geometry fixed).  Call index
+// 2 * mode + vel.
+struct StepGeo {
+  const double* geo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+
+// the part of a step after the body moved, transposed: pressureForcingField,
+// velocityForcingField (the geometry and kinematics of the step's end)
+int adjoint_step_second(std::vector<AdjBlock>& B, const std::vector<StepGeo>* geo) {
+  for (size_t q = 0; q < B.size(); ++q) {
+    AdjBlock& a = B[q];
+    if (!a.body) continue;
+    const AdjPtrs pin{{a.F(3), a.F(1), a.F(2), a.F(3)}, {a.F(3), a.F(1), a.F(2), a.F(3)}};
+    const AdjPtrs field{{a.F(3), a.F(0), a.F(1), a.F(2)}, {a.F(3), a.F(4), a.F(5), a.F(6)}};
+    ForceCoef fc = a.fc;
+    fc.geo = geo ? (*geo)[q].geo[2] : nullptr;
+    TRY_R(launch_forcing_adjoint(a.hb, 1, 0, pin, fc));
+    fc.geo = geo ? (*geo)[q].geo[3] : nullptr;
+    TRY_R(launch_forcing_adjoint(a.hb, 1, 1, field, fc));
+  }
+  return 0;
+}
+
+// the part of a step before the body moved, transposed (the geometry and
+// kinematics the step started with)
+int adjoint_step_first(std::vector<AdjBlock>& B, std::vector<IfaceMasks>& M, const bcfd_step_config& c, double tol,
+                       int64_t itmax, const std::vector<StepGeo>* geo) {
   std::vector<AdjBlock*> fine, first;
   for (AdjBlock& a : B) (a.hb->is_coarse ? first : fine).push_back(&a);
   auto tb = [](AdjBlock& a) {
     return std::array<double*, 3>{a.F(4), a.F(5), a.F(6)};
   };
-  // pressureForcingField, velocityForcingField, pressureForcing1
-  for (AdjBlock& a : B) {
+  // pressureForcing1
+  for (size_t q = 0; q < B.size(); ++q) {
+    AdjBlock& a = B[q];
     if (!a.body) continue;
     const AdjPtrs pin{{a.F(3), a.F(1), a.F(2), a.F(3)}, {a.F(3), a.F(1), a.F(2), a.F(3)}};
-    const AdjPtrs field{{a.F(3), a.F(0), a.F(1), a.F(2)}, {a.F(3), a.F(4), a.F(5), a.F(6)}};
-    TRY_R(launch_forcing_adjoint(a.hb, 1, 0, pin, a.fc));
-    TRY_R(launch_forcing_adjoint(a.hb, 1, 1, field, a.fc));
-    TRY_R(launch_forcing_adjoint(a.hb, 0, 0, pin, a.fc));
+    ForceCoef fc = a.fc;
+    fc.geo = geo ? (*geo)[q].geo[0] : nullptr;
+    TRY_R(launch_forcing_adjoint(a.hb, 0, 0, pin, fc));
   }
   // coarseUpdate (u,v,w,p) and fineUpdate_bd_mv (u,v,w,p), reversed
   const int f_of[4] = {3, 0, 1, 2};  // comp 0 p, 1 u, 2 v, 3 w -> state field
@@ -452,14 +478,17 @@ int adjoint_step(std::vector<AdjBlock>& B, std::vector<IfaceMasks>& M, const bcf
   for (auto m = M.rbegin(); m != M.rend(); ++m)
     for (int comp = 3; comp >= 1; --comp) TRY_R(face_fill_adj(*m, comp, m->b->F(3 + comp), m->a->F(3 + comp)));
   // per block: velocityBC, [velocityForcing1, solidCellBC], velocityBC, reversed
-  for (AdjBlock& a : B) {
+  for (size_t q = 0; q < B.size(); ++q) {
+    AdjBlock& a = B[q];
     auto t = tb(a);
     double* tt[3] = {t[0], t[1], t[2]};
     const Fields4 s{a.F(0), a.F(1), a.F(2), a.F(3)};
     if (a.hb->is_coarse) TRY_R(launch_vbc_adj(a.hb, c.deltat, c.uc, tt, s, a.ucl));
     if (a.body) {
       const AdjPtrs vin{{a.F(3), a.F(4), a.F(5), a.F(6)}, {a.F(3), a.F(4), a.F(5), a.F(6)}};
-      TRY_R(launch_forcing_adjoint(a.hb, 0, 1, vin, a.fc));
+      ForceCoef fc = a.fc;
+      fc.geo = geo ? (*geo)[q].geo[1] : nullptr;
+      TRY_R(launch_forcing_adjoint(a.hb, 0, 1, vin, fc));
       const int64_t ni = (int64_t)a.hb->d.d.nx * a.hb->d.d.ny * a.hb->d.d.nz;
       k_solid_adj<<<grid_for(ni, 256), 256, 0, stream()>>>(a.hb->d, a.F(4), a.F(5), a.F(6), a.F(3));
       BCFD_LAUNCHED();
@@ -477,6 +506,12 @@ int adjoint_step(std::vector<AdjBlock>& B, std::vector<IfaceMasks>& M, const bcf
     BCFD_LAUNCHED();
   }
   return 0;
+}
+
+int adjoint_step(std::vector<AdjBlock>& B, std::vector<IfaceMasks>& M, const bcfd_step_config& c, double tol,
+                 int64_t itmax) {
+  TRY_R(adjoint_step_second(B, nullptr));
+  return adjoint_step_first(B, M, c, tol, itmax, nullptr);
 }
 
 // the registered blocks in registration order
@@ -499,6 +534,94 @@ struct DevMem {
     ptrs.push_back(p);
     return static_cast<T*>(p);
   }
+};
+
+// ---- moving bodies -----------------------------------------------------------
+constexpr int kCalls = 6;  // forcing calls of a step, index 2 * mode + vel
+
+// what a recomputed step leaves for the transposes, for the moving body: the
+// tags and nodes after the step (its end geometry), the host motion state,
+// and the geometric partials of its forcing calls
+struct BodyRec {
+  int8_t* cell = nullptr;
+  int8_t* cell2 = nullptr;
+  int8_t* ntag = nullptr;
+  double* nodes = nullptr;
+  Kin kin{};
+  MotionStage stage{};
+  BodyMotion motion{};
+  double node_rmax = 0.0;
+  double* geo[kCalls] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  int64_t nt[kCalls] = {0, 0, 0, 0, 0, 0};
+};
+
+int save_body(HostBlock* hb, BodyRec& r, DevMem& mem) {
+  const DevBlock& D = hb->d;
+  const size_t np = (size_t)D.d.npts(), np3 = (size_t)D.d.npts3(), nn = (size_t)D.nn;
+  if (!r.cell) {
+    r.cell = mem.get<int8_t>(np);
+    r.cell2 = mem.get<int8_t>(np3);
+    r.ntag = mem.get<int8_t>(np3);
+    r.nodes = mem.get<double>(3 * nn);
+    if (!r.cell || !r.cell2 || !r.ntag || !r.nodes) return BCFD_E_NOMEM;
+  }
+  ACK(cudaMemcpyAsync(r.cell, D.cell, np, cudaMemcpyDeviceToDevice, stream()));
+  ACK(cudaMemcpyAsync(r.cell2, D.cell2, np3, cudaMemcpyDeviceToDevice, stream()));
+  ACK(cudaMemcpyAsync(r.ntag, D.nodeTag, np3, cudaMemcpyDeviceToDevice, stream()));
+  ACK(cudaMemcpyAsync(r.nodes, D.xnode1, nn * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
+  ACK(cudaMemcpyAsync(r.nodes + nn, D.ynode1, nn * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
+  ACK(cudaMemcpyAsync(r.nodes + 2 * nn, D.znode1, nn * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
+  r.kin = hb->kin;
+  r.stage = hb->stage;
+  r.motion = hb->motion;
+  r.node_rmax = hb->node_rmax;
+  return 0;
+}
+
+// the body's state after a recorded step: tags, nodes, kinematics and motion,
+// then what follows from them (normals, lists and masks, normal distances,
+// thin-surface list)
+int restore_body(HostBlock* hb, const BodyRec& r) {
+  DevBlock& D = hb->d;
+  const size_t np = (size_t)D.d.npts(), np3 = (size_t)D.d.npts3(), nn = (size_t)D.nn;
+  ACK(cudaMemcpyAsync(D.cell, r.cell, np, cudaMemcpyDeviceToDevice, stream()));
+  ACK(cudaMemcpyAsync(D.cell2, r.cell2, np3, cudaMemcpyDeviceToDevice, stream()));
+  ACK(cudaMemcpyAsync(D.nodeTag, r.ntag, np3, cudaMemcpyDeviceToDevice, stream()));
+  ACK(cudaMemcpyAsync(const_cast<double*>(D.xnode1), r.nodes, nn * sizeof(double), cudaMemcpyDeviceToDevice,
+                      stream()));
+  ACK(cudaMemcpyAsync(const_cast<double*>(D.ynode1), r.nodes + nn, nn * sizeof(double), cudaMemcpyDeviceToDevice,
+                      stream()));
+  ACK(cudaMemcpyAsync(const_cast<double*>(D.znode1), r.nodes + 2 * nn, nn * sizeof(double),
+                      cudaMemcpyDeviceToDevice, stream()));
+  hb->kin = r.kin;
+  hb->stage = r.stage;
+  hb->staged = false;
+  hb->motion = r.motion;
+  hb->node_rmax = r.node_rmax;
+  TRY_R(upload_kin(hb));
+  TRY_R(launch_surface_norm(hb, hb->inor));
+  TRY_R(launch_cellcount(hb, false));
+  TRY_R(launch_norm_distance(hb));
+  return launch_find_ts(hb);
+}
+
+// the recorder of a segment's recomputation: per step, the geometric
+// partials of the moving body's forcing calls
+struct MoveRecorder : ForceRecorder {
+  HostBlock* body = nullptr;
+  BodyRec* cur = nullptr;
+  DevMem* mem = nullptr;
+  double* sc = nullptr;
+  bool oom = false;
+  double* slot(HostBlock* hb, int mode, int vel, int64_t nt) override {
+    if (hb != body || !cur || nt <= 0) return nullptr;
+    const int c = 2 * mode + vel;
+    cur->nt[c] = nt;
+    cur->geo[c] = mem->get<double>(6 * (size_t)nt);
+    if (!cur->geo[c]) oom = true;
+    return cur->geo[c];
+  }
+  double* scratch(HostBlock* hb) override { return hb == body ? sc : nullptr; }
 };
 
 }  // namespace

@@ -10,7 +10,9 @@
 namespace bcfd {
 
 // the double overloads stay visible beside the dual ones
+using ::cos;
 using ::fabs;
+using ::sin;
 using ::sqrt;
 
 template <int N>
@@ -99,6 +101,23 @@ __host__ __device__ __forceinline__ DualN<N> sqrt(const DualN<N>& a) {
   const double h = r.v > 0.0 ? 0.5 / r.v : 0.0;
 #pragma unroll
   for (int q = 0; q < N; ++q) r.d[q] = a.d[q] * h;
+  return r;
+}
+
+template <int N>
+__host__ __device__ __forceinline__ DualN<N> sin(const DualN<N>& a) {
+  DualN<N> r(::sin(a.v));
+  const double c = ::cos(a.v);
+#pragma unroll
+  for (int q = 0; q < N; ++q) r.d[q] = a.d[q] * c;
+  return r;
+}
+template <int N>
+__host__ __device__ __forceinline__ DualN<N> cos(const DualN<N>& a) {
+  DualN<N> r(::cos(a.v));
+  const double sn = -::sin(a.v);
+#pragma unroll
+  for (int q = 0; q < N; ++q) r.d[q] = a.d[q] * sn;
   return r;
 }
 

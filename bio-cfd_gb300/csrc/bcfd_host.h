@@ -25,6 +25,11 @@ struct BodyMotion {
   // share (radians; 0 = the reference's single-phase kinematics) and the
   // shared pitch phase angle its initial placement is taken against
   double lag = 0, lag_phase = 0;
+  // the initial placement's inputs (shiftSurfaceNodesInitial) and the pitch
+  // amplitude as given in degrees, for the replay of the motion in the adjoint
+  bool placed = false;
+  double init_aoa = 0, init_piv_pt = 0, init_dxmin = 0, init_totime = 0, a0_deg = 0;
+  int64_t init_ita = 0;
 };
 
 // Node placement of one step (computeSurfaceVariables): the rotation's
@@ -362,7 +367,7 @@ struct ForceCoef {
   double* gk;  // kKinScalars accumulators: dJ/d(kinematic scalar p)
   int* elem;         // per task: its element (0-based)
   const double* geo; // per task: 6 geometric partials recorded forward (nullptr: geometry fixed)
-  double* ge;        // per element: 6 accumulators dJ/d(centroid, unit normal) (with geo)
+  double* ge;        // per element: 7 accumulators dJ/d(centroid, unit normal, length) (with geo)
 };
 // the 8 rigid-body kinematic scalars of a block, in bcfd_block_set_kinematics order
 __host__ __device__ inline double& kin_scalar(Kin& K, int p) {
@@ -387,6 +392,23 @@ struct AdjPtrs {
 int launch_stress_kin(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double* gk,
                       double* scratch);
 int launch_forcing_adjoint(HostBlock* hb, int mode, int vel, const AdjPtrs& a, const ForceCoef& fc);
+int launch_stress_geo(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double w, double* ge,
+                      double* scratch);
+
+// ---- adjoint through moving geometry (bcfd_adjoint_motion.cu) ----
+constexpr int kMotionParams = 5;  // yamp, a0 (deg), phase angle (rad), freq, bfreq
+// derivatives of one step's placement (rotation angle, y translation) and
+// kinematic scalars with respect to the motion parameters
+struct StepTangent {
+  double angle[kMotionParams];
+  double ty[kMotionParams];
+  double kin[kKinScalars][kMotionParams];
+};
+int motion_tangent(const HostBlock* hb, double phase_angle, double freq, double deltat, double tot_at_ita0,
+                   int64_t ita0, int64_t last, std::vector<StepTangent>& out);
+int build_node_csr(HostBlock* hb, std::vector<int>& off, std::vector<int>& ent);
+int launch_geometry_place_adj(HostBlock* hb, const double* ge, const int* off_dev, const int* ent_dev,
+                              const Place& P, double* scratch, double* place_bar);
 int launch_stress_weights(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double* w,
                           double* scratch);
 

@@ -603,7 +603,7 @@ __global__ void k_force_rev(DevBlock B, int vel, ForceCoef fc, AdjPtrs a) {
     for (int p = 0; p < kKinScalars; ++p) fc.gk[p] += fc.kc[kKinScalars * (int64_t)t + p] * o;
     if (fc.geo) {
       const int e = fc.elem[t];
-      for (int l = 0; l < 6; ++l) fc.ge[6 * (int64_t)e + l] += fc.geo[6 * (int64_t)t + l] * o;
+      for (int l = 0; l < 6; ++l) fc.ge[7 * (int64_t)e + l] += fc.geo[6 * (int64_t)t + l] * o;
     }
   }
 }

@@ -95,6 +95,13 @@ int shift_surface_nodes_initial(HostBlock* hb, double aoa, double piv_pt, int64_
                                 double dxmin, double totime) {
   BodyMotion& m = hb->motion;
   const double pi = 4.0 * std::atan(1.0);
+  m.placed = true;
+  m.init_aoa = aoa;
+  m.init_piv_pt = piv_pt;
+  m.init_dxmin = dxmin;
+  m.init_totime = totime;
+  m.init_ita = ita;
+  m.a0_deg = m.a0;
   // a lagging body starts where its lagged kinematics put it at t = 0 relative
   // to the shared ones: its angle differs by the pitch's change over the lag,
   // its heave position is yamp sin(-lag) (both 0 without a lag)

@@ -7,6 +7,7 @@
 #include <cstdio>
 
 #include "bcfd_host.h"
+#include "bcfd_dual.cuh"
 
 namespace bcfd {
 
@@ -278,7 +279,150 @@ __global__ void k_stress_sum(const double* part, int ne, double* out) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Geometric partials of the drag/lift objective (adjoint through moving
+// bodies): the derivatives of sum_t seed[t] C_t with respect to each
+// element's centroid (lanes 0-2), unit normal (3-5) and element length (6),
+// at the current fields, with every bracket and branch of the forward
+// evaluation held fixed.  C_t = 2 S_t / aS_t with S_t the sum of the element
+// terms and aS the projected-area sums, so an element moves both S_t and aS.
+// ---------------------------------------------------------------------------
+using G7 = DualN<7>;
+
+__device__ __forceinline__ G7 bil_g(const G7& x, const G7& y, double x1, double x2, double y1, double y2, double f0,
+                                    double f1, double f2, double f3) {
+  const G7 numer = f0 * (x2 - x) * (y2 - y) + f2 * (x2 - x) * (y - y1) + f1 * (x - x1) * (y2 - y) +
+                   f3 * (x - x1) * (y - y1);
+  return numer / ((x2 - x1) * (y2 - y1));
+}
+__device__ __forceinline__ G7 der_g(const G7& x, double x2, double x1, const G7& p_x, const G7& p_x2,
+                                    const G7& p_x1) {
+  const G7 h2 = fabs(x2 - x), h1 = fabs(x1 - x);
+  return (h1 * h1 * p_x2 - h2 * h2 * p_x1 + (h2 * h2 - h1 * h1) * p_x) / (h1 * h2 * (h1 + h2) + 1e-16);
+}
+__device__ void vad_eval_g(const G7& x, const G7& y, const G7& z, const double* xg, const double* yg,
+                           const double* zg, const int ijk[3], const double f[8], G7& val, G7 d3[3]) {
+  const int i = ijk[0], j = ijk[1], k = ijk[2];
+  const double yj = yg[j - 1], yj1 = yg[j], zk = zg[k - 1], zk1 = zg[k], xi = xg[i - 1], xi1 = xg[i];
+  const G7 t11 = bil_g(y, z, yj, yj1, zk, zk1, f[0], f[2], f[4], f[6]);
+  const G7 t12 = bil_g(y, z, yj, yj1, zk, zk1, f[1], f[3], f[5], f[7]);
+  const G7 t21 = bil_g(x, z, xi, xi1, zk, zk1, f[0], f[1], f[4], f[5]);
+  const G7 t22 = bil_g(x, z, xi, xi1, zk, zk1, f[2], f[3], f[6], f[7]);
+  const G7 t31 = bil_g(x, y, xi, xi1, yj, yj1, f[0], f[1], f[2], f[3]);
+  const G7 t32 = bil_g(x, y, xi, xi1, yj, yj1, f[4], f[5], f[6], f[7]);
+  val = t11 + (x - xi) * (t12 - t11) / (xi1 - xi);
+  d3[0] = der_g(x, xi1, xi, val, t12, t11);
+  d3[1] = der_g(y, yj1, yj, val, t22, t21);
+  d3[2] = der_g(z, zk1, zk, val, t32, t31);
+}
+
+// elem_terms with the element's geometry seeded: o[0..3] the four terms,
+// o[4] a_xz, o[5] a_yz
+__device__ void elem_terms_geo(const DevBlock& B, int e, double mu_f, double rho_f, const ElemStencil& S,
+                               const double f[4][8], G7 o[6]) {
+  const G7 cx = G7::seed(B.xcent[e], 0), cy = G7::seed(B.ycent[e], 1), cz = G7::seed(B.zcent[e], 2);
+  const G7 nrm[3] = {G7::seed(B.cosA[e], 3), G7::seed(B.cosB[e], 4), G7::seed(B.cosG[e], 5)};
+  const G7 alen = G7::seed(B.elen[e], 6);
+  const double nd = S.diag, diag = S.diag;
+  const G7 px = cx + nd * nrm[0], py = cy + nd * nrm[1], pz = cz + nd * nrm[2];
+  const int sid = B.surf_id[e];
+  const Kin& K = *B.kin;
+  const double td = sid == 51 ? K.thetaDot1 : (sid == 52 ? K.thetaDot2 : 0.0);
+  const double tdd = sid == 51 ? K.thetaDDot1 : (sid == 52 ? K.thetaDDot2 : 0.0);
+  const G7 us(K.xdot);
+  const G7 vs = -td * (cz - K.piv_z) + K.ydot;
+  const G7 ws = td * (cy - K.piv_y);
+  const G7 ac_z = -(td * td) * (cz - K.piv_z);
+  const G7 ac_y = -(td * td) * (cy - K.piv_y);
+  const G7 at_z = tdd * (cy - K.piv_y);
+  const G7 at_y = -tdd * (cz - K.piv_z);
+  const G7 dpdn = -((ac_z + at_z) * nrm[2] + (ac_y + at_y) * nrm[1]) - K.yddot * nrm[1];
+  G7 val, g[3], ddn[3];
+  vad_eval_g(px, py, pz, B.xu, B.yu, B.zu, S.ijk[0], f[0], val, g);
+  ddn[0] = (2.0 / nd) * (val - us) - (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]);
+  vad_eval_g(px, py, pz, B.xv, B.yv, B.zv, S.ijk[1], f[1], val, g);
+  ddn[1] = (2.0 / nd) * (val - vs) - (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]);
+  vad_eval_g(px, py, pz, B.xw, B.yw, B.zw, S.ijk[2], f[2], val, g);
+  ddn[2] = (2.0 / nd) * (val - ws) - (g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2]);
+  const G7 area = alen / 2.0;
+  o[5] = 0.5 * fabs(alen * nrm[0]);
+  o[4] = 0.5 * fabs(alen * nrm[1]);
+  const G7 dd = ddn[0] * nrm[0] + ddn[1] * nrm[1] + ddn[2] * nrm[2];
+  o[0] = (ddn[0] - dd * nrm[0]) * mu_f * area;
+  o[2] = (ddn[1] - dd * nrm[1]) * mu_f * area;
+  vad_eval_g(px, py, pz, B.xp, B.yp, B.zp, S.ijk[3], f[3], val, g);
+  const G7 dpdn_e = g[0] * nrm[0] + g[1] * nrm[1] + g[2] * nrm[2];
+  const G7 cval = val - (dpdn_e + dpdn) * diag * 0.5;
+  o[1] = -cval * area * nrm[0] * rho_f;
+  o[3] = -cval * area * nrm[1] * rho_f;
+}
+
+// sums[0..3] = S_t, sums[4] = aSx, sums[5] = aSy of the current evaluation
+// (k_stress_sum's reduction order)
+__global__ void k_stress_sums(const double* part, int ne, double* sums) {
+  __shared__ double s[7][256];
+  for (int q = 0; q < 7; ++q) {
+    double acc = 0.0;
+    for (int e = threadIdx.x; e < ne; e += blockDim.x) acc += part[7 * (int64_t)e + q];
+    s[q][threadIdx.x] = acc;
+  }
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w)
+      for (int q = 0; q < 7; ++q) s[q][threadIdx.x] += s[q][threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    for (int q = 0; q < 4; ++q) sums[q] = s[q][0];
+    sums[4] = 0.5 * s[5][0];
+    sums[5] = 0.5 * s[6][0];
+  }
+}
+
+// ge[7e + l] += w * d(sum_t seed[t] C_t)/d(geometry lane l of element e)
+__global__ void k_stress_geo(DevBlock B, double mu_f, double rho_f, const double* seed, const double* sums,
+                             double w, double* ge) {
+  const double* arr[4] = {B.u, B.v, B.w, B.p};
+  const double aS[4] = {sums[4], sums[5], sums[4], sums[5]};
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < B.ne; e += gridDim.x * blockDim.x) {
+    const ElemStencil S = elem_stencil(B, e);
+    double f[4][8];
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+#pragma unroll
+      for (int q = 0; q < 8; ++q) f[c][q] = arr[c][S.pos[c][q]];
+    G7 o[6];
+    elem_terms_geo(B, e, mu_f, rho_f, S, f, o);
+    for (int l = 0; l < 7; ++l) {
+      double g = 0.0;
+      for (int t = 0; t < 4; ++t) {
+        // d aS_t = 0.5 d(a_xz or a_yz) of this element
+        const double daS = 0.5 * ((t & 1) ? o[5].d[l] : o[4].d[l]);
+        g += seed[t] * 2.0 * (o[t].d[l] / aS[t] - sums[t] / (aS[t] * aS[t]) * daS);
+      }
+      ge[7 * (int64_t)e + l] += w * g;
+    }
+  }
+}
+
 }  // namespace
+
+// ge (7 per element) += w * the geometric derivative of sum_t seed[t] * C_t at
+// the block's current fields and geometry; scratch: 7 ne + 8 doubles
+int launch_stress_geo(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double w, double* ge,
+                      double* scratch) {
+  const int ne = hb->d.ne;
+  if (ne <= 0) return BCFD_E_STATE;
+  double* part = scratch;
+  double* sums = scratch + 7 * (size_t)ne;
+  k_stress_elem<<<grid_for(ne, 128), 128, 0, stream()>>>(hb->d, mu_f, rho_f, part);
+  TRY_R(note_launch());
+  k_stress_sums<<<1, 256, 0, stream()>>>(part, ne, sums);
+  TRY_R(note_launch());
+  k_stress_geo<<<grid_for(ne, 64), 64, 0, stream()>>>(hb->d, mu_f, rho_f, seed_dev, sums, w, ge);
+  TRY_R(note_launch());
+  return 0;
+}
 
 // w (4 fields, natural layout) += the gradient of sum_t seed[t] * coefficient t
 // with respect to (u, v, w, p) at the block's geometry (the coefficients are

@@ -368,9 +368,15 @@ def headline(args, torch, local, world):
                      "share": {k: v / step_ms for k, v in prof["phases_ms"].items()} if step_ms > 0 else {},
                      "note": "one eagerly issued step of the flagship path (CUDA events at phase boundaries on "
                              "the library stream); its total exceeds a graph replay by the launch gaps"}
-    traffic = profile_value("k_sor_dc_set_tandem.md", "traffic_bytes_per_launch")
+    # DRAM bytes per launch: the ratio of DRAM traffic to algorithmic bytes of
+    # the solve launches of one step of this workload (one ncu capture, the
+    # committed summary) times this run's algorithmic bytes per launch
+    ratio = profile_value("k_sor_dc_tandem_dram.md", "traffic_over_algorithmic")
+    per_launch = prof["sor_bytes"] / prof["sor_launches"] if prof["sor_launches"] else 0.0
+    traffic = ratio * per_launch if ratio is not None else None
     out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                        "frac": achieved / hbm, "traffic": traffic,
+                       "traffic_over_algorithmic": ratio,
                        "kernel": "mixed Poisson solve launches (k_sor_dc_set / k_sor_dc, as autotuned)",
                        "peak_source": peak_kind,
                        "launches": prof["sor_launches"], "ms": prof["sor_ms"], "bytes": prof["sor_bytes"],
@@ -596,7 +602,25 @@ def profile_run(args):
     them); prints the per-step time and the phase split of the last step."""
     import torch
     from biocfd import synth
+    from biocfd._lib import check
     torch.cuda.set_device(0)
+    if args.profile_case == "sweeps":
+        # FP64 sweeps of one body-free 384x256x256 block (25.2M cells): one
+        # launch of 8 sweep pairs with the reference's arithmetic, then one
+        # division-free, no autotuner
+        case = synth.uniform_block((384, 256, 256), noise=True)
+        s = new_solver(case, 0, tune=False)
+        g = s.handles[0]
+        check(s.L.bcfd_cellcount_solid(g), "cellcount_solid")
+        check(s.L.bcfd_compute_div(g), "compute_div")
+        out = {}
+        for key, prec in (("fp64_reference_sweeps", 0), ("fp64_division_free", 2)):
+            s.profile_begin()
+            check(s.L.bcfd_block_sor_sweeps(g, 8, prec), "sor_sweeps")
+            out[key] = s.profile_end()
+        print(json.dumps({"profile_case": "sweeps", "sweep_pairs": 8, "solve_log": out}), flush=True)
+        s.close()
+        return
     if args.profile_case == "tandem":
         case = synth.tandem_plates(n_steps=args.profile_steps + 2, moving=True)
     else:  # one 256x192x192 block with a plate: the fine-block size, ~1 GB on the device
@@ -619,6 +643,8 @@ def profile_run(args):
             prof = s.profile_end()
     print(json.dumps({"profile_case": args.profile_case, "ms_per_step": ts, "phases_ms": s.profile_phases(),
                       "kernel_launches_last_step": prof["kernel_launches"],
+                      "solve_log_last_step": {k: prof[k] for k in ("sor_launches", "sor_ms", "sor_bytes",
+                                                                   "sor_sweeps")},
                       "counts": [s.counts(g) for g in s.handles]}), flush=True)
     s.close()
 
@@ -712,7 +738,7 @@ def main():
                     help="timed steps of the flagship with zero-started solves, beside the warm-started value")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiler mode: set up without the autotuner and run this many eager mixed steps")
-    ap.add_argument("--profile-case", default="tandem", choices=["tandem", "block256"])
+    ap.add_argument("--profile-case", default="tandem", choices=["tandem", "block256", "sweeps"])
     args = ap.parse_args()
     global WARM_START
     WARM_START = not args.zero_start

@@ -65,8 +65,12 @@ _SIGS = {
     "bcfd_coupling_apply": [c_i64, c_int, c_int, P_d, P_d],
     "bcfd_momentum_tangent": [c_i64, c_double, c_double, P_d, P_d, P_d, P_d, P_d, P_d, P_d, P_d, P_d, P_d],
     "bcfd_momentum_adjoint": [c_i64, c_double, c_double, P_d, P_d, P_d, P_d, P_d, P_d, P_d],
+    "bcfd_momentum_adjoint_ts": [c_i64, c_double, c_double, P_d, P_d, P_d, P_d, P_d, P_d, P_d, P_d],
+    "bcfd_forcing_ghost_adjoint": [c_i64, P_d, P_d, P_d, P_d, P_d, P_d, P_d, P_d],
     "bcfd_adjoint_run": [c_i64, C.POINTER(StepConfig), c_i64, c_i64, P_d, P_d, P_d, P_d, P_d, c_double, c_double,
                          c_double, c_i64, P_d, P_d, P_d, P_d, P_d, P_d, P_d],
+    "bcfd_adjoint_run_motion": [c_i64, C.POINTER(StepConfig), c_i64, c_i64, P_d, P_d, P_d, P_d, P_d, c_double,
+                                c_double, c_double, c_i64, P_d, P_d, P_d, P_d, P_d, P_d, P_d],
     "bcfd_block_set_body_motion": [c_i64, P_d],
     "bcfd_shift_surface_nodes_initial": [c_i64, c_double, c_double, c_i64, c_double, c_double, c_double],
     "bcfd_block_set_body_lag": [c_i64, c_double, c_double],
@@ -101,6 +105,7 @@ _SIGS = {
     "bcfd_block_get_sor_stats": [c_i64, P_i64, P_d, P_d],
     "bcfd_block_set_sor_iter": [c_i64, c_i64],
     "bcfd_block_read": [c_i64, C.c_char_p, C.c_void_p, c_i64, P_i64],
+    "bcfd_block_write": [c_i64, C.c_char_p, P_d, c_i64],
     "bcfd_non_uni_coeff": [c_i64], "bcfd_coefficient_matrix": [c_i64, c_int],
     "bcfd_ns_momentum_2order": [c_i64, c_double, c_double],
     "bcfd_velocity_bc": [c_i64, c_double, c_double],

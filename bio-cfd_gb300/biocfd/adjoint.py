@@ -1,12 +1,19 @@
-"""Adjoint of the pressure Poisson solve as a torch.autograd.Function.
+"""Discrete adjoints of the solver as host calls and torch.autograd.Functions.
 
-forward:  x = A^{-1} r      (bcfd_poisson_solve_zero_bc)
-backward: r_bar = A^{-T} x_bar (bcfd_poisson_solve_adjoint: the same SOR kernel
-          with the transposed line tables and reversed colour order)
-
+The Poisson solve:
+  forward:  x = A^{-1} r      (bcfd_poisson_solve_zero_bc)
+  backward: r_bar = A^{-T} x_bar (bcfd_poisson_solve_adjoint: the same SOR
+            kernel with the transposed line tables and reversed colour order)
 A is the Poisson operator of one block restricted to its fluid cells (zero
-data on the other cells).  Arrays are natural-layout (nx+2, ny+2, nz+2) FP64,
-x-fastest, like the block's fields.
+data on the other cells).
+
+Whole runs of time steps: adjoint_run (fixed geometry), adjoint_run_motion
+(one moving body, gradients with respect to its motion parameters) and
+run_function, which wraps either as a torch.autograd.Function of the initial
+state and the scalar parameters.
+
+Arrays are natural-layout (nx+2, ny+2, nz+2) FP64, x-fastest, like the
+block's fields.
 """
 from __future__ import annotations
 
@@ -133,3 +140,85 @@ def adjoint_run(solver, weights: dict, n_steps: int, every: int = 20, uc: float 
     out = dict(zip(("u", "v", "w", "p"), grads))
     out["kin"] = kin
     return J.value, duc.value, out
+
+
+# the motion parameters of adjoint_run_motion, in the units of synth.Motion /
+# synth.MotionInputs (the C ABI's phase is in radians)
+MOTION_PARAMS = ("yamp", "a0_deg", "phase_deg", "freq", "bfreq")
+
+
+def adjoint_run_motion(solver, weights: dict, n_steps: int, every: int = 20, block: int = 0, uc: float | None = None,
+                       gradient: bool = True, adj_tol: float = 1e-13, adj_itmax: int = 200000, stress_seed=None,
+                       mu_f: float = 1.0, rho_f: float = 1.0):
+    """adjoint_run through a moving body (bcfd_adjoint_run_motion): J of
+    n_steps FP64 steps with the weights and drag/lift of block `block`, whose
+    body is the run's one moving body.  Returns J, or with `gradient`
+    (J, dJ/duc, {"u","v","w","p": dJ/dx^0 of the block, "motion": {name:
+    dJ/d name for MOTION_PARAMS}}).  The body's tags, nodes and motion state
+    are checkpointed with the fields; the block advances by n_steps exactly
+    as solver.run(n_steps) would.  A body with thin-surface cells (surfaces
+    51/52) is refused."""
+    c = solver.case
+    g = solver.handles[block]
+    shape = c.blocks[block].shape
+    W = [np.asfortranarray(weights.get(k, np.zeros(shape)), dtype=np.float64) for k in ("u", "v", "w", "p")]
+    cfg = solver.config(0)
+    if uc is not None:
+        cfg.uc = uc
+    P = C.POINTER(C.c_double)
+    J = C.c_double()
+    duc = C.c_double()
+    grads = [np.zeros(shape, order="F") for _ in range(4)] if gradient else None
+    dmot = np.zeros(5)
+    null = C.cast(None, P)
+    seed = None if stress_seed is None else np.ascontiguousarray(stress_seed, dtype=np.float64)
+    check(solver.L.bcfd_adjoint_run_motion(g, C.byref(cfg), n_steps, every, *(w.ctypes.data_as(P) for w in W),
+                                           null if seed is None else seed.ctypes.data_as(P), mu_f, rho_f,
+                                           adj_tol, adj_itmax, C.byref(J),
+                                           C.byref(duc) if gradient else null,
+                                           dmot.ctypes.data_as(P) if gradient else null,
+                                           *((a.ctypes.data_as(P) for a in grads) if gradient else (null,) * 4)),
+          "adjoint_run_motion")
+    if not gradient:
+        return J.value
+    dmot[2] *= np.pi / 180.0  # per radian -> per degree
+    out = dict(zip(("u", "v", "w", "p"), grads))
+    out["motion"] = dict(zip(MOTION_PARAMS, dmot))
+    return J.value, duc.value, out
+
+
+def run_function(make_solver, weights: dict, n_steps: int, every: int = 20, moving: bool = False, **kw):
+    """A torch.autograd.Function J = f(u0, v0, w0, p0, params) of n_steps FP64
+    time steps.  `params` is a float64 tensor: [uc], or with `moving`
+    [uc, yamp, a0_deg, phase_deg, freq, bfreq]; make_solver(list of params)
+    returns a set-up Solver for those values, and forward uploads the initial
+    state (tensors of block 0's point shape) to its block 0 before the run.
+    forward runs the forward steps and the reverse sweep in one call
+    (adjoint_run / adjoint_run_motion) and keeps the gradient; backward scales
+    it by the incoming gradient of J.  Remaining keywords go to the run
+    (stress_seed, mu_f, rho_f, adj_tol, ...)."""
+    import torch
+
+    class AdjointRun(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, u, v, w, p, params):
+            pv = [float(x) for x in params.detach().cpu().reshape(-1)]
+            s = make_solver(pv)
+            state = {k: np.asfortranarray(t.detach().cpu().numpy(), dtype=np.float64)
+                     for k, t in zip(("u", "v", "w", "p"), (u, v, w, p))}
+            s.upload_fields(s.handles[0], state)
+            if moving:
+                J, duc, g = adjoint_run_motion(s, weights, n_steps, every, uc=pv[0], **kw)
+                gpar = [duc] + [g["motion"][k] for k in MOTION_PARAMS]
+            else:
+                J, duc, g = adjoint_run(s, weights, n_steps, every, uc=pv[0], **kw)
+                gpar = [duc]
+            ctx.grads = [torch.from_numpy(np.ascontiguousarray(g[k])).to(u) for k in ("u", "v", "w", "p")]
+            ctx.gpar = torch.tensor(gpar, dtype=params.dtype, device=params.device)
+            return torch.tensor(J, dtype=torch.float64, device=u.device)
+
+        @staticmethod
+        def backward(ctx, gJ):
+            return (*(gJ * t for t in ctx.grads), gJ * ctx.gpar)
+
+    return AdjointRun

@@ -272,6 +272,31 @@ def moving_plate_single_block(n: int = 32, n_steps: int = 3, semi_axes=(0.25, 0.
     return case
 
 
+def heaving_sphere_single_block(n: int = 24, n_steps: int = 6, diameter: float = 0.3,
+                                center=(0.45, 0.5, 0.5), yamp: float = 0.05, bfreq: float = 0.5,
+                                a0_deg: float = 10.0, freq: float = 0.5, phase_deg: float = 90.0,
+                                piv_pt: float = 0.1, reynolds: float = 100.0, seed: int = SEED) -> Case:
+    """The sphere of sphere_single_block (surface 50) on the motion of
+    src/Search.F90:49-208: heave yamp sin(2 pi bfreq t), tow in -x by
+    0.05 dxmin per step, pitch a0 sin(2 pi freq t + phase) about x through
+    z = piv_pt.  Surface-50 nodes only translate, so the body has no
+    thin-surface cells and its IB cells are ordinary forcing cells."""
+    f = uniform_faces(0.0, 1.0, n)
+    dx = 1.0 / n
+    spec = BlockSpec(n, n, n, f, f.copy(), f.copy(), omega=1.7, is_coarse=True)
+    spec.mesh = fibonacci_sphere((0.0, 0.0, 0.0), diameter, dx)
+    spec.motion = Motion(a0_deg=a0_deg, bfreq=bfreq, yamp=yamp, shift=tuple(center))
+    c = np.asarray(center)
+    reach = np.full(3, 0.5 * diameter) + np.array([0.05 * dx * n_steps, yamp, 0.0])
+    spec.search_box = search_box_for(spec, c - reach, c + reach)
+    rng = np.random.default_rng(seed)
+    case = Case(name=f"heaving_sphere{n}", blocks=[spec], dt=0.3 * dx, re=reynolds / diameter, uc=1.0,
+                epsi=1e-6, pc_ita_max=5000, n_steps=n_steps)
+    case.motion = MotionInputs(aoa_deg=0.0, phase_deg=phase_deg, piv_pt=piv_pt, freq=freq, dxmin=dx)
+    case.init = [noisy_initial(spec, case.uc, rng)]
+    return case
+
+
 def sphere_two_block(nf: int = 64, n_steps: int = 200, diameter: float = 0.5,
                      reynolds: float = 300.0, omega_c: float = 1.7, omega_f: float = 1.7,
                      pc_ita_max: int = 5000, seed: int = SEED, coarse=(96, 64, 64),

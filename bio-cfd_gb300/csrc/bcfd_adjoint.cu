@@ -12,6 +12,8 @@
 // part of this entry point).
 #include <cstring>
 
+#include <algorithm>
+
 #include "bcfd_host.h"
 
 namespace bcfd {
@@ -204,6 +206,115 @@ int bcfd_momentum_adjoint(bcfd_handle h, double deltat, double re, const double*
   if (!r && cudaStreamSynchronize(stream()) != cudaSuccess) r = BCFD_E_CUDA;
   for (int q = 0; q < 4 && !r; ++q)
     if (d2h(outh[q], dab[q], np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
+  cudaFree(buf);
+  if (r) return r;
+  return take_block_error(hb);
+}
+
+int bcfd_momentum_adjoint_ts(bcfd_handle h, double deltat, double re, const double* utb, const double* vtb,
+                             const double* wtb, double* ub, double* vb, double* wb, double* pb, double* gb) {
+  LibLock lk;
+  HostBlock* hb = get_block(h);
+  if (!hb) return BCFD_E_HANDLE;
+  const double* in[3] = {utb, vtb, wtb};
+  double* io[4] = {ub, vb, wb, pb};
+  for (const double* p : in)
+    if (!p) return BCFD_E_ARG;
+  for (double* p : io)
+    if (!p) return BCFD_E_ARG;
+  if (!gb) return BCFD_E_ARG;
+  if (!hb->d.ca[0]) return BCFD_E_STATE;
+  int64_t cnt[N_COUNT];
+  if (d2h(cnt, hb->d.cnt, sizeof(cnt)) != cudaSuccess) return BCFD_E_CUDA;
+  const int64_t nts = std::min<int64_t>(cnt[C_TS], hb->d.cap_ib), cap = hb->d.cap_ib;
+  const size_t np = (size_t)hb->d.d.npts();
+  // 3 seeds, 4 adjoints, the overlay's scratch (7 ints and 14 doubles per
+  // point), the ghost adjoint, then the 16-word footprint
+  const size_t nd = 7 * np + 14 * np + 14 * (size_t)cap;
+  double* buf = nullptr;
+  int* last = nullptr;
+  if (cudaMalloc(&buf, nd * sizeof(double) + 64) != cudaSuccess) return BCFD_E_NOMEM;
+  if (cudaMalloc(&last, 7 * np * sizeof(int)) != cudaSuccess) {
+    cudaFree(buf);
+    return BCFD_E_NOMEM;
+  }
+  int r = 0;
+  const double* dsb[3];
+  double* dab[4];
+  for (int q = 0; q < 3 && !r; ++q) {
+    dsb[q] = buf + q * np;
+    if (h2d((void*)dsb[q], in[q], np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
+  }
+  for (int q = 0; q < 4 && !r; ++q) {
+    dab[q] = buf + (3 + q) * np;
+    if (h2d(dab[q], io[q], np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
+  }
+  MomTsAdj ts;
+  ts.last = last;
+  ts.contrib = buf + 7 * np;
+  ts.gb = buf + 21 * np;
+  ts.cap = cap;
+  if (!r && cudaMemsetAsync(ts.gb, 0, 14 * (size_t)cap * sizeof(double), stream()) != cudaSuccess) r = BCFD_E_CUDA;
+  if (!r) r = launch_momentum_adjoint(hb, deltat, re, dsb, dab, (uint32_t*)(buf + nd), &ts);
+  if (!r && cudaStreamSynchronize(stream()) != cudaSuccess) r = BCFD_E_CUDA;
+  for (int q = 0; q < 4 && !r; ++q)
+    if (d2h(io[q], dab[q], np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
+  for (int g = 0; g < 14 && !r && nts > 0; ++g)
+    if (d2h(gb + g * nts, ts.gb + g * cap, nts * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
+  cudaFree(last);
+  cudaFree(buf);
+  if (r) return r;
+  return take_block_error(hb);
+}
+
+int bcfd_forcing_ghost_adjoint(bcfd_handle h, const double* gb, double* ub, double* vb, double* wb, double* pb,
+                               double* utb, double* vtb, double* wtb) {
+  LibLock lk;
+  HostBlock* hb = get_block(h);
+  if (!hb) return BCFD_E_HANDLE;
+  double* io[7] = {ub, vb, wb, pb, utb, vtb, wtb};
+  if (!gb) return BCFD_E_ARG;
+  for (double* p : io)
+    if (!p) return BCFD_E_ARG;
+  if (!hb->has_body || hb->d.ne <= 0) return BCFD_E_STATE;
+  int64_t cnt[N_COUNT];
+  if (d2h(cnt, hb->d.cnt, sizeof(cnt)) != cudaSuccess) return BCFD_E_CUDA;
+  const int64_t nts = std::min<int64_t>(cnt[C_TS], hb->d.cap_ib), cap = hb->d.cap_ib;
+  const size_t np = (size_t)hb->d.d.npts(), ntask = 6 * (size_t)cap;
+  // 7 adjoint arrays, the ghost adjoint, the task coefficients
+  const size_t nd = 7 * np + 14 * (size_t)cap + 8 * ntask + kKinScalars * ntask + kKinScalars;
+  double* buf = nullptr;
+  void* ibuf = nullptr;
+  if (cudaMalloc(&buf, nd * sizeof(double)) != cudaSuccess) return BCFD_E_NOMEM;
+  if (cudaMalloc(&ibuf, ntask * (sizeof(int64_t) * 9 + sizeof(int))) != cudaSuccess) {
+    cudaFree(buf);
+    return BCFD_E_NOMEM;
+  }
+  int r = 0;
+  double* d[7];
+  for (int q = 0; q < 7 && !r; ++q) {
+    d[q] = buf + q * np;
+    if (h2d(d[q], io[q], np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
+  }
+  double* dg = buf + 7 * np;
+  if (!r && cudaMemsetAsync(dg, 0, 14 * (size_t)cap * sizeof(double), stream()) != cudaSuccess) r = BCFD_E_CUDA;
+  for (int g = 0; g < 14 && !r && nts > 0; ++g)
+    if (h2d(dg + g * cap, gb + g * nts, nts * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
+  ForceCoef fc{};
+  fc.coef = dg + 14 * cap;
+  fc.kc = fc.coef + 8 * ntask;
+  fc.gk = fc.kc + kKinScalars * ntask;
+  fc.pos = static_cast<int64_t*>(ibuf);
+  fc.tgt = fc.pos + 8 * ntask;
+  fc.axis = reinterpret_cast<int*>(fc.tgt + ntask);
+  // axis 0 p, 1..3 u/v/w (the t-ghost copies) and ut/vt/wt (the probes)
+  const AdjPtrs a{{d[3], d[0], d[1], d[2]}, {d[3], d[4], d[5], d[6]}};
+  if (!r) r = launch_ghost_adjoint(hb, 0, a, fc, dg, cap);
+  if (!r) r = launch_ghost_adjoint(hb, 1, a, fc, dg, cap);
+  if (!r && cudaStreamSynchronize(stream()) != cudaSuccess) r = BCFD_E_CUDA;
+  for (int q = 0; q < 7 && !r; ++q)
+    if (d2h(io[q], d[q], np * sizeof(double)) != cudaSuccess) r = BCFD_E_CUDA;
+  cudaFree(ibuf);
   cudaFree(buf);
   if (r) return r;
   return take_block_error(hb);

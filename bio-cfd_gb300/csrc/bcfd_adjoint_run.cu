@@ -251,7 +251,7 @@ __global__ void k_zero_fluid(DevBlock B, double* utb, double* vtb, double* wtb) 
     const int64_t r = t / d.nx;
     const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
     const int64_t c = d.idx(i, j, k);
-    if (B.cell[c] != 0 || B.tsnear[c]) continue;
+    if (B.cell[c] != 0) continue;
     utb[c] = 0.0;
     vtb[c] = 0.0;
     wtb[c] = 0.0;
@@ -324,6 +324,28 @@ int load_state(HostBlock* hb, const double* slot) {
   return 0;
 }
 
+// The ghost arrays (velocityForcingGhost / pressureForcingGhost, the last
+// calls of a step) are read by the next step's predictor.  At a step's end
+// they are a function of the state the step leaves and of the body's TS
+// list, so a loaded state regenerates them; at the run's start they are
+// whatever an earlier step or the caller left, and are saved.
+int save_ghosts(HostBlock* hb, double* slot) {
+  const size_t cap = (size_t)hb->d.cap_ib;
+  for (int g = 0; g < 14; ++g)
+    ACK(cudaMemcpyAsync(slot + g * cap, hb->d.ghost[g], cap * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
+  return 0;
+}
+int load_ghosts(HostBlock* hb, const double* slot) {
+  const size_t cap = (size_t)hb->d.cap_ib;
+  for (int g = 0; g < 14; ++g)
+    ACK(cudaMemcpyAsync(hb->d.ghost[g], slot + g * cap, cap * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
+  return 0;
+}
+int regen_ghosts(HostBlock* hb) {
+  TRY_R(launch_forcing_velocity(hb, 2));
+  return launch_forcing_pressure(hb, 2);
+}
+
 int launch_vbc_adj(HostBlock* hb, double dt, double uc, double* tb[3], const Fields4& s, double* ucl) {
   const Dims& d = hb->d.d;
   k_vbc_z_adj<<<grid_for((int64_t)d.nx * d.ny, 128), 128, 0, stream()>>>(hb->d, tb[0], tb[1], tb[2]);
@@ -344,11 +366,40 @@ struct AdjBlock {
   double* bb = nullptr;    // accumulated y of the block's solves (adjoint of b, times deltat)
   uint32_t* foot = nullptr;
   ForceCoef fc{};          // forcing coefficients and kinematic accumulators (body blocks)
+  MomTsAdj ts{};           // the thin-surface overlay's adjoint (body blocks)
   double* ucl = nullptr;   // dJ/duc per x-face line (coarse block)
   bool body = false;
   int64_t np = 0;
   double* F(int q) const { return A + q * np; }
 };
+
+// device allocations freed with the owner
+struct DevMem {
+  std::vector<void*> ptrs;
+  ~DevMem() {
+    for (void* p : ptrs) cudaFree(p);
+  }
+  template <typename T>
+  T* get(size_t n) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    return static_cast<T*>(p);
+  }
+};
+
+// the overlay's adjoint scratch of a body block (zeroed ghost adjoint)
+int alloc_ts_adj(AdjBlock& a, DevMem& mem) {
+  if (!a.body) return 0;
+  const int64_t cap = a.hb->d.cap_ib;
+  a.ts.last = mem.get<int>(7 * (size_t)a.np);
+  a.ts.contrib = mem.get<double>(14 * (size_t)a.np);
+  a.ts.gb = mem.get<double>(14 * (size_t)cap);
+  a.ts.cap = cap;
+  if (!a.ts.last || !a.ts.contrib || !a.ts.gb) return BCFD_E_NOMEM;
+  ACK(cudaMemsetAsync(a.ts.gb, 0, 14 * (size_t)cap * sizeof(double), stream()));
+  return 0;
+}
 
 // positions a coupling map overwrites, per interface and component: the fine
 // block's face-fill targets and the coarse block's restriction targets
@@ -404,8 +455,10 @@ struct StepGeo {
   const double* geo[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
 };
 
-// the part of a step after the body moved, transposed: pressureForcingField,
-// velocityForcingField (the geometry and kinematics of the step's end)
+// the part of a step after the body moved, transposed: pressureForcingGhost,
+// velocityForcingGhost (the ghost arrays the next step's predictor read),
+// pressureForcingField, velocityForcingField (the geometry and kinematics of
+// the step's end)
 int adjoint_step_second(std::vector<AdjBlock>& B, const std::vector<StepGeo>* geo) {
   for (size_t q = 0; q < B.size(); ++q) {
     AdjBlock& a = B[q];
@@ -413,6 +466,12 @@ int adjoint_step_second(std::vector<AdjBlock>& B, const std::vector<StepGeo>* ge
     const AdjPtrs pin{{a.F(3), a.F(1), a.F(2), a.F(3)}, {a.F(3), a.F(1), a.F(2), a.F(3)}};
     const AdjPtrs field{{a.F(3), a.F(0), a.F(1), a.F(2)}, {a.F(3), a.F(4), a.F(5), a.F(6)}};
     ForceCoef fc = a.fc;
+    if (a.ts.gb) {
+      fc.geo = geo ? (*geo)[q].geo[4] : nullptr;
+      TRY_R(launch_ghost_adjoint(a.hb, 0, field, fc, a.ts.gb, a.ts.cap));
+      fc.geo = geo ? (*geo)[q].geo[5] : nullptr;
+      TRY_R(launch_ghost_adjoint(a.hb, 1, field, fc, a.ts.gb, a.ts.cap));
+    }
     fc.geo = geo ? (*geo)[q].geo[2] : nullptr;
     TRY_R(launch_forcing_adjoint(a.hb, 1, 0, pin, fc));
     fc.geo = geo ? (*geo)[q].geo[3] : nullptr;
@@ -500,7 +559,7 @@ int adjoint_step_first(std::vector<AdjBlock>& B, std::vector<IfaceMasks>& M, con
     auto t = tb(a);
     const double* sb[3] = {t[0], t[1], t[2]};
     double* ab[4] = {a.F(0), a.F(1), a.F(2), a.F(3)};
-    TRY_R(launch_momentum_adjoint(a.hb, c.deltat, c.re, sb, ab, a.foot));
+    TRY_R(launch_momentum_adjoint(a.hb, c.deltat, c.re, sb, ab, a.foot, a.ts.gb ? &a.ts : nullptr));
     const int64_t ni = (int64_t)a.hb->d.d.nx * a.hb->d.d.ny * a.hb->d.d.nz;
     k_zero_fluid<<<grid_for(ni, 256), 256, 0, stream()>>>(a.hb->d, t[0], t[1], t[2]);
     BCFD_LAUNCHED();
@@ -521,20 +580,6 @@ std::vector<std::pair<bcfd_handle, HostBlock*>> registered_blocks() {
     if (lib().blocks[q]) v.push_back({(bcfd_handle)(q + 1), lib().blocks[q]});
   return v;
 }
-
-struct DevMem {
-  std::vector<void*> ptrs;
-  ~DevMem() {
-    for (void* p : ptrs) cudaFree(p);
-  }
-  template <typename T>
-  T* get(size_t n) {
-    void* p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) return nullptr;
-    ptrs.push_back(p);
-    return static_cast<T*>(p);
-  }
-};
 
 // ---- moving bodies -----------------------------------------------------------
 constexpr int kCalls = 6;  // forcing calls of a step, index 2 * mode + vel
@@ -703,6 +748,20 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
     ACK(cudaMemcpyAsync(b->d.wt, b->d.w, bytes, cudaMemcpyDeviceToDevice, stream()));
   }
   TRY_R(save_all(cps));
+  std::vector<double*> g0(nb, nullptr);
+  for (int q = 0; q < nb; ++q) {
+    HostBlock* b = all[q].second;
+    if (!b->has_body || b->d.ne <= 0) continue;
+    g0[q] = mem.get<double>(14 * (size_t)b->d.cap_ib);
+    if (!g0[q]) return BCFD_E_NOMEM;
+    TRY_R(save_ghosts(b, g0[q]));
+  }
+  // the ghost arrays of the state after step n (n = 0: the run's start)
+  auto ghosts_at = [&](int64_t n) -> int {
+    for (int q = 0; q < nb; ++q)
+      if (g0[q]) TRY_R(n == 0 ? load_ghosts(all[q].second, g0[q]) : regen_ghosts(all[q].second));
+    return 0;
+  };
   // the transpose assumes the tags the run starts with hold throughout
   // (stationary bodies: the per-step re-Search reproduces them)
   std::vector<std::vector<int8_t>> tags0(nb);
@@ -769,6 +828,7 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
     if (!a.A || !a.pcb || !a.y || !a.bb || !a.foot || !a.ucl || !a.fc.tgt || !a.fc.axis || !a.fc.pos ||
         !a.fc.coef || !a.fc.kc || !a.fc.gk)
       return BCFD_E_NOMEM;
+    TRY_R(alloc_ts_adj(a, mem));
     ACK(cudaMemsetAsync(a.A, 0, kStateFields * a.np * sizeof(double), stream()));
     ACK(cudaMemsetAsync(a.ucl, 0, (size_t)a.hb->d.d.ny * a.hb->d.d.nz * sizeof(double), stream()));
     ACK(cudaMemsetAsync(a.fc.gk, 0, kKinScalars * sizeof(double), stream()));
@@ -824,6 +884,7 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
     const double* cp = cps + (size_t)m * S;
     ACK(cudaMemcpyAsync(tape, cp, S * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
     TRY_R(load_all(cp));
+    TRY_R(ghosts_at(n0));
     L.ita = ita0 + n0;
     L.totime = tot0 + n0 * cfg->deltat;
     for (int64_t n = n0 + 1; n < n1; ++n) {
@@ -832,6 +893,7 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
     }
     for (int64_t n = n1; n > n0; --n) {
       TRY_R(load_all(tape + (size_t)(n - 1 - n0) * S));
+      TRY_R(ghosts_at(n - 1));
       TRY_R(adjoint_step(AB, M, c, adj_tol, adj_itmax));
       if (n - 1 >= 1) {
         k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, ah.A, 4 * np);
@@ -841,6 +903,7 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   }
   // leave the blocks at the forward run's final state
   TRY_R(load_all(fin));
+  TRY_R(ghosts_at(n_steps));
   L.ita = ita0 + n_steps;
   L.totime = tot0 + n_steps * cfg->deltat;
   // the run started from ut = u, vt = v, wt = w: their adjoints add up
@@ -858,6 +921,338 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
     for (double v : ul) duc += v;
   }
   if (dj_duc) *dj_duc = duc;
+  ACK(cudaStreamSynchronize(stream()));
+  for (auto& [g, b] : all) {
+    const int e = take_block_error(b);
+    if (e) return e;
+  }
+  return 0;
+}
+
+// The moving-body run: one moving body, on block h.  Forward as above, with
+// the body's tags, nodes and motion state checkpointed beside the fields.  In
+// reverse each segment is recomputed with the forcing recorder on (per step:
+// the forcing calls' geometric partials, the tags, nodes and motion state the
+// step leaves), then every step is transposed in two halves: the part after
+// the body moved with the step's end geometry and kinematics restored, then
+// the part before with the start's; after the first half the element-geometry
+// and kinematic adjoints of the end geometry are complete and go through the
+// nodes and the placement to the motion parameters.
+int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps, int64_t every,
+                            const double* wu, const double* wv, const double* ww, const double* wp,
+                            const double* stress_seed, double mu_f, double rho_f, double adj_tol, int64_t adj_itmax,
+                            double* J, double* dj_duc, double* dj_dmotion, double* gu, double* gv, double* gw,
+                            double* gp) {
+  LibLock lk;
+  HostBlock* hb = get_block(h);
+  if (!hb) return BCFD_E_HANDLE;
+  if (!cfg || n_steps < 1 || every < 1 || !wu || !wv || !ww || !wp || !J || !(adj_tol > 0.0) || adj_itmax < 1)
+    return BCFD_E_ARG;
+  if (cfg->precision != 0) return BCFD_E_STATE;
+  auto all = registered_blocks();
+  if (all.empty() || !all.front().second->is_coarse) return BCFD_E_STATE;
+  for (auto& [g, b] : all) {
+    if (!b->d.ca[0] || !b->d.Acx) return BCFD_E_STATE;
+    if (g != all.front().first && b->is_coarse) return BCFD_E_STATE;
+    if (b->motion.on && b != hb) return BCFD_E_STATE;  // one moving body, the objective's
+  }
+  if (!hb->motion.on || !hb->motion.placed || !hb->has_body || hb->d.ne <= 0 || hb->d.nn <= 0) return BCFD_E_STATE;
+  std::vector<HostInterface*> ifs;
+  for (HostInterface* it : lib().ifs)
+    if (it) ifs.push_back(it);
+  if (all.size() > 1 && ifs.empty()) return BCFD_E_STATE;
+  const bool use_stress = stress_seed != nullptr;
+  const int nb = (int)all.size();
+  int hidx = -1;
+  for (int q = 0; q < nb; ++q)
+    if (all[q].second == hb) hidx = q;
+  std::vector<int64_t> npb(nb), off(nb + 1, 0);
+  for (int q = 0; q < nb; ++q) {
+    npb[q] = all[q].second->d.d.npts();
+    off[q + 1] = off[q] + kStateFields * npb[q];
+  }
+  const size_t S = (size_t)off[nb];
+  const int64_t np = hb->d.d.npts();
+  const size_t fb = (size_t)np * sizeof(double);
+  const int64_t K = std::min(every, n_steps);
+  const int64_t ncp = (n_steps + K - 1) / K;
+  const int ne = hb->d.ne, nn = hb->d.nn;
+  DevMem mem;
+  double* W = mem.get<double>(4 * np);
+  double* cps = mem.get<double>((size_t)ncp * S);
+  double* fin = mem.get<double>(S);
+  double* part = mem.get<double>(kDotCtas);
+  if (!W || !cps || !fin || !part) return BCFD_E_NOMEM;
+  std::vector<BodyRec> cprec((size_t)ncp);
+  BodyRec finrec;
+  const double* wh[4] = {wu, wv, ww, wp};
+  for (int q = 0; q < 4; ++q) ACK(h2d(W + q * np, wh[q], fb));
+  ACK(cudaMemsetAsync(part, 0, kDotCtas * sizeof(double), stream()));
+  auto save_all = [&](double* slot) -> int {
+    for (int q = 0; q < nb; ++q) TRY_R(save_state(all[q].second, slot + off[q]));
+    return 0;
+  };
+  auto load_all = [&](const double* slot) -> int {
+    for (int q = 0; q < nb; ++q) TRY_R(load_state(all[q].second, slot + off[q]));
+    return 0;
+  };
+  Lib& L = lib();
+  const int64_t ita0 = L.ita;
+  const double tot0 = L.totime;
+  bcfd_step_config c = *cfg;
+  c.use_graph = 0;
+  const Fields4 bx{hb->d.u, hb->d.v, hb->d.w, hb->d.p};
+  auto fail = [&](int e) {
+    L.ita = ita0 + n_steps;
+    L.totime = tot0 + n_steps * cfg->deltat;
+    return e;
+  };
+
+  // forward, checkpointing fields and the body's state
+  for (auto& [g, b] : all) {
+    const size_t bytes = (size_t)b->d.d.npts() * sizeof(double);
+    ACK(cudaMemcpyAsync(b->d.ut, b->d.u, bytes, cudaMemcpyDeviceToDevice, stream()));
+    ACK(cudaMemcpyAsync(b->d.vt, b->d.v, bytes, cudaMemcpyDeviceToDevice, stream()));
+    ACK(cudaMemcpyAsync(b->d.wt, b->d.w, bytes, cudaMemcpyDeviceToDevice, stream()));
+  }
+  TRY_R(save_all(cps));
+  TRY_R(save_body(hb, cprec[0], mem));
+  std::vector<double*> g0(nb, nullptr);
+  for (int q = 0; q < nb; ++q) {
+    HostBlock* b = all[q].second;
+    if (!b->has_body || b->d.ne <= 0) continue;
+    g0[q] = mem.get<double>(14 * (size_t)b->d.cap_ib);
+    if (!g0[q]) return BCFD_E_NOMEM;
+    TRY_R(save_ghosts(b, g0[q]));
+  }
+  // the ghost arrays of the state after step n (n = 0: the run's start), with
+  // the body's state of that step restored
+  auto ghosts_at = [&](int64_t n) -> int {
+    for (int q = 0; q < nb; ++q)
+      if (g0[q]) TRY_R(n == 0 ? load_ghosts(all[q].second, g0[q]) : regen_ghosts(all[q].second));
+    return 0;
+  };
+  double jstress = 0.0;
+  for (int64_t n = 1; n <= n_steps; ++n) {
+    TRY_R(run_one_step(c));
+    // a fine-block move changes the blocks' structure: not differentiated
+    if (hb->move_amt[0] || hb->move_amt[1] || hb->move_amt[2]) return fail(BCFD_E_STATE);
+    k_dot_acc<<<kDotCtas, kDotThreads, 0, stream()>>>(W, bx, np, part);
+    BCFD_LAUNCHED();
+    if (use_stress) {
+      double co[4];
+      if (ne <= BCFD_STRESS_NOALLOC_MAX_ELEMS)
+        TRY_R(launch_stress_noalloc(hb, mu_f, rho_f, co));
+      else
+        TRY_R(launch_stress(hb, mu_f, rho_f, co));
+      for (int t = 0; t < 4; ++t) jstress += stress_seed[t] * co[t];
+    }
+    if (n % K == 0 && n < n_steps) {
+      TRY_R(save_all(cps + (size_t)(n / K) * S));
+      TRY_R(save_body(hb, cprec[(size_t)(n / K)], mem));
+    }
+  }
+  TRY_R(save_all(fin));
+  TRY_R(save_body(hb, finrec, mem));
+  std::vector<double> ph(kDotCtas);
+  ACK(d2h(ph.data(), part, kDotCtas * sizeof(double)));
+  double jsum = 0.0;
+  for (double v : ph) jsum += v;
+  *J = (jsum + jstress) / (double)n_steps;
+  for (int q = 0; q < nb; ++q) {
+    const int e = take_block_error(all[q].second);
+    if (e) return fail(e);
+  }
+  const bool grad = dj_duc || dj_dmotion || gu || gv || gw || gp;
+  if (!grad) return fail(0);
+
+  // the motion's parameter tangents for every driver step of the run
+  std::vector<StepTangent> tan;
+  TRY_R(motion_tangent(hb, L.phase_angle, L.freq, cfg->deltat, tot0, ita0, ita0 + n_steps, tan));
+  const int64_t first = hb->motion.init_ita;
+  if (ita0 < first) return fail(BCFD_E_STATE);
+  // per-block adjoint buffers
+  std::vector<AdjBlock> AB(nb);
+  for (int q = 0; q < nb; ++q) {
+    AdjBlock& a = AB[q];
+    a.hb = all[q].second;
+    a.np = npb[q];
+    a.body = a.hb->has_body && a.hb->d.ne > 0;
+    a.A = mem.get<double>(kStateFields * a.np);
+    a.pcb = mem.get<double>(a.np);
+    a.y = mem.get<double>(a.np);
+    a.bb = mem.get<double>(a.np);
+    a.foot = mem.get<uint32_t>(16);
+    a.ucl = mem.get<double>((size_t)a.hb->d.d.ny * a.hb->d.d.nz);
+    const size_t ntask = a.body ? 6 * (size_t)a.hb->cap_ib_alloc : 1;
+    a.fc.tgt = mem.get<int64_t>(ntask);
+    a.fc.axis = mem.get<int>(ntask);
+    a.fc.pos = mem.get<int64_t>(8 * ntask);
+    a.fc.coef = mem.get<double>(8 * ntask);
+    a.fc.kc = mem.get<double>(kKinScalars * ntask);
+    a.fc.gk = mem.get<double>(kKinScalars);
+    if (!a.A || !a.pcb || !a.y || !a.bb || !a.foot || !a.ucl || !a.fc.tgt || !a.fc.axis || !a.fc.pos ||
+        !a.fc.coef || !a.fc.kc || !a.fc.gk)
+      return fail(BCFD_E_NOMEM);
+    TRY_R(alloc_ts_adj(a, mem));
+    if (q == hidx) {
+      a.fc.elem = mem.get<int>(ntask);
+      a.fc.ge = mem.get<double>(7 * (size_t)ne);
+      if (!a.fc.elem || !a.fc.ge) return fail(BCFD_E_NOMEM);
+      ACK(cudaMemsetAsync(a.fc.ge, 0, 7 * (size_t)ne * sizeof(double), stream()));
+    }
+    ACK(cudaMemsetAsync(a.A, 0, kStateFields * a.np * sizeof(double), stream()));
+    ACK(cudaMemsetAsync(a.ucl, 0, (size_t)a.hb->d.d.ny * a.hb->d.d.nz * sizeof(double), stream()));
+    ACK(cudaMemsetAsync(a.fc.gk, 0, kKinScalars * sizeof(double), stream()));
+  }
+  std::vector<IfaceMasks> M;
+  for (HostInterface* it : ifs) {
+    IfaceMasks m;
+    m.it = it;
+    for (int q = 0; q < nb; ++q) {
+      if (all[q].first == it->a) m.a = &AB[q];
+      if (all[q].first == it->b) m.b = &AB[q];
+    }
+    if (!m.a || !m.b) return fail(BCFD_E_STATE);
+    double* ones_a = mem.get<double>(m.a->np);
+    double* ones_b = mem.get<double>(m.b->np);
+    if (!ones_a || !ones_b) return fail(BCFD_E_NOMEM);
+    k_fill<<<grid_for(m.a->np, 256), 256, 0, stream()>>>(m.a->np, ones_a, 1.0);
+    BCFD_LAUNCHED();
+    k_fill<<<grid_for(m.b->np, 256), 256, 0, stream()>>>(m.b->np, ones_b, 1.0);
+    BCFD_LAUNCHED();
+    for (int comp = 0; comp < 4; ++comp) {
+      m.face[comp] = mem.get<double>(m.b->np);
+      m.restr[comp] = mem.get<double>(m.a->np);
+      if (!m.face[comp] || !m.restr[comp]) return fail(BCFD_E_NOMEM);
+      ACK(cudaMemsetAsync(m.face[comp], 0, m.b->np * sizeof(double), stream()));
+      ACK(cudaMemsetAsync(m.restr[comp], 0, m.a->np * sizeof(double), stream()));
+      TRY_R(coupling_apply(it, comp, 0, ones_a, m.face[comp]));
+      TRY_R(coupling_apply(it, comp, 2, ones_b, m.restr[comp]));
+    }
+    M.push_back(m);
+  }
+  AdjBlock& ah = AB[hidx];
+  // the objective at the state the blocks hold (geometry and kinematics of
+  // the same step): field weights, drag/lift weights, their geometric and
+  // kinematic partials, each with the time average's 1/N
+  const double wn = 1.0 / (double)n_steps;
+  double* sd = mem.get<double>(4);
+  double* sdw = mem.get<double>(4);
+  double* ss = mem.get<double>(8 + (size_t)std::max(64, kKinScalars) * ne);
+  double* gscr = mem.get<double>(9 * (size_t)ne + 4 * (size_t)nn + 4);
+  double* pre = mem.get<double>(3 * (size_t)np);
+  int* csr_off = mem.get<int>((size_t)nn + 1);
+  if (!sd || !sdw || !ss || !gscr || !pre || !csr_off) return fail(BCFD_E_NOMEM);
+  if (use_stress) {
+    double sw[4];
+    for (int t = 0; t < 4; ++t) sw[t] = stress_seed[t] * wn;
+    ACK(h2d(sd, stress_seed, 4 * sizeof(double)));
+    ACK(h2d(sdw, sw, 4 * sizeof(double)));
+  }
+  std::vector<int> hoff, hent;
+  TRY_R(build_node_csr(hb, hoff, hent));
+  int* csr_ent = mem.get<int>(std::max<size_t>(hent.size(), 1));
+  if (!csr_ent) return fail(BCFD_E_NOMEM);
+  ACK(h2d(csr_off, hoff.data(), hoff.size() * sizeof(int)));
+  ACK(h2d(csr_ent, hent.data(), hent.size() * sizeof(int)));
+  auto objective = [&]() -> int {
+    k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, ah.A, 4 * np);
+    BCFD_LAUNCHED();
+    if (use_stress) {
+      TRY_R(launch_stress_weights(hb, mu_f, rho_f, sdw, ah.A, ss));
+      TRY_R(launch_stress_geo(hb, mu_f, rho_f, sd, wn, ah.fc.ge, ss));
+      TRY_R(launch_stress_kin(hb, mu_f, rho_f, sdw, ah.fc.gk, ss));
+    }
+    return 0;
+  };
+  // the geometry and kinematics of driver step `st` (the body's current
+  // state, placed by P) are complete: their adjoints go to the parameters
+  double dmot[kMotionParams] = {0, 0, 0, 0, 0};
+  auto flush = [&](int64_t st, const Place& P) -> int {
+    double pb[4], gk[kKinScalars];
+    TRY_R(launch_geometry_place_adj(hb, ah.fc.ge, csr_off, csr_ent, P, gscr, pb));
+    ACK(d2h(gk, ah.fc.gk, kKinScalars * sizeof(double)));
+    const StepTangent& T = tan[(size_t)(st - first)];
+    for (int q = 0; q < kMotionParams; ++q) {
+      double v = pb[0] * T.angle[q] + pb[2] * T.ty[q];
+      for (int p = 0; p < kKinScalars; ++p) v += gk[p] * T.kin[p][q];
+      dmot[q] += v;
+    }
+    ACK(cudaMemsetAsync(ah.fc.ge, 0, 7 * (size_t)ne * sizeof(double), stream()));
+    ACK(cudaMemsetAsync(ah.fc.gk, 0, kKinScalars * sizeof(double), stream()));
+    return 0;
+  };
+  double* tape = mem.get<double>((size_t)K * S);
+  if (!tape) return fail(BCFD_E_NOMEM);
+  TRY_R(objective());  // at x^N with the end geometry (the blocks' state now)
+  MoveRecorder rec;
+  rec.body = hb;
+  rec.sc = pre;
+  std::vector<StepGeo> geo((size_t)nb);
+  for (int64_t m = ncp - 1; m >= 0; --m) {
+    const int64_t n0 = m * K, n1 = std::min(n0 + K, n_steps);
+    const double* cp = cps + (size_t)m * S;
+    ACK(cudaMemcpyAsync(tape, cp, S * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
+    TRY_R(load_all(cp));
+    TRY_R(restore_body(hb, cprec[(size_t)m]));
+    TRY_R(ghosts_at(n0));
+    L.ita = ita0 + n0;
+    L.totime = tot0 + n0 * cfg->deltat;
+    DevMem seg;
+    std::vector<BodyRec> recs((size_t)(n1 - n0 + 1));
+    rec.mem = &seg;
+    L.recorder = &rec;
+    int r = 0;
+    for (int64_t n = n0 + 1; n <= n1 && !r; ++n) {
+      rec.cur = &recs[(size_t)(n - n0)];
+      r = run_one_step(c);
+      if (!r) r = save_body(hb, recs[(size_t)(n - n0)], seg);
+      if (!r && n < n1) r = save_all(tape + (size_t)(n - n0) * S);
+    }
+    L.recorder = nullptr;
+    rec.cur = nullptr;
+    if (r) return fail(r);
+    if (rec.oom) return fail(BCFD_E_NOMEM);
+    for (int64_t n = n1; n > n0; --n) {
+      const BodyRec& re = recs[(size_t)(n - n0)];
+      for (int k2 = 0; k2 < kCalls; ++k2) geo[(size_t)hidx].geo[k2] = re.geo[k2];
+      // after the body moved: the step's end geometry and kinematics
+      TRY_R(restore_body(hb, re));
+      TRY_R(adjoint_step_second(AB, &geo));
+      TRY_R(flush(ita0 + n, re.stage.place));
+      // before: the geometry, kinematics and state the step started from
+      const BodyRec& rs = (n - 1 == n0) ? cprec[(size_t)m] : recs[(size_t)(n - 1 - n0)];
+      TRY_R(restore_body(hb, rs));
+      TRY_R(load_all(tape + (size_t)(n - 1 - n0) * S));
+      TRY_R(ghosts_at(n - 1));
+      TRY_R(adjoint_step_first(AB, M, c, adj_tol, adj_itmax, &geo));
+      if (n - 1 >= 1) TRY_R(objective());
+    }
+  }
+  // the run's start: its geometry and kinematics
+  TRY_R(flush(ita0, cprec[0].stage.place));
+  // leave the blocks at the forward run's final state
+  TRY_R(load_all(fin));
+  TRY_R(restore_body(hb, finrec));
+  TRY_R(ghosts_at(n_steps));
+  L.ita = ita0 + n_steps;
+  L.totime = tot0 + n_steps * cfg->deltat;
+  k_axpy<<<grid_for(3 * np, 256), 256, 0, stream()>>>(ah.A + 4 * np, 1.0, ah.A, 3 * np);
+  BCFD_LAUNCHED();
+  double* ghp[4] = {gu, gv, gw, gp};
+  for (int q = 0; q < 4; ++q)
+    if (ghp[q]) ACK(cudaMemcpyAsync(ghp[q], ah.A + q * np, fb, cudaMemcpyDeviceToHost, stream()));
+  double duc = 0.0;
+  for (AdjBlock& a : AB) {
+    if (!a.hb->is_coarse) continue;
+    std::vector<double> ul((size_t)a.hb->d.d.ny * a.hb->d.d.nz);
+    ACK(d2h(ul.data(), a.ucl, ul.size() * sizeof(double)));
+    for (double v : ul) duc += v;
+  }
+  if (dj_duc) *dj_duc = duc;
+  if (dj_dmotion)
+    for (int q = 0; q < kMotionParams; ++q) dj_dmotion[q] = dmot[q];
   ACK(cudaStreamSynchronize(stream()));
   for (auto& [g, b] : all) {
     const int e = take_block_error(b);

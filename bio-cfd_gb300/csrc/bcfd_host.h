@@ -299,8 +299,16 @@ int launch_momentum_tangent(HostBlock* hb, double dt, double re, const double* c
                             double* const tan[3]);
 int solve_zero_bc_dev(HostBlock* hb, const double* r, double* x, double tol, int64_t itmax, bool transpose);
 int run_one_step(const bcfd_step_config& cfg);
+// scratch of the thin-surface overlay's adjoint: last (7 ints per point),
+// contrib (14 doubles per point), gb (the ghost arrays' adjoint, 14 x cap)
+struct MomTsAdj {
+  int* last = nullptr;
+  double* contrib = nullptr;
+  double* gb = nullptr;
+  int64_t cap = 0;
+};
 int launch_momentum_adjoint(HostBlock* hb, double dt, double re, const double* const sb[3], double* const ab[4],
-                            uint32_t* foot);
+                            uint32_t* foot, const MomTsAdj* ts = nullptr);
 int launch_velocity_bc(HostBlock* hb, double dt, double uc);
 int launch_solid_bc(HostBlock* hb, bool move);
 // k_search.cu
@@ -392,6 +400,7 @@ struct AdjPtrs {
 int launch_stress_kin(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double* gk,
                       double* scratch);
 int launch_forcing_adjoint(HostBlock* hb, int mode, int vel, const AdjPtrs& a, const ForceCoef& fc);
+int launch_ghost_adjoint(HostBlock* hb, int vel, const AdjPtrs& a, const ForceCoef& fc, double* gb, int64_t cap);
 int launch_stress_geo(HostBlock* hb, double mu_f, double rho_f, const double* seed_dev, double w, double* ge,
                       double* scratch);
 

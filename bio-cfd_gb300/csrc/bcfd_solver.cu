@@ -757,6 +757,29 @@ int bcfd_run_steps(const bcfd_step_config* cfg, int64_t n_steps) {
   return err;
 }
 
+int bcfd_block_write(bcfd_handle h, const char* name, const double* data, int64_t n) {
+  LOCK();
+  HostBlock* hb = get_block(h);
+  if (!hb) return BCFD_E_HANDLE;
+  if (!name || !data || n < 0) return BCFD_E_ARG;
+  const std::string s(name);
+  DevBlock& D = hb->d;
+  int64_t cnt[6];
+  BCFD_CUDA(cudaMemcpyAsync(cnt, D.cnt, sizeof(cnt), cudaMemcpyDeviceToHost, stream()));
+  BCFD_CUDA(cudaStreamSynchronize(stream()));
+  const int64_t nts = std::min<int64_t>(cnt[C_TS], D.cap_ib);
+  const char* gn[14] = {"p_ghost", "pt_ghost", "u2_ghost", "u2t_ghost", "v2_ghost", "v2t_ghost", "w2_ghost",
+                        "w2t_ghost", "u1_ghost", "u1t_ghost", "v1_ghost", "v1t_ghost", "w1_ghost", "w1t_ghost"};
+  for (int q = 0; q < 14; ++q)
+    if (s == gn[q]) {
+      if (n != nts) return BCFD_E_ARG;
+      if (n) BCFD_CUDA(cudaMemcpyAsync(D.ghost[q], data, n * sizeof(double), cudaMemcpyHostToDevice, stream()));
+      BCFD_CUDA(cudaStreamSynchronize(stream()));
+      return 0;
+    }
+  return BCFD_E_NOTFOUND;
+}
+
 int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64_t* written) {
   LOCK();
   HostBlock* hb = get_block(h);

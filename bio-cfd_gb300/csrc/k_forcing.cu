@@ -555,7 +555,7 @@ __global__ void k_p_ghost(DevBlock B) {
 // order.  One thread runs the reverse sweep, so the sums have a fixed order.
 // ---------------------------------------------------------------------------
 __global__ void k_force_coef(DevBlock B, int mode, int vel, ForceCoef fc) {
-  const int nib = (int)min(B.cnt[C_IB], (int64_t)B.cap_ib);
+  const int nib = (int)min(B.cnt[mode == 2 ? C_TS : C_IB], (int64_t)B.cap_ib);
   const int nt = vel ? 6 * nib : nib;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += gridDim.x * blockDim.x) {
     const int n = vel ? t / 6 : t, comp = vel ? t % 6 : -1;
@@ -608,6 +608,34 @@ __global__ void k_force_rev(DevBlock B, int vel, ForceCoef fc, AdjPtrs a) {
   }
 }
 
+// velocityForcingGhost / pressureForcingGhost transposed (tasks of TS entry
+// n, component comp; the ghost value is affine in the probe's 8 values of
+// ut/vt/wt or p, the t-ghost value a copy of u/v/w or p at the TS position):
+// the ghost arrays' adjoint gb (14 arrays of cap entries, ghost[] order)
+// goes to a.src (the read arrays) and a.tgt (the copied ones), then is zeroed
+__global__ void k_ghost_rev(DevBlock B, int vel, ForceCoef fc, AdjPtrs a, double* gb, int64_t cap) {
+  if (blockIdx.x || threadIdx.x) return;
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  const int nt = vel ? 6 * nts : nts;
+  for (int t = nt - 1; t >= 0; --t) {
+    const int n = vel ? t / 6 : t, comp = vel ? t % 6 : -1;
+    const int gs = vel ? ((comp & 1) ? G_U1 : G_U2) + 2 * (comp >> 1) : G_P;
+    const int ax = fc.axis[t];
+    const double o = gb[gs * cap + n];
+    gb[gs * cap + n] = 0.0;
+    double* S = a.src[ax];
+    for (int q = 0; q < 8; ++q) S[fc.pos[8 * (int64_t)t + q]] += fc.coef[8 * (int64_t)t + q] * o;
+    for (int p = 0; p < kKinScalars; ++p) fc.gk[p] += fc.kc[kKinScalars * (int64_t)t + p] * o;
+    if (fc.geo) {
+      const int e = fc.elem[t];
+      for (int l = 0; l < 6; ++l) fc.ge[7 * (int64_t)e + l] += fc.geo[6 * (int64_t)t + l] * o;
+    }
+    const double o2 = gb[(gs + 1) * cap + n];
+    gb[(gs + 1) * cap + n] = 0.0;
+    a.tgt[ax][fc.tgt[t]] += o2;
+  }
+}
+
 }  // namespace
 
 // Geometric partials of every task of one forcing call, at the stencil values
@@ -646,6 +674,19 @@ int launch_forcing_adjoint(HostBlock* hb, int mode, int vel, const AdjPtrs& a, c
   k_force_coef<<<grid_for(cap, 128, 2048), 128, 0, stream()>>>(hb->d, mode, vel, fc);
   BCFD_LAUNCHED();
   k_force_rev<<<1, 32, 0, stream()>>>(hb->d, vel, fc, a);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
+// transpose of the ghost calls (mode 2): a.src the adjoint of the probed
+// arrays by axis (0 p, 1 ut, 2 vt, 3 wt for velocity), a.tgt that of the
+// t-ghost sources (p, u, v, w), gb the ghost arrays' adjoint
+int launch_ghost_adjoint(HostBlock* hb, int vel, const AdjPtrs& a, const ForceCoef& fc, double* gb, int64_t cap) {
+  if (hb->d.ne <= 0) return 0;
+  const int64_t n = (vel ? 6 : 1) * (int64_t)hb->d.cap_ib;
+  k_force_coef<<<grid_for(n, 128, 2048), 128, 0, stream()>>>(hb->d, 2, vel, fc);
+  BCFD_LAUNCHED();
+  k_ghost_rev<<<1, 32, 0, stream()>>>(hb->d, vel, fc, a, gb, cap);
   BCFD_LAUNCHED();
   return 0;
 }

@@ -492,10 +492,10 @@ __device__ __forceinline__ void dir_vec(int dir, int& a, int& b, int& e) {
 }
 
 // latest restorer F (linear index < before) of position kind K of TS cell T;
-// updates best / val
+// updates best / val / kind
 __device__ __forceinline__ void latest_restore(const DevBlock& B, int ti, int tj, int tk, int K,
                                                int64_t before, const double* rconst, int64_t& best,
-                                               double& val) {
+                                               double& val, int& kind) {
   const Dims& d = B.d;
 #pragma unroll
   for (int dir = 0; dir < 6; ++dir) {
@@ -510,6 +510,7 @@ __device__ __forceinline__ void latest_restore(const DevBlock& B, int ti, int tj
     if (B.cell[lf] != 0) continue;
     best = lf;
     val = rconst[K];
+    kind = K;
   }
 }
 
@@ -531,6 +532,40 @@ __device__ __forceinline__ int owners(const DevBlock& B, int q, int xi, int xj, 
   return n;
 }
 
+// One read of position x (field q) by cell G near TS cells, in the
+// reference's serial order: the value and where it came from (how 0: the
+// array, 1: G's own substitution of kind K, the ghost value of TS entry
+// last[K]; 2: the restore of kind K, the t-ghost value of the last entry).
+struct TsHit {
+  double v;
+  int how, K;
+};
+// not inlined: one copy of the overlay logic serves all ~150 stencil reads
+__device__ __noinline__ TsHit ts_read(const DevBlock& B, int gi, int gj, int gk, int64_t glin, const int* last,
+                                      const double* rconst, int q, int xi, int xj, int xk, int64_t x) {
+  const double* f = q == 0 ? B.u : q == 1 ? B.v : q == 2 ? B.w : B.p;
+  const double orig = __ldg(f + x);
+  int ot[2][4];
+  const int n = owners(B, q, xi, xj, xk, ot);
+  if (n == 0) return TsHit{orig, 0, 0};
+  // own substitution: T is an axis neighbour of G and the direction handles K
+  for (int m = 0; m < n; ++m) {
+    const int di = ot[m][0] - gi, dj = ot[m][1] - gj, dk = ot[m][2] - gk;
+    const int ad = abs(di) + abs(dj) + abs(dk);
+    if (ad != 1) continue;
+    const int dir = di ? (di > 0 ? 0 : 1) : dj ? (dj > 0 ? 2 : 3) : (dk > 0 ? 4 : 5);
+    const int K = ot[m][3];
+    if (K == excluded_kind(dir)) continue;
+    if (last[K] >= 0) return TsHit{B.ghost[ghost_slot(K)][last[K]], 1, K};
+  }
+  int64_t best = -1;
+  double val = orig;
+  int kind = 0;
+  for (int m = 0; m < n; ++m)
+    latest_restore(B, ot[m][0], ot[m][1], ot[m][2], ot[m][3], glin, rconst, best, val, kind);
+  return best >= 0 ? TsHit{val, 2, kind} : TsHit{orig, 0, 0};
+}
+
 // Reads of a cell G near TS cells, in the reference's serial order.
 struct TsReader {
   const DevBlock* B;
@@ -538,28 +573,8 @@ struct TsReader {
   int64_t glin;
   int last[N_KIND];      // own substitution: last TS entry with a negative test, -1: none
   double rconst[N_KIND]; // restore value of each kind
-  // not inlined: one copy of the overlay logic serves all ~150 stencil reads
-  __device__ __noinline__ double get(int q, int xi, int xj, int xk, int64_t x) const {
-    const double* f = q == 0 ? B->u : q == 1 ? B->v : q == 2 ? B->w : B->p;
-    const double orig = __ldg(f + x);
-    int ot[2][4];
-    const int n = owners(*B, q, xi, xj, xk, ot);
-    if (n == 0) return orig;
-    // own substitution: T is an axis neighbour of G and the direction handles K
-    for (int m = 0; m < n; ++m) {
-      const int di = ot[m][0] - gi, dj = ot[m][1] - gj, dk = ot[m][2] - gk;
-      const int ad = abs(di) + abs(dj) + abs(dk);
-      if (ad != 1) continue;
-      const int dir = di ? (di > 0 ? 0 : 1) : dj ? (dj > 0 ? 2 : 3) : (dk > 0 ? 4 : 5);
-      const int K = ot[m][3];
-      if (K == excluded_kind(dir)) continue;
-      if (last[K] >= 0) return B->ghost[ghost_slot(K)][last[K]];
-    }
-    int64_t best = -1;
-    double val = orig;
-    for (int m = 0; m < n; ++m)
-      latest_restore(*B, ot[m][0], ot[m][1], ot[m][2], ot[m][3], glin, rconst, best, val);
-    return val;
+  __device__ __forceinline__ double get(int q, int xi, int xj, int xk, int64_t x) const {
+    return ts_read(*B, gi, gj, gk, glin, last, rconst, q, xi, xj, xk, x).v;
   }
 };
 
@@ -685,18 +700,50 @@ struct NullOut {
   __device__ __forceinline__ void put(int, int64_t, T) const {}
 };
 
-__global__ void k_mom_footprint(DevBlock B, MomArgs a, uint32_t* foot) {
+// the footprint of a cell near TS cells: its reads go through the overlay,
+// so its branches are those of the forward loop
+struct FootTsReader {
+  const DevBlock* B;
+  int gi, gj, gk;
+  int64_t glin;
+  const int* last;
+  const double* rconst;
+  uint32_t* m;
+  __device__ __forceinline__ double get(int q, int ii, int jj, int kk, int64_t x) const {
+    const int a = ii - gi, b = jj - gj, e = kk - gk;
+    if (a < -2 || a > 2 || b < -2 || b > 2 || e < -2 || e > 2) {
+      set_err(B->err, BCFD_E_STATE);
+    } else {
+      const int o = (a + 2) + 5 * (b + 2) + 25 * (e + 2);
+      m[4 * q + (o >> 5)] |= 1u << (o & 31);
+    }
+    return ts_read(*B, gi, gj, gk, glin, last, rconst, q, ii, jj, kk, x).v;
+  }
+};
+
+// ts_last: per point, the own-substitution entries of the cells near TS
+// cells (k_ts_last); nullptr: such cells are skipped
+__global__ void k_mom_footprint(DevBlock B, MomArgs a, uint32_t* foot, const int* ts_last) {
   uint32_t m[kFootWords];
 #pragma unroll
   for (int w = 0; w < kFootWords; ++w) m[w] = 0u;
   const Dims& d = B.d;
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  double rc[N_KIND];
+  restore_consts(B, nts, rc);
   const int64_t n = (int64_t)d.nx * d.ny * d.nz;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
     const int i = 2 + (int)(t % d.nx);
     const int64_t r = t / d.nx;
     const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
     const int64_t c = d.idx(i, j, k);
-    if (B.cell[c] != 0 || B.tsnear[c]) continue;
+    if (B.cell[c] != 0) continue;
+    if (B.tsnear[c]) {
+      if (!ts_last) continue;
+      const FootTsReader rd{&B, i, j, k, c, ts_last + N_KIND * c, rc, m};
+      momentum_cell<double>(B, a, i, j, k, c, rd, NullOut{});
+      continue;
+    }
     const FootReader rd{{B.u, B.v, B.w, B.p}, m, i, j, k, B.err};
     momentum_cell<double>(B, a, i, j, k, c, rd, NullOut{});
   }
@@ -719,6 +766,43 @@ struct SeedReader4 {
     return r;
   }
 };
+// the same for a cell near TS cells: a read the overlay redirects to a ghost
+// or t-ghost value does not depend on the array value at x
+struct TsSeedReader4 {
+  const DevBlock* B;
+  int gi, gj, gk;
+  int64_t glin;
+  const int* last;
+  const double* rconst;
+  int64_t sx;
+  __device__ __forceinline__ Dual4 get(int q, int xi, int xj, int xk, int64_t x) const {
+    const TsHit h = ts_read(*B, gi, gj, gk, glin, last, rconst, q, xi, xj, xk, x);
+    Dual4 r(h.v);
+    if (h.how == 0 && x == sx) r.d[q] = 1.0;
+    return r;
+  }
+};
+// lanes on the ghost scalars a cell near TS cells reads: scalar s (0..6 the
+// own substitution of kind s, 7..13 the restore of kind s - 7) is lane
+// s - 4 pass of the pass
+struct TsGhostReader4 {
+  const DevBlock* B;
+  int gi, gj, gk;
+  int64_t glin;
+  const int* last;
+  const double* rconst;
+  int pass;
+  __device__ __forceinline__ Dual4 get(int q, int xi, int xj, int xk, int64_t x) const {
+    const TsHit h = ts_read(*B, gi, gj, gk, glin, last, rconst, q, xi, xj, xk, x);
+    Dual4 r(h.v);
+    if (h.how) {
+      const int l = (h.how == 1 ? h.K : N_KIND + h.K) - 4 * pass;
+      if (l >= 0 && l < 4) r.d[l] = 1.0;
+    }
+    return r;
+  }
+};
+
 // adds seed_q(C) * dF_q(C)/dX_f to field f's sum, for the fields whose
 // footprint holds this offset (the others' partials are zero)
 struct AdjOut4 {
@@ -740,9 +824,12 @@ struct AdjOut4 {
 __global__ void __launch_bounds__(128) k_mom_adjoint(DevBlock B, MomArgs a, const uint32_t* __restrict__ foot,
                                                      const double* ubar_t, const double* vbar_t,
                                                      const double* wbar_t, double* ub, double* vb, double* wb,
-                                                     double* pb) {
+                                                     double* pb, const int* ts_last) {
   const Dims& d = B.d;
   const int64_t n = d.npts();
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  double rc[N_KIND];
+  restore_consts(B, nts, rc);
   uint32_t m[kFootWords];
 #pragma unroll
   for (int w = 0; w < kFootWords; ++w) m[w] = __ldg(foot + w);
@@ -761,7 +848,12 @@ __global__ void __launch_bounds__(128) k_mom_adjoint(DevBlock B, MomArgs a, cons
       const int64_t c = d.idx(ci, cj, ck);
       if (B.cell[c] != 0) continue;
       if (B.tsnear[c]) {
-        set_err(B.err, BCFD_E_STATE);  // the thin-surface overlay has no adjoint
+        if (!ts_last) {
+          set_err(B.err, BCFD_E_STATE);  // the overlay's entries are needed
+          continue;
+        }
+        const TsSeedReader4 rd{&B, ci, cj, ck, c, ts_last + N_KIND * c, rc, x};
+        momentum_cell<Dual4>(B, a, ci, cj, ck, c, rd, AdjOut4{{ubar_t, vbar_t, wbar_t}, acc, fmask});
         continue;
       }
       const SeedReader4 rd{{B.u, B.v, B.w, B.p}, x};
@@ -791,14 +883,135 @@ struct TsRestoreOp {
     const int n = owners(B, q, xi, xj, xk, ot);
     int64_t best = -1;
     double val = 0.0;
+    int kind = 0;
     for (int m = 0; m < n; ++m)
-      latest_restore(B, ot[m][0], ot[m][1], ot[m][2], ot[m][3], INT64_MAX, rc, best, val);
+      latest_restore(B, ot[m][0], ot[m][1], ot[m][2], ot[m][3], INT64_MAX, rc, best, val, kind);
     if (best < 0) continue;
     double* f = q == 0 ? B.u : q == 1 ? B.v : q == 2 ? B.w : B.p;
     f[d.idx(xi, xj, xk)] = val;
   }
   }
 };
+
+// ---------------------------------------------------------------------------
+// Adjoint of the thin-surface overlay.  A cell near TS cells reads, besides
+// array values, 14 scalars: the ghost value of kind K of TS entry last[K]
+// (its own substitution) and the t-ghost value of kind K of the last TS entry
+// (the restore).  Their adjoints go to the ghost arrays' adjoint gb (14
+// arrays of cap entries, the ghost[] order); the loop's final restore is
+// transposed first.  Sums in a fixed order: one thread per accumulation.
+// ---------------------------------------------------------------------------
+
+// the own-substitution entries of every fluid cell near TS cells
+__global__ void k_ts_last(DevBlock B, int* last) {
+  const Dims& d = B.d;
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(t % d.nx);
+    const int64_t r = t / d.nx;
+    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
+    const int64_t c = d.idx(i, j, k);
+    if (B.cell[c] != 0 || !B.tsnear[c]) continue;
+    int l[N_KIND];
+    if (!adj_ok(B.cell2, d, true, i, j, k, 1)) {
+      own_substitution(B, i, j, k, nts, l);
+    } else {
+#pragma unroll
+      for (int K = 0; K < N_KIND; ++K) l[K] = -1;
+    }
+#pragma unroll
+    for (int K = 0; K < N_KIND; ++K) last[N_KIND * c + K] = l[K];
+  }
+}
+
+// per fluid cell near TS cells: seed . dF/d(scalar s) for its 14 scalars
+__global__ void __launch_bounds__(128) k_mom_ghost_contrib(DevBlock B, MomArgs a, const int* last,
+                                                           const double* ubar_t, const double* vbar_t,
+                                                           const double* wbar_t, double* contrib) {
+  const Dims& d = B.d;
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  double rc[N_KIND];
+  restore_consts(B, nts, rc);
+  const int64_t n = (int64_t)d.nx * d.ny * d.nz;
+  for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int i = 2 + (int)(t % d.nx);
+    const int64_t r = t / d.nx;
+    const int j = 2 + (int)(r % d.ny), k = 2 + (int)(r / d.ny);
+    const int64_t c = d.idx(i, j, k);
+    if (B.cell[c] != 0 || !B.tsnear[c]) continue;
+    for (int pass = 0; pass < 4; ++pass) {
+      double acc[4] = {0.0, 0.0, 0.0, 0.0};
+      const TsGhostReader4 rd{&B, i, j, k, c, last + N_KIND * c, rc, pass};
+      momentum_cell<Dual4>(B, a, i, j, k, c, rd, AdjOut4{{ubar_t, vbar_t, wbar_t}, acc, 0xFu});
+#pragma unroll
+      for (int l = 0; l < 4; ++l)
+        if (4 * pass + l < 2 * N_KIND) contrib[2 * N_KIND * c + 4 * pass + l] = acc[l];
+    }
+  }
+}
+
+// the cells near TS cells in list (linear index) order, inside the box of the
+// TS cells grown by the stencil's reach: contributions into gb
+__global__ void k_mom_ghost_acc(DevBlock B, const int* last, const double* contrib, double* gb, int64_t cap) {
+  if (blockIdx.x || threadIdx.x) return;
+  const Dims& d = B.d;
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  if (nts <= 0) return;
+  int lo[3] = {d.nx + 1, d.ny + 1, d.nz + 1}, hi[3] = {2, 2, 2};
+  for (int nn = 0; nn < nts; ++nn) {
+    const int bt = B.ts_idx[nn] - 1;
+    const int p[3] = {B.ib_i[bt], B.ib_j[bt], B.ib_k[bt]};
+    for (int q = 0; q < 3; ++q) {
+      lo[q] = min(lo[q], p[q] - 3);
+      hi[q] = max(hi[q], p[q] + 3);
+    }
+  }
+  lo[0] = max(lo[0], 2); lo[1] = max(lo[1], 2); lo[2] = max(lo[2], 2);
+  hi[0] = min(hi[0], d.nx + 1); hi[1] = min(hi[1], d.ny + 1); hi[2] = min(hi[2], d.nz + 1);
+  for (int k = lo[2]; k <= hi[2]; ++k)
+    for (int j = lo[1]; j <= hi[1]; ++j)
+      for (int i = lo[0]; i <= hi[0]; ++i) {
+        const int64_t c = d.idx(i, j, k);
+        if (B.cell[c] != 0 || !B.tsnear[c]) continue;
+        for (int K = 0; K < N_KIND; ++K) {
+          const int l = last[N_KIND * c + K];
+          if (l >= 0) gb[ghost_slot(K) * cap + l] += contrib[2 * N_KIND * c + K];
+          gb[(ghost_slot(K) + 1) * cap + nts - 1] += contrib[2 * N_KIND * c + N_KIND + K];
+        }
+      }
+}
+
+// the final restore transposed: a restored position's adjoint goes to the
+// t-ghost value it received; positions shared by two TS cells are visited
+// twice, the second visit adds the zero the first left
+__global__ void k_ts_restore_adj(DevBlock B, double* ub, double* vb, double* wb, double* pb, double* gb,
+                                 int64_t cap) {
+  if (blockIdx.x || threadIdx.x) return;
+  const Dims& d = B.d;
+  const int nts = (int)min(B.cnt[C_TS], (int64_t)B.cap_ib);
+  double rc[N_KIND];
+  restore_consts(B, nts, rc);
+  for (int t = 0; t < nts * N_KIND; ++t) {
+    const int nn = t / N_KIND, K = t % N_KIND;
+    const int bt = B.ts_idx[nn] - 1;
+    const int ti = B.ib_i[bt], tj = B.ib_j[bt], tk = B.ib_k[bt];
+    const int q = K == K_P ? 3 : K >> 1;
+    const int xi = ti - (K == K_U1), xj = tj - (K == K_V1), xk = tk - (K == K_W1);
+    int ot[2][4];
+    const int n = owners(B, q, xi, xj, xk, ot);
+    int64_t best = -1;
+    double val = 0.0;
+    int kind = 0;
+    for (int m = 0; m < n; ++m)
+      latest_restore(B, ot[m][0], ot[m][1], ot[m][2], ot[m][3], INT64_MAX, rc, best, val, kind);
+    if (best < 0) continue;
+    double* f = q == 0 ? ub : q == 1 ? vb : q == 2 ? wb : pb;
+    const int64_t x = d.idx(xi, xj, xk);
+    gb[(ghost_slot(kind) + 1) * cap + nts - 1] += f[x];
+    f[x] = 0.0;
+  }
+}
 
 // velocityBC loop 1 (x faces), src/BoundaryConditions.f90:16-40
 __global__ void k_vbc_x(DevBlock B, double deltat, double uc) {
@@ -936,17 +1149,37 @@ int launch_momentum_tangent(HostBlock* hb, double dt, double re, const double* c
 
 // adjoint of nsMomentum2order at the block's current (u,v,w,p): (ub,vb,wb,pb)
 // += J^T (ubar_t, vbar_t, wbar_t), J the predictor's Jacobian on fluid cells;
-// foot is 16 words of device scratch
+// foot is 16 words of device scratch.  With ts (a block whose body has
+// thin-surface cells) the overlay is transposed too: ab at the positions the
+// loop's final restore writes goes to ts->gb first, then the cells near TS
+// cells read through the overlay and the ghost scalars' adjoints are added
+// to ts->gb (the block's ghost arrays must hold the values the forward step
+// read); without it such cells set BCFD_E_STATE.
 int launch_momentum_adjoint(HostBlock* hb, double dt, double re, const double* const sb[3], double* const ab[4],
-                            uint32_t* foot) {
+                            uint32_t* foot, const MomTsAdj* ts) {
   const MomArgs a{dt, re};
-  BCFD_CUDA(cudaMemsetAsync(foot, 0, kFootWords * sizeof(uint32_t), stream()));
   const int64_t ni = (int64_t)hb->d.d.nx * hb->d.d.ny * hb->d.d.nz;
-  k_mom_footprint<<<grid_for(ni, 128, 1u << 16), 128, 0, stream()>>>(hb->d, a, foot);
+  const int* last = nullptr;
+  if (ts) {
+    k_ts_restore_adj<<<1, 32, 0, stream()>>>(hb->d, ab[0], ab[1], ab[2], ab[3], ts->gb, ts->cap);
+    BCFD_LAUNCHED();
+    k_ts_last<<<grid_for(ni, 128, 1u << 16), 128, 0, stream()>>>(hb->d, ts->last);
+    BCFD_LAUNCHED();
+    last = ts->last;
+  }
+  BCFD_CUDA(cudaMemsetAsync(foot, 0, kFootWords * sizeof(uint32_t), stream()));
+  k_mom_footprint<<<grid_for(ni, 128, 1u << 16), 128, 0, stream()>>>(hb->d, a, foot, last);
   BCFD_LAUNCHED();
-  k_mom_adjoint<<<grid_for(hb->d.d.npts(), 128, 1u << 20), 128, 0, stream()>>>(hb->d, a, foot, sb[0], sb[1], sb[2],
-                                                                               ab[0], ab[1], ab[2], ab[3]);
+  k_mom_adjoint<<<grid_for(hb->d.d.npts(), 128, 1u << 20), 128, 0, stream()>>>(
+      hb->d, a, foot, sb[0], sb[1], sb[2], ab[0], ab[1], ab[2], ab[3], last);
   BCFD_LAUNCHED();
+  if (ts) {
+    k_mom_ghost_contrib<<<grid_for(ni, 128, 1u << 16), 128, 0, stream()>>>(hb->d, a, ts->last, sb[0], sb[1], sb[2],
+                                                                           ts->contrib);
+    BCFD_LAUNCHED();
+    k_mom_ghost_acc<<<1, 32, 0, stream()>>>(hb->d, ts->last, ts->contrib, ts->gb, ts->cap);
+    BCFD_LAUNCHED();
+  }
   return 0;
 }
 

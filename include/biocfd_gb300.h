@@ -138,6 +138,11 @@ int bcfd_block_set_sor_iter(bcfd_handle h, int64_t n_iter);
  * "blk_mv_tag", "move_amtx", ...  (reals as double, integers as int64);
  * n = capacity in elements, *written = elements written */
 int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64_t* written);
+/* named host write of the device arrays a caller may need to set besides
+ * the fields: the 14 TS ghost arrays ("p_ghost", "pt_ghost", ..., "w1t_ghost",
+ * Block_t's ghost components; n must equal the TS cell count), e.g. to resume
+ * a plate's state mid-run.  BCFD_E_NOTFOUND for other names. */
+int bcfd_block_write(bcfd_handle h, const char* name, const double* data, int64_t n);
 
 /* ---- setup routines ------------------------------------------------------ */
 int bcfd_non_uni_coeff(bcfd_handle h);                    /* src/NavierStokes.f90:13-250 */
@@ -259,6 +264,24 @@ int bcfd_momentum_tangent(bcfd_handle h, double deltat, double re, const double*
  * (deterministic).  Natural-layout host arrays; same thin-surface limit. */
 int bcfd_momentum_adjoint(bcfd_handle h, double deltat, double re, const double* utb, const double* vtb,
                           const double* wtb, double* ub, double* vb, double* wb, double* pb);
+/* The same with the thin-surface (TS) overlay of a plate (surfaces 51/52,
+ * src/NavierStokes.f90:310-490, 860-907) transposed (no counterpart in the
+ * reference).  ub,vb,wb,pb on entry: the adjoint of u,v,w,p after the call
+ * (the loop leaves t-ghost values at the TS positions it restores); on
+ * return: the adjoint of u,v,w,p before it.  gb (14 x n_ts, the ghost[]
+ * order p, pt, u2, u2t, v2, v2t, w2, w2t, u1, u1t, v1, v1t, w1, w1t of
+ * bcfd_block_read) receives the adjoint of the ghost arrays the predictor
+ * read.  The block's ghost arrays must hold the values of the forward call. */
+int bcfd_momentum_adjoint_ts(bcfd_handle h, double deltat, double re, const double* utb, const double* vtb,
+                             const double* wtb, double* ub, double* vb, double* wb, double* pb, double* gb);
+/* Transpose of velocityForcingGhost and pressureForcingGhost
+ * (src/Forcing.f90:450-734, 362-448) at the block's current geometry and
+ * kinematics (no counterpart in the reference): each ghost value is affine in
+ * the 8 probe values of ut/vt/wt (p for the pressure ghost), each t-ghost
+ * value a copy of u/v/w (p) at the TS position.  Adds G^T gb to
+ * (ub, vb, wb, pb, utb, vtb, wtb); gb as in bcfd_momentum_adjoint_ts. */
+int bcfd_forcing_ghost_adjoint(bcfd_handle h, const double* gb, double* ub, double* vb, double* wb, double* pb,
+                               double* utb, double* vtb, double* wtb);
 
 /* ---- coupling maps and their transposes (no counterpart in the reference) --
  * Interface h, component comp (0 p, 1 u, 2 v, 3 w), natural-layout host
@@ -346,6 +369,30 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
                      const double* wv, const double* ww, const double* wp, const double* stress_seed, double mu_f,
                      double rho_f, double adj_tol, int64_t adj_itmax, double* J, double* dj_duc,
                      double* dj_dkin, double* gu, double* gv, double* gw, double* gp);
+/* Discrete adjoint of n_steps whole time steps through a moving body (no
+ * counterpart in the reference): the objective J of bcfd_adjoint_run on block
+ * h, whose body is the one moving body of the run, and dj_dmotion[5] = dJ/d
+ * of its motion parameters (heave amplitude yamp, pitch amplitude a0 in
+ * degrees, the pitch phase angle in radians, the pitch frequency freq, the
+ * heave frequency bfreq of bcfd_block_set_body_motion and
+ * bcfd_set_motion_inputs), plus dJ/duc and dJ/d(u,v,w,p)^0 as there.  The
+ * parameters reach J through every step's node placement (rotation about x
+ * through the pivot, translation), the element centroids, normals and lengths
+ * (src/Search.F90:126-258), the normal distances and probe points of the IB
+ * forcing (src/Forcing.f90) and the drag/lift of the moving surface, and
+ * through the rigid-body kinematic scalars the forcing and drag/lift read; the
+ * discrete choices (tags, lists, nearest elements, probe brackets, upwind
+ * branches) are those of the forward run at each step.  Each segment of
+ * `every` steps is recomputed from its checkpoint (fields, tags, nodes and
+ * motion state).  Refused (BCFD_E_STATE): thin-surface cells (surfaces 51/52
+ * of a plate) at any step, a fine-block move during the run, any other
+ * moving body, precision /= 0.  The blocks are left at the forward run's
+ * final state. */
+int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps, int64_t every,
+                            const double* wu, const double* wv, const double* ww, const double* wp,
+                            const double* stress_seed, double mu_f, double rho_f, double adj_tol, int64_t adj_itmax,
+                            double* J, double* dj_duc, double* dj_dmotion, double* gu, double* gv, double* gw,
+                            double* gp);
 /* max over fluid cells of |div u| of the current u,v,w (FP64) */
 int bcfd_max_divergence(bcfd_handle h, double* out);
 /* out[0] = max over fluid cells of |div ut| right after the last velocity

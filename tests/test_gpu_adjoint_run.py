@@ -344,3 +344,96 @@ def test_adjoint_solver_precision_agrees():
         n = np.linalg.norm(g0[k])
         assert np.linalg.norm(g1[k] - g0[k]) <= 1e-8 * max(n, 1e-30), k
     assert np.allclose(g0["kin"], g1["kin"], rtol=1e-8, atol=1e-12 * np.abs(g0["kin"]).max())
+
+
+# ---- stationary thin plate: the predictor's thin-surface ghost substitution ----
+
+PLATE_STEPS = 6
+
+
+def _plate_case():
+    case = synth.plate_single_block(n=24, n_steps=1)
+    return synth.replace(case, epsi=1e-14, pc_ita_max=50000)
+
+
+def _plate_solver(case, state=None):
+    s = Solver(case)
+    s.setup()
+    s.run(1)  # the ghost arrays of the run's start come from this step
+    if state is not None:
+        s.upload_fields(s.handles[0], state)
+    return s
+
+
+def _plate_run(s, case, **kw):
+    return adjoint_run(s, {}, PLATE_STEPS, every=kw.pop("every", 2), stress_seed=DRAG,
+                       mu_f=1.0 / case.re, rho_f=1.0, **kw)
+
+
+def test_plate_drag_gradient_vs_fd():
+    """Every IB cell of the plate is a thin-surface cell: the transposes of
+    the ghost substitution, the final restore and the ghost calls carry the
+    gradient through them.  The ghost arrays the run starts from are held
+    fixed (they came from the step before), as in the forward runs of the
+    finite differences."""
+    case = _plate_case()
+    s0 = _plate_solver(case)
+    g0 = s0.handles[0]
+    assert s0.counts(g0)["TSCellCount"] > 0
+    state = {k: v.copy(order="F") for k, v in s0.fields(g0).items() if k in ("u", "v", "w", "p")}
+    J, duc, g = _plate_run(s0, case)
+    assert np.isfinite(J) and J != 0.0
+    h = 1e-4 * case.uc
+    jp = _plate_run(_plate_solver(case), case, uc=case.uc + h, gradient=False)
+    jm = _plate_run(_plate_solver(case), case, uc=case.uc - h, gradient=False)
+    fd = (jp - jm) / (2 * h)
+    assert abs(fd - duc) <= 1e-4 * abs(fd), (fd, duc)
+    spec = case.blocks[0]
+    m = np.zeros(spec.shape, bool, order="F")
+    m[1:-1, 1:-1, 1:-1] = True
+    m &= s0.tags(g0)["cell"] == 0
+    rng = np.random.default_rng(33)
+    eps = 1e-4
+    for field in ("u", "v", "p"):
+        scale = max(float(np.sqrt(np.mean(state[field] ** 2))), 1e-3)
+        d = np.asfortranarray(rng.normal(size=spec.shape) * m * scale)
+        jp = _plate_run(_plate_solver(case, {**state, field: state[field] + eps * d}), case, gradient=False)
+        jm = _plate_run(_plate_solver(case, {**state, field: state[field] - eps * d}), case, gradient=False)
+        fd = (jp - jm) / (2 * eps)
+        ad = float(np.sum(g[field] * d))
+        assert abs(fd - ad) <= 1e-4 * abs(fd), (field, fd, ad)
+
+
+def test_plate_checkpoint_spacing_does_not_change_the_gradient():
+    case = _plate_case()
+    out = [_plate_run(_plate_solver(case), case, every=k) for k in (1, 4, PLATE_STEPS)]
+    J0, d0, g0 = out[0]
+    for J, duc, g in out[1:]:
+        assert J == J0 and duc == d0
+        for k in g0:
+            np.testing.assert_array_equal(g[k], g0[k])
+
+
+PLATE_KIN0 = np.array([0.05, 0.1, 0.2, 0.3, 0.4, -0.3, -0.4, 0.0])
+
+
+@pytest.mark.parametrize("p", [1, 3, 4])
+def test_plate_drag_gradient_kinematics_vs_fd(p):
+    """dJ/d(ydot, thetaDot1, thetaDDot1) of the thin plate (surface 51):
+    rotation rates reach the surface velocities and dp/dn of the forcing, of
+    the ghost calls and of the drag/lift."""
+    case = _plate_case()
+
+    def run(kin, gradient):
+        s = _plate_solver(case)
+        _set_kin(s, case, kin)
+        return _plate_run(s, case, gradient=gradient)
+
+    J, duc, g = run(PLATE_KIN0, True)
+    # the plate's forward run jumps where a probe changes its bracketing cell
+    # (within 1e-4 of these rates), so the differences take a smaller step
+    h = 1e-6 * max(abs(PLATE_KIN0[p]), 1.0)
+    e = np.zeros(8)
+    e[p] = h
+    fd = (run(PLATE_KIN0 + e, False) - run(PLATE_KIN0 - e, False)) / (2 * h)
+    assert abs(fd - g["kin"][p]) <= 1e-4 * abs(fd), (p, fd, g["kin"][p])

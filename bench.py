@@ -595,6 +595,70 @@ def adjoint_bench(torch, local, steps=4, every=2):
     return out
 
 
+def adjoint_flapping(torch, steps=200, every=20, fd=(), size="full", epsi=1e-12):
+    """Discrete adjoint through the flapping plate of a coarse 128x96x96 +
+    fine 128^3 pair (Re 300, heave 0.5 sin(2 pi 0.25 t), pitch 30 deg
+    sin(2 pi 0.25 t + 90 deg), a thin-surface plate): `steps` FP64 drop-in
+    steps checkpointed every `every`, J = time-averaged drag + lift
+    coefficients, its gradient with respect to the five motion parameters and
+    the inflow velocity; optional central differences ("name:rel" items of
+    `fd`).  The forward solves relax with 2/(1 + sin(pi/n)) and stop at the
+    reference's increment test with epsi (1e-12 by default, so that the
+    differences see the discretisation, not the stopping noise)."""
+    import dataclasses
+    from biocfd import synth
+    from biocfd.adjoint import MOTION_PARAMS, adjoint_run_motion
+    from biocfd.solver import Solver
+    base = synth.with_mixed_omega(synth.replace(synth.flapping_plate_pair(n_steps=steps, size=size), epsi=epsi,
+                                                pc_ita_max=200000))
+    seed = (1.0, 1.0, 1.0, 1.0)
+
+    def make(**mv):
+        blocks = list(base.blocks)
+        own = {k: v for k, v in mv.items() if k in ("yamp", "a0_deg", "bfreq")}
+        inputs = {k: v for k, v in mv.items() if k in ("phase_deg", "freq")}
+        if own:
+            blocks[1] = dataclasses.replace(blocks[1], motion=dataclasses.replace(blocks[1].motion, **own))
+        return synth.replace(base, blocks=blocks, motion=dataclasses.replace(base.motion, **inputs))
+
+    def run(case, gradient):
+        s = Solver(case)
+        s.setup()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = adjoint_run_motion(s, {}, steps, every=every, block=1, gradient=gradient, stress_seed=seed,
+                               mu_f=1.0 / case.re, rho_f=1.0, adj_tol=1e-12)
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        counts = s.counts(s.handles[1])
+        s.close()
+        return r, secs, counts
+
+    (J, duc, g), secs, counts = run(base, True)
+    mo, mi = base.blocks[1].motion, base.motion
+    p0 = {"yamp": mo.yamp, "a0_deg": mo.a0_deg, "phase_deg": mi.phase_deg, "freq": mi.freq, "bfreq": mo.bfreq}
+    cells = sum(b.nx * b.ny * b.nz for b in base.blocks)
+    out = {"workload": f"flapping plate 0.5x0.125x0.0125 (surface 51, thin-surface cells), coarse "
+                       f"{base.blocks[0].nx}x{base.blocks[0].ny}x{base.blocks[0].nz} + fine "
+                       f"{base.blocks[1].nx}x{base.blocks[1].ny}x{base.blocks[1].nz} ({cells / 1e6:.2f}M cells), "
+                       f"Re 300, {steps} FP64 steps, checkpoint every {every}, J = mean of drag + lift coefficients",
+           "epsi": epsi, "adj_tol": 1e-12, "J": J, "dJ_duc": duc, "dJ_dmotion": g["motion"],
+           "seconds_forward_and_reverse": secs, "ms_per_step_forward_and_reverse": 1000.0 * secs / steps,
+           "ts_cells_at_end": counts["TSCellCount"], "ib_cells_at_end": counts["ibCellCount"],
+           "motion_params": p0, "fd": []}
+    for item in fd:
+        name, rel = item.split(":")
+        h = float(rel) * abs(p0[name])
+        jp, sp, _ = run(make(**{name: p0[name] + h}), False)
+        jm, sm, _ = run(make(**{name: p0[name] - h}), False)
+        fdv = (jp - jm) / (2 * h)
+        out["fd"].append({"param": name, "rel_step": float(rel), "fd": fdv, "adjoint": g["motion"][name],
+                          "rel_diff": abs(fdv - g["motion"][name]) / max(abs(fdv), 1e-300)})
+        out["ms_per_step_forward_only"] = 500.0 * (sp + sm) / steps
+        print(json.dumps(out["fd"][-1]), flush=True)
+    return out
+
+
 def profile_run(args):
     """A short run for profiler captures: the chosen workload set up without
     the autotuner, then `--profile-steps` eagerly issued steps of the mixed
@@ -731,6 +795,9 @@ def main():
                     help="nx,ny,nz[,fp32_pairs[,fp64_pairs]]: only the Poisson sweep measurement on that block")
     ap.add_argument("--twelve-only", action="store_true", help="only the twelve-block measurement")
     ap.add_argument("--adjoint-only", action="store_true", help="only the adjoint timing")
+    ap.add_argument("--adjoint-flapping", default="",
+                    help="STEPS[,EVERY[,name:rel;name:rel...]]: only the moving-plate adjoint on the coarse "
+                         "128x96x96 + fine 128^3 pair, with optional central differences")
     ap.add_argument("--alu-only", action="store_true", help="only the arithmetic-rate measurement")
     ap.add_argument("--zero-start", action="store_true",
                     help="start every residual-target solve from pc = 0 (the reference's start)")
@@ -760,6 +827,13 @@ def main():
         import torch
         torch.cuda.set_device(0)
         print(json.dumps(adjoint_bench(torch, 0)), flush=True)
+        return
+    if args.adjoint_flapping:
+        import torch
+        torch.cuda.set_device(0)
+        v = args.adjoint_flapping.split(",")
+        fd = tuple(x for x in v[2].split(";") if x) if len(v) > 2 else ()
+        print(json.dumps(adjoint_flapping(torch, int(v[0]), int(v[1]) if len(v) > 1 else 20, fd)), flush=True)
         return
     if args.alu_only:
         print(json.dumps(alu_rates(0)), flush=True)

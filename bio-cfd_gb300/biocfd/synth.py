@@ -396,6 +396,37 @@ def multi_block(coarse=(48, 32, 32), domain=(3.0, 2.0, 2.0),
     return case
 
 
+def flapping_plate_pair(n_steps: int = 200, size: str = "full", seed: int = SEED) -> Case:
+    """A coarse block with one nested fine block at ratio 2 around a flapping
+    plate (surface 51): heave yamp sin(2 pi 0.25 t), pitch 30 deg
+    sin(2 pi 0.25 t + 90 deg) about x, Re 300 on the chord, towed by 0.05
+    fine cells per step.  "full": coarse 128x96x96 over 8x6x6 + fine
+    128x128x128 over 4^3 (dx 1/32), plate 0.5x0.125x0.0125, yamp 0.5;
+    "small": coarse 64x48x48 over 4x3x3 + fine 80x80x64 (dx 1/32), plate
+    0.15x0.0625x0.01, yamp 0.1.  The fine block is wide enough that the
+    reference's block-move margins (src/Search.F90:1013-1040) never trigger."""
+    if size == "full":
+        coarse, domain, box = (128, 96, 96), (8.0, 6.0, 6.0), ((2.0, 6.0), (1.0, 5.0), (1.0, 5.0))
+        axes, yamp = (0.5, 0.125, 0.0125), 0.5
+    else:
+        coarse, domain, box = (64, 48, 48), (4.0, 3.0, 3.0), ((0.75, 3.25), (0.25, 2.75), (0.5, 2.5))
+        axes, yamp = (0.15, 0.0625, 0.01), 0.1
+    chord = 2.0 * axes[0]
+    mo = Motion(a0_deg=30.0, bfreq=0.25, yamp=yamp)
+    mi = MotionInputs(aoa_deg=0.0, phase_deg=90.0, piv_pt=0.0, freq=0.25, dxmin=1.0 / 32)
+    case = multi_block(coarse=coarse, domain=domain, fine_boxes=(box,), body=0, plate=True, plate_axes=axes,
+                       diameter=chord, reynolds=300.0, motion=mo, motion_inputs=mi, n_steps=n_steps, seed=seed)
+    # the search box also covers the tow in -x (0.05 dxmin per step)
+    fs = case.blocks[1]
+    c = np.array(fs.motion.shift)
+    ax = np.asarray(axes)
+    reach = ax + np.array([0.0, yamp + ax[1], ax[1]])
+    lo = c - reach
+    lo[0] -= 0.05 * mi.dxmin * (n_steps + 2)
+    fs.search_box = search_box_for(fs, lo, c + reach)
+    return replace(case, name=f"flapping_plate_pair_{size}")
+
+
 def moving_plate_block_move(n_steps: int = 3, seed: int = SEED) -> Case:
     """A coarse 48x32x32 block over 1.5x1x1 (dx 1/32) with one fine block at
     ratio 2 around a heaving, pitching, towed plate, sized so that the

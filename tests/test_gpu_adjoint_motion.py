@@ -6,7 +6,9 @@ over 6 FP64 steps from the set-up:
   so only the pitch kinematics reach J from the pitch parameters;
 * a plate thinner than a cell (surface 51) that heaves, pitches about x and
   is towed: every IB cell is a thin-surface (TS) cell, so the predictor's
-  ghost substitution, the ghost calls and the node rotation are transposed.
+  ghost substitution, the ghost calls and the node rotation are transposed;
+* the same kind of plate in the fine block of a coarse/fine pair (the
+  coupling transposes inside the moving run).
 The gradients with respect to the motion parameters, the inflow velocity
 and the initial state are checked against central finite differences of the
 forward run at 1e-4 relative perturbations (bar: 1e-4 relative, plus an
@@ -38,22 +40,29 @@ BODIES = ("sphere", "plate")
 def _base(body):
     if body == "sphere":
         return synth.heaving_sphere_single_block(n=24, n_steps=N_STEPS)
+    if body == "pair":
+        return synth.flapping_plate_pair(n_steps=N_STEPS, size="small")
     return synth.moving_plate_single_block(n=24, n_steps=N_STEPS)
+
+
+def _mover(case):
+    return next(q for q, b in enumerate(case.blocks) if b.motion is not None)
 
 
 def _case(body, **motion):
     case = synth.replace(_base(body), epsi=1e-14, pc_ita_max=50000)
-    spec = case.blocks[0]
+    q = _mover(case)
+    blocks = list(case.blocks)
     own = {k: v for k, v in motion.items() if k in ("yamp", "a0_deg", "bfreq")}
     inputs = {k: v for k, v in motion.items() if k in ("phase_deg", "freq")}
     if own:
-        spec = dataclasses.replace(spec, motion=dataclasses.replace(spec.motion, **own))
+        blocks[q] = dataclasses.replace(blocks[q], motion=dataclasses.replace(blocks[q].motion, **own))
     mi = dataclasses.replace(case.motion, **inputs)
-    return synth.replace(case, blocks=[spec], motion=mi)
+    return synth.replace(case, blocks=blocks, motion=mi)
 
 
 def _params(case):
-    mo, mi = case.blocks[0].motion, case.motion
+    mo, mi = case.blocks[_mover(case)].motion, case.motion
     return {"yamp": mo.yamp, "a0_deg": mo.a0_deg, "phase_deg": mi.phase_deg, "freq": mi.freq, "bfreq": mo.bfreq}
 
 
@@ -66,8 +75,8 @@ def _solver(case):
 
 
 def _run(case, every=2, gradient=True, uc=None):
-    return adjoint_run_motion(_solver(case), {}, N_STEPS, every=every, gradient=gradient, stress_seed=DRAG,
-                              mu_f=1.0 / case.re, rho_f=1.0, uc=uc)
+    return adjoint_run_motion(_solver(case), {}, N_STEPS, every=every, block=_mover(case), gradient=gradient,
+                              stress_seed=DRAG, mu_f=1.0 / case.re, rho_f=1.0, uc=uc)
 
 
 _BASE = {}
@@ -80,18 +89,18 @@ def _base_run(body):
     return _BASE[body]
 
 
-@pytest.mark.parametrize("body", BODIES)
+@pytest.mark.parametrize("body", BODIES + ("pair",))
 def test_moving_body_gradients_vs_fd(body):
     case, (J, duc, g) = _base_run(body)
     assert np.isfinite(J) and J != 0.0
-    if body == "plate":
+    if body != "sphere":
         s = _solver(case)
-        assert s.counts(s.handles[0])["TSCellCount"] > 0
+        assert s.counts(s.handles[_mover(case)])["TSCellCount"] > 0
     p0 = _params(case)
     gm = g["motion"]
     heave = abs(gm["yamp"]) * p0["yamp"]
     assert heave > 1e-6 * abs(J), gm  # the heave moves the drag
-    rel = 1e-6 if body == "plate" else 1e-4
+    rel = 1e-4 if body == "sphere" else 1e-6
     for name in MOTION_PARAMS:
         h = rel * abs(p0[name])
         jp = _run(_case(body, **{name: p0[name] + h}), gradient=False)

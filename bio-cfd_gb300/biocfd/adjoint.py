@@ -156,8 +156,8 @@ def adjoint_run_motion(solver, weights: dict, n_steps: int, every: int = 20, blo
     (J, dJ/duc, {"u","v","w","p": dJ/dx^0 of the block, "motion": {name:
     dJ/d name for MOTION_PARAMS}}).  The body's tags, nodes and motion state
     are checkpointed with the fields; the block advances by n_steps exactly
-    as solver.run(n_steps) would.  A body with thin-surface cells (surfaces
-    51/52) is refused."""
+    as solver.run(n_steps) would.  Thin-surface cells (surfaces 51/52) are
+    differentiated; a fine-block move during the run is refused."""
     c = solver.case
     g = solver.handles[block]
     shape = c.blocks[block].shape

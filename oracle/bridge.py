@@ -14,15 +14,21 @@ import numpy as np
 
 from . import build as _build
 
-_LIBS: Dict[bool, C.CDLL] = {}
+_LIBS: Dict[tuple, C.CDLL] = {}
 
 _f64 = C.c_double
 _i64 = C.c_int64
 
 
-def lib(checked: bool = True) -> C.CDLL:
-    if checked not in _LIBS:
-        L = C.CDLL(str(_build.build(checked=checked)))
+def lib(checked: bool = True, dual: bool = False) -> C.CDLL:
+    key = (checked, dual)
+    if key not in _LIBS:
+        L = C.CDLL(str(_build.build(checked=checked, dual=dual)))
+        L.orc_lanes.restype = C.c_int
+        L.orc_set_fd.argtypes = [_i64, C.c_char_p, C.c_int, _f64]
+        L.orc_get_fd.restype = _f64
+        L.orc_get_fd.argtypes = [_i64, C.c_char_p, C.c_int]
+        L.orc_arg_tangent.argtypes = [C.c_char_p, C.c_int, _f64]
         L.orc_block_new.restype = _i64
         L.orc_block_new.argtypes = [_i64, _i64, _i64]
         L.orc_alloc_surface.argtypes = [_i64, _i64, _i64]
@@ -65,21 +71,37 @@ def lib(checked: bool = True) -> C.CDLL:
             "orc_fine_update_mv": [_i64], "orc_stress_calculation": [_i64, _f64, _f64],
         }.items():
             getattr(L, name).argtypes = args
-        _LIBS[checked] = L
-    return _LIBS[checked]
+        _LIBS[key] = L
+    return _LIBS[key]
 
 
 class Oracle:
     """One oracle instance (the oracle keeps module-global block/interface lists)."""
 
-    def __init__(self, checked: bool = True):
-        self.L = lib(checked)
+    def __init__(self, checked: bool = True, dual: bool = False):
+        """``dual``: the tangent-linear build (``orc_lanes()`` tangents next
+        to every value; ``arr`` then returns the value part, ``tangent`` a
+        lane's tangent part, both as views into the oracle's storage)."""
+        self.L = lib(checked, dual)
+        self.lanes = int(self.L.orc_lanes())
         self.L.orc_reset()
+        self.L.orc_clear_arg_tangents()
+        # {(block, scalar name): [(lane, tangent)]}: seeds applied whenever
+        # setf sets that scalar (set-up sets the motion parameters)
+        self.scalar_seeds: Dict[tuple, list] = {}
         self.nblocks = 0
         self.case = None
 
     # ---- raw access -------------------------------------------------------
     def arr(self, g: int, name: str) -> np.ndarray:
+        return self._view(g, name, 0)
+
+    def tangent(self, g: int, name: str, lane: int) -> np.ndarray:
+        """Lane ``lane``'s tangent of a floating-point array (dual build)."""
+        assert 0 <= lane < self.lanes, lane
+        return self._view(g, name, 1 + lane)
+
+    def _view(self, g: int, name: str, part: int) -> np.ndarray:
         n, kind = _i64(), C.c_int()
         dims = (_i64 * 3)()
         p = self.L.orc_array(g, name.encode(), C.byref(n), dims, C.byref(kind))
@@ -90,7 +112,14 @@ class Oracle:
             shape.pop()
         shape = tuple(shape)
         if n.value == 0:
-            return np.zeros(shape, dtype=np.float64 if kind.value == 0 else np.int64, order="F")
+            return np.zeros(shape, dtype=np.int64 if kind.value == 1 else np.float64, order="F")
+        if kind.value == 2:
+            # dual numbers: (1 + lanes) doubles per element, value first
+            w = 1 + self.lanes
+            buf = (_f64 * (n.value * w)).from_address(p)
+            full = np.ndarray((w,) + shape, dtype=np.float64, buffer=buf, order="F")
+            return full[part]
+        assert part == 0, "tangents exist in the dual build only"
         ct = _f64 if kind.value == 0 else _i64
         buf = (ct * n.value).from_address(p)
         return np.ndarray(shape, dtype=np.float64 if kind.value == 0 else np.int64, buffer=buf, order="F")
@@ -106,6 +135,19 @@ class Oracle:
 
     def setf(self, g, name, v):
         assert self.L.orc_set_f(g, name.encode(), float(v)) == 0, name
+        for lane, d in self.scalar_seeds.get((g, name), ()):
+            self.setf_tangent(g, name, lane, d)
+
+    def setf_tangent(self, g, name, lane, d):
+        assert self.L.orc_set_fd(g, name.encode(), int(lane), float(d)) == 0, name
+
+    def getf_tangent(self, g, name, lane):
+        return float(self.L.orc_get_fd(g, name.encode(), int(lane)))
+
+    def seed_arg(self, name, lane, d):
+        """Tangent ``d`` in lane ``lane`` of a call argument ("uc",
+        "phase_angle", "freq", "aoa", "piv_pt") for every later call."""
+        assert self.L.orc_arg_tangent(name.encode(), int(lane), float(d)) == 0, name
 
     def err(self, g) -> int:
         return int(self.L.orc_err(g))
@@ -263,3 +305,41 @@ class Oracle:
 
     def iters(self):
         return [self.geti(g, "nIterPcor") for g in range(1, self.nblocks + 1)]
+
+
+# tangent lanes of drag_objective: the five motion parameters of the moving
+# body (pitch and phase in degrees) and the inflow velocity
+TANGENT_PARAMS = ("yamp", "a0_deg", "phase_deg", "freq", "bfreq", "uc")
+STRESS_NAMES = ("viscous_drag", "pressure_drag", "viscous_lift", "pressure_lift")
+
+
+def drag_objective(case, n_steps: int, block: int, stress_seed, mu_f: float, rho_f: float, dual: bool = False):
+    """J = (1/n_steps) sum over the steps of sum_t stress_seed[t] * C_t, C_t
+    the drag/lift coefficients of ``block`` (0-based) after each step, from
+    a run of the oracle from the set-up.  With ``dual`` the run is the FP64
+    tangent-linear model (the dual-number build) and the result is (J,
+    {name: dJ/d name for TANGENT_PARAMS}); otherwise J."""
+    o = Oracle(dual=dual)
+    g = block + 1
+    nl = len(TANGENT_PARAMS) if dual else 0
+    if dual:
+        assert o.lanes >= nl, o.lanes
+        o.scalar_seeds = {(g, "yamp"): [(0, 1.0)], (g, "a0"): [(1, 1.0)], (g, "bfreq"): [(4, 1.0)]}
+        o.seed_arg("phase_angle", 2, np.pi / 180.0)
+        o.seed_arg("freq", 3, 1.0)
+        o.seed_arg("uc", 5, 1.0)
+    o.setup(case)
+    J = 0.0
+    dJ = np.zeros(nl)
+    for _ in range(n_steps):
+        o.step()
+        o.L.orc_stress_calculation(g, mu_f, rho_f)
+        for t, nm in enumerate(STRESS_NAMES):
+            J += stress_seed[t] * o.getf(g, nm)
+            if dual:
+                dJ += stress_seed[t] * np.array([o.getf_tangent(g, nm, l) for l in range(nl)])
+    for g2 in range(1, o.nblocks + 1):
+        assert o.err(g2) == 0, (g2, o.err(g2))
+    if not dual:
+        return J / n_steps
+    return J / n_steps, dict(zip(TANGENT_PARAMS, dJ / n_steps))

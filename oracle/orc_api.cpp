@@ -41,7 +41,7 @@ I2* i2_of(Block& b, const std::string& n) {
 #undef M
   return nullptr;
 }
-A2<double>* f2_of(Block& b, const std::string& n) {
+A2<real>* f2_of(Block& b, const std::string& n) {
 #define M(x) if (n == #x) return &b.x;
   M(ca_uu) M(ck_uu) M(ca_vv) M(ck_vv) M(ca_ww) M(ck_ww) M(ca_uv) M(ck_uv) M(ca_uw) M(ck_uw)
   M(ca_vu) M(ck_vu) M(ca_vw) M(ck_vw) M(ca_wu) M(ck_wu) M(ca_wv) M(ck_wv) M(Acx) M(Acy) M(Acz)
@@ -55,7 +55,7 @@ I1* i1_of(Block& b, const std::string& n) {
 #undef M
   return nullptr;
 }
-double* fs_of(Block& b, const std::string& n) {
+real* fs_of(Block& b, const std::string& n) {
 #define M(x) if (n == #x) return &b.x;
   M(dx) M(dy) M(dz) M(omega) M(derr1) M(derr2) M(derrStdSt) M(xdot) M(ydot) M(yddot)
   M(thetaDot) M(thetaDDot) M(thetaDot1) M(thetaDDot1) M(thetaDot2) M(thetaDDot2) M(alphaDot)
@@ -75,9 +75,64 @@ int64_t* is_of(Block& b, const std::string& n) {
   return nullptr;
 }
 
+// tangents of the call arguments a run differentiates with respect to
+// (lane l of the dual build): "uc", "phase_angle", "freq", "aoa", "piv_pt"
+struct ArgTangent {
+  std::string name;
+  int lane;
+  double d;
+};
+std::vector<ArgTangent> g_arg_tangents;
+
+real arg(const char* name, double v) {
+  real r = v;
+#ifdef ORC_DUAL
+  for (const ArgTangent& t : g_arg_tangents)
+    if (t.name == name) r.d[t.lane] = t.d;
+#else
+  (void)name;
+#endif
+  return r;
+}
+
+// element kind of a floating-point array: 0 = double, 2 = dual number
+// (value followed by kLanes tangents)
+constexpr int kRealKind = kLanes ? 2 : 0;
+
 }  // namespace
 
 extern "C" {
+
+// number of tangent lanes (0: the plain double build)
+int orc_lanes() { return kLanes; }
+
+// tangent lane `lane` of a named block scalar (dual build only)
+int orc_set_fd(int64_t g, const char* name, int lane, double d) {
+  real* p = fs_of(blk_of(g), name);
+  if (!p || lane < 0 || lane >= kLanes) return -1;
+#ifdef ORC_DUAL
+  p->d[lane] = d;
+#else
+  (void)d;
+#endif
+  return 0;
+}
+double orc_get_fd(int64_t g, const char* name, int lane) {
+  real* p = fs_of(blk_of(g), name);
+  if (!p || lane < 0 || lane >= kLanes) return 0.0;
+#ifdef ORC_DUAL
+  return p->d[lane];
+#else
+  return 0.0;
+#endif
+}
+// seeds the tangent of a call argument for every later call that takes it
+int orc_arg_tangent(const char* name, int lane, double d) {
+  if (lane < 0 || lane >= kLanes) return -1;
+  g_arg_tangents.push_back({name, lane, d});
+  return 0;
+}
+void orc_clear_arg_tangents() { g_arg_tangents.clear(); }
 
 void orc_reset() {
   for (Block* b : g_blocks) delete b;
@@ -109,16 +164,17 @@ void orc_alloc_surface(int64_t g, int64_t n_elems, int64_t n_nodes) {
 }
 
 // Pointer to the storage of a named array; *n = element count, dims = extents
-// (column-major), *kind = 0 for double and 1 for int64.  nullptr if unknown.
+// (column-major), *kind = 0 for double, 1 for int64 and 2 for dual numbers
+// (value followed by orc_lanes() tangents per element).  nullptr if unknown.
 void* orc_array(int64_t g, const char* name, int64_t* n, int64_t dims[3], int* kind) {
   Block& b = blk_of(g);
   const std::string s(name);
   dims[0] = dims[1] = dims[2] = 1;
-  if (F1* a = f1_of(b, s)) { *n = a->size(); dims[0] = *n; *kind = 0; return a->d.data(); }
-  if (F3* a = f3_of(b, s)) { *n = (int64_t)a->d.size(); dims[0] = a->n1; dims[1] = a->n2; dims[2] = a->n3; *kind = 0; return a->d.data(); }
+  if (F1* a = f1_of(b, s)) { *n = a->size(); dims[0] = *n; *kind = kRealKind; return a->d.data(); }
+  if (F3* a = f3_of(b, s)) { *n = (int64_t)a->d.size(); dims[0] = a->n1; dims[1] = a->n2; dims[2] = a->n3; *kind = kRealKind; return a->d.data(); }
   if (I3* a = i3_of(b, s)) { *n = (int64_t)a->d.size(); dims[0] = a->n1; dims[1] = a->n2; dims[2] = a->n3; *kind = 1; return a->d.data(); }
   if (I2* a = i2_of(b, s)) { *n = (int64_t)a->d.size(); dims[0] = a->n1; dims[1] = a->n2; *kind = 1; return a->d.data(); }
-  if (auto* a = f2_of(b, s)) { *n = (int64_t)a->d.size(); dims[0] = a->n1; dims[1] = a->n2; *kind = 0; return a->d.data(); }
+  if (auto* a = f2_of(b, s)) { *n = (int64_t)a->d.size(); dims[0] = a->n1; dims[1] = a->n2; *kind = kRealKind; return a->d.data(); }
   if (I1* a = i1_of(b, s)) { *n = a->size(); dims[0] = *n; *kind = 1; return a->d.data(); }
   *n = 0;
   *kind = -1;
@@ -126,14 +182,14 @@ void* orc_array(int64_t g, const char* name, int64_t* n, int64_t dims[3], int* k
 }
 
 int orc_set_f(int64_t g, const char* name, double v) {
-  double* p = fs_of(blk_of(g), name);
+  real* p = fs_of(blk_of(g), name);
   if (!p) return -1;
   *p = v;
   return 0;
 }
 double orc_get_f(int64_t g, const char* name) {
-  double* p = fs_of(blk_of(g), name);
-  return p ? *p : 0.0;
+  real* p = fs_of(blk_of(g), name);
+  return p ? val(*p) : 0.0;
 }
 int orc_set_i(int64_t g, const char* name, int64_t v) {
   int64_t* p = is_of(blk_of(g), name);
@@ -146,11 +202,12 @@ int64_t orc_get_i(int64_t g, const char* name) {
   return p ? *p : 0;
 }
 double orc_linear_interpolation(double x, double x0, double x1, double y0, double y1) {
-  return linear_interpolation(x, x0, x1, y0, y1);
+  return val(linear_interpolation(x, x0, x1, y0, y1));
 }
 double orc_bilinear_interpolation(double x, double y, double x1, double x2, double y1, double y2,
                                   const double* f) {
-  return bilinear_interpolation(x, y, x1, x2, y1, y2, f);
+  const real fr[4] = {f[0], f[1], f[2], f[3]};
+  return val(bilinear_interpolation(x, y, x1, x2, y1, y2, fr));
 }
 
 int orc_err(int64_t g) { return blk_of(g).err; }
@@ -163,7 +220,7 @@ void orc_derive_grids(int64_t g) { derive_grids(blk_of(g)); }
 void orc_non_uni_coeff(int64_t g) { non_uni_coeff(blk_of(g)); }
 void orc_coefficient_matrix(int64_t g, int is_coarse) { coefficient_matrix(blk_of(g), is_coarse != 0); }
 void orc_ns_momentum(int64_t g, double dt, double re) { ns_momentum_2order(blk_of(g), dt, re); }
-void orc_velocity_bc(int64_t g, double dt, double uc) { velocity_bc(blk_of(g), dt, uc); }
+void orc_velocity_bc(int64_t g, double dt, double uc) { velocity_bc(blk_of(g), dt, arg("uc", uc)); }
 void orc_solid_cell_bc(int64_t g) { solid_cell_bc(blk_of(g)); }
 void orc_solid_cell_bc_move(int64_t g) { solid_cell_bc_move(blk_of(g)); }
 void orc_velocity_forcing1(int64_t g) { velocity_forcing1(blk_of(g)); }
@@ -191,11 +248,12 @@ void orc_block_move_stage() {
 void orc_tagging_th_move(int64_t g) { tagging_th_move(blk_of(g), g); }
 void orc_shift_surface_nodes_initial(int64_t g, double aoa, double piv_pt, int64_t ita, double deltat,
                                      double dxmin, double totime) {
-  shift_surface_nodes_initial(blk_of(g), aoa, piv_pt, ita, deltat, dxmin, totime);
+  shift_surface_nodes_initial(blk_of(g), arg("aoa", aoa), arg("piv_pt", piv_pt), ita, deltat, dxmin, totime);
 }
 void orc_compute_surface_variables(int64_t g, double phase_angle, double piv_pt, int64_t ita,
                                    double deltat, double dxmin, double freq, double totime) {
-  compute_surface_variables(blk_of(g), phase_angle, piv_pt, ita, deltat, dxmin, freq, totime);
+  compute_surface_variables(blk_of(g), arg("phase_angle", phase_angle), arg("piv_pt", piv_pt), ita, deltat,
+                            dxmin, arg("freq", freq), totime);
 }
 void orc_tagging_th_core(int64_t g) { tagging_th_core(blk_of(g)); }
 void orc_selective_retagging(int64_t g) { selective_retagging_th(blk_of(g)); }
@@ -211,7 +269,7 @@ void orc_redblack_sor(int64_t g, int64_t itmax, double dt, double epsi) {
   redblack_sor_linear(blk_of(g), itmax, dt, epsi);
 }
 void orc_poisson_solver(int64_t itmax, double epsi, double dt, double uc) {
-  poisson_solver(itmax, epsi, dt, uc, 1, (int64_t)g_blocks.size(), 1);
+  poisson_solver(itmax, epsi, dt, arg("uc", uc), 1, (int64_t)g_blocks.size(), 1);
 }
 void orc_fine_block_cell() { fine_block_cell(); }
 void orc_fine_update_pc_bd() { fine_update_pc_bd(); }

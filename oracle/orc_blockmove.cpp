@@ -26,7 +26,7 @@ int64_t round_move(int64_t m, int64_t factor) {
 }
 
 // first index i in [from, n] with v(i) > s; `fallback` when none
-int64_t first_above(const F1& v, int64_t from, int64_t n, double s, int64_t fallback) {
+int64_t first_above(const F1& v, int64_t from, int64_t n, real s, int64_t fallback) {
   for (int64_t i = from; i <= n; ++i)
     if (v(i) > s) return i;
   return fallback;
@@ -43,41 +43,41 @@ void block_move_check(int64_t& coarse_flcnt_check) {
     // a block without a moving plate has no such nodes (mk = 0, an
     // out-of-bounds read there) and is skipped, as the library does
     if (fb.mk < 1 || fb.mkx1 < 1) continue;
-    const double mg1 = (double)fb.cintp * blk_of(1).dx;
-    const double marginx = 4.5 * mg1, marginy = 5 * mg1, marginz = 1.52 * mg1;
+    const real mg1 = (real)fb.cintp * blk_of(1).dx;
+    const real marginx = 4.5 * mg1, marginy = 5 * mg1, marginz = 1.52 * mg1;
     const int64_t factor = it.b_msh / it.a_msh;
-    const double yval_up = std::fmax(fb.ynode1(fb.mk), fb.nxty_cent + 0.02);
-    const double yval_dw = std::fmin(fb.ynode1(fb.mk), fb.nxty_cent - 0.02);
-    const double xval_lt = fb.xnode1(fb.mkx1);
+    const real yval_up = fmax(fb.ynode1(fb.mk), fb.nxty_cent + 0.02);
+    const real yval_dw = fmin(fb.ynode1(fb.mk), fb.nxty_cent - 0.02);
+    const real xval_lt = fb.xnode1(fb.mkx1);
     fb.move_amty = fb.move_amtx = fb.move_amtz = 0;
-    const bool trig = std::fabs(xval_lt - it.xintf_start) <= marginx ||
-                      std::fabs(fb.piv_z - it.zintf_start) <= marginz ||
-                      std::fabs(fb.piv_z - it.zintf_end) <= marginz ||
-                      std::fabs(yval_dw - it.yintf_start) <= marginy || std::fabs(yval_up - it.yintf_end) <= marginy;
+    const bool trig = fabs(xval_lt - it.xintf_start) <= marginx ||
+                      fabs(fb.piv_z - it.zintf_start) <= marginz ||
+                      fabs(fb.piv_z - it.zintf_end) <= marginz ||
+                      fabs(yval_dw - it.yintf_start) <= marginy || fabs(yval_up - it.yintf_end) <= marginy;
     if (!trig) continue;
     fb.move_check = 1;
     fb.blk_mv_tag = 1;
     coarse_flcnt_check = 1;
-    if (std::fabs(yval_dw - it.yintf_start) <= marginy || std::fabs(yval_up - it.yintf_end) <= marginy) {
-      fb.move_amty = round_move((int64_t)std::floor((fb.nxty_cent - fb.inity_cent) / fb.dy), factor);
+    if (fabs(yval_dw - it.yintf_start) <= marginy || fabs(yval_up - it.yintf_end) <= marginy) {
+      fb.move_amty = round_move((int64_t)val(floor((fb.nxty_cent - fb.inity_cent) / fb.dy)), factor);
       fb.inity_cent = fb.nxty_cent;
     }
-    if (std::fabs(xval_lt - it.xintf_start) < marginx) {
-      fb.move_amtx = round_move((int64_t)std::floor((fb.nxtx_cent - fb.initx_cent) / fb.dx) - factor, factor);
+    if (fabs(xval_lt - it.xintf_start) < marginx) {
+      fb.move_amtx = round_move((int64_t)val(floor((fb.nxtx_cent - fb.initx_cent) / fb.dx)) - factor, factor);
       fb.initx_cent = fb.nxtx_cent;
     }
-    if (std::fabs(fb.piv_z - it.zintf_start) < (0.500 - 0.410 - mg1) ||
-        std::fabs(fb.piv_z - it.zintf_end) < (0.600 - 0.500 - mg1)) {
-      fb.move_amtz = round_move((int64_t)std::floor((fb.nxtz_cent - fb.initz_cent) / fb.dz), factor);
+    if (fabs(fb.piv_z - it.zintf_start) < (0.500 - 0.410 - mg1) ||
+        fabs(fb.piv_z - it.zintf_end) < (0.600 - 0.500 - mg1)) {
+      fb.move_amtz = round_move((int64_t)val(floor((fb.nxtz_cent - fb.initz_cent) / fb.dz)), factor);
       fb.initz_cent = fb.nxtz_cent;
     }
-    const double cx = fb.move_amtx * fb.dx, cy = fb.move_amty * fb.dy, cz = fb.move_amtz * fb.dz;
-    it.xintf_st_new = std::fmax(it.xintf_start, it.xintf_start + cx);
-    it.xintf_en_new = std::fmin(it.xintf_end, it.xintf_end + cx);
-    it.yintf_st_new = std::fmax(it.yintf_start, it.yintf_start + cy);
-    it.yintf_en_new = std::fmin(it.yintf_end, it.yintf_end + cy);
-    it.zintf_st_new = std::fmax(it.zintf_start, it.zintf_start + cz);
-    it.zintf_en_new = std::fmin(it.zintf_end, it.zintf_end + cz);
+    const real cx = fb.move_amtx * fb.dx, cy = fb.move_amty * fb.dy, cz = fb.move_amtz * fb.dz;
+    it.xintf_st_new = fmax(it.xintf_start, it.xintf_start + cx);
+    it.xintf_en_new = fmin(it.xintf_end, it.xintf_end + cx);
+    it.yintf_st_new = fmax(it.yintf_start, it.yintf_start + cy);
+    it.yintf_en_new = fmin(it.yintf_end, it.yintf_end + cy);
+    it.zintf_st_new = fmax(it.zintf_start, it.zintf_start + cz);
+    it.zintf_en_new = fmin(it.zintf_end, it.zintf_end + cz);
     it.xintf_start = it.xintf_start + cx;
     it.xintf_end = it.xintf_end + cx;
     it.yintf_start = it.yintf_start + cy;
@@ -101,7 +101,7 @@ void block_move_check(int64_t& coarse_flcnt_check) {
 // Search.F90:1208-1264: the grid shifted by whole cells (spacings unchanged)
 void change_block_coords(Block& b) {
   if (b.move_check != 1) return;
-  const double cz = b.move_amtz * b.dz, cy = b.move_amty * b.dy, cx = b.move_amtx * b.dx;
+  const real cz = b.move_amtz * b.dz, cy = b.move_amty * b.dy, cx = b.move_amtx * b.dx;
   for (int64_t i = 1; i <= b.nx + 3; ++i) b.x1(i) = b.x1(i) + cx;
   for (int64_t i = 1; i <= b.ny + 3; ++i) b.y1(i) = b.y1(i) + cy;
   for (int64_t i = 1; i <= b.nz + 3; ++i) b.z1(i) = b.z1(i) + cz;

@@ -29,6 +29,8 @@
 #include <vector>
 #include <string>
 
+#include "orc_real.h"
+
 #ifndef ORC_NOCHECK
 #define ORC_CHECK(cond, what)                                                    \
   do {                                                                           \
@@ -100,8 +102,8 @@ struct A3 {
   }
 };
 
-using F1 = A1<double>;
-using F3 = A3<double>;
+using F1 = A1<real>;
+using F3 = A3<real>;
 using I1 = A1<int64_t>;
 using I2 = A2<int64_t>;
 using I3 = A3<int64_t>;
@@ -109,9 +111,9 @@ using I3 = A3<int64_t>;
 // Mirror of Block_t (src/Blocks.f90:13-81), hot-path members only.
 struct Block {
   int64_t nx = 0, ny = 0, nz = 0;
-  double dx = 0, dy = 0, dz = 0;
-  double omega = 1.0;
-  double derr1 = 0, derr2 = 0, derrStdSt = 0;
+  real dx = 0, dy = 0, dz = 0;
+  real omega = 1.0;
+  real derr1 = 0, derr2 = 0, derrStdSt = 0;
   int64_t nIterPcor = 0, cintp = 3;
   int64_t i_startSearch = 0, i_endSearch = -1, j_startSearch = 0, j_endSearch = -1,
           k_startSearch = 0, k_endSearch = -1;
@@ -126,15 +128,15 @@ struct Block {
   int64_t cpy_x_start_mv = 0, cpy_x_end_mv = 0, cpy_y_start_mv = 0, cpy_y_end_mv = 0, cpy_z_start_mv = 0,
           cpy_z_end_mv = 0;
   // kinematics read by the forcing routines
-  double xdot = 0, ydot = 0, yddot = 0;
-  double thetaDot = 0, thetaDDot = 0, thetaDot1 = 0, thetaDDot1 = 0, thetaDot2 = 0,
+  real xdot = 0, ydot = 0, yddot = 0;
+  real thetaDot = 0, thetaDDot = 0, thetaDot1 = 0, thetaDDot1 = 0, thetaDot2 = 0,
          thetaDDot2 = 0, alphaDot = 0;
-  double piv_x = 0, piv_y = 0, piv_z = 0;
+  real piv_x = 0, piv_y = 0, piv_z = 0;
 
   F1 deltax, deltay, deltaz, x1, y1, z1, xu, yu, zu, xv, yv, zv, xw, yw, zw, xp, yp, zp;
-  A2<double> ca_uu, ck_uu, ca_vv, ck_vv, ca_ww, ck_ww, ca_uv, ck_uv, ca_uw, ck_uw, ca_vu,
+  A2<real> ca_uu, ck_uu, ca_vv, ck_vv, ca_ww, ck_ww, ca_uv, ck_uv, ca_uw, ck_uw, ca_vu,
       ck_vu, ca_vw, ck_vw, ca_wu, ck_wu, ca_wv, ck_wv;
-  A2<double> Acx, Acy, Acz;
+  A2<real> Acx, Acy, Acz;
   F3 b, u, ut, v, vt, w, wt, p, pc, pco;
   F3 u_dum, v_dum, w_dum, p_dum;
   I3 cell, cell2, cell_n, cell_pr, nodeIdTag;
@@ -151,15 +153,15 @@ struct Block {
   // rigid-body motion state of src/Search.F90:49-208
   F1 xnode, ynode, znode;
   I1 ibNodeId;
-  double a0 = 0, bfreq = 0, yamp = 0, xshift = 0, yshift = 0, zshift = 0;
+  real a0 = 0, bfreq = 0, yamp = 0, xshift = 0, yshift = 0, zshift = 0;
   // per-body phase lag of heave and pitch and the shared pitch phase (an
   // extension of the reference's kinematics; 0 = the reference)
-  double lag = 0, lag_phase = 0;
-  double xpth1 = 0, xpth2 = 0, ypth2 = 0, xchg = 0, ychg = 0, xmove = 0, ymove = 0, zmove = 0;
-  double xt = 0, yt = 0, inity_cent = 0, nxty_cent = 0, initx_cent = 0, nxtx_cent = 0,
+  real lag = 0, lag_phase = 0;
+  real xpth1 = 0, xpth2 = 0, ypth2 = 0, xchg = 0, ychg = 0, xmove = 0, ymove = 0, zmove = 0;
+  real xt = 0, yt = 0, inity_cent = 0, nxty_cent = 0, initx_cent = 0, nxtx_cent = 0,
          initz_cent = 0, nxtz_cent = 0;
   // drag/lift from the stress integration (src/StressCalc.f90)
-  double viscous_drag = 0, pressure_drag = 0, viscous_lift = 0, pressure_lift = 0;
+  real viscous_drag = 0, pressure_drag = 0, viscous_lift = 0, pressure_lift = 0;
   // first error raised by a routine on this block (0 = none); the reference
   // has undefined behaviour where the oracle records an error instead
   int err = 0;
@@ -168,9 +170,9 @@ struct Block {
 // Mirror of Interface_t (src/Interfaces.f90:8-25).
 struct Interface {
   I2 px, ux, vx, wx, py, uy, vy, wy, pz, uz, vz, wz;  // (3, n) tables
-  double xintf_start = 0, xintf_end = 0, yintf_start = 0, yintf_end = 0, zintf_start = 0,
+  real xintf_start = 0, xintf_end = 0, yintf_start = 0, yintf_end = 0, zintf_start = 0,
          zintf_end = 0;
-  double xintf_st_new = 0, xintf_en_new = 0, yintf_st_new = 0, yintf_en_new = 0, zintf_st_new = 0,
+  real xintf_st_new = 0, xintf_en_new = 0, yintf_st_new = 0, yintf_en_new = 0, zintf_st_new = 0,
          zintf_en_new = 0;
   int64_t a_blk = 1, b_blk = 2;
   int64_t a_msh = 1, b_msh = 2;
@@ -190,8 +192,8 @@ void allocate_arrays(Block& b);
 void derive_grids(Block& b);
 void non_uni_coeff(Block& b);
 void coefficient_matrix(Block& b, bool is_coarse);
-void ns_momentum_2order(Block& b, double deltat, double re);
-void velocity_bc(Block& b, double deltat, double uc);
+void ns_momentum_2order(Block& b, real deltat, real re);
+void velocity_bc(Block& b, real deltat, real uc);
 void solid_cell_bc(Block& b);
 void solid_cell_bc_move(Block& b);
 void velocity_forcing1(Block& b);
@@ -209,11 +211,11 @@ void find_ts_cells(Block& b);
 void update_velocity_newv(Block& b);
 void compute_div(Block& b);
 void correct_pressure(Block& b);
-void correct_velocity(Block& b, double deltat);
-void redblack_sor_linear(Block& b, int64_t pcItaMax, double deltat, double epsi);
-void poisson_solver(int64_t pcItaMax, double epsi, double deltat, double uc, int64_t start,
+void correct_velocity(Block& b, real deltat);
+void redblack_sor_linear(Block& b, int64_t pcItaMax, real deltat, real epsi);
+void poisson_solver(int64_t pcItaMax, real epsi, real deltat, real uc, int64_t start,
                     int64_t finish, int64_t step);
-void set_interface_detail(const F1& var, double s, double e, int64_t factor, I2& det,
+void set_interface_detail(const F1& var, real s, real e, int64_t factor, I2& det,
                            int64_t& counter, int64_t starter_in);
 void interface_detail(Interface& it);
 void fine_block_cell();
@@ -225,7 +227,7 @@ void coarse_update();
 void coarse_update_newv();
 void coarse_update_pc();
 void fine_update_mv(int64_t g);
-void stress_calculation(Block& b, double mu_f, double rho_f);
+void stress_calculation(Block& b, real mu_f, real rho_f);
 // rigid-body motion (src/Search.F90:49-208, src/ReadInput.f90:403-420)
 void node_ids_from_elements(Block& b);
 void find_dist_node(Block& b);
@@ -235,14 +237,14 @@ void change_block_coords_interfaces(Interface& it, Block& b);
 void change_block_interface(Interface& it, Block& a, Block& b);
 void cellcount_solid_coarse_mv(int64_t& coarse_flcnt_check);
 void tagging_th_move(Block& b, int64_t id);
-void shift_surface_nodes_initial(Block& b, double aoa, double piv_pt, int64_t ita, double deltat,
-                                 double dxmin, double totime);
-void compute_surface_variables(Block& b, double phase_angle, double piv_pt, int64_t ita,
-                               double deltat, double dxmin, double freq, double totime);
+void shift_surface_nodes_initial(Block& b, real aoa, real piv_pt, int64_t ita, real deltat,
+                                 real dxmin, real totime);
+void compute_surface_variables(Block& b, real phase_angle, real piv_pt, int64_t ita,
+                               real deltat, real dxmin, real freq, real totime);
 
 // interpolation primitives (src/Interpolation.f90:16-42)
-double linear_interpolation(double x, double x0, double x1, double y0, double y1);
-double bilinear_interpolation(double x, double y, double x1, double x2, double y1, double y2,
-                              const double f[4]);
+real linear_interpolation(real x, real x0, real x1, real y0, real y1);
+real bilinear_interpolation(real x, real y, real x1, real x2, real y1, real y2,
+                              const real f[4]);
 
 }  // namespace orc

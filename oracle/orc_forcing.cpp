@@ -7,25 +7,25 @@
 namespace orc {
 
 // src/Interpolation.f90:16-22
-double linear_interpolation(double x, double x0, double x1, double y0, double y1) {
+real linear_interpolation(real x, real x0, real x1, real y0, real y1) {
   return y0 + (x - x0) * (y1 - y0) / (x1 - x0);
 }
 
 // src/Interpolation.f90:27-42; f = values at (x1,y1),(x2,y1),(x1,y2),(x2,y2)
-double bilinear_interpolation(double x, double y, double x1, double x2, double y1, double y2,
-                              const double f[4]) {
-  const double numer = f[0] * (x2 - x) * (y2 - y) + f[2] * (x2 - x) * (y - y1) +
+real bilinear_interpolation(real x, real y, real x1, real x2, real y1, real y2,
+                              const real f[4]) {
+  const real numer = f[0] * (x2 - x) * (y2 - y) + f[2] * (x2 - x) * (y - y1) +
                        f[1] * (x - x1) * (y2 - y) + f[3] * (x - x1) * (y - y1);
-  const double denom = (x2 - x1) * (y2 - y1);
+  const real denom = (x2 - x1) * (y2 - y1);
   return numer / denom;
 }
 
 namespace {
 
 // compute_derivative, src/Forcing.f90:1080-1089
-double compute_derivative(double x, double x2, double x1, double p_x, double p_x2, double p_x1) {
-  const double h2 = std::fabs(x2 - x);
-  const double h1 = std::fabs(x1 - x);
+real compute_derivative(real x, real x2, real x1, real p_x, real p_x2, real p_x1) {
+  const real h2 = fabs(x2 - x);
+  const real h1 = fabs(x1 - x);
   return (h1 * h1 * p_x2 - h2 * h2 * p_x1 + (h2 * h2 - h1 * h1) * p_x) /
          (h1 * h2 * (h1 + h2) + 1e-16);
 }
@@ -35,9 +35,9 @@ double compute_derivative(double x, double x2, double x1, double p_x, double p_x
 // (a probe with no bracket, or the staggered offset at index 1); the oracle
 // records ORC_E_NOTFOUND in *err and clamps the corner into the array, as the
 // GPU library does.
-void value_and_derivatives(double x, double y, double z, int64_t i, int64_t j, int64_t k,
+void value_and_derivatives(real x, real y, real z, int64_t i, int64_t j, int64_t k,
                            const F1& xg, const F1& yg, const F1& zg, int offset_axis,
-                           const F3& var, double& val, double der[3], int* err) {
+                           const F3& var, real& val, real der[3], int* err) {
   int64_t ii = i, jj = j, kk = k;
   if (offset_axis == 1) ii = i - 1;
   if (offset_axis == 2) jj = j - 1;
@@ -48,19 +48,19 @@ void value_and_derivatives(double x, double y, double z, int64_t i, int64_t j, i
     jj = std::max<int64_t>(1, std::min<int64_t>(jj, var.n2 - 1));
     kk = std::max<int64_t>(1, std::min<int64_t>(kk, var.n3 - 1));
   }
-  double f[4];
+  real f[4];
   f[0] = var(ii, jj, kk); f[1] = var(ii, jj + 1, kk); f[2] = var(ii, jj, kk + 1); f[3] = var(ii, jj + 1, kk + 1);
-  const double t11 = bilinear_interpolation(y, z, yg(j), yg(j + 1), zg(k), zg(k + 1), f);
+  const real t11 = bilinear_interpolation(y, z, yg(j), yg(j + 1), zg(k), zg(k + 1), f);
   f[0] = var(ii + 1, jj, kk); f[1] = var(ii + 1, jj + 1, kk); f[2] = var(ii + 1, jj, kk + 1); f[3] = var(ii + 1, jj + 1, kk + 1);
-  const double t12 = bilinear_interpolation(y, z, yg(j), yg(j + 1), zg(k), zg(k + 1), f);
+  const real t12 = bilinear_interpolation(y, z, yg(j), yg(j + 1), zg(k), zg(k + 1), f);
   f[0] = var(ii, jj, kk); f[1] = var(ii + 1, jj, kk); f[2] = var(ii, jj, kk + 1); f[3] = var(ii + 1, jj, kk + 1);
-  const double t21 = bilinear_interpolation(x, z, xg(i), xg(i + 1), zg(k), zg(k + 1), f);
+  const real t21 = bilinear_interpolation(x, z, xg(i), xg(i + 1), zg(k), zg(k + 1), f);
   f[0] = var(ii, jj + 1, kk); f[1] = var(ii + 1, jj + 1, kk); f[2] = var(ii, jj + 1, kk + 1); f[3] = var(ii + 1, jj + 1, kk + 1);
-  const double t22 = bilinear_interpolation(x, z, xg(i), xg(i + 1), zg(k), zg(k + 1), f);
+  const real t22 = bilinear_interpolation(x, z, xg(i), xg(i + 1), zg(k), zg(k + 1), f);
   f[0] = var(ii, jj, kk); f[1] = var(ii + 1, jj, kk); f[2] = var(ii, jj + 1, kk); f[3] = var(ii + 1, jj + 1, kk);
-  const double t31 = bilinear_interpolation(x, y, xg(i), xg(i + 1), yg(j), yg(j + 1), f);
+  const real t31 = bilinear_interpolation(x, y, xg(i), xg(i + 1), yg(j), yg(j + 1), f);
   f[0] = var(ii, jj, kk + 1); f[1] = var(ii + 1, jj, kk + 1); f[2] = var(ii, jj + 1, kk + 1); f[3] = var(ii + 1, jj + 1, kk + 1);
-  const double t32 = bilinear_interpolation(x, y, xg(i), xg(i + 1), yg(j), yg(j + 1), f);
+  const real t32 = bilinear_interpolation(x, y, xg(i), xg(i + 1), yg(j), yg(j + 1), f);
   val = linear_interpolation(x, xg(i), xg(i + 1), t11, t12);
   der[0] = compute_derivative(x, xg(i + 1), xg(i), val, t12, t11);
   der[1] = compute_derivative(y, yg(j + 1), yg(j), val, t22, t21);
@@ -70,7 +70,7 @@ void value_and_derivatives(double x, double y, double z, int64_t i, int64_t j, i
 // find_index_in_array, src/Forcing.f90:1165-1183.  The reference leaves the
 // result undefined when no bracket exists; the oracle records an error and
 // returns the start index so that the caller stays in bounds.
-int64_t find_index(Block& b, double value, const F1& a, int64_t start, int64_t finish) {
+int64_t find_index(Block& b, real value, const F1& a, int64_t start, int64_t finish) {
   for (int64_t i = start; i <= finish; ++i) {
     if (i < 1 || i + 1 > a.size()) continue;
     if (value >= a(i) && value < a(i + 1)) return i;
@@ -81,26 +81,26 @@ int64_t find_index(Block& b, double value, const F1& a, int64_t start, int64_t f
   return s;
 }
 
-inline double pt1_of(Block& b, int64_t i, int64_t j, int64_t k, double s2n) {
-  return 1.5 * std::sqrt(b.deltax(i) * b.deltax(i) + b.deltay(j) * b.deltay(j) +
+inline real pt1_of(Block& b, int64_t i, int64_t j, int64_t k, real s2n) {
+  return 1.5 * sqrt(b.deltax(i) * b.deltax(i) + b.deltay(j) * b.deltay(j) +
                          b.deltaz(k) * b.deltaz(k)) +
-         (std::fabs(s2n) - s2n) * 0.5;
+         (fabs(s2n) - s2n) * 0.5;
 }
 
 // The quadratic velocity reconstruction shared by every velocity variant.
-inline double vel_quad(double pos_val, double surf, double dndn_e, double n1, double s2n) {
-  const double cval = surf;
-  const double bval = 2.0 / n1 * (pos_val - surf) - dndn_e;
-  const double aval = dndn_e / n1 - (pos_val - surf) / (n1 * n1);
+inline real vel_quad(real pos_val, real surf, real dndn_e, real n1, real s2n) {
+  const real cval = surf;
+  const real bval = 2.0 / n1 * (pos_val - surf) - dndn_e;
+  const real aval = dndn_e / n1 - (pos_val - surf) / (n1 * n1);
   return aval * (s2n * s2n) + bval * s2n + cval;
 }
 
-inline double dotn(Block& b, int64_t e, const double d[3]) {
+inline real dotn(Block& b, int64_t e, const real d[3]) {
   return d[0] * b.cosAlpha(e) + d[1] * b.cosBeta(e) + d[2] * b.cosGamma(e);
 }
 
 // dpdn of the rigid-body acceleration, src/Forcing.f90:29-52
-void accel_terms(Block& b, int64_t e, double& ac_y, double& ac_z, double& at_y, double& at_z) {
+void accel_terms(Block& b, int64_t e, real& ac_y, real& ac_z, real& at_y, real& at_z) {
   const int64_t sid = b.ibSurfId(e);
   if (sid == 50) {
     ac_z = ac_y = at_z = at_y = 0.0;
@@ -117,17 +117,17 @@ void accel_terms(Block& b, int64_t e, double& ac_y, double& ac_z, double& at_y, 
 // one pressure reconstruction (…1 and …Field variants), writes p(i,j,k)
 void p_recon(Block& b, int64_t n, bool field) {
   const int64_t e = b.nelp(n);
-  double ac_y = 0, ac_z = 0, at_y = 0, at_z = 0;
+  real ac_y = 0, ac_z = 0, at_y = 0, at_z = 0;
   accel_terms(b, e, ac_y, ac_z, at_y, at_z);
-  const double dpdn = -((ac_z + at_z) * b.cosGamma(e) + (ac_y + at_y) * b.cosBeta(e)) -
+  const real dpdn = -((ac_z + at_z) * b.cosGamma(e) + (ac_y + at_y) * b.cosBeta(e)) -
                       b.yddot * b.cosBeta(e);
   const int64_t i = b.interceptedIndexPtr(n, 1), j = b.interceptedIndexPtr(n, 2),
                 k = b.interceptedIndexPtr(n, 3);
-  const double s2n = b.pNormDis(n);
-  const double pt1 = pt1_of(b, i, j, k, s2n);
-  const double px = b.xp(i) + pt1 * b.cosAlpha(e);
-  const double py = b.yp(j) + pt1 * b.cosBeta(e);
-  const double pz = b.zp(k) + pt1 * b.cosGamma(e);
+  const real s2n = b.pNormDis(n);
+  const real pt1 = pt1_of(b, i, j, k, s2n);
+  const real px = b.xp(i) + pt1 * b.cosAlpha(e);
+  const real py = b.yp(j) + pt1 * b.cosBeta(e);
+  const real pz = b.zp(k) + pt1 * b.cosGamma(e);
   int64_t ix, iy, iz;
   if (!field) {
     ix = find_index(b, px, b.xp, 1, b.nx + 1);
@@ -138,13 +138,13 @@ void p_recon(Block& b, int64_t n, bool field) {
     iy = find_index(b, py, b.yp, j - 7, j + 7);
     iz = find_index(b, pz, b.zp, k - 7, k + 7);
   }
-  double val, der[3];
+  real val, der[3];
   value_and_derivatives(px, py, pz, ix, iy, iz, b.xp, b.yp, b.zp, 0, b.p, val, der, &b.err);
-  const double dpdn_e = dotn(b, e, der);
-  const double n1 = pt1 + s2n;
-  const double bval = dpdn;
-  const double aval = (dpdn_e - dpdn) / (2.0 * n1);
-  const double cval = val - (dpdn_e + dpdn) * n1 * 0.5;
+  const real dpdn_e = dotn(b, e, der);
+  const real n1 = pt1 + s2n;
+  const real bval = dpdn;
+  const real aval = (dpdn_e - dpdn) / (2.0 * n1);
+  const real cval = val - (dpdn_e + dpdn) * n1 * 0.5;
   b.p(i, j, k) = aval * (s2n * s2n) + bval * s2n + cval;
 }
 
@@ -155,7 +155,7 @@ enum Comp { CU2 = 0, CU1, CV2, CV1, CW2, CW1 };
 // mode: 0 = velocityForcing1, 1 = velocityForcingField, 2 = velocityForcingGhost.
 // The reference writes the surface-50 v sample as `0 + ydot` in two places
 // (Forcing.f90:237, :551); that form is kept because it maps -0.0 to +0.0.
-double surf_velocity(Block& b, int64_t e, int comp, int mode) {
+real surf_velocity(Block& b, int64_t e, int comp, int mode) {
   const int64_t sid = b.ibSurfId(e);
   const bool with_alpha = mode != 0;
   if (comp == CU2 || comp == CU1) return b.xdot;
@@ -192,7 +192,7 @@ CompGeo comp_geo(Block& b, int c) {
 }
 
 // node position of the velocity sample of component c at IB cell (i,j,k)
-void sample_pos(Block& b, int c, int64_t i, int64_t j, int64_t k, double q[3]) {
+void sample_pos(Block& b, int c, int64_t i, int64_t j, int64_t k, real q[3]) {
   const CompGeo g = comp_geo(b, c);
   q[0] = (*g.xg)(c == CU2 ? i + 1 : i);
   q[1] = (*g.yg)(c == CV2 ? j + 1 : j);
@@ -204,16 +204,16 @@ void sample_pos(Block& b, int c, int64_t i, int64_t j, int64_t k, double q[3]) {
 void v_recon(Block& b, int64_t n, int c, int mode) {
   const CompGeo g = comp_geo(b, c);
   const int64_t e = (*g.nel)(n);
-  const double surf = surf_velocity(b, e, c, mode);
+  const real surf = surf_velocity(b, e, c, mode);
   const int64_t i = b.interceptedIndexPtr(n, 1), j = b.interceptedIndexPtr(n, 2),
                 k = b.interceptedIndexPtr(n, 3);
-  const double s2n = (*g.nd)(n);
-  const double pt1 = pt1_of(b, i, j, k, s2n);
-  double q[3];
+  const real s2n = (*g.nd)(n);
+  const real pt1 = pt1_of(b, i, j, k, s2n);
+  real q[3];
   sample_pos(b, c, i, j, k, q);
-  const double px = q[0] + pt1 * b.cosAlpha(e);
-  const double py = q[1] + pt1 * b.cosBeta(e);
-  const double pz = q[2] + pt1 * b.cosGamma(e);
+  const real px = q[0] + pt1 * b.cosAlpha(e);
+  const real py = q[1] + pt1 * b.cosBeta(e);
+  const real pz = q[2] + pt1 * b.cosGamma(e);
   int64_t ix, iy, iz;
   if (mode == 0) {
     ix = find_index(b, px, *g.xg, 1, b.nx + (c == CU2 ? 2 : 1));
@@ -232,11 +232,11 @@ void v_recon(Block& b, int64_t n, int c, int mode) {
   }
   F3& src = g.axis == 1 ? b.ut : (g.axis == 2 ? b.vt : b.wt);
   F3& dst = mode == 0 ? src : (g.axis == 1 ? b.u : (g.axis == 2 ? b.v : b.w));
-  double val, der[3];
+  real val, der[3];
   value_and_derivatives(px, py, pz, ix, iy, iz, *g.xg, *g.yg, *g.zg, g.axis, src, val, der, &b.err);
-  const double dn = dotn(b, e, der);
-  const double n1 = pt1 + s2n;
-  const double r = vel_quad(val, surf, dn, n1, s2n);
+  const real dn = dotn(b, e, der);
+  const real n1 = pt1 + s2n;
+  const real r = vel_quad(val, surf, dn, n1, s2n);
   int64_t ti = i, tj = j, tk = k;
   if (c == CU1) ti = i - 1;
   if (c == CV1) tj = j - 1;
@@ -274,25 +274,25 @@ void pressure_forcing_ghost(Block& b) {
     const int64_t i = b.TSIndexPtr(n, 1), j = b.TSIndexPtr(n, 2), k = b.TSIndexPtr(n, 3);
     const int64_t it = b.index_ts(n);
     const int64_t e = b.nelp(it);
-    double ac_y = 0, ac_z = 0, at_y = 0, at_z = 0;
+    real ac_y = 0, ac_z = 0, at_y = 0, at_z = 0;
     accel_terms(b, e, ac_y, ac_z, at_y, at_z);
-    const double dpdn = ((ac_z + at_z) * b.cosGamma(e) + (ac_y + at_y) * b.cosBeta(e)) +
+    const real dpdn = ((ac_z + at_z) * b.cosGamma(e) + (ac_y + at_y) * b.cosBeta(e)) +
                         (b.yddot * (b.cosBeta(e)));
-    const double s2n = -b.pNormDis(it);
-    const double pt1 = pt1_of(b, i, j, k, s2n);
-    const double px = b.xp(i) - pt1 * b.cosAlpha(e);
-    const double py = b.yp(j) - pt1 * b.cosBeta(e);
-    const double pz = b.zp(k) - pt1 * b.cosGamma(e);
+    const real s2n = -b.pNormDis(it);
+    const real pt1 = pt1_of(b, i, j, k, s2n);
+    const real px = b.xp(i) - pt1 * b.cosAlpha(e);
+    const real py = b.yp(j) - pt1 * b.cosBeta(e);
+    const real pz = b.zp(k) - pt1 * b.cosGamma(e);
     const int64_t ix = find_index(b, px, b.xp, i - 7, i + 7);
     const int64_t iy = find_index(b, py, b.yp, j - 7, j + 7);
     const int64_t iz = find_index(b, pz, b.zp, k - 7, k + 7);
-    double val, der[3];
+    real val, der[3];
     value_and_derivatives(px, py, pz, ix, iy, iz, b.xp, b.yp, b.zp, 0, b.p, val, der, &b.err);
-    const double dpdn_e = -1.0 * dotn(b, e, der);
-    const double n1 = pt1 + s2n;
-    const double bval = dpdn;
-    const double aval = (dpdn_e - dpdn) / (2.0 * n1);
-    const double cval = val - (dpdn_e + dpdn) * n1 * 0.5;
+    const real dpdn_e = -1.0 * dotn(b, e, der);
+    const real n1 = pt1 + s2n;
+    const real bval = dpdn;
+    const real aval = (dpdn_e - dpdn) / (2.0 * n1);
+    const real cval = val - (dpdn_e + dpdn) * n1 * 0.5;
     b.p_ghost(n) = aval * (s2n * s2n) + bval * s2n + cval;
     b.pt_ghost(n) = b.p(i, j, k);
   }
@@ -309,23 +309,23 @@ void velocity_forcing_ghost(Block& b) {
     for (int c = 0; c < 6; ++c) {
       const CompGeo g = comp_geo(b, c);
       const int64_t e = (*g.nel)(it);
-      const double surf = surf_velocity(b, e, c, 2);
-      const double s2n = -(*g.nd)(it);
-      const double pt1 = pt1_of(b, i, j, k, s2n);
-      double q[3];
+      const real surf = surf_velocity(b, e, c, 2);
+      const real s2n = -(*g.nd)(it);
+      const real pt1 = pt1_of(b, i, j, k, s2n);
+      real q[3];
       sample_pos(b, c, i, j, k, q);
-      const double px = q[0] - pt1 * b.cosAlpha(e);
-      const double py = q[1] - pt1 * b.cosBeta(e);
-      const double pz = q[2] - pt1 * b.cosGamma(e);
+      const real px = q[0] - pt1 * b.cosAlpha(e);
+      const real py = q[1] - pt1 * b.cosBeta(e);
+      const real pz = q[2] - pt1 * b.cosGamma(e);
       const int64_t ix = find_index(b, px, *g.xg, i - 7, i + 7);
       const int64_t iy = find_index(b, py, *g.yg, j - 7, j + 7);
       const int64_t iz = find_index(b, pz, *g.zg, k - 7, k + 7);
       F3& src = g.axis == 1 ? b.ut : (g.axis == 2 ? b.vt : b.wt);
       F3& cur = g.axis == 1 ? b.u : (g.axis == 2 ? b.v : b.w);
-      double val, der[3];
+      real val, der[3];
       value_and_derivatives(px, py, pz, ix, iy, iz, *g.xg, *g.yg, *g.zg, g.axis, src, val, der, &b.err);
-      const double dn = -1.0 * dotn(b, e, der);
-      const double n1 = pt1 + s2n;
+      const real dn = -1.0 * dotn(b, e, der);
+      const real n1 = pt1 + s2n;
       (*ghost[c])(n) = vel_quad(val, surf, dn, n1, s2n);
       int64_t ti = i, tj = j, tk = k;
       if (c == CU1) ti = i - 1;

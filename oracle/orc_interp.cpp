@@ -8,7 +8,7 @@
 namespace orc {
 
 // set_interface_detail, src/InterfaceDetail.f90:168-241
-void set_interface_detail(const F1& var, double s, double e, int64_t factor, I2& det,
+void set_interface_detail(const F1& var, real s, real e, int64_t factor, I2& det,
                           int64_t& counter, int64_t starter_in) {
   int64_t starter = starter_in;
   int64_t xx1 = 0, xx2 = 0;
@@ -69,33 +69,33 @@ namespace {
 
 // trilinear_interpolation of src/FineInterp_bound.f90:554-603: coarse points
 // loc-1 and loc+1 along each axis.
-double tri_fine(double x, double y, double z, int64_t i, int64_t j, int64_t k, const F1& xg,
+real tri_fine(real x, real y, real z, int64_t i, int64_t j, int64_t k, const F1& xg,
                 const F1& yg, const F1& zg, int off, const F3& var) {
   int64_t vi = i, vj = j, vk = k;
   if (off == 1) vi = i - 1;
   if (off == 2) vj = j - 1;
   if (off == 3) vk = k - 1;
-  double f[4] = {var(vi - 1, vj - 1, vk - 1), var(vi + 1, vj - 1, vk - 1),
+  real f[4] = {var(vi - 1, vj - 1, vk - 1), var(vi + 1, vj - 1, vk - 1),
                  var(vi - 1, vj + 1, vk - 1), var(vi + 1, vj + 1, vk - 1)};
-  const double z1 = bilinear_interpolation(x, y, xg(i - 1), xg(i + 1), yg(j - 1), yg(j + 1), f);
-  double g[4] = {var(vi - 1, vj - 1, vk + 1), var(vi + 1, vj - 1, vk + 1),
+  const real z1 = bilinear_interpolation(x, y, xg(i - 1), xg(i + 1), yg(j - 1), yg(j + 1), f);
+  real g[4] = {var(vi - 1, vj - 1, vk + 1), var(vi + 1, vj - 1, vk + 1),
                  var(vi - 1, vj + 1, vk + 1), var(vi + 1, vj + 1, vk + 1)};
-  const double z2 = bilinear_interpolation(x, y, xg(i - 1), xg(i + 1), yg(j - 1), yg(j + 1), g);
+  const real z2 = bilinear_interpolation(x, y, xg(i - 1), xg(i + 1), yg(j - 1), yg(j + 1), g);
   return linear_interpolation(z, zg(k - 1), zg(k + 1), z1, z2);
 }
 
 // trilinear_interpolation of src/CoarseInterp.f90:447-502: adjacent fine points.
-double tri_coarse(double x, double y, double z, int64_t i, int64_t j, int64_t k, const F1& xg,
+real tri_coarse(real x, real y, real z, int64_t i, int64_t j, int64_t k, const F1& xg,
                   const F1& yg, const F1& zg, int off, const F3& var) {
   int64_t ii = i, jj = j, kk = k, vi = i, vj = j, vk = k;
   if (off == 1) { ii = i - 1; vi = i - 2; }
   if (off == 2) { jj = j - 1; vj = j - 2; }
   if (off == 3) { kk = k - 1; vk = k - 2; }
-  double f[4] = {var(vi, vj, vk), var(vi + 1, vj, vk), var(vi, vj + 1, vk), var(vi + 1, vj + 1, vk)};
-  const double z1 = bilinear_interpolation(x, y, xg(ii), xg(ii + 1), yg(jj), yg(jj + 1), f);
-  double g[4] = {var(vi, vj, vk + 1), var(vi + 1, vj, vk + 1), var(vi, vj + 1, vk + 1),
+  real f[4] = {var(vi, vj, vk), var(vi + 1, vj, vk), var(vi, vj + 1, vk), var(vi + 1, vj + 1, vk)};
+  const real z1 = bilinear_interpolation(x, y, xg(ii), xg(ii + 1), yg(jj), yg(jj + 1), f);
+  real g[4] = {var(vi, vj, vk + 1), var(vi + 1, vj, vk + 1), var(vi, vj + 1, vk + 1),
                  var(vi + 1, vj + 1, vk + 1)};
-  const double z2 = bilinear_interpolation(x, y, xg(ii), xg(ii + 1), yg(jj), yg(jj + 1), g);
+  const real z2 = bilinear_interpolation(x, y, xg(ii), xg(ii + 1), yg(jj), yg(jj + 1), g);
   return linear_interpolation(z, zg(kk), zg(kk + 1), z1, z2);
 }
 
@@ -146,7 +146,7 @@ void face_fill(Interface& it, int comp, F3& src, F3& dst, F3* dst2) {
           for (int64_t tz = vz1; tz <= vz2; ++tz)
             for (int64_t ty = vy1; ty <= vy2; ++ty)
               for (int64_t tx = vx1; tx <= vx2; ++tx) {
-                const double r =
+                const real r =
                     tri_fine((*bx)(tx), (*by)(ty), (*bz)(tz), lx, ly, lz, *ax, *ay, *az, comp, src);
                 int64_t ox = tx, oy = ty, oz = tz;
                 if (comp == 1) ox = tx - 1;
@@ -179,7 +179,7 @@ void restrict_fill(Interface& it, int comp, F3& src, F3& dst, F3* dst2) {
         if (comp == 1) lx = (*t.tx)(3, i);
         if (comp == 2) ly = (*t.ty)(3, j);
         if (comp == 3) lz = (*t.tz)(3, k);
-        const double r =
+        const real r =
             tri_coarse((*ax)(tx), (*ay)(ty), (*az)(tz), lx, ly, lz, *bx, *by, *bz, comp, src);
         int64_t ox = tx, oy = ty, oz = tz;
         if (comp == 1) ox = tx - 1;
@@ -284,24 +284,24 @@ void fine_update_mv(int64_t g) {
             for (int64_t l = vy1; l <= vy2; ++l)
               for (int64_t s = vx1; s <= vx2; ++s) {
                 if (b.cell_n(s, l, q) == 1) continue;
-                const double valx = (*bx)(s), valy = (*by)(l), valz = (*bz)(q);
-                const double x1 = (*ax)(lx - 1), x2 = (*ax)(lx + 1);
-                const double y1 = (*ay)(ly - 1), y2 = (*ay)(ly + 1);
-                const double z1 = (*az)(lz - 1), z2 = (*az)(lz + 1);
-                const double deno = (x2 - x1) * (y2 - y1);
-                const double xtx = (x2 - valx), xxo = (valx - x1);
-                const double yty = (y2 - valy), yyo = (valy - y1);
-                double f1 = src(xm, ym, zm), f2 = src(xq, ym, zm), f3 = src(xq, yq, zm),
+                const real valx = (*bx)(s), valy = (*by)(l), valz = (*bz)(q);
+                const real x1 = (*ax)(lx - 1), x2 = (*ax)(lx + 1);
+                const real y1 = (*ay)(ly - 1), y2 = (*ay)(ly + 1);
+                const real z1 = (*az)(lz - 1), z2 = (*az)(lz + 1);
+                const real deno = (x2 - x1) * (y2 - y1);
+                const real xtx = (x2 - valx), xxo = (valx - x1);
+                const real yty = (y2 - valy), yyo = (valy - y1);
+                real f1 = src(xm, ym, zm), f2 = src(xq, ym, zm), f3 = src(xq, yq, zm),
                        f4 = src(xm, yq, zm);
-                double num = (f1 * xtx + f2 * xxo) * yty + (f4 * xtx + f3 * xxo) * yyo;
-                const double a1 = (num / deno);
+                real num = (f1 * xtx + f2 * xxo) * yty + (f4 * xtx + f3 * xxo) * yyo;
+                const real a1 = (num / deno);
                 f1 = src(xm, ym, zq);
                 f2 = src(xq, ym, zq);
                 f3 = src(xq, yq, zq);
                 f4 = src(xm, yq, zq);
                 num = (f1 * xtx + f2 * xxo) * yty + (f4 * xtx + f3 * xxo) * yyo;
-                const double a2 = (num / deno);
-                const double r = a1 + ((valz - z1) * ((a2 - a1) / (z2 - z1)));
+                const real a2 = (num / deno);
+                const real r = a1 + ((valz - z1) * ((a2 - a1) / (z2 - z1)));
                 int64_t ox = s, oy = l, oz = q;
                 if (comp == 1) ox = s - 1;
                 if (comp == 2) oy = l - 1;

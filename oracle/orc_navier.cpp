@@ -83,12 +83,12 @@ void derive_grids(Block& b) {
 // power x**2.0 folds to x*x and x**3.0 / x**4.0 call pow().
 // ---------------------------------------------------------------------------
 namespace {
-inline double p2(double x) { return x * x; }
-inline double p3(double x) { return (x * x) * x; }
-inline double p4(double x) { double s = x * x; return s * s; }
+inline real p2(real x) { return x * x; }
+inline real p3(real x) { return (x * x) * x; }
+inline real p4(real x) { real s = x * x; return s * s; }
 
-void compute_f(const double t[3], double f[9]) {  // f[1..8]
-  const double t1 = t[0], t2 = t[1], t3 = t[2];
+void compute_f(const real t[3], real f[9]) {  // f[1..8]
+  const real t1 = t[0], t2 = t[1], t3 = t[2];
   f[1] = t3;
   f[2] = 2.0 * t3 + p2(t3);
   f[3] = 3.0 * t3 + 3.0 * p2(t3) + p3(t3);
@@ -100,9 +100,9 @@ void compute_f(const double t[3], double f[9]) {  // f[1..8]
 }
 
 // s(5:10,1:7) stored as s[r][c] with r in 5..10, c in 1..7
-struct S { double v[11][8]; };
+struct S { real v[11][8]; };
 
-S compute_s(double t2, const double f[9]) {
+S compute_s(real t2, const real f[9]) {
   S s{};
   auto& a = s.v;
   a[5][1] = -1.0 / p4(t2);
@@ -128,7 +128,7 @@ S compute_s(double t2, const double f[9]) {
   a[7][5] = (f[4] - f[2]);
   a[7][6] = (f[4] - f[3]);
 
-  const double r4 = std::pow(t2, 4.0), r2 = t2 * t2, r3 = std::pow(t2, 3.0);
+  const real r4 = pow(t2, 4.0), r2 = t2 * t2, r3 = pow(t2, 3.0);
   a[8][1] = -1.0 / r4;
   a[8][2] = (f[8] + (1.0 / r4));
   a[8][3] = f[8];
@@ -154,8 +154,8 @@ S compute_s(double t2, const double f[9]) {
   return s;
 }
 
-void compute_ak(const double t[3], double ak[8]) {
-  const double t1 = t[0], t2 = t[1], t3 = t[2];
+void compute_ak(const real t[3], real ak[8]) {
+  const real t1 = t[0], t2 = t[1], t3 = t[2];
   ak[1] = (1.0 + 2.0 * t1) * (t3 + p2(t3)) * t2;
   ak[2] = (1.0 + t1) * (2.0 * t3 + p2(t3));
   ak[3] = (1.0 + t1);
@@ -165,8 +165,8 @@ void compute_ak(const double t[3], double ak[8]) {
   ak[7] = (1.0 + t1) * (t3 + p2(t3)) * t2;
 }
 
-void fill_ca_ck(A2<double>& ca, A2<double>& ck, int64_t i, const double th[3]) {
-  double f[9];
+void fill_ca_ck(A2<real>& ca, A2<real>& ck, int64_t i, const real th[3]) {
+  real f[9];
   compute_f(th, f);
   const S s = compute_s(th[1], f);
   const auto& a = s.v;
@@ -176,7 +176,7 @@ void fill_ca_ck(A2<double>& ca, A2<double>& ck, int64_t i, const double th[3]) {
   ca(4, i) = a[9][4] * a[10][7] + a[10][4] * a[9][7];
   ca(5, i) = a[9][7] * a[10][3] - a[10][7] * a[9][2];
   ca(6, i) = a[9][7] * a[10][6] - a[10][7] * a[9][6];
-  double ak[8];
+  real ak[8];
   compute_ak(th, ak);
   ck(1, i) = ak[3];
   ck(2, i) = -ak[4];
@@ -186,7 +186,7 @@ void fill_ca_ck(A2<double>& ca, A2<double>& ck, int64_t i, const double th[3]) {
   ck(6, i) = ak[7];
 }
 
-void copy_col(A2<double>& dst, const A2<double>& src, int64_t i) {
+void copy_col(A2<real>& dst, const A2<real>& src, int64_t i) {
   for (int64_t r = 1; r <= 6; ++r) dst(r, i) = src(r, i);
 }
 }  // namespace
@@ -198,9 +198,9 @@ void non_uni_coeff(Block& b) {
   for (auto* a : {&b.ca_ww, &b.ck_ww, &b.ca_wu, &b.ck_wu, &b.ca_wv, &b.ck_wv}) a->alloc(6, nz + 2);
 
   // same-direction tables: theta = delta(i:i+2) / delta(i-1:i+1)
-  auto same = [](F1& d, A2<double>& ca, A2<double>& ck, int64_t n) {
+  auto same = [](F1& d, A2<real>& ca, A2<real>& ck, int64_t n) {
     for (int64_t i = 2; i <= n; ++i) {
-      const double th[3] = {d(i) / d(i - 1), d(i + 1) / d(i), d(i + 2) / d(i + 1)};
+      const real th[3] = {d(i) / d(i - 1), d(i + 1) / d(i), d(i + 2) / d(i + 1)};
       fill_ca_ck(ca, ck, i, th);
     }
   };
@@ -209,18 +209,18 @@ void non_uni_coeff(Block& b) {
   same(b.deltaz, b.ca_ww, b.ck_ww, nz);
 
   // cross-direction tables on the staggered (mid-cell) spacing
-  auto cross = [](F1& d, A2<double>& ca, A2<double>& ck, A2<double>& ca2, A2<double>& ck2,
+  auto cross = [](F1& d, A2<real>& ca, A2<real>& ck, A2<real>& ca2, A2<real>& ck2,
                   int64_t n) {
     for (int64_t i = 2; i <= n; ++i) {
-      double t1;
+      real t1;
       if (i == 2)
         t1 = d(i - 1);
       else
         t1 = 0.5 * (d(i - 1) + d(i - 2));
-      const double t2 = 0.5 * (d(i) + d(i - 1));
-      const double t3 = 0.5 * (d(i) + d(i + 1));
-      const double t4 = 0.5 * (d(i + 1) + d(i + 2));
-      const double th[3] = {t2 / t1, t3 / t2, t4 / t3};
+      const real t2 = 0.5 * (d(i) + d(i - 1));
+      const real t3 = 0.5 * (d(i) + d(i + 1));
+      const real t4 = 0.5 * (d(i + 1) + d(i + 2));
+      const real th[3] = {t2 / t1, t3 / t2, t4 / t3};
       fill_ca_ck(ca, ck, i, th);
       copy_col(ca2, ca, i);
       copy_col(ck2, ck, i);
@@ -235,19 +235,19 @@ void non_uni_coeff(Block& b) {
 void coefficient_matrix(Block& b, bool is_coarse) {
   const int64_t nx = b.nx, ny = b.ny, nz = b.nz;
   for (int64_t j = 2; j <= ny + 1; ++j) {
-    const double r1 = b.yp(j) - b.yp(j - 1), r2 = b.yp(j + 1) - b.yp(j), rs = r1 + r2;
+    const real r1 = b.yp(j) - b.yp(j - 1), r2 = b.yp(j + 1) - b.yp(j), rs = r1 + r2;
     b.Acy(j - 1, 1) = 2.0 / (r1 * rs);
     b.Acy(j - 1, 2) = -2.0 / (r1 * r2);
     b.Acy(j - 1, 3) = 2.0 / (r2 * rs);
   }
   for (int64_t i = 2; i <= nx + 1; ++i) {
-    const double r1 = b.xp(i) - b.xp(i - 1), r2 = b.xp(i + 1) - b.xp(i), rs = r1 + r2;
+    const real r1 = b.xp(i) - b.xp(i - 1), r2 = b.xp(i + 1) - b.xp(i), rs = r1 + r2;
     b.Acx(i - 1, 1) = 2.0 / (r1 * rs);
     b.Acx(i - 1, 2) = -2.0 / (r1 * r2);
     b.Acx(i - 1, 3) = 2.0 / (r2 * rs);
   }
   for (int64_t i = 2; i <= nz + 1; ++i) {
-    const double r1 = b.zp(i) - b.zp(i - 1), r2 = b.zp(i + 1) - b.zp(i), rs = r1 + r2;
+    const real r1 = b.zp(i) - b.zp(i - 1), r2 = b.zp(i + 1) - b.zp(i), rs = r1 + r2;
     b.Acz(i - 1, 1) = 2.0 / (r1 * rs);
     b.Acz(i - 1, 2) = -2.0 / (r1 * r2);
     b.Acz(i - 1, 3) = 2.0 / (r2 * rs);
@@ -285,8 +285,8 @@ static bool check_adjacent(const I3& c, int64_t i, int64_t j, int64_t k, int64_t
 // of the last TS index.  Without TS cells (cell2 /= 2 everywhere) no cell
 // writes u, v, w or p and each writes only its own ut, vt, wt, so the loop
 // then runs in parallel (OpenMP) with the serial loop's results.
-void ns_momentum_2order(Block& b, double deltat, double re) {
-  const double alpha = 1.0;
+void ns_momentum_2order(Block& b, real deltat, real re) {
+  const real alpha = 1.0;
   const int64_t nx_var = b.nx, ny_var = b.ny, nz_var = b.nz;
   F3 &u = b.u, &v = b.v, &w = b.w, &p = b.p;
   I3& c2 = b.cell2;
@@ -300,17 +300,17 @@ void ns_momentum_2order(Block& b, double deltat, double re) {
         c2(i, j - 1, k) == 2 || c2(i, j, k + 1) == 2 || c2(i, j, k - 1) == 2) {
       for (int64_t nn = 1; nn <= b.TSCellCount; ++nn) {
         const int64_t bt = b.index_ts(nn);
-        auto dot = [&](int64_t idx, double px, double py, double pz) {
+        auto dot = [&](int64_t idx, real px, real py, real pz) {
           return (px - b.xcent(idx)) * b.cosAlpha(idx) + (py - b.ycent(idx)) * b.cosBeta(idx) +
                  (pz - b.zcent(idx)) * b.cosGamma(idx);
         };
-        const double u2 = dot(b.nelu2(bt), b.x1(i + 1), b.yp(j), b.zp(k));
-        const double u1 = dot(b.nelu1(bt), b.x1(i), b.yp(j), b.zp(k));
-        const double v2 = dot(b.nelv2(bt), b.xp(i), b.y1(j + 1), b.zp(k));
-        const double v1 = dot(b.nelv1(bt), b.xp(i), b.y1(j), b.zp(k));
-        const double w2 = dot(b.nelw2(bt), b.xp(i), b.yp(j), b.z1(k + 1));
-        const double w1 = dot(b.nelw1(bt), b.xp(i), b.yp(j), b.z1(k));
-        const double pd = dot(b.nelp(bt), b.xp(i), b.yp(j), b.zp(k));
+        const real u2 = dot(b.nelu2(bt), b.x1(i + 1), b.yp(j), b.zp(k));
+        const real u1 = dot(b.nelu1(bt), b.x1(i), b.yp(j), b.zp(k));
+        const real v2 = dot(b.nelv2(bt), b.xp(i), b.y1(j + 1), b.zp(k));
+        const real v1 = dot(b.nelv1(bt), b.xp(i), b.y1(j), b.zp(k));
+        const real w2 = dot(b.nelw2(bt), b.xp(i), b.yp(j), b.z1(k + 1));
+        const real w1 = dot(b.nelw1(bt), b.xp(i), b.yp(j), b.z1(k));
+        const real pd = dot(b.nelp(bt), b.xp(i), b.yp(j), b.zp(k));
         if (c2(i + 1, j, k) == 2) {
           index_ip1 = nn;
           if (u2 < 0) u(i + 1, j, k) = b.u2_ghost(nn);
@@ -367,95 +367,95 @@ void ns_momentum_2order(Block& b, double deltat, double re) {
         }
       }
     }
-    const double dxr = b.deltax(i + 1), dx = b.deltax(i), dxl = b.deltax(i - 1);
-    const double dye = b.deltay(j + 1), dy = b.deltay(j), dyw = b.deltay(j - 1);
-    const double dzt = b.deltaz(k + 1), dz = b.deltaz(k), dzb = b.deltaz(k - 1);
+    const real dxr = b.deltax(i + 1), dx = b.deltax(i), dxl = b.deltax(i - 1);
+    const real dye = b.deltay(j + 1), dy = b.deltay(j), dyw = b.deltay(j - 1);
+    const real dzt = b.deltaz(k + 1), dz = b.deltaz(k), dzb = b.deltaz(k - 1);
 
-    const double u1a = u(i - 1, j, k) + u(i, j, k);
-    const double u22 = u(i - 1, j, k) - u(i, j, k);
-    const double u3 = u(i, j, k) + u(i + 1, j, k);
-    const double u4 = u(i, j, k) - u(i + 1, j, k);
-    const double u5 = u(i, j - 1, k) + u(i, j, k);
-    const double u6 = u(i, j - 1, k) - u(i, j, k);
-    const double u7 = u(i, j, k) + u(i, j + 1, k);
-    const double u8 = u(i, j, k) - u(i, j + 1, k);
-    const double u9 = u(i, j, k - 1) + u(i, j, k);
-    const double u10 = u(i, j, k - 1) - u(i, j, k);
-    const double u11 = u(i, j, k) + u(i, j, k + 1);
-    const double u12 = u(i, j, k) - u(i, j, k + 1);
-    const double u13 = u(i - 1, j, k) + u(i - 1, j + 1, k);
-    const double u14 = u7;
-    const double u15 = u(i - 1, j, k) + u(i - 1, j, k + 1);
-    const double u16 = u11;
+    const real u1a = u(i - 1, j, k) + u(i, j, k);
+    const real u22 = u(i - 1, j, k) - u(i, j, k);
+    const real u3 = u(i, j, k) + u(i + 1, j, k);
+    const real u4 = u(i, j, k) - u(i + 1, j, k);
+    const real u5 = u(i, j - 1, k) + u(i, j, k);
+    const real u6 = u(i, j - 1, k) - u(i, j, k);
+    const real u7 = u(i, j, k) + u(i, j + 1, k);
+    const real u8 = u(i, j, k) - u(i, j + 1, k);
+    const real u9 = u(i, j, k - 1) + u(i, j, k);
+    const real u10 = u(i, j, k - 1) - u(i, j, k);
+    const real u11 = u(i, j, k) + u(i, j, k + 1);
+    const real u12 = u(i, j, k) - u(i, j, k + 1);
+    const real u13 = u(i - 1, j, k) + u(i - 1, j + 1, k);
+    const real u14 = u7;
+    const real u15 = u(i - 1, j, k) + u(i - 1, j, k + 1);
+    const real u16 = u11;
 
-    const double v1a = v(i, j - 1, k) + v(i + 1, j - 1, k);
-    const double v22 = v(i, j, k) + v(i + 1, j, k);
-    const double v3 = v(i - 1, j, k) + v(i, j, k);
-    const double v4 = v(i - 1, j, k) - v(i, j, k);
-    const double v5 = v(i, j, k) + v(i + 1, j, k);
-    const double v6 = v(i, j, k) - v(i + 1, j, k);
-    const double v7 = v(i, j - 1, k) + v(i, j, k);
-    const double v8 = v(i, j - 1, k) - v(i, j, k);
-    const double v9 = v(i, j, k) + v(i, j + 1, k);
-    const double v10 = v(i, j, k) - v(i, j + 1, k);
-    const double v11 = v(i, j, k - 1) + v(i, j, k);
-    const double v12 = v(i, j, k - 1) - v(i, j, k);
-    const double v13 = v(i, j, k) + v(i, j, k + 1);
-    const double v14 = v(i, j, k) - v(i, j, k + 1);
-    const double v15 = v(i, j - 1, k) + v(i, j - 1, k + 1);
-    const double v16 = v13;
+    const real v1a = v(i, j - 1, k) + v(i + 1, j - 1, k);
+    const real v22 = v(i, j, k) + v(i + 1, j, k);
+    const real v3 = v(i - 1, j, k) + v(i, j, k);
+    const real v4 = v(i - 1, j, k) - v(i, j, k);
+    const real v5 = v(i, j, k) + v(i + 1, j, k);
+    const real v6 = v(i, j, k) - v(i + 1, j, k);
+    const real v7 = v(i, j - 1, k) + v(i, j, k);
+    const real v8 = v(i, j - 1, k) - v(i, j, k);
+    const real v9 = v(i, j, k) + v(i, j + 1, k);
+    const real v10 = v(i, j, k) - v(i, j + 1, k);
+    const real v11 = v(i, j, k - 1) + v(i, j, k);
+    const real v12 = v(i, j, k - 1) - v(i, j, k);
+    const real v13 = v(i, j, k) + v(i, j, k + 1);
+    const real v14 = v(i, j, k) - v(i, j, k + 1);
+    const real v15 = v(i, j - 1, k) + v(i, j - 1, k + 1);
+    const real v16 = v13;
 
-    const double w1a = w(i, j, k - 1) + w(i + 1, j, k - 1);
-    const double w22 = w(i, j, k) + w(i + 1, j, k);
-    const double w3 = w(i, j, k - 1) + w(i, j + 1, k - 1);
-    const double w4 = w(i, j, k) + w(i, j + 1, k);
-    const double w5 = w(i - 1, j, k) + w(i, j, k);
-    const double w6 = w(i - 1, j, k) - w(i, j, k);
-    const double w7 = w(i, j, k) + w(i + 1, j, k);
-    const double w8 = w(i, j, k) - w(i + 1, j, k);
-    const double w9 = w(i, j - 1, k) + w(i, j, k);
-    const double w10 = w(i, j - 1, k) - w(i, j, k);
-    const double w11 = w(i, j, k) + w(i, j + 1, k);
-    const double w12 = w(i, j, k) - w(i, j + 1, k);
-    const double w13 = w(i, j, k - 1) + w(i, j, k);
-    const double w14 = w(i, j, k - 1) - w(i, j, k);
-    const double w15 = w(i, j, k) + w(i, j, k + 1);
-    const double w16 = w(i, j, k) - w(i, j, k + 1);
+    const real w1a = w(i, j, k - 1) + w(i + 1, j, k - 1);
+    const real w22 = w(i, j, k) + w(i + 1, j, k);
+    const real w3 = w(i, j, k - 1) + w(i, j + 1, k - 1);
+    const real w4 = w(i, j, k) + w(i, j + 1, k);
+    const real w5 = w(i - 1, j, k) + w(i, j, k);
+    const real w6 = w(i - 1, j, k) - w(i, j, k);
+    const real w7 = w(i, j, k) + w(i + 1, j, k);
+    const real w8 = w(i, j, k) - w(i + 1, j, k);
+    const real w9 = w(i, j - 1, k) + w(i, j, k);
+    const real w10 = w(i, j - 1, k) - w(i, j, k);
+    const real w11 = w(i, j, k) + w(i, j + 1, k);
+    const real w12 = w(i, j, k) - w(i, j + 1, k);
+    const real w13 = w(i, j, k - 1) + w(i, j, k);
+    const real w14 = w(i, j, k - 1) - w(i, j, k);
+    const real w15 = w(i, j, k) + w(i, j, k + 1);
+    const real w16 = w(i, j, k) - w(i, j, k + 1);
 
-    const double dpdx = (p(i, j, k) - p(i + 1, j, k)) / (0.5 * (dxr + dx));
-    const double dpdy = (p(i, j, k) - p(i, j + 1, k)) / (0.5 * (dye + dy));
-    const double dpdz = (p(i, j, k) - p(i, j, k + 1)) / (0.5 * (dzt + dz));
+    const real dpdx = (p(i, j, k) - p(i + 1, j, k)) / (0.5 * (dxr + dx));
+    const real dpdy = (p(i, j, k) - p(i, j + 1, k)) / (0.5 * (dye + dy));
+    const real dpdz = (p(i, j, k) - p(i, j, k + 1)) / (0.5 * (dzt + dz));
 
-    const double dx2xr = dx + dxr, dx2xl = dx + dxl, dy2ye = dy + dye, dy2yw = dy + dyw,
+    const real dx2xr = dx + dxr, dx2xl = dx + dxl, dy2ye = dy + dye, dy2yw = dy + dyw,
                  dz2zt = dz + dzt, dz2zb = dz + dzb;
 
     // ---------------- U momentum ----------------
-    const double vu_e = v(i + 1, j, k) + (dxr / (dx2xr)) * (v(i, j, k) - v(i + 1, j, k));
-    const double vu_w =
+    const real vu_e = v(i + 1, j, k) + (dxr / (dx2xr)) * (v(i, j, k) - v(i + 1, j, k));
+    const real vu_w =
         v(i + 1, j - 1, k) + (dxr / (dx2xr)) * (v(i, j - 1, k) - v(i + 1, j - 1, k));
-    const double v_in_um = 0.5 * (vu_e + vu_w);
-    const double wu_n = w(i + 1, j, k) + (dxr / (dx2xr)) * (w(i, j, k) - w(i + 1, j, k));
-    const double wu_s =
+    const real v_in_um = 0.5 * (vu_e + vu_w);
+    const real wu_n = w(i + 1, j, k) + (dxr / (dx2xr)) * (w(i, j, k) - w(i + 1, j, k));
+    const real wu_s =
         w(i + 1, j, k - 1) + (dxr / (dx2xr)) * (w(i, j, k - 1) - w(i + 1, j, k - 1));
-    const double w_in_um = 0.5 * (wu_n + wu_s);
+    const real w_in_um = 0.5 * (wu_n + wu_s);
 
-    double duudx, dvudy, dwudz;
+    real duudx, dvudy, dwudz;
     bool third = false;
     if (i > 2 && i < nx_var && j > 2 && j < ny_var + 1 && k > 2 && k < nz_var + 1)
       if (check_adjacent(b.cell, i, j, k, 1))
         if (check_adjacent(b.cell2, i, j, k, 2)) third = true;
     if (third) {
-      const double ddy = 0.5 * (b.deltay(j) + b.deltay(j - 1));
-      const double ddye = 0.5 * (b.deltay(j) + b.deltay(j + 1));
-      const double ddz = 0.5 * (b.deltaz(k) + b.deltaz(k - 1));
-      const double ddzr = 0.5 * (b.deltaz(k) + b.deltaz(k + 1));
+      const real ddy = 0.5 * (b.deltay(j) + b.deltay(j - 1));
+      const real ddye = 0.5 * (b.deltay(j) + b.deltay(j + 1));
+      const real ddz = 0.5 * (b.deltaz(k) + b.deltaz(k - 1));
+      const real ddzr = 0.5 * (b.deltaz(k) + b.deltaz(k + 1));
       auto& ca = b.ca_uu;
       auto& ck = b.ck_uu;
       duudx = u(i, j, k) *
                   (ca(1, i) * u(i + 2, j, k) + ca(2, i) * u(i + 1, j, k) +
                    ca(3, i) * u(i, j, k) + ca(4, i) * u(i - 1, j, k) + ca(5, i) * u(i - 2, j, k)) /
                   (ca(6, i) * b.deltax(i + 1)) +
-              std::fabs(u(i, j, k)) *
+              fabs(u(i, j, k)) *
                   (ck(1, i) * u(i + 2, j, k) + ck(2, i) * u(i + 1, j, k) +
                    ck(3, i) * u(i, j, k) + ck(4, i) * u(i - 1, j, k) + ck(5, i) * u(i - 2, j, k)) /
                   (2.0 * ck(6, i) * b.deltax(i));
@@ -465,7 +465,7 @@ void ns_momentum_2order(Block& b, double deltat, double re) {
                   (cav(1, j) * u(i, j + 2, k) + cav(2, j) * u(i, j + 1, k) +
                    cav(3, j) * u(i, j, k) + cav(4, j) * u(i, j - 1, k) + cav(5, j) * u(i, j - 2, k)) /
                   (cav(6, j) * ddye) +
-              std::fabs(v_in_um) *
+              fabs(v_in_um) *
                   (ckv(1, j) * u(i, j + 2, k) + ckv(2, j) * u(i, j + 1, k) +
                    ckv(3, j) * u(i, j, k) + ckv(4, j) * u(i, j - 1, k) + ckv(5, j) * u(i, j - 2, k)) /
                   (2.0 * ckv(6, j) * ddy);
@@ -475,56 +475,56 @@ void ns_momentum_2order(Block& b, double deltat, double re) {
                   (caw(1, k) * u(i, j, k + 2) + caw(2, k) * u(i, j, k + 1) +
                    caw(3, k) * u(i, j, k) + caw(4, k) * u(i, j, k - 1) + caw(5, k) * u(i, j, k - 2)) /
                   (caw(6, k) * ddzr) +
-              std::fabs(w_in_um) *
+              fabs(w_in_um) *
                   (ckw(1, k) * u(i, j, k + 2) + ckw(2, k) * u(i, j, k + 1) +
                    ckw(3, k) * u(i, j, k) + ckw(4, k) * u(i, j, k - 1) + ckw(5, k) * u(i, j, k - 2)) /
                   (2.0 * ckw(6, k) * ddz);
     } else {
-      duudx = -0.25 * (u1a * u1a + alpha * std::fabs(u1a) * u22 - u3 * u3 -
-                       alpha * std::fabs(u3) * u4) /
+      duudx = -0.25 * (u1a * u1a + alpha * fabs(u1a) * u22 - u3 * u3 -
+                       alpha * fabs(u3) * u4) /
               b.deltax(i);
-      dvudy = -0.25 * (v1a * u5 + alpha * std::fabs(v1a) * u6 - v22 * u7 -
-                       alpha * std::fabs(v22) * u8) /
+      dvudy = -0.25 * (v1a * u5 + alpha * fabs(v1a) * u6 - v22 * u7 -
+                       alpha * fabs(v22) * u8) /
               b.deltay(j);
-      dwudz = -0.25 * (w1a * u9 + alpha * std::fabs(w1a) * u10 - w22 * u11 -
-                       alpha * std::fabs(w22) * u12) /
+      dwudz = -0.25 * (w1a * u9 + alpha * fabs(w1a) * u10 - w22 * u11 -
+                       alpha * fabs(w22) * u12) /
               b.deltaz(k);
     }
-    const double d2udx2 = (2.0 / dx2xr) * ((-u4 / dxr) + (u22 / dx));
-    const double d2udy2 =
+    const real d2udx2 = (2.0 / dx2xr) * ((-u4 / dxr) + (u22 / dx));
+    const real d2udy2 =
         (2.0 / (0.5 * (dy2ye + dy2yw))) * ((-u8 / (0.5 * dy2ye)) + (u6 / (0.5 * dy2yw)));
-    const double d2udz2 =
+    const real d2udz2 =
         (2.0 / (0.5 * (dz2zt + dz2zb))) * ((-u12 / (0.5 * dz2zt)) + (u10 / (0.5 * dz2zb)));
-    const double xtt2 = (d2udx2 + d2udy2 + d2udz2) / re;
-    const double residu = (-duudx - dvudy - dwudz + xtt2);
+    const real xtt2 = (d2udx2 + d2udy2 + d2udz2) / re;
+    const real residu = (-duudx - dvudy - dwudz + xtt2);
     b.ut(i, j, k) = u(i, j, k) + deltat * (residu + dpdx);
 
     // ---------------- V momentum ----------------
-    const double uv_e = u(i, j + 1, k) + (dye / (dy2ye)) * (u(i, j, k) - u(i, j + 1, k));
-    const double uv_w =
+    const real uv_e = u(i, j + 1, k) + (dye / (dy2ye)) * (u(i, j, k) - u(i, j + 1, k));
+    const real uv_w =
         u(i - 1, j + 1, k) + (dye / (dy2ye)) * (u(i - 1, j, k) - u(i - 1, j + 1, k));
-    const double u_in_vm = 0.5 * (uv_e + uv_w);
-    const double wv_n = w(i, j + 1, k) + (dye / (dy2ye)) * (w(i, j, k) - w(i, j + 1, k));
-    const double wv_s =
+    const real u_in_vm = 0.5 * (uv_e + uv_w);
+    const real wv_n = w(i, j + 1, k) + (dye / (dy2ye)) * (w(i, j, k) - w(i, j + 1, k));
+    const real wv_s =
         w(i, j + 1, k - 1) + (dye / (dy2ye)) * (w(i, j, k - 1) - w(i, j + 1, k - 1));
-    const double w_in_vm = 0.5 * (wv_n + wv_s);
-    double duvdx, dvvdy, dwvdz;
+    const real w_in_vm = 0.5 * (wv_n + wv_s);
+    real duvdx, dvvdy, dwvdz;
     third = false;
     if (i > 2 && i < nx_var + 1 && j > 2 && j < ny_var && k > 2 && k < nz_var + 1)
       if (check_adjacent(b.cell, i, j, k, 1))
         if (check_adjacent(b.cell2, i, j, k, 2)) third = true;
     if (third) {
-      const double ddx = 0.5 * (b.deltax(i) + b.deltax(i - 1));
-      const double ddxr = 0.5 * (b.deltax(i) + b.deltax(i + 1));
-      const double ddz = 0.5 * (b.deltaz(k) + b.deltaz(k - 1));
-      const double ddzr = 0.5 * (b.deltaz(k) + b.deltaz(k + 1));
+      const real ddx = 0.5 * (b.deltax(i) + b.deltax(i - 1));
+      const real ddxr = 0.5 * (b.deltax(i) + b.deltax(i + 1));
+      const real ddz = 0.5 * (b.deltaz(k) + b.deltaz(k - 1));
+      const real ddzr = 0.5 * (b.deltaz(k) + b.deltaz(k + 1));
       auto& ca = b.ca_uw;
       auto& ck = b.ck_uw;
       duvdx = u_in_vm *
                   (ca(1, i) * v(i + 2, j, k) + ca(2, i) * v(i + 1, j, k) +
                    ca(3, i) * v(i, j, k) + ca(4, i) * v(i - 1, j, k) + ca(5, i) * v(i - 2, j, k)) /
                   (ca(6, i) * ddxr) +
-              std::fabs(u_in_vm) *
+              fabs(u_in_vm) *
                   (ck(1, i) * v(i + 2, j, k) + ck(2, i) * v(i + 1, j, k) +
                    ck(3, i) * v(i, j, k) + ck(4, i) * v(i - 1, j, k) + ck(5, i) * v(i - 2, j, k)) /
                   (2.0 * ck(6, i) * ddx);
@@ -534,7 +534,7 @@ void ns_momentum_2order(Block& b, double deltat, double re) {
                   (cv(1, j) * v(i, j + 2, k) + cv(2, j) * v(i, j + 1, k) +
                    cv(3, j) * v(i, j, k) + cv(4, j) * v(i, j - 1, k) + cv(5, j) * v(i, j - 2, k)) /
                   (cv(6, j) * b.deltay(j + 1)) +
-              std::fabs(v(i, j, k)) *
+              fabs(v(i, j, k)) *
                   (kv(1, j) * v(i, j + 2, k) + kv(2, j) * v(i, j + 1, k) +
                    kv(3, j) * v(i, j, k) + kv(4, j) * v(i, j - 1, k) + kv(5, j) * v(i, j - 2, k)) /
                   (2.0 * kv(6, j) * b.deltay(j));
@@ -544,56 +544,56 @@ void ns_momentum_2order(Block& b, double deltat, double re) {
                   (cw(1, k) * v(i, j, k + 2) + cw(2, k) * v(i, j, k + 1) +
                    cw(3, k) * v(i, j, k) + cw(4, k) * v(i, j, k - 1) + cw(5, k) * v(i, j, k - 2)) /
                   (cw(6, k) * ddzr) +
-              std::fabs(w_in_vm) *
+              fabs(w_in_vm) *
                   (kw(1, k) * v(i, j, k + 2) + kw(2, k) * v(i, j, k + 1) +
                    kw(3, k) * v(i, j, k) + kw(4, k) * v(i, j, k - 1) + kw(5, k) * v(i, j, k - 2)) /
                   (2.0 * kw(6, k) * ddz);
     } else {
-      duvdx = -0.25 * (u13 * v3 + alpha * std::fabs(u13) * v4 - u14 * v5 -
-                       alpha * std::fabs(u14) * v6) /
+      duvdx = -0.25 * (u13 * v3 + alpha * fabs(u13) * v4 - u14 * v5 -
+                       alpha * fabs(u14) * v6) /
               b.deltax(i);
-      dvvdy = -0.25 * (v7 * v7 + alpha * std::fabs(v7) * v8 - v9 * v9 -
-                       alpha * std::fabs(v9) * v10) /
+      dvvdy = -0.25 * (v7 * v7 + alpha * fabs(v7) * v8 - v9 * v9 -
+                       alpha * fabs(v9) * v10) /
               b.deltay(j);
-      dwvdz = -0.25 * (w3 * v11 + alpha * std::fabs(w3) * v12 - w4 * v13 -
-                       alpha * std::fabs(w4) * v14) /
+      dwvdz = -0.25 * (w3 * v11 + alpha * fabs(w3) * v12 - w4 * v13 -
+                       alpha * fabs(w4) * v14) /
               b.deltaz(k);
     }
-    const double d2vdx2 =
+    const real d2vdx2 =
         (2.0 / (0.5 * (dx2xr + dx2xl))) * ((-v6 / (0.5 * dx2xr)) + (v4 / (0.5 * dx2xl)));
-    const double d2vdy2 = (2.0 / dy2ye) * ((-v10 / dye) + (v8 / dy));
-    const double d2vdz2 =
+    const real d2vdy2 = (2.0 / dy2ye) * ((-v10 / dye) + (v8 / dy));
+    const real d2vdz2 =
         (2.0 / (0.5 * (dz2zt + dz2zb))) * ((-v14 / (0.5 * dz2zt)) + (v12 / (0.5 * dz2zb)));
-    const double ytt2 = (d2vdx2 + d2vdy2 + d2vdz2) / re;
-    const double residv = (-duvdx - dvvdy - dwvdz + ytt2);
+    const real ytt2 = (d2vdx2 + d2vdy2 + d2vdz2) / re;
+    const real residv = (-duvdx - dvvdy - dwvdz + ytt2);
     b.vt(i, j, k) = v(i, j, k) + deltat * (residv + dpdy);
 
     // ---------------- W momentum ----------------
-    const double uw_e = u(i, j, k + 1) + (dzt / (dz2zt)) * (u(i, j, k) - u(i, j, k + 1));
-    const double uw_w =
+    const real uw_e = u(i, j, k + 1) + (dzt / (dz2zt)) * (u(i, j, k) - u(i, j, k + 1));
+    const real uw_w =
         u(i - 1, j, k + 1) + (dzt / (dz2zt)) * (u(i - 1, j, k) - u(i - 1, j, k + 1));
-    const double u_in_wm = 0.5 * (uw_e + uw_w);
-    const double vw_n = v(i, j, k + 1) + (dzt / (dz2zt)) * (v(i, j, k) - v(i, j, k + 1));
-    const double vw_s =
+    const real u_in_wm = 0.5 * (uw_e + uw_w);
+    const real vw_n = v(i, j, k + 1) + (dzt / (dz2zt)) * (v(i, j, k) - v(i, j, k + 1));
+    const real vw_s =
         v(i, j - 1, k + 1) + (dzt / (dz2zt)) * (v(i, j - 1, k) - v(i, j - 1, k + 1));
-    const double v_in_wm = 0.5 * (vw_n + vw_s);
-    double duwdx, dvwdy, dwwdz;
+    const real v_in_wm = 0.5 * (vw_n + vw_s);
+    real duwdx, dvwdy, dwwdz;
     third = false;
     if (i > 2 && i < nx_var + 1 && j > 2 && j < ny_var + 1 && k > 2 && k < nz_var)
       if (check_adjacent(b.cell, i, j, k, 1))
         if (check_adjacent(b.cell2, i, j, k, 2)) third = true;
     if (third) {
-      const double ddx = 0.5 * (b.deltax(i) + b.deltax(i - 1));
-      const double ddxr = 0.5 * (b.deltax(i) + b.deltax(i + 1));
-      const double ddy = 0.5 * (b.deltay(j) + b.deltay(j - 1));
-      const double ddye = 0.5 * (b.deltay(j) + b.deltay(j + 1));
+      const real ddx = 0.5 * (b.deltax(i) + b.deltax(i - 1));
+      const real ddxr = 0.5 * (b.deltax(i) + b.deltax(i + 1));
+      const real ddy = 0.5 * (b.deltay(j) + b.deltay(j - 1));
+      const real ddye = 0.5 * (b.deltay(j) + b.deltay(j + 1));
       auto& ca = b.ca_uw;
       auto& ck = b.ck_uw;
       duwdx = u_in_wm *
                   (ca(1, i) * w(i + 2, j, k) + ca(2, i) * w(i + 1, j, k) +
                    ca(3, i) * w(i, j, k) + ca(4, i) * w(i - 1, j, k) + ca(5, i) * w(i - 2, j, k)) /
                   (ca(6, i) * ddxr) +
-              std::fabs(u_in_wm) *
+              fabs(u_in_wm) *
                   (ck(1, i) * w(i + 2, j, k) + ck(2, i) * w(i + 1, j, k) +
                    ck(3, i) * w(i, j, k) + ck(4, i) * w(i - 1, j, k) + ck(5, i) * w(i - 2, j, k)) /
                   (2.0 * ck(6, i) * ddx);
@@ -603,7 +603,7 @@ void ns_momentum_2order(Block& b, double deltat, double re) {
                   (cv(1, j) * w(i, j + 2, k) + cv(2, j) * w(i, j + 1, k) +
                    cv(3, j) * w(i, j, k) + cv(4, j) * w(i, j - 1, k) + cv(5, j) * w(i, j - 2, k)) /
                   (cv(6, j) * ddye) +
-              std::fabs(v_in_wm) *
+              fabs(v_in_wm) *
                   (kv(1, j) * w(i, j + 2, k) + kv(2, j) * w(i, j + 1, k) +
                    kv(3, j) * w(i, j, k) + kv(4, j) * w(i, j - 1, k) + kv(5, j) * w(i, j - 2, k)) /
                   (2.0 * kv(6, j) * ddy);
@@ -613,28 +613,28 @@ void ns_momentum_2order(Block& b, double deltat, double re) {
                   (cw(1, k) * w(i, j, k + 2) + cw(2, k) * w(i, j, k + 1) +
                    cw(3, k) * w(i, j, k) + cw(4, k) * w(i, j, k - 1) + cw(5, k) * w(i, j, k - 2)) /
                   (cw(6, k) * b.deltaz(k + 1)) +
-              std::fabs(w(i, j, k)) *
+              fabs(w(i, j, k)) *
                   (kw(1, k) * w(i, j, k + 2) + kw(2, k) * w(i, j, k + 1) +
                    kw(3, k) * w(i, j, k) + kw(4, k) * w(i, j, k - 1) + kw(5, k) * w(i, j, k - 2)) /
                   (2.0 * kw(6, k) * b.deltaz(k));
     } else {
-      duwdx = -0.5 * (u15 * w5 + alpha * std::fabs(u15) * w6 - u16 * w7 -
-                      alpha * std::fabs(u16) * w8) /
+      duwdx = -0.5 * (u15 * w5 + alpha * fabs(u15) * w6 - u16 * w7 -
+                      alpha * fabs(u16) * w8) /
               b.deltax(i);
-      dvwdy = -0.5 * (v15 * w9 + alpha * std::fabs(v15) * w10 - v16 * w11 -
-                      alpha * std::fabs(v16) * w12) /
+      dvwdy = -0.5 * (v15 * w9 + alpha * fabs(v15) * w10 - v16 * w11 -
+                      alpha * fabs(v16) * w12) /
               b.deltay(j);
-      dwwdz = -0.5 * (w13 * w13 + alpha * std::fabs(w13) * w14 - w15 * w15 -
-                      alpha * std::fabs(w15) * w16) /
+      dwwdz = -0.5 * (w13 * w13 + alpha * fabs(w13) * w14 - w15 * w15 -
+                      alpha * fabs(w15) * w16) /
               b.deltaz(k);
     }
-    const double d2wdx2 =
+    const real d2wdx2 =
         (2.0 / (0.5 * (dx2xr + dx2xl))) * ((-w8 / (0.5 * dx2xr)) + (w6 / (0.5 * dx2xl)));
-    const double d2wdy2 =
+    const real d2wdy2 =
         (2.0 / (0.5 * (dy2ye + dy2yw))) * ((-w12 / (0.5 * dy2ye)) + (w10 / (0.5 * dy2yw)));
-    const double d2wdz2 = (2.0 / dz2zt) * ((-w16 / dzt) + (w14 / dz));
-    const double ztt2 = (d2wdx2 + d2wdy2 + d2wdz2) / re;
-    const double residw = (-duwdx - dvwdy - dwwdz + ztt2);
+    const real d2wdz2 = (2.0 / dz2zt) * ((-w16 / dzt) + (w14 / dz));
+    const real ztt2 = (d2wdx2 + d2wdy2 + d2wdz2) / re;
+    const real residw = (-duwdx - dvwdy - dwwdz + ztt2);
     b.wt(i, j, k) = w(i, j, k) + deltat * (residw + dpdz);
 
     // restore with the t-ghosts of the last TS index (src/NavierStokes.f90:860-907)
@@ -690,7 +690,7 @@ void ns_momentum_2order(Block& b, double deltat, double re) {
 }
 
 // velocityBC, src/BoundaryConditions.f90:11-74 (three loops in order)
-void velocity_bc(Block& b, double deltat, double uc) {
+void velocity_bc(Block& b, real deltat, real uc) {
   const int64_t nx = b.nx, ny = b.ny, nz = b.nz;
   for (int64_t k = 2; k <= nz + 1; ++k)
     for (int64_t j = 2; j <= ny + 1; ++j) {

@@ -26,7 +26,7 @@ void correct_pressure(Block& b) {
 }
 
 // correctVelocity, src/PcorVcor.F90:261-286
-void correct_velocity(Block& b, double deltat) {
+void correct_velocity(Block& b, real deltat) {
 #pragma omp parallel for schedule(static)
   for (int64_t n = 1; n <= b.fluidCellCount; ++n) {
     const int64_t i = b.fluidIndexPtr(n, 1), j = b.fluidIndexPtr(n, 2), k = b.fluidIndexPtr(n, 3);
@@ -46,9 +46,9 @@ void correct_velocity(Block& b, double deltat) {
 // write (the other colour, pco, b), and a maximum does not depend on the
 // order of its operands, so the loops run in parallel (OpenMP) with results
 // identical to the serial order.
-void redblack_sor_linear(Block& b, int64_t pcItaMax, double deltat, double epsi) {
-  const double omega = b.omega;
-  double derr4 = 11111.0;
+void redblack_sor_linear(Block& b, int64_t pcItaMax, real deltat, real epsi) {
+  const real omega = b.omega;
+  real derr4 = 11111.0;
   b.derr2 = 0.0;
   for (;;) {
     b.nIterPcor = b.nIterPcor + 1;
@@ -56,7 +56,7 @@ void redblack_sor_linear(Block& b, int64_t pcItaMax, double deltat, double epsi)
     for (int64_t n = 1; n <= b.redCellCount; ++n) {
       const int64_t i = b.redCellIndexPtr(n, 1), j = b.redCellIndexPtr(n, 2),
                     k = b.redCellIndexPtr(n, 3);
-      double v = (b.b(i, j, k) / deltat - b.Acx(i - 1, 1) * b.pco(i - 1, j, k) -
+      real v = (b.b(i, j, k) / deltat - b.Acx(i - 1, 1) * b.pco(i - 1, j, k) -
                   b.Acx(i - 1, 3) * b.pco(i + 1, j, k) - b.Acy(j - 1, 1) * b.pco(i, j - 1, k) -
                   b.Acy(j - 1, 3) * b.pco(i, j + 1, k) - b.Acz(k - 1, 1) * b.pco(i, j, k - 1) -
                   b.Acz(k - 1, 3) * b.pco(i, j, k + 1)) /
@@ -68,7 +68,7 @@ void redblack_sor_linear(Block& b, int64_t pcItaMax, double deltat, double epsi)
     for (int64_t n = 1; n <= b.blackCellCount; ++n) {
       const int64_t i = b.blackCellIndexPtr(n, 1), j = b.blackCellIndexPtr(n, 2),
                     k = b.blackCellIndexPtr(n, 3);
-      double v = (b.b(i, j, k) / deltat - b.Acx(i - 1, 1) * b.pc(i - 1, j, k) -
+      real v = (b.b(i, j, k) / deltat - b.Acx(i - 1, 1) * b.pc(i - 1, j, k) -
                   b.Acx(i - 1, 3) * b.pc(i + 1, j, k) - b.Acy(j - 1, 1) * b.pc(i, j - 1, k) -
                   b.Acy(j - 1, 3) * b.pc(i, j + 1, k) - b.Acz(k - 1, 1) * b.pc(i, j, k - 1) -
                   b.Acz(k - 1, 3) * b.pc(i, j, k + 1)) /
@@ -77,20 +77,20 @@ void redblack_sor_linear(Block& b, int64_t pcItaMax, double deltat, double epsi)
       b.pc(i, j, k) = (1.0 - omega) * b.pco(i, j, k) + omega * b.pc(i, j, k);
     }
     if (b.nIterPcor % 5 == 0) {
-      double m = 0.0;
+      double m = 0.0;  // the stop test reads values only
 #pragma omp parallel for schedule(static) reduction(max : m)
       for (int64_t n = 1; n <= b.fluidCellCount; ++n) {
         const int64_t i = b.fluidIndexPtr(n, 1), j = b.fluidIndexPtr(n, 2),
                       k = b.fluidIndexPtr(n, 3);
-        const double var = std::fabs(b.pc(i, j, k) - b.pco(i, j, k));
-        m = std::fmax(m, var);
+        const double var = val(fabs(b.pc(i, j, k) - b.pco(i, j, k)));
+        m = fmax(m, var);
       }
       derr4 = m;
     }
     {
       const size_t nd = b.pc.d.size();
-      const double* src = b.pc.d.data();
-      double* dst = b.pco.d.data();
+      const real* src = b.pc.d.data();
+      real* dst = b.pco.d.data();
 #pragma omp parallel for schedule(static)
       for (size_t q = 0; q < nd; ++q) dst[q] = src[q];
     }
@@ -110,7 +110,7 @@ void update_velocity_newv(Block& b) {
 // poissonSolver, src/PcorVcor.F90:22-220 over blocks start..finish by step.
 // Block 1 is the coarse block; the OpenMP regions run their block loops in
 // order (the blocks are independent inside each region).
-void poisson_solver(int64_t pcItaMax, double epsi, double deltat, double uc, int64_t start,
+void poisson_solver(int64_t pcItaMax, real epsi, real deltat, real uc, int64_t start,
                     int64_t finish, int64_t step) {
   for (int64_t g = start; g <= finish; g += step) {
     Block& b = blk_of(g);
@@ -142,14 +142,14 @@ void poisson_solver(int64_t pcItaMax, double epsi, double deltat, double uc, int
     if (g == 1) velocity_bc(blk_of(1), deltat, uc);
   for (int64_t g = start; g <= finish; g += step) {
     Block& b = blk_of(g);
-    double err_ds = 0.0;
+    double err_ds = 0.0;  // a statistic: values only
 #pragma omp parallel for schedule(static) reduction(max : err_ds)
     for (int64_t n = 1; n <= b.fluidCellCount; ++n) {
       const int64_t i = b.fluidIndexPtr(n, 1), j = b.fluidIndexPtr(n, 2), k = b.fluidIndexPtr(n, 3);
-      const double eu = std::fabs((b.ut(i, j, k) - b.u(i, j, k))) / deltat;
-      const double ev = std::fabs((b.vt(i, j, k) - b.v(i, j, k))) / deltat;
-      const double ew = std::fabs((b.wt(i, j, k) - b.w(i, j, k))) / deltat;
-      err_ds = std::fmax(std::fmax(std::fmax(err_ds, eu), ev), ew);
+      const double eu = val(fabs((b.ut(i, j, k) - b.u(i, j, k))) / deltat);
+      const double ev = val(fabs((b.vt(i, j, k) - b.v(i, j, k))) / deltat);
+      const double ew = val(fabs((b.wt(i, j, k) - b.w(i, j, k))) / deltat);
+      err_ds = fmax(fmax(fmax(err_ds, eu), ev), ew);
     }
     b.derrStdSt = err_ds;
   }

@@ -11,19 +11,19 @@ namespace orc {
 // computeSurfaceNorm, src/Search.F90:210-258
 void compute_surface_norm(Block& b, int64_t inor) {
   for (int64_t n = 1; n <= b.ibElems; ++n) {
-    const double p1x = b.xnode1(b.ibElP1(n)), p1y = b.ynode1(b.ibElP1(n)), p1z = b.znode1(b.ibElP1(n));
-    const double p2x = b.xnode1(b.ibElP2(n)), p2y = b.ynode1(b.ibElP2(n)), p2z = b.znode1(b.ibElP2(n));
-    const double p3x = b.xnode1(b.ibElP3(n)), p3y = b.ynode1(b.ibElP3(n)), p3z = b.znode1(b.ibElP3(n));
+    const real p1x = b.xnode1(b.ibElP1(n)), p1y = b.ynode1(b.ibElP1(n)), p1z = b.znode1(b.ibElP1(n));
+    const real p2x = b.xnode1(b.ibElP2(n)), p2y = b.ynode1(b.ibElP2(n)), p2z = b.znode1(b.ibElP2(n));
+    const real p3x = b.xnode1(b.ibElP3(n)), p3y = b.ynode1(b.ibElP3(n)), p3z = b.znode1(b.ibElP3(n));
     b.xcent(n) = (p2x + p1x + p3x) / 3.0;
     b.ycent(n) = (p2y + p1y + p3y) / 3.0;
     b.zcent(n) = (p2z + p1z + p3z) / 3.0;
     b.cosAlpha(n) = (p2y - p1y) * (p3z - p1z) - (p3y - p1y) * (p2z - p1z);
     b.cosBeta(n) = (p2z - p1z) * (p3x - p1x) - (p3z - p1z) * (p2x - p1x);
     b.cosGamma(n) = (p2x - p1x) * (p3y - p1y) - (p3x - p1x) * (p2y - p1y);
-    const double len = std::sqrt(b.cosAlpha(n) * b.cosAlpha(n) + b.cosBeta(n) * b.cosBeta(n) +
+    const real len = sqrt(b.cosAlpha(n) * b.cosAlpha(n) + b.cosBeta(n) * b.cosBeta(n) +
                                  b.cosGamma(n) * b.cosGamma(n));
     b.element_length(n) = len;
-    const double fin = (double)inor;
+    const real fin = (real)inor;
     b.cosAlpha(n) = fin * b.cosAlpha(n) / len;
     b.cosBeta(n) = fin * b.cosBeta(n) / len;
     b.cosGamma(n) = fin * b.cosGamma(n) / len;
@@ -31,16 +31,16 @@ void compute_surface_norm(Block& b, int64_t inor) {
 }
 
 namespace {
-inline double sq3(double a, double b, double c) { return a * a + b * b + c * c; }
+inline real sq3(real a, real b, real c) { return a * a + b * b + c * c; }
 
 // one cell of the nearest-element tagging (src/Search.F90:294-338 and the
 // identical body of selectiveRetagging_th, :553-591)
 void tag_cell(Block& b, int64_t i, int64_t j, int64_t k) {
-  double minDis = 1e14, minDis1 = 1e14;
+  real minDis = 1e14, minDis1 = 1e14;
   int64_t nel2Cen = 0, nel2Pnt = 0;
   for (int64_t m = 1; m <= b.ibElems; ++m) {
-    const double dis_cen = sq3(b.xp(i) - b.xcent(m), b.yp(j) - b.ycent(m), b.zp(k) - b.zcent(m));
-    const double dis_pnt = sq3(b.x1(i) - b.xcent(m), b.y1(j) - b.ycent(m), b.z1(k) - b.zcent(m));
+    const real dis_cen = sq3(b.xp(i) - b.xcent(m), b.yp(j) - b.ycent(m), b.zp(k) - b.zcent(m));
+    const real dis_pnt = sq3(b.x1(i) - b.xcent(m), b.y1(j) - b.ycent(m), b.z1(k) - b.zcent(m));
     if (dis_cen < minDis) {
       minDis = dis_cen;
       nel2Cen = m;
@@ -54,7 +54,7 @@ void tag_cell(Block& b, int64_t i, int64_t j, int64_t k) {
       (b.y1(j) <= b.ycent(nel2Cen) && b.y1(j + 1) >= b.ycent(nel2Cen)) &&
       (b.z1(k) <= b.zcent(nel2Cen) && b.z1(k + 1) >= b.zcent(nel2Cen)))
     b.cell(i, j, k) = 2;
-  const double n2dotn = (b.x1(i) - b.xcent(nel2Pnt)) * b.cosAlpha(nel2Pnt) +
+  const real n2dotn = (b.x1(i) - b.xcent(nel2Pnt)) * b.cosAlpha(nel2Pnt) +
                         (b.y1(j) - b.ycent(nel2Pnt)) * b.cosBeta(nel2Pnt) +
                         (b.z1(k) - b.zcent(nel2Pnt)) * b.cosGamma(nel2Pnt);
   b.nodeIdTag(i, j, k) = (n2dotn >= -1e-16) ? 0 : 1;
@@ -241,14 +241,14 @@ void compute_norm_distance(Block& b) {
   for (int64_t k = 1; k <= nib; ++k) {
     const int64_t ci = b.interceptedIndexPtr(k, 1), cj = b.interceptedIndexPtr(k, 2),
                   ck = b.interceptedIndexPtr(k, 3);
-    const double n1x = b.xp(ci), n2x = b.x1(ci), n3x = b.x1(ci + 1);
-    const double n1y = b.yp(cj), n2y = b.y1(cj), n3y = b.y1(cj + 1);
-    const double n1z = b.zp(ck), n2z = b.z1(ck), n3z = b.z1(ck + 1);
-    double md[7] = {1e14, 1e14, 1e14, 1e14, 1e14, 1e14, 1e14};
+    const real n1x = b.xp(ci), n2x = b.x1(ci), n3x = b.x1(ci + 1);
+    const real n1y = b.yp(cj), n2y = b.y1(cj), n3y = b.y1(cj + 1);
+    const real n1z = b.zp(ck), n2z = b.z1(ck), n3z = b.z1(ck + 1);
+    real md[7] = {1e14, 1e14, 1e14, 1e14, 1e14, 1e14, 1e14};
     int64_t nel[7] = {0, 0, 0, 0, 0, 0, 0};
     for (int64_t m = 1; m <= b.ibElems; ++m) {
-      const double cx = b.xcent(m), cy = b.ycent(m), cz = b.zcent(m);
-      const double d[7] = {
+      const real cx = b.xcent(m), cy = b.ycent(m), cz = b.zcent(m);
+      const real d[7] = {
           sq3(n1x - cx, n1y - cy, n1z - cz), sq3(n2x - cx, n1y - cy, n1z - cz),
           sq3(n3x - cx, n1y - cy, n1z - cz), sq3(n1x - cx, n2y - cy, n1z - cz),
           sq3(n1x - cx, n3y - cy, n1z - cz), sq3(n1x - cx, n1y - cy, n2z - cz),
@@ -266,7 +266,7 @@ void compute_norm_distance(Block& b) {
     b.nelv2(k) = nel[4];
     b.nelw1(k) = nel[5];
     b.nelw2(k) = nel[6];
-    auto nd = [&](int64_t e, double x, double y, double z) {
+    auto nd = [&](int64_t e, real x, real y, real z) {
       return (x - b.xcent(e)) * b.cosAlpha(e) + (y - b.ycent(e)) * b.cosBeta(e) +
              (z - b.zcent(e)) * b.cosGamma(e);
     };
@@ -328,7 +328,7 @@ void fine_block_cell() {
     for (int64_t k = 2; k <= a.nz + 1; ++k)
       for (int64_t j = 2; j <= a.ny + 1; ++j)
         for (int64_t i = 2; i <= a.nx + 1; ++i) {
-          const double ci = (double)fb.cintp;
+          const real ci = (real)fb.cintp;
           if (a.xp(i) >= it.xintf_start + ci * a.dx && a.xp(i) <= it.xintf_end - ci * a.dx &&
               a.zp(k) >= it.zintf_start + ci * a.dz && a.zp(k) <= it.zintf_end - ci * a.dz &&
               a.yp(j) >= it.yintf_start + ci * a.dy && a.yp(j) <= it.yintf_end - ci * a.dy) {

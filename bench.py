@@ -495,8 +495,15 @@ def sweep_roofline(torch, local, hbm, block=(384, 256, 256), fp32_pairs=40, fp64
     cells = block[0] * block[1] * block[2]
     out = {"block": "x".join(map(str, block)) + f" ({cells / 1e6:.1f}M cells), no body",
            "l2": f"FP32 working set {17 * cells / 1e6:.0f} MB vs 129 MB L2", "solve_launch": s.solve_launch(g)}
-    for prec, pairs, key in ((1, fp32_pairs, "fp32"), (0, fp64_pairs, "fp64_reference_sweeps"),
+    tuned = s.solve_launch(g)
+    for prec, pairs, key in ((1, fp32_pairs, "fp32"), (1, fp32_pairs, "fp32_tiled_neighbour_sync"),
+                             (1, fp32_pairs, "fp32_zmarch_tma"), (0, fp64_pairs, "fp64_reference_sweeps"),
                              (2, fp64_pairs, "fp64_division_free")):
+        # fp32: the autotuned variant; then the tiled sweeps with neighbour
+        # sync (variant 3) and the z-marching TMA sweeps (variant 5) alone
+        variant = {"fp32": tuned["fp32_variant"], "fp32_tiled_neighbour_sync": 3, "fp32_zmarch_tma": 5}.get(key)
+        if variant is not None:
+            s.set_mixed_params(variant=variant, block=g)
         runs = {}
         for n in (pairs, 2 * pairs):
             s.profile_begin()
@@ -619,7 +626,8 @@ def adjoint_flapping(torch, steps=200, every=20, fd=(), size="full", epsi=1e-12)
         inputs = {k: v for k, v in mv.items() if k in ("phase_deg", "freq")}
         if own:
             blocks[1] = dataclasses.replace(blocks[1], motion=dataclasses.replace(blocks[1].motion, **own))
-        return synth.replace(base, blocks=blocks, motion=dataclasses.replace(base.motion, **inputs))
+        kw = {"uc": mv["uc"]} if "uc" in mv else {}
+        return synth.replace(base, blocks=blocks, motion=dataclasses.replace(base.motion, **inputs), **kw)
 
     def run(case, gradient):
         s = Solver(case)
@@ -636,7 +644,8 @@ def adjoint_flapping(torch, steps=200, every=20, fd=(), size="full", epsi=1e-12)
 
     (J, duc, g), secs, counts = run(base, True)
     mo, mi = base.blocks[1].motion, base.motion
-    p0 = {"yamp": mo.yamp, "a0_deg": mo.a0_deg, "phase_deg": mi.phase_deg, "freq": mi.freq, "bfreq": mo.bfreq}
+    p0 = {"yamp": mo.yamp, "a0_deg": mo.a0_deg, "phase_deg": mi.phase_deg, "freq": mi.freq, "bfreq": mo.bfreq,
+          "uc": base.uc}
     cells = sum(b.nx * b.ny * b.nz for b in base.blocks)
     out = {"workload": f"flapping plate 0.5x0.125x0.0125 (surface 51, thin-surface cells), coarse "
                        f"{base.blocks[0].nx}x{base.blocks[0].ny}x{base.blocks[0].nz} + fine "
@@ -652,10 +661,69 @@ def adjoint_flapping(torch, steps=200, every=20, fd=(), size="full", epsi=1e-12)
         jp, sp, _ = run(make(**{name: p0[name] + h}), False)
         jm, sm, _ = run(make(**{name: p0[name] - h}), False)
         fdv = (jp - jm) / (2 * h)
-        out["fd"].append({"param": name, "rel_step": float(rel), "fd": fdv, "adjoint": g["motion"][name],
-                          "rel_diff": abs(fdv - g["motion"][name]) / max(abs(fdv), 1e-300)})
+        adj = duc if name == "uc" else g["motion"][name]
+        out["fd"].append({"param": name, "rel_step": float(rel), "fd": fdv, "adjoint": adj, "J_plus": jp,
+                          "J_minus": jm, "rel_diff": abs(fdv - adj) / max(abs(fdv), 1e-300)})
         out["ms_per_step_forward_only"] = 500.0 * (sp + sm) / steps
         print(json.dumps(out["fd"][-1]), flush=True)
+    return out
+
+
+def tandem_long(torch, local, fwd=1000, cmp=100, adj=20, every=5, adj_tol=1e-10):
+    """The tandem-plate workload (44.0M cells, both plates heaving and
+    pitching, the trailing plate 90 deg behind) over a long horizon:
+    (1) the mixed path and the division-free FP64 path (at the mixed path's
+    relaxation factor) from the same initial state for `cmp` steps, and the
+    mixed path's error in every field and in each plate's drag/lift
+    coefficients after them; (2) the mixed path continued to `fwd` steps
+    (time per step, residual); (3) from there the discrete adjoint of the next
+    `adj` FP64 drop-in steps, checkpointed every `every` steps: J = the leading
+    plate's time-averaged drag coefficient (viscous + pressure), its gradient
+    with respect to the leading plate's heave and pitch amplitude and heave
+    frequency, the shared phase angle and pitch frequency (both plates move
+    with them) and the inflow velocity, with the adjoint Poisson solves to
+    the residual adj_tol."""
+    from biocfd import synth
+    from biocfd.adjoint import adjoint_run_motion
+    case = synth.with_mixed_omega(synth.tandem_plates(n_steps=fwd + adj + 4, moving=True))
+    mu_f = 1.0 / case.re
+    out = {"workload": "tandem plates, 44.0M cells: coarse 384x256x256 + two fine 256x192x192, both plates "
+                       "heaving 0.125 sin(2 pi 0.25 t) and pitching 15 deg sin(2 pi 0.25 t + 90 deg), trailing "
+                       "plate 90 deg behind, Re 1000, Search every step",
+           "omega": [b.omega for b in case.blocks]}
+    sa = new_solver(case, local)
+    ta, _ = timed_steps(sa, torch, cmp, 1)
+    snap_a = ([sa.fields(g) for g in sa.handles], [sa.stress(g, mu_f).tolist() for g in sa.handles[1:]])
+    sb = new_solver(case, local)
+    tb, _ = timed_steps(sb, torch, cmp, 3)
+    snap_b = ([sb.fields(g) for g in sb.handles], [sb.stress(g, mu_f).tolist() for g in sb.handles[1:]])
+    res_b, _ = residual_stats(sb)
+    sb.close()
+    err, coef = field_errors(snap_a[0], snap_b[0], snap_a[1], snap_b[1])
+    out["mixed_vs_fp64"] = {"after_steps": cmp, "field_rel_l2": err, "coef_rel": coef,
+                            "coefficients": "per plate: viscous drag, pressure drag, viscous lift, pressure lift",
+                            "mixed_ms_per_step": statistics.mean(ta), "fp64_ms_per_step": statistics.mean(tb),
+                            "fp64_div_residual": res_b,
+                            "fp64": "FP64 momentum + division-free FP64 SOR to the residual 1e-6"}
+    del snap_b
+    tc, _ = timed_steps(sa, torch, fwd - cmp, 1)
+    res_a, pairs_a = residual_stats(sa)
+    out["forward"] = {"steps": fwd, "ms_per_step_last": statistics.mean(tc[-50:]),
+                      "ms_per_step_all": statistics.mean(ta + tc), "seconds": (sum(ta) + sum(tc)) / 1000.0,
+                      "div_residual_last_step": res_a, "sweep_pairs_last_step": pairs_a,
+                      "leading_plate_coefficients": sa.stress(sa.handles[1], mu_f).tolist()}
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    J, duc, g = adjoint_run_motion(sa, {}, adj, every=every, block=1, stress_seed=(1.0, 1.0, 0.0, 0.0), mu_f=mu_f,
+                                   rho_f=1.0, adj_tol=adj_tol)
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    out["adjoint"] = {"steps": adj, "every": every, "adj_tol": adj_tol, "J": J, "dJ_duc": duc,
+                      "dJ_dmotion": g["motion"], "seconds_forward_and_reverse": secs,
+                      "s_per_step_forward_and_reverse": secs / adj,
+                      "objective": "mean over the adjoint steps of the leading plate's viscous + pressure drag "
+                                   "coefficients (FP64 drop-in steps from the mixed path's state)"}
+    sa.close()
     return out
 
 
@@ -798,6 +866,9 @@ def main():
     ap.add_argument("--adjoint-flapping", default="",
                     help="STEPS[,EVERY[,name:rel;name:rel...]]: only the moving-plate adjoint on the coarse "
                          "128x96x96 + fine 128^3 pair, with optional central differences")
+    ap.add_argument("--tandem-long", default="",
+                    help="FWD,CMP,ADJ[,EVERY]: only the long tandem-plate run: mixed vs FP64 after CMP steps, FWD "
+                         "mixed steps, then the adjoint of ADJ FP64 steps")
     ap.add_argument("--alu-only", action="store_true", help="only the arithmetic-rate measurement")
     ap.add_argument("--zero-start", action="store_true",
                     help="start every residual-target solve from pc = 0 (the reference's start)")
@@ -834,6 +905,12 @@ def main():
         v = args.adjoint_flapping.split(",")
         fd = tuple(x for x in v[2].split(";") if x) if len(v) > 2 else ()
         print(json.dumps(adjoint_flapping(torch, int(v[0]), int(v[1]) if len(v) > 1 else 20, fd)), flush=True)
+        return
+    if args.tandem_long:
+        import torch
+        torch.cuda.set_device(0)
+        v = [int(x) for x in args.tandem_long.split(",")]
+        print(json.dumps(tandem_long(torch, 0, v[0], v[1], v[2], v[3] if len(v) > 3 else 5)), flush=True)
         return
     if args.alu_only:
         print(json.dumps(alu_rates(0)), flush=True)

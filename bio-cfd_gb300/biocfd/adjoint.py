@@ -8,7 +8,8 @@ A is the Poisson operator of one block restricted to its fluid cells (zero
 data on the other cells).
 
 Whole runs of time steps: adjoint_run (fixed geometry), adjoint_run_motion
-(one moving body, gradients with respect to its motion parameters) and
+(moving bodies, gradients with respect to the motion parameters of the
+objective's body) and
 run_function, which wraps either as a torch.autograd.Function of the initial
 state and the scalar parameters.
 
@@ -152,7 +153,9 @@ def adjoint_run_motion(solver, weights: dict, n_steps: int, every: int = 20, blo
                        mu_f: float = 1.0, rho_f: float = 1.0):
     """adjoint_run through a moving body (bcfd_adjoint_run_motion): J of
     n_steps FP64 steps with the weights and drag/lift of block `block`, whose
-    body is the run's one moving body.  Returns J, or with `gradient`
+    body moves (other moving bodies, e.g. a plate in tandem, move with the
+    run and count towards the shared phase and pitch frequency).  Returns J,
+    or with `gradient`
     (J, dJ/duc, {"u","v","w","p": dJ/dx^0 of the block, "motion": {name:
     dJ/d name for MOTION_PARAMS}}).  The body's tags, nodes and motion state
     are checkpointed with the fields; the block advances by n_steps exactly

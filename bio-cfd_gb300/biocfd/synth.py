@@ -479,7 +479,8 @@ def twelve_block(n_steps: int = 10, seed: int = SEED, moving: bool = False) -> C
                        plate_axes=(0.5, 0.125, 0.0125), motion=motion, motion_inputs=inputs)
 
 
-def tandem_plates(n_steps: int = 2, seed: int = SEED, moving: bool = False, lag_deg: float = 90.0) -> Case:
+def tandem_plates(n_steps: int = 2, seed: int = SEED, moving: bool = False, lag_deg: float = 90.0,
+                  size: str = "full") -> Case:
     """Two thin plates in tandem on the 44M-cell layout: a coarse 384x256x256
     block over 6x4x4 (dx 1/64) and two fine 256x192x192 blocks at ratio 2
     (dx 1/128), each holding a rigid ellipsoidal plate of semi-axes
@@ -490,7 +491,22 @@ def tandem_plates(n_steps: int = 2, seed: int = SEED, moving: bool = False, lag_
     (15 deg); the trailing plate does the same `lag_deg` behind
     (bcfd_block_set_body_lag), starting at its own t = 0 state.  The
     amplitudes keep each plate inside its block's move margins
-    (src/Search.F90:1010-1040)."""
+    (src/Search.F90:1010-1040).  "small": the same arrangement at test size --
+    coarse 96x48x24 over 6x3x1.5 (dx 1/16), two fine 64x72x24 blocks (dx
+    1/32) just wide enough for the move margins, plates 0.1 x 0.05 x 0.008
+    (thinner than a fine cell), heave 0.05, pitch 10 deg, Re 300."""
+    if size == "small":
+        boxes = (((0.5, 2.5), (0.375, 2.625), (0.375, 1.125)),
+                 ((3.0, 5.0), (0.375, 2.625), (0.375, 1.125)))
+        motion = inputs = None
+        if moving:
+            motion = Motion(a0_deg=10.0, bfreq=0.25, yamp=0.05)
+            inputs = MotionInputs(aoa_deg=10.0, phase_deg=90.0, piv_pt=0.0, freq=0.25, dxmin=1.0 / 32.0)
+        case = multi_block(coarse=(96, 48, 24), domain=(6.0, 3.0, 1.5), fine_boxes=boxes, body=(0, 1),
+                           diameter=0.2, reynolds=300.0, n_steps=n_steps, seed=seed, plate=True,
+                           plate_axes=(0.1, 0.05, 0.008), motion=motion, motion_inputs=inputs,
+                           lags_deg=(0.0, lag_deg) if moving else None)
+        return replace(case, name="tandem_plates_small")
     boxes = (((0.75, 2.75), (1.25, 2.75), (1.25, 2.75)),
              ((3.25, 5.25), (1.25, 2.75), (1.25, 2.75)))
     motion = inputs = None

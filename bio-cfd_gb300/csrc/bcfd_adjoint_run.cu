@@ -651,22 +651,32 @@ int restore_body(HostBlock* hb, const BodyRec& r) {
 }
 
 // the recorder of a segment's recomputation: per step, the geometric
-// partials of the moving body's forcing calls
+// partials of every moving body's forcing calls
 struct MoveRecorder : ForceRecorder {
-  HostBlock* body = nullptr;
-  BodyRec* cur = nullptr;
+  std::vector<HostBlock*> bodies;
+  std::vector<BodyRec*> cur;  // per body: the record of the step being recomputed
+  std::vector<double*> sc;    // per body: 3 point arrays of scratch
   DevMem* mem = nullptr;
-  double* sc = nullptr;
   bool oom = false;
-  double* slot(HostBlock* hb, int mode, int vel, int64_t nt) override {
-    if (hb != body || !cur || nt <= 0) return nullptr;
-    const int c = 2 * mode + vel;
-    cur->nt[c] = nt;
-    cur->geo[c] = mem->get<double>(6 * (size_t)nt);
-    if (!cur->geo[c]) oom = true;
-    return cur->geo[c];
+  int find(HostBlock* hb) const {
+    for (size_t i = 0; i < bodies.size(); ++i)
+      if (bodies[i] == hb) return (int)i;
+    return -1;
   }
-  double* scratch(HostBlock* hb) override { return hb == body ? sc : nullptr; }
+  double* slot(HostBlock* hb, int mode, int vel, int64_t nt) override {
+    const int i = find(hb);
+    if (i < 0 || !cur[(size_t)i] || nt <= 0) return nullptr;
+    BodyRec* r = cur[(size_t)i];
+    const int c = 2 * mode + vel;
+    r->nt[c] = nt;
+    r->geo[c] = mem->get<double>(6 * (size_t)nt);
+    if (!r->geo[c]) oom = true;
+    return r->geo[c];
+  }
+  double* scratch(HostBlock* hb) override {
+    const int i = find(hb);
+    return i < 0 ? nullptr : sc[(size_t)i];
+  }
 };
 
 }  // namespace
@@ -929,8 +939,9 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
   return 0;
 }
 
-// The moving-body run: one moving body, on block h.  Forward as above, with
-// the body's tags, nodes and motion state checkpointed beside the fields.  In
+// The moving-body run: the objective's moving body on block h, and any other
+// moving bodies.  Forward as above, with every moving body's tags, nodes and
+// motion state checkpointed beside the fields.  In
 // reverse each segment is recomputed with the forcing recorder on (per step:
 // the forcing calls' geometric partials, the tags, nodes and motion state the
 // step leaves), then every step is transposed in two halves: the part after
@@ -954,9 +965,17 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
   for (auto& [g, b] : all) {
     if (!b->d.ca[0] || !b->d.Acx) return BCFD_E_STATE;
     if (g != all.front().first && b->is_coarse) return BCFD_E_STATE;
-    if (b->motion.on && b != hb) return BCFD_E_STATE;  // one moving body, the objective's
   }
-  if (!hb->motion.on || !hb->motion.placed || !hb->has_body || hb->d.ne <= 0 || hb->d.nn <= 0) return BCFD_E_STATE;
+  if (!hb->motion.on) return BCFD_E_STATE;
+  // the moving bodies (the objective's and any others, e.g. a plate in tandem)
+  std::vector<int> movers;
+  for (int q = 0; q < (int)all.size(); ++q) {
+    HostBlock* b = all[q].second;
+    if (!b->motion.on) continue;
+    if (!b->motion.placed || !b->has_body || b->d.ne <= 0 || b->d.nn <= 0) return BCFD_E_STATE;
+    movers.push_back(q);
+  }
+  const int nmov = (int)movers.size();
   std::vector<HostInterface*> ifs;
   for (HostInterface* it : lib().ifs)
     if (it) ifs.push_back(it);
@@ -976,15 +995,21 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
   const size_t fb = (size_t)np * sizeof(double);
   const int64_t K = std::min(every, n_steps);
   const int64_t ncp = (n_steps + K - 1) / K;
-  const int ne = hb->d.ne, nn = hb->d.nn;
+  const int ne = hb->d.ne;
   DevMem mem;
   double* W = mem.get<double>(4 * np);
   double* cps = mem.get<double>((size_t)ncp * S);
   double* fin = mem.get<double>(S);
   double* part = mem.get<double>(kDotCtas);
   if (!W || !cps || !fin || !part) return BCFD_E_NOMEM;
-  std::vector<BodyRec> cprec((size_t)ncp);
-  BodyRec finrec;
+  // per moving body: its state at the checkpoints and at the end
+  std::vector<std::vector<BodyRec>> cprec((size_t)nmov, std::vector<BodyRec>((size_t)ncp));
+  std::vector<BodyRec> finrec((size_t)nmov);
+  auto mover = [&](int mi) { return all[(size_t)movers[(size_t)mi]].second; };
+  auto save_bodies = [&](std::vector<BodyRec>* recs, size_t at, DevMem& m) -> int {
+    for (int mi = 0; mi < nmov; ++mi) TRY_R(save_body(mover(mi), recs[mi][at], m));
+    return 0;
+  };
   const double* wh[4] = {wu, wv, ww, wp};
   for (int q = 0; q < 4; ++q) ACK(h2d(W + q * np, wh[q], fb));
   ACK(cudaMemsetAsync(part, 0, kDotCtas * sizeof(double), stream()));
@@ -1016,7 +1041,7 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
     ACK(cudaMemcpyAsync(b->d.wt, b->d.w, bytes, cudaMemcpyDeviceToDevice, stream()));
   }
   TRY_R(save_all(cps));
-  TRY_R(save_body(hb, cprec[0], mem));
+  TRY_R(save_bodies(cprec.data(), 0, mem));
   std::vector<double*> g0(nb, nullptr);
   for (int q = 0; q < nb; ++q) {
     HostBlock* b = all[q].second;
@@ -1036,7 +1061,10 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
   for (int64_t n = 1; n <= n_steps; ++n) {
     TRY_R(run_one_step(c));
     // a fine-block move changes the blocks' structure: not differentiated
-    if (hb->move_amt[0] || hb->move_amt[1] || hb->move_amt[2]) return fail(BCFD_E_STATE);
+    for (int mi = 0; mi < nmov; ++mi) {
+      const HostBlock* b = mover(mi);
+      if (b->move_amt[0] || b->move_amt[1] || b->move_amt[2]) return fail(BCFD_E_STATE);
+    }
     k_dot_acc<<<kDotCtas, kDotThreads, 0, stream()>>>(W, bx, np, part);
     BCFD_LAUNCHED();
     if (use_stress) {
@@ -1049,11 +1077,11 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
     }
     if (n % K == 0 && n < n_steps) {
       TRY_R(save_all(cps + (size_t)(n / K) * S));
-      TRY_R(save_body(hb, cprec[(size_t)(n / K)], mem));
+      TRY_R(save_bodies(cprec.data(), (size_t)(n / K), mem));
     }
   }
   TRY_R(save_all(fin));
-  TRY_R(save_body(hb, finrec, mem));
+  for (int mi = 0; mi < nmov; ++mi) TRY_R(save_body(mover(mi), finrec[(size_t)mi], mem));
   std::vector<double> ph(kDotCtas);
   ACK(d2h(ph.data(), part, kDotCtas * sizeof(double)));
   double jsum = 0.0;
@@ -1066,11 +1094,15 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
   const bool grad = dj_duc || dj_dmotion || gu || gv || gw || gp;
   if (!grad) return fail(0);
 
-  // the motion's parameter tangents for every driver step of the run
-  std::vector<StepTangent> tan;
-  TRY_R(motion_tangent(hb, L.phase_angle, L.freq, cfg->deltat, tot0, ita0, ita0 + n_steps, tan));
-  const int64_t first = hb->motion.init_ita;
-  if (ita0 < first) return fail(BCFD_E_STATE);
+  // each moving body's parameter tangents for every driver step of the run
+  std::vector<std::vector<StepTangent>> tan((size_t)nmov);
+  std::vector<int64_t> first((size_t)nmov);
+  for (int mi = 0; mi < nmov; ++mi) {
+    HostBlock* b = mover(mi);
+    TRY_R(motion_tangent(b, L.phase_angle, L.freq, cfg->deltat, tot0, ita0, ita0 + n_steps, tan[(size_t)mi]));
+    first[(size_t)mi] = b->motion.init_ita;
+    if (ita0 < first[(size_t)mi]) return fail(BCFD_E_STATE);
+  }
   // per-block adjoint buffers
   std::vector<AdjBlock> AB(nb);
   for (int q = 0; q < nb; ++q) {
@@ -1095,11 +1127,12 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
         !a.fc.coef || !a.fc.kc || !a.fc.gk)
       return fail(BCFD_E_NOMEM);
     TRY_R(alloc_ts_adj(a, mem));
-    if (q == hidx) {
+    if (a.hb->motion.on) {
+      const size_t ne_q = (size_t)a.hb->d.ne;
       a.fc.elem = mem.get<int>(ntask);
-      a.fc.ge = mem.get<double>(7 * (size_t)ne);
+      a.fc.ge = mem.get<double>(7 * ne_q);
       if (!a.fc.elem || !a.fc.ge) return fail(BCFD_E_NOMEM);
-      ACK(cudaMemsetAsync(a.fc.ge, 0, 7 * (size_t)ne * sizeof(double), stream()));
+      ACK(cudaMemsetAsync(a.fc.ge, 0, 7 * ne_q * sizeof(double), stream()));
     }
     ACK(cudaMemsetAsync(a.A, 0, kStateFields * a.np * sizeof(double), stream()));
     ACK(cudaMemsetAsync(a.ucl, 0, (size_t)a.hb->d.d.ny * a.hb->d.d.nz * sizeof(double), stream()));
@@ -1137,25 +1170,36 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
   // the same step): field weights, drag/lift weights, their geometric and
   // kinematic partials, each with the time average's 1/N
   const double wn = 1.0 / (double)n_steps;
+  int ne_max = 0, nn_max = 0;
+  for (int mi = 0; mi < nmov; ++mi) {
+    ne_max = std::max(ne_max, mover(mi)->d.ne);
+    nn_max = std::max(nn_max, mover(mi)->d.nn);
+  }
   double* sd = mem.get<double>(4);
   double* sdw = mem.get<double>(4);
   double* ss = mem.get<double>(8 + (size_t)std::max(64, kKinScalars) * ne);
-  double* gscr = mem.get<double>(9 * (size_t)ne + 4 * (size_t)nn + 4);
-  double* pre = mem.get<double>(3 * (size_t)np);
-  int* csr_off = mem.get<int>((size_t)nn + 1);
-  if (!sd || !sdw || !ss || !gscr || !pre || !csr_off) return fail(BCFD_E_NOMEM);
+  double* gscr = mem.get<double>(9 * (size_t)ne_max + 4 * (size_t)nn_max + 4);
+  if (!sd || !sdw || !ss || !gscr) return fail(BCFD_E_NOMEM);
+  // per moving body: the recorder's scratch and the node -> element CSR
+  std::vector<double*> pre((size_t)nmov);
+  std::vector<int*> csr_off((size_t)nmov), csr_ent((size_t)nmov);
+  for (int mi = 0; mi < nmov; ++mi) {
+    HostBlock* b = mover(mi);
+    pre[(size_t)mi] = mem.get<double>(3 * (size_t)b->d.d.npts());
+    std::vector<int> hoff, hent;
+    TRY_R(build_node_csr(b, hoff, hent));
+    csr_off[(size_t)mi] = mem.get<int>(hoff.size());
+    csr_ent[(size_t)mi] = mem.get<int>(std::max<size_t>(hent.size(), 1));
+    if (!pre[(size_t)mi] || !csr_off[(size_t)mi] || !csr_ent[(size_t)mi]) return fail(BCFD_E_NOMEM);
+    ACK(h2d(csr_off[(size_t)mi], hoff.data(), hoff.size() * sizeof(int)));
+    if (!hent.empty()) ACK(h2d(csr_ent[(size_t)mi], hent.data(), hent.size() * sizeof(int)));
+  }
   if (use_stress) {
     double sw[4];
     for (int t = 0; t < 4; ++t) sw[t] = stress_seed[t] * wn;
     ACK(h2d(sd, stress_seed, 4 * sizeof(double)));
     ACK(h2d(sdw, sw, 4 * sizeof(double)));
   }
-  std::vector<int> hoff, hent;
-  TRY_R(build_node_csr(hb, hoff, hent));
-  int* csr_ent = mem.get<int>(std::max<size_t>(hent.size(), 1));
-  if (!csr_ent) return fail(BCFD_E_NOMEM);
-  ACK(h2d(csr_off, hoff.data(), hoff.size() * sizeof(int)));
-  ACK(h2d(csr_ent, hent.data(), hent.size() * sizeof(int)));
   auto objective = [&]() -> int {
     k_axpy<<<grid_for(4 * np, 256), 256, 0, stream()>>>(W, wn, ah.A, 4 * np);
     BCFD_LAUNCHED();
@@ -1166,64 +1210,82 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
     }
     return 0;
   };
-  // the geometry and kinematics of driver step `st` (the body's current
-  // state, placed by P) are complete: their adjoints go to the parameters
+  // the geometry and kinematics of driver step `st` (each moving body's
+  // current state, placed by its Place) are complete: their adjoints go to
+  // the parameters.  The objective's body contributes to all five; another
+  // moving body only to those it shares (the pitch phase angle and
+  // frequency), its own amplitudes and heave frequency being other parameters.
   double dmot[kMotionParams] = {0, 0, 0, 0, 0};
-  auto flush = [&](int64_t st, const Place& P) -> int {
-    double pb[4], gk[kKinScalars];
-    TRY_R(launch_geometry_place_adj(hb, ah.fc.ge, csr_off, csr_ent, P, gscr, pb));
-    ACK(d2h(gk, ah.fc.gk, kKinScalars * sizeof(double)));
-    const StepTangent& T = tan[(size_t)(st - first)];
-    for (int q = 0; q < kMotionParams; ++q) {
-      double v = pb[0] * T.angle[q] + pb[2] * T.ty[q];
-      for (int p = 0; p < kKinScalars; ++p) v += gk[p] * T.kin[p][q];
-      dmot[q] += v;
+  auto flush = [&](int64_t st, const std::vector<const Place*>& P) -> int {
+    for (int mi = 0; mi < nmov; ++mi) {
+      const int q0 = movers[(size_t)mi];
+      HostBlock* b = all[(size_t)q0].second;
+      AdjBlock& a = AB[(size_t)q0];
+      double pb[4], gk[kKinScalars];
+      TRY_R(launch_geometry_place_adj(b, a.fc.ge, csr_off[(size_t)mi], csr_ent[(size_t)mi], *P[(size_t)mi], gscr,
+                                      pb));
+      ACK(d2h(gk, a.fc.gk, kKinScalars * sizeof(double)));
+      const StepTangent& T = tan[(size_t)mi][(size_t)(st - first[(size_t)mi])];
+      for (int q = 0; q < kMotionParams; ++q) {
+        if (q0 != hidx && q != 2 && q != 3) continue;
+        double v = pb[0] * T.angle[q] + pb[2] * T.ty[q];
+        for (int p = 0; p < kKinScalars; ++p) v += gk[p] * T.kin[p][q];
+        dmot[q] += v;
+      }
+      ACK(cudaMemsetAsync(a.fc.ge, 0, 7 * (size_t)b->d.ne * sizeof(double), stream()));
+      ACK(cudaMemsetAsync(a.fc.gk, 0, kKinScalars * sizeof(double), stream()));
     }
-    ACK(cudaMemsetAsync(ah.fc.ge, 0, 7 * (size_t)ne * sizeof(double), stream()));
-    ACK(cudaMemsetAsync(ah.fc.gk, 0, kKinScalars * sizeof(double), stream()));
     return 0;
   };
   double* tape = mem.get<double>((size_t)K * S);
   if (!tape) return fail(BCFD_E_NOMEM);
   TRY_R(objective());  // at x^N with the end geometry (the blocks' state now)
   MoveRecorder rec;
-  rec.body = hb;
+  for (int mi = 0; mi < nmov; ++mi) rec.bodies.push_back(mover(mi));
+  rec.cur.assign((size_t)nmov, nullptr);
   rec.sc = pre;
   std::vector<StepGeo> geo((size_t)nb);
+  std::vector<const Place*> places((size_t)nmov);
   for (int64_t m = ncp - 1; m >= 0; --m) {
     const int64_t n0 = m * K, n1 = std::min(n0 + K, n_steps);
     const double* cp = cps + (size_t)m * S;
     ACK(cudaMemcpyAsync(tape, cp, S * sizeof(double), cudaMemcpyDeviceToDevice, stream()));
     TRY_R(load_all(cp));
-    TRY_R(restore_body(hb, cprec[(size_t)m]));
+    for (int mi = 0; mi < nmov; ++mi) TRY_R(restore_body(mover(mi), cprec[(size_t)mi][(size_t)m]));
     TRY_R(ghosts_at(n0));
     L.ita = ita0 + n0;
     L.totime = tot0 + n0 * cfg->deltat;
     DevMem seg;
-    std::vector<BodyRec> recs((size_t)(n1 - n0 + 1));
+    std::vector<std::vector<BodyRec>> recs((size_t)nmov, std::vector<BodyRec>((size_t)(n1 - n0 + 1)));
     rec.mem = &seg;
     L.recorder = &rec;
     int r = 0;
     for (int64_t n = n0 + 1; n <= n1 && !r; ++n) {
-      rec.cur = &recs[(size_t)(n - n0)];
+      for (int mi = 0; mi < nmov; ++mi) rec.cur[(size_t)mi] = &recs[(size_t)mi][(size_t)(n - n0)];
       r = run_one_step(c);
-      if (!r) r = save_body(hb, recs[(size_t)(n - n0)], seg);
+      if (!r) r = save_bodies(recs.data(), (size_t)(n - n0), seg);
       if (!r && n < n1) r = save_all(tape + (size_t)(n - n0) * S);
     }
     L.recorder = nullptr;
-    rec.cur = nullptr;
+    rec.cur.assign((size_t)nmov, nullptr);
     if (r) return fail(r);
     if (rec.oom) return fail(BCFD_E_NOMEM);
     for (int64_t n = n1; n > n0; --n) {
-      const BodyRec& re = recs[(size_t)(n - n0)];
-      for (int k2 = 0; k2 < kCalls; ++k2) geo[(size_t)hidx].geo[k2] = re.geo[k2];
-      // after the body moved: the step's end geometry and kinematics
-      TRY_R(restore_body(hb, re));
+      for (int mi = 0; mi < nmov; ++mi) {
+        const BodyRec& re = recs[(size_t)mi][(size_t)(n - n0)];
+        for (int k2 = 0; k2 < kCalls; ++k2) geo[(size_t)movers[(size_t)mi]].geo[k2] = re.geo[k2];
+        // after the bodies moved: the step's end geometry and kinematics
+        TRY_R(restore_body(mover(mi), re));
+        places[(size_t)mi] = &re.stage.place;
+      }
       TRY_R(adjoint_step_second(AB, &geo));
-      TRY_R(flush(ita0 + n, re.stage.place));
+      TRY_R(flush(ita0 + n, places));
       // before: the geometry, kinematics and state the step started from
-      const BodyRec& rs = (n - 1 == n0) ? cprec[(size_t)m] : recs[(size_t)(n - 1 - n0)];
-      TRY_R(restore_body(hb, rs));
+      for (int mi = 0; mi < nmov; ++mi) {
+        const BodyRec& rs =
+            (n - 1 == n0) ? cprec[(size_t)mi][(size_t)m] : recs[(size_t)mi][(size_t)(n - 1 - n0)];
+        TRY_R(restore_body(mover(mi), rs));
+      }
       TRY_R(load_all(tape + (size_t)(n - 1 - n0) * S));
       TRY_R(ghosts_at(n - 1));
       TRY_R(adjoint_step_first(AB, M, c, adj_tol, adj_itmax, &geo));
@@ -1231,10 +1293,11 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
     }
   }
   // the run's start: its geometry and kinematics
-  TRY_R(flush(ita0, cprec[0].stage.place));
+  for (int mi = 0; mi < nmov; ++mi) places[(size_t)mi] = &cprec[(size_t)mi][0].stage.place;
+  TRY_R(flush(ita0, places));
   // leave the blocks at the forward run's final state
   TRY_R(load_all(fin));
-  TRY_R(restore_body(hb, finrec));
+  for (int mi = 0; mi < nmov; ++mi) TRY_R(restore_body(mover(mi), finrec[(size_t)mi]));
   TRY_R(ghosts_at(n_steps));
   L.ita = ita0 + n_steps;
   L.totime = tot0 + n_steps * cfg->deltat;

@@ -1352,7 +1352,7 @@ int bcfd_block_get_solve_launch(bcfd_handle h, int* out) {
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant) {
   LOCK();
   GETB(h);
-  if (inner_sweeps < 0 || inner_sweeps > 100000 || omega < 0.0 || omega >= 2.0 || variant < 0 || variant > 4 ||
+  if (inner_sweeps < 0 || inner_sweeps > 100000 || omega < 0.0 || omega >= 2.0 || variant < 0 || variant > 5 ||
       variant == 2)  // the cluster-resident variant was withdrawn
     return BCFD_E_ARG;
   hb->dc_inner = (int)inner_sweeps;
@@ -1412,6 +1412,11 @@ int bcfd_profile_end(bcfd_profile_report* out) {
     out->sor_sweeps += e[4 * q];
     if (e[4 * q + 3] == 0) {
       out->sor_bytes += sw * fl * 33.0;  // 4w + 1, w = 8
+    } else if (e[4 * q + 3] == 2) {
+      // z-marching sweeps: one pass per two sweep pairs reads e, the rhs
+      // and the mask once and writes e once (4 + 4 + 1 + 4 B); the FP64
+      // residual and update passes as below
+      out->sor_bytes += 0.5 * sw * fl * 13.0 + rp * fl * 29.0 + (rp - 1.0) * fl * 25.0;
     } else {
       // FP32 sweeps 4w + 1 (w = 4); FP64 residual: pc own + neighbours + b/dt
       // read, r written as FP32, mask (8+8+8+4+1); update x += e: pc r/w,

@@ -5,7 +5,10 @@
 // and the phase synchronisation (grid barrier or neighbour tiles).  None of
 // these changes the arithmetic, so the tuned solver computes exactly what the
 // untuned one does.  The block's solve state is saved before the trials and
-// restored after them; results are cached per block shape.
+// restored after them; results are cached per block shape.  A block whose
+// solves run side by side with other blocks' in one batched launch keeps
+// that launch unless the z-marching TMA sweeps (variant 5, a launch of its
+// own) beat the default shape on it.
 #include <cstring>
 #include <map>
 #include <tuple>
@@ -16,13 +19,14 @@ namespace bcfd {
 namespace {
 
 struct Shape {
-  int threads, ctas_per_sm, sync;  // sync: FP64 0 neighbour / 1 grid; FP32 variant 1 grid / 3 neighbour
+  int threads, ctas_per_sm, sync;  // sync: FP64 0 neighbour / 1 grid; FP32 variant 1 grid / 3 neighbour,
+                                   // 4 temporal-blocked, 5 z-marching TMA
 };
 struct Tuned {
   Shape fp64, fp32;
 };
-std::map<std::tuple<int, int, int>, Tuned>& cache() {
-  static std::map<std::tuple<int, int, int>, Tuned> c;
+std::map<std::tuple<int, int, int, int>, Tuned>& cache() {
+  static std::map<std::tuple<int, int, int, int>, Tuned> c;
   return c;
 }
 
@@ -100,12 +104,15 @@ void apply(HostBlock* hb, const Shape& s, bool fp32) {
   }
 }
 
-int tune_block(HostBlock* hb, Tuned* out) {
+// batched: only the default FP32 shape against the z-marching sweeps
+int tune_block(HostBlock* hb, Tuned* out, bool batched) {
   static const Shape c64[] = {{256, 0, 0}, {512, 0, 0}, {256, 0, 1}, {512, 0, 1}, {512, 1, 0}};
   // {256, 4, *} selects the 64-register instantiation of the FP32 solve
   // {512, 0, 4}: the temporal-blocked sweeps (small blocks)
-  static const Shape c32[] = {{128, 0, 1}, {256, 0, 1}, {128, 0, 3}, {256, 0, 3},
-                              {256, 2, 1}, {256, 1, 1}, {256, 4, 1}, {256, 4, 3}, {512, 0, 4}};
+  // {384, 0, 5}: the z-marching TMA sweeps (large blocks)
+  static const Shape c32[] = {{128, 0, 1}, {256, 0, 1}, {128, 0, 3}, {256, 0, 3}, {256, 2, 1},
+                              {256, 1, 1}, {256, 4, 1}, {256, 4, 3}, {512, 0, 4}, {384, 0, 5}};
+  static const Shape c32b[] = {{256, 0, 1}, {384, 0, 5}};
   Saved sv;
   TRY_R(save_state(hb, sv, false));
   const int t0 = hb->solve_threads, c0 = hb->solve_ctas_per_sm, s0 = hb->solve_sync, v0 = hb->dc_variant,
@@ -114,15 +121,19 @@ int tune_block(HostBlock* hb, Tuned* out) {
   float best = 1e30f;
   Shape b64 = c64[0], b32 = c32[0];
   for (const Shape& s : c64) {
+    if (batched) break;
     apply(hb, s, false);
     float ms = 0;
     if ((r = time_trial(hb, false, 5, &ms))) break;
     if (ms < best) best = ms, b64 = s;
   }
   best = 1e30f;
-  for (const Shape& s : c32) {
+  const size_t n32 = batched ? sizeof(c32b) / sizeof(c32b[0]) : sizeof(c32) / sizeof(c32[0]);
+  for (size_t q = 0; q < n32; ++q) {
+    const Shape& s = batched ? c32b[q] : c32[q];
     if (r) break;
     if (s.sync == 4 && !tb_solve_fits(hb)) continue;
+    if (s.sync == 5 && !zm_solve_fits(hb)) continue;
     apply(hb, s, true);
     float ms = 0;
     if ((r = time_trial(hb, true, 16, &ms))) break;
@@ -161,17 +172,23 @@ extern "C" int bcfd_autotune(int64_t* n_tuned) {
   for (size_t q = 0; q < lib().blocks.size(); ++q) {
     HostBlock* hb = lib().blocks[q];
     if (!hb || !hb->d.Acx || !hb->d.Acxf) continue;
-    if (q > 0 && lib().batch && others > 1) continue;
+    const bool batched = q > 0 && lib().batch && others > 1;
+    if (batched && !zm_solve_fits(hb)) continue;
     const Dims& d = hb->d.d;
-    const auto key = std::make_tuple(d.nx, d.ny, d.nz);
+    const auto key = std::make_tuple(d.nx, d.ny, d.nz, batched ? 1 : 0);
     auto it = cache().find(key);
     Tuned t;
     if (it != cache().end()) {
       t = it->second;
     } else {
-      TRY_R(tune_block(hb, &t));
+      TRY_R(tune_block(hb, &t, batched));
       cache()[key] = t;
       ++n;
+    }
+    if (batched) {
+      // leaves the batched launch only for the z-marching sweeps
+      if (t.fp32.sync == 5) apply(hb, t.fp32, true);
+      continue;
     }
     apply(hb, t.fp64, false);
     apply(hb, t.fp32, true);

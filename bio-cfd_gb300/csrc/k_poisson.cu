@@ -11,6 +11,9 @@
 // the new red values -- exactly an in-place red-black sweep on one array, so
 // no pco array and no copy exist here.  The stop test max|pc - pco| over the
 // fluid cells is the max of |new - old| of both half-sweeps, fused into them.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
 #include "bcfd_host.h"
 
 namespace bcfd {
@@ -886,6 +889,380 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_sor_tb(DevBlock B, DcArgs a, 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Z-marching two-pair FP32 sweeps (variant 5): TMA-fed temporal blocking for
+// blocks far larger than L2.  One pass applies four half-sweeps (two sweep
+// pairs) while reading the correction from HBM once: each CTA owns a tile of
+// rows j0..j0+nj-1 (every h of both colours) and planes k0..k0+nk-1, and
+// marches through its planes with the four half-sweeps skewed by one plane
+// each (level L = 1..4 at step k works on plane k-L+1; levels 1 and 3 red,
+// 2 and 4 black).  The planes in use (k-4 .. k+1) and the one in flight
+// (k+2) sit in a ring of seven shared-memory slots, each the plane's rows
+// j0-4 .. j0+nj+3 of both colours, filled by two cp.async.bulk.tensor loads
+// (TMA) completing on the slot's mbarrier; the tile's rows are recomputed up
+// to four rows (and planes) beyond the tile with exactly the operations of
+// the owning CTA, so every cell receives the values of four plain
+// half-sweeps, bit for bit.  A pass reads one buffer and writes the tile's
+// rows of the other (ping-pong), so no CTA's writes race with a neighbour's
+// halo reads; passes are separated by the grid barrier.  The right-hand side
+// and the masks are pulled into L2 two steps ahead (bulk prefetches) and
+// into registers at the start of each step, all four levels' at once, so
+// their latencies overlap.  HBM traffic per cell and pass: e 4 B read + 4 B written, rhs 4 B
+// and mask 1 B read -- 13 B for two sweep pairs, against 34 B for two plain
+// pairs.
+// ---------------------------------------------------------------------------
+constexpr int kZmThreads = 384;
+constexpr int kZmSlots = 7;
+constexpr int kZmHalo = 4;
+constexpr int kZmGuard = 128;  // bytes before and after the ring
+
+struct ZmArgs {
+  int tj, ntj, tk, nzs;  // rows per tile along j, tiles along j; planes per tile along k, tiles along k
+  int rows;              // rows of a staged plane (tj + 2 * kZmHalo), the TMA box height
+  int slot_floats;       // floats of one colour of one staged plane (a multiple of 32)
+  float* e2;             // the second correction buffer: colour c at e2 + c * npacked
+};
+
+// the tensor maps of the four correction arrays: [buffer * 2 + colour]
+struct ZmMaps {
+  CUtensorMap m[4];
+};
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait for a slot's load; false once the limit passed
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, unsigned long long limit_ns) {
+  if (mbar_try_wait(bar, parity)) return true;
+  const unsigned long long t0 = globaltimer_ns();
+  while (!mbar_try_wait(bar, parity))
+    if (globaltimer_ns() - t0 > limit_ns) return false;
+  return true;
+}
+// rows [y, y + box) of plane z of a packed colour array into shared memory
+__device__ __forceinline__ void tma_load_plane(float* dst, const CUtensorMap* map, int y, int z, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(0), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_shared() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
+struct ZmRing {
+  float* base;      // slot 0, colour 0
+  int slot_floats;  // per colour
+  int jrow0;        // j of a slot's row 0
+  unsigned pbits;   // expected mbarrier parity per slot
+  uint64_t* bars;
+  __device__ __forceinline__ static int slot(int p) { return (p + 4 * kZmSlots) % kZmSlots; }
+  __device__ __forceinline__ float* at(int p, int c) const {
+    return base + (size_t)(2 * slot(p) + c) * slot_floats;
+  }
+};
+
+// the rows and runs of one level at one step (clamped to the interior)
+struct ZmSpan {
+  int p, ja, n;  // plane, first row, runs (rows x NXH/4); n = 0: nothing to do
+};
+
+__device__ __forceinline__ ZmSpan zm_span(const Dims& d, int p, int ja, int jb, bool on) {
+  ZmSpan z;
+  z.p = p;
+  z.ja = max(ja, 2);
+  jb = min(jb, d.ny + 1);
+  z.n = (on && p >= 2 && p <= d.nz + 1 && z.ja <= jb) ? (jb - z.ja + 1) * (d.NXH >> 2) : 0;
+  return z;
+}
+
+// the right-hand side and masks of this thread's runs of one level (at most
+// kZmRuns runs per thread: the tiling guarantees it), loaded into registers
+// before the step's barrier waits so that all their latencies overlap
+constexpr int kZmRuns = 2;
+template <int C>
+__device__ __forceinline__ void zm_fetch(const DevBlock& B, const ZmSpan& z, float4 (&r)[kZmRuns],
+                                         uchar4 (&m)[kZmRuns]) {
+  const Dims& d = B.d;
+  const int nq = d.NXH >> 2;
+  const int64_t gz = (int64_t)d.NXH * d.NY * (z.p - 1);
+#pragma unroll
+  for (int u = 0; u < kZmRuns; ++u) {
+    const int q = threadIdx.x + u * blockDim.x;
+    if (q < z.n) {
+      const int a = q % nq, j = z.ja + q / nq;
+      const int64_t pi = gz + (int64_t)d.NXH * (j - 1) + 4 * a;
+      r[u] = __ldg(reinterpret_cast<const float4*>(B.rhsf[C] + pi));
+      m[u] = *reinterpret_cast<const uchar4*>(B.upd[C] + pi);
+    }
+  }
+}
+
+// one half-sweep of colour C on the level's rows of plane z.p: the arithmetic
+// of tile_half32 with the correction read from the ring and the right-hand
+// side and masks from registers
+template <int C>
+__device__ __forceinline__ void zm_level(const DevBlock& B, const ZmRing& R, const ZmSpan& z,
+                                         const float4 (&rr)[kZmRuns], const uchar4 (&mm)[kZmRuns], float omega) {
+  const Dims& d = B.d;
+  const int nq = d.NXH >> 2;
+  const int p = z.p;
+  const float* __restrict__ om = R.at(p - 1, 1 - C);
+  const float* __restrict__ oc = R.at(p, 1 - C);
+  const float* __restrict__ op = R.at(p + 1, 1 - C);
+  float* __restrict__ own = R.at(p, C);
+  const int sy = d.NXH;
+#pragma unroll
+  for (int uu = 0; uu < kZmRuns; ++uu) {
+    const int q = threadIdx.x + uu * blockDim.x;
+    if (q >= z.n) break;
+    const int a = q % nq, j = z.ja + q / nq;
+    const int so = (j - R.jrow0) * sy + 4 * a;
+    const uchar4 m = mm[uu];
+    const float4 r4 = rr[uu];
+    const int par = ((1 + j + p) & 1) != C;
+    const float4 c0 = *reinterpret_cast<const float4*>(oc + so);
+    const float4 os = *reinterpret_cast<const float4*>(oc + so - sy);
+    const float4 on = *reinterpret_cast<const float4*>(oc + so + sy);
+    const float4 ob = *reinterpret_cast<const float4*>(om + so);
+    const float4 ot = *reinterpret_cast<const float4*>(op + so);
+    const float4 e4 = *reinterpret_cast<const float4*>(own + so);
+    const float ox = par ? oc[so + 4] : oc[so - 1];
+    const float4 cy = B.ayr[j - 2], cz = B.azr[p - 2];
+    const float ay1 = cy.x, ay2 = cy.y, ay3 = cy.z;
+    const float az1 = cz.x, az2 = cz.y, az3 = cz.z;
+    const float4* __restrict__ ar = B.axr + (int64_t)(3 * par) * nq + a;
+    const float4 c1 = ar[0], c2 = ar[nq], c3 = ar[2 * nq];
+    const float axv1[4] = {c1.x, c1.y, c1.z, c1.w}, axv2[4] = {c2.x, c2.y, c2.z, c2.w},
+                axv3[4] = {c3.x, c3.y, c3.z, c3.w};
+    const float oxs[6] = {par ? c0.x : ox, c0.x, c0.y, c0.z, c0.w, par ? ox : c0.w};
+    const float sv[4] = {os.x, os.y, os.z, os.w}, nv4[4] = {on.x, on.y, on.z, on.w};
+    const float bv[4] = {ob.x, ob.y, ob.z, ob.w}, tv[4] = {ot.x, ot.y, ot.z, ot.w};
+    const float rv[4] = {r4.x, r4.y, r4.z, r4.w};
+    float ev[4] = {e4.x, e4.y, e4.z, e4.w};
+    const unsigned char mv[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const float left = par ? oxs[u + 1] : oxs[u];
+      const float right = par ? oxs[u + 2] : oxs[u + 1];
+      const float ax1 = axv1[u], ax2 = axv2[u], ax3 = axv3[u];
+      float sm = rv[u];
+      sm = __fmaf_rn(-ax1, left, sm);
+      sm = __fmaf_rn(-ax3, right, sm);
+      sm = __fmaf_rn(-ay1, sv[u], sm);
+      sm = __fmaf_rn(-ay3, nv4[u], sm);
+      sm = __fmaf_rn(-az1, bv[u], sm);
+      sm = __fmaf_rn(-az3, tv[u], sm);
+      const float nvv = __fmaf_rn(omega, __fdividef(sm, ax2 + ay2 + az2) - ev[u], ev[u]);
+      ev[u] = mv[u] ? nvv : ev[u];
+    }
+    *reinterpret_cast<float4*>(own + so) = make_float4(ev[0], ev[1], ev[2], ev[3]);
+  }
+}
+
+// pull rows ja..jb of plane p of colour C's right-hand side and mask into L2
+// (bulk prefetches on the copy engine; the byte range is trimmed inward to
+// 16-byte boundaries so it never leaves the arrays)
+__device__ __forceinline__ void zm_prefetch_l2(const DevBlock& B, int C, const ZmSpan& z) {
+  if (z.n <= 0) return;
+  const Dims& d = B.d;
+  const int rows = z.n / (d.NXH >> 2);
+  const int64_t pi = (int64_t)d.NXH * d.NY * (z.p - 1) + (int64_t)d.NXH * (z.ja - 1);
+  const char* ranges[2] = {reinterpret_cast<const char*>(B.rhsf[C] + pi),
+                           reinterpret_cast<const char*>(B.upd[C] + pi)};
+  const int64_t bytes[2] = {(int64_t)rows * d.NXH * 4, (int64_t)rows * d.NXH};
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const uintptr_t a0 = reinterpret_cast<uintptr_t>(ranges[q]);
+    const uintptr_t lo = (a0 + 15) & ~(uintptr_t)15, hi = (a0 + (uintptr_t)bytes[q]) & ~(uintptr_t)15;
+    if (hi > lo)
+      asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(lo), "r"((unsigned)(hi - lo)) : "memory");
+  }
+}
+
+// the tile's rows of plane p (both colours) from the ring to E
+__device__ __forceinline__ void zm_writeout(const DevBlock& B, const ZmRing& R, const Tile& t, int p,
+                                            float* const E[2]) {
+  const Dims& d = B.d;
+  const int nq = d.NXH >> 2;
+  const int per = t.nj * nq, n = 2 * per;
+  const int64_t gz = (int64_t)d.NXH * d.NY * (p - 1);
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int c = q / per, rem = q - c * per;
+    const int a = rem % nq, j = t.j0 + rem / nq;
+    const float4 v = *reinterpret_cast<const float4*>(R.at(p, c) + (j - R.jrow0) * d.NXH + 4 * a);
+    *reinterpret_cast<float4*>(E[c] + gz + (int64_t)d.NXH * (j - 1) + 4 * a) = v;
+  }
+}
+
+// One pass of `nlev` (4, or 2 for an odd final pair) half-sweeps over the
+// tile, reading buffer `cur` through the tensor maps and writing the tile's
+// rows of the other buffer.  false (on every thread) once a load wait gave up.
+__device__ bool zm_pass(const DevBlock& B, const ZmArgs& z, const ZmMaps& maps, ZmRing& R, const Tile& t, int cur,
+                        int nlev, float omega, float* const Eout[2], unsigned long long limit_ns) {
+  const CUtensorMap* m0 = &maps.m[2 * cur];
+  const CUtensorMap* m1 = &maps.m[2 * cur + 1];
+  const int y0 = R.jrow0 - 1;  // 0-based row of a slot's row 0
+  const int k1 = t.k0 + t.nk - 1;
+  const int kb = t.k0 - nlev, ke = k1 + nlev;            // planes loaded
+  const int ks = t.k0 - (nlev - 1), kf = k1 + (nlev - 1);  // steps
+  const unsigned bytes = 2u * (unsigned)z.rows * (unsigned)B.d.NXH * 4u;
+  auto issue = [&](int p) {
+    if (threadIdx.x == 0) {
+      uint64_t* bar = R.bars + ZmRing::slot(p);
+      fence_proxy_async_shared();
+      mbar_expect_tx(bar, bytes);
+      tma_load_plane(R.at(p, 0), m0, y0, p - 1, bar);
+      tma_load_plane(R.at(p, 1), m1, y0, p - 1, bar);
+    }
+  };
+  bool ok = true;
+  auto wait = [&](int p) {
+    const int s = ZmRing::slot(p);
+    ok = mbar_wait(R.bars + s, (R.pbits >> s) & 1u, limit_ns) && ok;
+    R.pbits ^= 1u << s;
+  };
+  auto span = [&](int k, int L) {
+    const int sp = nlev - L;  // rows and planes beyond the tile at this level
+    const int p = k - L + 1;
+    return zm_span(B.d, p, t.j0 - sp, t.j0 + t.nj - 1 + sp, L <= nlev && p >= t.k0 - sp && p <= k1 + sp);
+  };
+  issue(kb);
+  issue(kb + 1);
+  issue(kb + 2);
+  for (int k = ks; k <= kf; ++k) {
+    if (k + 2 <= ke) issue(k + 2);
+    if (threadIdx.x == 32) {
+      // the right-hand side rows that levels 1 and 2 first touch two steps on
+      zm_prefetch_l2(B, 1, span(k + 2, 1));
+      zm_prefetch_l2(B, 0, span(k + 2, 2));
+    }
+    const ZmSpan z1 = span(k, 1), z2 = span(k, 2), z3 = span(k, 3), z4 = span(k, 4);
+    float4 r1[kZmRuns], r2[kZmRuns], r3[kZmRuns], r4[kZmRuns];
+    uchar4 m1[kZmRuns], m2[kZmRuns], m3[kZmRuns], m4[kZmRuns];
+    zm_fetch<1>(B, z1, r1, m1);
+    zm_fetch<0>(B, z2, r2, m2);
+    zm_fetch<1>(B, z3, r3, m3);
+    zm_fetch<0>(B, z4, r4, m4);
+    if (k == ks) {
+      wait(kb);
+      wait(kb + 1);
+    }
+    wait(k + 1);
+    zm_level<1>(B, R, z1, r1, m1, omega);
+    if (__syncthreads_or(!ok)) return false;
+    zm_level<0>(B, R, z2, r2, m2, omega);
+    __syncthreads();
+    if (nlev == 4) {
+      zm_level<1>(B, R, z3, r3, m3, omega);
+      __syncthreads();
+      zm_level<0>(B, R, z4, r4, m4, omega);
+      __syncthreads();
+    }
+    const int pw = k - (nlev - 1);
+    if (pw >= t.k0 && pw <= k1) zm_writeout(B, R, t, pw, Eout);
+  }
+  return true;
+}
+
+__global__ void __launch_bounds__(kZmThreads, 1) k_sor_zm(DevBlock B, DcArgs a, GridBar gb, ZmArgs z,
+                                                          const __grid_constant__ ZmMaps maps) {
+  extern __shared__ __align__(128) unsigned char zm_raw[];
+  __shared__ __align__(8) uint64_t bars[kZmSlots];
+  __shared__ double sh[32];
+  const int cta = (int)blockIdx.x;
+  Tile t;
+  t.a = cta % z.ntj;
+  t.b = cta / z.ntj;
+  t.j0 = 2 + t.a * z.tj;
+  t.k0 = 2 + t.b * z.tk;
+  t.nj = min(z.tj, B.d.ny + 2 - t.j0);
+  t.nk = min(z.tk, B.d.nz + 2 - t.k0);
+  ZmRing R;
+  // the ring starts 128-byte aligned in shared memory, after a guard
+  const unsigned pad = (128u - (smem_u32(zm_raw) & 127u)) & 127u;
+  R.base = reinterpret_cast<float*>(zm_raw + pad + kZmGuard);
+  R.slot_floats = z.slot_floats;
+  R.jrow0 = t.j0 - kZmHalo;
+  R.pbits = 0;
+  R.bars = bars;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kZmSlots; ++s) mbar_init(bars + s);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    fence_proxy_async_shared();
+  }
+  __syncthreads();
+  const int64_t np = B.d.npacked();
+  float* const E0[2] = {B.pcf[0], B.pcf[1]};
+  float* const E1[2] = {z.e2, z.e2 + np};
+  BlockStats* st = B.stats;
+  int64_t sweeps = 0;
+  double res = 0.0;
+  int outer = 0;
+  for (;; ++outer) {
+    double m = nmax(tile_residual64v<1>(B, t, a.inv_dt), tile_residual64v<0>(B, t, a.inv_dt));
+    fence_proxy_async_global();
+    m = block_max(m, sh);
+    if (threadIdx.x == 0) atomic_max_nonneg(&st->slot[outer % 3], m);
+    if (!grid_sync(gb)) return;
+    res = take_slot(st, outer, cta);
+    if (a.dt * res <= a.div_tol || outer >= a.max_outer || non_finite(res)) break;
+    const int passes = (a.inner + 1) / 2;
+    int cur = 0;
+    for (int ps = 0; ps < passes; ++ps) {
+      const int nlev = (ps == passes - 1 && (a.inner & 1)) ? 2 : 4;
+      if (!zm_pass(B, z, maps, R, t, cur, nlev, a.omega, cur ? E0 : E1, gb.limit_ns)) {
+        if (threadIdx.x == 0) {
+          atomicCAS(gb.err, 0, BCFD_E_TIMEOUT);
+          atomicOr(gb.ctr, kBarAbandon);
+        }
+        return;
+      }
+      fence_proxy_async_global();
+      cur ^= 1;
+      if (!grid_sync(gb)) return;
+    }
+    sweeps += a.inner;
+    if (cur) {
+      const float* e1c[2] = {E1[0], E1[1]};
+      tb_copy_back(B, t, e1c);
+      __syncthreads();
+    }
+    tile_apply4<1>(B, t);
+    tile_apply4<0>(B, t);
+    fence_proxy_async_global();
+    if (!grid_sync(gb)) return;
+  }
+  if (cta == 0 && threadIdx.x == 0) {
+    log_solve(a.log, sweeps, outer + 1, B.cnt[C_FLUID], 2);
+    st->niter = st->niter + sweeps;
+    st->derr2 = a.dt * res;
+    st->pad[1] = a.dt * res;
+    if (non_finite(res)) set_err(B.err, BCFD_E_NONFINITE);
+  }
+}
+
 // Several blocks' solves in one cooperative launch: member m owns CTAs
 // [cta0, cta0 + its tile count) and has its own barrier, tiles and slots.
 constexpr int kMaxSolveBatch = 16;
@@ -1250,12 +1627,149 @@ static int launch_sor_tb(HostBlock* hb, int64_t itmax, double dt, double div_tol
   return 0;
 }
 
+// Z-marching TMA solve (variant 5): tiles of tj rows x tk planes, one CTA of
+// kZmThreads per tile and at most one per SM (the plane ring fills most of
+// the shared memory), all co-resident.
+static size_t zm_smem_bytes(const Dims& d, int rows) {
+  const size_t slot = ((size_t)rows * d.NXH + 31) / 32 * 32;  // floats, 128-byte multiple
+  return 128 + 2 * (size_t)kZmGuard + (size_t)kZmSlots * 2 * slot * sizeof(float);
+}
+
+// the tiling with the least work per CTA: steps marched (tk + 6 for the
+// three planes before and after the tile) x rows handled per step (tj + 8
+// loaded, 4 tj + 12 computed, tj written) plus a per-step sync allowance
+// worth eight rows, among the tilings whose level-1 rows give no thread more
+// than kZmRuns runs; 0 when the block does not fit this variant (a packed
+// row wider than one TMA box, or a plane ring beyond shared memory)
+static int zm_tiles(HostBlock* hb, ZmArgs* z) {
+  const Dims& d = hb->d.d;
+  if (d.NXH > 256) return 0;
+  int smem_max = 0;
+  if (cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, lib().device) != cudaSuccess)
+    return 0;
+  const size_t cap = (size_t)smem_max - 1024;  // static shared memory of the kernel
+  const int nsm = num_sms();
+  double best = 0.0;
+  int found = 0;
+  for (int ntj = 1; ntj <= std::min(d.ny, nsm); ++ntj) {
+    const int tj = (d.ny + ntj - 1) / ntj;
+    if ((d.ny + tj - 1) / tj != ntj) continue;
+    if (zm_smem_bytes(d, tj + 2 * kZmHalo) > cap) continue;
+    // every thread holds the right-hand side of at most kZmRuns runs per level
+    if ((tj + 2 * (kZmHalo - 1)) * (d.NXH / 4) > kZmRuns * kZmThreads) continue;
+    for (int nzs = 1; nzs <= std::min(d.nz, nsm / ntj); ++nzs) {
+      const int tk = (d.nz + nzs - 1) / nzs;
+      if ((d.nz + tk - 1) / tk != nzs) continue;
+      const double cost = (double)(tk + 6) * (6.0 * tj + 28.0);
+      if (!found || cost < best) {
+        best = cost;
+        found = 1;
+        z->tj = tj;
+        z->ntj = ntj;
+        z->tk = tk;
+        z->nzs = nzs;
+      }
+    }
+  }
+  if (!found) return 0;
+  z->rows = z->tj + 2 * kZmHalo;
+  z->slot_floats = (int)(((size_t)z->rows * d.NXH + 31) / 32 * 32);
+  return 1;
+}
+
+bool zm_solve_fits(HostBlock* hb) {
+  ZmArgs z{};
+  return zm_tiles(hb, &z) != 0;
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// against the driver library)
+static PFN_cuTensorMapEncodeTiled_v12000 tmap_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// one packed colour array (NXH x NY x NZ FP32, x fastest) read in boxes of
+// `rows` full rows of one plane; rows outside the array read as zero
+static int encode_plane_map(CUtensorMap* m, const float* base, const Dims& d, int rows) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = tmap_encoder();
+  if (!fn) return BCFD_E_STATE;
+  const cuuint64_t dims[3] = {(cuuint64_t)d.NXH, (cuuint64_t)d.NY, (cuuint64_t)d.NZ};
+  const cuuint64_t strides[2] = {(cuuint64_t)d.NXH * sizeof(float), (cuuint64_t)d.NXH * d.NY * sizeof(float)};
+  const cuuint32_t box[3] = {(cuuint32_t)d.NXH, (cuuint32_t)rows, 1u};
+  const cuuint32_t estride[3] = {1u, 1u, 1u};
+  const CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float*>(base), dims, strides, box, estride,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                        CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : BCFD_E_STATE;
+}
+
+static int ensure_second_buffer(HostBlock* hb) {
+  if (hb->pcf2) return 0;
+  const int64_t np = hb->d.d.npacked();
+  void* p = nullptr;
+  if (cudaMalloc(&p, 2 * (size_t)np * sizeof(float)) != cudaSuccess) return BCFD_E_NOMEM;
+  hb->allocs.push_back(p);
+  hb->pcf2 = static_cast<float*>(p);
+  BCFD_CUDA(cudaMemsetAsync(hb->pcf2, 0, 2 * (size_t)np * sizeof(float), stream()));
+  lib().gen++;
+  return 0;
+}
+
+static int launch_sor_zm(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
+  DevBlock& B = hb->d;
+  ZmArgs z{};
+  if (!zm_tiles(hb, &z)) return BCFD_E_STATE;
+  TRY_R(ensure_second_buffer(hb));
+  z.e2 = hb->pcf2;
+  const int64_t np = B.d.npacked();
+  ZmMaps maps;
+  TRY_R(encode_plane_map(&maps.m[0], B.pcf[0], B.d, z.rows));
+  TRY_R(encode_plane_map(&maps.m[1], B.pcf[1], B.d, z.rows));
+  TRY_R(encode_plane_map(&maps.m[2], z.e2, B.d, z.rows));
+  TRY_R(encode_plane_map(&maps.m[3], z.e2 + np, B.d, z.rows));
+  TileMap tm{z.tj, z.tk, z.ntj, z.nzs, hb->prog, 1};
+  TRY_R(reset_solve_state(hb, tm));
+  const size_t smem = zm_smem_bytes(B.d, z.rows);
+  BCFD_CUDA(cudaFuncSetAttribute((const void*)k_sor_zm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const unsigned grid = (unsigned)(z.ntj * z.nzs);
+  const int nmax = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
+  DcArgs a;
+  a.inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
+  double om = hb->dc_omega > 0 ? hb->dc_omega : 2.0 / (1.0 + std::sin(3.14159265358979323846 / nmax));
+  a.omega = (float)std::min(1.97, std::max(1.0, om));
+  a.max_outer = itmax / a.inner + 1;
+  a.dt = dt;
+  a.inv_dt = 1.0 / dt;
+  a.div_tol = div_tol;
+  a.log = prof_log();
+  GridBar gb = make_bar(B.err, grid);
+  gb.ctr = reinterpret_cast<unsigned long long*>(hb->bar);
+  void* args[] = {(void*)&B, (void*)&a, (void*)&gb, (void*)&z, (void*)&maps};
+  prof_mark(true);
+  BCFD_CUDA(launch_coop((const void*)k_sor_zm, grid, kZmThreads, args, smem));
+  prof_mark(false);
+  BCFD_LAUNCHED();
+  return 0;
+}
+
 int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   DevBlock& B = hb->d;
   const int64_t np = B.d.npacked();
   const int nmax0 = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
   for (int c = 0; c < 2; ++c) BCFD_CUDA(cudaMemsetAsync(B.pcf[c], 0, np * sizeof(float), stream()));
   if (hb->dc_variant == 4 && tb_solve_fits(hb)) return launch_sor_tb(hb, itmax, dt, div_tol);
+  if (hb->dc_variant == 5 && zm_solve_fits(hb)) return launch_sor_zm(hb, itmax, dt, div_tol);
   const int threads = hb->dc_threads > 0 ? std::min(hb->dc_threads, kDcThreads) : kDcThreads;
   // variant 3: point-to-point tile sync; otherwise grid-wide phase barriers
   // four CTAs per SM asked for: the 64-register instantiation

@@ -369,13 +369,16 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
                      const double* wv, const double* ww, const double* wp, const double* stress_seed, double mu_f,
                      double rho_f, double adj_tol, int64_t adj_itmax, double* J, double* dj_duc,
                      double* dj_dkin, double* gu, double* gv, double* gw, double* gp);
-/* Discrete adjoint of n_steps whole time steps through a moving body (no
+/* Discrete adjoint of n_steps whole time steps through moving bodies (no
  * counterpart in the reference): the objective J of bcfd_adjoint_run on block
- * h, whose body is the one moving body of the run, and dj_dmotion[5] = dJ/d
- * of its motion parameters (heave amplitude yamp, pitch amplitude a0 in
- * degrees, the pitch phase angle in radians, the pitch frequency freq, the
- * heave frequency bfreq of bcfd_block_set_body_motion and
- * bcfd_set_motion_inputs), plus dJ/duc and dJ/d(u,v,w,p)^0 as there.  The
+ * h, whose body moves, and dj_dmotion[5] = dJ/d of its motion parameters
+ * (heave amplitude yamp, pitch amplitude a0 in degrees, the pitch phase angle
+ * in radians, the pitch frequency freq, the heave frequency bfreq of
+ * bcfd_block_set_body_motion and bcfd_set_motion_inputs), plus dJ/duc and
+ * dJ/d(u,v,w,p)^0 as there.  Other moving bodies of the run (a plate in
+ * tandem, with its own phase lag) move with the run and contribute to the
+ * parameters they share with block h's body -- the phase angle and the
+ * pitch frequency -- through their geometry and kinematics too.  The
  * parameters reach J through every step's node placement (rotation about x
  * through the pivot, translation), the element centroids, normals and lengths
  * (src/Search.F90:126-258), the normal distances and probe points of the IB
@@ -384,10 +387,11 @@ int bcfd_adjoint_run(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps
  * discrete choices (tags, lists, nearest elements, probe brackets, upwind
  * branches) are those of the forward run at each step.  Each segment of
  * `every` steps is recomputed from its checkpoint (fields, tags, nodes and
- * motion state).  Refused (BCFD_E_STATE): thin-surface cells (surfaces 51/52
- * of a plate) at any step, a fine-block move during the run, any other
- * moving body, precision /= 0.  The blocks are left at the forward run's
- * final state. */
+ * motion state).  Thin-surface cells (surfaces 51/52 of a plate) are
+ * differentiated through the predictor's ghost substitution and restore and
+ * through the ghost calls.  Refused (BCFD_E_STATE): a fine-block move during
+ * the run, precision /= 0.  The blocks are left at the forward run's final
+ * state. */
 int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t n_steps, int64_t every,
                             const double* wu, const double* wv, const double* ww, const double* wp,
                             const double* stress_seed, double mu_f, double rho_f, double adj_tol, int64_t adj_itmax,
@@ -405,8 +409,10 @@ int bcfd_block_get_divergence(bcfd_handle h, double* out);
  * (0: the library's choice, 1: tiled cooperative with grid-wide phase
  * barriers, 3: tiled cooperative with point-to-point neighbour sync, 4:
  * temporal-blocked sweeps, one grid barrier per sweep pair, when the block's
- * halo'd tiles fit in shared memory, else 1; 1, 3 and 4 give bitwise the
- * same corrections; 2 is not accepted) */
+ * halo'd tiles fit in shared memory, else 1; 5: z-marching sweeps, two
+ * sweep pairs per pass over the block with the correction staged in shared
+ * memory by TMA, when a packed row fits one TMA box (nx <= 509), else 1;
+ * 1, 3, 4 and 5 give bitwise the same corrections; 2 is not accepted) */
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant);
 /* launch shape of a block's tiled Poisson solves (the autotuner's knobs; no
  * effect on results): threads per CTA (0 = the default: 512 for the FP64
@@ -437,8 +443,9 @@ typedef struct bcfd_profile_report {
   int64_t sor_launches;   /* persistent Poisson-solve launches in the window      */
   double sor_ms;          /* their summed device time (CUDA events, library stream) */
   double sor_bytes;       /* algorithmic bytes they moved (4w+1 B per cell sweep
-                             pair, w = 8 FP64 / 4 FP32, plus the FP64 residual and
-                             update passes of the mixed solve)                     */
+                             pair, w = 8 FP64 / 4 FP32; 13 B per cell per two
+                             pairs for the z-marching sweeps; plus the FP64
+                             residual and update passes of the mixed solve)       */
   int64_t sor_sweeps;     /* red+black sweep pairs done by them                    */
   int64_t kernel_launches;/* kernels launched in the window                        */
 } bcfd_profile_report;

@@ -8,7 +8,11 @@ over 6 FP64 steps from the set-up:
   is towed: every IB cell is a thin-surface (TS) cell, so the predictor's
   ghost substitution, the ghost calls and the node rotation are transposed;
 * the same kind of plate in the fine block of a coarse/fine pair (the
-  coupling transposes inside the moving run).
+  coupling transposes inside the moving run);
+* two such plates in tandem, each in its own fine block, the trailing one
+  90 degrees behind: J is the leading plate's drag, its own amplitudes and
+  heave frequency are differentiated, and the shared phase angle and pitch
+  frequency move both plates (both bodies' geometry transposed).
 The gradients with respect to the motion parameters, the inflow velocity
 and the initial state are checked against central finite differences of the
 forward run at 1e-4 relative perturbations (bar: 1e-4 relative, plus an
@@ -42,6 +46,8 @@ def _base(body):
         return synth.heaving_sphere_single_block(n=24, n_steps=N_STEPS)
     if body == "pair":
         return synth.flapping_plate_pair(n_steps=N_STEPS, size="small")
+    if body == "tandem":
+        return synth.tandem_plates(n_steps=N_STEPS, moving=True, size="small")
     return synth.moving_plate_single_block(n=24, n_steps=N_STEPS)
 
 
@@ -89,7 +95,7 @@ def _base_run(body):
     return _BASE[body]
 
 
-@pytest.mark.parametrize("body", BODIES + ("pair",))
+@pytest.mark.parametrize("body", BODIES + ("pair", "tandem"))
 def test_moving_body_gradients_vs_fd(body):
     case, (J, duc, g) = _base_run(body)
     assert np.isfinite(J) and J != 0.0

@@ -753,6 +753,24 @@ def profile_run(args):
         print(json.dumps({"profile_case": "sweeps", "sweep_pairs": 8, "solve_log": out}), flush=True)
         s.close()
         return
+    if args.profile_case == "zmarch":
+        # FP32 sweeps of one body-free 256x192x192 block (9.4M cells, ~1.5 GB
+        # on the device): one correction of 8 sweep pairs with the tiled
+        # sweeps (variant 3), then one with the z-marching TMA sweeps (5)
+        case = synth.uniform_block((256, 192, 192), noise=True)
+        s = new_solver(case, 0, tune=False)
+        g = s.handles[0]
+        check(s.L.bcfd_cellcount_solid(g), "cellcount_solid")
+        check(s.L.bcfd_compute_div(g), "compute_div")
+        out = {}
+        for key, variant in (("tiled_neighbour_sync", 3), ("zmarch_tma", 5)):
+            s.set_mixed_params(variant=variant, block=g)
+            s.profile_begin()
+            check(s.L.bcfd_block_sor_sweeps(g, 8, 1), "sor_sweeps")
+            out[key] = s.profile_end()
+        print(json.dumps({"profile_case": "zmarch", "sweep_pairs": 8, "solve_log": out}), flush=True)
+        s.close()
+        return
     if args.profile_case == "tandem":
         case = synth.tandem_plates(n_steps=args.profile_steps + 2, moving=True)
     else:  # one 256x192x192 block with a plate: the fine-block size, ~1 GB on the device
@@ -876,7 +894,7 @@ def main():
                     help="timed steps of the flagship with zero-started solves, beside the warm-started value")
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiler mode: set up without the autotuner and run this many eager mixed steps")
-    ap.add_argument("--profile-case", default="tandem", choices=["tandem", "block256", "sweeps"])
+    ap.add_argument("--profile-case", default="tandem", choices=["tandem", "block256", "sweeps", "zmarch"])
     args = ap.parse_args()
     global WARM_START
     WARM_START = not args.zero_start

@@ -20,17 +20,6 @@ namespace bcfd {
 
 namespace {
 
-// interior-row decomposition of one colour: item t -> (h, j, k)
-struct RowMap {
-  int NXH, ny;
-  __device__ void at(int64_t t, int& h, int& j, int& k) const {
-    h = (int)(t % NXH);
-    const int64_t r = t / NXH;
-    j = 2 + (int)(r % ny);
-    k = 2 + (int)(r / ny);
-  }
-};
-
 // computeDiv (src/PcorVcor.F90:222-243) over the fluid cells; b lands in the
 // packed layout.  Non-fluid cells keep the zero of the start of the solve.
 struct DivOp {
@@ -292,7 +281,7 @@ __device__ __forceinline__ double tile_resid_max64(const DevBlock& B, const Tile
 
 // max over fluid cells of colour C of |b/dt - A pc| (grid-stride; measurement)
 template <int C>
-__device__ __forceinline__ double resid_max64(const DevBlock& B, const RowMap& rm, int64_t total) {
+__device__ __forceinline__ double resid_max64(const DevBlock& B, int64_t total) {
   const Dims& d = B.d;
   const double* own = B.pc[C];
   const double* o = B.pc[1 - C];
@@ -1313,8 +1302,7 @@ __global__ void __launch_bounds__(kDcThreads, 3) k_sor_dc_set(SolveSet<DcArgs> S
 __global__ void k_resid(DevBlock B, double dt) {
   __shared__ double sh[32];
   const int64_t total = (int64_t)B.d.NXH * B.d.ny * B.d.nz;
-  const RowMap rm{B.d.NXH, B.d.ny};
-  const double m = block_max(nmax(resid_max64<1>(B, rm, total), resid_max64<0>(B, rm, total)), sh);
+  const double m = block_max(nmax(resid_max64<1>(B, total), resid_max64<0>(B, total)), sh);
   if (threadIdx.x == 0) atomic_max_nonneg(&B.stats->pad[1], m * dt);
 }
 
@@ -1557,6 +1545,20 @@ int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_
   return launch_residual(hb, dt);
 }
 
+// the second FP32 correction buffer (both colours, zeroed once) of the
+// temporal-blocked and z-marching sweeps
+static int ensure_second_buffer(HostBlock* hb) {
+  if (hb->pcf2) return 0;
+  const int64_t np = hb->d.d.npacked();
+  void* p = nullptr;
+  if (cudaMalloc(&p, 2 * (size_t)np * sizeof(float)) != cudaSuccess) return BCFD_E_NOMEM;
+  hb->allocs.push_back(p);
+  hb->pcf2 = static_cast<float*>(p);
+  BCFD_CUDA(cudaMemsetAsync(hb->pcf2, 0, 2 * (size_t)np * sizeof(float), stream()));
+  lib().gen++;
+  return 0;
+}
+
 // Temporal-blocked solve: tiles of tj x tk rows with their two halo rows per
 // side in shared memory, one CTA of 512 threads per tile, all co-resident.
 static size_t tb_bytes(const Dims& d, int tj, int tk) {
@@ -1590,15 +1592,7 @@ bool tb_solve_fits(HostBlock* hb) {
 
 static int launch_sor_tb(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   DevBlock& B = hb->d;
-  const int64_t np = B.d.npacked();
-  if (!hb->pcf2) {
-    void* p = nullptr;
-    if (cudaMalloc(&p, 2 * (size_t)np * sizeof(float)) != cudaSuccess) return BCFD_E_NOMEM;
-    hb->allocs.push_back(p);
-    hb->pcf2 = static_cast<float*>(p);
-    BCFD_CUDA(cudaMemsetAsync(hb->pcf2, 0, 2 * (size_t)np * sizeof(float), stream()));
-    lib().gen++;
-  }
+  TRY_R(ensure_second_buffer(hb));
   int tj = 0, tk = 0;
   if (!tb_tiles(hb, &tj, &tk)) return BCFD_E_STATE;
   TileMap tm{tj, tk, (B.d.ny + tj - 1) / tj, (B.d.nz + tk - 1) / tk, hb->prog, 1};
@@ -1712,18 +1706,6 @@ static int encode_plane_map(CUtensorMap* m, const float* base, const Dims& d, in
                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? 0 : BCFD_E_STATE;
-}
-
-static int ensure_second_buffer(HostBlock* hb) {
-  if (hb->pcf2) return 0;
-  const int64_t np = hb->d.d.npacked();
-  void* p = nullptr;
-  if (cudaMalloc(&p, 2 * (size_t)np * sizeof(float)) != cudaSuccess) return BCFD_E_NOMEM;
-  hb->allocs.push_back(p);
-  hb->pcf2 = static_cast<float*>(p);
-  BCFD_CUDA(cudaMemsetAsync(hb->pcf2, 0, 2 * (size_t)np * sizeof(float), stream()));
-  lib().gen++;
-  return 0;
 }
 
 static int launch_sor_zm(HostBlock* hb, int64_t itmax, double dt, double div_tol) {

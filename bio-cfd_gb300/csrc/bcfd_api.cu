@@ -241,6 +241,9 @@ int upload_grids(HostBlock* hb) {
   hb->d.dxf = hb->grid_f32;
   hb->d.dyf = hb->grid_f32 + hb->dxa.size();
   hb->d.dzf = hb->grid_f32 + hb->dxa.size() + hb->dya.size();
+  if (!hb->lcoef) TRY(dalloc(hb, &hb->lcoef, hb->dxa.size() + hb->dya.size() + hb->dza.size()));
+  hb->d.lcoef = hb->lcoef;
+  hb->lcoef_dt = 0.0;  // the spacings may have changed
   return 0;
 }
 

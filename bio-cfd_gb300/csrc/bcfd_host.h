@@ -95,6 +95,8 @@ struct HostBlock {
   double* grid_buf = nullptr;      // device buffer holding all 1-D arrays
   double* coef_buf = nullptr;      // device Acx/Acy/Acz + ca/ck tables
   float* grid_f32 = nullptr;       // device dxa/dya/dza rounded to FP32
+  double* lcoef = nullptr;         // device per-line factors of correctVelocity (see DevBlock::lcoef)
+  double lcoef_dt = 0.0;           // the deltat they were computed for (0: not computed)
   float* coef_f32 = nullptr;       // device Acx/Acy/Acz rounded to FP32
   float* pcf2 = nullptr;           // second FP32 correction buffer (both colours) of the temporal-blocked sweeps
   int64_t mk = 0, mkx1 = 0, mkx2 = 0;  // findDistnode's extreme surface nodes (1-based)

@@ -241,7 +241,15 @@ int upload_grids(HostBlock* hb) {
   hb->d.dxf = hb->grid_f32;
   hb->d.dyf = hb->grid_f32 + hb->dxa.size();
   hb->d.dzf = hb->grid_f32 + hb->dxa.size() + hb->dya.size();
-  if (!hb->lcoef) TRY(dalloc(hb, &hb->lcoef, hb->dxa.size() + hb->dya.size() + hb->dza.size()));
+  // per-line tables: correctVelocity's factors (first half, filled per deltat
+  // on the device) and the reciprocal spacings (second half, here)
+  const size_t nl = hb->dxa.size() + hb->dya.size() + hb->dza.size();
+  if (!hb->lcoef) TRY(dalloc(hb, &hb->lcoef, 2 * nl));
+  std::vector<double> rec;
+  for (const auto* a : {&hb->dxa, &hb->dya, &hb->dza})
+    for (double x : *a) rec.push_back(1.0 / x);
+  BCFD_CUDA(cudaMemcpyAsync(hb->lcoef + nl, rec.data(), nl * sizeof(double), cudaMemcpyHostToDevice, stream()));
+  BCFD_CUDA(cudaStreamSynchronize(stream()));
   hb->d.lcoef = hb->lcoef;
   hb->lcoef_dt = 0.0;  // the spacings may have changed
   return 0;

@@ -142,9 +142,10 @@ struct DevBlock {
   const struct Kin* kin;
   int* err;             // device error word of this block (first error wins)
   double* scratch;      // per-block reduction scratch
-  // correctVelocity's per-line factors deltat / (0.5 (delta_i + delta_{i+1}))
-  // along x, y, z (index i, j, k; nx+2, ny+2, nz+2 entries each), computed
-  // once per deltat with the reference's operations
+  // per-line tables, NX + NY + NZ entries each: correctVelocity's factors
+  // deltat / (0.5 (delta_i + delta_{i+1})) along x, y, z (index i, j, k),
+  // computed once per deltat with the reference's operations; then the
+  // reciprocal spacings 1 / deltax(i) etc. (index i-1, like dxa)
   const double* lcoef;
   double* bpk[2];       // colour-packed divergence b (the reference's Block_t%b)
   struct BlockStats* stats;

@@ -1394,12 +1394,18 @@ struct MaxDivOp {
     const double* U = tfield ? B.ut : B.u;
     const double* V = tfield ? B.vt : B.v;
     const double* W = tfield ? B.wt : B.w;
+    // a measurement (not a reference routine): the divergence with the
+    // reciprocal spacings, within an ulp of the divided form, without three
+    // FP64 divisions per cell
+    const double* rx = B.lcoef + (d.NX + d.NY + d.NZ);
+    const double* ry = rx + d.NX;
+    const double* rz = ry + d.NY;
     double m = 0.0;
     FOR_INTERIOR(B, cta, ncta) {
       INTERIOR_CELL(B);
       if (B.cell[c] != 0) continue;
-      const double dv = (U[c] - U[c - 1]) / B.dxa[i - 1] + (V[c] - V[c - d.NX]) / B.dya[j - 1] +
-                        (W[c] - W[c - (int64_t)d.NX * d.NY]) / B.dza[k - 1];
+      const double dv = (U[c] - U[c - 1]) * rx[i - 1] + (V[c] - V[c - d.NX]) * ry[j - 1] +
+                        (W[c] - W[c - (int64_t)d.NX * d.NY]) * rz[k - 1];
       m = nmax(m, fabs(dv));
     }
     m = block_max(m, sh);

@@ -397,7 +397,9 @@ int bcfd_adjoint_run_motion(bcfd_handle h, const bcfd_step_config* cfg, int64_t 
                             const double* stress_seed, double mu_f, double rho_f, double adj_tol, int64_t adj_itmax,
                             double* J, double* dj_duc, double* dj_dmotion, double* gu, double* gv, double* gw,
                             double* gp);
-/* max over fluid cells of |div u| of the current u,v,w (FP64) */
+/* max over fluid cells of |div u| of the current u,v,w (FP64, the backward
+ * differences times the reciprocal spacings: within an ulp of the divided
+ * form of computeDiv) */
 int bcfd_max_divergence(bcfd_handle h, double* out);
 /* out[0] = max over fluid cells of |div ut| right after the last velocity
  * correction; out[1] = deltat * max over fluid cells of |b/deltat - A pc|, the

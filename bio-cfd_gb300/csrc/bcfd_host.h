@@ -252,7 +252,9 @@ int launch_compute_div(HostBlock* hb);
 int launch_correct_pressure(HostBlock* hb);
 int launch_correct_velocity(HostBlock* hb, double dt);
 // the same phases over several blocks (one launch per phase when batching)
-int launch_compute_div(const std::vector<HostBlock*>& hbs);
+// fast: reciprocal spacings (residual-target solves) instead of the
+// reference's divisions
+int launch_compute_div(const std::vector<HostBlock*>& hbs, bool fast);
 int launch_correct_pressure(const std::vector<HostBlock*>& hbs);
 int launch_correct_velocity(const std::vector<HostBlock*>& hbs, double dt);
 int launch_steady_state(const std::vector<HostBlock*>& hbs, double dt);

@@ -186,7 +186,7 @@ int poisson(const SolveCfg& c, int start, int finish, int step) {
   TRY(fine_update_newv_bd());
   TRY(coarse_update_newv());
   phase_mark(PH_CORRECTION);
-  TRY(launch_compute_div(set));
+  TRY(launch_compute_div(set, c.precision >= 1));
   phase_mark(PH_SOLVE);
   TRY(sor_set(fine, c));
   phase_mark(PH_COUPLING);

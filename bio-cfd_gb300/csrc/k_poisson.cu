@@ -22,15 +22,23 @@ namespace {
 
 // computeDiv (src/PcorVcor.F90:222-243) over the fluid cells; b lands in the
 // packed layout.  Non-fluid cells keep the zero of the start of the solve.
+// With `fast` (the residual-target solves, which reproduce no reference bits)
+// the differences are multiplied by the reciprocal spacings instead of divided
+// by the spacings: b within an ulp, without three FP64 divisions per cell.
 struct DivOp {
+  int fast;
   __device__ void run(const DevBlock& B, int cta, int ncta) const {
     const Dims& d = B.d;
+    const double* rx = B.lcoef + (d.NX + d.NY + d.NZ);
+    const double* ry = rx + d.NX;
+    const double* rz = ry + d.NY;
     FOR_INTERIOR(B, cta, ncta) {
       INTERIOR_CELL(B);
       if (B.cell[c] != 0) continue;
-      const double bv = (B.ut[c] - B.ut[c - 1]) / B.dxa[i - 1] +
-                        (B.vt[c] - B.vt[c - d.NX]) / B.dya[j - 1] +
-                        (B.wt[c] - B.wt[c - (int64_t)d.NX * d.NY]) / B.dza[k - 1];
+      const double du = B.ut[c] - B.ut[c - 1], dv = B.vt[c] - B.vt[c - d.NX],
+                   dw = B.wt[c] - B.wt[c - (int64_t)d.NX * d.NY];
+      const double bv = fast ? du * rx[i - 1] + dv * ry[j - 1] + dw * rz[k - 1]
+                             : du / B.dxa[i - 1] + dv / B.dya[j - 1] + dw / B.dza[k - 1];
       B.bpk[colour_of(i, j, k)][d.pidx(i, j, k)] = bv;
     }
   }
@@ -1471,10 +1479,10 @@ __global__ void k_unpack(DevBlock B, const double* p0, const double* p1, double*
 
 constexpr unsigned kCellCap = 152u * 32u;
 
-int launch_compute_div(const std::vector<HostBlock*>& hbs) {
-  return launch_op<DivOp, 256>(hbs, DivOp{}, Extent::Interior, kCellCap);
+int launch_compute_div(const std::vector<HostBlock*>& hbs, bool fast) {
+  return launch_op<DivOp, 256>(hbs, DivOp{fast ? 1 : 0}, Extent::Interior, kCellCap);
 }
-int launch_compute_div(HostBlock* hb) { return launch_compute_div(std::vector<HostBlock*>{hb}); }
+int launch_compute_div(HostBlock* hb) { return launch_compute_div(std::vector<HostBlock*>{hb}, false); }
 
 int launch_correct_pressure(const std::vector<HostBlock*>& hbs) {
   return launch_op<CorrectPOp, 256>(hbs, CorrectPOp{}, Extent::Interior, kCellCap);

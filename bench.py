@@ -691,22 +691,25 @@ def tandem_long(torch, local, fwd=1000, cmp=100, adj=20, every=5, adj_tol=1e-10)
                        "heaving 0.125 sin(2 pi 0.25 t) and pitching 15 deg sin(2 pi 0.25 t + 90 deg), trailing "
                        "plate 90 deg behind, Re 1000, Search every step",
            "omega": [b.omega for b in case.blocks]}
-    # one solver at a time (the library holds one set of blocks)
-    sb = new_solver(case, local)
-    tb, _ = timed_steps(sb, torch, cmp, 3)
-    snap_b = ([sb.fields(g) for g in sb.handles], [sb.stress(g, mu_f).tolist() for g in sb.handles[1:]])
-    res_b, _ = residual_stats(sb)
-    sb.close()
+    ta = []
+    if cmp > 0:
+        # one solver at a time (the library holds one set of blocks)
+        sb = new_solver(case, local)
+        tb, _ = timed_steps(sb, torch, cmp, 3)
+        snap_b = ([sb.fields(g) for g in sb.handles], [sb.stress(g, mu_f).tolist() for g in sb.handles[1:]])
+        res_b, _ = residual_stats(sb)
+        sb.close()
     sa = new_solver(case, local)
-    ta, _ = timed_steps(sa, torch, cmp, 1)
-    snap_a = ([sa.fields(g) for g in sa.handles], [sa.stress(g, mu_f).tolist() for g in sa.handles[1:]])
-    err, coef = field_errors(snap_a[0], snap_b[0], snap_a[1], snap_b[1])
-    out["mixed_vs_fp64"] = {"after_steps": cmp, "field_rel_l2": err, "coef_rel": coef,
-                            "coefficients": "per plate: viscous drag, pressure drag, viscous lift, pressure lift",
-                            "mixed_ms_per_step": statistics.mean(ta), "fp64_ms_per_step": statistics.mean(tb),
-                            "fp64_div_residual": res_b,
-                            "fp64": "FP64 momentum + division-free FP64 SOR to the residual 1e-6"}
-    del snap_b
+    if cmp > 0:
+        ta, _ = timed_steps(sa, torch, cmp, 1)
+        snap_a = ([sa.fields(g) for g in sa.handles], [sa.stress(g, mu_f).tolist() for g in sa.handles[1:]])
+        err, coef = field_errors(snap_a[0], snap_b[0], snap_a[1], snap_b[1])
+        out["mixed_vs_fp64"] = {"after_steps": cmp, "field_rel_l2": err, "coef_rel": coef,
+                                "coefficients": "per plate: viscous drag, pressure drag, viscous lift, pressure lift",
+                                "mixed_ms_per_step": statistics.mean(ta), "fp64_ms_per_step": statistics.mean(tb),
+                                "fp64_div_residual": res_b,
+                                "fp64": "FP64 momentum + division-free FP64 SOR to the residual 1e-6"}
+        del snap_b
     tc, _ = timed_steps(sa, torch, fwd - cmp, 1)
     res_a, pairs_a = residual_stats(sa)
     out["forward"] = {"steps": fwd, "ms_per_step_last": statistics.mean(tc[-50:]),

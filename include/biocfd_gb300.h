@@ -425,11 +425,14 @@ int bcfd_block_set_solve_launch(bcfd_handle h, int threads, int ctas_per_sm, int
 /* out[6] = FP64 solve threads, CTAs/SM cap, sync; FP32 correction threads,
  * CTAs/SM cap, variant (0 = library default) */
 int bcfd_block_get_solve_launch(bcfd_handle h, int* out);
-/* Autotuner (no counterpart in the reference): for every block solved alone,
- * times short solves under each candidate launch shape of the FP64 solve and
- * of the FP32 correction (threads per CTA, CTAs per SM, which sets the tile
- * shape, and the phase synchronisation) and keeps the fastest; results are
- * cached per block shape.  None of these changes the arithmetic.  The block's
+/* Autotuner (no counterpart in the reference): for every block, times short
+ * solves under each candidate launch shape of the FP64 solve and of the FP32
+ * correction (threads per CTA, CTAs per SM, which sets the tile shape, the
+ * phase synchronisation, the sweep variant) and keeps the fastest; results are
+ * cached per block shape.  The blocks whose solves batching would run side
+ * by side in one launch (every block after the first, when there are several)
+ * keep that launch only if it beats their best launches one after the other
+ * (timed, per precision).  None of these changes the arithmetic.  The blocks'
  * solve state is restored afterwards.  *n_tuned = shapes newly timed. */
 int bcfd_autotune(int64_t* n_tuned);
 /* measurement: exactly n_pairs red-black sweep pairs of the block's Poisson

@@ -732,8 +732,8 @@ def tandem_long(torch, local, fwd=1000, cmp=100, adj=20, every=5, adj_tol=1e-10)
 
 
 def profile_run(args):
-    """A short run for profiler captures: the chosen workload set up without
-    the autotuner, then `--profile-steps` eagerly issued steps of the mixed
+    """A short run for profiler captures: the chosen workload set up (without
+    the autotuner unless `--profile-tune`), then `--profile-steps` eagerly issued steps of the mixed
     path (one kernel launch per phase and block, as a replayed graph holds
     them); prints the per-step time and the phase split of the last step."""
     import torch
@@ -779,7 +779,7 @@ def profile_run(args):
         case = synth.tandem_plates(n_steps=args.profile_steps + 2, moving=True)
     else:  # one 256x192x192 block with a plate: the fine-block size, ~1 GB on the device
         case = synth.plate_block(n=(256, 192, 192), n_steps=args.profile_steps + 2)
-    s = new_solver(case, 0, tune=False)
+    s = new_solver(case, 0, tune=args.profile_tune)
     stream = torch.cuda.ExternalStream(s.stream_ptr())
     ts = []
     for q in range(args.profile_steps):
@@ -899,6 +899,8 @@ def main():
     ap.add_argument("--profile-steps", type=int, default=0,
                     help="profiler mode: set up without the autotuner and run this many eager mixed steps")
     ap.add_argument("--profile-case", default="tandem", choices=["tandem", "block256", "sweeps", "zmarch"])
+    ap.add_argument("--profile-tune", action="store_true",
+                    help="profiling run: autotune the solves first (the bench's launch shapes)")
     args = ap.parse_args()
     global WARM_START
     WARM_START = not args.zero_start

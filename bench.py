@@ -609,7 +609,7 @@ def adjoint_flapping(torch, steps=200, every=20, fd=(), size="full", epsi=1e-12)
     steps checkpointed every `every`, J = time-averaged drag + lift
     coefficients, its gradient with respect to the five motion parameters and
     the inflow velocity; optional central differences ("name:rel" items of
-    `fd`).  The forward solves relax with 2/(1 + sin(pi/n)) and stop at the
+    `fd`).  The forward solves relax with the mixed path's default factor and stop at the
     reference's increment test with epsi (1e-12 by default, so that the
     differences see the discretisation, not the stopping noise)."""
     import dataclasses
@@ -732,8 +732,9 @@ def tandem_long(torch, local, fwd=1000, cmp=100, adj=20, every=5, adj_tol=1e-10)
 
 
 def profile_run(args):
-    """A short run for profiler captures: the chosen workload set up (without
-    the autotuner unless `--profile-tune`), then `--profile-steps` eagerly issued steps of the mixed
+    """A short run for profiler captures: the chosen workload set up without
+    the autotuner (with `--profile-tune`, the shapes it picks on the tandem
+    plates, set directly), then `--profile-steps` eagerly issued steps of the mixed
     path (one kernel launch per phase and block, as a replayed graph holds
     them); prints the per-step time and the phase split of the last step."""
     import torch
@@ -779,7 +780,15 @@ def profile_run(args):
         case = synth.tandem_plates(n_steps=args.profile_steps + 2, moving=True)
     else:  # one 256x192x192 block with a plate: the fine-block size, ~1 GB on the device
         case = synth.plate_block(n=(256, 192, 192), n_steps=args.profile_steps + 2)
-    s = new_solver(case, 0, tune=args.profile_tune)
+    s = new_solver(case, 0, tune=False)
+    if args.profile_tune:
+        # the launch shapes the autotuner picks on the tandem plates, set
+        # directly (timings under a profiler would mislead the autotuner):
+        # every block's FP32 correction with neighbour-synchronised tiles and
+        # its FP64 solve with grid-synchronised tiles, each in launches of its own
+        for q, g in enumerate(s.handles):
+            s.set_mixed_params(variant=3, block=g)
+            s.set_solve_launch(512, 0, 1, block=q)
     stream = torch.cuda.ExternalStream(s.stream_ptr())
     ts = []
     for q in range(args.profile_steps):
@@ -900,7 +909,7 @@ def main():
                     help="profiler mode: set up without the autotuner and run this many eager mixed steps")
     ap.add_argument("--profile-case", default="tandem", choices=["tandem", "block256", "sweeps", "zmarch"])
     ap.add_argument("--profile-tune", action="store_true",
-                    help="profiling run: autotune the solves first (the bench's launch shapes)")
+                    help="profiling run: the launch shapes the autotuner picks on the tandem plates, set directly")
     args = ap.parse_args()
     global WARM_START
     WARM_START = not args.zero_start

@@ -564,13 +564,21 @@ def small_two_block(n_steps: int = 2, seed: int = SEED) -> Case:
                             pc_ita_max=2000, seed=seed)
 
 
+def mixed_omega(nx: int, ny: int, nz: int) -> float:
+    """The relaxation factor the mixed path's FP32 sweeps use by default: the
+    classical red-black SOR optimum 2 / (1 + sqrt(1 - rho^2)) for the 7-point
+    Laplacian on an nx x ny x nz box with Dirichlet boundaries, rho = (cos(pi/nx)
+    + cos(pi/ny) + cos(pi/nz)) / 3, at most 1.99 (the library's expression)."""
+    e = sum(2.0 * np.sin(np.pi / (2.0 * n)) ** 2 for n in (nx, ny, nz)) / 3.0
+    return float(min(1.99, 2.0 / (1.0 + np.sqrt(e * (2.0 - e)))))
+
+
 def with_mixed_omega(case: Case) -> Case:
     """A copy of `case` whose blocks relax with the factor the mixed path's FP32
-    sweeps use by default, 2 / (1 + sin(pi / n_max)) for the block's largest
-    extent n_max, instead of the input's omega: the plain FP64 solve at the same
-    relaxation separates the gain of the precision from that of the factor."""
-    blocks = [dataclasses.replace(b, omega=2.0 / (1.0 + np.sin(np.pi / max(b.nx, b.ny, b.nz))))
-              for b in case.blocks]
+    sweeps use by default (`mixed_omega`) instead of the input's omega: the
+    plain FP64 solve at the same relaxation separates the gain of the precision
+    from that of the factor."""
+    blocks = [dataclasses.replace(b, omega=mixed_omega(b.nx, b.ny, b.nz)) for b in case.blocks]
     return dataclasses.replace(case, blocks=blocks)
 
 

@@ -416,6 +416,24 @@ __device__ __forceinline__ void sor64_body(const DevBlock& B, const SorArgs& a, 
 //   red-black FP32 SOR sweeps from e = 0 (non-fluid cells are zero Dirichlet
 //   data for e) and update x += e in FP64.
 // ---------------------------------------------------------------------------
+// largest relaxation factor of the FP32 correction sweeps
+constexpr double kMixedOmegaMax = 1.99;
+
+// the default relaxation factor of the FP32 correction sweeps: the classical
+// optimum 2 / (1 + sqrt(1 - rho^2)) of red-black SOR for the 7-point Laplacian
+// on an nx x ny x nz box with Dirichlet boundaries, rho = (cos(pi/nx) +
+// cos(pi/ny) + cos(pi/nz)) / 3 the Jacobi spectral radius (1 - rho formed
+// from sin^2 terms, free of cancellation)
+double mixed_omega_default(const Dims& d) {
+  const double pi = 3.14159265358979323846;
+  auto s2 = [&](int n) {
+    const double x = std::sin(pi / (2.0 * n));
+    return 2.0 * x * x;  // 1 - cos(pi / n)
+  };
+  const double e = (s2(d.nx) + s2(d.ny) + s2(d.nz)) / 3.0;  // 1 - rho
+  return 2.0 / (1.0 + std::sqrt(e * (2.0 - e)));
+}
+
 struct DcArgs {
   int64_t max_outer;
   int inner;          // FP32 sweeps per correction
@@ -1649,11 +1667,10 @@ static int launch_sor_tb(HostBlock* hb, int64_t itmax, double dt, double div_tol
   const size_t smem = tb_bytes(B.d, tj, tk);
   BCFD_CUDA(cudaFuncSetAttribute((const void*)k_sor_tb, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const unsigned grid = (unsigned)(tm.ntj * tm.ntk);
-  const int nmax = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
   DcArgs a;
   a.inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
-  double om = hb->dc_omega > 0 ? hb->dc_omega : 2.0 / (1.0 + std::sin(3.14159265358979323846 / nmax));
-  a.omega = (float)std::min(1.97, std::max(1.0, om));
+  double om = hb->dc_omega > 0 ? hb->dc_omega : mixed_omega_default(B.d);
+  a.omega = (float)std::min(kMixedOmegaMax, std::max(1.0, om));
   a.max_outer = itmax / a.inner + 1;
   a.dt = dt;
   a.inv_dt = 1.0 / dt;
@@ -1774,11 +1791,10 @@ static int launch_sor_zm(HostBlock* hb, int64_t itmax, double dt, double div_tol
   const size_t smem = zm_smem_bytes(B.d, z.rows);
   BCFD_CUDA(cudaFuncSetAttribute((const void*)k_sor_zm, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   const unsigned grid = (unsigned)(z.ntj * z.nzs);
-  const int nmax = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
   DcArgs a;
   a.inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
-  double om = hb->dc_omega > 0 ? hb->dc_omega : 2.0 / (1.0 + std::sin(3.14159265358979323846 / nmax));
-  a.omega = (float)std::min(1.97, std::max(1.0, om));
+  double om = hb->dc_omega > 0 ? hb->dc_omega : mixed_omega_default(B.d);
+  a.omega = (float)std::min(kMixedOmegaMax, std::max(1.0, om));
   a.max_outer = itmax / a.inner + 1;
   a.dt = dt;
   a.inv_dt = 1.0 / dt;
@@ -1797,7 +1813,6 @@ static int launch_sor_zm(HostBlock* hb, int64_t itmax, double dt, double div_tol
 int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   DevBlock& B = hb->d;
   const int64_t np = B.d.npacked();
-  const int nmax0 = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
   for (int c = 0; c < 2; ++c) BCFD_CUDA(cudaMemsetAsync(B.pcf[c], 0, np * sizeof(float), stream()));
   if (hb->dc_variant == 4 && tb_solve_fits(hb)) return launch_sor_tb(hb, itmax, dt, div_tol);
   if (hb->dc_variant == 5 && zm_solve_fits(hb)) return launch_sor_zm(hb, itmax, dt, div_tol);
@@ -1808,11 +1823,10 @@ int launch_sor_mixed(HostBlock* hb, int64_t itmax, double dt, double div_tol) {
   TileMap tm = choose_tiles(hb, fn, threads, hb->dc_variant == 3 ? 0 : 1, hb->dc_ctas_per_sm);
   TRY_R(reset_solve_state(hb, tm));
   const unsigned grid = (unsigned)(tm.ntj * tm.ntk);
-  const int nmax = std::max(B.d.nx, std::max(B.d.ny, B.d.nz));
   DcArgs a;
   a.inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
-  double om = hb->dc_omega > 0 ? hb->dc_omega : 2.0 / (1.0 + std::sin(3.14159265358979323846 / nmax));
-  a.omega = (float)std::min(1.97, std::max(1.0, om));
+  double om = hb->dc_omega > 0 ? hb->dc_omega : mixed_omega_default(B.d);
+  a.omega = (float)std::min(kMixedOmegaMax, std::max(1.0, om));
   a.max_outer = itmax / a.inner + 1;
   a.dt = dt;
   a.inv_dt = 1.0 / dt;
@@ -1924,10 +1938,9 @@ int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, doub
   }
   auto make = [&](HostBlock* hb, DcArgs& a) -> int {
     const Dims& d = hb->d.d;
-    const int nmax = std::max(d.nx, std::max(d.ny, d.nz));
     a.inner = hb->dc_inner > 0 ? hb->dc_inner : 64;
-    const double om = hb->dc_omega > 0 ? hb->dc_omega : 2.0 / (1.0 + std::sin(3.14159265358979323846 / nmax));
-    a.omega = (float)std::min(1.97, std::max(1.0, om));
+    const double om = hb->dc_omega > 0 ? hb->dc_omega : mixed_omega_default(d);
+    a.omega = (float)std::min(kMixedOmegaMax, std::max(1.0, om));
     a.max_outer = itmax / a.inner + 1;
     a.dt = dt;
     a.inv_dt = 1.0 / dt;

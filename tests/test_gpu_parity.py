@@ -127,7 +127,7 @@ def test_stress_calculation(maker):
 
 
 def test_steps_100_single_block_bitwise():
-    # the spec bar is rel L2 1e-8 after 100 steps; the drop-in path is bitwise
+    # the drop-in path must stay within rel L2 1e-8 after 100 steps; it is bitwise
     case = synth.sphere_single_block(n=24, n_steps=100, diameter=0.3)
     o, s = _pair(case)
     for _ in range(100):

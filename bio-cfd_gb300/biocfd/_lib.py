@@ -53,6 +53,7 @@ class ProfileReport(C.Structure):
 _SIGS = {
     "bcfd_block_get_divergence": [c_i64, P_d],
     "bcfd_block_set_mixed_params": [c_i64, c_i64, c_double, c_int],
+    "bcfd_block_get_mixed_omega": [c_i64, P_d],
     "bcfd_block_set_solve_launch": [c_i64, c_int, c_int, c_int],
     "bcfd_set_batching": [c_int],
     "bcfd_set_warm_start": [c_int],

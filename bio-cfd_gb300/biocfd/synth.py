@@ -569,8 +569,15 @@ def mixed_omega(nx: int, ny: int, nz: int) -> float:
     classical red-black SOR optimum 2 / (1 + sqrt(1 - rho^2)) for the 7-point
     Laplacian on an nx x ny x nz box with Dirichlet boundaries, rho = (cos(pi/nx)
     + cos(pi/ny) + cos(pi/nz)) / 3, at most 1.99 (the library's expression)."""
-    e = sum(2.0 * np.sin(np.pi / (2.0 * n)) ** 2 for n in (nx, ny, nz)) / 3.0
-    return float(min(1.99, 2.0 / (1.0 + np.sqrt(e * (2.0 - e)))))
+    import math
+    pi = 3.14159265358979323846
+
+    def s2(n):
+        x = math.sin(pi / (2.0 * n))
+        return 2.0 * x * x
+
+    e = (s2(nx) + s2(ny) + s2(nz)) / 3.0
+    return min(1.99, max(1.0, 2.0 / (1.0 + math.sqrt(e * (2.0 - e)))))
 
 
 def with_mixed_omega(case: Case) -> Case:

@@ -1360,6 +1360,14 @@ int bcfd_block_get_solve_launch(bcfd_handle h, int* out) {
   return 0;
 }
 
+int bcfd_block_get_mixed_omega(bcfd_handle h, double* omega) {
+  LOCK();
+  GETB(h);
+  if (!omega) return BCFD_E_ARG;
+  *omega = mixed_omega_of(hb);
+  return 0;
+}
+
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant) {
   LOCK();
   GETB(h);

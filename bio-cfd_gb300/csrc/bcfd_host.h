@@ -266,6 +266,7 @@ int launch_sor_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt,
                    int fast = 0);
 bool tb_solve_fits(HostBlock* hb);
 bool zm_solve_fits(HostBlock* hb);
+double mixed_omega_of(const HostBlock* hb);
 int launch_sor_mixed_set(const std::vector<HostBlock*>& hbs, int64_t itmax, double dt, double div_tol);
 // res_tol > 0: stop on the FP64 residual dt*max|b/dt - A pc| <= res_tol
 int launch_sor(HostBlock* hb, int64_t itmax, double dt, double epsi, double res_tol = 0.0, int fast = 0);

@@ -1532,6 +1532,13 @@ __global__ void k_pc_warm(DevBlock B) {
   }
 }
 
+// the relaxation factor a block's FP32 correction sweeps use (the block's
+// setting or the default, within [1, kMixedOmegaMax]), before the FP32 rounding
+double mixed_omega_of(const HostBlock* hb) {
+  const double om = hb->dc_omega > 0 ? hb->dc_omega : mixed_omega_default(hb->d.d);
+  return std::min(kMixedOmegaMax, std::max(1.0, om));
+}
+
 int launch_zero_poisson(HostBlock* hb, bool warm) {
   const size_t bytes = (size_t)hb->d.d.npacked() * sizeof(double);
   if (warm) {

@@ -416,6 +416,11 @@ int bcfd_block_get_divergence(bcfd_handle h, double* out);
  * memory by TMA, when a packed row fits one TMA box (nx <= 509), else 1;
  * 1, 3, 4 and 5 give bitwise the same corrections; 2 is not accepted) */
 int bcfd_block_set_mixed_params(bcfd_handle h, int64_t inner_sweeps, double omega, int variant);
+/* the relaxation factor block h's FP32 correction sweeps use (its setting or
+ * the default: 2 / (1 + sqrt(1 - rho^2)), rho = (cos(pi/nx) + cos(pi/ny) +
+ * cos(pi/nz)) / 3; at most 1.99), before its rounding to FP32 (no counterpart
+ * in the reference) */
+int bcfd_block_get_mixed_omega(bcfd_handle h, double* omega);
 /* launch shape of a block's tiled Poisson solves (the autotuner's knobs; no
  * effect on results): threads per CTA (0 = the default: 512 for the FP64
  * solve, 256 for the mixed one, which takes at most 256; else 128/256/512), cap

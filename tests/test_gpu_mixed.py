@@ -100,3 +100,22 @@ def test_warm_start_reaches_tolerance_and_agrees(precision):
             # further than the velocities
             e = rel_l2(bz[nm], bw[nm])
             assert e < (P_TOL if nm == "p" else FIELD_TOL), (nm, e)
+
+
+def test_fp64_arm_relaxes_with_the_mixed_paths_factor():
+    """synth.with_mixed_omega gives the FP64 comparison arms exactly the factor
+    the library's FP32 sweeps use by default (to the last ulp)."""
+    import ctypes as C
+
+    from biocfd._lib import check
+    for case in (synth.small_two_block(n_steps=1), synth.uniform_block(n=(23, 17, 13), lengths=(3.0, 2.0, 2.0))):
+        s = Solver(case)
+        s.setup()
+        try:
+            for g, spec in zip(s.handles, case.blocks):
+                w = C.c_double()
+                check(s.L.bcfd_block_get_mixed_omega(g, C.byref(w)), "get_mixed_omega")
+                want = synth.mixed_omega(spec.nx, spec.ny, spec.nz)
+                assert abs(w.value - want) <= 1e-15 * want, (w.value, want, spec.nx, spec.ny, spec.nz)
+        finally:
+            s.close()

@@ -436,11 +436,27 @@ double mixed_omega_default(const Dims& d) {
 
 struct DcArgs {
   int64_t max_outer;
-  int inner;          // FP32 sweeps per correction
+  int inner;          // FP32 sweep pairs of the first correction (and the most of any)
   float omega;        // relaxation of the FP32 sweeps
   double dt, inv_dt, div_tol;
   int64_t* log;
 };
+
+// Sweep pairs of the next correction.  The first takes a.inner; each later
+// one takes what the residual reduction per pair measured over the previous
+// correction needs to reach the target (15% and two pairs of margin), at
+// least kMinInner and at most a.inner, so the last correction of a solve does
+// not run a full a.inner pairs past the target.  Every CTA computes it from
+// the same two residuals, so all agree.
+constexpr int kMinInner = 16;
+__device__ __forceinline__ int next_inner(const DcArgs& a, int outer, double res, double res_prev, int prev) {
+  const double target = a.div_tol * a.inv_dt;
+  if (outer == 0 || !(res < res_prev) || !(res > target) || !(target > 0.0)) return a.inner;
+  const double per_pair = log(res / res_prev) / (double)prev;  // < 0
+  const double need = log(target / res) / per_pair;             // > 0
+  if (!(need < (double)a.inner)) return a.inner;
+  return min(a.inner, max(kMinInner, (int)ceil(need * 1.15) + 2));
+}
 
 // one FP32 half-sweep of colour C over the tile.  Each thread updates a run
 // of four consecutive packed cells h0..h0+3 of one row (h0 a multiple of 4;
@@ -610,7 +626,8 @@ __device__ __forceinline__ void sor_dc_body(const DevBlock& B, const DcArgs& a, 
   const Tile t = my_tile(B.d, tm, cta);
   BlockStats* st = B.stats;
   int64_t sweeps = 0;
-  double res = 0.0;
+  double res = 0.0, res_prev = 0.0;
+  int inner = a.inner;
   unsigned ph = 0;
   int outer = 0;
   for (;; ++outer) {
@@ -622,7 +639,9 @@ __device__ __forceinline__ void sor_dc_body(const DevBlock& B, const DcArgs& a, 
     if (!grid_sync(gb)) return;
     res = take_slot(st, outer, cta);
     if (a.dt * res <= a.div_tol || outer >= a.max_outer || non_finite(res)) break;
-    for (int it = 0; it < a.inner; ++it) {
+    inner = next_inner(a, outer, res, res_prev, inner);
+    res_prev = res;
+    for (int it = 0; it < inner; ++it) {
       if (!tile_wait(tm, gb, t, ph)) return;
       tile_half32<1>(B, t, a.omega);
       tile_publish(tm, t, ++ph);
@@ -630,7 +649,7 @@ __device__ __forceinline__ void sor_dc_body(const DevBlock& B, const DcArgs& a, 
       tile_half32<0>(B, t, a.omega);
       tile_publish(tm, t, ++ph);
     }
-    sweeps += a.inner;
+    sweeps += inner;
     if (!tile_wait(tm, gb, t, ph)) return;
     tile_apply4<1>(B, t);
     tile_apply4<0>(B, t);
@@ -862,7 +881,8 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_sor_tb(DevBlock B, DcArgs a, 
   BlockStats* st = B.stats;
   tb_zero_pads(s);
   int64_t sweeps = 0;
-  double res = 0.0;
+  double res = 0.0, res_prev = 0.0;
+  int inner = a.inner;
   int outer = 0;
   for (;; ++outer) {
     double m = nmax(tile_residual64v<1>(B, t, a.inv_dt), tile_residual64v<0>(B, t, a.inv_dt));
@@ -871,8 +891,10 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_sor_tb(DevBlock B, DcArgs a, 
     if (!grid_sync(gb)) return;
     res = take_slot(st, outer, cta);
     if (a.dt * res <= a.div_tol || outer >= a.max_outer || non_finite(res)) break;
+    inner = next_inner(a, outer, res, res_prev, inner);
+    res_prev = res;
     int cur = 0;
-    for (int it = 0; it < a.inner; ++it) {
+    for (int it = 0; it < inner; ++it) {
       const float* const* src = cur ? E1 : E0;
       const float* srcc[2] = {src[0], src[1]};
       tb_load(B, t, s, srcc, it == 0);
@@ -885,7 +907,7 @@ __global__ void __launch_bounds__(kTbThreads, 1) k_sor_tb(DevBlock B, DcArgs a, 
       cur ^= 1;
       if (!grid_sync(gb)) return;
     }
-    sweeps += a.inner;
+    sweeps += inner;
     if (cur) {
       const float* e1c[2] = {E1[0], E1[1]};
       tb_copy_back(B, t, e1c);
@@ -1233,7 +1255,8 @@ __global__ void __launch_bounds__(kZmThreads, 1) k_sor_zm(DevBlock B, DcArgs a, 
   float* const E1[2] = {z.e2, z.e2 + np};
   BlockStats* st = B.stats;
   int64_t sweeps = 0;
-  double res = 0.0;
+  double res = 0.0, res_prev = 0.0;
+  int inner = a.inner;
   int outer = 0;
   for (;; ++outer) {
     double m = nmax(tile_residual64v<1>(B, t, a.inv_dt), tile_residual64v<0>(B, t, a.inv_dt));
@@ -1243,10 +1266,12 @@ __global__ void __launch_bounds__(kZmThreads, 1) k_sor_zm(DevBlock B, DcArgs a, 
     if (!grid_sync(gb)) return;
     res = take_slot(st, outer, cta);
     if (a.dt * res <= a.div_tol || outer >= a.max_outer || non_finite(res)) break;
-    const int passes = (a.inner + 1) / 2;
+    inner = next_inner(a, outer, res, res_prev, inner);
+    res_prev = res;
+    const int passes = (inner + 1) / 2;
     int cur = 0;
     for (int ps = 0; ps < passes; ++ps) {
-      const int nlev = (ps == passes - 1 && (a.inner & 1)) ? 2 : 4;
+      const int nlev = (ps == passes - 1 && (inner & 1)) ? 2 : 4;
       if (!zm_pass(B, z, maps, R, t, cur, nlev, a.omega, cur ? E0 : E1, gb.limit_ns)) {
         if (threadIdx.x == 0) {
           atomicCAS(gb.err, 0, BCFD_E_TIMEOUT);
@@ -1258,7 +1283,7 @@ __global__ void __launch_bounds__(kZmThreads, 1) k_sor_zm(DevBlock B, DcArgs a, 
       cur ^= 1;
       if (!grid_sync(gb)) return;
     }
-    sweeps += a.inner;
+    sweeps += inner;
     if (cur) {
       const float* e1c[2] = {E1[0], E1[1]};
       tb_copy_back(B, t, e1c);

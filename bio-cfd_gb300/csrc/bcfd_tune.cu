@@ -227,15 +227,23 @@ extern "C" int bcfd_autotune(int64_t* n_tuned) {
     apply(hb, t.fp32, true);
   }
   if (!group.empty()) {
-    // the group in one batched launch (default shapes) against its members
-    // solved one after the other in their best shapes
+    // the group in one batched launch (default shapes: what an earlier call
+    // applied is reset first) against its members solved one after the other
+    // in their best shapes
+    const Shape dflt{0, 0, 0};
+    for (HostBlock* hb : group) {
+      apply(hb, dflt, true);
+      apply(hb, dflt, false);
+    }
     std::vector<Saved> sv(group.size());
-    for (size_t q = 0; q < group.size(); ++q) TRY_R(save_state(group[q], sv[q], false));
+    int r = 0;
+    for (size_t q = 0; q < group.size() && !r; ++q) r = save_state(group[q], sv[q], false);
     float g32 = 0.f, g64 = 0.f;
-    int r = time_group(group, true, 16, &g32);
+    if (!r) r = time_group(group, true, 16, &g32);
     if (!r) r = time_group(group, false, 5, &g64);
     int rr = 0;
     for (size_t q = 0; q < group.size(); ++q) {
+      if (!sv[q].buf) continue;
       const int e = save_state(group[q], sv[q], true);
       if (!rr) rr = e;
     }

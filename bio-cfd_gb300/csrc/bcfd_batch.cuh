@@ -62,10 +62,22 @@ __global__ void __launch_bounds__(NT) k_set(BlockSet S, Op op) {
   for (int64_t _t = (int64_t)(cta_) * blockDim.x + threadIdx.x,                        \
                _n = (int64_t)(B_).d.nx * (B_).d.ny * (B_).d.nz;                        \
        _t < _n; _t += (int64_t)(ncta_) * blockDim.x)
+// (i, j, k) of item _t: 32-bit divisions while the interior count fits them
+// (a 64-bit division costs several times as many instructions)
 #define INTERIOR_CELL(B_)                                                              \
-  const int i = 2 + (int)(_t % (B_).d.nx);                                             \
-  const int64_t _r = _t / (B_).d.nx;                                                   \
-  const int j = 2 + (int)(_r % (B_).d.ny), k = 2 + (int)(_r / (B_).d.ny);              \
+  int i, j, k;                                                                         \
+  if (_n <= 0x7fffffffLL) {                                                            \
+    const unsigned _u = (unsigned)_t, _nx = (unsigned)(B_).d.nx, _ny = (unsigned)(B_).d.ny; \
+    const unsigned _r = _u / _nx;                                                      \
+    i = 2 + (int)(_u - _r * _nx);                                                      \
+    k = 2 + (int)(_r / _ny);                                                           \
+    j = 2 + (int)(_r - (unsigned)(k - 2) * _ny);                                       \
+  } else {                                                                             \
+    i = 2 + (int)(_t % (B_).d.nx);                                                     \
+    const int64_t _r = _t / (B_).d.nx;                                                 \
+    j = 2 + (int)(_r % (B_).d.ny);                                                     \
+    k = 2 + (int)(_r / (B_).d.ny);                                                     \
+  }                                                                                    \
   const int64_t c = (B_).d.idx(i, j, k)
 
 }  // namespace bcfd

@@ -355,7 +355,11 @@ __device__ __forceinline__ double take_slot(BlockStats* st, int c, int cta) {
 // REDBLACKSOR_linear (src/PcorVcor.F90:288-377) as one cooperative launch.
 // nIterPcor continues from stats->niter (the fine blocks accumulate it over
 // two solves per step, :78, :98, :116) and the stop test runs whenever the
-// accumulated count is a multiple of 5, exactly as the reference does.
+// accumulated count is a multiple of 5, exactly as the reference does.  In
+// residual-target mode (not a reference routine) the FP64 residual is checked
+// first after 5 pairs, then after as many pairs as the reduction per pair
+// measured between the last two checks needs to reach the target (15% and one
+// pair of margin, 5 to 64): each check is a full FP64 residual pass.
 // `cta` is this CTA's index among the block's CTAs (a batched launch runs
 // several blocks' solves side by side, each with its own barrier and tiles)
 __device__ __forceinline__ void sor64_body(const DevBlock& B, const SorArgs& a, const GridBar& gb,
@@ -372,6 +376,9 @@ __device__ __forceinline__ void sor64_body(const DevBlock& B, const SorArgs& a, 
   int check = 0;
   unsigned ph = 0;
   bool ok = true;
+  const bool target_mode = a.res_tol > 0.0;
+  int64_t next_check = it0 + 5, it_prev = it0;  // residual-target mode
+  double res_prev = -1.0;
   for (;;) {
     ++it;
     if (++r5 == 5) r5 = 0;
@@ -384,8 +391,8 @@ __device__ __forceinline__ void sor64_body(const DevBlock& B, const SorArgs& a, 
     if (a.rev) tile_half64<1>(B, t, a.omega, lmax, a.fast);
     else tile_half64<0>(B, t, a.omega, lmax, a.fast);
     tile_publish(tm, t, ++ph);
-    if (r5 == 0) {
-      if (a.res_tol > 0.0) {
+    if (target_mode ? it >= next_check : r5 == 0) {
+      if (target_mode) {
         // residual-target mode: the residual needs the neighbours' sweep pair
         if (!tile_wait(tm, gb, t, ph)) { ok = false; break; }
         lmax = nmax(tile_resid_max64<1>(B, t), tile_resid_max64<0>(B, t)) * a.dt;
@@ -396,6 +403,17 @@ __device__ __forceinline__ void sor64_body(const DevBlock& B, const SorArgs& a, 
       if (!grid_sync(gb)) { ok = false; break; }
       derr4 = take_slot(st, check, cta);
       ++check;
+      if (target_mode) {
+        int64_t gap = 5;
+        if (res_prev > 0.0 && derr4 < res_prev && derr4 > a.res_tol) {
+          const double per_pair = log(derr4 / res_prev) / (double)(it - it_prev);  // < 0
+          const double need = log(a.res_tol / derr4) / per_pair;                   // > 0
+          gap = (int64_t)fmin(64.0, fmax(5.0, ceil(need * 1.15) + 1.0));
+        }
+        res_prev = derr4;
+        it_prev = it;
+        next_check = it + gap;
+      }
     }
     if (a.res_tol > 0.0 ? (derr4 <= a.res_tol) : (derr4 < a.epsi)) break;
     if (it > a.itmax || non_finite(derr4)) break;

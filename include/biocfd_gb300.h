@@ -326,7 +326,10 @@ typedef struct bcfd_step_config {
                              inverse diagonal by Newton-Raphson) to div_tol   */
   double div_tol;      /* precision 1-3: target FP64 Poisson residual in
                           divergence units, deltat * max|b/deltat - A pc|;
-                          must be > 0 (BCFD_E_ARG otherwise)                   */
+                          must be > 0 (BCFD_E_ARG otherwise).  The residual
+                          is checked at an adaptive cadence (after each FP32
+                          correction, whose length follows the measured
+                          reduction rate; every 5 to 64 FP64 sweep pairs)    */
   int use_graph;       /* capture the step in a CUDA graph and replay it       */
 } bcfd_step_config;
 
@@ -406,8 +409,9 @@ int bcfd_max_divergence(bcfd_handle h, double* out);
  * FP64 Poisson residual of the last solve in divergence units (the divergence
  * the correction leaves wherever the operators are consistent) */
 int bcfd_block_get_divergence(bcfd_handle h, double* out);
-/* mixed-precision solve parameters of a block: FP32 sweeps per correction,
- * their relaxation factor (0 selects the defaults) and the kernel variant
+/* mixed-precision solve parameters of a block: FP32 sweep pairs of the first
+ * correction and the most of any later one (0: 64), their relaxation factor
+ * (0 selects the default, bcfd_block_get_mixed_omega) and the kernel variant
  * (0: the library's choice, 1: tiled cooperative with grid-wide phase
  * barriers, 3: tiled cooperative with point-to-point neighbour sync, 4:
  * temporal-blocked sweeps, one grid barrier per sweep pair, when the block's

@@ -531,11 +531,6 @@ int alloc_surface(HostBlock* hb, int ne, int nn) {
   return 0;
 }
 
-int block_sync_err(HostBlock* hb) {
-  BCFD_CUDA(cudaStreamSynchronize(stream()));
-  return take_block_error(hb);
-}
-
 }  // namespace
 
 // change_block_coords (src/Search.F90:1208-1264): the faces move by whole

@@ -149,14 +149,8 @@ struct SolveCfg {
 
 // precision 0: FP64, the reference's stop test (drop-in arithmetic);
 // 1: FP32 SOR + FP64 defect correction to div_tol; 2: FP64 SOR (reference
-// sweeps) to div_tol; 3: division-free FP64 SOR to div_tol
-int sor(HostBlock* hb, const SolveCfg& c) {
-  if (c.precision == 1) return launch_sor_mixed(hb, c.itmax, c.dt, c.div_tol);
-  if (c.precision >= 2) return launch_sor(hb, c.itmax, c.dt, c.epsi, c.div_tol, c.precision == 3);
-  return launch_sor(hb, c.itmax, c.dt, c.epsi);
-}
-
-// the same dispatch over several blocks (one batched launch when batching)
+// sweeps) to div_tol; 3: division-free FP64 SOR to div_tol.  One batched
+// launch over several blocks when batching.
 int sor_set(const std::vector<HostBlock*>& v, const SolveCfg& c) {
   if (c.precision == 1) return launch_sor_mixed_set(v, c.itmax, c.dt, c.div_tol);
   if (c.precision >= 2) return launch_sor_set(v, c.itmax, c.dt, c.epsi, c.div_tol, c.precision == 3);
@@ -517,7 +511,7 @@ std::vector<unsigned char> step_key(const bcfd_step_config& c) {
     const unsigned char none = 0;
     if (!hb) { put(&none, 1); continue; }
     put(&hb->d, sizeof hb->d);
-    const int sw[11] = {hb->is_coarse, hb->has_body, hb->move_check, hb->blk_mv_tag, hb->dc_inner,
+    const int sw[11] = {hb->is_coarse, hb->has_body, (int)hb->move_check, (int)hb->blk_mv_tag, hb->dc_inner,
                         hb->dc_variant, hb->solve_threads, hb->solve_ctas_per_sm, hb->solve_sync,
                         hb->dc_threads, hb->dc_ctas_per_sm};
     put(sw, sizeof sw);

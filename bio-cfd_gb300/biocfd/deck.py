@@ -20,8 +20,11 @@ so a run cannot restart from its own checkpoints without renaming them;
 Field output (src/WriteOutput_corner1.F90:74-104): the ASCII zone file
 ``out/{char_f}_butter_fielddata.{ita:09d}.{id:03d}.{re:7.1f}.{dx:8.6f}.{nblocks:03d}.dat``
 with cell-centred velocities, every 200 steps and at steps 0-2; the surface
-file ``out/butterfly_{id:03d}.dat`` at step 1.  Files are written by a
-background thread from host copies, so the time loop does not wait for them.
+file ``out/butterfly_{id:03d}.dat`` at step 1.  With ``output_format="hdf5"``
+the field files are the reference's HDF5 build's instead
+(src/WriteOutput_corner1.F90:21-78, ``out/timestep_{ita:05d}_block_{id:05d}.h5``,
+written by ``h5io``) at the same cadence.  Files are written by a background
+thread from host copies, so the time loop does not wait for them.
 """
 from __future__ import annotations
 
@@ -36,7 +39,7 @@ from typing import Dict, List, Optional
 
 import numpy as np
 
-from . import synth
+from . import h5io, synth
 
 BLK_START = 2  # the first fine block (src/ReadInput.f90:10)
 
@@ -462,11 +465,16 @@ class AsyncWriter:
 # ---------------------------------------------------------------------------
 
 def run_deck(directory, n_steps: Optional[int] = None, precision: int = 0, div_tol: float = 1e-6,
-             out_dir: Optional[str] = None, outputs: bool = True, mesh_file: str = "geometries/butterflyMedium.msh"):
+             out_dir: Optional[str] = None, outputs: bool = True, mesh_file: str = "geometries/butterflyMedium.msh",
+             output_format: str = "ascii"):
     """app/main.F90 on the GB300 path: read the deck, set up (restart fields
     when istart = 1), write the step-0 output, run n_steps (default itamax)
-    with field output at steps <= 2 and every 200, checkpoints every 500 and
-    the surface at step 1.  Returns the Solver (blocks left on the device)."""
+    with field output at steps <= 2 and every 200 (ASCII zone files, or the
+    HDF5 files of the reference's USE_HDF5 build with output_format="hdf5"),
+    checkpoints every 500 and the surface at step 1.  Returns the Solver
+    (blocks left on the device)."""
+    if output_format not in ("ascii", "hdf5"):
+        raise ValueError(f"output_format {output_format!r}: 'ascii' or 'hdf5'")
     from .solver import Solver
     deck = read_deck(directory, mesh_file)
     case = deck_to_case(deck)
@@ -489,8 +497,12 @@ def run_deck(directory, n_steps: Optional[int] = None, precision: int = 0, div_t
                 f = s.fields(h)
                 t = s.tags(h)
                 tags = {"cell": t["cell"], "cell_n": t["cell_n"], "cell_pr": t["cell_pr"][:-1, :-1, :-1]}
-                writer.submit(write_fields_ascii, out / field_name(deck.char_f, ita, g, deck.re, b.d[0], nb),
-                              b.x1, b.y1, b.z1, f, tags, totime)
+                if output_format == "hdf5":
+                    writer.submit(h5io.write_fields_hdf5, out / h5io.field_name_hdf5(ita, g),
+                                  b.x1, b.y1, b.z1, f, tags, totime)
+                else:
+                    writer.submit(write_fields_ascii, out / field_name(deck.char_f, ita, g, deck.re, b.d[0], nb),
+                                  b.x1, b.y1, b.z1, f, tags, totime)
             if ita % 500 == 0 and ita > 0:
                 f = s.fields(h)
                 for name in (checkpoint_name(deck.char_f, g, deck.re, b.d[0]), restart_name(g, deck.re)):

@@ -929,7 +929,11 @@ int bcfd_block_read(bcfd_handle h, const char* name, void* out, int64_t n, int64
     int r = launch_build_list(hb, which, buf, cap, &m);
     std::vector<int> t(3 * (size_t)cap);
     if (!r) {
-      BCFD_CUDA(d2h(t.data(), buf, 3 * cap * sizeof(int)));
+      const cudaError_t e = d2h(t.data(), buf, 3 * cap * sizeof(int));
+      if (e != cudaSuccess) {
+        report_cuda(e, "index lists to host", __FILE__, __LINE__);
+        r = BCFD_E_CUDA;
+      }
     }
     cudaFree(buf);
     if (r) return r;

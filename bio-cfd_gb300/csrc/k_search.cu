@@ -861,11 +861,18 @@ int launch_build_list(HostBlock* hb, int which, int* out_ijk, int64_t cap, int64
   if (int r = ensure_scratch(hb)) return r;
   int64_t* tot;
   BCFD_CUDA(cudaMalloc(&tot, sizeof(int64_t)));
-  BCFD_CUDA(cudaMemsetAsync(tot, 0, sizeof(int64_t), stream()));
-  int r = compact(hb, which, out_ijk, out_ijk + cap, out_ijk + 2 * cap, (int)cap, nullptr, tot);
-  if (r == 0) {
-    BCFD_CUDA(cudaMemcpyAsync(count_host, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, stream()));
-    BCFD_CUDA(cudaStreamSynchronize(stream()));
+  int r = 0;
+  cudaError_t e = cudaMemsetAsync(tot, 0, sizeof(int64_t), stream());
+  if (e == cudaSuccess) {
+    r = compact(hb, which, out_ijk, out_ijk + cap, out_ijk + 2 * cap, (int)cap, nullptr, tot);
+    if (r == 0) {
+      e = cudaMemcpyAsync(count_host, tot, sizeof(int64_t), cudaMemcpyDeviceToHost, stream());
+      if (e == cudaSuccess) e = cudaStreamSynchronize(stream());
+    }
+  }
+  if (e != cudaSuccess) {
+    report_cuda(e, "list count to host", __FILE__, __LINE__);
+    r = BCFD_E_CUDA;
   }
   cudaFree(tot);
   return r;

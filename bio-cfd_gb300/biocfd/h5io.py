@@ -516,7 +516,9 @@ def _parse_attr(b: bytes):
     return name, (v.astype(dt.newbyteorder("=")) if dims else v.item())
 
 
-def _load(r: _In, oh: int):
+def _load(r: _In, oh: int, path=()):
+    if oh in path:
+        raise H5FormatError(f"group at {oh:#x} links to itself")
     msgs = r.messages(oh)
     attrs = dict(_parse_attr(m[2]) for m in msgs if m[0] == MSG_ATTR)
     stab = [m for m in msgs if m[0] == MSG_STAB]
@@ -525,7 +527,7 @@ def _load(r: _In, oh: int):
         heap = r.heap(hp)
         g = Group(attrs=attrs)
         for name, child in r.symbols(bt, heap):
-            g.children[name] = _load(r, child)
+            g.children[name] = _load(r, child, path + (oh,))
         return g
     kinds = {m[0]: m[2] for m in msgs}
     if MSG_LAYOUT not in kinds or MSG_TYPE not in kinds or MSG_SPACE not in kinds:
@@ -551,6 +553,8 @@ def read_file(path) -> Group:
     r = _In(path)
     try:
         return _load(r, r.root_oh)
+    except (struct.error, IndexError, UnicodeDecodeError) as e:
+        raise H5FormatError(f"{path}: malformed HDF5 structure ({e})") from e
     finally:
         r.close()
 

@@ -195,3 +195,14 @@ def test_rejects_what_is_not_hdf5(tmp_path):
     p.write_bytes(bytes(b))
     with pytest.raises(h5io.H5FormatError, match="messages"):
         h5io.read_file(p)
+
+
+def test_truncated_file_is_a_format_error(tmp_path):
+    good = tmp_path / "good.h5"
+    h5io.hdf5_write_real(good, array_input_1d=np.ones(4), key="x", group="/")
+    b = good.read_bytes()
+    bad = tmp_path / "cut.h5"
+    for cut in (100, len(b) // 2, len(b) - 8):
+        bad.write_bytes(b[:cut])
+        with pytest.raises(h5io.H5FormatError):
+            h5io.read_file(bad).children["x"].read()

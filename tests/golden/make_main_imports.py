@@ -2,17 +2,20 @@
 of the reference's driver (app/main.F90, the caller the Fortran shim must
 relink against), the module name and the names it imports, lower-cased.
 
-Run in a checkout that has the reference at REF (default /root/reference):
+Run in a checkout that has the reference at REF (default: $BIOCFD_REFERENCE,
+else /root/reference):
     python tests/golden/make_main_imports.py [REF]
 """
 from __future__ import annotations
 
 import json
+import os
 import re
 import sys
 from pathlib import Path
 
 HERE = Path(__file__).resolve().parent
+REFERENCE = Path(os.environ.get("BIOCFD_REFERENCE", "/root/reference"))
 
 
 def parse_use_lists(text: str) -> dict:
@@ -62,7 +65,7 @@ def subroutine_signatures(text: str) -> dict:
 
 
 def main():
-    ref = Path(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    ref = Path(sys.argv[1]) if len(sys.argv) > 1 else REFERENCE
     src = ref / "app" / "main.F90"
     uses = parse_use_lists(src.read_text())
     sigs = {}

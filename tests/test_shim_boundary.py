@@ -8,7 +8,6 @@ The imports and the reference's signatures are a committed fixture
 tests/golden/make_main_imports.py from the reference's sources); when the
 reference's sources are present the fixture is also checked against them."""
 import json
-import os
 import re
 import sys
 from pathlib import Path
@@ -69,7 +68,7 @@ def shim_modules():
 
 
 def test_fixture_matches_reference_sources():
-    ref = Path(os.environ.get("BIOCFD_REFERENCE", "/root/reference"))
+    ref = make_main_imports.REFERENCE
     if not (ref / "app" / "main.F90").exists():
         pytest.skip("reference sources not present (the committed fixture stands)")
     fx = json.loads(FIXTURE.read_text())

@@ -71,7 +71,11 @@ int save_state(HostBlock* hb, Saved& s, bool restore) {
 int time_trial(HostBlock* hb, bool fp32, int pairs, float* ms) {
   cudaEvent_t e0, e1;
   BCFD_CUDA(cudaEventCreate(&e0));
-  BCFD_CUDA(cudaEventCreate(&e1));
+  if (const cudaError_t ee = cudaEventCreate(&e1); ee != cudaSuccess) {
+    cudaEventDestroy(e0);
+    report_cuda(ee, "cudaEventCreate(&e1)", __FILE__, __LINE__);
+    return BCFD_E_CUDA;
+  }
   float best = 1e30f;
   int r = 0;
   for (int rep = 0; rep < 3 && !r; ++rep) {
@@ -101,7 +105,11 @@ int time_trial(HostBlock* hb, bool fp32, int pairs, float* ms) {
 int time_group(const std::vector<HostBlock*>& g, bool fp32, int pairs, float* ms) {
   cudaEvent_t e0, e1;
   BCFD_CUDA(cudaEventCreate(&e0));
-  BCFD_CUDA(cudaEventCreate(&e1));
+  if (const cudaError_t ee = cudaEventCreate(&e1); ee != cudaSuccess) {
+    cudaEventDestroy(e0);
+    report_cuda(ee, "cudaEventCreate(&e1)", __FILE__, __LINE__);
+    return BCFD_E_CUDA;
+  }
   float best = 1e30f;
   int r = 0;
   for (int rep = 0; rep < 3 && !r; ++rep) {
@@ -147,7 +155,10 @@ int tune_block(HostBlock* hb, Tuned* out) {
   static const Shape c32[] = {{128, 0, 1}, {256, 0, 1}, {128, 0, 3}, {256, 0, 3}, {256, 2, 1},
                               {256, 1, 1}, {256, 4, 1}, {256, 4, 3}, {512, 0, 4}, {384, 0, 5}};
   Saved sv;
-  TRY_R(save_state(hb, sv, false));
+  if (const int e = save_state(hb, sv, false)) {
+    cudaFree(sv.buf);
+    return e;
+  }
   const int t0 = hb->solve_threads, c0 = hb->solve_ctas_per_sm, s0 = hb->solve_sync, v0 = hb->dc_variant,
             dt0 = hb->dc_threads, dc0 = hb->dc_ctas_per_sm;
   int r = 0;
@@ -236,14 +247,18 @@ extern "C" int bcfd_autotune(int64_t* n_tuned) {
       apply(hb, dflt, false);
     }
     std::vector<Saved> sv(group.size());
+    std::vector<char> saved(group.size(), 0);  // restore only complete copies
     int r = 0;
-    for (size_t q = 0; q < group.size() && !r; ++q) r = save_state(group[q], sv[q], false);
+    for (size_t q = 0; q < group.size() && !r; ++q) {
+      r = save_state(group[q], sv[q], false);
+      saved[q] = r == 0;
+    }
     float g32 = 0.f, g64 = 0.f;
     if (!r) r = time_group(group, true, 16, &g32);
     if (!r) r = time_group(group, false, 5, &g64);
     int rr = 0;
     for (size_t q = 0; q < group.size(); ++q) {
-      if (!sv[q].buf) continue;
+      if (!saved[q]) continue;
       const int e = save_state(group[q], sv[q], true);
       if (!rr) rr = e;
     }
